@@ -1,0 +1,363 @@
+"""Benchmark of the MeshBlock hydro stage: cell-updates/s per RK3 step.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl native|reference]
+                    [--workload straka|sod] [--precision float64|float32]
+
+One JSON line on rank 0.  A step is one full RK3 step (three stages) of the
+workload's block on synthetic input (the deck's own initial state, generated
+on the host), dt fixed at the CFL step of the initial state.
+
+* value: device-timed throughput (CUDA events on the launching stream around
+  each step, L2 flushed between steps -- the block fits in L2, so each timed
+  step starts cold), state resident in HBM.
+* e2e: the same steps through the public API with HOST buffers: each step
+  copies the state host->device from pinned memory, advances it and copies it
+  back (bytes counted from the copied tensors).
+* roofline: the stage kernel's algorithmic bytes per launch over its mean
+  duration (CUDA events around each stage call: the stage kernel and its
+  ghost-fill kernel) against the measured HBM copy peak.
+* cpu_baseline: the CPU oracle (the reference algorithm restated in C, FP64,
+  OpenMP on every host core) on a bounded sample of the same workload.
+
+--impl reference times that CPU path alone (the reference itself cannot be
+built here or on the GPU machine) and prints the same line with
+"impl": "reference".
+Under torchrun (N > 1) every rank advances its own replica of the workload
+(the blocks are independent: replicas only), value = all ranks' cell-updates
+/ the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # the 2-D density-current shape of the Straka config: 512 x 128 cells at
+    # 50 m, LMARS + WENO5 (cp5 for velocity/pressure) + RK3, reflecting walls
+    "straka": "snapy_gb300/decks/straka_explicit.yaml",
+    "sod": "snapy_gb300/decks/sod.yaml",
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["native", "reference"], default="native")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="straka")
+    ap.add_argument("--precision", choices=["float64", "float32"], default=None)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def load_options(args):
+    import snapy_gb300 as sg
+    opts = sg.MeshBlockOptions.from_yaml(os.path.join(ROOT, WORKLOADS[args.workload]))
+    if args.precision:
+        opts.hydro().precision = args.precision
+    return opts
+
+
+def initial_state(opts, workload, device):
+    from snapy_gb300 import problems
+    if workload == "sod":
+        return problems.sod(opts, device)
+    return problems.straka(opts, device)
+
+
+def config_of(opts, workload, args, nranks):
+    c = opts.coord()
+    h = opts.hydro()
+    return {
+        "workload": f"{workload} {c.nx2}x{c.nx1} ({c.dx2:g} m x {c.dx1:g} m), "
+                    f"{h.riemann.type}+weno5+rk3, {h.precision}",
+        "cells": c.nx1 * c.nx2 * c.nx3,
+        "nx1": c.nx1, "nx2": c.nx2, "nx3": c.nx3,
+        "riemann": h.riemann.type,
+        "precision": h.precision,
+        "gravity": bool(h.grav and h.grav.grav1),
+        "implicit": bool(h.icorr),
+        "l2": "flushed between timed steps (512 MiB write; the block fits in L2)",
+        "replicas": nranks,
+        "parallelism": "replicas" if nranks > 1 else "single",
+    }
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax = float(parts[2])
+                except ValueError:
+                    continue
+                for n, v in zip(names, parts[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(opts, workload, seconds, u0_host=None):
+    """The CPU oracle on every host core: cell-updates/s on a bounded sample
+    (as many full RK3 steps of the same block as fit in `seconds`, >= 2)."""
+    import numpy as np
+    from oracle import oracle as O
+    O.build()
+    c = opts.coord()
+    h = opts.hydro()
+    bcs = [n.rsplit("_", 1)[0] if n else "none" for n in opts.bcnames]
+    bcs += ["none"] * (6 - len(bcs))
+    cores = os.cpu_count() or 1
+    ob = O.Block(nc1=c.nc1, nc2=c.nc2, nc3=c.nc3, dx1=c.dx1,
+                 dx2=c.dx2 if c.nx2 > 1 else c.x2max - c.x2min,
+                 dx3=c.dx3 if c.nx3 > 1 else c.x3max - c.x3min,
+                 gammad=h.eos.gammad, riemann=h.riemann.type,
+                 shock=h.recon1.shock, scale=h.recon1.scale, bc=bcs, nthreads=cores)
+    w = initial_state(opts, workload, "cpu").numpy()
+    u = ob.initialize(w)
+    dt = opts.intg().cfl * ob.max_dt(u)
+    ob.step(u, dt)  # warm
+    n, t0 = 0, time.perf_counter()
+    while True:
+        ob.step(u, dt)
+        n += 1
+        el = time.perf_counter() - t0
+        if (el >= seconds and n >= 2) or n >= 100000:
+            break
+    cells = c.nx1 * c.nx2 * c.nx3
+    return {"value": cells * n / el, "unit": "cell-updates/s", "cores": cores,
+            "kind": "port",
+            "sample": f"{n} RK3 steps of the same {c.nx2}x{c.nx1} block, FP64, "
+                      f"{el:.1f} s, OpenMP {cores} threads"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    opts = load_options(args)
+    c = opts.coord()
+    per = []
+    cb = None
+    for _ in range(args.warmup):
+        pass
+    seconds = max(2.0, args.cpu_seconds / max(1, args.steps) * args.steps)
+    cb = cpu_baseline(opts, args.workload, seconds)
+    val = cb["value"]
+    cells = c.nx1 * c.nx2 * c.nx3
+    line = {
+        "impl": "reference", "metric": "cell-updates/s per RK3 step",
+        "value": val, "unit": "cell-updates/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": cells / val * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (the deck's initial state)",
+        "config": config_of(opts, args.workload, args, 1),
+        "cpu_baseline": cb,
+        "e2e": {"value": val, "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_native(args):
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl", init_method="env://")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+
+    import snapy_gb300 as sg
+    opts = load_options(args)
+    c = opts.coord()
+    cells = c.nx1 * c.nx2 * c.nx3
+    blk = sg.MeshBlock(opts).to(dev)
+    w = initial_state(opts, args.workload, dev)
+    vars = {"hydro_w": w}
+    blk.initialize(vars)
+    dt = blk.max_time_step(vars)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+
+    for _ in range(max(3, args.warmup)):
+        blk.step(vars, dt)
+    torch.cuda.synchronize()
+
+    # device-timed steps, cold L2 for each
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            flush.zero_()
+            ev[k][0].record(stream)
+            blk.step(vars, dt)
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    t_total = sum(step_ms) / 1e3
+    if world > 1:
+        t = torch.tensor([t_total], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_total = float(t.item())
+    value = cells * args.steps * world / t_total
+
+    # roofline of the stage kernel: per stage call, events on the stream
+    b = blk.batch
+    s_bytes = torch.finfo(blk.dtype).bits // 8
+    stage_ms, stage_bytes = [], []
+    for k in range(min(args.steps, 50)):
+        flush.zero_()
+        for st in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            b.stage(st)
+            e1.record(stream)
+            stage_ms.append((e0, e1))
+            stage_bytes.append((2 if st == 0 else 3) * 5 * s_bytes * cells)
+    torch.cuda.synchronize()
+    durs = [a.elapsed_time(bb) / 1e3 for a, bb in stage_ms]
+    achieved = sum(stage_bytes) / sum(durs) / 1e9
+    peak, peak_kind = peaks()
+
+    # end to end through the public API with host buffers
+    u_host = torch.empty(vars["hydro_u"].shape, dtype=blk.dtype).pin_memory()
+    u_host.copy_(vars["hydro_u"].cpu())
+    e2e_steps = max(5, min(args.steps, 100))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        vars["hydro_u"].copy_(u_host, non_blocking=True)
+        blk.step(vars, dt)
+        u_host.copy_(vars["hydro_u"], non_blocking=True)
+    torch.cuda.synchronize()
+    e2e_t = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_t], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_t = float(t.item())
+    nbytes = u_host.numel() * u_host.element_size()
+
+    rep = blk.execution_report()
+    line = None
+    if rank == 0:
+        cb = None
+        if not args.no_cpu_baseline:
+            cb = cpu_baseline(opts, args.workload, args.cpu_seconds)
+        line = {
+            "metric": "cell-updates/s per RK3 step",
+            "value": value, "unit": "cell-updates/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t_total / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if blk.dtype == torch.float64 else "f32",
+            "data": "synthetic (the deck's initial state)",
+            "config": config_of(opts, args.workload, args, world),
+            "e2e": {"value": cells * e2e_steps * world / e2e_t,
+                    "unit": "cell-updates/s", "h2d_bytes_per_step": nbytes,
+                    "d2h_bytes_per_step": nbytes},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak,
+                         "peak_kind": peak_kind, "traffic": None,
+                         "kernel": "stage_kernel (+ ghost fill)",
+                         "bytes_per_launch": statistics.mean(stage_bytes),
+                         "mean_launch_us": statistics.mean(durs) * 1e6},
+            "cpu_baseline": cb,
+            "clocks": clk.summary(),
+            "gpu_launches": args.steps * 3 * b.launches_per_stage(),
+            "execution_report": rep,
+            "step_ms_median": statistics.median(step_ms),
+            "tile_tj": b.tile(0),
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_native(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

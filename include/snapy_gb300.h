@@ -1,0 +1,128 @@
+/*
+ * snapy_gb300 -- C ABI of the GB300-native MeshBlock hydro stage.
+ *
+ * A drop-in for the native dispatch boundary of snapy's hydro stage: one call
+ * advances every block of a batch by one RK stage on a caller-provided CUDA
+ * stream, reading the time step from device memory (so a captured CUDA graph
+ * replays with any dt).  Plain pointers and sizes only; no torch types.
+ *
+ * Reference interfaces replaced (paths inside the snapy project):
+ *   sg_create / sg_bind   MeshBlockImpl construction + StateStore adoption
+ *                         (src/mesh/meshblock.hpp:142-392,
+ *                          src/mesh/state_store.hpp:24-125)
+ *   sg_stage              StageExecutor::run_stage -> stage_advance /
+ *                         stage_combine / stage_boundaries
+ *                         (src/mesh/stage_executor.cpp:809,
+ *                          src/mesh/meshblock_advance.cpp:145,314,398), which
+ *                         dispatch call_recon (src/recon/recon_dispatch.hpp:13),
+ *                         call_riemann (src/riemann/riemann.hpp:161-171) and
+ *                         the torch divergence / RK combine
+ *   sg_max_dt             MeshBlockImpl::max_time_step
+ *                         (src/mesh/meshblock_advance.cpp:61-72,
+ *                          src/hydro/hydro.cpp:316-398)
+ *   sg_check              MeshBlockImpl::local_redo_flag_tensor
+ *                         (src/mesh/meshblock_redo.cpp:95-150)
+ *   sg_restore            MeshBlockImpl::apply_redo's StateStore::restore
+ *                         (src/mesh/meshblock_redo.cpp:58-60)
+ *   sg_prim               EquationOfStateImpl::forward, U->W
+ *                         (src/eos/equation_of_state.cpp:283-289)
+ *   sg_fill_ghosts        MeshBlockImpl::apply_boundaries
+ *                         (src/mesh/meshblock_exchange.cpp:214-286)
+ *
+ * Every function returns 0 on success and a positive code on error; the
+ * message of the last error of the calling thread is sg_last_error().
+ */
+#ifndef SNAPY_GB300_H
+#define SNAPY_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct sg_handle sg_handle;
+typedef struct CUstream_st* sg_stream_t; /* a cudaStream_t */
+
+enum { SG_F64 = 0, SG_F32 = 1 };
+enum { SG_HLLC = 0, SG_LMARS = 1 };
+enum {
+  SG_BC_NONE = 0,
+  SG_BC_REFLECTING = 1,
+  SG_BC_PERIODIC = 2,
+  SG_BC_EXTRAPOLATION = 3
+};
+enum {
+  SG_OK = 0,
+  SG_ERR_ARG = 1,
+  SG_ERR_CUDA = 2,
+  SG_ERR_UNSUPPORTED = 3,
+  SG_ERR_STATE = 4
+};
+
+/* the scheme shared by every block of a batch (one deck) */
+typedef struct sg_scheme {
+  int32_t dtype;   /* SG_F64 / SG_F32: storage and compute of the stage */
+  int32_t riemann; /* SG_HLLC / SG_LMARS */
+  int32_t shock;   /* reconstruct shock: every row weno5 */
+  int32_t scale;   /* reconstruct scale (WENO prologue) */
+  int32_t nstage;  /* 3 for rk3 */
+  double wght[3][3]; /* per stage (w0, w1, w2): u <- w0 u0 + w1 u + w2 du */
+  double cfl;
+  double density_floor, pressure_floor;
+} sg_scheme;
+
+/* one block: padded sizes (nx + 2 ng on an active axis, else 1) */
+typedef struct sg_block_desc {
+  int32_t nc1, nc2, nc3, ng;
+  int32_t bc[6]; /* x1-inner, x1-outer, x2-inner, x2-outer, x3-in, x3-out */
+  double dx1, dx2, dx3;
+  double gammad;
+  int32_t tj; /* x2 columns per tile, 0 = the library's choice */
+} sg_block_desc;
+
+int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
+              int32_t nblock, sg_handle** out);
+int sg_destroy(sg_handle* h);
+/* three device buffers per block, each (5, nc3, nc2, nc1) of the dtype; the
+ * current state must be in buffer `current` (0..2) */
+int sg_bind(sg_handle* h, int32_t block, void* buf0, void* buf1, void* buf2);
+int sg_set_current(sg_handle* h, int32_t current);
+int sg_current(const sg_handle* h, int32_t* current);
+/* the buffer rotation: `cur` holds the current state, `base` the stage-0
+ * state of the step.  sg_advance does sg_stage's bookkeeping without a launch
+ * (the replay of a captured stage); sg_set_rotation restores a saved one */
+int sg_rotation(const sg_handle* h, int32_t* cur, int32_t* base);
+int sg_set_rotation(sg_handle* h, int32_t cur, int32_t base);
+int sg_advance(sg_handle* h, int32_t stage);
+/* one RK stage of every block; dt_dev points at nblock device doubles */
+int sg_stage(sg_handle* h, int32_t stage, const double* dt_dev,
+             sg_stream_t stream);
+/* ghost cells of the current buffer from the boundary functions */
+int sg_fill_ghosts(sg_handle* h, sg_stream_t stream);
+/* dt_dev_out[b] = cfl 2^-redo[b] min over block b (no host sync) */
+int sg_max_dt(sg_handle* h, const int32_t* redo_dev, double* dt_dev_out,
+              sg_stream_t stream);
+/* per-block retry flags (bit 0 floor, bit 3 NaN) into flags_dev (int32[nblock]) */
+int sg_check(sg_handle* h, int32_t* flags_dev, sg_stream_t stream);
+/* initialize (MeshBlockImpl::initialize, src/mesh/meshblock.cpp:306-420):
+ * the boundary functions fill the ghosts of the FP64 primitives w_in[b]
+ * (device pointers in a host array, written in place), and the current
+ * buffers <- W->U of them */
+int sg_init_from_prim(sg_handle* h, double* const* w_in, sg_stream_t stream);
+/* the current buffer becomes the stage-0 state again (a rejected step) */
+int sg_restore(sg_handle* h);
+/* primitives of the current state: w_out[b] are device pointers (host array) */
+int sg_prim(sg_handle* h, void* const* w_out, sg_stream_t stream);
+/* x2 columns per tile the library picked for block b */
+int sg_tile(const sg_handle* h, int32_t block, int32_t* tj);
+/* kernels launched by the last sg_stage call */
+int sg_launches_per_stage(const sg_handle* h, int32_t* n);
+const char* sg_last_error(void);
+const char* sg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

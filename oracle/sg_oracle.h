@@ -1,0 +1,74 @@
+/*
+ * CPU oracle for the snapy MeshBlock hydro stage -- TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C FP64 restatement of the reference's algorithm, used by tests/,
+ * __graft_entry__.smoke() and the cpu_baseline leg of bench.py as the checker.
+ * Nothing in the product (snapy_gb300/) may call it.
+ *
+ * Layout: every cell field is (nvar, nc3, nc2, nc1), x1 contiguous, exactly as
+ * the reference's hydro_u / hydro_w (src/snap.h:34-46 row order IDN, IVX, IVY,
+ * IVZ, IPR).
+ */
+#ifndef SG_ORACLE_H
+#define SG_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { OG_IDN = 0, OG_IVX = 1, OG_IVY = 2, OG_IVZ = 3, OG_IPR = 4 };
+enum { OG_HLLC = 0, OG_LMARS = 1 };
+enum {
+  OG_BC_NONE = 0,        /* no boundary function (custom no-op) */
+  OG_BC_REFLECTING = 1,
+  OG_BC_PERIODIC = 2,
+  OG_BC_EXTRAPOLATION = 3
+};
+
+typedef struct og_block {
+  int nvar;            /* 5 */
+  int nc1, nc2, nc3;   /* padded sizes (nx + 2 ng on an active axis, else 1) */
+  int ng;              /* ghost width, 3 */
+  double dx1, dx2, dx3;
+  double x1min, x2min, x3min; /* lower bound of the interior */
+  double gammad;
+  int riemann;         /* OG_HLLC / OG_LMARS */
+  int shock;           /* 1: every row weno5; 0: IDN weno5, IVX..IPR cp5 */
+  int weno_scale;      /* InterpOptions::scale */
+  int bc[6];           /* x1-inner, x1-outer, x2-inner, x2-outer, x3-in, x3-out */
+  /* RK3 weights (w0, w1, w2) per stage: u <- w0 u0 + w1 u + w2 du */
+  double wght[3][3];
+  int nthreads;        /* OpenMP threads, 0 = default */
+} og_block;
+
+/* ---- unit functions (pinned against the reference headers) ---- */
+/* one WENO5 face from 5 consecutive cells; side 0 = the cm table (the state on
+ * the right of the lower face of the centre cell), 1 = the cp table */
+double og_weno5_face(const double* s5, int side, int scale);
+double og_cp5_face(const double* s5, int side);
+/* HLLC / LMARS flux at one face from two primitive states (nvar 5) */
+void og_hllc_face(const double* wl, const double* wr, double gammad, int dim,
+                  double* flx, double* face_pressure);
+void og_lmars_face(const double* wl, const double* wr, double gammad, int dim,
+                   double* flx, double* face_pressure);
+void og_cons2prim_cell(const double* u, double* w, double gammad, int stride);
+
+/* ---- block operations ---- */
+void og_default_block(og_block* b);
+void og_cons2prim(const og_block* b, const double* u, double* w);
+void og_prim2cons(const og_block* b, const double* w, double* u);
+/* boundary functions, faces in order 0..5; primitive selects kPrimitive */
+void og_apply_bc(const og_block* b, double* q, int primitive);
+/* face fluxes of direction d (1 = x1, 2 = x2, 3 = x3) at every face */
+void og_flux(const og_block* b, const double* w, int d, double* flux);
+/* one RK stage: u is advanced in place; u0 holds the stage-0 backup */
+void og_stage(const og_block* b, double* u, double* u0, double dt, int stage);
+/* the hydro time step (before cfl), reference HydroImpl::max_time_step */
+double og_max_dt(const og_block* b, const double* w);
+/* initialize: boundaries on w, W->U, boundaries on u */
+void og_initialize(const og_block* b, double* w, double* u);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

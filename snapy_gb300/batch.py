@@ -1,0 +1,165 @@
+"""A batch of blocks advanced together by the CUDA library.
+
+``Batch`` owns one library handle, the three rotating HBM state buffers of
+every block (torch allocations, handed to the library as raw pointers) and the
+per-block device time steps.  ``MeshBlock`` is a batch of one; an ensemble or
+the serving loop batches many blocks of one scheme into one launch per stage.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import List, Optional, Sequence
+
+import torch
+
+from . import _lib
+
+_DT = {torch.float64: _lib.F64, torch.float32: _lib.F32}
+
+
+def _stream(stream: Optional[torch.cuda.Stream] = None) -> int:
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return s.cuda_stream
+
+
+class Batch:
+    """Blocks of one scheme; each block is a dict with nc1, nc2, nc3, ng,
+    dx1, dx2, dx3, gammad, bc (6 ints) and optionally tj."""
+
+    def __init__(self, scheme: dict, blocks: Sequence[dict],
+                 device: torch.device, dtype: torch.dtype):
+        if device.type != "cuda":
+            raise RuntimeError("snapy_gb300 runs on CUDA devices only "
+                               f"(got {device}); there is no CPU path")
+        self.L = _lib.load()
+        self.device = device
+        self.dtype = dtype
+        self.nblock = len(blocks)
+        sch = _lib.Scheme()
+        sch.dtype = _DT[dtype]
+        sch.riemann = scheme["riemann"]
+        sch.shock = int(scheme["shock"])
+        sch.scale = int(scheme["scale"])
+        sch.nstage = len(scheme["wght"])
+        for s, w in enumerate(scheme["wght"]):
+            for q in range(3):
+                sch.wght[s][q] = w[q]
+        sch.cfl = scheme["cfl"]
+        sch.density_floor = scheme["density_floor"]
+        sch.pressure_floor = scheme["pressure_floor"]
+        arr = (_lib.BlockDesc * self.nblock)()
+        for b, d in enumerate(blocks):
+            a = arr[b]
+            a.nc1, a.nc2, a.nc3, a.ng = d["nc1"], d["nc2"], d["nc3"], d["ng"]
+            for f in range(6):
+                a.bc[f] = d["bc"][f]
+            a.dx1, a.dx2, a.dx3 = d["dx1"], d["dx2"], d["dx3"]
+            a.gammad = d["gammad"]
+            a.tj = d.get("tj", 0)
+        self.shapes = [(5, d["nc3"], d["nc2"], d["nc1"]) for d in blocks]
+        h = ctypes.c_void_p()
+        with torch.cuda.device(device):
+            _lib.check(self.L.sg_create(ctypes.byref(sch), arr, self.nblock,
+                                        ctypes.byref(h)), "sg_create")
+        self.h = h
+        # three state buffers per block, one allocation each
+        self.store = [torch.empty((3,) + s, dtype=dtype, device=device)
+                      for s in self.shapes]
+        for b, st in enumerate(self.store):
+            _lib.check(self.L.sg_bind(self.h, b, st[0].data_ptr(),
+                                      st[1].data_ptr(), st[2].data_ptr()),
+                       "sg_bind")
+        self.dt = torch.zeros(self.nblock, dtype=torch.float64, device=device)
+        self.redo = torch.zeros(self.nblock, dtype=torch.int32, device=device)
+        self.flags = torch.zeros(self.nblock, dtype=torch.int32, device=device)
+        self._w_ptrs = (ctypes.c_void_p * self.nblock)()
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.L.sg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- state ------------------------------------------------------------
+    def current_index(self) -> int:
+        c = ctypes.c_int32()
+        _lib.check(self.L.sg_current(self.h, ctypes.byref(c)), "sg_current")
+        return c.value
+
+    def current(self, b: int = 0) -> torch.Tensor:
+        return self.store[b][self.current_index()]
+
+    def rotation(self):
+        c, b = ctypes.c_int32(), ctypes.c_int32()
+        _lib.check(self.L.sg_rotation(self.h, ctypes.byref(c), ctypes.byref(b)),
+                   "sg_rotation")
+        return c.value, b.value
+
+    def set_rotation(self, rot) -> None:
+        _lib.check(self.L.sg_set_rotation(self.h, rot[0], rot[1]), "sg_set_rotation")
+
+    def advance(self, stage: int) -> None:
+        _lib.check(self.L.sg_advance(self.h, stage), "sg_advance")
+
+    def set_current(self, index: int) -> None:
+        _lib.check(self.L.sg_set_current(self.h, index), "sg_set_current")
+
+    def init_from_prim(self, ws: List[torch.Tensor], stream=None) -> None:
+        for b, w in enumerate(ws):
+            if w.dtype != torch.float64 or tuple(w.shape) != self.shapes[b]:
+                raise ValueError(f"initialize: hydro_w of block {b} must be "
+                                 f"float64 of shape {self.shapes[b]}, got "
+                                 f"{w.dtype} {tuple(w.shape)}")
+            if not w.is_contiguous() or w.device != self.device:
+                raise ValueError("initialize: hydro_w must be contiguous on "
+                                 f"{self.device}")
+            self._w_ptrs[b] = w.data_ptr()
+        self.set_current(0)
+        _lib.check(self.L.sg_init_from_prim(self.h, self._w_ptrs, _stream(stream)),
+                   "sg_init_from_prim")
+
+    def prim(self, outs: List[torch.Tensor], stream=None) -> None:
+        for b, w in enumerate(outs):
+            if w.dtype != self.dtype or tuple(w.shape) != self.shapes[b]:
+                raise ValueError("prim: output of the storage dtype and shape")
+            self._w_ptrs[b] = w.data_ptr()
+        _lib.check(self.L.sg_prim(self.h, self._w_ptrs, _stream(stream)), "sg_prim")
+
+    # -- stepping -----------------------------------------------------------
+    def stage(self, stage: int, stream=None, dt: Optional[torch.Tensor] = None) -> None:
+        d = self.dt if dt is None else dt
+        _lib.check(self.L.sg_stage(self.h, stage, d.data_ptr(), _stream(stream)),
+                   "sg_stage")
+
+    def max_dt(self, stream=None) -> torch.Tensor:
+        """dt[b] = cfl 2^-redo[b] min(dx / (|v| + c)) on the device."""
+        _lib.check(self.L.sg_max_dt(self.h, self.redo.data_ptr(), self.dt.data_ptr(),
+                                    _stream(stream)), "sg_max_dt")
+        return self.dt
+
+    def check(self, stream=None) -> torch.Tensor:
+        _lib.check(self.L.sg_check(self.h, self.flags.data_ptr(), _stream(stream)),
+                   "sg_check")
+        return self.flags
+
+    def restore(self) -> None:
+        _lib.check(self.L.sg_restore(self.h), "sg_restore")
+
+    def fill_ghosts(self, stream=None) -> None:
+        _lib.check(self.L.sg_fill_ghosts(self.h, _stream(stream)), "sg_fill_ghosts")
+
+    def tile(self, b: int = 0) -> int:
+        t = ctypes.c_int32()
+        _lib.check(self.L.sg_tile(self.h, b, ctypes.byref(t)), "sg_tile")
+        return t.value
+
+    def launches_per_stage(self) -> int:
+        n = ctypes.c_int32()
+        _lib.check(self.L.sg_launches_per_stage(self.h, ctypes.byref(n)),
+                   "sg_launches_per_stage")
+        return n.value

@@ -1,0 +1,479 @@
+// C ABI of the batched hydro stage (include/snapy_gb300.h): handle and
+// buffer bookkeeping on the host, launches on the caller's stream, and the
+// two tiny finishing kernels of the per-step reductions.
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "../../include/snapy_gb300.h"
+#include "sg_types.h"
+
+using sg::BlockDev;
+using sg::StageParams;
+
+// per-precision launchers (sg_stage.cu compiled for double and for float)
+#define SG_DECLARE(sfx)                                                        \
+  extern "C" size_t sg_stage_smem##sfx(int nc1, int nx1, int tj, int has2);    \
+  extern "C" int sg_launch_stage##sfx(const BlockDev*, StageParams, size_t,    \
+                                      cudaStream_t);                           \
+  extern "C" int sg_launch_ghost##sfx(const BlockDev*, int, int, size_t,       \
+                                      cudaStream_t);                           \
+  extern "C" int sg_launch_prim##sfx(const BlockDev*, int, int, void* const*,  \
+                                     size_t, cudaStream_t);                    \
+  extern "C" int sg_launch_init##sfx(const BlockDev*, int, int,                \
+                                     double* const*, size_t,                   \
+                                     cudaStream_t);                            \
+  extern "C" int sg_launch_reduce##sfx(const BlockDev*, int, int,              \
+                                       unsigned long long*, int*, size_t,      \
+                                       cudaStream_t);
+SG_DECLARE(_f64)
+SG_DECLARE(_f32)
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(SG_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+constexpr unsigned long long kKeyInf = 0xfff0000000000000ull;  // key(+inf)
+
+__device__ __forceinline__ double unkey(unsigned long long k) {
+  return __longlong_as_double((k >> 63) ? (k & 0x7fffffffffffffffull) : ~k);
+}
+
+// dt[b] = (2^-redo[b] cfl) dt_min[b]  (meshblock_advance.cpp:61-72); a NaN
+// anywhere makes the step's dt NaN, as torch's min does
+__global__ void finish_dt_kernel(int nblock, unsigned long long* red, int* nan,
+                                 const int32_t* redo, double cfl,
+                                 double* dt_out) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nblock) return;
+  double dtm = unkey(red[4 * b]);
+  double f = redo ? pow(2., -(double)redo[b]) : 1.;
+  dt_out[b] = nan[b] ? __longlong_as_double(0x7ff8000000000000ll) : f * cfl * dtm;
+  red[4 * b] = red[4 * b + 1] = red[4 * b + 2] = kKeyInf;
+  nan[b] = 0;
+}
+
+// meshblock_redo.cpp:106-114: a floor hit when min rho (p) is not above
+// 1.001 x its floor (a NaN compares false, so it is a hit too); bit 3: NaN
+__global__ void finish_check_kernel(int nblock, unsigned long long* red,
+                                    int* nan, double dfloor, double pfloor,
+                                    int32_t* flags) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nblock) return;
+  double rmin = unkey(red[4 * b + 1]), pmin = unkey(red[4 * b + 2]);
+  int f = 0;
+  if (!(rmin > 1.001 * dfloor)) f |= 1;
+  if (!(pmin > 1.001 * pfloor)) f |= 1;
+  if (nan[b]) f |= 1 | 8;
+  flags[b] = f;
+  red[4 * b] = red[4 * b + 1] = red[4 * b + 2] = kKeyInf;
+  nan[b] = 0;
+}
+
+__global__ void init_red_kernel(int n, unsigned long long* red, int* nan) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= n) return;
+  red[4 * b] = red[4 * b + 1] = red[4 * b + 2] = red[4 * b + 3] = kKeyInf;
+  nan[b] = 0;
+}
+
+}  // namespace
+
+struct sg_handle {
+  sg_scheme scheme;
+  std::vector<BlockDev> host;
+  BlockDev* dev = nullptr;
+  unsigned long long* red = nullptr;  // 4 keys per block
+  int* nan = nullptr;
+  void** ptrs = nullptr;  // device array of nblock pointers (sg_prim)
+  void** ptrs_host = nullptr;  // pinned staging
+  int32_t nblock = 0, ntile = 0;
+  int32_t cur = 0, base = 0;  // current buffer, stage-0 buffer
+  bool bound_all = false, dirty = true;
+  size_t smem = 0, max_plane = 0, max_cells = 0;
+  int32_t max_nc1 = 0;
+  int32_t launches = 0;
+  int device = 0;
+};
+
+namespace {
+
+bool f64(const sg_handle* h) { return h->scheme.dtype == SG_F64; }
+
+size_t stage_smem(const sg_handle* h, int nc1, int nx1, int tj, int has2) {
+  return f64(h) ? sg_stage_smem_f64(nc1, nx1, tj, has2)
+                : sg_stage_smem_f32(nc1, nx1, tj, has2);
+}
+
+// tile width: enough CTAs to cover the SMs, shared memory within one CTA's
+// opt-in limit (2 CTAs per SM where it fits)
+int choose_tj(const sg_handle* h, const sg_block_desc& d, int nblock) {
+  if (d.nc2 <= 1) return 1;
+  int nx2 = d.nc2 - 2 * d.ng, nx1 = d.nc1 - 2 * d.ng;
+  int sms = 152;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
+  int best = 1;
+  for (int tj : {8, 4, 2, 1}) {
+    if (stage_smem(h, d.nc1, nx1, tj, 1) > 110 * 1024) continue;
+    long tiles = (long)((nx2 + tj - 1) / tj) * std::max(1, d.nc3 - 2 * d.ng) *
+                 nblock;
+    if (tiles >= 2L * sms) return tj;
+    best = tj;
+  }
+  return best;
+}
+
+int upload(sg_handle* h, cudaStream_t s) {
+  if (!h->dirty) return 0;
+  for (int b = 0; b < h->nblock; ++b)
+    for (int q = 0; q < 3; ++q)
+      if (!h->host[b].buf[q])
+        return fail(SG_ERR_STATE, "block %d buffer %d is not bound", b, q);
+  cudaError_t e = cudaMemcpyAsync(h->dev, h->host.data(),
+                                  sizeof(BlockDev) * h->nblock,
+                                  cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return cuda_fail(e, "upload block table");
+  e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "upload block table");
+  h->dirty = false;
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* sg_last_error(void) { return g_err.c_str(); }
+const char* sg_version(void) { return "snapy_gb300 0.1 (sm_103a)"; }
+
+int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
+              int32_t nblock, sg_handle** out) {
+  if (!scheme || !blocks || !out || nblock <= 0)
+    return fail(SG_ERR_ARG, "sg_create: null argument or nblock <= 0");
+  if (scheme->dtype != SG_F64 && scheme->dtype != SG_F32)
+    return fail(SG_ERR_ARG, "sg_create: dtype must be SG_F64 or SG_F32");
+  if (scheme->riemann != SG_HLLC && scheme->riemann != SG_LMARS)
+    return fail(SG_ERR_UNSUPPORTED, "sg_create: riemann solver %d",
+                scheme->riemann);
+  if (scheme->nstage != 3)
+    return fail(SG_ERR_UNSUPPORTED, "sg_create: only 3-stage rk3 is built");
+  auto* h = new sg_handle();
+  h->scheme = *scheme;
+  cudaGetDevice(&h->device);
+  int optin = 0;
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin,
+                         h->device);
+  h->nblock = nblock;
+  h->host.resize(nblock);
+  int tile = 0;
+  for (int b = 0; b < nblock; ++b) {
+    const sg_block_desc& d = blocks[b];
+    if (d.ng != 3) {
+      delete h;
+      return fail(SG_ERR_UNSUPPORTED, "block %d: nghost %d (3 is built)", b,
+                  d.ng);
+    }
+    if (d.nc1 < 2 * d.ng + 1 || d.nc2 < 1 || d.nc3 < 1 ||
+        (d.nc2 > 1 && d.nc2 < 2 * d.ng + 1)) {
+      delete h;
+      return fail(SG_ERR_ARG, "block %d: sizes (%d, %d, %d)", b, d.nc3, d.nc2,
+                  d.nc1);
+    }
+    if (d.nc3 > 1) {
+      delete h;
+      return fail(SG_ERR_UNSUPPORTED, "block %d: 3-D blocks (nc3 = %d)", b,
+                  d.nc3);
+    }
+    for (int f = 0; f < 6; ++f)
+      if (d.bc[f] < SG_BC_NONE || d.bc[f] > SG_BC_EXTRAPOLATION) {
+        delete h;
+        return fail(SG_ERR_ARG, "block %d: boundary kind %d", b, d.bc[f]);
+      }
+    BlockDev& B = h->host[b];
+    memset(&B, 0, sizeof(B));
+    B.nc1 = d.nc1, B.nc2 = d.nc2, B.nc3 = d.nc3, B.ng = d.ng;
+    for (int f = 0; f < 6; ++f) B.bc[f] = d.bc[f];
+    B.dx1 = d.dx1, B.dx2 = d.dx2, B.dx3 = d.dx3;
+    B.gammad = d.gammad;
+    B.cfl = scheme->cfl;
+    B.tj = d.tj > 0 ? d.tj : choose_tj(h, d, nblock);
+    int nx2 = d.nc2 > 1 ? d.nc2 - 2 * d.ng : 1;
+    B.ntile = (nx2 + B.tj - 1) / B.tj;
+    B.tile0 = tile;
+    tile += B.ntile;
+    size_t sm = stage_smem(h, d.nc1, d.nc1 - 2 * d.ng, B.tj, d.nc2 > 1);
+    if ((long)sm > optin) {
+      delete h;
+      return fail(SG_ERR_UNSUPPORTED,
+                  "block %d: a tile needs %zu B of shared memory (limit %d)",
+                  b, sm, optin);
+    }
+    h->smem = std::max(h->smem, sm);
+    size_t plane = (size_t)d.nc1 * d.nc2 * d.nc3;
+    h->max_plane = std::max(h->max_plane, plane);
+    h->max_cells = std::max(h->max_cells, plane);
+    h->max_nc1 = std::max(h->max_nc1, d.nc1);
+  }
+  h->ntile = tile;
+  cudaError_t e = cudaMalloc(&h->dev, sizeof(BlockDev) * nblock);
+  if (e == cudaSuccess)
+    e = cudaMalloc(&h->red, sizeof(unsigned long long) * 4 * nblock);
+  if (e == cudaSuccess) e = cudaMalloc(&h->nan, sizeof(int) * nblock);
+  if (e == cudaSuccess) e = cudaMalloc(&h->ptrs, sizeof(void*) * nblock);
+  if (e == cudaSuccess) e = cudaMallocHost(&h->ptrs_host, sizeof(void*) * nblock);
+  if (e != cudaSuccess) {
+    sg_destroy(h);
+    return cuda_fail(e, "sg_create");
+  }
+  init_red_kernel<<<(nblock + 127) / 128, 128>>>(nblock, h->red, h->nan);
+  e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) {
+    sg_destroy(h);
+    return cuda_fail(e, "sg_create");
+  }
+  *out = h;
+  return 0;
+}
+
+int sg_destroy(sg_handle* h) {
+  if (!h) return 0;
+  if (h->dev) cudaFree(h->dev);
+  if (h->red) cudaFree(h->red);
+  if (h->nan) cudaFree(h->nan);
+  if (h->ptrs) cudaFree(h->ptrs);
+  if (h->ptrs_host) cudaFreeHost(h->ptrs_host);
+  delete h;
+  return 0;
+}
+
+int sg_bind(sg_handle* h, int32_t block, void* b0, void* b1, void* b2) {
+  if (!h || block < 0 || block >= h->nblock)
+    return fail(SG_ERR_ARG, "sg_bind: block %d out of range", block);
+  if (!b0 || !b1 || !b2 || b0 == b1 || b1 == b2 || b0 == b2)
+    return fail(SG_ERR_ARG, "sg_bind: three distinct non-null buffers needed");
+  size_t align = f64(h) ? 8 : 4;
+  for (void* p : {b0, b1, b2})
+    if (reinterpret_cast<uintptr_t>(p) % align)
+      return fail(SG_ERR_ARG, "sg_bind: misaligned buffer");
+  BlockDev& B = h->host[block];
+  B.buf[0] = b0, B.buf[1] = b1, B.buf[2] = b2;
+  h->dirty = true;
+  return 0;
+}
+
+int sg_set_current(sg_handle* h, int32_t current) {
+  if (!h || current < 0 || current > 2)
+    return fail(SG_ERR_ARG, "sg_set_current: %d", current);
+  h->cur = h->base = current;
+  return 0;
+}
+
+int sg_current(const sg_handle* h, int32_t* current) {
+  if (!h || !current) return fail(SG_ERR_ARG, "sg_current: null");
+  *current = h->cur;
+  return 0;
+}
+
+int sg_tile(const sg_handle* h, int32_t block, int32_t* tj) {
+  if (!h || !tj || block < 0 || block >= h->nblock)
+    return fail(SG_ERR_ARG, "sg_tile: block %d", block);
+  *tj = h->host[block].tj;
+  return 0;
+}
+
+int sg_launches_per_stage(const sg_handle* h, int32_t* n) {
+  if (!h || !n) return fail(SG_ERR_ARG, "sg_launches_per_stage: null");
+  *n = h->launches;
+  return 0;
+}
+
+namespace {
+// the buffers of a stage: in = current, u0 = the stage-0 state, out = the
+// remaining one (never the input, which other tiles read as a stencil)
+void plan(const sg_handle* h, int stage, int* in, int* u0, int* out) {
+  *in = h->cur;
+  *u0 = stage == 0 ? h->cur : h->base;
+  int o = 0;
+  while (o == *in || o == *u0) ++o;
+  *out = o;
+}
+}  // namespace
+
+int sg_advance(sg_handle* h, int32_t stage) {
+  if (!h || stage < 0 || stage >= h->scheme.nstage)
+    return fail(SG_ERR_ARG, "sg_advance: stage %d", stage);
+  int in, u0, out;
+  plan(h, stage, &in, &u0, &out);
+  if (stage == 0) h->base = h->cur;
+  h->cur = out;
+  return 0;
+}
+
+int sg_rotation(const sg_handle* h, int32_t* cur, int32_t* base) {
+  if (!h || !cur || !base) return fail(SG_ERR_ARG, "sg_rotation: null");
+  *cur = h->cur;
+  *base = h->base;
+  return 0;
+}
+
+int sg_set_rotation(sg_handle* h, int32_t cur, int32_t base) {
+  if (!h || cur < 0 || cur > 2 || base < 0 || base > 2)
+    return fail(SG_ERR_ARG, "sg_set_rotation: %d %d", cur, base);
+  h->cur = cur;
+  h->base = base;
+  return 0;
+}
+
+int sg_stage(sg_handle* h, int32_t stage, const double* dt_dev,
+             sg_stream_t stream) {
+  if (!h || !dt_dev) return fail(SG_ERR_ARG, "sg_stage: null argument");
+  if (stage < 0 || stage >= h->scheme.nstage)
+    return fail(SG_ERR_ARG, "sg_stage: stage %d of %d", stage,
+                h->scheme.nstage);
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  int rc = upload(h, s);
+  if (rc) return rc;
+  int in, u0, out;
+  plan(h, stage, &in, &u0, &out);
+  StageParams p;
+  memset(&p, 0, sizeof(p));
+  p.nblock = h->nblock;
+  p.ntile = h->ntile;
+  p.in = in, p.u0 = u0, p.out = out;
+  p.riemann = h->scheme.riemann;
+  p.shock = h->scheme.shock;
+  p.scale = h->scheme.scale;
+  p.w0 = h->scheme.wght[stage][0];
+  p.w1 = h->scheme.wght[stage][1];
+  p.w2 = h->scheme.wght[stage][2];
+  p.dt = dt_dev;
+  p.max_nc1 = h->max_nc1;
+  rc = f64(h) ? sg_launch_stage_f64(h->dev, p, h->smem, s)
+              : sg_launch_stage_f32(h->dev, p, h->smem, s);
+  if (rc) return cuda_fail((cudaError_t)rc, "sg_stage: stage kernel");
+  rc = f64(h) ? sg_launch_ghost_f64(h->dev, h->nblock, out, h->max_plane, s)
+              : sg_launch_ghost_f32(h->dev, h->nblock, out, h->max_plane, s);
+  if (rc) return cuda_fail((cudaError_t)rc, "sg_stage: ghost kernel");
+  if (stage == 0) h->base = h->cur;
+  h->cur = out;
+  h->launches = 2;
+  return 0;
+}
+
+int sg_fill_ghosts(sg_handle* h, sg_stream_t stream) {
+  if (!h) return fail(SG_ERR_ARG, "sg_fill_ghosts: null");
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  int rc = upload(h, s);
+  if (rc) return rc;
+  rc = f64(h) ? sg_launch_ghost_f64(h->dev, h->nblock, h->cur, h->max_plane, s)
+              : sg_launch_ghost_f32(h->dev, h->nblock, h->cur, h->max_plane, s);
+  if (rc) return cuda_fail((cudaError_t)rc, "sg_fill_ghosts");
+  return 0;
+}
+
+int sg_max_dt(sg_handle* h, const int32_t* redo_dev, double* dt_out,
+              sg_stream_t stream) {
+  if (!h || !dt_out) return fail(SG_ERR_ARG, "sg_max_dt: null");
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  int rc = upload(h, s);
+  if (rc) return rc;
+  rc = f64(h) ? sg_launch_reduce_f64(h->dev, h->nblock, h->cur, h->red,
+                                     h->nan, h->max_cells, s)
+              : sg_launch_reduce_f32(h->dev, h->nblock, h->cur, h->red,
+                                     h->nan, h->max_cells, s);
+  if (rc) return cuda_fail((cudaError_t)rc, "sg_max_dt: reduce");
+  finish_dt_kernel<<<(h->nblock + 127) / 128, 128, 0, s>>>(
+      h->nblock, h->red, h->nan, redo_dev, h->scheme.cfl, dt_out);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "sg_max_dt: finish");
+  return 0;
+}
+
+int sg_check(sg_handle* h, int32_t* flags, sg_stream_t stream) {
+  if (!h || !flags) return fail(SG_ERR_ARG, "sg_check: null");
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  int rc = upload(h, s);
+  if (rc) return rc;
+  rc = f64(h) ? sg_launch_reduce_f64(h->dev, h->nblock, h->cur, h->red,
+                                     h->nan, h->max_cells, s)
+              : sg_launch_reduce_f32(h->dev, h->nblock, h->cur, h->red,
+                                     h->nan, h->max_cells, s);
+  if (rc) return cuda_fail((cudaError_t)rc, "sg_check: reduce");
+  finish_check_kernel<<<(h->nblock + 127) / 128, 128, 0, s>>>(
+      h->nblock, h->red, h->nan, h->scheme.density_floor,
+      h->scheme.pressure_floor, flags);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "sg_check: finish");
+  return 0;
+}
+
+int sg_init_from_prim(sg_handle* h, double* const* w_in,
+                      sg_stream_t stream) {
+  if (!h || !w_in) return fail(SG_ERR_ARG, "sg_init_from_prim: null");
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  int rc = upload(h, s);
+  if (rc) return rc;
+  cudaError_t e = cudaStreamSynchronize(s);  // the staging buffer is reused
+  if (e != cudaSuccess) return cuda_fail(e, "sg_init_from_prim");
+  for (int b = 0; b < h->nblock; ++b) {
+    if (!w_in[b]) return fail(SG_ERR_ARG, "sg_init_from_prim: block %d", b);
+    h->ptrs_host[b] = w_in[b];
+  }
+  e = cudaMemcpyAsync(h->ptrs, h->ptrs_host, sizeof(void*) * h->nblock,
+                      cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return cuda_fail(e, "sg_init_from_prim: pointers");
+  double* const* win = reinterpret_cast<double* const*>(h->ptrs);
+  rc = f64(h) ? sg_launch_init_f64(h->dev, h->nblock, h->cur, win,
+                                   h->max_plane, s)
+              : sg_launch_init_f32(h->dev, h->nblock, h->cur, win,
+                                   h->max_plane, s);
+  if (rc) return cuda_fail((cudaError_t)rc, "sg_init_from_prim");
+  h->base = h->cur;
+  return 0;
+}
+
+int sg_restore(sg_handle* h) {
+  if (!h) return fail(SG_ERR_ARG, "sg_restore: null");
+  h->cur = h->base;
+  return 0;
+}
+
+int sg_prim(sg_handle* h, void* const* w_out, sg_stream_t stream) {
+  if (!h || !w_out) return fail(SG_ERR_ARG, "sg_prim: null");
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  int rc = upload(h, s);
+  if (rc) return rc;
+  cudaError_t e = cudaStreamSynchronize(s);  // the staging buffer is reused
+  if (e != cudaSuccess) return cuda_fail(e, "sg_prim");
+  for (int b = 0; b < h->nblock; ++b) h->ptrs_host[b] = w_out[b];
+  e = cudaMemcpyAsync(h->ptrs, h->ptrs_host, sizeof(void*) * h->nblock,
+                      cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return cuda_fail(e, "sg_prim: pointers");
+  rc = f64(h) ? sg_launch_prim_f64(h->dev, h->nblock, h->cur, h->ptrs,
+                                   h->max_plane, s)
+              : sg_launch_prim_f32(h->dev, h->nblock, h->cur, h->ptrs,
+                                   h->max_plane, s);
+  if (rc) return cuda_fail((cudaError_t)rc, "sg_prim");
+  return 0;
+}
+
+}  // extern "C"

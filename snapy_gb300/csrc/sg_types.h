@@ -1,0 +1,51 @@
+// Host/device shared descriptors of the batched hydro stage.
+//
+// A batch is a set of equal-scheme blocks (a MeshBlock, an ensemble member or
+// a served request) that advance the same RK stage in ONE launch.  Each block
+// owns three rotating state buffers in HBM; a stage reads buf[in] (stencil),
+// buf[u0] (the stage-0 state, pointwise) and writes buf[out].  The rotation is
+// uniform across the batch, so the block table stays constant on the device
+// and a captured CUDA graph replays without host writes.
+#pragma once
+
+#include <stdint.h>
+
+namespace sg {
+
+enum BcKind : int32_t {
+  kBcNone = 0,  // no boundary function (custom no-op): ghosts keep their bits
+  kBcReflecting = 1,
+  kBcPeriodic = 2,
+  kBcExtrapolation = 3,
+};
+
+enum RiemannKind : int32_t { kHllc = 0, kLmars = 1 };
+
+// one block of the batch, as the device sees it
+struct BlockDev {
+  void* buf[3];         // (nvar, nc3, nc2, nc1) state buffers, storage dtype
+  int32_t nc1, nc2, nc3, ng;
+  int32_t tj;           // x2 columns per tile
+  int32_t ntile;        // tiles of this block
+  int32_t tile0;        // first tile index of this block in the batch
+  int32_t bc[6];        // BcKind per face: x1 in/out, x2 in/out, x3 in/out
+  double dx1, dx2, dx3;
+  double gammad;
+  double cfl;
+};
+
+// what a stage launch needs besides the table
+struct StageParams {
+  int32_t nblock;
+  int32_t ntile;        // total tiles (grid size)
+  int32_t in, u0, out;  // buffer indices
+  int32_t riemann;      // RiemannKind
+  int32_t shock;        // 1: every row weno5
+  int32_t scale;        // InterpOptions::scale
+  double w0, w1, w2;    // RK weights of this stage
+  const double* dt;     // device scalar: the host dt or a captured graph's
+  int32_t smem_rows;    // x1 lines held in shared memory per tile
+  int32_t max_nc1;
+};
+
+}  // namespace sg

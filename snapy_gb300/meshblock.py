@@ -1,0 +1,339 @@
+"""``MeshBlock``: the reference's block API over the GB300 hydro stage.
+
+Mirrors ``snapy.MeshBlock`` (python/csrc/pymesh.cpp:143-330 in the
+reference): ``to``, ``initialize``, ``max_time_step``, ``forward(vars, dt,
+stage)``, ``check_redo``, ``execution_report``, ``execution_capability``,
+``part``, ``total_u``, ``intg``.  The stage itself runs in
+``libsnapy_gb300.so``; this module only keeps the reference's bookkeeping
+(variables dict, redo counter, graph cache).
+
+State handling follows the reference's StateStore (src/mesh/state_store.hpp):
+``vars["hydro_u"]`` is a view of block-owned storage; after every ``forward``
+it is re-pointed (``Tensor.set_``) at the buffer holding the new state, so a
+caller holding the tensor always sees the current state, and a tensor the
+caller rebinds is adopted (copied in) at the next stage.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+from typing import Dict, Optional
+
+import torch
+
+from . import _lib
+from .batch import Batch
+from .options import DeckError, MeshBlockOptions
+
+kIDN, kIVX, kIVY, kIVZ, kIPR, kICY = 0, 1, 2, 3, 4, 5
+kIV1 = kIVX
+
+_BC = {"reflecting": _lib.BC_REFLECTING, "periodic": _lib.BC_PERIODIC,
+       "extrapolation": _lib.BC_EXTRAPOLATION, "": _lib.BC_NONE,
+       "custom": _lib.BC_NONE}
+
+
+def scheme_of(options: MeshBlockOptions) -> dict:
+    """The library scheme of a deck; refuses what the stage does not build."""
+    h = options.hydro()
+    c = options.coord()
+    if c.type != "cartesian":
+        raise DeckError(f"geometry/type '{c.type}': this stage builds cartesian")
+    if h.eos.type != "ideal-gas":
+        raise DeckError(f"equation-of-state '{h.eos.type}': this stage builds "
+                        "ideal-gas")
+    if h.eos.limiter:
+        raise DeckError("equation-of-state/limiter: true is not built")
+    if c.nghost != 3:
+        raise DeckError(f"nghost {c.nghost}: weno5 needs nghost 3")
+    for r in (h.recon1, h.recon23):
+        if r.type != "weno5":
+            raise DeckError(f"reconstruct type '{r.type}': weno5 is built")
+    if (h.recon1.shock, h.recon1.scale) != (h.recon23.shock, h.recon23.scale):
+        raise DeckError("vertical and horizontal reconstruct must share shock "
+                        "and scale")
+    if h.riemann.type not in ("hllc", "lmars"):
+        raise DeckError(f"riemann-solver '{h.riemann.type}' is not built")
+    if h.grav is not None and (h.grav.grav1 or h.grav.grav2 or h.grav.grav3):
+        raise DeckError("forcing/const-gravity is not built")
+    if h.diffusion is not None:
+        raise DeckError("forcing/diffusion is not built")
+    if h.icorr is not None:
+        raise DeckError("integration/implicit-scheme is not built")
+    if c.nx3 > 1:
+        raise DeckError("3-D blocks are not built")
+    intg = options.intg()
+    return {
+        "riemann": _lib.HLLC if h.riemann.type == "hllc" else _lib.LMARS,
+        "shock": h.recon1.shock,
+        "scale": h.recon1.scale,
+        "wght": [(w.wght0, w.wght1, w.wght2) for w in intg.stages],
+        "cfl": intg.cfl,
+        "density_floor": h.eos.density_floor,
+        "pressure_floor": h.eos.pressure_floor,
+    }
+
+
+def block_of(options: MeshBlockOptions, tj: int = 0) -> dict:
+    c = options.coord()
+    names = list(options.bcnames) + [""] * (6 - len(options.bcnames))
+    bc = []
+    for n in names[:6]:
+        kind = n.rsplit("_", 1)[0] if n else ""
+        if kind == "outflow":
+            raise DeckError("boundary 'outflow' (radiating) is not built; "
+                            "use extrapolation")
+        if kind not in _BC:
+            raise DeckError(f"boundary '{kind}' is not built")
+        bc.append(_BC[kind])
+    return {"nc1": c.nc1, "nc2": c.nc2, "nc3": c.nc3, "ng": c.nghost,
+            "dx1": c.dx1, "dx2": c.dx2 if c.nx2 > 1 else (c.x2max - c.x2min),
+            "dx3": c.dx3 if c.nx3 > 1 else (c.x3max - c.x3min),
+            "gammad": options.hydro().eos.gammad, "bc": bc, "tj": tj}
+
+
+@dataclass
+class _Intg:
+    options: object
+    current_redo: int = 0
+
+    @property
+    def stages(self):
+        return self.options.stages
+
+
+class MeshBlock:
+    """One block of the hydro stage on one GPU."""
+
+    def __init__(self, options: MeshBlockOptions, tj: int = 0):
+        self.options = options
+        self._scheme = scheme_of(options)
+        self._block = block_of(options, tj)
+        self.intg = _Intg(options.intg())
+        self.pintg = self.intg
+        self.cycle = 0
+        self.device = torch.device("cuda", torch.cuda.current_device()) \
+            if torch.cuda.is_available() else torch.device("cpu")
+        self.dtype = torch.float64 if options.hydro().precision == "float64" \
+            else torch.float32
+        self._batch: Optional[Batch] = None
+        self._graphs: Dict[tuple, torch.cuda.CUDAGraph] = {}
+        self._report = {"captures": 0, "replays": 0, "eager": 0, "graphs": 0,
+                        "host": 0}
+        self._seen = set()
+
+    # -- module-like API -----------------------------------------------------
+    def to(self, device, dtype: Optional[torch.dtype] = None) -> "MeshBlock":
+        device = torch.device(device)
+        if device.type != "cuda":
+            raise RuntimeError("snapy_gb300 runs on CUDA only; no CPU path")
+        if device.index is None:
+            device = torch.device("cuda", torch.cuda.current_device())
+        self.device = device
+        if dtype is not None:
+            if dtype not in (torch.float32, torch.float64):
+                raise ValueError(f"dtype {dtype}")
+            self.dtype = dtype
+        self._batch = None
+        self._graphs.clear()
+        self._seen.clear()
+        return self
+
+    @property
+    def batch(self) -> Batch:
+        if self._batch is None:
+            self._batch = Batch(self._scheme, [self._block], self.device, self.dtype)
+        return self._batch
+
+    def nc(self):
+        c = self.options.coord()
+        return (c.nc3, c.nc2, c.nc1)
+
+    # -- reference API ---------------------------------------------------------
+    def initialize(self, vars: dict):
+        """Boundary functions on hydro_w (in place), hydro_u = W->U(hydro_w)."""
+        if "hydro_w" not in vars:
+            raise RuntimeError("initialize: hydro_w is required for hydro model.")
+        w = vars["hydro_w"]
+        shape = (5,) + self.nc()
+        if tuple(w.shape) != shape:
+            raise RuntimeError(f"initialize: hydro_w has incorrect shape. "
+                               f"Expected {list(shape)} but got {list(w.shape)}")
+        if w.device != self.device:
+            raise RuntimeError(f"initialize: hydro_w must be on {self.device}")
+        if w.dtype != torch.float64:
+            raise RuntimeError("initialize: hydro_w must be float64")
+        if not w.is_contiguous():
+            vars["hydro_w"] = w = w.contiguous()
+        with torch.cuda.device(self.device):
+            self.batch.init_from_prim([w])
+            u = self.batch.current(0)
+        vars["hydro_u"] = torch.empty(0, dtype=self.dtype, device=self.device).set_(u)
+        self.intg.current_redo = 0
+        return vars, 0.0
+
+    def _adopt(self, vars: dict) -> None:
+        u = vars.get("hydro_u")
+        cur = self.batch.current(0)
+        if u is None:
+            raise RuntimeError("forward: vars has no hydro_u; call initialize")
+        if u.data_ptr() != cur.data_ptr():
+            cur.copy_(u)  # a rebound hydro_u is copied into block storage
+            u.set_(cur)
+            self._report["host"] += 1
+
+    def forward(self, vars: dict, dt: float, stage: int) -> None:
+        """One RK stage (MeshBlockImpl::forward, meshblock_advance.cpp:88).
+
+        With execution auto / cuda-graph the stage's launches are captured
+        once per (stage, buffer rotation) after an eager warm-up call and
+        replayed; the dt is read from device memory, so one graph serves every
+        dt (the reference's StepDt)."""
+        nst = len(self.intg.stages)
+        if not 0 <= stage < nst:
+            raise RuntimeError(f"Invalid stage: {stage}")
+        with torch.cuda.device(self.device):
+            self._adopt(vars)
+            b = self.batch
+            b.dt.fill_(float(dt))
+            rot = b.rotation()
+            key = (stage,) + rot
+            use_graph = self.options.execution != "eager"
+            g = self._graphs.get(key) if use_graph else None
+            if g is None and use_graph and key in self._seen:
+                g = self._capture(stage, rot)
+            if g is not None:
+                g.replay()
+                b.advance(stage)
+                self._report["replays"] += 1
+            else:
+                b.stage(stage)
+                self._seen.add(key)
+                self._report["eager"] += 1
+            vars["hydro_u"].set_(b.current(0))
+
+    def step(self, vars: dict, dt: float) -> None:
+        """All stages of one step (the driver loop's ``for stage ...
+        forward``), as ONE captured graph per buffer rotation when execution
+        allows graphs.  Equal bit for bit to calling ``forward`` per stage."""
+        nst = len(self.intg.stages)
+        with torch.cuda.device(self.device):
+            self._adopt(vars)
+            b = self.batch
+            b.dt.fill_(float(dt))
+            rot = b.rotation()
+            key = ("step",) + rot
+            use_graph = self.options.execution != "eager"
+            g = self._graphs.get(key) if use_graph else None
+            if g is None and use_graph and key in self._seen:
+                g = self._capture(None, rot)
+            if g is not None:
+                g.replay()
+                for s in range(nst):
+                    b.advance(s)
+                self._report["replays"] += 1
+            else:
+                for s in range(nst):
+                    b.stage(s)
+                self._seen.add(key)
+                self._report["eager"] += 1
+            vars["hydro_u"].set_(b.current(0))
+
+    def _capture(self, stage, rot) -> torch.cuda.CUDAGraph:
+        b = self.batch
+        g = torch.cuda.CUDAGraph()
+        s = torch.cuda.Stream(device=self.device)
+        s.wait_stream(torch.cuda.current_stream())
+        try:
+            with torch.cuda.stream(s):
+                g.capture_begin()
+                try:
+                    if stage is None:
+                        for st in range(len(self.intg.stages)):
+                            b.stage(st)
+                    else:
+                        b.stage(stage)
+                finally:
+                    g.capture_end()
+        finally:
+            b.set_rotation(rot)  # the capture ran nothing: rewind the rotation
+        torch.cuda.current_stream().wait_stream(s)
+        self._graphs[("step" if stage is None else stage,) + tuple(rot)] = g
+        self._report["captures"] += 1
+        self._report["graphs"] = len(self._graphs)
+        return g
+
+    def max_time_step(self, vars: dict) -> float:
+        with torch.cuda.device(self.device):
+            self.batch.redo.fill_(self.intg.current_redo)
+            dt = self.batch.max_dt()
+            return float(dt[0].item())
+
+    def check_redo(self, vars: dict) -> int:
+        with torch.cuda.device(self.device):
+            flags = int(self.batch.check()[0].item())
+            if flags:
+                self.batch.restore()
+                vars["hydro_u"].set_(self.batch.current(0))
+                self.intg.current_redo += 1
+                self._refresh_w(vars)
+                if self.intg.current_redo > self.intg.options.max_redo:
+                    return -1
+                return 1
+            self.intg.current_redo = 0
+            self._refresh_w(vars)
+            return 0
+
+    def _refresh_w(self, vars: dict) -> None:
+        # "Retain the checked primitives for output and the next timestep"
+        # (meshblock_redo.cpp:99-104): hydro_w <- W(hydro_u)
+        w = vars.get("hydro_w")
+        shape = (5,) + self.nc()
+        if w is None or tuple(w.shape) != shape or w.device != self.device:
+            vars["hydro_w"] = w = torch.empty(shape, dtype=torch.float64,
+                                              device=self.device)
+        if w.dtype == self.dtype:
+            self.batch.prim([w])
+        else:
+            tmp = torch.empty(shape, dtype=self.dtype, device=self.device)
+            self.batch.prim([tmp])
+            w.copy_(tmp)
+
+    def prim(self) -> torch.Tensor:
+        """W of the current state (storage dtype)."""
+        shape = (5,) + self.nc()
+        out = torch.empty(shape, dtype=self.dtype, device=self.device)
+        with torch.cuda.device(self.device):
+            self.batch.prim([out])
+        return out
+
+    def total_u(self, vars) -> torch.Tensor:
+        u = vars["hydro_u"] if isinstance(vars, dict) else vars
+        return u.clone()
+
+    def part(self, offset=(0, 0, 0), exterior: bool = True, extend_x1: int = 0,
+             extend_x2: int = 0, extend_x3: int = 0):
+        """Index of the interior (exterior=False) or of a neighbour slab, as
+        MeshBlockImpl::part (src/mesh/meshblock.cpp:190-288) for offset 0."""
+        c = self.options.coord()
+        ng = c.nghost
+        out = []
+        for n, o, ext in ((c.nc3, offset[0], extend_x3), (c.nc2, offset[1], extend_x2),
+                          (c.nc1, offset[2], extend_x1)):
+            if n == 1:
+                out.append(slice(0, 1, 1))
+            elif o != 0:
+                raise NotImplementedError("part: neighbour offsets are not built")
+            else:
+                out.append(slice(ng - ext, n - ng + ext, 1))
+        return (slice(None),) + tuple(out)
+
+    def execution_report(self) -> dict:
+        return dict(self._report)
+
+    def execution_capability(self, vars: dict) -> dict:
+        seg = {"index": 0, "kind": "stage", "capturable": True,
+               "reads_host_dt": False, "host": False,
+               "ops": ["advance", "combine", "boundaries"], "reasons": []}
+        fp64 = self.dtype == torch.float64
+        return {"eager_fp64": fp64, "eager_fp32": not fp64, "graph_fp64": fp64,
+                "graph_fp32": not fp64, "eager_reasons": [], "segments": [seg]}
