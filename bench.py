@@ -45,7 +45,8 @@ sys.path.insert(0, ROOT)
 WORKLOADS = {
     # the 2-D density-current shape of the Straka config: 512 x 128 cells at
     # 50 m, LMARS + WENO5 (cp5 for velocity/pressure) + RK3, reflecting walls
-    "straka": "snapy_gb300/decks/straka_explicit.yaml",
+    "straka": "snapy_gb300/decks/straka_noimplicit.yaml",
+    "straka-shape": "snapy_gb300/decks/straka_explicit.yaml",
     "sod": "snapy_gb300/decks/sod.yaml",
 }
 
@@ -172,15 +173,8 @@ def cpu_baseline(opts, workload, seconds, u0_host=None):
     from oracle import oracle as O
     O.build()
     c = opts.coord()
-    h = opts.hydro()
-    bcs = [n.rsplit("_", 1)[0] if n else "none" for n in opts.bcnames]
-    bcs += ["none"] * (6 - len(bcs))
     cores = os.cpu_count() or 1
-    ob = O.Block(nc1=c.nc1, nc2=c.nc2, nc3=c.nc3, dx1=c.dx1,
-                 dx2=c.dx2 if c.nx2 > 1 else c.x2max - c.x2min,
-                 dx3=c.dx3 if c.nx3 > 1 else c.x3max - c.x3min,
-                 gammad=h.eos.gammad, riemann=h.riemann.type,
-                 shock=h.recon1.shock, scale=h.recon1.scale, bc=bcs, nthreads=cores)
+    ob = O.block_from_options(opts, nthreads=cores)
     w = initial_state(opts, workload, "cpu").numpy()
     u = ob.initialize(w)
     dt = opts.intg().cfl * ob.max_dt(u)

@@ -80,6 +80,17 @@ typedef struct sg_block_desc {
   double dx1, dx2, dx3;
   double gammad;
   int32_t tj; /* x2 columns per tile, 0 = the library's choice */
+  /* forcing/const-gravity/grav1 (0: none); with it the x1 reconstruction is
+   * the well-balanced one (src/recon/well_balanced_x1.cpp) */
+  double grav1;
+  double nu_iso;         /* forcing/diffusion/nu_iso (0: none) */
+  int32_t flux_cov;      /* dynamics/flux-covariance */
+  int32_t wb_wall_clamp; /* dynamics/wb-wall-clamp */
+  /* FP64 x1 geometry on the device: faces [nc1 + 1] and centres [nc1]
+   * (the reference's linspace faces), read by the covariance row and the
+   * gravity work; may be null without gravity and covariance */
+  const double* x1f;
+  const double* x1v;
 } sg_block_desc;
 
 int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,

@@ -27,7 +27,6 @@ BC_CODES = {
     "reflecting": BC_REFLECTING,
     "periodic": BC_PERIODIC,
     "extrapolation": BC_EXTRAPOLATION,
-    "outflow": BC_EXTRAPOLATION,
 }
 
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -53,6 +52,13 @@ class OgBlock(ctypes.Structure):
         ("bc", ctypes.c_int * 6),
         ("wght", (ctypes.c_double * 3) * 3),
         ("nthreads", ctypes.c_int),
+        ("grav1", ctypes.c_double),
+        ("nu_iso", ctypes.c_double),
+        ("flux_cov", ctypes.c_int),
+        ("wb_wall_clamp", ctypes.c_int),
+        ("x1f", _dp),
+        ("x1v", _dp),
+        ("x2v", _dp),
     ]
 
 
@@ -94,6 +100,9 @@ def lib():
         L.og_max_dt.restype = ctypes.c_double
         L.og_max_dt.argtypes = [bp, _dp]
         L.og_initialize.argtypes = [bp, _dp, _dp]
+        L.og_tendency.argtypes = [bp, _dp, ctypes.c_double, _dp]
+        L.og_ref_column.argtypes = [bp, _dp, ctypes.c_size_t, _dp, _dp, _dp,
+                                    _dp, _dp, _dp]
         _lib = L
     return _lib
 
@@ -113,8 +122,44 @@ def ref():
         R.ref_cons2prim.argtypes = [_dp, _dp, ctypes.c_double]
         R.ref_pressure_scan.argtypes = [_dp, _dp, _dp, _dp, ctypes.c_int,
                                         ctypes.c_int, ctypes.c_double]
+        R.ref_hydro_ref_column.argtypes = [_dp, _dp, _dp, _dp, _dp, _dp, _dp,
+                                           ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_double, ctypes.c_int,
+                                           ctypes.c_int, ctypes.c_int]
         _ref = R
     return _ref
+
+
+def faces_linspace(xmin, dx, nc, ng=3):
+    """Face coordinates of a padded axis as the reference builds them:
+    torch.linspace(min - ng dx, max + ng dx, n + 2 ng + 1) in FP64 (callers
+    with a deck pass the deck's own faces, CoordinateOptions.faces)."""
+    import torch
+    if nc <= 1:
+        return np.array([xmin, xmin + dx])
+    n = nc - 2 * ng
+    xmax = xmin + n * dx
+    return torch.linspace(xmin - ng * dx, xmax + ng * dx, nc + 1,
+                          dtype=torch.float64).numpy()
+
+
+def block_from_options(opts, nthreads=0):
+    """An oracle block of a snapy_gb300 deck (options parsed by the product's
+    reader; the geometry arrays come from the same linspace)."""
+    c = opts.coord()
+    h = opts.hydro()
+    bcs = [n.rsplit("_", 1)[0] if n else "none" for n in opts.bcnames]
+    bcs += ["none"] * (6 - len(bcs))
+    g = h.grav.grav1 if h.grav else 0.0
+    nu = h.diffusion.nu_iso if h.diffusion else 0.0
+    return Block(nc1=c.nc1, nc2=c.nc2, nc3=c.nc3, dx1=c.dx1,
+                 dx2=c.dx2 if c.nx2 > 1 else c.x2max - c.x2min,
+                 dx3=c.dx3 if c.nx3 > 1 else c.x3max - c.x3min,
+                 gammad=h.eos.gammad, riemann=h.riemann.type,
+                 shock=h.recon1.shock, scale=h.recon1.scale, bc=bcs,
+                 nthreads=nthreads, x1min=c.x1min, x2min=c.x2min,
+                 x3min=c.x3min, grav1=g, nu_iso=nu,
+                 flux_cov=h.flux_covariance, x1f=c.faces(1), x2f=c.faces(2))
 
 
 def ptr(a: np.ndarray):
@@ -128,7 +173,8 @@ class Block:
     def __init__(self, *, nc1, nc2=1, nc3=1, dx1=1.0, dx2=1.0, dx3=1.0,
                  gammad=1.4, riemann="hllc", shock=True, scale=False,
                  bc=("extrapolation",) * 6, nthreads=0, x1min=0.0, x2min=0.0,
-                 x3min=0.0):
+                 x3min=0.0, grav1=0.0, nu_iso=0.0, flux_cov=True,
+                 wb_wall_clamp=True, x1f=None, x2f=None):
         L = lib()
         b = OgBlock()
         L.og_default_block(ctypes.byref(b))
@@ -143,6 +189,19 @@ class Block:
         for f in range(6):
             b.bc[f] = BC_CODES[bc[f]] if isinstance(bc[f], str) else int(bc[f])
         b.nthreads = nthreads
+        b.grav1, b.nu_iso = grav1, nu_iso
+        b.flux_cov, b.wb_wall_clamp = int(bool(flux_cov)), int(bool(wb_wall_clamp))
+        # the reference's faces: a linspace over the padded extent
+        # (CoordinateImpl::block_faces_, src/coord/coordinate.cpp:410-425)
+        if x1f is None:
+            x1f = faces_linspace(x1min, dx1, nc1)
+        if x2f is None:
+            x2f = faces_linspace(x2min, dx2, nc2)
+        self.x1f = np.ascontiguousarray(x1f, dtype=np.float64)
+        self.x1v = np.ascontiguousarray(0.5 * (self.x1f[:-1] + self.x1f[1:]))
+        self.x2f = np.ascontiguousarray(x2f, dtype=np.float64)
+        self.x2v = np.ascontiguousarray(0.5 * (self.x2f[:-1] + self.x2f[1:]))
+        b.x1f, b.x1v, b.x2v = ptr(self.x1f), ptr(self.x1v), ptr(self.x2v)
         self.b = b
         self.shape = (5, nc3, nc2, nc1)
         self.u0 = np.zeros(self.shape)
@@ -167,6 +226,11 @@ class Block:
     def step(self, u: np.ndarray, dt: float) -> None:
         for s in range(3):
             self.stage(u, dt, s)
+
+    def tendency(self, w: np.ndarray, dt: float) -> np.ndarray:
+        du = np.zeros(self.shape)
+        lib().og_tendency(ctypes.byref(self.b), ptr(np.ascontiguousarray(w)), dt, ptr(du))
+        return du
 
     def flux(self, w: np.ndarray, d: int) -> np.ndarray:
         f = np.zeros(self.shape)

@@ -74,4 +74,16 @@ void ref_pressure_scan(const double* w, const double* dx1f, double* psf_lo,
                                        nc1, iu, grav);
 }
 
+// the whole per-column reference of hydro_ref_x1_impl (scan, cell pressure,
+// face and cell densities) on a uniform x1 grid, one column
+void ref_hydro_ref_column(const double* w, const double* dx1f, double* psf_lo,
+                          double* psf_hi, double* pref, double* dsf,
+                          double* dref, int nc1, int iu, double grav,
+                          int phys_in, int phys_out, int wall_clamp) {
+  snap::hydro_ref_x1_impl<double>(w, dx1f, nullptr, psf_lo, psf_hi, pref, dsf,
+                                  dref, 0, 1, nc1, iu, grav,
+                                  snap::kX1RefUniform, phys_in != 0,
+                                  phys_out != 0, wall_clamp != 0, nullptr);
+}
+
 }  // extern "C"

@@ -36,6 +36,7 @@
 #include "sg_oracle.h"
 
 #include <math.h>
+#include <stddef.h>
 #include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
@@ -319,6 +320,8 @@ void og_default_block(og_block* b) {
   b->wght[0][0] = 1.;      b->wght[0][1] = 0.;      b->wght[0][2] = 1.;
   b->wght[1][0] = 3. / 4.; b->wght[1][1] = 1. / 4.; b->wght[1][2] = 1. / 4.;
   b->wght[2][0] = 1. / 3.; b->wght[2][1] = 2. / 3.; b->wght[2][2] = 2. / 3.;
+  b->flux_cov = 1;
+  b->wb_wall_clamp = 1;
 }
 
 static size_t ncell(const og_block* b) {
@@ -465,28 +468,492 @@ void og_flux(const og_block* b, const double* w, int d, double* flux) {
   }
 }
 
-/* flux_register.cpp:700-740 with supply_prescribed (seam_register.cpp:184):
- * on a reflecting (wall) face plane the rows other than the momenta are
- * zeroed */
-static void prescribe_walls(const og_block* b, double* flux, int d) {
-  int n = dir_size(b, d);
-  size_t s = dir_stride(b, d), nc = ncell(b);
-  int n1 = b->nc1, n2 = b->nc2, n3 = b->nc3;
-  int la = d == 1 ? n2 : n1, lb = d == 3 ? n2 : n3;
-  for (int side = 0; side < 2; ++side) {
-    if (b->bc[2 * (d - 1) + side] != OG_BC_REFLECTING) continue;
-    int plane = side ? n - b->ng : b->ng;
-    for (int bidx = 0; bidx < lb; ++bidx)
-      for (int a = 0; a < la; ++a) {
-        size_t base;
-        if (d == 1) base = ((size_t)bidx * n2 + a) * n1;
-        else if (d == 2) base = (size_t)bidx * n2 * n1 + a;
-        else base = (size_t)bidx * n1 + a;
-        flux[OG_IDN * nc + base + plane * s] = 0.;
-        flux[OG_IPR * nc + base + plane * s] = 0.;
-      }
+/* ------------------------------------------------------------------ */
+/* well-balanced x1 reference (src/hydro/hydro_ref_x1_impl.h:20-272,   */
+/* src/recon/x1_reference.cpp:96-240), uniform x1 grid, one block     */
+/* column with physical x1 boundaries                                 */
+/* ------------------------------------------------------------------ */
+static double ref_face(const double* lo, const double* hi, int f, int nc1) {
+  return f < nc1 ? lo[f] : hi[nc1 - 1];
+}
+
+static double wall_rop(double r0, double r1, double k) {
+  double q = r0 / r1, qk = k == floor(k) ? q : pow(q, k);
+  for (int n = 1; k == floor(k) && n < k; ++n) qk *= q;
+  double e = r1 > r0 ? r0 * qk : r0 + k * (r0 - r1);
+  return e > 0. ? e : r0;
+}
+
+static double rop_at(const double* w, size_t plane, int j) {
+  return w[OG_IDN * plane + j] / w[OG_IPR * plane + j];
+}
+
+static double rop_smooth(const double* w, size_t plane, int i, int jlo,
+                         int jhi, int ext_lo, int ext_hi) {
+  if (!(ext_lo && i - 2 < jlo) && !(ext_hi && i + 2 > jhi))
+    return rop_at(w, plane, i < jlo ? jlo : (i > jhi ? jhi : i));
+  double v[5];
+  for (int m = -2; m <= 2; ++m) {
+    int j = i + m;
+    if (j < jlo)
+      v[m + 2] = ext_lo ? wall_rop(rop_at(w, plane, jlo),
+                                   rop_at(w, plane, jlo + 1), (double)(jlo - j))
+                        : rop_at(w, plane, jlo);
+    else if (j > jhi)
+      v[m + 2] = ext_hi ? wall_rop(rop_at(w, plane, jhi),
+                                   rop_at(w, plane, jhi - 1), (double)(j - jhi))
+                        : rop_at(w, plane, jhi);
+    else
+      v[m + 2] = rop_at(w, plane, j);
+  }
+  return (v[0] + 4. * v[1] + 6. * v[2] + 4. * v[3] + v[4]) / 16.;
+}
+
+void og_ref_column(const og_block* b, const double* w, size_t plane,
+                   double* psf_lo, double* psf_hi, double* pref, double* dsf,
+                   double* dref, double* dsf_lr) {
+  build_tables();
+  const int nc1 = b->nc1, iu = nc1 - 1 - b->ng, il = nc1 - 1 - iu;
+  const double grav = -b->grav1; /* the downward magnitude */
+  const double dx = b->dx1;
+  const int phys_in = b->bc[0] != OG_BC_NONE, phys_out = b->bc[1] != OG_BC_NONE;
+  const int wall_clamp = b->wb_wall_clamp;
+  /* hydro_ref_x1_scan_impl: anchored half a cell above the top cell */
+  double rho_top = w[OG_IDN * plane + iu], pres_top = w[OG_IPR * plane + iu];
+  double rdt_top = pres_top / rho_top;
+  double top_anchor = pres_top * exp(-grav * 0.5 * dx / rdt_top);
+  const double minp = 2.2250738585072014e-308; /* DBL_MIN */
+  double face = top_anchor;
+  for (int i = iu; i >= 0; --i) {
+    double dp = grav * w[OG_IDN * plane + i] * dx;
+    double lo = face + dp, hi = face;
+    psf_lo[i] = lo > minp ? lo : minp;
+    psf_hi[i] = hi > minp ? hi : minp;
+    face = lo;
+  }
+  face = top_anchor;
+  for (int i = iu + 1; i < nc1; ++i) {
+    double dp = grav * w[OG_IDN * plane + i] * dx;
+    double lo = face, hi = lo - dp;
+    psf_lo[i] = lo > minp ? lo : minp;
+    psf_hi[i] = hi > minp ? hi : minp;
+    face = hi;
+  }
+  /* hydro_ref_x1_cell_impl, uniform grid */
+  static const double w6[6] = {11. / 1440., -31. / 480., 401. / 720.,
+                               401. / 720., -31. / 480., 11. / 1440.};
+  static const double w6e[2][6] = {
+      {95. / 288., 1427. / 1440., -133. / 240., 241. / 720., -173. / 1440.,
+       3. / 160.},
+      {-3. / 160., 637. / 1440., 511. / 720., -43. / 240., 77. / 1440.,
+       -11. / 1440.}};
+  int thin = (iu - il + 1) < 5, fits = iu >= 4;
+  int jlo = (wall_clamp && phys_in) ? il : 0;
+  int jhi = (wall_clamp && phys_out) ? iu : nc1 - 1;
+  int ext_lo = wall_clamp && phys_in && il + 1 <= iu;
+  int ext_hi = wall_clamp && phys_out && iu - 1 >= il;
+  double rs_prev = 0.;
+  for (int i = 0; i < nc1; ++i) {
+    int wall_in = wall_clamp && phys_in && i >= il && i < il + 2;
+    int wall_out = wall_clamp && phys_out && i > iu - 2 && i <= iu;
+    int clamp_in = wall_in && fits && !(thin && phys_out);
+    int clamp_out = wall_out && fits && !(thin && phys_in);
+    double lo = psf_lo[i], hi = psf_hi[i];
+    double cell_pref = 0.5 * (lo + hi);
+    double lower = lo < hi ? lo : hi, upper = lo > hi ? lo : hi;
+#define SIX(start, wt, rev)                                              \
+  do {                                                                   \
+    double value = 0.;                                                   \
+    for (int m = 0; m < 6; ++m)                                          \
+      value += (wt)[(rev) ? 5 - m : m] *                                 \
+               ref_face(psf_lo, psf_hi, (start) + m, nc1);               \
+    if (value >= lower && value <= upper) cell_pref = value;             \
+  } while (0)
+    if (i >= 2 && i < nc1 - 2 && !wall_in && !wall_out) SIX(i - 2, w6, 0);
+    if (clamp_in) SIX(il, w6e[i - il], 0);
+    if (clamp_out) {
+      int s0 = iu + 1 - 5;
+      SIX(s0, w6e[4 - (i - s0)], 1);
+    }
+    if (!phys_in && i < 2) SIX(0, w6e[i], 0);
+    if (!phys_out && i >= nc1 - 2) SIX(nc1 - 5, w6e[4 - (i - (nc1 - 5))], 1);
+#undef SIX
+    pref[i] = cell_pref;
+    double rs = rop_smooth(w, plane, i, jlo, jhi, ext_lo, ext_hi);
+    double rf = rs;
+    if (i > 0) rf = 0.5 * (rs_prev + rs);
+    rs_prev = rs;
+    dref[i] = cell_pref * rs;
+    dsf[i] = lo * rf;
+  }
+  /* x1_reference.cpp:183-238: per-side face density from the cp5 row on
+   * dref, guarded by the two cells' range; a reflecting wall face takes the
+   * mean of its two sides */
+  double* dl = dsf_lr;       /* ILT */
+  double* dr = dsf_lr + nc1; /* IRT */
+  for (int f = 0; f < nc1; ++f) dl[f] = dr[f] = dsf[f];
+  if (nc1 >= 6) {
+    int il5 = 3, iu5 = nc1 - 3;
+    double lin_l[nc1], lin_r[nc1];
+    for (int f = 0; f < nc1; ++f) lin_l[f] = lin_r[f] = dsf[f];
+    for (int f = il5 - 1; f <= iu5; ++f) lin_r[f] = poly5_point(dref + f - 2, 1, g_cp5_cm);
+    for (int f = il5; f <= iu5 + 1 && f < nc1; ++f)
+      lin_l[f] = poly5_point(dref + f - 3, 1, g_cp5_cp);
+    for (int f = il5 - 1; f <= iu5 + 1; ++f) {
+      double a = dref[f - 1], c = dref[f];
+      double lo = a < c ? a : c, hi = a > c ? a : c;
+      if (lin_l[f] >= lo && lin_l[f] <= hi) dl[f] = lin_l[f];
+      if (lin_r[f] >= lo && lin_r[f] <= hi) dr[f] = lin_r[f];
+    }
+    for (int side = 0; side < 2; ++side) {
+      if (b->bc[side] != OG_BC_REFLECTING) continue;
+      int f = side == 0 ? il : iu + 1;
+      double mean = 0.5 * (dl[f] + dr[f]);
+      dl[f] = dr[f] = mean;
+    }
   }
 }
+
+/* ------------------------------------------------------------------ */
+/* the hydro tendency (src/hydro/hydro_forward.cpp:299-1235)           */
+/* ------------------------------------------------------------------ */
+static double recon_one(const double* c, size_t s, int weno, int side,
+                        int scale) {
+  double st[5];
+  for (int k = 0; k < 5; ++k) st[k] = c[(ptrdiff_t)k * (ptrdiff_t)s];
+  if (weno) return weno5_point(st, 1, side ? g_weno5_cp : g_weno5_cm, scale);
+  return poly5_point(st, 1, side ? g_cp5_cp : g_cp5_cm);
+}
+
+/* face f states of a line (cell stride s, variable stride plane):
+ * ILT from cells f-3..f+1 (cp), IRT from cells f-2..f+2 (cm) */
+static void face_lr(const og_block* b, const double* line, size_t s,
+                    size_t plane, int f, double* wl, double* wr) {
+  for (int v = 0; v < 5; ++v) {
+    int weno = b->shock || v == OG_IDN;
+    const double* q = line + v * plane;
+    wl[v] = recon_one(q + (ptrdiff_t)(f - 3) * (ptrdiff_t)s, s, weno, 1,
+                      b->weno_scale);
+    wr[v] = recon_one(q + (ptrdiff_t)(f - 2) * (ptrdiff_t)s, s, weno, 0,
+                      b->weno_scale);
+  }
+}
+
+static void riemann_face(const og_block* b, const double* wl, const double* wr,
+                         int d, double* fx) {
+  if (b->riemann == OG_HLLC)
+    og_hllc_face(wl, wr, b->gammad, 4 - d, fx, NULL);
+  else
+    og_lmars_face(wl, wr, b->gammad, 4 - d, fx, NULL);
+}
+
+#define CELL(v, j, i) ((size_t)(v) * nc + (size_t)(j) * n1 + (size_t)(i))
+
+void og_tendency(const og_block* b, const double* w, double dt, double* du) {
+  build_tables();
+  const int n1 = b->nc1, n2 = b->nc2, ng = b->ng;
+  const size_t nc = ncell(b);
+  if (b->nc3 > 1) { /* the 3-D path is not restated */
+    memset(du, 0, sizeof(double) * 5 * nc);
+    return;
+  }
+  const int has2 = n2 > 1;
+  const int il = ng, iu1 = n1 - ng; /* interior x1 cells il..iu1-1 */
+  const int jl = has2 ? ng : 0, ju1 = has2 ? n2 - ng : 1;
+  const int wb = b->grav1 != 0.;
+  double* f1 = (double*)calloc(5 * nc, sizeof(double));
+  double* f2 = has2 ? (double*)calloc(5 * nc, sizeof(double)) : NULL;
+
+  /* (2) x1 faces il..iu1 of every interior column j */
+#pragma omp parallel for schedule(static)
+  for (int j = jl; j < ju1; ++j) {
+    const double* col = w + (size_t)j * n1;
+    double wl[5], wr[5], fx[5];
+    if (!wb) {
+      for (int f = il; f <= iu1; ++f) {
+        face_lr(b, col, 1, nc, f, wl, wr);
+        riemann_face(b, wl, wr, 1, fx);
+        for (int v = 0; v < 5; ++v) f1[CELL(v, j, f)] = fx[v];
+      }
+    } else {
+      double psf_lo[n1], psf_hi[n1], pref[n1], dsf[n1], dref[n1], dlr[2 * n1];
+      og_ref_column(b, col, nc, psf_lo, psf_hi, pref, dsf, dref, dlr);
+      /* WellBalancedX1::forward: the perturbations of p and rho about the
+       * reference, even-mirrored into the wall ghosts */
+      double wx[5 * n1];
+      for (int v = 0; v < 5; ++v)
+        for (int i = 0; i < n1; ++i) wx[v * n1 + i] = col[v * nc + i];
+      for (int i = 0; i < n1; ++i) {
+        wx[OG_IPR * n1 + i] -= pref[i];
+        wx[OG_IDN * n1 + i] -= dref[i];
+      }
+      for (int c = 0; c < 2; ++c) {
+        int v = c ? OG_IDN : OG_IPR;
+        if (b->bc[0] != OG_BC_NONE)
+          for (int g = 0; g < ng; ++g) wx[v * n1 + g] = wx[v * n1 + 2 * ng - 1 - g];
+        if (b->bc[1] != OG_BC_NONE)
+          for (int g = 0; g < ng; ++g)
+            wx[v * n1 + iu1 + g] = wx[v * n1 + iu1 - 1 - g];
+      }
+      for (int f = il; f <= iu1; ++f) {
+        face_lr(b, wx, 1, n1, f, wl, wr);
+        double pl = wl[OG_IPR] + psf_lo[f], pr = wr[OG_IPR] + psf_lo[f];
+        wl[OG_IPR] = pl > 0. ? pl : psf_lo[f];
+        wr[OG_IPR] = pr > 0. ? pr : psf_lo[f];
+        double dl = wl[OG_IDN] + dlr[f], dr = wr[OG_IDN] + dlr[n1 + f];
+        double below = col[OG_IDN * nc + (f > 0 ? f - 1 : 0)];
+        wl[OG_IDN] = dl > 0. ? dl : below;
+        wr[OG_IDN] = dr > 0. ? dr : col[OG_IDN * nc + f];
+        riemann_face(b, wl, wr, 1, fx);
+        for (int v = 0; v < 5; ++v) f1[CELL(v, j, f)] = fx[v];
+      }
+    }
+    /* boundary.prescribed: rows IDN and IPR on the x1 wall faces */
+    if (b->bc[0] == OG_BC_REFLECTING) f1[CELL(OG_IDN, j, il)] = f1[CELL(OG_IPR, j, il)] = 0.;
+    if (b->bc[1] == OG_BC_REFLECTING) f1[CELL(OG_IDN, j, iu1)] = f1[CELL(OG_IPR, j, iu1)] = 0.;
+  }
+
+  /* (3-4) x2 faces jl..ju1 of the x1-interior cells, with the covariance
+   * row of _flux_covariance (Cartesian: IPR only, x1 cells 1..n1-2) */
+  if (has2) {
+    const int cov = b->flux_cov && n1 >= 3;
+#pragma omp parallel for schedule(static)
+    for (int j = jl; j <= ju1; ++j) {
+      double wl[5], wr[5], fx[5];
+      double h[n1], un[n1], rho[n1];
+      for (int i = 0; i < n1; ++i) {
+        face_lr(b, w + i, n1, nc, j, wl, wr);
+        if (cov) {
+          double wb_[5];
+          for (int v = 0; v < 5; ++v) wb_[v] = 0.5 * (wl[v] + wr[v]);
+          double p = wb_[OG_IPR];
+          double enth = p / (b->gammad - 1) + p;
+          rho[i] = wb_[OG_IDN];
+          h[i] = enth / rho[i];
+          un[i] = wb_[OG_IVY];
+        }
+        if (i >= il && i < iu1) {
+          riemann_face(b, wl, wr, 2, fx);
+          for (int v = 0; v < 5; ++v) f2[CELL(v, j, i)] = fx[v];
+        }
+      }
+      if (cov) {
+        for (int i = il; i < iu1; ++i) {
+          double dx1 = b->x1v[i + 1] - b->x1v[i - 1];
+          double s2 = b->dx1 * b->dx1 / 12.;
+          double s2rho = s2 * rho[i];
+          double d1h = (h[i + 1] - h[i - 1]) / dx1;
+          double dun = (un[i + 1] - un[i - 1]) / dx1;
+          f2[CELL(OG_IPR, j, i)] += s2rho * d1h * dun;
+        }
+      }
+      int wall = (j == jl && b->bc[2] == OG_BC_REFLECTING) ||
+                 (j == ju1 && b->bc[3] == OG_BC_REFLECTING);
+      if (wall)
+        for (int i = il; i < iu1; ++i)
+          f2[CELL(OG_IDN, j, i)] = f2[CELL(OG_IPR, j, i)] = 0.;
+    }
+  }
+
+  /* viscous fluxes (src/forcing/diffusion.cpp:553-683, Cartesian, kinematic
+   * nu_iso, no heat conduction): momentum rows separately (vf1, vf2),
+   * the energy row posted into the totals */
+  double *vf1 = NULL, *vf2 = NULL;
+  if (b->nu_iso > 0.) {
+    vf1 = (double*)calloc(5 * nc, sizeof(double));
+    vf2 = has2 ? (double*)calloc(5 * nc, sizeof(double)) : NULL;
+    double* divv = (double*)calloc(nc, sizeof(double));
+    /* div of velocity on the interior extended by one cell in each active
+     * direction */
+    int ja = has2 ? jl - 1 : 0, jb = has2 ? ju1 + 1 : 1;
+    for (int j = ja; j < jb; ++j)
+      for (int i = il - 1; i < iu1 + 1; ++i) {
+        double dv = divv[(size_t)j * n1 + i];
+        dv += (w[CELL(OG_IVX, j, i + 1)] - w[CELL(OG_IVX, j, i - 1)]) / (2. * b->dx1);
+        if (has2)
+          dv += (w[CELL(OG_IVY, j + 1, i)] - w[CELL(OG_IVY, j - 1, i)]) / (2. * b->dx2);
+        divv[(size_t)j * n1 + i] = dv;
+      }
+    const double nu = b->nu_iso;
+    /* x1 faces f = il..iu1, x2 cells jl..ju1-1 */
+    int wall_lo = b->bc[0] == OG_BC_REFLECTING, wall_hi = b->bc[1] == OG_BC_REFLECTING;
+    int nface1 = iu1 + 1 - il;
+    for (int j = jl; j < ju1; ++j)
+      for (int f = il; f <= iu1; ++f) {
+        double rf = 0.5 * (w[CELL(OG_IDN, j, f)] + w[CELL(OG_IDN, j, f - 1)]);
+        if (nface1 >= 3) {
+          double t = b->dx1 / (b->dx1 + b->dx1);
+          if (f == il && wall_lo) {
+            double vn = w[CELL(OG_IDN, j, il)], vx = w[CELL(OG_IDN, j, il + 1)];
+            double wall = (1. + t) * vn - t * vx;
+            rf = wall > 0. ? wall : vn;
+          }
+          if (f == iu1 && wall_hi) {
+            double vn = w[CELL(OG_IDN, j, iu1 - 1)], vx = w[CELL(OG_IDN, j, iu1 - 2)];
+            double wall = (1. + t) * vn - t * vx;
+            rf = wall > 0. ? wall : vn;
+          }
+        }
+        double divf = 0.5 * (divv[(size_t)j * n1 + f] + divv[(size_t)j * n1 + f - 1]);
+        double e = 0.;
+        for (int ivar = 0; ivar < 3; ++ivar) {
+          int v = OG_IVX + ivar;
+          double stress = (w[CELL(v, j, f)] - w[CELL(v, j, f - 1)]) / b->dx1;
+          if (ivar == 0) {
+            stress = 2. * stress - (2. / 3.) * divf;
+          } else if (ivar == 1 && has2) {
+            double below = (w[CELL(OG_IVX, j + 1, f - 1)] - w[CELL(OG_IVX, j - 1, f - 1)]) / (2. * b->dx2);
+            double above = (w[CELL(OG_IVX, j + 1, f)] - w[CELL(OG_IVX, j - 1, f)]) / (2. * b->dx2);
+            stress += 0.5 * (above + below);
+          }
+          double mf = -nu * rf * stress;
+          vf1[CELL(v, j, f)] = mf;
+          e += 0.5 * (w[CELL(v, j, f)] + w[CELL(v, j, f - 1)]) * mf;
+        }
+        vf1[CELL(OG_IPR, j, f)] = e;
+      }
+    /* x2 faces j = jl..ju1, x1 cells il..iu1-1 */
+    if (has2)
+      for (int j = jl; j <= ju1; ++j)
+        for (int i = il; i < iu1; ++i) {
+          double rf = 0.5 * (w[CELL(OG_IDN, j, i)] + w[CELL(OG_IDN, j - 1, i)]);
+          double divf = 0.5 * (divv[(size_t)j * n1 + i] + divv[(size_t)(j - 1) * n1 + i]);
+          double e = 0.;
+          for (int ivar = 0; ivar < 3; ++ivar) {
+            int v = OG_IVX + ivar;
+            double stress = (w[CELL(v, j, i)] - w[CELL(v, j - 1, i)]) / b->dx2;
+            if (ivar == 1) {
+              stress = 2. * stress - (2. / 3.) * divf;
+            } else if (ivar == 0) {
+              double below = (w[CELL(OG_IVY, j - 1, i + 1)] - w[CELL(OG_IVY, j - 1, i - 1)]) / (2. * b->dx1);
+              double above = (w[CELL(OG_IVY, j, i + 1)] - w[CELL(OG_IVY, j, i - 1)]) / (2. * b->dx1);
+              stress += 0.5 * (above + below);
+            }
+            double mf = -nu * rf * stress;
+            vf2[CELL(v, j, i)] = mf;
+            e += 0.5 * (w[CELL(v, j, i)] + w[CELL(v, j - 1, i)]) * mf;
+          }
+          vf2[CELL(OG_IPR, j, i)] = e;
+        }
+    free(divv);
+    /* post_fluxes: the energy rows join the totals; boundary.prescribed
+     * again on the wall faces */
+    for (int j = jl; j < ju1; ++j) {
+      for (int f = il; f <= iu1; ++f) f1[CELL(OG_IPR, j, f)] += vf1[CELL(OG_IPR, j, f)];
+      if (b->bc[0] == OG_BC_REFLECTING) f1[CELL(OG_IDN, j, il)] = f1[CELL(OG_IPR, j, il)] = 0.;
+      if (b->bc[1] == OG_BC_REFLECTING) f1[CELL(OG_IDN, j, iu1)] = f1[CELL(OG_IPR, j, iu1)] = 0.;
+    }
+    if (has2)
+      for (int j = jl; j <= ju1; ++j) {
+        for (int i = il; i < iu1; ++i) f2[CELL(OG_IPR, j, i)] += vf2[CELL(OG_IPR, j, i)];
+        int wall = (j == jl && b->bc[2] == OG_BC_REFLECTING) ||
+                   (j == ju1 && b->bc[3] == OG_BC_REFLECTING);
+        if (wall)
+          for (int i = il; i < iu1; ++i) f2[CELL(OG_IDN, j, i)] = f2[CELL(OG_IPR, j, i)] = 0.;
+      }
+  }
+
+  /* (5-6) divergence and du = -dt div on the interior */
+  const double a1 = b->dx3 * b->dx2, a2 = b->dx3 * b->dx1;
+  const double vol = b->dx3 * (b->dx2 * b->dx1);
+  memset(du, 0, sizeof(double) * 5 * nc);
+  const double mdt = -dt;
+  for (int v = 0; v < 5; ++v)
+    for (int j = jl; j < ju1; ++j)
+      for (int i = il; i < iu1; ++i) {
+        size_t q = CELL(v, j, i);
+        double dv = a1 * f1[q + 1] - a1 * f1[q];
+        if (has2) dv = dv + (a2 * f2[q + n1] - a2 * f2[q]);
+        du[q] = mdt * (dv / vol);
+      }
+
+  /* constant gravity (src/forcing/const_gravity.cpp:37-42, nh = 1) */
+  if (b->grav1 != 0.) {
+    const double g = b->grav1, nh = 1.;
+    for (int j = jl; j < ju1; ++j)
+      for (int i = il; i < iu1; ++i) {
+        double rho = w[CELL(OG_IDN, j, i)], vx = w[CELL(OG_IVX, j, i)];
+        du[CELL(OG_IVX, j, i)] += dt * rho * g * nh;
+        du[CELL(OG_IPR, j, i)] += dt * rho * vx * g * nh;
+      }
+  }
+
+  /* the viscous momentum rows (DiffusionImpl::add): du -= dt div */
+  if (vf1) {
+    for (int v = 0; v < OG_IPR; ++v)
+      for (int j = jl; j < ju1; ++j)
+        for (int i = il; i < iu1; ++i) {
+          size_t q = CELL(v, j, i);
+          double dv = a1 * vf1[q + 1] - a1 * vf1[q];
+          if (has2) dv = dv + (a2 * vf2[q + n1] - a2 * vf2[q]);
+          du[q] = du[q] - dt * (dv / vol);
+        }
+  }
+
+  /* the x1 gravity energy correction (hydro_forward.cpp:1049-1124):
+   * face-form work + corrected potential-energy work - the cell work */
+  if (b->grav1 != 0.) {
+    const double g = b->grav1;
+    const int nx1 = iu1 - il;
+    /* centroid slope stencil on x1v[il..iu1) (gravity_work.hpp:93-115) */
+    double wt0[nx1], wt1[nx1], wt2[nx1];
+    int i0[nx1];
+    const double* x = b->x1v + il;
+    if (nx1 >= 3) {
+      double a = x[1] - x[0], bb = x[2] - x[1], c = x[nx1 - 2] - x[nx1 - 3],
+             d = x[nx1 - 1] - x[nx1 - 2];
+      for (int k = 0; k < nx1; ++k) {
+        if (k == 0) {
+          wt0[k] = -(2. * a + bb) / (a * (a + bb));
+          wt1[k] = (a + bb) / (a * bb);
+          wt2[k] = -(a / ((a + bb) * bb));
+        } else if (k == nx1 - 1) {
+          wt0[k] = d / (c * (c + d));
+          wt1[k] = -((c + d) / (c * d));
+          wt2[k] = (c + 2. * d) / ((c + d) * d);
+        } else {
+          double hm = x[k] - x[k - 1], hp = x[k + 1] - x[k];
+          wt0[k] = -hp / (hm * (hm + hp));
+          wt1[k] = (hp - hm) / (hm * hp);
+          wt2[k] = hm / (hp * (hm + hp));
+        }
+        int jj = k < 1 ? 1 : (k > nx1 - 2 ? nx1 - 2 : k);
+        i0[k] = jj - 1;
+      }
+    }
+    for (int j = jl; j < ju1; ++j) {
+      double drho[nx1];
+      for (int k = 0; k < nx1; ++k) {
+        int i = il + k;
+        double vmd = (a1 * f1[CELL(OG_IDN, j, i + 1)] - a1 * f1[CELL(OG_IDN, j, i)]) / vol;
+        drho[k] = mdt * vmd;
+      }
+      for (int k = 0; k < nx1; ++k) {
+        int i = il + k;
+        double hi = g * (b->x1f[i + 1] - b->x1v[i]);
+        double lo = g * (b->x1f[i] - b->x1v[i]);
+        double fm_hi = a1 * f1[CELL(OG_IDN, j, i + 1)], fm_lo = a1 * f1[CELL(OG_IDN, j, i)];
+        double fgw = dt * ((hi * fm_hi - lo * fm_lo) / vol);
+        if (nx1 >= 3) {
+          double h = b->x1f[i + 1] - b->x1f[i];
+          double gvar = g * (h * h / 12.);
+          double sl = wt0[k] * drho[i0[k]];
+          sl += wt1[k] * drho[i0[k] + 1];
+          sl += wt2[k] * drho[i0[k] + 2];
+          fgw += gvar * sl;
+        }
+        double rho = w[CELL(OG_IDN, j, i)], vx = w[CELL(OG_IVX, j, i)];
+        double orig = dt * rho * vx * g * 1.;
+        du[CELL(OG_IPR, j, i)] += fgw - orig;
+      }
+    }
+  }
+  free(f1);
+  free(f2);
+  free(vf1);
+  free(vf2);
+}
+#undef CELL
 
 void og_stage(const og_block* b, double* u, double* u0, double dt, int stage) {
 #ifdef _OPENMP
@@ -496,56 +963,17 @@ void og_stage(const og_block* b, double* u, double* u0, double dt, int stage) {
   size_t nall = nc * b->nvar;
   if (stage == 0) memcpy(u0, u, sizeof(double) * nall);
   double* w = (double*)malloc(sizeof(double) * nall);
-  double* f1 = (double*)calloc(nall, sizeof(double));
-  double* f2 = b->nc2 > 1 ? (double*)calloc(nall, sizeof(double)) : NULL;
-  double* f3 = b->nc3 > 1 ? (double*)calloc(nall, sizeof(double)) : NULL;
+  double* du = (double*)malloc(sizeof(double) * nall);
   og_cons2prim(b, u, w);
-  if (b->nc1 > 1) {
-    og_flux(b, w, 1, f1);
-    prescribe_walls(b, f1, 1);
-  }
-  if (f2) {
-    og_flux(b, w, 2, f2);
-    prescribe_walls(b, f2, 2);
-  }
-  if (f3) {
-    og_flux(b, w, 3, f3);
-    prescribe_walls(b, f3, 3);
-  }
-  /* coordinate.cpp:488-515: area1 = dx3 dx2, area2 = dx3 dx1,
-   * area3 = dx2 dx1, vol = dx3 (dx2 dx1) */
-  double a1 = b->dx3 * b->dx2, a2 = b->dx3 * b->dx1, a3 = b->dx2 * b->dx1;
-  double vol = b->dx3 * (b->dx2 * b->dx1);
-  int ng = b->ng;
-  int i0 = b->nc1 > 1 ? ng : 0, i1 = b->nc1 > 1 ? b->nc1 - ng : 1;
-  int j0 = b->nc2 > 1 ? ng : 0, j1 = b->nc2 > 1 ? b->nc2 - ng : 1;
-  int k0 = b->nc3 > 1 ? ng : 0, k1 = b->nc3 > 1 ? b->nc3 - ng : 1;
+  og_tendency(b, w, dt, du);
   const double* wt = b->wght[stage];
-  double mdt = -dt;
   /* the RK combine runs on every cell; du is zero outside the interior */
-#pragma omp parallel for schedule(static) if (nc > 4096)
-  for (long c = 0; c < (long)nc; ++c) {
-    int i = (int)(c % b->nc1), j = (int)((c / b->nc1) % b->nc2),
-        k = (int)(c / ((size_t)b->nc1 * b->nc2));
-    int inner = i >= i0 && i < i1 && j >= j0 && j < j1 && k >= k0 && k < k1;
-    for (int v = 0; v < b->nvar; ++v) {
-      size_t q = v * nc + c;
-      double du = 0.;
-      if (inner) {
-        double dv = 0.;
-        if (b->nc1 > 1) dv = dv + (a1 * f1[q + 1] - a1 * f1[q]);
-        if (f2) dv = dv + (a2 * f2[q + b->nc1] - a2 * f2[q]);
-        if (f3) dv = dv + (a3 * f3[q + (size_t)b->nc1 * b->nc2] - a3 * f3[q]);
-        du = mdt * (dv / vol);
-      }
-      u[q] = wt[0] * u0[q] + wt[1] * u[q] + wt[2] * du;
-    }
-  }
+#pragma omp parallel for schedule(static) if (nall > 4096)
+  for (long q = 0; q < (long)nall; ++q)
+    u[q] = wt[0] * u0[q] + wt[1] * u[q] + wt[2] * du[q];
   og_apply_bc(b, u, 0);
   free(w);
-  free(f1);
-  free(f2);
-  free(f3);
+  free(du);
 }
 
 double og_max_dt(const og_block* b, const double* w) {
@@ -573,6 +1001,19 @@ double og_max_dt(const og_block* b, const double* w) {
   double dt = dtm[0];
   if (dtm[1] < dt) dt = dtm[1];
   if (dtm[2] < dt) dt = dtm[2];
+  /* sources.max_time_step: the viscous bound dx^2 / (2 ndim nu)
+   * (src/forcing/diffusion.cpp:686-740) */
+  if (b->nu_iso > 0.) {
+    int ndim = 0;
+    double dxm = 1.7976931348623157e308;
+    for (int d = 0; d < 3; ++d)
+      if (nn[d] > 1) {
+        ++ndim;
+        if (dx[d] < dxm) dxm = dx[d];
+      }
+    double dtv = dxm * dxm / (2. * ndim * b->nu_iso);
+    if (dtv < dt) dt = dtv;
+  }
   return dt;
 }
 

@@ -12,6 +12,8 @@
 #ifndef SG_ORACLE_H
 #define SG_ORACLE_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -39,6 +41,16 @@ typedef struct og_block {
   /* RK3 weights (w0, w1, w2) per stage: u <- w0 u0 + w1 u + w2 du */
   double wght[3][3];
   int nthreads;        /* OpenMP threads, 0 = default */
+  /* the Straka-class physics (0 = off) */
+  double grav1;        /* forcing/const-gravity/grav1 (x1 acceleration) */
+  double nu_iso;       /* forcing/diffusion/nu_iso (kinematic viscosity) */
+  int flux_cov;        /* dynamics/flux-covariance */
+  int wb_wall_clamp;   /* dynamics/wb-wall-clamp */
+  /* geometry of the padded block: x1f[nc1 + 1], x1v[nc1] (the reference's
+   * linspace faces), x2v[nc2] */
+  const double* x1f;
+  const double* x1v;
+  const double* x2v;
 } og_block;
 
 /* ---- unit functions (pinned against the reference headers) ---- */
@@ -63,6 +75,14 @@ void og_apply_bc(const og_block* b, double* q, int primitive);
 void og_flux(const og_block* b, const double* w, int d, double* flux);
 /* one RK stage: u is advanced in place; u0 holds the stage-0 backup */
 void og_stage(const og_block* b, double* u, double* u0, double dt, int stage);
+/* the hydro tendency of one stage (HydroImpl::forward): du on every cell
+ * (zero outside the interior), from the primitives w */
+void og_tendency(const og_block* b, const double* w, double dt, double* du);
+/* the well-balanced x1 reference of one column (w strided by `plane`):
+ * psf_lo, psf_hi, pref, dsf, dref [nc1] and dsf_lr [2][nc1] */
+void og_ref_column(const og_block* b, const double* w, size_t plane,
+                   double* psf_lo, double* psf_hi, double* pref, double* dsf,
+                   double* dref, double* dsf_lr);
 /* the hydro time step (before cfl), reference HydroImpl::max_time_step */
 double og_max_dt(const og_block* b, const double* w);
 /* initialize: boundaries on w, W->U, boundaries on u */

@@ -47,6 +47,12 @@ class BlockDesc(ctypes.Structure):
         ("dx3", ctypes.c_double),
         ("gammad", ctypes.c_double),
         ("tj", _i32),
+        ("grav1", ctypes.c_double),
+        ("nu_iso", ctypes.c_double),
+        ("flux_cov", _i32),
+        ("wb_wall_clamp", _i32),
+        ("x1f", _vp),
+        ("x1v", _vp),
     ]
 
 

@@ -48,6 +48,14 @@ class Batch:
         sch.density_floor = scheme["density_floor"]
         sch.pressure_floor = scheme["pressure_floor"]
         arr = (_lib.BlockDesc * self.nblock)()
+        # FP64 x1 geometry per block on the device (kept alive here)
+        self.geom = []
+        for d in blocks:
+            f = torch.as_tensor(d["x1f"], dtype=torch.float64, device=device) \
+                if d.get("x1f") is not None else None
+            v = torch.as_tensor(d["x1v"], dtype=torch.float64, device=device) \
+                if d.get("x1v") is not None else None
+            self.geom.append((f, v))
         for b, d in enumerate(blocks):
             a = arr[b]
             a.nc1, a.nc2, a.nc3, a.ng = d["nc1"], d["nc2"], d["nc3"], d["ng"]
@@ -56,6 +64,13 @@ class Batch:
             a.dx1, a.dx2, a.dx3 = d["dx1"], d["dx2"], d["dx3"]
             a.gammad = d["gammad"]
             a.tj = d.get("tj", 0)
+            a.grav1 = d.get("grav1", 0.0)
+            a.nu_iso = d.get("nu_iso", 0.0)
+            a.flux_cov = int(bool(d.get("flux_cov", True)))
+            a.wb_wall_clamp = int(bool(d.get("wb_wall_clamp", True)))
+            f, v = self.geom[b]
+            a.x1f = f.data_ptr() if f is not None else None
+            a.x1v = v.data_ptr() if v is not None else None
         self.shapes = [(5, d["nc3"], d["nc2"], d["nc1"]) for d in blocks]
         h = ctypes.c_void_p()
         with torch.cuda.device(device):

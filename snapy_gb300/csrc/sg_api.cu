@@ -2,6 +2,7 @@
 // buffer bookkeeping on the host, launches on the caller's stream, and the
 // two tiny finishing kernels of the per-step reductions.
 #include <cuda_runtime.h>
+#include <math.h>
 #include <stdarg.h>
 #include <stdio.h>
 #include <string.h>
@@ -18,7 +19,8 @@ using sg::StageParams;
 
 // per-precision launchers (sg_stage.cu compiled for double and for float)
 #define SG_DECLARE(sfx)                                                        \
-  extern "C" size_t sg_stage_smem##sfx(int nc1, int nx1, int tj, int has2);    \
+  extern "C" size_t sg_stage_smem##sfx(int nc1, int tj, int has2, int wb,      \
+                                       int cov, int visc);                     \
   extern "C" int sg_launch_stage##sfx(const BlockDev*, StageParams, size_t,    \
                                       cudaStream_t);                           \
   extern "C" int sg_launch_ghost##sfx(const BlockDev*, int, int, size_t,       \
@@ -119,21 +121,23 @@ namespace {
 
 bool f64(const sg_handle* h) { return h->scheme.dtype == SG_F64; }
 
-size_t stage_smem(const sg_handle* h, int nc1, int nx1, int tj, int has2) {
-  return f64(h) ? sg_stage_smem_f64(nc1, nx1, tj, has2)
-                : sg_stage_smem_f32(nc1, nx1, tj, has2);
+size_t stage_smem(const sg_handle* h, const sg_block_desc& d, int tj) {
+  int has2 = d.nc2 > 1, wb = d.grav1 != 0., cov = d.flux_cov && d.nc1 >= 3;
+  int visc = d.nu_iso > 0.;
+  return f64(h) ? sg_stage_smem_f64(d.nc1, tj, has2, wb, cov, visc)
+                : sg_stage_smem_f32(d.nc1, tj, has2, wb, cov, visc);
 }
 
 // tile width: enough CTAs to cover the SMs, shared memory within one CTA's
 // opt-in limit (2 CTAs per SM where it fits)
 int choose_tj(const sg_handle* h, const sg_block_desc& d, int nblock) {
   if (d.nc2 <= 1) return 1;
-  int nx2 = d.nc2 - 2 * d.ng, nx1 = d.nc1 - 2 * d.ng;
+  int nx2 = d.nc2 - 2 * d.ng;
   int sms = 152;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
   int best = 1;
   for (int tj : {8, 4, 2, 1}) {
-    if (stage_smem(h, d.nc1, nx1, tj, 1) > 110 * 1024) continue;
+    if (stage_smem(h, d, tj) > 110 * 1024) continue;
     long tiles = (long)((nx2 + tj - 1) / tj) * std::max(1, d.nc3 - 2 * d.ng) *
                  nblock;
     if (tiles >= 2L * sms) return tj;
@@ -215,12 +219,45 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
     B.dx1 = d.dx1, B.dx2 = d.dx2, B.dx3 = d.dx3;
     B.gammad = d.gammad;
     B.cfl = scheme->cfl;
+    B.grav1 = d.grav1;
+    B.nu_iso = d.nu_iso;
+    B.flux_cov = d.flux_cov;
+    B.wb_wall_clamp = d.wb_wall_clamp;
+    B.x1f = d.x1f;
+    B.x1v = d.x1v;
+    B.dt_src = INFINITY;
+    if (d.nu_iso > 0.) {  // DiffusionImpl::max_time_step, kinematic nu
+      int ndim = 0;
+      double dxm = 1.7976931348623157e308;
+      const double dxs[3] = {d.dx1, d.dx2, d.dx3};
+      const int ns[3] = {d.nc1, d.nc2, d.nc3};
+      for (int q = 0; q < 3; ++q)
+        if (ns[q] > 1) {
+          ++ndim;
+          if (dxs[q] < dxm) dxm = dxs[q];
+        }
+      B.dt_src = dxm * dxm / (2. * ndim * d.nu_iso);
+    }
+    if ((d.grav1 != 0. || (d.flux_cov && d.nc2 > 1)) && (!d.x1f || !d.x1v)) {
+      delete h;
+      return fail(SG_ERR_ARG, "block %d: gravity and the covariance row need "
+                  "the x1 geometry (x1f, x1v)", b);
+    }
+    if (d.grav1 != 0. && scheme->dtype != SG_F64) {
+      delete h;
+      return fail(SG_ERR_UNSUPPORTED, "block %d: gravity in the FP32 stage "
+                  "kernel", b);
+    }
+    if (d.grav1 != 0. && (d.bc[0] == SG_BC_PERIODIC || d.bc[1] == SG_BC_PERIODIC)) {
+      delete h;
+      return fail(SG_ERR_UNSUPPORTED, "block %d: gravity with a periodic x1", b);
+    }
     B.tj = d.tj > 0 ? d.tj : choose_tj(h, d, nblock);
     int nx2 = d.nc2 > 1 ? d.nc2 - 2 * d.ng : 1;
     B.ntile = (nx2 + B.tj - 1) / B.tj;
     B.tile0 = tile;
     tile += B.ntile;
-    size_t sm = stage_smem(h, d.nc1, d.nc1 - 2 * d.ng, B.tj, d.nc2 > 1);
+    size_t sm = stage_smem(h, d, B.tj);
     if ((long)sm > optin) {
       delete h;
       return fail(SG_ERR_UNSUPPORTED,

@@ -96,6 +96,152 @@ __device__ __forceinline__ void riemann(const real* wl, const real* wr,
     lmars_flux<real>(wl, wr, gammad, d, flx, nullptr);
 }
 
+// smem layout of a tile (counts in `real`), shared by the kernel and the
+// host-side size query
+struct TileLayout {
+  int R, ntj, nc1, nx1;
+  bool has2, wb, cov, visc;
+  int w, f1, f2, ref, cov_arr, divv, vf1, vf2;  // offsets
+  int total;
+  __host__ __device__ TileLayout(int ntj_, int nc1_, int ng, bool has2_,
+                                 bool wb_, bool cov_, bool visc_)
+      : ntj(ntj_), nc1(nc1_), has2(has2_), wb(wb_), cov(cov_ && has2_),
+        visc(visc_) {
+    nx1 = nc1 - 2 * ng;
+    int hj = has2 ? ng : 0;
+    R = ntj + 2 * hj;
+    int o = 0;
+    w = o;
+    o += NHYDRO * R * nc1;
+    f1 = o;
+    o += NHYDRO * ntj * (nx1 + 1);
+    f2 = o;
+    o += has2 ? NHYDRO * (ntj + 1) * nx1 : 0;
+    ref = o;  // psf_lo, psf_hi, pref, dref, dsf_l, dsf_r per tile row
+    o += wb ? 6 * ntj * nc1 : 0;
+    cov_arr = o;  // rho, h, un of the x2 face means, x1 rows 0..nc1-1
+    o += cov ? 3 * (ntj + 1) * nc1 : 0;
+    divv = o;  // div v on tile rows -1..ntj, all x1 cells
+    o += visc ? (ntj + 2) * nc1 : 0;
+    vf1 = o;  // viscous momentum fluxes, x1 faces
+    o += visc ? 3 * ntj * (nx1 + 1) : 0;
+    vf2 = o;  // viscous momentum fluxes, x2 faces
+    o += (visc && has2) ? 3 * (ntj + 1) * nx1 : 0;
+    total = o;
+  }
+};
+
+// the well-balanced x1 reference of one column (src/hydro/hydro_ref_x1_impl.h
+// :20-272 and src/recon/x1_reference.cpp:183-238): one thread runs the
+// column's serial face-pressure scan, in the reference's order, so the face
+// pressures carry the reference's rounding
+__device__ __forceinline__ void ref_scan(const real* rho, const real* pres,
+                                         int nc1, int iu, double dx,
+                                         double grav, real* psf_lo,
+                                         real* psf_hi) {
+  const double minp = 2.2250738585072014e-308;
+  double rdt_top = (double)pres[iu] / (double)rho[iu];
+  double top = (double)pres[iu] * exp(-grav * 0.5 * dx / rdt_top);
+  double face = top;
+  for (int i = iu; i >= 0; --i) {
+    double dp = grav * (double)rho[i] * dx;
+    double lo = face + dp, hi = face;
+    psf_lo[i] = lo > minp ? lo : minp;
+    psf_hi[i] = hi > minp ? hi : minp;
+    face = lo;
+  }
+  face = top;
+  for (int i = iu + 1; i < nc1; ++i) {
+    double dp = grav * (double)rho[i] * dx;
+    double lo = face, hi = lo - dp;
+    psf_lo[i] = lo > minp ? lo : minp;
+    psf_hi[i] = hi > minp ? hi : minp;
+    face = hi;
+  }
+}
+
+__device__ __forceinline__ double wall_rop(double r0, double r1, double k) {
+  double q = r0 / r1, qk = k == floor(k) ? q : pow(q, k);
+  for (int n = 1; k == floor(k) && n < k; ++n) qk *= q;
+  double e = r1 > r0 ? r0 * qk : r0 + k * (r0 - r1);
+  return e > 0. ? e : r0;
+}
+
+__device__ __forceinline__ double rop_smooth(const real* rho, const real* pres,
+                                             int i, int jlo, int jhi,
+                                             bool ext_lo, bool ext_hi) {
+  auto rop = [&](int j) { return (double)rho[j] / (double)pres[j]; };
+  if (!(ext_lo && i - 2 < jlo) && !(ext_hi && i + 2 > jhi))
+    return rop(i < jlo ? jlo : (i > jhi ? jhi : i));
+  double v[5];
+#pragma unroll
+  for (int m = -2; m <= 2; ++m) {
+    int j = i + m;
+    if (j < jlo)
+      v[m + 2] = ext_lo ? wall_rop(rop(jlo), rop(jlo + 1), (double)(jlo - j))
+                        : rop(jlo);
+    else if (j > jhi)
+      v[m + 2] = ext_hi ? wall_rop(rop(jhi), rop(jhi - 1), (double)(j - jhi))
+                        : rop(jhi);
+    else
+      v[m + 2] = rop(j);
+  }
+  return (v[0] + 4. * v[1] + 6. * v[2] + 4. * v[3] + v[4]) / 16.;
+}
+
+__constant__ double c_w6[6] = {11. / 1440., -31. / 480., 401. / 720.,
+                               401. / 720., -31. / 480., 11. / 1440.};
+__constant__ double c_w6e[2][6] = {
+    {95. / 288., 1427. / 1440., -133. / 240., 241. / 720., -173. / 1440.,
+     3. / 160.},
+    {-3. / 160., 637. / 1440., 511. / 720., -43. / 240., 77. / 1440.,
+     -11. / 1440.}};
+
+// hydro_ref_x1_cell_impl (uniform grid) for cell i of one column
+__device__ __forceinline__ void ref_cell(const real* rho, const real* pres,
+                                         const real* psf_lo,
+                                         const real* psf_hi, int i, int nc1,
+                                         int iu, bool phys_in, bool phys_out,
+                                         bool wall_clamp, real* pref,
+                                         real* dref, real* dsf) {
+  const int il = nc1 - 1 - iu;
+  bool thin = (iu - il + 1) < 5, fits = iu >= 4;
+  bool wall_in = wall_clamp && phys_in && i >= il && i < il + 2;
+  bool wall_out = wall_clamp && phys_out && i > iu - 2 && i <= iu;
+  bool clamp_in = wall_in && fits && !(thin && phys_out);
+  bool clamp_out = wall_out && fits && !(thin && phys_in);
+  double lo = psf_lo[i], hi = psf_hi[i];
+  double cell_pref = 0.5 * (lo + hi);
+  double lower = lo < hi ? lo : hi, upper = lo > hi ? lo : hi;
+  auto face = [&](int f) -> double {
+    return f < nc1 ? (double)psf_lo[f] : (double)psf_hi[nc1 - 1];
+  };
+  auto six = [&](int start, const double* wt, bool rev) {
+    double value = 0.;
+    for (int m = 0; m < 6; ++m) value += wt[rev ? 5 - m : m] * face(start + m);
+    if (value >= lower && value <= upper) cell_pref = value;
+  };
+  if (i >= 2 && i < nc1 - 2 && !wall_in && !wall_out) six(i - 2, c_w6, false);
+  if (clamp_in) six(il, c_w6e[i - il], false);
+  if (clamp_out) {
+    int s0 = iu + 1 - 5;
+    six(s0, c_w6e[4 - (i - s0)], true);
+  }
+  if (!phys_in && i < 2) six(0, c_w6e[i], false);
+  if (!phys_out && i >= nc1 - 2) six(nc1 - 5, c_w6e[4 - (i - (nc1 - 5))], true);
+  pref[i] = cell_pref;
+  int jlo = (wall_clamp && phys_in) ? il : 0;
+  int jhi = (wall_clamp && phys_out) ? iu : nc1 - 1;
+  bool ext_lo = wall_clamp && phys_in && il + 1 <= iu;
+  bool ext_hi = wall_clamp && phys_out && iu - 1 >= il;
+  double rs = rop_smooth(rho, pres, i, jlo, jhi, ext_lo, ext_hi);
+  double rf = rs;
+  if (i > 0)
+    rf = 0.5 * (rop_smooth(rho, pres, i - 1, jlo, jhi, ext_lo, ext_hi) + rs);
+  dref[i] = cell_pref * rs;
+  dsf[i] = lo * rf;
+}
+
 template <int RK, bool SHOCK>
 __global__ void __launch_bounds__(kThreads)
     stage_kernel(const BlockDev* __restrict__ tab, StageParams p) {
@@ -112,20 +258,26 @@ __global__ void __launch_bounds__(kThreads)
   const int j0 = (has2 ? ng : 0) + t * B.tj;
   const int jend = has2 ? nc2 - ng : 1;
   const int ntj = min(B.tj, jend - j0);
-  const int R = ntj + 2 * hj;
+  const bool wb = B.grav1 != 0.;
+  const bool visc = B.nu_iso > 0.;
+  const TileLayout L(ntj, nc1, ng, has2, wb, B.flux_cov != 0 && nc1 >= 3,
+                     visc);
+  const int R = L.R;
   const size_t plane = (size_t)nc1 * nc2 * B.nc3;
   const real* __restrict__ uin = static_cast<const real*>(B.buf[p.in]);
   const real* __restrict__ u0 = static_cast<const real*>(B.buf[p.u0]);
   real* uout = static_cast<real*>(B.buf[p.out]);
   const real gammad = real(B.gammad);
   const bool scale = p.scale != 0;
+  const int il = ng, iu1 = nc1 - ng;  // interior x1 cells il..iu1-1
+  const double dt = p.dt[bi];
 
   const int wstride = R * nc1;  // one variable of the W tile
-  real* W = sm;
+  real* W = sm + L.w;
   const int nf1 = nx1 + 1;
-  real* F1 = W + NHYDRO * wstride;
+  real* F1 = sm + L.f1;
   const int f1stride = ntj * nf1;
-  real* F2 = F1 + NHYDRO * f1stride;
+  real* F2 = sm + L.f2;
   const int f2stride = (ntj + 1) * nx1;
 
   // (1) the tile and its x2 halo, U -> W
@@ -140,12 +292,113 @@ __global__ void __launch_bounds__(kThreads)
   }
   __syncthreads();
 
-  // (2) x1 faces ng .. nc1-ng of the tile rows
+  // (2) the well-balanced x1 reference of each tile column
+  real* REF = sm + L.ref;
+  const int rs_ = ntj * nc1;  // one reference array of the tile
+  const bool phys_in = B.bc[0] != kBcNone, phys_out = B.bc[1] != kBcNone;
+  const int iu = nc1 - 1 - ng;
+  if (wb) {
+    for (int jt = threadIdx.x; jt < ntj; jt += blockDim.x) {
+      const real* rho = W + IDN * wstride + (hj + jt) * nc1;
+      const real* pres = W + IPR * wstride + (hj + jt) * nc1;
+      ref_scan(rho, pres, nc1, iu, B.dx1, -B.grav1, REF + 0 * rs_ + jt * nc1,
+               REF + 1 * rs_ + jt * nc1);
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < ntj * nc1; idx += blockDim.x) {
+      const int jt = idx / nc1, i = idx - jt * nc1;
+      const real* rho = W + IDN * wstride + (hj + jt) * nc1;
+      const real* pres = W + IPR * wstride + (hj + jt) * nc1;
+      ref_cell(rho, pres, REF + jt * nc1, REF + rs_ + jt * nc1, i, nc1, iu,
+               phys_in, phys_out, B.wb_wall_clamp != 0,
+               REF + 2 * rs_ + jt * nc1, REF + 3 * rs_ + jt * nc1,
+               REF + 4 * rs_ + jt * nc1 /* dsf, becomes dsf_l */);
+    }
+    __syncthreads();
+    // dsf_lr: the cp5 row on dref guarded by the two cells' range; a
+    // reflecting wall face takes the mean of its two sides.  Face f reads
+    // dsf[f] alone, so the ILT side overwrites dsf in place (slot 4); the
+    // IRT side goes to slot 5
+    for (int idx = threadIdx.x; idx < ntj * nc1; idx += blockDim.x) {
+      const int jt = idx / nc1, f = idx - jt * nc1;
+      const real* dref = REF + 3 * rs_ + jt * nc1;
+      real* DL = REF + 4 * rs_ + jt * nc1;
+      real* DR = REF + 5 * rs_ + jt * nc1;
+      double dsf = DL[f];
+      double l = dsf, r = dsf;
+      if (nc1 >= 6 && f >= 2 && f <= nc1 - 2) {
+        double a = dref[f - 1], c = dref[f];
+        double lo = a < c ? a : c, hi = a > c ? a : c;
+        if (f <= nc1 - 3) {
+          double lin = cp5_cm<double>(dref[f - 2], dref[f - 1], dref[f],
+                                      dref[f + 1], dref[f + 2]);
+          if (lin >= lo && lin <= hi) r = lin;
+        }
+        if (f >= 3) {
+          double lin = cp5_cp<double>(dref[f - 3], dref[f - 2], dref[f - 1],
+                                      dref[f], dref[f + 1]);
+          if (lin >= lo && lin <= hi) l = lin;
+        }
+        if ((f == il && B.bc[0] == kBcReflecting) ||
+            (f == iu + 1 && B.bc[1] == kBcReflecting)) {
+          double mean = 0.5 * (l + r);
+          l = r = mean;
+        }
+      }
+      DL[f] = l;
+      DR[f] = r;
+    }
+    __syncthreads();
+  }
+
+  // (3) x1 faces il..iu1 of the tile rows; with gravity the face states are
+  // the reference plus the reconstructed perturbation (WellBalancedX1)
   for (int idx = threadIdx.x; idx < ntj * nf1; idx += blockDim.x) {
     const int jt = idx / nf1, fi = idx - jt * nf1;
-    const real* q = W + (hj + jt) * nc1 + ng + fi;
+    const int f = il + fi;
+    const real* q = W + (hj + jt) * nc1 + f;
     real wl[NHYDRO], wr[NHYDRO], flx[NHYDRO];
-    face_states<SHOCK>(q, wstride, 1, scale, wl, wr);
+    if (!wb) {
+      face_states<SHOCK>(q, wstride, 1, scale, wl, wr);
+    } else {
+      const real* pref = REF + 2 * rs_ + jt * nc1;
+      const real* dref = REF + 3 * rs_ + jt * nc1;
+      // the perturbation of p (v = IPR) and rho (v = IDN) at cell c, even-
+      // mirrored into the x1 wall ghosts
+      auto pert = [&](int v, int c) -> real {
+        if (c < il && phys_in) c = 2 * il - 1 - c;
+        if (c >= iu1 && phys_out) c = 2 * iu1 - 1 - c;
+        const real* col = W + v * wstride + (hj + jt) * nc1;
+        return col[c] - (v == IPR ? pref[c] : dref[c]);
+      };
+#pragma unroll
+      for (int v = 0; v < NHYDRO; ++v) {
+        real s[6];
+        if (v == IPR || v == IDN) {
+#pragma unroll
+          for (int k = 0; k < 6; ++k) s[k] = pert(v, f - 3 + k);
+        } else {
+#pragma unroll
+          for (int k = 0; k < 6; ++k) s[k] = q[v * wstride + k - 3];
+        }
+        if (SHOCK || v == IDN) {
+          wl[v] = weno5_cp(s[0], s[1], s[2], s[3], s[4], scale);
+          wr[v] = weno5_cm(s[1], s[2], s[3], s[4], s[5], scale);
+        } else {
+          wl[v] = cp5_cp(s[0], s[1], s[2], s[3], s[4]);
+          wr[v] = cp5_cm(s[1], s[2], s[3], s[4], s[5]);
+        }
+      }
+      const real psf = REF[0 * rs_ + jt * nc1 + f];
+      real pl = wl[IPR] + psf, pr = wr[IPR] + psf;
+      wl[IPR] = pl > real(0) ? pl : psf;
+      wr[IPR] = pr > real(0) ? pr : psf;
+      real dl = wl[IDN] + REF[4 * rs_ + jt * nc1 + f];
+      real dr = wr[IDN] + REF[5 * rs_ + jt * nc1 + f];
+      const real* rho = W + IDN * wstride + (hj + jt) * nc1;
+      wl[IDN] = dl > real(0) ? dl : rho[f > 0 ? f - 1 : 0];
+      wr[IDN] = dr > real(0) ? dr : rho[f];
+    }
     riemann<RK>(wl, wr, gammad, 1, flx);
     if ((fi == 0 && B.bc[0] == kBcReflecting) ||
         (fi == nx1 && B.bc[1] == kBcReflecting))
@@ -154,32 +407,180 @@ __global__ void __launch_bounds__(kThreads)
     for (int v = 0; v < NHYDRO; ++v) F1[v * f1stride + idx] = flx[v];
   }
 
-  // (3) x2 faces j0 .. j0+ntj of the tile, x1-interior cells
+  // (4) x2 faces j0..j0+ntj: the Riemann flux on the x1-interior cells and,
+  // with the covariance row, the face means on x1 rows 1..nc1-2
+  real* COV = sm + L.cov_arr;
+  const int cstride = (ntj + 1) * nc1;
   if (has2) {
-    for (int idx = threadIdx.x; idx < (ntj + 1) * nx1; idx += blockDim.x) {
-      const int jf = idx / nx1, ii = idx - jf * nx1;
-      const real* q = W + (hj + jf) * nc1 + ng + ii;
+    const int r0 = L.cov ? 1 : il, r1 = L.cov ? nc1 - 1 : iu1;
+    const int nr = r1 - r0;
+    for (int idx = threadIdx.x; idx < (ntj + 1) * nr; idx += blockDim.x) {
+      const int jf = idx / nr, i = r0 + (idx - jf * nr);
+      const real* q = W + (hj + jf) * nc1 + i;
       real wl[NHYDRO], wr[NHYDRO], flx[NHYDRO];
       face_states<SHOCK>(q, wstride, nc1, scale, wl, wr);
-      riemann<RK>(wl, wr, gammad, 2, flx);
-      const int jface = j0 + jf;
-      if ((jface == ng && B.bc[2] == kBcReflecting) ||
-          (jface == nc2 - ng && B.bc[3] == kBcReflecting))
-        flx[IDN] = flx[IPR] = real(0);
+      if (L.cov) {
+        real wb_[NHYDRO];
 #pragma unroll
-      for (int v = 0; v < NHYDRO; ++v) F2[v * f2stride + idx] = flx[v];
+        for (int v = 0; v < NHYDRO; ++v) wb_[v] = real(0.5) * (wl[v] + wr[v]);
+        real pbar = wb_[IPR];
+        real enth = pbar / (gammad - real(1)) + pbar;
+        COV[0 * cstride + jf * nc1 + i] = wb_[IDN];
+        COV[1 * cstride + jf * nc1 + i] = enth / wb_[IDN];
+        COV[2 * cstride + jf * nc1 + i] = wb_[IVY];
+      }
+      if (i >= il && i < iu1) {
+        riemann<RK>(wl, wr, gammad, 2, flx);
+#pragma unroll
+        for (int v = 0; v < NHYDRO; ++v)
+          F2[v * f2stride + jf * nx1 + (i - il)] = flx[v];
+      }
+    }
+  }
+
+  // div v for the viscous stress: tile rows -1..ntj, x1 cells il-1..iu1
+  real* DIVV = sm + L.divv;
+  if (visc) {
+    // without x2 only the tile row itself (rr = 1) is needed
+    const int rlo = has2 ? 0 : 1, nr = has2 ? ntj + 2 : 1, nci = nx1 + 2;
+    for (int idx = threadIdx.x; idx < nr * nci; idx += blockDim.x) {
+      const int rr = rlo + idx / nci, i = il - 1 + (idx - (rr - rlo) * nci);
+      const int r = hj + rr - 1;  // W row
+      const real* vx = W + IVX * wstride + r * nc1;
+      real dv = real(0);
+      dv += (vx[i + 1] - vx[i - 1]) / (real(2.) * real(B.dx1));
+      if (has2) {
+        const real* vy = W + IVY * wstride;
+        dv += (vy[(r + 1) * nc1 + i] - vy[(r - 1) * nc1 + i]) /
+              (real(2.) * real(B.dx2));
+      }
+      DIVV[rr * nc1 + i] = dv;
     }
   }
   __syncthreads();
 
-  // (4) divergence, du = -dt div, RK combine on the interior cells
+  // (5) the x2 covariance row, then the x2 wall faces
+  if (has2) {
+    for (int idx = threadIdx.x; idx < (ntj + 1) * nx1; idx += blockDim.x) {
+      const int jf = idx / nx1, ii = idx - jf * nx1, i = il + ii;
+      if (L.cov) {
+        const double* x1v = B.x1v;
+        real dx1 = real(x1v[i + 1] - x1v[i - 1]);
+        real s2 = real(B.dx1 * B.dx1 / 12.);
+        const real* rho = COV + jf * nc1;
+        const real* h = COV + cstride + jf * nc1;
+        const real* un = COV + 2 * cstride + jf * nc1;
+        real s2rho = s2 * rho[i];
+        real d1h = (h[i + 1] - h[i - 1]) / dx1;
+        real dun = (un[i + 1] - un[i - 1]) / dx1;
+        F2[IPR * f2stride + idx] += s2rho * d1h * dun;
+      }
+      const int jface = j0 + jf;
+      if ((jface == ng && B.bc[2] == kBcReflecting) ||
+          (jface == nc2 - ng && B.bc[3] == kBcReflecting))
+        F2[IDN * f2stride + idx] = F2[IPR * f2stride + idx] = real(0);
+    }
+  }
+  // viscous fluxes (src/forcing/diffusion.cpp:553-683): the momentum rows
+  // into VF1/VF2, the energy row posted into the totals
+  real* VF1 = sm + L.vf1;
+  real* VF2 = sm + L.vf2;
+  if (visc) {
+    const real nu = real(B.nu_iso);
+    const real dx1 = real(B.dx1), dx2 = real(B.dx2);
+    const real* vx = W + IVX * wstride;
+    const real* vy = W + IVY * wstride;
+    const real* vz = W + IVZ * wstride;
+    const real* rho = W + IDN * wstride;
+    const bool wlo = B.bc[0] == kBcReflecting, whi = B.bc[1] == kBcReflecting;
+    for (int idx = threadIdx.x; idx < ntj * nf1; idx += blockDim.x) {
+      const int jt = idx / nf1, fi = idx - jt * nf1, f = il + fi;
+      const int r = hj + jt;
+      const int o = r * nc1;
+      real rf = real(0.5) * (rho[o + f] + rho[o + f - 1]);
+      if (nf1 >= 3) {
+        real tt = dx1 / (dx1 + dx1);
+        if (f == il && wlo) {
+          real vn = rho[o + il], vq = rho[o + il + 1];
+          real wall = (real(1.) + tt) * vn - tt * vq;
+          rf = wall > real(0) ? wall : vn;
+        }
+        if (f == iu1 && whi) {
+          real vn = rho[o + iu1 - 1], vq = rho[o + iu1 - 2];
+          real wall = (real(1.) + tt) * vn - tt * vq;
+          rf = wall > real(0) ? wall : vn;
+        }
+      }
+      const real* dvr = DIVV + (jt + 1) * nc1;
+      real divf = real(0.5) * (dvr[f] + dvr[f - 1]);
+      real e = real(0);
+#pragma unroll
+      for (int ivar = 0; ivar < 3; ++ivar) {
+        const real* vc = ivar == 0 ? vx : (ivar == 1 ? vy : vz);
+        real stress = (vc[o + f] - vc[o + f - 1]) / dx1;
+        if (ivar == 0) {
+          stress = real(2.) * stress - real(2. / 3.) * divf;
+        } else if (ivar == 1 && has2) {
+          real below = (vx[o + nc1 + f - 1] - vx[o - nc1 + f - 1]) / (real(2.) * dx2);
+          real above = (vx[o + nc1 + f] - vx[o - nc1 + f]) / (real(2.) * dx2);
+          stress += real(0.5) * (above + below);
+        }
+        real mf = -nu * rf * stress;
+        VF1[ivar * f1stride + idx] = mf;
+        e += real(0.5) * (vc[o + f] + vc[o + f - 1]) * mf;
+      }
+      F1[IPR * f1stride + idx] += e;
+      if ((fi == 0 && wlo) || (fi == nx1 && whi))
+        F1[IDN * f1stride + idx] = F1[IPR * f1stride + idx] = real(0);
+    }
+    if (has2) {
+      for (int idx = threadIdx.x; idx < (ntj + 1) * nx1; idx += blockDim.x) {
+        const int jf = idx / nx1, ii = idx - jf * nx1, i = il + ii;
+        const int r = hj + jf;  // the cell above face jf
+        const int o = r * nc1, om = (r - 1) * nc1;
+        real rf = real(0.5) * (rho[o + i] + rho[om + i]);
+        const real* dva = DIVV + (jf + 1) * nc1;
+        const real* dvb = DIVV + jf * nc1;
+        real divf = real(0.5) * (dva[i] + dvb[i]);
+        real e = real(0);
+#pragma unroll
+        for (int ivar = 0; ivar < 3; ++ivar) {
+          const real* vc = ivar == 0 ? vx : (ivar == 1 ? vy : vz);
+          real stress = (vc[o + i] - vc[om + i]) / dx2;
+          if (ivar == 1) {
+            stress = real(2.) * stress - real(2. / 3.) * divf;
+          } else if (ivar == 0) {
+            real below = (vy[om + i + 1] - vy[om + i - 1]) / (real(2.) * dx1);
+            real above = (vy[o + i + 1] - vy[o + i - 1]) / (real(2.) * dx1);
+            stress += real(0.5) * (above + below);
+          }
+          real mf = -nu * rf * stress;
+          VF2[ivar * f2stride + idx] = mf;
+          e += real(0.5) * (vc[o + i] + vc[om + i]) * mf;
+        }
+        F2[IPR * f2stride + idx] += e;
+        const int jface = j0 + jf;
+        if ((jface == ng && B.bc[2] == kBcReflecting) ||
+            (jface == nc2 - ng && B.bc[3] == kBcReflecting))
+          F2[IDN * f2stride + idx] = F2[IPR * f2stride + idx] = real(0);
+      }
+    }
+  }
+  __syncthreads();
+
+  // (6) divergence, du = -dt div, gravity, viscous momentum, the x1 gravity
+  // energy correction, and the RK combine on the interior cells
   const real a1 = real(B.dx3 * B.dx2), a2 = real(B.dx3 * B.dx1);
   const real vol = real(B.dx3 * (B.dx2 * B.dx1));
-  const real mdt = real(-p.dt[bi]);
+  const real rdt = real(dt), mdt = real(-dt);
   const real w0 = real(p.w0), w1 = real(p.w1), w2 = real(p.w2);
+  const real g = real(B.grav1);
   for (int idx = threadIdx.x; idx < ntj * nx1; idx += blockDim.x) {
     const int jt = idx / nx1, ii = idx - jt * nx1;
-    const size_t c = (size_t)(j0 + jt) * nc1 + ng + ii;
+    const int i = il + ii;
+    const size_t c = (size_t)(j0 + jt) * nc1 + i;
+    const int wc = (hj + jt) * nc1 + i;
+    real du[NHYDRO];
 #pragma unroll
     for (int v = 0; v < NHYDRO; ++v) {
       const real* f1 = F1 + v * f1stride + jt * nf1 + ii;
@@ -188,9 +589,74 @@ __global__ void __launch_bounds__(kThreads)
         const real* f2 = F2 + v * f2stride + jt * nx1 + ii;
         dv = dv + (a2 * f2[nx1] - a2 * f2[0]);
       }
-      real du = mdt * (dv / vol);
+      du[v] = mdt * (dv / vol);
+    }
+    if (wb) {
+      const real rho = W[IDN * wstride + wc], vx = W[IVX * wstride + wc];
+      du[IVX] += rdt * rho * g * real(1.);
+      du[IPR] += rdt * rho * vx * g * real(1.);
+    }
+    if (visc) {
+      // the momentum rows (IDN has no viscous flux: du - dt 0 == du)
+#pragma unroll
+      for (int v = IVX; v <= IVZ; ++v) {
+        const real* f1 = VF1 + (v - IVX) * f1stride + jt * nf1 + ii;
+        real dv = a1 * f1[1] - a1 * f1[0];
+        if (has2) {
+          const real* f2 = VF2 + (v - IVX) * f2stride + jt * nx1 + ii;
+          dv = dv + (a2 * f2[nx1] - a2 * f2[0]);
+        }
+        du[v] = du[v] - rdt * (dv / vol);
+      }
+    }
+    if (wb) {
+      // face-form work + corrected potential-energy work - the cell work
+      const double* x1f = B.x1f;
+      const double* x = B.x1v + il;
+      const int k = ii;
+      const real* fm = F1 + IDN * f1stride + jt * nf1;  // fm[k] = face il+k
+      auto drho = [&](int kk) -> real {
+        real vmd = (a1 * fm[kk + 1] - a1 * fm[kk]) / vol;
+        return mdt * vmd;
+      };
+      real hi = real(B.grav1 * (x1f[i + 1] - B.x1v[i]));
+      real lo = real(B.grav1 * (x1f[i] - B.x1v[i]));
+      real fgw = rdt * ((hi * (a1 * fm[k + 1]) - lo * (a1 * fm[k])) / vol);
+      if (nx1 >= 3) {
+        double w0_, w1_, w2_;
+        if (k == 0) {
+          double a = x[1] - x[0], b2 = x[2] - x[1];
+          w0_ = -(2. * a + b2) / (a * (a + b2));
+          w1_ = (a + b2) / (a * b2);
+          w2_ = -(a / ((a + b2) * b2));
+        } else if (k == nx1 - 1) {
+          double c = x[nx1 - 2] - x[nx1 - 3], d = x[nx1 - 1] - x[nx1 - 2];
+          w0_ = d / (c * (c + d));
+          w1_ = -((c + d) / (c * d));
+          w2_ = (c + 2. * d) / ((c + d) * d);
+        } else {
+          double hm = x[k] - x[k - 1], hp = x[k + 1] - x[k];
+          w0_ = -hp / (hm * (hm + hp));
+          w1_ = (hp - hm) / (hm * hp);
+          w2_ = hm / (hp * (hm + hp));
+        }
+        int kc = k < 1 ? 1 : (k > nx1 - 2 ? nx1 - 2 : k);
+        int k0 = kc - 1;
+        double h = x1f[i + 1] - x1f[i];
+        real gvar = real(B.grav1 * (h * h / 12.));
+        real sl = real(w0_) * drho(k0);
+        sl += real(w1_) * drho(k0 + 1);
+        sl += real(w2_) * drho(k0 + 2);
+        fgw += gvar * sl;
+      }
+      const real rho = W[IDN * wstride + wc], vx = W[IVX * wstride + wc];
+      real orig = rdt * rho * vx * g * real(1.);
+      du[IPR] += fgw - orig;
+    }
+#pragma unroll
+    for (int v = 0; v < NHYDRO; ++v) {
       const size_t q = v * plane + c;
-      uout[q] = w0 * u0[q] + w1 * uin[q] + w2 * du;
+      uout[q] = w0 * u0[q] + w1 * uin[q] + w2 * du[v];
     }
   }
 }
@@ -403,7 +869,7 @@ __global__ void __launch_bounds__(kThreads)
       unsigned long long k = __double_as_longlong(x);
       return (k >> 63) ? ~k : (k | 0x8000000000000000ull);
     };
-    atomicMin(&red[4 * b + 0], key(dtm));
+    atomicMin(&red[4 * b + 0], key(fmin(dtm, B.dt_src)));
     atomicMin(&red[4 * b + 1], key(rmin));
     atomicMin(&red[4 * b + 2], key(pmin));
     if (nan) atomicOr(&flag[b], 1);
@@ -418,12 +884,10 @@ using namespace sg;
 // ---------------------------------------------------------------------------
 // host launchers (called by sg_api.cpp); all asynchronous on `stream`
 // ---------------------------------------------------------------------------
-extern "C" size_t SG_NAME(sg_stage_smem)(int nc1, int nx1, int tj, int has2) {
-  int hj = has2 ? 3 : 0;
-  size_t w = (size_t)NHYDRO * (tj + 2 * hj) * nc1;
-  size_t f1 = (size_t)NHYDRO * tj * (nx1 + 1);
-  size_t f2 = has2 ? (size_t)NHYDRO * (tj + 1) * nx1 : 0;
-  return (w + f1 + f2) * sizeof(real);
+extern "C" size_t SG_NAME(sg_stage_smem)(int nc1, int tj, int has2, int wb,
+                                          int cov, int visc) {
+  TileLayout L(tj, nc1, 3, has2 != 0, wb != 0, cov != 0, visc != 0);
+  return (size_t)L.total * sizeof(real);
 }
 
 extern "C" int SG_NAME(sg_launch_stage)(const BlockDev* tab, StageParams p,

@@ -32,6 +32,17 @@ struct BlockDev {
   double dx1, dx2, dx3;
   double gammad;
   double cfl;
+  // the Straka-class physics: x1 gravity (0 = off), kinematic viscosity,
+  // the x2-face covariance row and the well-balanced wall clamp
+  double grav1;
+  double nu_iso;
+  int32_t flux_cov;
+  int32_t wb_wall_clamp;
+  // FP64 x1 geometry of the padded block: faces [nc1 + 1], centres [nc1]
+  const double* x1f;
+  const double* x1v;
+  // the sources' time-step bound (the viscous dx^2 / (2 ndim nu)), or +inf
+  double dt_src;
 };
 
 // what a stage launch needs besides the table

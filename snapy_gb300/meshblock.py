@@ -53,10 +53,16 @@ def scheme_of(options: MeshBlockOptions) -> dict:
                         "and scale")
     if h.riemann.type not in ("hllc", "lmars"):
         raise DeckError(f"riemann-solver '{h.riemann.type}' is not built")
-    if h.grav is not None and (h.grav.grav1 or h.grav.grav2 or h.grav.grav3):
-        raise DeckError("forcing/const-gravity is not built")
+    if h.grav is not None:
+        if h.grav.grav2 or h.grav.grav3:
+            raise DeckError("forcing/const-gravity: grav2/grav3 are not built")
+        if h.grav.non_hydrostatic != 1.0:
+            raise DeckError("forcing/const-gravity/non-hydrostatic < 1 is not built")
     if h.diffusion is not None:
-        raise DeckError("forcing/diffusion is not built")
+        extra = set(h.diffusion.raw) - {"nu_iso", "nu-iso"}
+        if extra:
+            raise DeckError(f"forcing/diffusion: {sorted(extra)} are not built "
+                            "(nu_iso only)")
     if h.icorr is not None:
         raise DeckError("integration/implicit-scheme is not built")
     if c.nx3 > 1:
@@ -85,10 +91,18 @@ def block_of(options: MeshBlockOptions, tj: int = 0) -> dict:
         if kind not in _BC:
             raise DeckError(f"boundary '{kind}' is not built")
         bc.append(_BC[kind])
+    h = options.hydro()
+    x1f = c.faces(1)
+    x1v = 0.5 * (x1f[:-1] + x1f[1:])  # CoordinateImpl::x1_metrics_
     return {"nc1": c.nc1, "nc2": c.nc2, "nc3": c.nc3, "ng": c.nghost,
             "dx1": c.dx1, "dx2": c.dx2 if c.nx2 > 1 else (c.x2max - c.x2min),
             "dx3": c.dx3 if c.nx3 > 1 else (c.x3max - c.x3min),
-            "gammad": options.hydro().eos.gammad, "bc": bc, "tj": tj}
+            "gammad": h.eos.gammad, "bc": bc, "tj": tj,
+            "grav1": h.grav.grav1 if h.grav else 0.0,
+            "nu_iso": h.diffusion.nu_iso if h.diffusion else 0.0,
+            "flux_cov": h.flux_covariance,
+            "wb_wall_clamp": bool(h.extra.get("wb-wall-clamp", True)),
+            "x1f": x1f, "x1v": x1v}
 
 
 @dataclass

@@ -92,15 +92,16 @@ class CoordinateOptions:
         """Global face coordinates of one axis, ghosts included, computed as
         the reference's block_faces_ (coordinate.cpp:410-425): a linspace over
         [min - ng dx, max + ng dx]."""
-        import numpy as np
+        import torch
         lo, hi, n = {1: (self.x1min, self.x1max, self.nx1),
                      2: (self.x2min, self.x2max, self.nx2),
                      3: (self.x3min, self.x3max, self.nx3)}[axis]
         if n <= 1:
-            return np.linspace(lo, hi, n + 1)
+            return torch.linspace(lo, hi, n + 1, dtype=torch.float64).numpy()
         dx = (hi - lo) / n
         ng = self.nghost
-        return np.linspace(lo - ng * dx, hi + ng * dx, n + 2 * ng + 1)
+        return torch.linspace(lo - ng * dx, hi + ng * dx, n + 2 * ng + 1,
+                              dtype=torch.float64).numpy()
 
     def centers(self, axis: int):
         f = self.faces(axis)

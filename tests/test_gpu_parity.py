@@ -33,15 +33,7 @@ def deck(tmp_path, text):
 
 
 def oracle_block(O, opts):
-    c = opts.coord()
-    h = opts.hydro()
-    bcs = [n.rsplit("_", 1)[0] if n else "none" for n in opts.bcnames]
-    bcs += ["none"] * (6 - len(bcs))
-    return O.Block(nc1=c.nc1, nc2=c.nc2, nc3=c.nc3, dx1=c.dx1,
-                   dx2=c.dx2 if c.nx2 > 1 else c.x2max - c.x2min,
-                   dx3=c.dx3 if c.nx3 > 1 else c.x3max - c.x3min,
-                   gammad=h.eos.gammad, riemann=h.riemann.type,
-                   shock=h.recon1.shock, scale=h.recon1.scale, bc=bcs)
+    return O.block_from_options(opts)
 
 
 SOD = "snapy_gb300/decks/sod.yaml"
@@ -211,3 +203,51 @@ def test_redo_restores_step(cuda, tmp_path):
     assert blk.intg.current_redo == 1
     dt2 = blk.max_time_step(vars)
     assert dt2 == pytest.approx(dt / 2, rel=1e-15)
+
+
+STRAKA = "snapy_gb300/decks/straka_noimplicit.yaml"
+
+
+@pytest.mark.parametrize("nu,cov", [(75.0, True), (0.0, False)])
+def test_straka_explicit_parity(oracle, cuda, nu, cov):
+    """Gravity (well-balanced x1 reference, face-form gravity work),
+    viscosity and the x2 covariance row: a 64 x 48 window of the Straka
+    density current at 50 m, 8 steps of fixed dt."""
+    opts = sg.MeshBlockOptions.from_yaml(STRAKA)
+    c = opts.coord()
+    c.nx1, c.nx2 = 48, 64
+    c.x1max, c.x2max = 48 * 50.0, 64 * 50.0
+    opts.hydro().diffusion.nu_iso = nu
+    opts.hydro().flux_covariance = cov
+    opts.execution = "eager"
+    blk = sg.MeshBlock(opts).to(cuda)
+    w = problems.straka(opts, "cpu", xc=1600.0, zc=1200.0, xr=800.0, zr=600.0)
+    vars = {"hydro_w": w.to(cuda)}
+    blk.initialize(vars)
+    ob = oracle_block(oracle, opts)
+    u = ob.initialize(w.numpy())
+    np.testing.assert_array_equal(vars["hydro_u"].cpu().numpy(), u)
+    for step in range(8):
+        dt = blk.max_time_step(vars)
+        assert dt == pytest.approx(0.9 * ob.max_dt(u), rel=1e-15)
+        for s in range(3):
+            blk.forward(vars, dt, s)
+            ob.stage(u, dt, s)
+        err = rel_l2(vars["hydro_u"].cpu().numpy(), u)
+        assert err.max() <= TOL, (step, err)
+
+
+def test_straka_rest_state_balanced(cuda):
+    """An isentropic atmosphere at rest keeps its momentum at round-off: the
+    well-balanced x1 reference cancels the hydrostatic pressure gradient."""
+    opts = sg.MeshBlockOptions.from_yaml(STRAKA)
+    c = opts.coord()
+    c.nx1, c.nx2 = 64, 32
+    c.x1max, c.x2max = 64 * 50.0, 32 * 50.0
+    blk = sg.MeshBlock(opts).to(cuda)
+    vars = {"hydro_w": problems.straka(opts, cuda, dT=0.0)}
+    blk.initialize(vars)
+    for _ in range(10):
+        blk.step(vars, 0.1)
+    w = blk.prim()
+    assert w[1:4].abs().max().item() < 1e-9

@@ -32,3 +32,19 @@ def test_sod_to_t02(oracle):
     plateau = w[4][(xi > 0.55) & (xi < 0.8)]
     assert np.allclose(plateau, 0.30313, rtol=2e-2)
     assert abs(u[0, 0, 0, 3:-3].sum() - m0) <= 1e-13 * m0
+
+
+def test_oracle_straka_rest_is_balanced(oracle):
+    """The well-balanced x1 reference: a resting isentropic column has a
+    tendency at round-off (momentum) with gravity, viscosity and the
+    covariance row on."""
+    import snapy_gb300 as sg
+    from snapy_gb300 import problems
+    opts = sg.MeshBlockOptions.from_yaml("snapy_gb300/decks/straka_noimplicit.yaml")
+    c = opts.coord()
+    c.nx1, c.nx2, c.x1max, c.x2max = 64, 16, 3200.0, 800.0
+    ob = oracle.block_from_options(opts)
+    u = ob.initialize(problems.straka(opts, "cpu", dT=0.0).numpy())
+    du = ob.tendency(ob.prim(u), 1.0)
+    assert np.abs(du[1]).max() < 1e-11 * np.abs(u[0]).max() * 9.8
+    assert np.abs(du[2]).max() == 0.0
