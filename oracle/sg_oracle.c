@@ -473,6 +473,39 @@ void og_flux(const og_block* b, const double* w, int d, double* flux) {
 /* src/recon/x1_reference.cpp:96-240), uniform x1 grid, one block     */
 /* column with physical x1 boundaries                                 */
 /* ------------------------------------------------------------------ */
+/* exp for the scan anchor, the same operations as the CUDA kernel's sg_exp
+ * (snapy_gb300/csrc/sg_device.cuh), so oracle and GPU agree bit for bit:
+ * Cody-Waite reduction x = k ln2 + r with a split ln2, then the Taylor
+ * series of exp(r) to r^16 in Horner form, scaled by 2^k (about 2 ulp; the
+ * reference calls libm's exp here, an ulp-level difference) */
+static double sg_exp(double x) {
+  const double ln2_hi = 6.93147180369123816490e-01;
+  const double ln2_lo = 1.90821492927058770002e-10;
+  const double inv_ln2 = 1.44269504088896338700e+00;
+  double k = rint(x * inv_ln2);
+  double r = (x - k * ln2_hi) - k * ln2_lo;
+  double p = 1.0 / 20922789888000.0;
+  p = p * r + 1.0 / 1307674368000.0;
+  p = p * r + 1.0 / 87178291200.0;
+  p = p * r + 1.0 / 6227020800.0;
+  p = p * r + 1.0 / 479001600.0;
+  p = p * r + 1.0 / 39916800.0;
+  p = p * r + 1.0 / 3628800.0;
+  p = p * r + 1.0 / 362880.0;
+  p = p * r + 1.0 / 40320.0;
+  p = p * r + 1.0 / 5040.0;
+  p = p * r + 1.0 / 720.0;
+  p = p * r + 1.0 / 120.0;
+  p = p * r + 1.0 / 24.0;
+  p = p * r + 1.0 / 6.0;
+  p = p * r + 0.5;
+  p = p * r + 1.0;
+  p = p * r + 1.0;
+  return scalbn(p, (int)k);
+}
+
+double og_exp(double x) { return sg_exp(x); }
+
 static double ref_face(const double* lo, const double* hi, int f, int nc1) {
   return f < nc1 ? lo[f] : hi[nc1 - 1];
 }
@@ -521,7 +554,7 @@ void og_ref_column(const og_block* b, const double* w, size_t plane,
   /* hydro_ref_x1_scan_impl: anchored half a cell above the top cell */
   double rho_top = w[OG_IDN * plane + iu], pres_top = w[OG_IPR * plane + iu];
   double rdt_top = pres_top / rho_top;
-  double top_anchor = pres_top * exp(-grav * 0.5 * dx / rdt_top);
+  double top_anchor = pres_top * sg_exp(-grav * 0.5 * dx / rdt_top);
   const double minp = 2.2250738585072014e-308; /* DBL_MIN */
   double face = top_anchor;
   for (int i = iu; i >= 0; --i) {

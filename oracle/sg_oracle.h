@@ -65,6 +65,9 @@ void og_lmars_face(const double* wl, const double* wr, double gammad, int dim,
                    double* flx, double* face_pressure);
 void og_cons2prim_cell(const double* u, double* w, double gammad, int stride);
 
+/* the portable exp of the reference anchor (same operations as the GPU) */
+double og_exp(double x);
+
 /* ---- block operations ---- */
 void og_default_block(og_block* b);
 void og_cons2prim(const og_block* b, const double* u, double* w);

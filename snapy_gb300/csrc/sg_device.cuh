@@ -25,6 +25,39 @@ __device__ __forceinline__ T sqr(T x) {
   return x * x;
 }
 
+// exp(x) for the well-balanced reference's anchor, written out so that the
+// GPU kernel and the CPU oracle evaluate the same operations and agree bit
+// for bit (libm's and CUDA's exp may differ by an ulp, which the anchor
+// turns into a 1e-12 difference of small pressure perturbations).  Method:
+// Cody-Waite argument reduction x = k ln2 + r, |r| <= ln2/2, with ln2 split
+// into a 32-bit head and a tail, then the Taylor series of exp(r) to r^16
+// in Horner form, scaled by 2^k.  Accurate to about 2 ulp for |x| < 700.
+__device__ __forceinline__ double sg_exp(double x) {
+  const double ln2_hi = 6.93147180369123816490e-01;  // 0x3fe62e42fee00000
+  const double ln2_lo = 1.90821492927058770002e-10;
+  const double inv_ln2 = 1.44269504088896338700e+00;
+  double k = rint(x * inv_ln2);
+  double r = (x - k * ln2_hi) - k * ln2_lo;
+  double p = 1.0 / 20922789888000.0;  // 1/16!
+  p = p * r + 1.0 / 1307674368000.0;
+  p = p * r + 1.0 / 87178291200.0;
+  p = p * r + 1.0 / 6227020800.0;
+  p = p * r + 1.0 / 479001600.0;
+  p = p * r + 1.0 / 39916800.0;
+  p = p * r + 1.0 / 3628800.0;
+  p = p * r + 1.0 / 362880.0;
+  p = p * r + 1.0 / 40320.0;
+  p = p * r + 1.0 / 5040.0;
+  p = p * r + 1.0 / 720.0;
+  p = p * r + 1.0 / 120.0;
+  p = p * r + 1.0 / 24.0;
+  p = p * r + 1.0 / 6.0;
+  p = p * r + 0.5;
+  p = p * r + 1.0;
+  p = p * r + 1.0;
+  return scalbn(p, (int)k);
+}
+
 // WENO5 with the cm table: the state on the +side of the LOWER face of the
 // centre cell f2 (phi = f0..f4 = cells c-2..c+2). scale: InterpOptions::scale.
 template <typename T>

@@ -141,7 +141,7 @@ __device__ __forceinline__ void ref_scan(const real* rho, const real* pres,
                                          real* psf_hi) {
   const double minp = 2.2250738585072014e-308;
   double rdt_top = (double)pres[iu] / (double)rho[iu];
-  double top = (double)pres[iu] * exp(-grav * 0.5 * dx / rdt_top);
+  double top = (double)pres[iu] * sg_exp(-grav * 0.5 * dx / rdt_top);
   double face = top;
   for (int i = iu; i >= 0; --i) {
     double dp = grav * (double)rho[i] * dx;

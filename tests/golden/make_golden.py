@@ -89,9 +89,28 @@ def main(n=1000, seed=20261203):
         R.ref_pressure_scan(O.ptr(np.ascontiguousarray(w.ravel())), O.ptr(dx1f),
                             O.ptr(lo), O.ptr(hi), nc1, iu, -9.8)
         scan[c, 0], scan[c, 1] = lo, hi
+    # the whole well-balanced x1 reference of stratified columns (uniform
+    # grid, reflecting walls, wall clamp on): psf_lo, psf_hi, pref, dsf, dref
+    ncol, nr = 6, 70
+    zc = (np.arange(nr) - 2.5) * 50.0
+    refcols = np.zeros((ncol, 5, nr))
+    refw = np.zeros((ncol, 5, nr))
+    for c in range(ncol):
+        temp = 300.0 - 9.8 * zc / 1004.5 + rng.normal(size=nr) * c
+        p = 1e5 * (temp / 300.0) ** 3.5
+        w = np.zeros((5, nr))
+        w[0], w[4] = p / (287.0 * temp), p
+        w[1] = rng.normal(size=nr)
+        w = np.ascontiguousarray(w)
+        outs = [np.zeros(nr) for _ in range(5)]
+        R.ref_hydro_ref_column(O.ptr(w.ravel()), O.ptr(np.full(nr, 50.0)),
+                               *[O.ptr(o) for o in outs], nr, nr - 4, 9.8, 1, 1, 1)
+        refw[c] = w
+        refcols[c] = np.stack(outs)
     np.savez_compressed(OUT, stencils=st, weno=weno, cp5=cp5, wl=wl, wr=wr,
                         hllc=hllc, lmars=lmars, gammad=g, cons=u, prim=prim,
-                        scan_rho=rho, scan=scan, scan_iu=iu)
+                        scan_rho=rho, scan=scan, scan_iu=iu, refw=refw,
+                        refcols=refcols)
     print("wrote", OUT)
 
 

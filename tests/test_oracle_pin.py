@@ -74,3 +74,33 @@ def test_fresh_cases_against_reference_build(oracle):
                        np.sqrt(g * wl[4] / wl[0]), np.sqrt(g * wr[4] / wr[0]), dim,
                        oracle.ptr(p2))
             np.testing.assert_array_equal(f1, f2)
+
+
+def test_reference_column_golden(oracle, golden):
+    """The well-balanced x1 reference of a column (face pressures, cell
+    pressure, face and cell densities) against the reference's own kernel.
+    The anchor's exp is the oracle's portable one (libm's differs by at most
+    an ulp), hence a 1e-15 relative bound instead of bit equality."""
+    L = oracle.lib()
+    refw, refcols = golden["refw"], golden["refcols"]
+    nr = refw.shape[-1]
+    b = oracle.Block(nc1=nr, dx1=50.0, grav1=-9.8,
+                     bc=("reflecting", "reflecting", "none", "none", "none", "none"))
+    for c in range(refw.shape[0]):
+        w = np.ascontiguousarray(refw[c])
+        outs = [np.zeros(nr) for _ in range(5)]
+        dlr = np.zeros(2 * nr)
+        L.og_ref_column(ctypes.byref(b.b), oracle.ptr(w.ravel()), nr,
+                        *[oracle.ptr(o) for o in outs], oracle.ptr(dlr))
+        for k in range(5):
+            np.testing.assert_allclose(outs[k], refcols[c, k], rtol=1e-15, atol=0)
+
+
+def test_portable_exp_within_an_ulp(oracle):
+    L = oracle.lib()
+    L.og_exp.restype = ctypes.c_double
+    L.og_exp.argtypes = [ctypes.c_double]
+    import math
+    for x in np.concatenate([np.linspace(-0.05, 0.05, 4001), np.linspace(-600, 600, 4001)]):
+        a, b = L.og_exp(float(x)), math.exp(float(x))
+        assert abs(a - b) <= math.ulp(b), x
