@@ -56,6 +56,7 @@ class OgBlock(ctypes.Structure):
         ("nu_iso", ctypes.c_double),
         ("flux_cov", ctypes.c_int),
         ("wb_wall_clamp", ctypes.c_int),
+        ("implicit_scheme", ctypes.c_int),
         ("x1f", _dp),
         ("x1v", _dp),
         ("x2v", _dp),
@@ -101,6 +102,8 @@ def lib():
         L.og_max_dt.argtypes = [bp, _dp]
         L.og_initialize.argtypes = [bp, _dp, _dp]
         L.og_tendency.argtypes = [bp, _dp, ctypes.c_double, _dp]
+        L.og_implicit.restype = ctypes.c_int
+        L.og_implicit.argtypes = [bp, _dp, ctypes.c_double, _dp]
         L.og_ref_column.argtypes = [bp, _dp, ctypes.c_size_t, _dp, _dp, _dp,
                                     _dp, _dp, _dp]
         _lib = L
@@ -159,7 +162,8 @@ def block_from_options(opts, nthreads=0):
                  shock=h.recon1.shock, scale=h.recon1.scale, bc=bcs,
                  nthreads=nthreads, x1min=c.x1min, x2min=c.x2min,
                  x3min=c.x3min, grav1=g, nu_iso=nu,
-                 flux_cov=h.flux_covariance, x1f=c.faces(1), x2f=c.faces(2))
+                 flux_cov=h.flux_covariance, x1f=c.faces(1), x2f=c.faces(2),
+                 implicit_scheme=h.icorr.scheme if h.icorr else 0)
 
 
 def ptr(a: np.ndarray):
@@ -174,7 +178,7 @@ class Block:
                  gammad=1.4, riemann="hllc", shock=True, scale=False,
                  bc=("extrapolation",) * 6, nthreads=0, x1min=0.0, x2min=0.0,
                  x3min=0.0, grav1=0.0, nu_iso=0.0, flux_cov=True,
-                 wb_wall_clamp=True, x1f=None, x2f=None):
+                 wb_wall_clamp=True, x1f=None, x2f=None, implicit_scheme=0):
         L = lib()
         b = OgBlock()
         L.og_default_block(ctypes.byref(b))
@@ -191,6 +195,7 @@ class Block:
         b.nthreads = nthreads
         b.grav1, b.nu_iso = grav1, nu_iso
         b.flux_cov, b.wb_wall_clamp = int(bool(flux_cov)), int(bool(wb_wall_clamp))
+        b.implicit_scheme = int(implicit_scheme)
         # the reference's faces: a linspace over the padded extent
         # (CoordinateImpl::block_faces_, src/coord/coordinate.cpp:410-425)
         if x1f is None:

@@ -1000,6 +1000,9 @@ void og_stage(const og_block* b, double* u, double* u0, double dt, int stage) {
   og_cons2prim(b, u, w);
   og_tendency(b, w, dt, du);
   const double* wt = b->wght[stage];
+  /* the vertical implicit correction with dt_corr = wght2 dt
+   * (hydro_forward.cpp:1153-1168) */
+  if (b->implicit_scheme == 9) og_implicit(b, w, wt[2] * dt, du);
   /* the RK combine runs on every cell; du is zero outside the interior */
 #pragma omp parallel for schedule(static) if (nall > 4096)
   for (long q = 0; q < (long)nall; ++q)

@@ -46,6 +46,7 @@ typedef struct og_block {
   double nu_iso;       /* forcing/diffusion/nu_iso (kinematic viscosity) */
   int flux_cov;        /* dynamics/flux-covariance */
   int wb_wall_clamp;   /* dynamics/wb-wall-clamp */
+  int implicit_scheme; /* integration/implicit-scheme: 0 off, 9 full 5x5 */
   /* geometry of the padded block: x1f[nc1 + 1], x1v[nc1] (the reference's
    * linspace faces), x2v[nc2] */
   const double* x1f;
@@ -81,6 +82,11 @@ void og_stage(const og_block* b, double* u, double* u0, double dt, int stage);
 /* the hydro tendency of one stage (HydroImpl::forward): du on every cell
  * (zero outside the interior), from the primitives w */
 void og_tendency(const og_block* b, const double* w, double dt, double* du);
+/* the vertical implicit correction (scheme 9) of every interior column:
+ * du (the explicit tendency, gravity work included) is replaced by the
+ * corrected one; dtc = wght2 dt.  Returns the number of failed columns
+ * (their du is left as it came in) */
+int og_implicit(const og_block* b, const double* w, double dtc, double* du);
 /* the well-balanced x1 reference of one column (w strided by `plane`):
  * psf_lo, psf_hi, pref, dsf, dref [nc1] and dsf_lr [2][nc1] */
 void og_ref_column(const og_block* b, const double* w, size_t plane,
