@@ -45,7 +45,10 @@ sys.path.insert(0, ROOT)
 WORKLOADS = {
     # the 2-D density-current shape of the Straka config: 512 x 128 cells at
     # 50 m, LMARS + WENO5 (cp5 for velocity/pressure) + RK3, reflecting walls
-    "straka": "snapy_gb300/decks/straka_noimplicit.yaml",
+    # the Straka configuration: gravity (well-balanced x1 reference),
+    # viscosity 75 m^2/s and the vertical implicit solve (scheme 9)
+    "straka": "snapy_gb300/decks/straka.yaml",
+    "straka-explicit": "snapy_gb300/decks/straka_noimplicit.yaml",
     "straka-shape": "snapy_gb300/decks/straka_explicit.yaml",
     "sod": "snapy_gb300/decks/sod.yaml",
 }

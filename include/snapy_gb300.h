@@ -91,6 +91,9 @@ typedef struct sg_block_desc {
    * gravity work; may be null without gravity and covariance */
   const double* x1f;
   const double* x1v;
+  /* integration/implicit-scheme: 0 (none) or 9 (the full 5x5 vertical
+   * implicit solve, FP64; needs const-gravity and reflecting x1 walls) */
+  int32_t implicit_scheme;
 } sg_block_desc;
 
 int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
@@ -99,6 +102,11 @@ int sg_destroy(sg_handle* h);
 /* three device buffers per block, each (5, nc3, nc2, nc1) of the dtype; the
  * current state must be in buffer `current` (0..2) */
 int sg_bind(sg_handle* h, int32_t block, void* buf0, void* buf1, void* buf2);
+/* the FP64 scratch of a block's vertical implicit solve (0 bytes without
+ * one): the caller allocates it, 16-byte aligned, and binds it before the
+ * first sg_stage (ImplicitHydroImpl::prepare, src/implicit/implicit_hydro.hpp) */
+int sg_scratch_bytes(const sg_handle* h, int32_t block, size_t* bytes);
+int sg_bind_scratch(sg_handle* h, int32_t block, void* scratch, size_t bytes);
 int sg_set_current(sg_handle* h, int32_t current);
 int sg_current(const sg_handle* h, int32_t* current);
 /* the buffer rotation: `cur` holds the current state, `base` the stage-0
@@ -115,7 +123,8 @@ int sg_fill_ghosts(sg_handle* h, sg_stream_t stream);
 /* dt_dev_out[b] = cfl 2^-redo[b] min over block b (no host sync) */
 int sg_max_dt(sg_handle* h, const int32_t* redo_dev, double* dt_dev_out,
               sg_stream_t stream);
-/* per-block retry flags (bit 0 floor, bit 3 NaN) into flags_dev (int32[nblock]) */
+/* per-block retry flags into flags_dev (int32[nblock]): bit 0 floor, bit 3
+ * NaN, bit 5 a failed column of the implicit solve (meshblock_redo.cpp) */
 int sg_check(sg_handle* h, int32_t* flags_dev, sg_stream_t stream);
 /* initialize (MeshBlockImpl::initialize, src/mesh/meshblock.cpp:306-420):
  * the boundary functions fill the ghosts of the FP64 primitives w_in[b]

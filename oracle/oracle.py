@@ -57,6 +57,7 @@ class OgBlock(ctypes.Structure):
         ("flux_cov", ctypes.c_int),
         ("wb_wall_clamp", ctypes.c_int),
         ("implicit_scheme", ctypes.c_int),
+        ("cfl", ctypes.c_double),
         ("x1f", _dp),
         ("x1v", _dp),
         ("x2v", _dp),
@@ -163,7 +164,8 @@ def block_from_options(opts, nthreads=0):
                  nthreads=nthreads, x1min=c.x1min, x2min=c.x2min,
                  x3min=c.x3min, grav1=g, nu_iso=nu,
                  flux_cov=h.flux_covariance, x1f=c.faces(1), x2f=c.faces(2),
-                 implicit_scheme=h.icorr.scheme if h.icorr else 0)
+                 implicit_scheme=h.icorr.scheme if h.icorr else 0,
+                 cfl=opts.intg().cfl)
 
 
 def ptr(a: np.ndarray):
@@ -178,7 +180,8 @@ class Block:
                  gammad=1.4, riemann="hllc", shock=True, scale=False,
                  bc=("extrapolation",) * 6, nthreads=0, x1min=0.0, x2min=0.0,
                  x3min=0.0, grav1=0.0, nu_iso=0.0, flux_cov=True,
-                 wb_wall_clamp=True, x1f=None, x2f=None, implicit_scheme=0):
+                 wb_wall_clamp=True, x1f=None, x2f=None, implicit_scheme=0,
+                 cfl=0.9):
         L = lib()
         b = OgBlock()
         L.og_default_block(ctypes.byref(b))
@@ -196,6 +199,7 @@ class Block:
         b.grav1, b.nu_iso = grav1, nu_iso
         b.flux_cov, b.wb_wall_clamp = int(bool(flux_cov)), int(bool(wb_wall_clamp))
         b.implicit_scheme = int(implicit_scheme)
+        b.cfl = cfl
         # the reference's faces: a linspace over the padded extent
         # (CoordinateImpl::block_faces_, src/coord/coordinate.cpp:410-425)
         if x1f is None:

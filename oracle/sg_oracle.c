@@ -1030,6 +1030,10 @@ double og_max_dt(const og_block* b, const double* w) {
           size_t c = ((size_t)k * b->nc2 + j) * b->nc1 + i;
           double cs = sqrt(b->gammad * w[OG_IPR * nc + c] / w[OG_IDN * nc + c]);
           double v = dx[d] / (fabs(w[(OG_IVX + d) * nc + c]) + cs);
+          /* an implicit x1 (scheme bit 0, more than a column) drops the x1
+           * acoustic bound: dx1 / (|v1| cfl / advection_cfl) */
+          if (d == 0 && (b->implicit_scheme & 1) && !(b->nc2 == 1 && b->nc3 == 1))
+            v = dx[d] / (fabs(w[OG_IVX * nc + c]) * (b->cfl / 1.0));
           if (v < best) best = v;
         }
     dtm[d] = best;

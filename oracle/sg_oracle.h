@@ -47,6 +47,7 @@ typedef struct og_block {
   int flux_cov;        /* dynamics/flux-covariance */
   int wb_wall_clamp;   /* dynamics/wb-wall-clamp */
   int implicit_scheme; /* integration/implicit-scheme: 0 off, 9 full 5x5 */
+  double cfl;          /* integration/cfl (the implicit x1 time-step rule) */
   /* geometry of the padded block: x1f[nc1 + 1], x1v[nc1] (the reference's
    * linspace faces), x2v[nc2] */
   const double* x1f;

@@ -53,6 +53,7 @@ class BlockDesc(ctypes.Structure):
         ("wb_wall_clamp", _i32),
         ("x1f", _vp),
         ("x1v", _vp),
+        ("implicit_scheme", _i32),
     ]
 
 
@@ -62,6 +63,8 @@ SIGNATURES = {
                                  _i32, ctypes.POINTER(_vp)]),
     "sg_destroy": (ctypes.c_int, [_vp]),
     "sg_bind": (ctypes.c_int, [_vp, _i32, _vp, _vp, _vp]),
+    "sg_scratch_bytes": (ctypes.c_int, [_vp, _i32, ctypes.POINTER(ctypes.c_size_t)]),
+    "sg_bind_scratch": (ctypes.c_int, [_vp, _i32, _vp, ctypes.c_size_t]),
     "sg_set_current": (ctypes.c_int, [_vp, _i32]),
     "sg_current": (ctypes.c_int, [_vp, ctypes.POINTER(_i32)]),
     "sg_rotation": (ctypes.c_int, [_vp, ctypes.POINTER(_i32), ctypes.POINTER(_i32)]),

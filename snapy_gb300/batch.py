@@ -71,6 +71,7 @@ class Batch:
             f, v = self.geom[b]
             a.x1f = f.data_ptr() if f is not None else None
             a.x1v = v.data_ptr() if v is not None else None
+            a.implicit_scheme = int(d.get("implicit_scheme", 0))
         self.shapes = [(5, d["nc3"], d["nc2"], d["nc1"]) for d in blocks]
         h = ctypes.c_void_p()
         with torch.cuda.device(device):
@@ -84,6 +85,17 @@ class Batch:
             _lib.check(self.L.sg_bind(self.h, b, st[0].data_ptr(),
                                       st[1].data_ptr(), st[2].data_ptr()),
                        "sg_bind")
+        # the FP64 scratch of the implicit solves (torch allocations)
+        self.scratch = []
+        for b in range(self.nblock):
+            nb = ctypes.c_size_t()
+            _lib.check(self.L.sg_scratch_bytes(self.h, b, ctypes.byref(nb)),
+                       "sg_scratch_bytes")
+            if nb.value:
+                t = torch.empty(nb.value // 8, dtype=torch.float64, device=device)
+                _lib.check(self.L.sg_bind_scratch(self.h, b, t.data_ptr(), nb.value),
+                           "sg_bind_scratch")
+                self.scratch.append(t)
         self.dt = torch.zeros(self.nblock, dtype=torch.float64, device=device)
         self.redo = torch.zeros(self.nblock, dtype=torch.int32, device=device)
         self.flags = torch.zeros(self.nblock, dtype=torch.int32, device=device)

@@ -30,6 +30,8 @@ using sg::StageParams;
   extern "C" int sg_launch_init##sfx(const BlockDev*, int, int,                \
                                      double* const*, size_t,                   \
                                      cudaStream_t);                            \
+  extern "C" int sg_launch_vic##sfx(const BlockDev*, StageParams, size_t,     \
+                                    size_t, int*, cudaStream_t);               \
   extern "C" int sg_launch_reduce##sfx(const BlockDev*, int, int,              \
                                        unsigned long long*, int*, size_t,      \
                                        cudaStream_t);
@@ -77,8 +79,8 @@ __global__ void finish_dt_kernel(int nblock, unsigned long long* red, int* nan,
 // meshblock_redo.cpp:106-114: a floor hit when min rho (p) is not above
 // 1.001 x its floor (a NaN compares false, so it is a hit too); bit 3: NaN
 __global__ void finish_check_kernel(int nblock, unsigned long long* red,
-                                    int* nan, double dfloor, double pfloor,
-                                    int32_t* flags) {
+                                    int* nan, int* status, double dfloor,
+                                    double pfloor, int32_t* flags) {
   int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= nblock) return;
   double rmin = unkey(red[4 * b + 1]), pmin = unkey(red[4 * b + 2]);
@@ -86,6 +88,9 @@ __global__ void finish_check_kernel(int nblock, unsigned long long* red,
   if (!(rmin > 1.001 * dfloor)) f |= 1;
   if (!(pmin > 1.001 * pfloor)) f |= 1;
   if (nan[b]) f |= 1 | 8;
+  // bit 5: a column of the vertical implicit solve failed this step
+  if (status[b]) f |= 32;
+  status[b] = 0;
   flags[b] = f;
   red[4 * b] = red[4 * b + 1] = red[4 * b + 2] = kKeyInf;
   nan[b] = 0;
@@ -114,6 +119,10 @@ struct sg_handle {
   size_t smem = 0, max_plane = 0, max_cells = 0;
   int32_t max_nc1 = 0;
   int32_t launches = 0;
+  int* status = nullptr;  // per-block solve status bits (VIC failures)
+  bool implicit = false;
+  size_t max_icells = 0, max_icols = 0;
+  std::vector<size_t> scratch_bytes;
   int device = 0;
 };
 
@@ -148,10 +157,14 @@ int choose_tj(const sg_handle* h, const sg_block_desc& d, int nblock) {
 
 int upload(sg_handle* h, cudaStream_t s) {
   if (!h->dirty) return 0;
-  for (int b = 0; b < h->nblock; ++b)
+  for (int b = 0; b < h->nblock; ++b) {
     for (int q = 0; q < 3; ++q)
       if (!h->host[b].buf[q])
         return fail(SG_ERR_STATE, "block %d buffer %d is not bound", b, q);
+    if (h->host[b].implicit && !h->host[b].vic)
+      return fail(SG_ERR_STATE, "block %d: the implicit solve's scratch is not "
+                  "bound (sg_bind_scratch)", b);
+  }
   cudaError_t e = cudaMemcpyAsync(h->dev, h->host.data(),
                                   sizeof(BlockDev) * h->nblock,
                                   cudaMemcpyHostToDevice, s);
@@ -225,6 +238,22 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
     B.wb_wall_clamp = d.wb_wall_clamp;
     B.x1f = d.x1f;
     B.x1v = d.x1v;
+    B.implicit = d.implicit_scheme;
+    B.vic = nullptr;
+    if (d.implicit_scheme != 0) {
+      if (d.implicit_scheme != 9) {
+        delete h;
+        return fail(SG_ERR_UNSUPPORTED, "block %d: implicit-scheme %d (the "
+                    "full 5x5 scheme 9 is built)", b, d.implicit_scheme);
+      }
+      if (d.grav1 == 0. || d.bc[0] != SG_BC_REFLECTING ||
+          d.bc[1] != SG_BC_REFLECTING || d.nc1 - 2 * d.ng < 3) {
+        delete h;
+        return fail(SG_ERR_UNSUPPORTED, "block %d: the vertical implicit solve "
+                    "needs const-gravity, reflecting x1 walls and nx1 >= 3", b);
+      }
+      h->implicit = true;
+    }
     B.dt_src = INFINITY;
     if (d.nu_iso > 0.) {  // DiffusionImpl::max_time_step, kinematic nu
       int ndim = 0;
@@ -269,6 +298,16 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
     h->max_plane = std::max(h->max_plane, plane);
     h->max_cells = std::max(h->max_cells, plane);
     h->max_nc1 = std::max(h->max_nc1, d.nc1);
+    size_t icells = (size_t)(d.nc1 - 2 * d.ng) *
+                    (size_t)(d.nc2 > 1 ? d.nc2 - 2 * d.ng : 1);
+    h->scratch_bytes.push_back(d.implicit_scheme ? icells * sg::kVicDoublesPerCell *
+                                                       sizeof(double)
+                                                 : 0);
+    if (d.implicit_scheme) {
+      h->max_icells = std::max(h->max_icells, icells);
+      h->max_icols = std::max(h->max_icols,
+                              (size_t)(d.nc2 > 1 ? d.nc2 - 2 * d.ng : 1));
+    }
   }
   h->ntile = tile;
   cudaError_t e = cudaMalloc(&h->dev, sizeof(BlockDev) * nblock);
@@ -276,6 +315,8 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
     e = cudaMalloc(&h->red, sizeof(unsigned long long) * 4 * nblock);
   if (e == cudaSuccess) e = cudaMalloc(&h->nan, sizeof(int) * nblock);
   if (e == cudaSuccess) e = cudaMalloc(&h->ptrs, sizeof(void*) * nblock);
+  if (e == cudaSuccess) e = cudaMalloc(&h->status, sizeof(int) * nblock);
+  if (e == cudaSuccess) e = cudaMemset(h->status, 0, sizeof(int) * nblock);
   if (e == cudaSuccess) e = cudaMallocHost(&h->ptrs_host, sizeof(void*) * nblock);
   if (e != cudaSuccess) {
     sg_destroy(h);
@@ -297,6 +338,7 @@ int sg_destroy(sg_handle* h) {
   if (h->red) cudaFree(h->red);
   if (h->nan) cudaFree(h->nan);
   if (h->ptrs) cudaFree(h->ptrs);
+  if (h->status) cudaFree(h->status);
   if (h->ptrs_host) cudaFreeHost(h->ptrs_host);
   delete h;
   return 0;
@@ -313,6 +355,26 @@ int sg_bind(sg_handle* h, int32_t block, void* b0, void* b1, void* b2) {
       return fail(SG_ERR_ARG, "sg_bind: misaligned buffer");
   BlockDev& B = h->host[block];
   B.buf[0] = b0, B.buf[1] = b1, B.buf[2] = b2;
+  h->dirty = true;
+  return 0;
+}
+
+int sg_scratch_bytes(const sg_handle* h, int32_t block, size_t* bytes) {
+  if (!h || !bytes || block < 0 || block >= h->nblock)
+    return fail(SG_ERR_ARG, "sg_scratch_bytes: block %d", block);
+  *bytes = h->scratch_bytes[block];
+  return 0;
+}
+
+int sg_bind_scratch(sg_handle* h, int32_t block, void* scratch, size_t bytes) {
+  if (!h || block < 0 || block >= h->nblock)
+    return fail(SG_ERR_ARG, "sg_bind_scratch: block %d", block);
+  if (bytes < h->scratch_bytes[block] || (h->scratch_bytes[block] && !scratch))
+    return fail(SG_ERR_ARG, "sg_bind_scratch: block %d needs %zu bytes, got %zu",
+                block, h->scratch_bytes[block], bytes);
+  if (reinterpret_cast<uintptr_t>(scratch) % 16)
+    return fail(SG_ERR_ARG, "sg_bind_scratch: misaligned scratch");
+  h->host[block].vic = static_cast<double*>(scratch);
   h->dirty = true;
   return 0;
 }
@@ -407,12 +469,21 @@ int sg_stage(sg_handle* h, int32_t stage, const double* dt_dev,
   rc = f64(h) ? sg_launch_stage_f64(h->dev, p, h->smem, s)
               : sg_launch_stage_f32(h->dev, p, h->smem, s);
   if (rc) return cuda_fail((cudaError_t)rc, "sg_stage: stage kernel");
+  int launches = 2;
+  if (h->implicit) {
+    rc = f64(h) ? sg_launch_vic_f64(h->dev, p, h->max_icells, h->max_icols,
+                                    h->status, s)
+                : sg_launch_vic_f32(h->dev, p, h->max_icells, h->max_icols,
+                                    h->status, s);
+    if (rc) return cuda_fail((cudaError_t)rc, "sg_stage: implicit solve");
+    launches += 3;
+  }
   rc = f64(h) ? sg_launch_ghost_f64(h->dev, h->nblock, out, h->max_plane, s)
               : sg_launch_ghost_f32(h->dev, h->nblock, out, h->max_plane, s);
   if (rc) return cuda_fail((cudaError_t)rc, "sg_stage: ghost kernel");
   if (stage == 0) h->base = h->cur;
   h->cur = out;
-  h->launches = 2;
+  h->launches = launches;
   return 0;
 }
 
@@ -456,7 +527,7 @@ int sg_check(sg_handle* h, int32_t* flags, sg_stream_t stream) {
                                      h->nan, h->max_cells, s);
   if (rc) return cuda_fail((cudaError_t)rc, "sg_check: reduce");
   finish_check_kernel<<<(h->nblock + 127) / 128, 128, 0, s>>>(
-      h->nblock, h->red, h->nan, h->scheme.density_floor,
+      h->nblock, h->red, h->nan, h->status, h->scheme.density_floor,
       h->scheme.pressure_floor, flags);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "sg_check: finish");

@@ -653,6 +653,16 @@ __global__ void __launch_bounds__(kThreads)
       real orig = rdt * rho * vx * g * real(1.);
       du[IPR] += fgw - orig;
     }
+    if (B.implicit) {
+      // the vertical implicit correction follows: hand the explicit
+      // tendency to it (interior cell (column, layer) of the VIC scratch)
+      double* DU = B.vic;
+      const size_t cells = (size_t)nx1 * (has2 ? nc2 - 2 * ng : 1);
+      const size_t vc = (size_t)(j0 + jt - (has2 ? ng : 0)) * nx1 + ii;
+#pragma unroll
+      for (int v = 0; v < NHYDRO; ++v) DU[v * cells + vc] = (double)du[v];
+      continue;
+    }
 #pragma unroll
     for (int v = 0; v < NHYDRO; ++v) {
       const size_t q = v * plane + c;
@@ -834,7 +844,12 @@ __global__ void __launch_bounds__(kThreads)
     for (int v = 0; v < NHYDRO; ++v) uc[v] = u[v * plane + c];
     cons2prim<real>(uc, w, gammad);
     const real cs = sqrt(gammad * w[IPR] / w[IDN]);
-    if (nc1 > 1) dtm = fmin(dtm, (double)(real(B.dx1) / (fabs(w[IVX]) + cs)));
+    // an implicit x1 (scheme bit 0, more than one column) keeps only the
+    // advective bound dx1 / (|v1| cfl / advection_cfl) (hydro.cpp:327-340)
+    if (nc1 > 1 && (B.implicit & 1) && !(nc2 == 1 && nc3 == 1))
+      dtm = fmin(dtm, (double)(real(B.dx1) / (fabs(w[IVX]) * real(B.cfl / 1.0))));
+    else if (nc1 > 1)
+      dtm = fmin(dtm, (double)(real(B.dx1) / (fabs(w[IVX]) + cs)));
     if (nc2 > 1) dtm = fmin(dtm, (double)(real(B.dx2) / (fabs(w[IVY]) + cs)));
     if (nc3 > 1) dtm = fmin(dtm, (double)(real(B.dx3) / (fabs(w[IVZ]) + cs)));
     rmin = fmin(rmin, (double)w[IDN]);
@@ -875,6 +890,8 @@ __global__ void __launch_bounds__(kThreads)
     if (nan) atomicOr(&flag[b], 1);
   }
 }
+
+#include "sg_vic.cuh"
 
 }  // namespace
 }  // namespace sg
@@ -936,6 +953,24 @@ extern "C" int SG_NAME(sg_launch_init)(const BlockDev* tab, int nblock,
   int gx = (int)((max_plane + kThreads - 1) / kThreads);
   if (gx > 1024) gx = 1024;
   init_kernel<<<dim3(gx, nblock), kThreads, 0, stream>>>(tab, which, win);
+  return (int)cudaGetLastError();
+}
+
+// the three VIC launches of a stage (after the stage kernel wrote the
+// explicit tendency of the implicit blocks)
+extern "C" int SG_NAME(sg_launch_vic)(const BlockDev* tab, StageParams p,
+                                      size_t max_cells, size_t max_cols,
+                                      int* status, cudaStream_t stream) {
+  int ga = (int)((max_cells + kThreads - 1) / kThreads);
+  if (ga > 4096) ga = 4096;
+  vic_assemble_kernel<<<dim3(ga, p.nblock), kThreads, 0, stream>>>(tab, p);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return (int)e;
+  int gc = (int)((max_cols + 127) / 128);
+  vic_solve_kernel<<<dim3(gc, p.nblock), 128, 0, stream>>>(tab, p, status);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return (int)e;
+  vic_finish_kernel<<<dim3(gc, p.nblock), 128, 0, stream>>>(tab, p);
   return (int)cudaGetLastError();
 }
 

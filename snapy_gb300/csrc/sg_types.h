@@ -43,7 +43,16 @@ struct BlockDev {
   const double* x1v;
   // the sources' time-step bound (the viscous dx^2 / (2 ndim nu)), or +inf
   double dt_src;
+  // the vertical implicit correction: scheme (0 off, 9 the full 5x5 blocks)
+  // and its FP64 scratch (kVicDoublesPerCell per interior cell), laid out
+  // as in vic_scratch()
+  int32_t implicit;
+  double* vic;
 };
+
+// doubles of VIC scratch per interior cell: du, du0 (5 each), the blocks
+// a, b, c (25 each), the solution and the two Woodbury vectors (5 each)
+constexpr int kVicDoublesPerCell = 100;
 
 // what a stage launch needs besides the table
 struct StageParams {

@@ -64,7 +64,12 @@ def scheme_of(options: MeshBlockOptions) -> dict:
             raise DeckError(f"forcing/diffusion: {sorted(extra)} are not built "
                             "(nu_iso only)")
     if h.icorr is not None:
-        raise DeckError("integration/implicit-scheme is not built")
+        if h.icorr.scheme != 9:
+            raise DeckError(f"integration/implicit-scheme {h.icorr.scheme}: the "
+                            "full 5x5 scheme 9 is built")
+        if options.hydro().precision != "float64" and h.icorr.precision == "float32":
+            raise DeckError("integration/implicit-precision float32 is not built "
+                            "(the implicit solve runs in FP64)")
     if c.nx3 > 1:
         raise DeckError("3-D blocks are not built")
     intg = options.intg()
@@ -102,7 +107,8 @@ def block_of(options: MeshBlockOptions, tj: int = 0) -> dict:
             "nu_iso": h.diffusion.nu_iso if h.diffusion else 0.0,
             "flux_cov": h.flux_covariance,
             "wb_wall_clamp": bool(h.extra.get("wb-wall-clamp", True)),
-            "x1f": x1f, "x1v": x1v}
+            "x1f": x1f, "x1v": x1v,
+            "implicit_scheme": h.icorr.scheme if h.icorr else 0}
 
 
 @dataclass

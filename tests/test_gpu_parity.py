@@ -251,3 +251,45 @@ def test_straka_rest_state_balanced(cuda):
         blk.step(vars, 0.1)
     w = blk.prim()
     assert w[1:4].abs().max().item() < 1e-9
+
+
+STRAKA_VIC = "snapy_gb300/decks/straka.yaml"
+
+
+def test_straka_implicit_parity(oracle, cuda):
+    """The full Straka stage with the vertical implicit correction (scheme 9:
+    5x5 blocks, Woodbury wall rows, redistribution, gravity-work remainder)
+    against the oracle on a 48 x 40 window, 6 steps."""
+    opts = sg.MeshBlockOptions.from_yaml(STRAKA_VIC)
+    c = opts.coord()
+    c.nx1, c.nx2 = 48, 40
+    c.x1max, c.x2max = 48 * 50.0, 40 * 50.0
+    opts.execution = "eager"
+    blk = sg.MeshBlock(opts).to(cuda)
+    w = problems.straka(opts, "cpu", xc=1000.0, zc=1200.0, xr=800.0, zr=600.0)
+    vars = {"hydro_w": w.to(cuda)}
+    blk.initialize(vars)
+    ob = oracle_block(oracle, opts)
+    u = ob.initialize(w.numpy())
+    for step in range(6):
+        dt = blk.max_time_step(vars)
+        assert dt == pytest.approx(0.9 * ob.max_dt(u), rel=1e-15)
+        for s in range(3):
+            blk.forward(vars, dt, s)
+            ob.stage(u, dt, s)
+        assert blk.check_redo(vars) == 0
+        err = rel_l2(vars["hydro_u"].cpu().numpy(), u)
+        assert err.max() <= TOL, (step, err)
+
+
+def test_implicit_rest_state_balanced(cuda):
+    opts = sg.MeshBlockOptions.from_yaml(STRAKA_VIC)
+    c = opts.coord()
+    c.nx1, c.nx2 = 64, 24
+    c.x1max, c.x2max = 64 * 50.0, 24 * 50.0
+    blk = sg.MeshBlock(opts).to(cuda)
+    vars = {"hydro_w": problems.straka(opts, cuda, dT=0.0)}
+    blk.initialize(vars)
+    for _ in range(10):
+        blk.step(vars, 0.1)
+    assert blk.prim()[1:4].abs().max().item() < 1e-9
