@@ -139,8 +139,26 @@ int sg_prim(sg_handle* h, void* const* w_out, sg_stream_t stream);
 int sg_tile(const sg_handle* h, int32_t block, int32_t* tj);
 /* kernels launched by the last sg_stage call */
 int sg_launches_per_stage(const sg_handle* h, int32_t* n);
+/* Per-kernel device time of sg_stage (no counterpart in the reference, whose
+ * profiling is host-side timers).  With timing on, each sg_stage that is not
+ * being captured into a graph records events around its launches on its
+ * stream; sg_kernel_times waits for them and returns, per kernel, the summed
+ * milliseconds and the launch count since the previous call (arrays of
+ * SG_NKERNEL).  Call it now and then while timing: the events of every
+ * timed stage are held until it is called. */
+enum {
+  SG_KERNEL_STAGE = 0,        /* reconstruction, fluxes, sources, update */
+  SG_KERNEL_VIC_ASSEMBLE = 1, /* implicit solve: block rows of each cell */
+  SG_KERNEL_VIC_SOLVE = 2,    /* implicit solve: block-Thomas sweep */
+  SG_KERNEL_VIC_FINISH = 3,   /* implicit solve: redistribution, update */
+  SG_KERNEL_GHOST = 4,        /* ghost fill of the new state */
+  SG_NKERNEL = 5
+};
+int sg_set_timing(sg_handle* h, int32_t on);
+int sg_kernel_times(sg_handle* h, double* ms, int64_t* launches);
 const char* sg_last_error(void);
 const char* sg_version(void);
+
 
 #ifdef __cplusplus
 }

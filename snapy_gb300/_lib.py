@@ -57,6 +57,11 @@ class BlockDesc(ctypes.Structure):
     ]
 
 
+# SG_KERNEL_* of sg_kernel_times
+KERNELS = ("stage_kernel", "vic_assemble_kernel", "vic_solve_kernel",
+           "vic_finish_kernel", "ghost_kernel")
+
+
 # every symbol include/snapy_gb300.h declares, with its ctypes signature
 SIGNATURES = {
     "sg_create": (ctypes.c_int, [ctypes.POINTER(Scheme), ctypes.POINTER(BlockDesc),
@@ -79,6 +84,9 @@ SIGNATURES = {
     "sg_prim": (ctypes.c_int, [_vp, ctypes.POINTER(_vp), _vp]),
     "sg_tile": (ctypes.c_int, [_vp, _i32, ctypes.POINTER(_i32)]),
     "sg_launches_per_stage": (ctypes.c_int, [_vp, ctypes.POINTER(_i32)]),
+    "sg_set_timing": (ctypes.c_int, [_vp, _i32]),
+    "sg_kernel_times": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double),
+                                       ctypes.POINTER(ctypes.c_int64)]),
     "sg_last_error": (ctypes.c_char_p, []),
     "sg_version": (ctypes.c_char_p, []),
 }

@@ -190,3 +190,16 @@ class Batch:
         _lib.check(self.L.sg_launches_per_stage(self.h, ctypes.byref(n)),
                    "sg_launches_per_stage")
         return n.value
+
+    def set_timing(self, on: bool) -> None:
+        """Record device events around each kernel of every eager stage."""
+        _lib.check(self.L.sg_set_timing(self.h, int(bool(on))), "sg_set_timing")
+
+    def kernel_times(self) -> dict:
+        """{kernel: (milliseconds, launches)} since the previous call (waits
+        for the recorded events)."""
+        n = len(_lib.KERNELS)
+        ms = (ctypes.c_double * n)()
+        cnt = (ctypes.c_int64 * n)()
+        _lib.check(self.L.sg_kernel_times(self.h, ms, cnt), "sg_kernel_times")
+        return {k: (ms[i], cnt[i]) for i, k in enumerate(_lib.KERNELS) if cnt[i]}

@@ -34,14 +34,19 @@ def _units():
     common = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
                      "-Xptxas", "-O3", "--expt-relaxed-constexpr"]
     stage = os.path.join(CSRC, "sg_stage.cu")
-    return [
+    units = [
         (stage, os.path.join(BUILD, "sg_stage_f64.o"),
          common + ["-DSG_REAL=double", "-fmad=false"]),
         (stage, os.path.join(BUILD, "sg_stage_f32.o"),
          common + ["-DSG_REAL=float", "-DSG_REAL_IS_FLOAT"]),
-        (os.path.join(CSRC, "sg_api.cu"), os.path.join(BUILD, "sg_api.o"),
-         common),
     ]
+    # every other translation unit once, FP64 parity rules (no contraction)
+    for f in sorted(os.listdir(CSRC)):
+        if f.endswith(".cu") and f != "sg_stage.cu":
+            units.append((os.path.join(CSRC, f),
+                          os.path.join(BUILD, f[:-3] + ".o"),
+                          common + ["-fmad=false"]))
+    return units
 
 
 def _sources():
@@ -72,7 +77,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
             sys.stdout.write(r.stdout + r.stderr)
         return obj
 
-    with cf.ThreadPoolExecutor(max_workers=3) as ex:
+    with cf.ThreadPoolExecutor(max_workers=4) as ex:
         objs = list(ex.map(compile_one, _units()))
     tmp = LIB + ".tmp"
     cmd = [nv] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]

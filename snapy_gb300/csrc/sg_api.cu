@@ -31,7 +31,8 @@ using sg::StageParams;
                                      double* const*, size_t,                   \
                                      cudaStream_t);                            \
   extern "C" int sg_launch_vic##sfx(const BlockDev*, StageParams, size_t,     \
-                                    size_t, int*, cudaStream_t);               \
+                                    size_t, int*, cudaStream_t,                \
+                                    cudaEvent_t*);                             \
   extern "C" int sg_launch_reduce##sfx(const BlockDev*, int, int,              \
                                        unsigned long long*, int*, size_t,      \
                                        cudaStream_t);
@@ -124,6 +125,16 @@ struct sg_handle {
   size_t max_icells = 0, max_icols = 0;
   std::vector<size_t> scratch_bytes;
   int device = 0;
+  // per-kernel timing (sg_set_timing): events recorded between the launches
+  // of each eager sg_stage, reused from a pool; each pending interval is
+  // (kernel, start event, end event)
+  bool timing = false;
+  std::vector<cudaEvent_t> events;
+  size_t events_used = 0;
+  struct Interval {
+    int kernel, e0, e1;
+  };
+  std::vector<Interval> pending;
 };
 
 namespace {
@@ -180,6 +191,7 @@ int upload(sg_handle* h, cudaStream_t s) {
 extern "C" {
 
 const char* sg_last_error(void) { return g_err.c_str(); }
+
 const char* sg_version(void) { return "snapy_gb300 0.1 (sm_103a)"; }
 
 int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
@@ -340,6 +352,7 @@ int sg_destroy(sg_handle* h) {
   if (h->ptrs) cudaFree(h->ptrs);
   if (h->status) cudaFree(h->status);
   if (h->ptrs_host) cudaFreeHost(h->ptrs_host);
+  for (cudaEvent_t e : h->events) cudaEventDestroy(e);
   delete h;
   return 0;
 }
@@ -406,6 +419,48 @@ int sg_launches_per_stage(const sg_handle* h, int32_t* n) {
 }
 
 namespace {
+// an event of the timing pool (created on first use, reused after each
+// sg_kernel_times)
+int take_event(sg_handle* h, int* idx) {
+  if (h->events_used == h->events.size()) {
+    cudaEvent_t e;
+    cudaError_t err = cudaEventCreate(&e);
+    if (err != cudaSuccess) return cuda_fail(err, "sg_stage: timing event");
+    h->events.push_back(e);
+  }
+  *idx = (int)h->events_used++;
+  return 0;
+}
+}  // namespace
+
+int sg_set_timing(sg_handle* h, int32_t on) {
+  if (!h) return fail(SG_ERR_ARG, "sg_set_timing: null");
+  h->timing = on != 0;
+  return 0;
+}
+
+int sg_kernel_times(sg_handle* h, double* ms, int64_t* launches) {
+  if (!h || !ms || !launches) return fail(SG_ERR_ARG, "sg_kernel_times: null");
+  for (int k = 0; k < SG_NKERNEL; ++k) ms[k] = 0., launches[k] = 0;
+  for (const auto& iv : h->pending) {
+    cudaError_t e = cudaEventSynchronize(h->events[iv.e1]);
+    float t = 0.f;
+    if (e == cudaSuccess)
+      e = cudaEventElapsedTime(&t, h->events[iv.e0], h->events[iv.e1]);
+    if (e != cudaSuccess) {
+      h->pending.clear();
+      h->events_used = 0;
+      return cuda_fail(e, "sg_kernel_times");
+    }
+    ms[iv.kernel] += t;
+    launches[iv.kernel] += 1;
+  }
+  h->pending.clear();
+  h->events_used = 0;
+  return 0;
+}
+
+namespace {
 // the buffers of a stage: in = current, u0 = the stage-0 state, out = the
 // remaining one (never the input, which other tiles read as a stencil)
 void plan(const sg_handle* h, int stage, int* in, int* u0, int* out) {
@@ -466,21 +521,55 @@ int sg_stage(sg_handle* h, int32_t stage, const double* dt_dev,
   p.w2 = h->scheme.wght[stage][2];
   p.dt = dt_dev;
   p.max_nc1 = h->max_nc1;
+  // events between the launches when timing is on and the stream is not
+  // being captured: ev[0] stage ev[1] (assemble ev[2] solve ev[3] finish
+  // ev[4]) ghost ev[5]
+  cudaEvent_t ev[6] = {};
+  int eidx[6] = {};
+  bool timed = false;
+  if (h->timing) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess)
+      return cuda_fail(cudaGetLastError(), "sg_stage: capture query");
+    timed = cs == cudaStreamCaptureStatusNone;
+  }
+  if (timed) {
+    for (int k = 0; k < 6; ++k) {
+      rc = take_event(h, &eidx[k]);
+      if (rc) return rc;
+      ev[k] = h->events[eidx[k]];
+    }
+    cudaEventRecord(ev[0], s);
+  }
   rc = f64(h) ? sg_launch_stage_f64(h->dev, p, h->smem, s)
               : sg_launch_stage_f32(h->dev, p, h->smem, s);
   if (rc) return cuda_fail((cudaError_t)rc, "sg_stage: stage kernel");
+  if (timed) cudaEventRecord(ev[1], s);
   int launches = 2;
   if (h->implicit) {
     rc = f64(h) ? sg_launch_vic_f64(h->dev, p, h->max_icells, h->max_icols,
-                                    h->status, s)
+                                    h->status, s, timed ? ev + 2 : nullptr)
                 : sg_launch_vic_f32(h->dev, p, h->max_icells, h->max_icols,
-                                    h->status, s);
+                                    h->status, s, timed ? ev + 2 : nullptr);
     if (rc) return cuda_fail((cudaError_t)rc, "sg_stage: implicit solve");
+    if (timed) cudaEventRecord(ev[4], s);
     launches += 3;
   }
   rc = f64(h) ? sg_launch_ghost_f64(h->dev, h->nblock, out, h->max_plane, s)
               : sg_launch_ghost_f32(h->dev, h->nblock, out, h->max_plane, s);
   if (rc) return cuda_fail((cudaError_t)rc, "sg_stage: ghost kernel");
+  if (timed) {
+    cudaEventRecord(ev[5], s);
+    h->pending.push_back({SG_KERNEL_STAGE, eidx[0], eidx[1]});
+    if (h->implicit) {
+      h->pending.push_back({SG_KERNEL_VIC_ASSEMBLE, eidx[1], eidx[2]});
+      h->pending.push_back({SG_KERNEL_VIC_SOLVE, eidx[2], eidx[3]});
+      h->pending.push_back({SG_KERNEL_VIC_FINISH, eidx[3], eidx[4]});
+      h->pending.push_back({SG_KERNEL_GHOST, eidx[4], eidx[5]});
+    } else {
+      h->pending.push_back({SG_KERNEL_GHOST, eidx[1], eidx[5]});
+    }
+  }
   if (stage == 0) h->base = h->cur;
   h->cur = out;
   h->launches = launches;

@@ -242,12 +242,11 @@ __device__ __forceinline__ void ref_cell(const real* rho, const real* pres,
   dsf[i] = lo * rf;
 }
 
+// one tile of the batch: `tj` x2 columns of one block over its full x1
 template <int RK, bool SHOCK>
-__global__ void __launch_bounds__(kThreads)
-    stage_kernel(const BlockDev* __restrict__ tab, StageParams p) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  real* sm = reinterpret_cast<real*>(smem_raw);
-  const int tile = blockIdx.x;
+__device__ __forceinline__ void stage_tile(const BlockDev* __restrict__ tab,
+                                           const StageParams& p, int tile,
+                                           real* sm) {
   const int bi = find_block(tab, p.nblock, tile);
   const BlockDev& B = tab[bi];
   const int t = tile - B.tile0;
@@ -671,6 +670,20 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// the stage of every tile of the batch in ONE persistent launch: a grid of
+// (SMs x resident CTAs) walks the tiles of all blocks, uneven blocks
+// interleaved so the work per CTA evens out
+template <int RK, bool SHOCK>
+__global__ void __launch_bounds__(kThreads)
+    stage_kernel(const BlockDev* __restrict__ tab, StageParams p) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  real* sm = reinterpret_cast<real*>(smem_raw);
+  for (int tile = blockIdx.x; tile < p.ntile; tile += gridDim.x) {
+    stage_tile<RK, SHOCK>(tab, p, tile, sm);
+    __syncthreads();  // the next tile reuses the shared memory
+  }
+}
+
 // one index of a ghost cell mapped to the interior cell its value comes from
 // (src/bc/bc_func.cpp:10-70); flips the sign when a reflecting face maps it
 __device__ __forceinline__ int ghost_src(int i, int n, int ng, int lo_kind,
@@ -925,7 +938,20 @@ extern "C" int SG_NAME(sg_launch_stage)(const BlockDev* tab, StageParams p,
     if (e != cudaSuccess) return (int)e;
     g = smem;
   }
-  k<<<p.ntile, kThreads, smem, stream>>>(tab, p);
+  // a persistent grid: as many CTAs as fit on the GPU at once, never more
+  // than there are tiles
+  static int resident[4][2] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
+  int kid = (p.riemann == kHllc ? 0 : 2) + (p.shock ? 1 : 0);
+  if (resident[kid][1] != (int)smem) {
+    int per_sm = 0, dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kThreads, smem);
+    resident[kid][0] = (per_sm > 0 ? per_sm : 1) * sms;
+    resident[kid][1] = (int)smem;
+  }
+  int grid = p.ntile < resident[kid][0] ? p.ntile : resident[kid][0];
+  k<<<grid, kThreads, smem, stream>>>(tab, p);
   return (int)cudaGetLastError();
 }
 
@@ -960,17 +986,22 @@ extern "C" int SG_NAME(sg_launch_init)(const BlockDev* tab, int nblock,
 // explicit tendency of the implicit blocks)
 extern "C" int SG_NAME(sg_launch_vic)(const BlockDev* tab, StageParams p,
                                       size_t max_cells, size_t max_cols,
-                                      int* status, cudaStream_t stream) {
+                                      int* status, cudaStream_t stream,
+                                      cudaEvent_t* ev) {
   int ga = (int)((max_cells + kThreads - 1) / kThreads);
   if (ga > 4096) ga = 4096;
   vic_assemble_kernel<<<dim3(ga, p.nblock), kThreads, 0, stream>>>(tab, p);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return (int)e;
-  int gc = (int)((max_cols + 127) / 128);
-  vic_solve_kernel<<<dim3(gc, p.nblock), 128, 0, stream>>>(tab, p, status);
+  if (ev) cudaEventRecord(ev[0], stream);
+  // one warp per column
+  int gc = (int)((max_cols + kVicWarps - 1) / kVicWarps);
+  vic_solve_kernel<<<dim3(gc, p.nblock), 32 * kVicWarps, 0, stream>>>(tab, p,
+                                                                      status);
   e = cudaGetLastError();
   if (e != cudaSuccess) return (int)e;
-  vic_finish_kernel<<<dim3(gc, p.nblock), 128, 0, stream>>>(tab, p);
+  if (ev) cudaEventRecord(ev[1], stream);
+  vic_finish_kernel<<<dim3(gc, p.nblock), 32 * kVicWarps, 0, stream>>>(tab, p);
   return (int)cudaGetLastError();
 }
 

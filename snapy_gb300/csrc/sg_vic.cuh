@@ -16,10 +16,14 @@
 //   src/implicit/vic_redistribute_impl.h      constituent column, cell map
 //   src/implicit/implicit_hydro.cpp:713-792   the gravity-work remainder
 // Three launches per stage, as the work's parallelism dictates: the blocks
-// of every cell in parallel (vic_assemble_kernel), the serial block-Thomas
-// sweep of each column (vic_solve_kernel, one thread per column), and the
-// column's redistribution, remainder and RK combine (vic_finish_kernel).
-// Products are summed in index order, bit for bit the CPU oracle's.
+// of every cell in parallel (vic_assemble_kernel, one thread per cell), the
+// serial block-Thomas sweep of each column (vic_solve_kernel, one WARP per
+// column: the 5x5 block products run one entry per lane through warp
+// shuffles, the 8 right-hand sides of the LU back-solve one per lane, the
+// factorisation on the warp's shared-memory tile), and the column's
+// redistribution, remainder and RK combine (vic_finish_kernel, one warp per
+// column).  Every product is summed in index order, so the results are bit
+// for bit the CPU oracle's.
 #pragma once
 
 struct VicScratch {
@@ -58,17 +62,6 @@ __device__ __forceinline__ void vmat_mul(const double* a, const double* b,
       for (int k = 1; k < 5; ++k) s += a[r * 5 + k] * b[k * 5 + c];
       out[r * 5 + c] = s;
     }
-}
-
-__device__ __forceinline__ void vmat_vec(const double* a, const double* v,
-                                         double* out) {
-#pragma unroll
-  for (int r = 0; r < 5; ++r) {
-    double s = a[r * 5] * v[0];
-#pragma unroll
-    for (int k = 1; k < 5; ++k) s += a[r * 5 + k] * v[k];
-    out[r] = s;
-  }
 }
 
 __device__ __forceinline__ void vflux_jacobian(double* J, double gm1,
@@ -300,7 +293,8 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
-// ludcmp<double, 5, Implicit> on a row-major 5x5 (src/math/ludcmp.h)
+// ludcmp<double, 5, Implicit> on a row-major 5x5 in shared memory
+// (src/math/ludcmp.h); one lane runs it
 __device__ __forceinline__ int vludcmp(double* a, int* indx) {
   int i, imax = 0, j, k, d;
   double big, dum, sum, temp, vv[5], scale[5];
@@ -361,18 +355,33 @@ __device__ __forceinline__ int vludcmp(double* a, int* indx) {
   return d;
 }
 
+constexpr int kVicWarps = 4;  // columns per CTA of the solve and finish
+
+// the per-warp shared tile of the sweep
+struct VicWarpTile {
+  double lu[25];      // a[i] - b[i] a'[i-1], factorised in place
+  double bm[25];      // b[i]
+  double sol[5 * 8];  // [row][col]: c[i] | rhs - b d' | e0 - b z0 | e1 - b z1
+  double prev[3 * 5];  // d, z0, z1 of layer i - 1
+  int indx[5];
+  int ok;
+};
+
 // (2) the block-Thomas sweep, back substitution and Woodbury update of
-// each column (one thread per column, layers in order)
-__global__ void __launch_bounds__(128)
+// each column, one warp per column
+__global__ void __launch_bounds__(32 * kVicWarps)
     vic_solve_kernel(const BlockDev* __restrict__ tab, StageParams p,
                      int* status) {
+  __shared__ VicWarpTile tiles[kVicWarps];
   const BlockDev& B = tab[blockIdx.y];
   if (!B.implicit) return;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  VicWarpTile& T = tiles[wid];
   const VicScratch S = vic_scratch(B);
   const int ng = B.ng, n = B.nc1 - 2 * ng;
   const size_t ncol = S.cells / n;
-  const size_t col = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (col >= ncol) return;
+  const size_t col = (size_t)blockIdx.x * kVicWarps + wid;
+  if (col >= ncol) return;  // whole warps leave together
   const double dtc = p.w2 * p.dt[blockIdx.y];
   const bool wood = n >= 3;
   const int m = wood ? 8 : 6;
@@ -382,105 +391,123 @@ __global__ void __launch_bounds__(128)
   double* D = S.D + col * n * 5;
   double* Z0 = S.Z0 + col * n * 5;
   double* Z1 = S.Z1 + col * n * 5;
-  bool ok = true;
-  for (int i = 0; i < n && ok; ++i)
-    for (int v = 0; v < 5; ++v)
-      if (!isfinite(S.du[v * S.cells + col * n + i])) ok = false;
+  const int r = lane / 5, c = lane % 5;  // lane < 25 owns entry (r, c)
+  // the input screen: du of every layer finite
+  bool fin = true;
+  for (int e = lane; e < 5 * n; e += 32)
+    fin = fin && isfinite(S.du[(e / n) * S.cells + col * n + (e % n)]);
+  bool ok = __all_sync(0xffffffffu, fin);
+  double aprev = 0.;  // a'[i-1] entry (r, c) of this lane
   for (int i = 0; i < n && ok; ++i) {
     const size_t cell = col * n + i;
-    double rhs[5];
-#pragma unroll
-    for (int v = 0; v < 5; ++v) rhs[v] = S.du[v * S.cells + cell] / dtc;
-    double ai[25], bi[25];
-#pragma unroll
-    for (int k = 0; k < 25; ++k) {
-      ai[k] = A[i * 25 + k];
-      bi[k] = Bm[i * 25 + k];
+    double aij = 0., bij = 0.;
+    if (lane < 25) {
+      aij = A[i * 25 + lane];
+      bij = Bm[i * 25 + lane];
+      T.bm[lane] = bij;
+      T.sol[r * 8 + c] = C[i * 25 + lane];
     }
+    // a[i] -= b[i] a'[i-1], entry (r, c) summed over k in order
     if (i > 0) {
-      double t[25];
-      vmat_mul(bi, A + (i - 1) * 25, t);
+      double t = 0.;
 #pragma unroll
-      for (int k = 0; k < 25; ++k) ai[k] -= t[k];
+      for (int k = 0; k < 5; ++k) {
+        double bk = __shfl_sync(0xffffffffu, bij, r * 5 + k);
+        double ak = __shfl_sync(0xffffffffu, aprev, k * 5 + c);
+        t = k == 0 ? bk * ak : t + bk * ak;
+      }
+      aij -= t;
     }
-    int indx[5] = {0, 1, 2, 3, 4};
-    if (vludcmp(ai, indx) == 0) {
+    if (lane < 25) T.lu[lane] = aij;
+    __syncwarp();
+    // the right-hand sides: lane q5 * 5 + rr (q5 < 3) forms column 5 + q5
+    if (lane < 15) {
+      const int q5 = lane / 5, rr = lane % 5;
+      double base;
+      if (q5 == 0)
+        base = S.du[rr * S.cells + cell] / dtc;
+      else
+        base = (rr == 4 && ((q5 == 1 && i == 0) || (q5 == 2 && i == n - 1)))
+                   ? 1. : 0.;
+      if (i > 0) {
+        const double* v = T.prev + q5 * 5;
+        double t = T.bm[rr * 5] * v[0];
+#pragma unroll
+        for (int k = 1; k < 5; ++k) t += T.bm[rr * 5 + k] * v[k];
+        base = base - t;
+      }
+      T.sol[rr * 8 + 5 + q5] = base;
+    }
+    __syncwarp();
+    if (lane == 0) {
+#pragma unroll
+      for (int q = 0; q < 5; ++q) T.indx[q] = q;
+      T.ok = vludcmp(T.lu, T.indx) != 0;
+    }
+    __syncwarp();
+    if (!T.ok) {
       ok = false;
       break;
     }
-    double sol[5][8];
-#pragma unroll
-    for (int r = 0; r < 5; ++r)
-#pragma unroll
-      for (int q = 0; q < 5; ++q) sol[r][q] = C[i * 25 + r * 5 + q];
-    const double e0[5] = {0, 0, 0, 0, i == 0 ? 1. : 0.};
-    const double e1[5] = {0, 0, 0, 0, i == n - 1 ? 1. : 0.};
-    if (i > 0) {
-      double t[5];
-      vmat_vec(bi, D + (i - 1) * 5, t);
-#pragma unroll
-      for (int r = 0; r < 5; ++r) sol[r][5] = rhs[r] - t[r];
-      if (wood) {
-        vmat_vec(bi, Z0 + (i - 1) * 5, t);
-#pragma unroll
-        for (int r = 0; r < 5; ++r) sol[r][6] = e0[r] - t[r];
-        vmat_vec(bi, Z1 + (i - 1) * 5, t);
-#pragma unroll
-        for (int r = 0; r < 5; ++r) sol[r][7] = e1[r] - t[r];
-      }
-    } else {
-#pragma unroll
-      for (int r = 0; r < 5; ++r) {
-        sol[r][5] = rhs[r];
-        sol[r][6] = e0[r];
-        sol[r][7] = e1[r];
-      }
-    }
-    // lubksb with m right-hand sides (src/math/lubksb.h)
-    for (int r = 0; r < 5; ++r) {
-      int ip = indx[r];
-      if (ip != r)
-        for (int q = 0; q < m; ++q) {
-          double tt = sol[ip][q];
-          sol[ip][q] = sol[r][q];
-          sol[r][q] = tt;
+    // lubksb on the m right-hand sides, one column per lane
+    if (lane < m) {
+      const int q = lane;
+      double* s = T.sol;
+      for (int rr = 0; rr < 5; ++rr) {
+        int ip = T.indx[rr];
+        if (ip != rr) {
+          double tt = s[ip * 8 + q];
+          s[ip * 8 + q] = s[rr * 8 + q];
+          s[rr * 8 + q] = tt;
         }
-      for (int jj = 0; jj < r; ++jj)
-        for (int q = 0; q < m; ++q) sol[r][q] -= ai[r * 5 + jj] * sol[jj][q];
-    }
-    for (int r = 4; r >= 0; --r) {
-      for (int jj = r + 1; jj < 5; ++jj)
-        for (int q = 0; q < m; ++q) sol[r][q] -= ai[r * 5 + jj] * sol[jj][q];
-      for (int q = 0; q < m; ++q) sol[r][q] /= ai[r * 5 + r];
-    }
-    for (int r = 0; r < 5; ++r)
-      for (int q = 0; q < m; ++q)
-        if (!isfinite(sol[r][q])) ok = false;
-    if (!ok) break;
-#pragma unroll
-    for (int r = 0; r < 5; ++r) {
-#pragma unroll
-      for (int q = 0; q < 5; ++q) A[i * 25 + r * 5 + q] = sol[r][q];
-      D[i * 5 + r] = sol[r][5];
-      if (wood) {
-        Z0[i * 5 + r] = sol[r][6];
-        Z1[i * 5 + r] = sol[r][7];
+        for (int jj = 0; jj < rr; ++jj) s[rr * 8 + q] -= T.lu[rr * 5 + jj] * s[jj * 8 + q];
+      }
+      for (int rr = 4; rr >= 0; --rr) {
+        for (int jj = rr + 1; jj < 5; ++jj)
+          s[rr * 8 + q] -= T.lu[rr * 5 + jj] * s[jj * 8 + q];
+        s[rr * 8 + q] /= T.lu[rr * 5 + rr];
       }
     }
+    __syncwarp();
+    bool f = true;
+    for (int e = lane; e < 5 * m; e += 32) f = f && isfinite(T.sol[(e / m) * 8 + (e % m)]);
+    ok = __all_sync(0xffffffffu, f);
+    if (!ok) break;
+    if (lane < 25) {
+      aprev = T.sol[r * 8 + c];
+      A[i * 25 + lane] = aprev;
+    }
+    if (lane < 15) {
+      const int q5 = lane / 5, rr = lane % 5;
+      double v = T.sol[rr * 8 + 5 + q5];
+      (q5 == 0 ? D : (q5 == 1 ? Z0 : Z1))[i * 5 + rr] = v;
+      T.prev[q5 * 5 + rr] = v;
+    }
+    __syncwarp();
   }
   if (ok) {
+    // back substitution: d[i] -= a'[i] d[i+1] (and z0, z1); lane q5*5+rr
+    // owns row rr of vector q5, the running vector in T.prev
     for (int i = n - 2; i >= 0; --i) {
-      double t[5];
-      vmat_vec(A + i * 25, D + (i + 1) * 5, t);
-      for (int r = 0; r < 5; ++r) D[i * 5 + r] -= t[r];
-      if (wood) {
-        vmat_vec(A + i * 25, Z0 + (i + 1) * 5, t);
-        for (int r = 0; r < 5; ++r) Z0[i * 5 + r] -= t[r];
-        vmat_vec(A + i * 25, Z1 + (i + 1) * 5, t);
-        for (int r = 0; r < 5; ++r) Z1[i * 5 + r] -= t[r];
+      if (lane < 25) T.lu[lane] = A[i * 25 + lane];
+      __syncwarp();
+      double v = 0.;
+      if (lane < 15) {
+        const int q5 = lane / 5, rr = lane % 5;
+        const double* x = T.prev + q5 * 5;
+        double t = T.lu[rr * 5] * x[0];
+#pragma unroll
+        for (int k = 1; k < 5; ++k) t += T.lu[rr * 5 + k] * x[k];
+        double* vec = q5 == 0 ? D : (q5 == 1 ? Z0 : Z1);
+        v = vec[i * 5 + rr] - t;
+        vec[i * 5 + rr] = v;
       }
+      __syncwarp();
+      if (lane < 15) T.prev[lane] = v;
+      __syncwarp();
     }
     if (wood) {
+      __syncwarp();
       VicK K0 = vic_krows(B, n, 0), K1 = vic_krows(B, n, n - 1);
       double k0 = -K0.t0 / dtc, k1 = -K1.t1 / dtc;
       k0 = k0 * 1.;
@@ -492,33 +519,39 @@ __global__ void __launch_bounds__(128)
       double det = m00 * m11 - m01 * m10;
       double al0 = (m11 * r0 - m01 * r1) / det;
       double al1 = (m00 * r1 - m10 * r0) / det;
-      for (int i = 0; i < n; ++i)
-        for (int r = 0; r < 5; ++r) {
-          D[i * 5 + r] -= Z0[i * 5 + r] * al0;
-          D[i * 5 + r] -= Z1[i * 5 + r] * al1;
-        }
+      __syncwarp();
+      for (int e = lane; e < 5 * n; e += 32) {
+        double d = D[e];
+        d -= Z0[e] * al0;
+        d -= Z1[e] * al1;
+        D[e] = d;
+      }
     }
-    for (int i = 0; i < n && ok; ++i)
-      for (int r = 0; r < 5; ++r)
-        if (!isfinite(D[i * 5 + r])) ok = false;
+    __syncwarp();
+    bool f = true;
+    for (int e = lane; e < 5 * n; e += 32) f = f && isfinite(D[e]);
+    ok = __all_sync(0xffffffffu, f);
   }
   // a failed column is marked in its solution: the finish keeps du0
-  if (!ok) {
+  if (!ok && lane == 0) {
     D[0] = __longlong_as_double(0x7ff8000000000000ll);
     atomicOr(&status[blockIdx.y], kVicFailed);
   }
 }
 
 // (3) redistribution, the gravity-work remainder and the RK combine of each
-// column (one thread per column)
-__global__ void __launch_bounds__(128)
+// column, one warp per column: the serial passes of the constituent column
+// (sums, face-mass prefix, availability clamp) on lane 0, the per-layer maps
+// on every lane
+__global__ void __launch_bounds__(32 * kVicWarps)
     vic_finish_kernel(const BlockDev* __restrict__ tab, StageParams p) {
   const BlockDev& B = tab[blockIdx.y];
   if (!B.implicit) return;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const VicScratch S = vic_scratch(B);
   const int ng = B.ng, nc1 = B.nc1, n = nc1 - 2 * ng;
   const size_t ncol = S.cells / n;
-  const size_t col = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t col = (size_t)blockIdx.x * kVicWarps + wid;
   if (col >= ncol) return;
   const size_t plane = (size_t)nc1 * B.nc2 * B.nc3;
   const real* uin = static_cast<const real*>(B.buf[p.in]);
@@ -540,52 +573,51 @@ __global__ void __launch_bounds__(128)
   double* mM = S.Z0 + col * n * 5;  // n + 1: the face mass below layer i
   double* mq = mM + (n + 1);        // n + 1: the moved total mass
   double* mdn = mq + (n + 1);       // n: the dry-gas increment
+  double* rho = mdn + n;            // n: the density of each layer
   if (ok) {
-    double R = 0, Ssum = 0;
-    for (int i = 0; i < n; ++i) {
+    for (int i = lane; i < n; i += 32) {
       double w[5];
       vic_prim(uin, plane, base + i, B.gammad, w);
-      double phi = (D[i * 5] - du[i]) * vol;
-      mq[i] = phi;  // staged: phi of layer i
-      R += phi;
-      Ssum += w[0] * vol;
+      rho[i] = w[0];
+      mdn[i] = 0.;
+      mq[i] = (D[i * 5] - du[i]) * vol;  // staged: phi of layer i
     }
-    double M = 0;
-    for (int i = 0; i < n; ++i) {
-      double w[5];
-      vic_prim(uin, plane, base + i, B.gammad, w);
-      mM[i] = M;
-      M -= mq[i] - R * (w[0] * vol / Ssum);
+    __syncwarp();
+    if (lane == 0) {
+      double R = 0, Ssum = 0;
+      for (int i = 0; i < n; ++i) {
+        R += mq[i];
+        Ssum += rho[i] * vol;
+      }
+      double M = 0;
+      for (int i = 0; i < n; ++i) {
+        mM[i] = M;
+        M -= mq[i] - R * (rho[i] * vol / Ssum);
+      }
+      mM[n] = 0.;
+      for (int i = 0; i <= n; ++i) mq[i] = 0.;
+      double avail = (rho[0] * 1. + du[0]) * vol;
+      if (avail < 0) avail = 0;
+      for (int i = 0; i + 1 < n; ++i) {
+        double avail_up = (rho[i + 1] * 1. + du[i + 1]) * vol;
+        if (avail_up < 0) avail_up = 0;
+        double Mf = mM[i + 1];
+        double q = Mf > 0 ? Mf * 1. : Mf * 1.;
+        if (q > avail) q = avail;
+        if (q < -avail_up) q = -avail_up;
+        mdn[i] -= q / vol;
+        mdn[i + 1] += q / vol;
+        mq[i + 1] = q;
+        avail = avail_up + q;
+      }
     }
-    mM[n] = 0.;
-    for (int i = 0; i <= n; ++i) mq[i] = 0.;
-    for (int i = 0; i < n; ++i) mdn[i] = 0.;
-    double w0c[5];
-    vic_prim(uin, plane, base, B.gammad, w0c);
-    double avail = (w0c[0] * 1. + du[0]) * vol;
-    if (avail < 0) avail = 0;
-    for (int i = 0; i + 1 < n; ++i) {
-      double wu[5];
-      vic_prim(uin, plane, base + i + 1, B.gammad, wu);
-      double avail_up = (wu[0] * 1. + du[i + 1]) * vol;
-      if (avail_up < 0) avail_up = 0;
-      double Mf = mM[i + 1];
-      double q = Mf > 0 ? Mf * 1. : Mf * 1.;
-      if (q > avail) q = avail;
-      if (q < -avail_up) q = -avail_up;
-      mdn[i] -= q / vol;
-      mdn[i + 1] += q / vol;
-      mq[i + 1] = q;
-      avail = avail_up + q;
-    }
-    for (int i = 0; i < n; ++i) {
+    __syncwarp();
+    for (int i = lane; i < n; i += 32) {
       du[i] += mdn[i];
       du[cs + i] = D[i * 5 + 1];
       du[2 * cs + i] = D[i * 5 + 2];
       du[3 * cs + i] = D[i * 5 + 3];
-      du[4 * cs + i] = D[i * 5 + 4];
-    }
-    for (int i = 0; i < n; ++i) {
+      double e = D[i * 5 + 4];
       double projected = (mM[i] - mM[i + 1]) / vol;
       double ph = -grav * x1v[i];
       double pw = ph * (D[i * 5] - du0[i] - projected);
@@ -593,12 +625,15 @@ __global__ void __launch_bounds__(128)
       double dp_hi = -grav * (x1f[i + 1] - x1v[i]);
       double mv_lo = mq[i] - mM[i], mv_hi = mq[i + 1] - mM[i + 1];
       double cw = -(dp_hi * mv_hi - dp_lo * mv_lo) / vol;
-      du[4 * cs + i] += pw + cw;
+      du[4 * cs + i] = e + (pw + cw);
     }
+    __syncwarp();
     if (wood) {
-      // remainder g1 sigma^2 s[du - du0] - K (raw - du0), reading the moved
-      // and raw mass changes of the neighbours
-      for (int i = 0; i < n; ++i) {
+      // the remainder g1 sigma^2 s[du - du0] - K (raw - du0) of each layer,
+      // from the final IDN row of its neighbours
+      // staged in mdn (free again): every layer's work reads the IDN row
+      // only, so the IPR row is written after all of them
+      for (int i = lane; i < n; i += 32) {
         double wt[3];
         int i0;
         vic_slope(x1v, n, i, wt, &i0);
@@ -608,23 +643,25 @@ __global__ void __launch_bounds__(128)
         double sl = wt[0] * mv0;
         sl += wt[1] * mv1;
         sl += wt[2] * mv2;
-        double work = K.gv * sl;
+        double wk = K.gv * sl;
         auto rw = [&](int k) { return D[k * 5] - du0[k]; };
         double s = K.mid * rw(i);
         if (i >= 1) s += K.lo * rw(i - 1);
         if (i <= n - 2) s += K.hi * rw(i + 1);
         if (i == 0) s += K.t0 * rw(2);
         if (i == n - 1) s += K.t1 * rw(n - 3);
-        work -= s;
-        mdn[i] = work;  // staged: the IDN row above is final before writes
+        wk -= s;
+        mdn[i] = wk;
       }
-      for (int i = 0; i < n; ++i) du[4 * cs + i] += mdn[i];
+      __syncwarp();
+      for (int i = lane; i < n; i += 32) du[4 * cs + i] += mdn[i];
     }
+    __syncwarp();
   }
   // the RK combine of the column (a failed column keeps the explicit du)
   const double* dsel = ok ? S.du + col * n : du0;
   const real w0 = real(p.w0), w1 = real(p.w1), w2 = real(p.w2);
-  for (int i = 0; i < n; ++i) {
+  for (int i = lane; i < n; i += 32) {
     const size_t c = base + i;
 #pragma unroll
     for (int v = 0; v < NHYDRO; ++v) {

@@ -5,6 +5,7 @@ current), as FP64 primitive tensors ``hydro_w`` of shape (5, nc3, nc2, nc1).
 from __future__ import annotations
 
 import math
+from typing import Optional
 
 import torch
 
@@ -29,6 +30,39 @@ def sod(options: MeshBlockOptions, device="cuda") -> torch.Tensor:
     w[0] = torch.where(left, float(p.get("rho_l", 1.0)), float(p.get("rho_r", 0.125)))
     w[4] = torch.where(left, float(p.get("p_l", 1.0)), float(p.get("p_r", 0.1)))
     return w
+
+
+def ensemble_members(n: int = 64, seed: int = 20261203,
+                     deck: str = "straka.yaml", precision: Optional[str] = None,
+                     nx2_choices=(128, 256, 384, 512),
+                     nx1_choices=(32, 64, 96, 128), dx: float = 50.0,
+                     device="cpu"):
+    """Members of a Straka-type ensemble: member k draws, from a generator
+    seeded with seed + k, its size (nx2, nx1) uniformly from the choices, a
+    bubble amplitude dT ~ U[-20, -10] K, a centre xc ~ U[0, 0.25 Lx],
+    zc ~ U[0.3, 0.6] Lz, and radii min(4 km, 0.15 Lx), min(2 km, 0.3 Lz).
+    Returns [(options, hydro_w)]."""
+    import os
+    path = deck if os.path.isabs(deck) else os.path.join(
+        os.path.dirname(os.path.abspath(__file__)), "decks", deck)
+    out = []
+    for k in range(n):
+        g = torch.Generator().manual_seed(seed + k)
+        pick = lambda seq: seq[int(torch.randint(len(seq), (1,), generator=g))]
+        nx2, nx1 = pick(nx2_choices), pick(nx1_choices)
+        u = torch.rand(3, generator=g, dtype=torch.float64)
+        opts = MeshBlockOptions.from_yaml(path)
+        c = opts.coord()
+        c.nx1, c.nx2 = nx1, nx2
+        c.x1max, c.x2max = nx1 * dx, nx2 * dx
+        if precision:
+            opts.hydro().precision = precision
+        Lx, Lz = nx2 * dx, nx1 * dx
+        w = straka(opts, device, dT=-20.0 + 10.0 * float(u[0]),
+                   xc=0.25 * Lx * float(u[1]), zc=(0.3 + 0.3 * float(u[2])) * Lz,
+                   xr=min(4.e3, 0.15 * Lx), zr=min(2.e3, 0.3 * Lz))
+        out.append((opts, w))
+    return out
 
 
 def straka(options: MeshBlockOptions, device="cuda", dT=None, xc=None, zc=None,
