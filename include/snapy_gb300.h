@@ -159,6 +159,27 @@ int sg_kernel_times(sg_handle* h, double* ms, int64_t* launches);
 const char* sg_last_error(void);
 const char* sg_version(void);
 
+/* Allocation-free time step.  No counterpart in the reference: it is for
+ * callers that may not allocate device memory at all (a host that hands in
+ * views of its own pre-allocated arena, a serving loop held to a fixed HBM
+ * budget).  It computes what sg_max_dt computes for up to
+ * SG_NOALLOC_MAX_BLOCKS blocks described by value, with its reduction scratch
+ * in a file-scope device array (SG_NOALLOC_MAX_BLOCKS x 16 bytes per GPU);
+ * more blocks are refused with an error.  The scratch is cleared by each
+ * call's first kernel; calls that overlap on the GPU race on it, so the
+ * caller serialises them.  The first call on each device looks the array's
+ * address up and must come before any stream capture on that device. */
+#define SG_NOALLOC_MAX_BLOCKS 64
+typedef struct sg_dt_block {
+  const void* u;      /* current conserved state, (5, nc3, nc2, nc1) */
+  int32_t nc1, nc2, nc3, ng;
+  double dx1, dx2, dx3, gammad;
+  double dt_src;      /* source-term bound (0: none) */
+  int32_t implicit;   /* 1: vertical implicit solve, x1 acoustic bound off */
+} sg_dt_block;
+int sg_max_dt_noalloc(const sg_dt_block* blocks, int32_t nblock, int32_t dtype,
+                      double cfl, const int32_t* redo_dev, double* dt_out_dev,
+                      sg_stream_t stream);
 
 #ifdef __cplusplus
 }

@@ -57,6 +57,16 @@ class BlockDesc(ctypes.Structure):
     ]
 
 
+class DtBlock(ctypes.Structure):
+    """sg_dt_block: one block of the allocation-free time step."""
+    _fields_ = [("u", _vp), ("nc1", _i32), ("nc2", _i32), ("nc3", _i32),
+                ("ng", _i32), ("dx1", ctypes.c_double), ("dx2", ctypes.c_double),
+                ("dx3", ctypes.c_double), ("gammad", ctypes.c_double),
+                ("dt_src", ctypes.c_double), ("implicit", _i32)]
+
+
+NOALLOC_MAX_BLOCKS = 64  # SG_NOALLOC_MAX_BLOCKS
+
 # SG_KERNEL_* of sg_kernel_times
 KERNELS = ("stage_kernel", "vic_assemble_kernel", "vic_solve_kernel",
            "vic_finish_kernel", "ghost_kernel")
@@ -89,6 +99,8 @@ SIGNATURES = {
                                        ctypes.POINTER(ctypes.c_int64)]),
     "sg_last_error": (ctypes.c_char_p, []),
     "sg_version": (ctypes.c_char_p, []),
+    "sg_max_dt_noalloc": (ctypes.c_int, [ctypes.POINTER(DtBlock), _i32, _i32,
+                                         ctypes.c_double, _vp, _vp, _vp]),
 }
 
 _lib = None

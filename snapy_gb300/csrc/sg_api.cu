@@ -192,6 +192,9 @@ extern "C" {
 
 const char* sg_last_error(void) { return g_err.c_str(); }
 
+// records `msg` as the calling thread's last error for entry points defined
+// in other translation units; returns `code`
+int sg_fail_message(int code, const char* msg) { return fail(code, "%s", msg); }
 const char* sg_version(void) { return "snapy_gb300 0.1 (sm_103a)"; }
 
 int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
