@@ -13,9 +13,10 @@ on the host), dt fixed at the CFL step of the initial state.
 * e2e: the same steps through the public API with HOST buffers: each step
   copies the state host->device from pinned memory, advances it and copies it
   back (bytes counted from the copied tensors).
-* roofline: the stage kernel's algorithmic bytes per launch over its mean
-  duration (CUDA events around each stage call: the stage kernel and its
-  ghost-fill kernel) against the measured HBM copy peak.
+* roofline: the dominant kernel's algorithmic bytes per launch over its mean
+  duration (CUDA events the library records around each kernel of an eager
+  stage, on the launching stream) against the measured HBM copy peak; the
+  "kernels" object gives every kernel's launches, mean time and share.
 * cpu_baseline: the CPU oracle (the reference algorithm restated in C, FP64,
   OpenMP on every host core) on a bounded sample of the same workload.
 
@@ -275,23 +276,39 @@ def run_native(args):
         t_total = float(t.item())
     value = cells * args.steps * world / t_total
 
-    # roofline of the stage kernel: per stage call, events on the stream
+    # roofline of the dominant kernel: the library records events around
+    # each kernel of every eager stage on the launching stream
     b = blk.batch
     s_bytes = torch.finfo(blk.dtype).bits // 8
-    stage_ms, stage_bytes = [], []
-    for k in range(min(args.steps, 50)):
+    implicit = bool(opts.hydro().icorr)
+    b.set_timing(True)
+    nrep = min(args.steps, 50)
+    for k in range(nrep):
         flush.zero_()
         for st in range(3):
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
             b.stage(st)
-            e1.record(stream)
-            stage_ms.append((e0, e1))
-            stage_bytes.append((2 if st == 0 else 3) * 5 * s_bytes * cells)
     torch.cuda.synchronize()
-    durs = [a.elapsed_time(bb) / 1e3 for a, bb in stage_ms]
-    achieved = sum(stage_bytes) / sum(durs) / 1e9
+    kt = b.kernel_times()
+    b.set_timing(False)
+    # algorithmic bytes per launch of each kernel (per interior cell, times
+    # the cells one launch covers; stages 2-3 of an explicit stage also read u0)
+    ghost_cells = c.nc1 * c.nc2 * max(1, c.nc3) - cells
+    per_launch = {
+        "stage_kernel": ((5 * s_bytes + 40) if implicit else
+                         5 * s_bytes * (2 + 3 + 3) / 3) * cells,
+        "vic_assemble_kernel": (5 * s_bytes + 40 + 40 + 600) * cells,
+        "vic_solve_kernel": (600 + 40 + 200 + 120 + 200 + 120 + 120) * cells,
+        "vic_finish_kernel": (120 + 15 * s_bytes) * cells,
+        "ghost_kernel": 2 * 5 * s_bytes * ghost_cells,
+    }
+    dom = max(kt, key=lambda k: kt[k][0])
+    dom_ms, dom_n = kt[dom]
+    achieved = per_launch[dom] * dom_n / (dom_ms / 1e3) / 1e9
     peak, peak_kind = peaks()
+    kernels = {k: {"launches": n, "mean_us": ms / n * 1e3,
+                   "share": ms / sum(v[0] for v in kt.values()),
+                   "bytes_per_launch": per_launch.get(k)}
+               for k, (ms, n) in kt.items()}
 
     # end to end through the public API with host buffers
     u_host = torch.empty(vars["hydro_u"].shape, dtype=blk.dtype).pin_memory()
@@ -332,9 +349,13 @@ def run_native(args):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak,
                          "peak_kind": peak_kind, "traffic": None,
-                         "kernel": "stage_kernel (+ ghost fill)",
-                         "bytes_per_launch": statistics.mean(stage_bytes),
-                         "mean_launch_us": statistics.mean(durs) * 1e6},
+                         "kernel": dom,
+                         "bytes_per_launch": per_launch[dom],
+                         "mean_launch_us": dom_ms / dom_n * 1e3,
+                         "limiter": "FP64 issue rate (one FP64 warp "
+                                    "instruction per SM per 16 cycles)"
+                                    if blk.dtype == torch.float64 else None},
+            "kernels": kernels,
             "cpu_baseline": cb,
             "clocks": clk.summary(),
             "gpu_launches": args.steps * 3 * b.launches_per_stage(),

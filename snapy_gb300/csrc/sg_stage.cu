@@ -995,12 +995,13 @@ extern "C" int SG_NAME(sg_launch_vic)(const BlockDev* tab, StageParams p,
   if (e != cudaSuccess) return (int)e;
   if (ev) cudaEventRecord(ev[0], stream);
   // one warp per column
-  int gc = (int)((max_cols + kVicWarps - 1) / kVicWarps);
-  vic_solve_kernel<<<dim3(gc, p.nblock), 32 * kVicWarps, 0, stream>>>(tab, p,
-                                                                      status);
+  // the solve: kVicCols columns per single-warp CTA
+  int gs = (int)((max_cols + kVicCols - 1) / kVicCols);
+  vic_solve_kernel<<<dim3(gs, p.nblock), 32, 0, stream>>>(tab, p, status);
   e = cudaGetLastError();
   if (e != cudaSuccess) return (int)e;
   if (ev) cudaEventRecord(ev[1], stream);
+  int gc = (int)((max_cols + kVicWarps - 1) / kVicWarps);
   vic_finish_kernel<<<dim3(gc, p.nblock), 32 * kVicWarps, 0, stream>>>(tab, p);
   return (int)cudaGetLastError();
 }

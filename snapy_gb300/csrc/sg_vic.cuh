@@ -295,220 +295,316 @@ __global__ void __launch_bounds__(kThreads)
 
 // ludcmp<double, 5, Implicit> on a row-major 5x5 in shared memory
 // (src/math/ludcmp.h); one lane runs it
-__device__ __forceinline__ int vludcmp(double* a, int* indx) {
-  int i, imax = 0, j, k, d;
-  double big, dum, sum, temp, vv[5], scale[5];
-  const double tolerance = 8. * 5 * 2.220446049250313e-16;
-  for (int q = 0; q < 25; ++q)
-    if (!isfinite(a[q])) return 0;
-  d = 1;
-  for (i = 0; i < 5; i++) {
-    big = 0.0;
-    for (j = 0; j < 5; j++)
-      if ((temp = fabs(a[i * 5 + j])) > big) big = temp;
-    if (big == 0.0) return 0;
-    scale[i] = big;
-    vv[i] = 1.0 / big;
-    if (!isfinite(vv[i])) return 0;
-  }
-  for (j = 0; j < 5; j++) {
-    for (i = 0; i < j; i++) {
-      sum = a[i * 5 + j];
-      for (k = 0; k < i; k++) sum -= a[i * 5 + k] * a[k * 5 + j];
-      if (!isfinite(sum)) return 0;
-      a[i * 5 + j] = sum;
-    }
-    big = 0.0;
-    for (i = j; i < 5; i++) {
-      sum = a[i * 5 + j];
-      for (k = 0; k < j; k++) sum -= a[i * 5 + k] * a[k * 5 + j];
-      if (!isfinite(sum)) return 0;
-      a[i * 5 + j] = sum;
-      dum = vv[i] * fabs(sum);
-      if (!isfinite(dum)) return 0;
-      if (dum >= big) {
-        big = dum;
-        imax = i;
-      }
-    }
-    if (j != imax) {
-      for (k = 0; k < 5; k++) {
-        dum = a[imax * 5 + k];
-        a[imax * 5 + k] = a[j * 5 + k];
-        a[j * 5 + k] = dum;
-      }
-      d = -d;
-      vv[imax] = vv[j];
-      temp = scale[imax];
-      scale[imax] = scale[j];
-      scale[j] = temp;
-    }
-    indx[j] = imax;
-    if (fabs(a[j * 5 + j]) / scale[j] <= tolerance) return 0;
-    if (j != 4) {
-      dum = (1.0 / a[j * 5 + j]);
-      for (i = j + 1; i < 5; i++) a[i * 5 + j] *= dum;
-    }
-  }
-  for (int q = 0; q < 25; ++q)
-    if (!isfinite(a[q])) return 0;
-  return d;
+// ---------------------------------------------------------------------------
+// (2) the block-Thomas sweep, back substitution and Woodbury update.
+//
+// GB300 issues one FP64 warp instruction per SM every 16 cycles however many
+// lanes it carries, so the solve packs kVicCols columns into each warp with
+// kVicLanes lanes per column, and gives every lane work in every FP64
+// instruction: lane q of a column owns right-hand-side column q of the
+// layer's system  lu [a' | d' | z0' | z1'] = [c | rhs | e0 | e1]  (q < 5: the
+// columns of c and a'; 5: d; 6, 7: the Woodbury vectors), and during the
+// factorisation column q of the block (q < 5).
+//
+// The LU is the reference's scaled partial-pivot Crout factorisation
+// (src/math/ludcmp.h) run column-per-lane in right-looking order: at step j
+// the pivot column's lane picks the pivot, every lane swaps its own column's
+// rows, and the later columns subtract L[i][j] U[j][c].  Each entry receives
+// exactly the Crout subtractions, k ascending, so the factors are bit for
+// bit the sequential ones; the failure screens of ludcmp (non-finite sums,
+// zero rows, the pivot tolerance) are evaluated on the same values and any
+// failure fails the column, as in the reference.  The back-solve is lubksb
+// (src/math/lubksb.h) per lane: its row exchanges touch only rows not yet
+// reduced, so they are applied first.
+constexpr int kVicCols = 4;   // columns per warp (one warp per CTA)
+constexpr int kVicLanes = 8;  // lanes per column
+
+// a group-wide AND over the kVicLanes lanes of this lane's column
+__device__ __forceinline__ bool vgroup_all(bool v, int g) {
+  unsigned bad = __ballot_sync(0xffffffffu, !v);
+  return ((bad >> (kVicLanes * g)) & 0xffu) == 0u;
 }
 
-constexpr int kVicWarps = 4;  // columns per CTA of the solve and finish
+__device__ __forceinline__ double vshfl(double v, int src) {
+  return __shfl_sync(0xffffffffu, v, src, kVicLanes);
+}
 
-// the per-warp shared tile of the sweep
-struct VicWarpTile {
-  double lu[25];      // a[i] - b[i] a'[i-1], factorised in place
-  double bm[25];      // b[i]
-  double sol[5 * 8];  // [row][col]: c[i] | rhs - b d' | e0 - b z0 | e1 - b z1
-  double prev[3 * 5];  // d, z0, z1 of layer i - 1
-  int indx[5];
-  int ok;
+// non-negative finite doubles order like their bit patterns
+__device__ __forceinline__ unsigned long long vbits(double x) {
+  return static_cast<unsigned long long>(__double_as_longlong(x));
+}
+
+template <typename T>
+__device__ __forceinline__ T vpick5(int k, T a0, T a1, T a2, T a3, T a4) {
+  return k == 0 ? a0 : k == 1 ? a1 : k == 2 ? a2 : k == 3 ? a3 : a4;
+}
+
+// step J of the factorisation on this lane's column x (lanes q < 5 hold the
+// block's columns; vv, scale and indx are per-lane copies of the row data)
+template <int J>
+__device__ __forceinline__ void vlu_step(double (&x)[5], double (&vv)[5],
+                                         double (&scale)[5], int (&indx)[5],
+                                         bool& good, int q, bool colane) {
+  // pivot search on column J: the last row of the largest vv |a|
+  unsigned long long best = 0ull;
+  int imax = J;
+#pragma unroll
+  for (int i2 = J; i2 < 5; ++i2) {
+    double dum = vv[i2] * fabs(x[i2]);
+    if (q == J) good = good && isfinite(dum);
+    if (vbits(dum) >= best) {
+      best = vbits(dum);
+      imax = i2;
+    }
+  }
+  imax = __shfl_sync(0xffffffffu, imax, J, kVicLanes);
+  indx[J] = imax;
+#pragma unroll
+  for (int i2 = J + 1; i2 < 5; ++i2)
+    if (imax == i2) {
+      if (colane) {
+        double t = x[J];
+        x[J] = x[i2];
+        x[i2] = t;
+      }
+      vv[i2] = vv[J];
+      double t = scale[J];
+      scale[J] = scale[i2];
+      scale[i2] = t;
+    }
+  if (J < 4) {
+    double dinv = 1.0 / vshfl(x[J], J);
+    double l[5];
+#pragma unroll
+    for (int i2 = J + 1; i2 < 5; ++i2) {
+      l[i2] = vshfl(x[i2], J) * dinv;
+      if (q == J) x[i2] = l[i2];
+    }
+    if (colane && q > J) {
+#pragma unroll
+      for (int i2 = J + 1; i2 < 5; ++i2) x[i2] = x[i2] - l[i2] * x[J];
+    }
+  }
+}
+
+struct VicSolveSmem {
+  double lu[kVicCols][25];         // the factorised block of each column
+  double vec[kVicCols][2][15];     // back substitution: d, z0, z1 of a layer
 };
 
-// (2) the block-Thomas sweep, back substitution and Woodbury update of
-// each column, one warp per column
-__global__ void __launch_bounds__(32 * kVicWarps)
+__global__ void __launch_bounds__(32)
     vic_solve_kernel(const BlockDev* __restrict__ tab, StageParams p,
                      int* status) {
-  __shared__ VicWarpTile tiles[kVicWarps];
-  const BlockDev& B = tab[blockIdx.y];
-  if (!B.implicit) return;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  VicWarpTile& T = tiles[wid];
-  const VicScratch S = vic_scratch(B);
-  const int ng = B.ng, n = B.nc1 - 2 * ng;
+  __shared__ VicSolveSmem sm;
+  const BlockDev& Bk = tab[blockIdx.y];
+  if (!Bk.implicit) return;
+  const VicScratch S = vic_scratch(Bk);
+  const int n = Bk.nc1 - 2 * Bk.ng;
   const size_t ncol = S.cells / n;
-  const size_t col = (size_t)blockIdx.x * kVicWarps + wid;
-  if (col >= ncol) return;  // whole warps leave together
+  if ((size_t)blockIdx.x * kVicCols >= ncol) return;  // the whole warp
+  const int lane = threadIdx.x, g = lane / kVicLanes, q = lane % kVicLanes;
+  const size_t col = (size_t)blockIdx.x * kVicCols + g;
+  const bool valid = col < ncol;
+  // a group past the last column shadows it and never stores
+  const size_t cc = valid ? col : ncol - 1;
   const double dtc = p.w2 * p.dt[blockIdx.y];
   const bool wood = n >= 3;
-  const int m = wood ? 8 : 6;
-  double* A = S.A + col * n * 25;
-  const double* Bm = S.B + col * n * 25;
-  const double* C = S.C + col * n * 25;
-  double* D = S.D + col * n * 5;
-  double* Z0 = S.Z0 + col * n * 5;
-  double* Z1 = S.Z1 + col * n * 5;
-  const int r = lane / 5, c = lane % 5;  // lane < 25 owns entry (r, c)
+  const int m = wood ? 8 : 6;  // right-hand sides in use
+  double* A = S.A + cc * n * 25;
+  const double* Bm = S.B + cc * n * 25;
+  const double* C = S.C + cc * n * 25;
+  double* D = S.D + cc * n * 5;
+  double* Z0 = S.Z0 + cc * n * 5;
+  double* Z1 = S.Z1 + cc * n * 5;
+  const double* du = S.du + cc * n;  // row v at du[v * cells + i]
+  double* vout = q == 5 ? D : (q == 6 ? Z0 : Z1);
+  const unsigned full = 0xffffffffu;
+
   // the input screen: du of every layer finite
   bool fin = true;
-  for (int e = lane; e < 5 * n; e += 32)
-    fin = fin && isfinite(S.du[(e / n) * S.cells + col * n + (e % n)]);
-  bool ok = __all_sync(0xffffffffu, fin);
-  double aprev = 0.;  // a'[i-1] entry (r, c) of this lane
-  for (int i = 0; i < n && ok; ++i) {
-    const size_t cell = col * n + i;
-    double aij = 0., bij = 0.;
-    if (lane < 25) {
-      aij = A[i * 25 + lane];
-      bij = Bm[i * 25 + lane];
-      T.bm[lane] = bij;
-      T.sol[r * 8 + c] = C[i * 25 + lane];
+  for (int e = q; e < 5 * n; e += kVicLanes)
+    fin = fin && isfinite(du[(size_t)(e / n) * S.cells + (e % n)]);
+  // every ballot runs on all 32 lanes: evaluate before combining
+  const bool fin_all = vgroup_all(fin, g);
+  bool ok = valid && fin_all;
+
+  double s[5];   // this lane's solution column of the previous layer
+  double b[25];  // the b block of the layer (loaded one layer ahead)
+#pragma unroll
+  for (int k = 0; k < 5; ++k) s[k] = 0.;
+#pragma unroll
+  for (int e = 0; e < 25; ++e) b[e] = Bm[e];
+  for (int i = 0; i < n; ++i) {
+    if (!__any_sync(full, ok)) break;
+    // this lane's column of a (q < 5), of c, and the right-hand sides
+    double x[5], c5[5];
+    if (q < 5) {
+#pragma unroll
+      for (int r = 0; r < 5; ++r) {
+        x[r] = A[i * 25 + r * 5 + q];
+        c5[r] = C[i * 25 + r * 5 + q];
+      }
+    } else {
+#pragma unroll
+      for (int r = 0; r < 5; ++r) {
+        x[r] = (r == 4 && ((q == 6 && i == 0) || (q == 7 && i == n - 1))) ? 1.
+                                                                         : 0.;
+        c5[r] = 0.;
+      }
     }
-    // a[i] -= b[i] a'[i-1], entry (r, c) summed over k in order
+    // du / dt_corr, one row per lane, gathered on lane 5
+    double dq = q < 5 ? du[(size_t)q * S.cells + i] / dtc : 0.;
+#pragma unroll
+    for (int r = 0; r < 5; ++r) {
+      double v = vshfl(dq, r);
+      if (q == 5) x[r] = v;
+    }
+    // x -= b s'  (a[i] - b[i] a'[i-1] and rhs - b[i] d'[i-1]), k in order
     if (i > 0) {
-      double t = 0.;
 #pragma unroll
-      for (int k = 0; k < 5; ++k) {
-        double bk = __shfl_sync(0xffffffffu, bij, r * 5 + k);
-        double ak = __shfl_sync(0xffffffffu, aprev, k * 5 + c);
-        t = k == 0 ? bk * ak : t + bk * ak;
+      for (int r = 0; r < 5; ++r) {
+        double t = b[r * 5] * s[0];
+#pragma unroll
+        for (int k = 1; k < 5; ++k) t = t + b[r * 5 + k] * s[k];
+        x[r] = x[r] - t;
       }
-      aij -= t;
     }
-    if (lane < 25) T.lu[lane] = aij;
-    __syncwarp();
-    // the right-hand sides: lane q5 * 5 + rr (q5 < 3) forms column 5 + q5
-    if (lane < 15) {
-      const int q5 = lane / 5, rr = lane % 5;
-      double base;
-      if (q5 == 0)
-        base = S.du[rr * S.cells + cell] / dtc;
-      else
-        base = (rr == 4 && ((q5 == 1 && i == 0) || (q5 == 2 && i == n - 1)))
-                   ? 1. : 0.;
-      if (i > 0) {
-        const double* v = T.prev + q5 * 5;
-        double t = T.bm[rr * 5] * v[0];
+    if (i + 1 < n) {
 #pragma unroll
-        for (int k = 1; k < 5; ++k) t += T.bm[rr * 5 + k] * v[k];
-        base = base - t;
+      for (int e = 0; e < 25; ++e) b[e] = Bm[(i + 1) * 25 + e];
+    }
+
+    // ---- the factorisation (lanes q < 5 hold the columns) ----
+    bool good = true;
+    const bool colane = q < 5;
+    unsigned long long mx[5];
+#pragma unroll
+    for (int r = 0; r < 5; ++r) {
+      if (colane) good = good && isfinite(x[r]);
+      mx[r] = colane ? vbits(fabs(x[r])) : 0ull;
+    }
+#pragma unroll
+    for (int off = 4; off >= 1; off >>= 1)
+#pragma unroll
+      for (int r = 0; r < 5; ++r) {
+        unsigned long long o = __shfl_xor_sync(full, mx[r], off, kVicLanes);
+        mx[r] = o > mx[r] ? o : mx[r];
       }
-      T.sol[rr * 8 + 5 + q5] = base;
-    }
-    __syncwarp();
-    if (lane == 0) {
+    double scale[5], vv[5];
 #pragma unroll
-      for (int q = 0; q < 5; ++q) T.indx[q] = q;
-      T.ok = vludcmp(T.lu, T.indx) != 0;
+    for (int r = 0; r < 5; ++r) {
+      scale[r] = __longlong_as_double(static_cast<long long>(mx[r]));
+      good = good && mx[r] != 0ull;
     }
+    {
+      double big = vpick5(q < 5 ? q : 0, scale[0], scale[1], scale[2],
+                          scale[3], scale[4]);
+      double inv = 1.0 / big;
+#pragma unroll
+      for (int r = 0; r < 5; ++r) vv[r] = vshfl(inv, r);
+    }
+#pragma unroll
+    for (int r = 0; r < 5; ++r) good = good && isfinite(vv[r]);
+    int indx[5];
+    vlu_step<0>(x, vv, scale, indx, good, q, colane);
+    vlu_step<1>(x, vv, scale, indx, good, q, colane);
+    vlu_step<2>(x, vv, scale, indx, good, q, colane);
+    vlu_step<3>(x, vv, scale, indx, good, q, colane);
+    vlu_step<4>(x, vv, scale, indx, good, q, colane);
+    if (colane) {
+#pragma unroll
+      for (int r = 0; r < 5; ++r) good = good && isfinite(x[r]);
+      // the pivot tolerance of every step, on the final diagonal and scale
+      double dg = vpick5(q, x[0], x[1], x[2], x[3], x[4]);
+      double sc = vpick5(q, scale[0], scale[1], scale[2], scale[3], scale[4]);
+      good = good && !(fabs(dg) / sc <= 8. * 5 * 2.220446049250313e-16);
+      // stage the factors for every lane's back-solve
+#pragma unroll
+      for (int r = 0; r < 5; ++r) sm.lu[g][r * 5 + q] = x[r];
+    }
+    const bool good_all = vgroup_all(good, g);
+    ok = ok && good_all;
     __syncwarp();
-    if (!T.ok) {
-      ok = false;
-      break;
-    }
-    // lubksb on the m right-hand sides, one column per lane
-    if (lane < m) {
-      const int q = lane;
-      double* s = T.sol;
-      for (int rr = 0; rr < 5; ++rr) {
-        int ip = T.indx[rr];
-        if (ip != rr) {
-          double tt = s[ip * 8 + q];
-          s[ip * 8 + q] = s[rr * 8 + q];
-          s[rr * 8 + q] = tt;
+
+    // ---- lubksb on this lane's right-hand side ----
+    double sol[5];
+#pragma unroll
+    for (int r = 0; r < 5; ++r) sol[r] = colane ? c5[r] : x[r];
+#pragma unroll
+    for (int rr = 0; rr < 5; ++rr) {
+      const int ip = indx[rr];
+#pragma unroll
+      for (int k = rr + 1; k < 5; ++k)
+        if (ip == k) {
+          double t = sol[k];
+          sol[k] = sol[rr];
+          sol[rr] = t;
         }
-        for (int jj = 0; jj < rr; ++jj) s[rr * 8 + q] -= T.lu[rr * 5 + jj] * s[jj * 8 + q];
-      }
-      for (int rr = 4; rr >= 0; --rr) {
-        for (int jj = rr + 1; jj < 5; ++jj)
-          s[rr * 8 + q] -= T.lu[rr * 5 + jj] * s[jj * 8 + q];
-        s[rr * 8 + q] /= T.lu[rr * 5 + rr];
-      }
     }
-    __syncwarp();
+    const double* lu = sm.lu[g];
+#pragma unroll
+    for (int rr = 1; rr < 5; ++rr)
+#pragma unroll
+      for (int jj = 0; jj < rr; ++jj) sol[rr] = sol[rr] - lu[rr * 5 + jj] * sol[jj];
+#pragma unroll
+    for (int rr = 4; rr >= 0; --rr) {
+#pragma unroll
+      for (int jj = rr + 1; jj < 5; ++jj)
+        sol[rr] = sol[rr] - lu[rr * 5 + jj] * sol[jj];
+      sol[rr] = sol[rr] / lu[rr * 5 + rr];
+    }
     bool f = true;
-    for (int e = lane; e < 5 * m; e += 32) f = f && isfinite(T.sol[(e / m) * 8 + (e % m)]);
-    ok = __all_sync(0xffffffffu, f);
-    if (!ok) break;
-    if (lane < 25) {
-      aprev = T.sol[r * 8 + c];
-      A[i * 25 + lane] = aprev;
+    if (q < m) {
+#pragma unroll
+      for (int r = 0; r < 5; ++r) f = f && isfinite(sol[r]);
     }
-    if (lane < 15) {
-      const int q5 = lane / 5, rr = lane % 5;
-      double v = T.sol[rr * 8 + 5 + q5];
-      (q5 == 0 ? D : (q5 == 1 ? Z0 : Z1))[i * 5 + rr] = v;
-      T.prev[q5 * 5 + rr] = v;
+    const bool f_all = vgroup_all(f, g);
+    ok = ok && f_all;
+    if (valid) {
+      if (colane) {
+#pragma unroll
+        for (int r = 0; r < 5; ++r) A[i * 25 + r * 5 + q] = sol[r];
+      } else if (q < m) {
+#pragma unroll
+        for (int r = 0; r < 5; ++r) vout[i * 5 + r] = sol[r];
+      }
     }
+#pragma unroll
+    for (int r = 0; r < 5; ++r) s[r] = sol[r];
     __syncwarp();
   }
-  if (ok) {
-    // back substitution: d[i] -= a'[i] d[i+1] (and z0, z1); lane q5*5+rr
-    // owns row rr of vector q5, the running vector in T.prev
-    for (int i = n - 2; i >= 0; --i) {
-      if (lane < 25) T.lu[lane] = A[i * 25 + lane];
-      __syncwarp();
-      double v = 0.;
-      if (lane < 15) {
-        const int q5 = lane / 5, rr = lane % 5;
-        const double* x = T.prev + q5 * 5;
-        double t = T.lu[rr * 5] * x[0];
+
+  // ---- back substitution: x[i] -= a'[i] x[i+1] for d, z0, z1 ----
+  // lane q handles the (vector, row) pairs q and q + 8 of the 15
+  if (__any_sync(full, ok)) {
+    if (q >= 5) {
 #pragma unroll
-        for (int k = 1; k < 5; ++k) t += T.lu[rr * 5 + k] * x[k];
-        double* vec = q5 == 0 ? D : (q5 == 1 ? Z0 : Z1);
-        v = vec[i * 5 + rr] - t;
-        vec[i * 5 + rr] = v;
+      for (int r = 0; r < 5; ++r) sm.vec[g][0][(q - 5) * 5 + r] = s[r];
+    }
+    __syncwarp();
+    int cur = 0;
+    for (int i = n - 2; i >= 0; --i) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int pr = q + kVicLanes * h;
+        if (pr < 15) {
+          const int v = pr / 5, r = pr % 5;
+          const double* xn = sm.vec[g][cur] + v * 5;
+          const double* ar = A + i * 25 + r * 5;
+          double t = ar[0] * xn[0];
+#pragma unroll
+          for (int k = 1; k < 5; ++k) t = t + ar[k] * xn[k];
+          double* vec = v == 0 ? D : (v == 1 ? Z0 : Z1);
+          double val = vec[i * 5 + r] - t;
+          if (ok) vec[i * 5 + r] = val;
+          sm.vec[g][cur ^ 1][pr] = val;
+        }
       }
       __syncwarp();
-      if (lane < 15) T.prev[lane] = v;
-      __syncwarp();
+      cur ^= 1;
     }
-    if (wood) {
-      __syncwarp();
-      VicK K0 = vic_krows(B, n, 0), K1 = vic_krows(B, n, n - 1);
+    if (wood && ok) {
+      VicK K0 = vic_krows(Bk, n, 0), K1 = vic_krows(Bk, n, n - 1);
       double k0 = -K0.t0 / dtc, k1 = -K1.t1 / dtc;
       k0 = k0 * 1.;
       k1 = k1 * 1.;
@@ -519,8 +615,10 @@ __global__ void __launch_bounds__(32 * kVicWarps)
       double det = m00 * m11 - m01 * m10;
       double al0 = (m11 * r0 - m01 * r1) / det;
       double al1 = (m00 * r1 - m10 * r0) / det;
-      __syncwarp();
-      for (int e = lane; e < 5 * n; e += 32) {
+      // this column's lanes (ok and wood are uniform over them) finish
+      // reading D and Z before any of them updates D
+      __syncwarp(0xffu << (kVicLanes * g));
+      for (int e = q; e < 5 * n; e += kVicLanes) {
         double d = D[e];
         d -= Z0[e] * al0;
         d -= Z1[e] * al1;
@@ -529,15 +627,19 @@ __global__ void __launch_bounds__(32 * kVicWarps)
     }
     __syncwarp();
     bool f = true;
-    for (int e = lane; e < 5 * n; e += 32) f = f && isfinite(D[e]);
-    ok = __all_sync(0xffffffffu, f);
+    if (ok)
+      for (int e = q; e < 5 * n; e += kVicLanes) f = f && isfinite(D[e]);
+    const bool d_all = vgroup_all(f, g);
+    ok = ok && d_all;
   }
   // a failed column is marked in its solution: the finish keeps du0
-  if (!ok && lane == 0) {
+  if (valid && !ok && q == 0) {
     D[0] = __longlong_as_double(0x7ff8000000000000ll);
     atomicOr(&status[blockIdx.y], kVicFailed);
   }
 }
+
+constexpr int kVicWarps = 4;  // columns per CTA of the finish (a warp each)
 
 // (3) redistribution, the gravity-work remainder and the RK combine of each
 // column, one warp per column: the serial passes of the constituent column
