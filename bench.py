@@ -96,6 +96,7 @@ def config_of(opts, workload, args, nranks):
         "gravity": bool(h.grav and h.grav.grav1),
         "implicit": bool(h.icorr),
         "l2": "flushed between timed steps (512 MiB write; the block fits in L2)",
+        "graphs": "one per buffer rotation, captured before the warm-up steps",
         "replicas": nranks,
         "parallelism": "replicas" if nranks > 1 else "single",
     }
@@ -251,6 +252,13 @@ def run_native(args):
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream()
 
+    # capture the step graphs of both steady buffer rotations first (steps
+    # 1-3 run eagerly, 4 and 5 capture), so no capture lands in the timed
+    # region; then the warm-up steps
+    for _ in range(8):
+        if blk.execution_report()["captures"] >= 2:
+            break
+        blk.step(vars, dt)
     for _ in range(max(3, args.warmup)):
         blk.step(vars, dt)
     torch.cuda.synchronize()

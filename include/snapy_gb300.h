@@ -94,6 +94,14 @@ typedef struct sg_block_desc {
   /* integration/implicit-scheme: 0 (none) or 9 (the full 5x5 vertical
    * implicit solve, FP64; needs const-gravity and reflecting x1 walls) */
   int32_t implicit_scheme;
+  /* SG_F32 with gravity: the FP64 hydrostatic base the FP32 state is stored
+   * about (the buffers hold u - u_b), 5 nc1 + 1 device doubles:
+   *   rho_b[nc1] | p_b[nc1] | e_b[nc1] = p_b/(gamma-1) |
+   *   pf_b[nc1+1] (face f between cells f-1 and f) |
+   *   r_b[nc1] = rho_b grav1 - (pf_b[i+1] - pf_b[i]) / dx1
+   * The contents may be written after sg_create, before sg_init_from_prim.
+   * Must be null otherwise. */
+  const double* base;
 } sg_block_desc;
 
 int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,

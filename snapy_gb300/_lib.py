@@ -54,6 +54,7 @@ class BlockDesc(ctypes.Structure):
         ("x1f", _vp),
         ("x1v", _vp),
         ("implicit_scheme", _i32),
+        ("base", _vp),
     ]
 
 

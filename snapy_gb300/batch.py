@@ -72,6 +72,16 @@ class Batch:
             a.x1f = f.data_ptr() if f is not None else None
             a.x1v = v.data_ptr() if v is not None else None
             a.implicit_scheme = int(d.get("implicit_scheme", 0))
+        # FP32 under gravity: the state is stored as anomalies about an FP64
+        # hydrostatic base per block (filled from the initial state)
+        self.bases = []
+        for b, d in enumerate(blocks):
+            t = None
+            if dtype == torch.float32 and d.get("grav1", 0.0) != 0.0:
+                t = torch.zeros(5 * d["nc1"] + 1, dtype=torch.float64, device=device)
+                arr[b].base = t.data_ptr()
+            self.bases.append(t)
+        self.blocks = [dict(d) for d in blocks]
         self.shapes = [(5, d["nc3"], d["nc2"], d["nc1"]) for d in blocks]
         h = ctypes.c_void_p()
         with torch.cuda.device(device):
@@ -146,9 +156,46 @@ class Batch:
                 raise ValueError("initialize: hydro_w must be contiguous on "
                                  f"{self.device}")
             self._w_ptrs[b] = w.data_ptr()
+            if self.bases[b] is not None:
+                self._set_base(b, w)
         self.set_current(0)
         _lib.check(self.L.sg_init_from_prim(self.h, self._w_ptrs, _stream(stream)),
                    "sg_init_from_prim")
+
+    def _set_base(self, b: int, w: torch.Tensor) -> None:
+        """The FP64 hydrostatic base of an anomaly block from its initial
+        primitives: the horizontal mean of rho and p on each x1 row, e_b =
+        p_b / (gamma - 1), face pressures pf_b (mean of the two cells beside
+        a face, end faces copy the end cells) and the base's residual
+        r_b = rho_b g1 - (pf_b[i + 1] - pf_b[i]) / dx1.  Any base gives the
+        same equations; one near the state keeps the FP32 anomalies small."""
+        d = self.blocks[b]
+        nc1, nc2, nc3, ng = d["nc1"], d["nc2"], d["nc3"], d["ng"]
+        j = slice(ng, nc2 - ng) if nc2 > 1 else slice(0, 1)
+        k = slice(ng, nc3 - ng) if nc3 > 1 else slice(0, 1)
+        rho = w[0, k, j, :].mean(dim=(0, 1))
+        pres = w[4, k, j, :].mean(dim=(0, 1))
+        pf = torch.empty(nc1 + 1, dtype=torch.float64, device=w.device)
+        pf[1:nc1] = 0.5 * (pres[:-1] + pres[1:])
+        pf[0], pf[nc1] = pres[0], pres[-1]
+        r = rho * d["grav1"] - (pf[1:] - pf[:-1]) / d["dx1"]
+        t = self.bases[b]
+        t[0:nc1] = rho
+        t[nc1:2 * nc1] = pres
+        t[2 * nc1:3 * nc1] = pres / (d["gammad"] - 1.0)
+        t[3 * nc1:4 * nc1 + 1] = pf
+        t[4 * nc1 + 1:5 * nc1 + 1] = r
+
+    def totals(self, b: int, u: torch.Tensor) -> torch.Tensor:
+        """The total conserved state (FP64) of block b's stored state u (an
+        anomaly block adds its base)."""
+        out = u.to(torch.float64)
+        t = self.bases[b]
+        if t is not None:
+            nc1 = self.blocks[b]["nc1"]
+            out[0] += t[0:nc1]
+            out[4] += t[2 * nc1:3 * nc1]
+        return out
 
     def prim(self, outs: List[torch.Tensor], stream=None) -> None:
         for b, w in enumerate(outs):

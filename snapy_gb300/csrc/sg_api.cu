@@ -287,11 +287,26 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
       return fail(SG_ERR_ARG, "block %d: gravity and the covariance row need "
                   "the x1 geometry (x1f, x1v)", b);
     }
-    if (d.grav1 != 0. && scheme->dtype != SG_F64) {
+    if (d.grav1 != 0. && scheme->dtype == SG_F32) {
+      // FP32 under gravity stores anomalies about an FP64 hydrostatic base;
+      // the anomaly Riemann solver is LMARS's (its face pressure is affine
+      // in the two sides' pressures)
+      if (!d.base) {
+        delete h;
+        return fail(SG_ERR_ARG, "block %d: FP32 with gravity needs the FP64 "
+                    "hydrostatic base (sg_block_desc.base)", b);
+      }
+      if (scheme->riemann != SG_LMARS) {
+        delete h;
+        return fail(SG_ERR_UNSUPPORTED, "block %d: FP32 with gravity is built "
+                    "for the lmars solver", b);
+      }
+    } else if (d.base) {
       delete h;
-      return fail(SG_ERR_UNSUPPORTED, "block %d: gravity in the FP32 stage "
-                  "kernel", b);
+      return fail(SG_ERR_ARG, "block %d: a hydrostatic base is only used by "
+                  "FP32 blocks with gravity", b);
     }
+    B.base = d.base;
     if (d.grav1 != 0. && (d.bc[0] == SG_BC_PERIODIC || d.bc[1] == SG_BC_PERIODIC)) {
       delete h;
       return fail(SG_ERR_UNSUPPORTED, "block %d: gravity with a periodic x1", b);

@@ -275,6 +275,40 @@ __device__ __forceinline__ void lmars_flux(const T* wl, const T* wr, T gammad,
   }
 }
 
+// LMARS on pressure ANOMALIES: wl[IPR], wr[IPR] are p - pb, with pb the
+// base pressure at the face (the same on both sides).  The totals give the
+// sound speed and the enthalpy; the face pressure is affine in (pl, pr)
+// with weights summing to one, so the momentum flux carries pbar - pb and
+// the base's share (pb itself) is left to the caller's hydrostatic balance.
+// Used by the FP32 state, whose pressure only has the precision of an
+// anomaly.
+template <typename T>
+__device__ __forceinline__ void lmars_flux_anom(const T* wl, const T* wr,
+                                                T gammad, int d, T pb,
+                                                T* flx) {
+  Axes ax = face_axes(d);
+  const int ivx = ax.x, ivy = ax.y, ivz = ax.z;
+  T l0 = wl[IDN], l1 = wl[ivx], l2 = wl[ivy], l3 = wl[ivz], l4 = wl[IPR];
+  T r0 = wr[IDN], r1 = wr[ivx], r2 = wr[ivy], r3 = wr[ivz], r4 = wr[IPR];
+  T pl = pb + l4, pr = pb + r4;
+  T hl = pl / (gammad - T(1)) / l0;
+  T hr = pr / (gammad - T(1)) / r0;
+  hl += T(0.5) * (sqr(l1) + sqr(l2) + sqr(l3)) + pl / l0;
+  hr += T(0.5) * (sqr(r1) + sqr(r2) + sqr(r3)) + pr / r0;
+  T rhobar = T(0.5) * (l0 + r0);
+  T cbar = sqrt(T(0.5) * gammad * (pl + pr) / rhobar);
+  T pbar = T(0.5) * (l4 + r4) + T(0.5) * (rhobar * cbar) * (l1 - r1);
+  T ubar = T(0.5) * (l1 + r1) + T(0.5) / (rhobar * cbar) * (l4 - r4);
+  const T m0 = ubar > T(0) ? l0 : r0;
+  const T v1 = ubar > T(0) ? l1 : r1, v2 = ubar > T(0) ? l2 : r2,
+          v3 = ubar > T(0) ? l3 : r3, h = ubar > T(0) ? hl : hr;
+  flx[IDN] = ubar * m0;
+  flx[ivx] = ubar * m0 * v1 + pbar;
+  flx[ivy] = ubar * m0 * v2;
+  flx[ivz] = ubar * m0 * v3;
+  flx[IPR] = ubar * m0 * h;
+}
+
 // ideal-gas U->W of one cell (Cartesian: the metric raise is the identity)
 template <typename T>
 __device__ __forceinline__ void cons2prim(const T* u, T* w, T gammad) {

@@ -117,8 +117,12 @@ struct TileLayout {
     o += NHYDRO * ntj * (nx1 + 1);
     f2 = o;
     o += has2 ? NHYDRO * (ntj + 1) * nx1 : 0;
-    ref = o;  // psf_lo, psf_hi, pref, dref, dsf_l, dsf_r per tile row
-    o += wb ? 6 * ntj * nc1 : 0;
+    // psf_lo, psf_hi, pref, dref, dsf_l, dsf_r per tile row, FP64 in both
+    // builds (the FP32 build keeps the hydrostatic reference in FP64)
+    constexpr int kDw = (int)(sizeof(double) / sizeof(real));
+    o += (o % kDw) ? kDw - (o % kDw) : 0;
+    ref = o;
+    o += wb ? 6 * ntj * nc1 * kDw : 0;
     cov_arr = o;  // rho, h, un of the x2 face means, x1 rows 0..nc1-1
     o += cov ? 3 * (ntj + 1) * nc1 : 0;
     divv = o;  // div v on tile rows -1..ntj, all x1 cells
@@ -135,13 +139,20 @@ struct TileLayout {
 // :20-272 and src/recon/x1_reference.cpp:183-238): one thread runs the
 // column's serial face-pressure scan, in the reference's order, so the face
 // pressures carry the reference's rounding
+// pressure of cell j of a column in FP64: the stored value, plus the base
+// where the column holds anomalies (pb non-null)
+__device__ __forceinline__ double col_p(const real* pres, const double* pb,
+                                        int j) {
+  return pb ? (double)pres[j] + pb[j] : (double)pres[j];
+}
+
 __device__ __forceinline__ void ref_scan(const real* rho, const real* pres,
-                                         int nc1, int iu, double dx,
-                                         double grav, real* psf_lo,
-                                         real* psf_hi) {
+                                         const double* pb, int nc1, int iu,
+                                         double dx, double grav,
+                                         double* psf_lo, double* psf_hi) {
   const double minp = 2.2250738585072014e-308;
-  double rdt_top = (double)pres[iu] / (double)rho[iu];
-  double top = (double)pres[iu] * sg_exp(-grav * 0.5 * dx / rdt_top);
+  double rdt_top = col_p(pres, pb, iu) / (double)rho[iu];
+  double top = col_p(pres, pb, iu) * sg_exp(-grav * 0.5 * dx / rdt_top);
   double face = top;
   for (int i = iu; i >= 0; --i) {
     double dp = grav * (double)rho[i] * dx;
@@ -168,9 +179,10 @@ __device__ __forceinline__ double wall_rop(double r0, double r1, double k) {
 }
 
 __device__ __forceinline__ double rop_smooth(const real* rho, const real* pres,
-                                             int i, int jlo, int jhi,
-                                             bool ext_lo, bool ext_hi) {
-  auto rop = [&](int j) { return (double)rho[j] / (double)pres[j]; };
+                                             const double* pb, int i, int jlo,
+                                             int jhi, bool ext_lo,
+                                             bool ext_hi) {
+  auto rop = [&](int j) { return (double)rho[j] / col_p(pres, pb, j); };
   if (!(ext_lo && i - 2 < jlo) && !(ext_hi && i + 2 > jhi))
     return rop(i < jlo ? jlo : (i > jhi ? jhi : i));
   double v[5];
@@ -199,11 +211,12 @@ __constant__ double c_w6e[2][6] = {
 
 // hydro_ref_x1_cell_impl (uniform grid) for cell i of one column
 __device__ __forceinline__ void ref_cell(const real* rho, const real* pres,
-                                         const real* psf_lo,
-                                         const real* psf_hi, int i, int nc1,
+                                         const double* pb,
+                                         const double* psf_lo,
+                                         const double* psf_hi, int i, int nc1,
                                          int iu, bool phys_in, bool phys_out,
-                                         bool wall_clamp, real* pref,
-                                         real* dref, real* dsf) {
+                                         bool wall_clamp, double* pref,
+                                         double* dref, double* dsf) {
   const int il = nc1 - 1 - iu;
   bool thin = (iu - il + 1) < 5, fits = iu >= 4;
   bool wall_in = wall_clamp && phys_in && i >= il && i < il + 2;
@@ -234,10 +247,11 @@ __device__ __forceinline__ void ref_cell(const real* rho, const real* pres,
   int jhi = (wall_clamp && phys_out) ? iu : nc1 - 1;
   bool ext_lo = wall_clamp && phys_in && il + 1 <= iu;
   bool ext_hi = wall_clamp && phys_out && iu - 1 >= il;
-  double rs = rop_smooth(rho, pres, i, jlo, jhi, ext_lo, ext_hi);
+  double rs = rop_smooth(rho, pres, pb, i, jlo, jhi, ext_lo, ext_hi);
   double rf = rs;
   if (i > 0)
-    rf = 0.5 * (rop_smooth(rho, pres, i - 1, jlo, jhi, ext_lo, ext_hi) + rs);
+    rf = 0.5 * (rop_smooth(rho, pres, pb, i - 1, jlo, jhi, ext_lo, ext_hi) +
+                rs);
   dref[i] = cell_pref * rs;
   dsf[i] = lo * rf;
 }
@@ -270,6 +284,14 @@ __device__ __forceinline__ void stage_tile(const BlockDev* __restrict__ tab,
   const bool scale = p.scale != 0;
   const int il = ng, iu1 = nc1 - ng;  // interior x1 cells il..iu1-1
   const double dt = p.dt[bi];
+  // FP32 under gravity: the buffers hold anomalies about the FP64 base
+  // (rho_b, 0, 0, 0, e_b)(x1); the tile keeps the total rho and the
+  // pressure anomaly p - p_b, and every Riemann solve works on anomalies
+  const double* base = B.base;
+  const double* rb = base ? base_rho(base, nc1) : nullptr;
+  const double* pbc = base ? base_p(base, nc1) : nullptr;
+  const double* pbf = base ? base_pf(base, nc1) : nullptr;
+  const double* rrb = base ? base_r(base, nc1) : nullptr;
 
   const int wstride = R * nc1;  // one variable of the W tile
   real* W = sm + L.w;
@@ -285,6 +307,9 @@ __device__ __forceinline__ void stage_tile(const BlockDev* __restrict__ tab,
     real uc[NHYDRO], wc[NHYDRO];
 #pragma unroll
     for (int v = 0; v < NHYDRO; ++v) uc[v] = uin[v * plane + row0 + idx];
+    // with a base: rho_b + rho', and p' = (g - 1)(E' - ke) since p_b is
+    // (g - 1) e_b
+    if (rb) uc[IDN] = real(rb[idx % nc1]) + uc[IDN];
     cons2prim<real>(uc, wc, gammad);
 #pragma unroll
     for (int v = 0; v < NHYDRO; ++v) W[v * wstride + idx] = wc[v];
@@ -292,7 +317,7 @@ __device__ __forceinline__ void stage_tile(const BlockDev* __restrict__ tab,
   __syncthreads();
 
   // (2) the well-balanced x1 reference of each tile column
-  real* REF = sm + L.ref;
+  double* REF = reinterpret_cast<double*>(sm + L.ref);
   const int rs_ = ntj * nc1;  // one reference array of the tile
   const bool phys_in = B.bc[0] != kBcNone, phys_out = B.bc[1] != kBcNone;
   const int iu = nc1 - 1 - ng;
@@ -300,15 +325,16 @@ __device__ __forceinline__ void stage_tile(const BlockDev* __restrict__ tab,
     for (int jt = threadIdx.x; jt < ntj; jt += blockDim.x) {
       const real* rho = W + IDN * wstride + (hj + jt) * nc1;
       const real* pres = W + IPR * wstride + (hj + jt) * nc1;
-      ref_scan(rho, pres, nc1, iu, B.dx1, -B.grav1, REF + 0 * rs_ + jt * nc1,
-               REF + 1 * rs_ + jt * nc1);
+      ref_scan(rho, pres, pbc, nc1, iu, B.dx1, -B.grav1,
+               REF + 0 * rs_ + jt * nc1, REF + 1 * rs_ + jt * nc1);
     }
     __syncthreads();
     for (int idx = threadIdx.x; idx < ntj * nc1; idx += blockDim.x) {
       const int jt = idx / nc1, i = idx - jt * nc1;
       const real* rho = W + IDN * wstride + (hj + jt) * nc1;
       const real* pres = W + IPR * wstride + (hj + jt) * nc1;
-      ref_cell(rho, pres, REF + jt * nc1, REF + rs_ + jt * nc1, i, nc1, iu,
+      ref_cell(rho, pres, pbc, REF + jt * nc1, REF + rs_ + jt * nc1, i, nc1,
+               iu,
                phys_in, phys_out, B.wb_wall_clamp != 0,
                REF + 2 * rs_ + jt * nc1, REF + 3 * rs_ + jt * nc1,
                REF + 4 * rs_ + jt * nc1 /* dsf, becomes dsf_l */);
@@ -320,9 +346,9 @@ __device__ __forceinline__ void stage_tile(const BlockDev* __restrict__ tab,
     // IRT side goes to slot 5
     for (int idx = threadIdx.x; idx < ntj * nc1; idx += blockDim.x) {
       const int jt = idx / nc1, f = idx - jt * nc1;
-      const real* dref = REF + 3 * rs_ + jt * nc1;
-      real* DL = REF + 4 * rs_ + jt * nc1;
-      real* DR = REF + 5 * rs_ + jt * nc1;
+      const double* dref = REF + 3 * rs_ + jt * nc1;
+      double* DL = REF + 4 * rs_ + jt * nc1;
+      double* DR = REF + 5 * rs_ + jt * nc1;
       double dsf = DL[f];
       double l = dsf, r = dsf;
       if (nc1 >= 6 && f >= 2 && f <= nc1 - 2) {
@@ -360,15 +386,16 @@ __device__ __forceinline__ void stage_tile(const BlockDev* __restrict__ tab,
     if (!wb) {
       face_states<SHOCK>(q, wstride, 1, scale, wl, wr);
     } else {
-      const real* pref = REF + 2 * rs_ + jt * nc1;
-      const real* dref = REF + 3 * rs_ + jt * nc1;
+      const double* pref = REF + 2 * rs_ + jt * nc1;
+      const double* dref = REF + 3 * rs_ + jt * nc1;
       // the perturbation of p (v = IPR) and rho (v = IDN) at cell c, even-
       // mirrored into the x1 wall ghosts
       auto pert = [&](int v, int c) -> real {
         if (c < il && phys_in) c = 2 * il - 1 - c;
         if (c >= iu1 && phys_out) c = 2 * iu1 - 1 - c;
         const real* col = W + v * wstride + (hj + jt) * nc1;
-        return col[c] - (v == IPR ? pref[c] : dref[c]);
+        if (v == IPR) return real(col_p(col, pbc, c) - pref[c]);
+        return real((double)col[c] - dref[c]);
       };
 #pragma unroll
       for (int v = 0; v < NHYDRO; ++v) {
@@ -388,17 +415,24 @@ __device__ __forceinline__ void stage_tile(const BlockDev* __restrict__ tab,
           wr[v] = cp5_cm(s[1], s[2], s[3], s[4], s[5]);
         }
       }
-      const real psf = REF[0 * rs_ + jt * nc1 + f];
-      real pl = wl[IPR] + psf, pr = wr[IPR] + psf;
-      wl[IPR] = pl > real(0) ? pl : psf;
-      wr[IPR] = pr > real(0) ? pr : psf;
-      real dl = wl[IDN] + REF[4 * rs_ + jt * nc1 + f];
-      real dr = wr[IDN] + REF[5 * rs_ + jt * nc1 + f];
+      // the totals in FP64; the Riemann solve takes the anomaly about the
+      // base face pressure where there is a base
+      const double psf = REF[0 * rs_ + jt * nc1 + f];
+      double pl = (double)wl[IPR] + psf, pr = (double)wr[IPR] + psf;
+      pl = pl > 0. ? pl : psf;
+      pr = pr > 0. ? pr : psf;
+      wl[IPR] = real(pbf ? pl - pbf[f] : pl);
+      wr[IPR] = real(pbf ? pr - pbf[f] : pr);
+      real dl = real((double)wl[IDN] + REF[4 * rs_ + jt * nc1 + f]);
+      real dr = real((double)wr[IDN] + REF[5 * rs_ + jt * nc1 + f]);
       const real* rho = W + IDN * wstride + (hj + jt) * nc1;
       wl[IDN] = dl > real(0) ? dl : rho[f > 0 ? f - 1 : 0];
       wr[IDN] = dr > real(0) ? dr : rho[f];
     }
-    riemann<RK>(wl, wr, gammad, 1, flx);
+    if (pbf)
+      lmars_flux_anom<real>(wl, wr, gammad, 1, real(pbf[f]), flx);
+    else
+      riemann<RK>(wl, wr, gammad, 1, flx);
     if ((fi == 0 && B.bc[0] == kBcReflecting) ||
         (fi == nx1 && B.bc[1] == kBcReflecting))
       flx[IDN] = flx[IPR] = real(0);
@@ -423,13 +457,17 @@ __device__ __forceinline__ void stage_tile(const BlockDev* __restrict__ tab,
 #pragma unroll
         for (int v = 0; v < NHYDRO; ++v) wb_[v] = real(0.5) * (wl[v] + wr[v]);
         real pbar = wb_[IPR];
+        if (pbc) pbar = real(pbc[i]) + pbar;  // the total
         real enth = pbar / (gammad - real(1)) + pbar;
         COV[0 * cstride + jf * nc1 + i] = wb_[IDN];
         COV[1 * cstride + jf * nc1 + i] = enth / wb_[IDN];
         COV[2 * cstride + jf * nc1 + i] = wb_[IVY];
       }
       if (i >= il && i < iu1) {
-        riemann<RK>(wl, wr, gammad, 2, flx);
+        if (pbc)
+          lmars_flux_anom<real>(wl, wr, gammad, 2, real(pbc[i]), flx);
+        else
+          riemann<RK>(wl, wr, gammad, 2, flx);
 #pragma unroll
         for (int v = 0; v < NHYDRO; ++v)
           F2[v * f2stride + jf * nx1 + (i - il)] = flx[v];
@@ -592,7 +630,15 @@ __device__ __forceinline__ void stage_tile(const BlockDev* __restrict__ tab,
     }
     if (wb) {
       const real rho = W[IDN * wstride + wc], vx = W[IVX * wstride + wc];
-      du[IVX] += rdt * rho * g * real(1.);
+      if (rrb) {
+        // the x1 fluxes carried p* - pf_b: the base's face-pressure
+        // difference and weight balance to r_b (FP64), which leaves the
+        // anomaly's weight rho' g
+        const real rho_a = uin[IDN * plane + c];
+        du[IVX] += rdt * rho_a * g + rdt * real(rrb[i]);
+      } else {
+        du[IVX] += rdt * rho * g * real(1.);
+      }
       du[IPR] += rdt * rho * vx * g * real(1.);
     }
     if (visc) {
@@ -738,6 +784,13 @@ __global__ void __launch_bounds__(kThreads)
         val = val * real(-1);
       q[v * plane + c] = val;
     }
+    // anomalies: the total copied from x1 row si to row i changes base
+    if (B.base && si != i) {
+      const double* rb = base_rho(B.base, nc1);
+      const double* eb = base_e(B.base, nc1);
+      q[IDN * plane + c] += real(rb[si] - rb[i]);
+      q[IPR * plane + c] += real(eb[si] - eb[i]);
+    }
   }
 }
 
@@ -754,7 +807,9 @@ __global__ void __launch_bounds__(kThreads)
     real uc[NHYDRO], wc[NHYDRO];
 #pragma unroll
     for (int v = 0; v < NHYDRO; ++v) uc[v] = u[v * plane + c];
+    if (B.base) uc[IDN] = real(base_rho(B.base, B.nc1)[c % B.nc1]) + uc[IDN];
     cons2prim<real>(uc, wc, gammad);
+    if (B.base) wc[IPR] = real(base_p(B.base, B.nc1)[c % B.nc1]) + wc[IPR];
 #pragma unroll
     for (int v = 0; v < NHYDRO; ++v) w[v * plane + c] = wc[v];
   }
@@ -811,6 +866,10 @@ __global__ void __launch_bounds__(kThreads)
       for (int v = 0; v < NHYDRO; ++v) w[v * plane + c] = wc[v];
     }
     prim2cons64(wc, uc, B.gammad);
+    if (B.base) {  // the anomaly about the base, formed in FP64
+      uc[IDN] = uc[IDN] - base_rho(B.base, nc1)[i];
+      uc[IPR] = uc[IPR] - base_e(B.base, nc1)[i];
+    }
 #pragma unroll
     for (int v = 0; v < NHYDRO; ++v) q[v * plane + c] = real(uc[v]);
   }
@@ -855,7 +914,9 @@ __global__ void __launch_bounds__(kThreads)
     real uc[NHYDRO], w[NHYDRO];
 #pragma unroll
     for (int v = 0; v < NHYDRO; ++v) uc[v] = u[v * plane + c];
+    if (B.base) uc[IDN] = real(base_rho(B.base, nc1)[i]) + uc[IDN];
     cons2prim<real>(uc, w, gammad);
+    if (B.base) w[IPR] = real(base_p(B.base, nc1)[i]) + w[IPR];
     const real cs = sqrt(gammad * w[IPR] / w[IDN]);
     // an implicit x1 (scheme bit 0, more than one column) keeps only the
     // advective bound dx1 / (|v1| cfl / advection_cfl) (hydro.cpp:327-340)

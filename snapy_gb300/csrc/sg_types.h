@@ -48,7 +48,21 @@ struct BlockDev {
   // as in vic_scratch()
   int32_t implicit;
   double* vic;
+  // FP32 under gravity: the state buffers hold anomalies u - u_b about an
+  // FP64 hydrostatic base that depends on x1 only, laid out as
+  //   rho_b[nc1] | p_b[nc1] | e_b[nc1] = p_b / (gamma - 1) | pf_b[nc1 + 1]
+  //   (the base pressure at x1 face f, between cells f - 1 and f) |
+  //   r_b[nc1] = rho_b g1 - (pf_b[i + 1] - pf_b[i]) / dx1
+  // (null: the buffers hold totals)
+  const double* base;
 };
+
+// offsets into BlockDev::base
+__host__ __device__ inline const double* base_rho(const double* b, int nc1) { return b; }
+__host__ __device__ inline const double* base_p(const double* b, int nc1) { return b + nc1; }
+__host__ __device__ inline const double* base_e(const double* b, int nc1) { return b + 2 * nc1; }
+__host__ __device__ inline const double* base_pf(const double* b, int nc1) { return b + 3 * nc1; }
+__host__ __device__ inline const double* base_r(const double* b, int nc1) { return b + 4 * nc1 + 1; }
 
 // doubles of VIC scratch per interior cell: du, du0 (5 each), the blocks
 // a, b, c (25 each), the solution and the two Woodbury vectors (5 each)

@@ -133,13 +133,21 @@ __device__ __forceinline__ void vabs_jacobian(double* A, double gm1,
   vmat_mul(RL, Ri, A);
 }
 
-// the primitives of layer i of a column (u of the storage type -> FP64 W)
+// the primitives of a cell (u of the storage type -> FP64 W); an FP32
+// block under gravity stores anomalies, to which the base's FP64 totals
+// are added first (base null: u holds totals)
 __device__ __forceinline__ void vic_prim(const real* u, size_t plane,
                                          size_t cell, double gammad,
-                                         double* w) {
+                                         double* w, const double* base = nullptr,
+                                         int nc1 = 0) {
   double uc[NHYDRO];
 #pragma unroll
   for (int v = 0; v < NHYDRO; ++v) uc[v] = (double)u[v * plane + cell];
+  if (base) {
+    const int i = (int)(cell % nc1);
+    uc[IDN] = base_rho(base, nc1)[i] + uc[IDN];
+    uc[IPR] = base_e(base, nc1)[i] + uc[IPR];
+  }
   cons2prim<double>(uc, w, gammad);
 }
 
@@ -216,9 +224,9 @@ __global__ void __launch_bounds__(kThreads)
     const size_t jrow = B.nc2 > 1 ? col + ng : 0;
     const size_t base = jrow * nc1 + ng;  // padded cell of layer 0
     double wl[5], wr[5], wn[5];
-    vic_prim(uin, plane, base + i - 1, B.gammad, wl);
-    vic_prim(uin, plane, base + i, B.gammad, wr);
-    vic_prim(uin, plane, base + i + 1, B.gammad, wn);
+    vic_prim(uin, plane, base + i - 1, B.gammad, wl, B.base, nc1);
+    vic_prim(uin, plane, base + i, B.gammad, wr, B.base, nc1);
+    vic_prim(uin, plane, base + i + 1, B.gammad, wn, B.base, nc1);
     double Jp[25], Jc[25], Jn[25], Am[25], Ap[25];
     vflux_jacobian(Jp, gm1, wl);
     vflux_jacobian(Jc, gm1, wr);
@@ -679,7 +687,7 @@ __global__ void __launch_bounds__(32 * kVicWarps)
   if (ok) {
     for (int i = lane; i < n; i += 32) {
       double w[5];
-      vic_prim(uin, plane, base + i, B.gammad, w);
+      vic_prim(uin, plane, base + i, B.gammad, w, B.base, nc1);
       rho[i] = w[0];
       mdn[i] = 0.;
       mq[i] = (D[i * 5] - du[i]) * vol;  // staged: phi of layer i

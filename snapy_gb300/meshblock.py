@@ -58,6 +58,10 @@ def scheme_of(options: MeshBlockOptions) -> dict:
             raise DeckError("forcing/const-gravity: grav2/grav3 are not built")
         if h.grav.non_hydrostatic != 1.0:
             raise DeckError("forcing/const-gravity/non-hydrostatic < 1 is not built")
+        if h.grav.grav1 and h.precision == "float32" and h.riemann.type != "lmars":
+            raise DeckError("dynamics/precision float32 under gravity is built "
+                            "for the lmars solver (its state is stored as "
+                            "anomalies about an FP64 hydrostatic base)")
     if h.diffusion is not None:
         extra = set(h.diffusion.raw) - {"nu_iso", "nu-iso"}
         if extra:
@@ -327,7 +331,12 @@ class MeshBlock:
         return out
 
     def total_u(self, vars) -> torch.Tensor:
+        """The conserved totals: a copy of hydro_u, which in FP32 under
+        gravity holds anomalies about the FP64 hydrostatic base, so there
+        the base is added (the result is FP64)."""
         u = vars["hydro_u"] if isinstance(vars, dict) else vars
+        if self.batch.bases[0] is not None:
+            return self.batch.totals(0, u)
         return u.clone()
 
     def part(self, offset=(0, 0, 0), exterior: bool = True, extend_x1: int = 0,
