@@ -52,7 +52,12 @@ WORKLOADS = {
     "straka-explicit": "snapy_gb300/decks/straka_noimplicit.yaml",
     "straka-shape": "snapy_gb300/decks/straka_explicit.yaml",
     "sod": "snapy_gb300/decks/sod.yaml",
+    # 64 Straka-type members of uneven size (nx2 in {128..512}, nx1 in
+    # {32..128}, seeded bubbles) in one handle: one persistent launch per
+    # kernel and stage, each member's dt on the device, one graph per step
+    "ensemble": "snapy_gb300/decks/straka.yaml",
 }
+ENSEMBLE_MEMBERS, ENSEMBLE_SEED = 64, 20261203
 
 
 def parse():
@@ -378,8 +383,245 @@ def run_native(args):
     return 0
 
 
+def ensemble_cpu_baseline(members, seconds):
+    """The CPU oracle (FP64, OpenMP on every host core) on the first members
+    of the ensemble, as many RK3 steps as fit in `seconds`."""
+    from oracle import oracle as O
+    O.build()
+    cores = os.cpu_count() or 1
+    blocks = []
+    for opts, w in members[:4]:
+        ob = O.block_from_options(opts, nthreads=cores)
+        u = ob.initialize(w.numpy())
+        blocks.append((opts, ob, u))
+    n, cells, t0 = 0, 0, time.perf_counter()
+    while True:
+        for opts, ob, u in blocks:
+            dt = opts.intg().cfl * ob.max_dt(u)
+            ob.step(u, dt)
+            c = opts.coord()
+            cells += c.nx1 * c.nx2
+        n += 1
+        el = time.perf_counter() - t0
+        if (el >= seconds and n >= 1) or n >= 10000:
+            break
+    return {"value": cells / el, "unit": "cell-updates/s", "cores": cores,
+            "kind": "port",
+            "sample": f"{n} RK3 steps of ensemble members 0-3 (their own CFL dt), "
+                      f"FP64, {el:.1f} s, OpenMP {cores} threads"}
+
+
+def ensemble_config(members, precision, nranks):
+    cells = sum(o.coord().nx1 * o.coord().nx2 for o, _ in members)
+    return {"workload": f"ensemble of {len(members)} Straka-type members "
+                        f"(nx2 in 128..512, nx1 in 32..128, 50 m, seed "
+                        f"{ENSEMBLE_SEED}), lmars+weno5+rk3+VIC, {precision} "
+                        "bulk, FP64 implicit solve",
+            "members": len(members), "cells": cells, "precision": precision,
+            "gravity": True, "implicit": True,
+            "dt": "each member's own CFL step, on the device, every step",
+            "l2": "inputs larger than L2 (no flush needed)",
+            "graphs": "one whole-step graph per buffer rotation, captured "
+                      "before the warm-up steps",
+            "replicas": nranks,
+            "parallelism": "replicas" if nranks > 1 else "single"}
+
+
+def run_ensemble(args):
+    """The batched form: every member in one handle.  Beside it, the plain
+    FP64 GPU path on the same members: each its own FP64 MeshBlock, stepped
+    one after another with its own CFL dt (graphs on)."""
+    import torch
+    import torch.distributed as dist
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl", init_method="env://")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    import snapy_gb300 as sg
+    from snapy_gb300 import problems
+    from snapy_gb300.ensemble import Ensemble
+    precision = args.precision or "float32"
+    members = problems.ensemble_members(ENSEMBLE_MEMBERS, ENSEMBLE_SEED,
+                                        precision=precision)
+    cells = sum(o.coord().nx1 * o.coord().nx2 for o, _ in members)
+    ens = Ensemble([o for o, _ in members], device=dev)
+    ens.initialize([w for _, w in members])
+    for _ in range(8):  # the two steady rotations' graphs
+        if ens.captures >= 2:
+            break
+        ens.step()
+    for _ in range(max(3, args.warmup)):
+        ens.step()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            ev[k][0].record(stream)
+            ens.step()
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    t_total = sum(step_ms) / 1e3
+    if world > 1:
+        t = torch.tensor([t_total], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_total = float(t.item())
+    value = cells * args.steps * world / t_total
+    flags = ens.check()
+    assert int(flags.abs().sum()) == 0, f"ensemble retry flags {flags.tolist()}"
+
+    # per-kernel device time of eager stages (graph replays record none)
+    b = ens.batch
+    b.set_timing(True)
+    for _ in range(3):
+        b.max_dt()
+        for st in range(3):
+            b.stage(st)
+    torch.cuda.synchronize()
+    kt = b.kernel_times()
+    b.set_timing(False)
+    s_bytes = 4 if precision == "float32" else 8
+    per_launch = {
+        "stage_kernel": (5 * s_bytes + 40) * cells,
+        "vic_assemble_kernel": (5 * s_bytes + 40 + 40 + 600) * cells,
+        "vic_solve_kernel": (600 + 40 + 200 + 120 + 200 + 120 + 120) * cells,
+        "vic_finish_kernel": (120 + 15 * s_bytes) * cells,
+        "ghost_kernel": 0,
+    }
+    dom = max(kt, key=lambda k: kt[k][0])
+    dom_ms, dom_n = kt[dom]
+    achieved = per_launch[dom] * dom_n / (dom_ms / 1e3) / 1e9
+    peak, peak_kind = peaks()
+    kernels = {k: {"launches": n, "mean_us": ms / n * 1e3,
+                   "share": ms / sum(v[0] for v in kt.values())}
+               for k, (ms, n) in kt.items()}
+
+    # end to end with host buffers: every member's state in and out
+    host = [torch.empty_like(ens.state(k), device="cpu").pin_memory()
+            for k in range(len(members))]
+    for k in range(len(members)):
+        host[k].copy_(ens.state(k))
+    nbytes = sum(h.numel() * h.element_size() for h in host)
+    e2e_steps = max(3, min(args.steps, 20))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for k in range(len(members)):
+            ens.state(k).copy_(host[k], non_blocking=True)
+        ens.step()
+        for k in range(len(members)):
+            host[k].copy_(ens.state(k), non_blocking=True)
+    torch.cuda.synchronize()
+    e2e_t = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_t], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_t = float(t.item())
+    del ens
+
+    # the plain FP64 GPU path on the same members
+    plain_steps = max(2, min(args.steps, 5))
+    blocks = []
+    for opts, w in members:
+        o64 = sg.MeshBlockOptions.from_yaml(os.path.join(ROOT, WORKLOADS["ensemble"]))
+        c, c0 = o64.coord(), opts.coord()
+        c.nx1, c.nx2, c.x1max, c.x2max = c0.nx1, c0.nx2, c0.x1max, c0.x2max
+        o64.hydro().precision = "float64"
+        blk = sg.MeshBlock(o64).to(dev)
+        vars = {"hydro_w": w.to(dev)}
+        blk.initialize(vars)
+        blocks.append((blk, vars))
+    for _ in range(6):  # eager steps and both graphs of every block
+        for blk, vars in blocks:
+            blk.step(vars, blk.max_time_step(vars))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(plain_steps):
+        for blk, vars in blocks:
+            blk.step(vars, blk.max_time_step(vars))
+    torch.cuda.synchronize()
+    plain = cells * plain_steps / (time.perf_counter() - t0)
+    del blocks
+
+    if rank == 0:
+        cb = None if args.no_cpu_baseline else ensemble_cpu_baseline(members, args.cpu_seconds)
+        line = {
+            "metric": "cell-updates/s per RK3 step",
+            "value": value, "unit": "cell-updates/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t_total / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32" if precision == "float32" else "f64",
+            "data": "synthetic (seeded Straka-type members)",
+            "config": ensemble_config(members, precision, world),
+            "e2e": {"value": cells * e2e_steps * world / e2e_t,
+                    "unit": "cell-updates/s", "h2d_bytes_per_step": nbytes,
+                    "d2h_bytes_per_step": nbytes},
+            "plain_fp64": {"value": plain, "unit": "cell-updates/s",
+                           "how": "each member its own FP64 MeshBlock, one "
+                                  "after another, own CFL dt (host read), "
+                                  "step graphs on", "steps": plain_steps},
+            "vs_plain_fp64": value / plain,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak,
+                         "peak_kind": peak_kind, "traffic": None,
+                         "kernel": dom, "bytes_per_launch": per_launch[dom],
+                         "mean_launch_us": dom_ms / dom_n * 1e3,
+                         "limiter": "FP64 issue rate (one FP64 warp "
+                                    "instruction per SM sub-partition per 64 "
+                                    "cycles)"},
+            "kernels": kernels,
+            "cpu_baseline": cb,
+            "clocks": clk.summary(),
+            "gpu_launches": args.steps * (2 + 3 * b.launches_per_stage()),
+            "step_ms_median": statistics.median(step_ms),
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def run_reference_ensemble(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    from snapy_gb300 import problems
+    precision = args.precision or "float32"
+    members = problems.ensemble_members(ENSEMBLE_MEMBERS, ENSEMBLE_SEED,
+                                        precision=precision)
+    cb = ensemble_cpu_baseline(members, max(2.0, args.cpu_seconds))
+    val = cb["value"]
+    cells = sum(o.coord().nx1 * o.coord().nx2 for o, _ in members)
+    print(json.dumps({
+        "impl": "reference", "metric": "cell-updates/s per RK3 step",
+        "value": val, "unit": "cell-updates/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": cells / val * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded Straka-type members)",
+        "config": ensemble_config(members, precision, 1),
+        "cpu_baseline": cb,
+        "e2e": {"value": val, "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0}}), flush=True)
+    return 0
+
+
 def main():
     args = parse()
+    if args.workload == "ensemble":
+        if args.impl == "reference":
+            return run_reference_ensemble(args)
+        return run_ensemble(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_native(args)

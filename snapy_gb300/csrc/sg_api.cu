@@ -97,6 +97,45 @@ __global__ void finish_check_kernel(int nblock, unsigned long long* red,
   nan[b] = 0;
 }
 
+// the x1 geometry constants of the gravity-work correction for interior
+// cell k of a block (BlockDev::x1tab); the stage kernel formerly evaluated
+// these per cell and launch, with the same operations
+__global__ void x1tab_kernel(const double* x1f, const double* x1v, int ng,
+                             int nx1, double grav1, double* tab) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nx1) return;
+  const int i = ng + k;
+  const double* x = x1v + ng;
+  double w0 = 0., w1 = 0., w2 = 0., gvar = 0.;
+  if (nx1 >= 3) {
+    if (k == 0) {
+      double a = x[1] - x[0], b2 = x[2] - x[1];
+      w0 = -(2. * a + b2) / (a * (a + b2));
+      w1 = (a + b2) / (a * b2);
+      w2 = -(a / ((a + b2) * b2));
+    } else if (k == nx1 - 1) {
+      double c = x[nx1 - 2] - x[nx1 - 3], d = x[nx1 - 1] - x[nx1 - 2];
+      w0 = d / (c * (c + d));
+      w1 = -((c + d) / (c * d));
+      w2 = (c + 2. * d) / ((c + d) * d);
+    } else {
+      double hm = x[k] - x[k - 1], hp = x[k + 1] - x[k];
+      w0 = -hp / (hm * (hm + hp));
+      w1 = (hp - hm) / (hm * hp);
+      w2 = hm / (hp * (hm + hp));
+    }
+    double h = x1f[i + 1] - x1f[i];
+    gvar = grav1 * (h * h / 12.);
+  }
+  double* t = tab + 6 * k;
+  t[0] = w0;
+  t[1] = w1;
+  t[2] = w2;
+  t[3] = gvar;
+  t[4] = grav1 * (x1f[i + 1] - x1v[i]);
+  t[5] = grav1 * (x1f[i] - x1v[i]);
+}
+
 __global__ void init_red_kernel(int n, unsigned long long* red, int* nan) {
   int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= n) return;
@@ -121,6 +160,7 @@ struct sg_handle {
   int32_t max_nc1 = 0;
   int32_t launches = 0;
   int* status = nullptr;  // per-block solve status bits (VIC failures)
+  std::vector<double*> x1tabs;  // per-block geometry tables (gravity)
   bool implicit = false;
   size_t max_icells = 0, max_icols = 0;
   std::vector<size_t> scratch_bytes;
@@ -220,24 +260,24 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
   for (int b = 0; b < nblock; ++b) {
     const sg_block_desc& d = blocks[b];
     if (d.ng != 3) {
-      delete h;
+      sg_destroy(h);
       return fail(SG_ERR_UNSUPPORTED, "block %d: nghost %d (3 is built)", b,
                   d.ng);
     }
     if (d.nc1 < 2 * d.ng + 1 || d.nc2 < 1 || d.nc3 < 1 ||
         (d.nc2 > 1 && d.nc2 < 2 * d.ng + 1)) {
-      delete h;
+      sg_destroy(h);
       return fail(SG_ERR_ARG, "block %d: sizes (%d, %d, %d)", b, d.nc3, d.nc2,
                   d.nc1);
     }
     if (d.nc3 > 1) {
-      delete h;
+      sg_destroy(h);
       return fail(SG_ERR_UNSUPPORTED, "block %d: 3-D blocks (nc3 = %d)", b,
                   d.nc3);
     }
     for (int f = 0; f < 6; ++f)
       if (d.bc[f] < SG_BC_NONE || d.bc[f] > SG_BC_EXTRAPOLATION) {
-        delete h;
+        sg_destroy(h);
         return fail(SG_ERR_ARG, "block %d: boundary kind %d", b, d.bc[f]);
       }
     BlockDev& B = h->host[b];
@@ -257,13 +297,13 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
     B.vic = nullptr;
     if (d.implicit_scheme != 0) {
       if (d.implicit_scheme != 9) {
-        delete h;
+        sg_destroy(h);
         return fail(SG_ERR_UNSUPPORTED, "block %d: implicit-scheme %d (the "
                     "full 5x5 scheme 9 is built)", b, d.implicit_scheme);
       }
       if (d.grav1 == 0. || d.bc[0] != SG_BC_REFLECTING ||
           d.bc[1] != SG_BC_REFLECTING || d.nc1 - 2 * d.ng < 3) {
-        delete h;
+        sg_destroy(h);
         return fail(SG_ERR_UNSUPPORTED, "block %d: the vertical implicit solve "
                     "needs const-gravity, reflecting x1 walls and nx1 >= 3", b);
       }
@@ -283,7 +323,7 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
       B.dt_src = dxm * dxm / (2. * ndim * d.nu_iso);
     }
     if ((d.grav1 != 0. || (d.flux_cov && d.nc2 > 1)) && (!d.x1f || !d.x1v)) {
-      delete h;
+      sg_destroy(h);
       return fail(SG_ERR_ARG, "block %d: gravity and the covariance row need "
                   "the x1 geometry (x1f, x1v)", b);
     }
@@ -292,23 +332,42 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
       // the anomaly Riemann solver is LMARS's (its face pressure is affine
       // in the two sides' pressures)
       if (!d.base) {
-        delete h;
+        sg_destroy(h);
         return fail(SG_ERR_ARG, "block %d: FP32 with gravity needs the FP64 "
                     "hydrostatic base (sg_block_desc.base)", b);
       }
       if (scheme->riemann != SG_LMARS) {
-        delete h;
+        sg_destroy(h);
         return fail(SG_ERR_UNSUPPORTED, "block %d: FP32 with gravity is built "
                     "for the lmars solver", b);
       }
     } else if (d.base) {
-      delete h;
+      sg_destroy(h);
       return fail(SG_ERR_ARG, "block %d: a hydrostatic base is only used by "
                   "FP32 blocks with gravity", b);
     }
     B.base = d.base;
+    B.x1tab = nullptr;
+    if (d.grav1 != 0.) {
+      const int nx1 = d.nc1 - 2 * d.ng;
+      double* t = nullptr;
+      cudaError_t e = cudaMalloc(&t, sizeof(double) * 6 * (size_t)nx1);
+      if (e == cudaSuccess) {
+        h->x1tabs.push_back(t);
+        x1tab_kernel<<<(nx1 + 127) / 128, 128>>>(d.x1f, d.x1v, d.ng, nx1,
+                                                 d.grav1, t);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+      }
+      if (e != cudaSuccess) {
+        int rc = cuda_fail(e, "sg_create: x1 geometry table");
+        sg_destroy(h);
+        return rc;
+      }
+      B.x1tab = t;
+    }
     if (d.grav1 != 0. && (d.bc[0] == SG_BC_PERIODIC || d.bc[1] == SG_BC_PERIODIC)) {
-      delete h;
+      sg_destroy(h);
       return fail(SG_ERR_UNSUPPORTED, "block %d: gravity with a periodic x1", b);
     }
     B.tj = d.tj > 0 ? d.tj : choose_tj(h, d, nblock);
@@ -318,7 +377,7 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
     tile += B.ntile;
     size_t sm = stage_smem(h, d, B.tj);
     if ((long)sm > optin) {
-      delete h;
+      sg_destroy(h);
       return fail(SG_ERR_UNSUPPORTED,
                   "block %d: a tile needs %zu B of shared memory (limit %d)",
                   b, sm, optin);
@@ -371,6 +430,7 @@ int sg_destroy(sg_handle* h) {
   if (h->status) cudaFree(h->status);
   if (h->ptrs_host) cudaFreeHost(h->ptrs_host);
   for (cudaEvent_t e : h->events) cudaEventDestroy(e);
+  for (double* t : h->x1tabs) cudaFree(t);
   delete h;
   return 0;
 }

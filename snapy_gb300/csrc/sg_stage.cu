@@ -101,7 +101,7 @@ __device__ __forceinline__ void riemann(const real* wl, const real* wr,
 struct TileLayout {
   int R, ntj, nc1, nx1;
   bool has2, wb, cov, visc;
-  int w, f1, f2, ref, cov_arr, divv, vf1, vf2;  // offsets
+  int w, f1, f2, ref, pert, cov_arr, divv, vf1, vf2;  // offsets
   int total;
   __host__ __device__ TileLayout(int ntj_, int nc1_, int ng, bool has2_,
                                  bool wb_, bool cov_, bool visc_)
@@ -117,12 +117,14 @@ struct TileLayout {
     o += NHYDRO * ntj * (nx1 + 1);
     f2 = o;
     o += has2 ? NHYDRO * (ntj + 1) * nx1 : 0;
-    // psf_lo, psf_hi, pref, dref, dsf_l, dsf_r per tile row, FP64 in both
-    // builds (the FP32 build keeps the hydrostatic reference in FP64)
+    // psf_lo, psf_hi, pref, dref, dsf_l, dsf_r, rho/p per tile row, FP64 in
+    // both builds (the FP32 build keeps the hydrostatic reference in FP64)
     constexpr int kDw = (int)(sizeof(double) / sizeof(real));
     o += (o % kDw) ? kDw - (o % kDw) : 0;
     ref = o;
-    o += wb ? 6 * ntj * nc1 * kDw : 0;
+    o += wb ? 7 * ntj * nc1 * kDw : 0;
+    pert = o;  // the reconstructed perturbations of p and rho per cell
+    o += wb ? 2 * ntj * nc1 : 0;
     cov_arr = o;  // rho, h, un of the x2 face means, x1 rows 0..nc1-1
     o += cov ? 3 * (ntj + 1) * nc1 : 0;
     divv = o;  // div v on tile rows -1..ntj, all x1 cells
@@ -171,6 +173,62 @@ __device__ __forceinline__ void ref_scan(const real* rho, const real* pres,
   }
 }
 
+// the same face pressures with the sums taken by a warp (all 32 lanes call
+// it for one column): below the top cell psf_lo[i] = top + sum_{k=i..iu} dp_k
+// and psf_hi[i] = top + sum_{k=i+1..iu} dp_k; above it psf_lo[i] = top -
+// sum_{k=iu+1..i-1} dp_k and psf_hi[i] = top - sum_{k=iu+1..i} dp_k, with
+// dp_k = grav rho_k dx.  The sums are warp prefix sums in chunks of 32, so
+// their rounding differs from the serial scan's (used by the FP32 build).
+__device__ __forceinline__ void ref_scan_warp(const real* rho, const real* pres,
+                                              const double* pb, int nc1,
+                                              int iu, double dx, double grav,
+                                              double* psf_lo, double* psf_hi) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const double minp = 2.2250738585072014e-308;
+  const double ptop = col_p(pres, pb, iu);
+  const double rdt_top = ptop / (double)rho[iu];
+  const double top = ptop * sg_exp(-grav * 0.5 * dx / rdt_top);
+  double carry = 0.;
+  for (int c0 = iu; c0 >= 0; c0 -= 32) {
+    const int i = c0 - lane;
+    double v = i >= 0 ? grav * (double)rho[i] * dx : 0.;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      double t = __shfl_up_sync(full, v, d);
+      if (lane >= d) v += t;
+    }
+    const double S = carry + v;  // sum over cells i..iu
+    double above = __shfl_up_sync(full, S, 1);
+    if (lane == 0) above = carry;
+    if (i >= 0) {
+      double lo = top + S, hi = top + above;
+      psf_lo[i] = lo > minp ? lo : minp;
+      psf_hi[i] = hi > minp ? hi : minp;
+    }
+    carry = __shfl_sync(full, S, 31);
+  }
+  carry = 0.;
+  for (int c0 = iu + 1; c0 < nc1; c0 += 32) {
+    const int i = c0 + lane;
+    double v = i < nc1 ? grav * (double)rho[i] * dx : 0.;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      double t = __shfl_up_sync(full, v, d);
+      if (lane >= d) v += t;
+    }
+    const double S = carry + v;  // sum over cells iu+1..i
+    double below = __shfl_up_sync(full, S, 1);
+    if (lane == 0) below = carry;
+    if (i < nc1) {
+      double lo = top - below, hi = top - S;
+      psf_lo[i] = lo > minp ? lo : minp;
+      psf_hi[i] = hi > minp ? hi : minp;
+    }
+    carry = __shfl_sync(full, S, 31);
+  }
+}
+
 __device__ __forceinline__ double wall_rop(double r0, double r1, double k) {
   double q = r0 / r1, qk = k == floor(k) ? q : pow(q, k);
   for (int n = 1; k == floor(k) && n < k; ++n) qk *= q;
@@ -178,11 +236,10 @@ __device__ __forceinline__ double wall_rop(double r0, double r1, double k) {
   return e > 0. ? e : r0;
 }
 
-__device__ __forceinline__ double rop_smooth(const real* rho, const real* pres,
-                                             const double* pb, int i, int jlo,
-                                             int jhi, bool ext_lo,
+__device__ __forceinline__ double rop_smooth(const double* ropc, int i,
+                                             int jlo, int jhi, bool ext_lo,
                                              bool ext_hi) {
-  auto rop = [&](int j) { return (double)rho[j] / col_p(pres, pb, j); };
+  auto rop = [&](int j) { return ropc[j]; };
   if (!(ext_lo && i - 2 < jlo) && !(ext_hi && i + 2 > jhi))
     return rop(i < jlo ? jlo : (i > jhi ? jhi : i));
   double v[5];
@@ -210,8 +267,7 @@ __constant__ double c_w6e[2][6] = {
      -11. / 1440.}};
 
 // hydro_ref_x1_cell_impl (uniform grid) for cell i of one column
-__device__ __forceinline__ void ref_cell(const real* rho, const real* pres,
-                                         const double* pb,
+__device__ __forceinline__ void ref_cell(const double* ropc,
                                          const double* psf_lo,
                                          const double* psf_hi, int i, int nc1,
                                          int iu, bool phys_in, bool phys_out,
@@ -247,11 +303,9 @@ __device__ __forceinline__ void ref_cell(const real* rho, const real* pres,
   int jhi = (wall_clamp && phys_out) ? iu : nc1 - 1;
   bool ext_lo = wall_clamp && phys_in && il + 1 <= iu;
   bool ext_hi = wall_clamp && phys_out && iu - 1 >= il;
-  double rs = rop_smooth(rho, pres, pb, i, jlo, jhi, ext_lo, ext_hi);
+  double rs = rop_smooth(ropc, i, jlo, jhi, ext_lo, ext_hi);
   double rf = rs;
-  if (i > 0)
-    rf = 0.5 * (rop_smooth(rho, pres, pb, i - 1, jlo, jhi, ext_lo, ext_hi) +
-                rs);
+  if (i > 0) rf = 0.5 * (rop_smooth(ropc, i - 1, jlo, jhi, ext_lo, ext_hi) + rs);
   dref[i] = cell_pref * rs;
   dsf[i] = lo * rf;
 }
@@ -321,21 +375,39 @@ __device__ __forceinline__ void stage_tile(const BlockDev* __restrict__ tab,
   const int rs_ = ntj * nc1;  // one reference array of the tile
   const bool phys_in = B.bc[0] != kBcNone, phys_out = B.bc[1] != kBcNone;
   const int iu = nc1 - 1 - ng;
+  real* PP = sm + L.pert;  // p - pref of each tile cell
+  real* PD = PP + rs_;     // rho - dref
   if (wb) {
+#ifdef SG_REAL_IS_FLOAT
+    // one warp per column: the face-pressure scan as a warp prefix sum (the
+    // FP32 build is checked against the FP64 oracle at 1e-5; the FP64 build
+    // keeps the reference's serial order below)
+    for (int jt = threadIdx.x >> 5; jt < ntj; jt += blockDim.x >> 5) {
+      const real* rho = W + IDN * wstride + (hj + jt) * nc1;
+      const real* pres = W + IPR * wstride + (hj + jt) * nc1;
+      ref_scan_warp(rho, pres, pbc, nc1, iu, B.dx1, -B.grav1,
+                    REF + 0 * rs_ + jt * nc1, REF + 1 * rs_ + jt * nc1);
+    }
+#else
     for (int jt = threadIdx.x; jt < ntj; jt += blockDim.x) {
       const real* rho = W + IDN * wstride + (hj + jt) * nc1;
       const real* pres = W + IPR * wstride + (hj + jt) * nc1;
       ref_scan(rho, pres, pbc, nc1, iu, B.dx1, -B.grav1,
                REF + 0 * rs_ + jt * nc1, REF + 1 * rs_ + jt * nc1);
     }
-    __syncthreads();
+#endif
+    // rho / p of every cell once (rop_smooth reads up to five per cell)
     for (int idx = threadIdx.x; idx < ntj * nc1; idx += blockDim.x) {
       const int jt = idx / nc1, i = idx - jt * nc1;
       const real* rho = W + IDN * wstride + (hj + jt) * nc1;
       const real* pres = W + IPR * wstride + (hj + jt) * nc1;
-      ref_cell(rho, pres, pbc, REF + jt * nc1, REF + rs_ + jt * nc1, i, nc1,
-               iu,
-               phys_in, phys_out, B.wb_wall_clamp != 0,
+      REF[6 * rs_ + idx] = (double)rho[i] / col_p(pres, pbc, i);
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < ntj * nc1; idx += blockDim.x) {
+      const int jt = idx / nc1, i = idx - jt * nc1;
+      ref_cell(REF + 6 * rs_ + jt * nc1, REF + jt * nc1, REF + rs_ + jt * nc1,
+               i, nc1, iu, phys_in, phys_out, B.wb_wall_clamp != 0,
                REF + 2 * rs_ + jt * nc1, REF + 3 * rs_ + jt * nc1,
                REF + 4 * rs_ + jt * nc1 /* dsf, becomes dsf_l */);
     }
@@ -372,6 +444,11 @@ __device__ __forceinline__ void stage_tile(const BlockDev* __restrict__ tab,
       }
       DL[f] = l;
       DR[f] = r;
+      // the perturbations the x1 reconstruction reads, once per cell
+      const real* rho = W + IDN * wstride + (hj + jt) * nc1;
+      const real* pres = W + IPR * wstride + (hj + jt) * nc1;
+      PP[idx] = real(col_p(pres, pbc, f) - REF[2 * rs_ + idx]);
+      PD[idx] = real((double)rho[f] - REF[3 * rs_ + idx]);
     }
     __syncthreads();
   }
@@ -386,16 +463,12 @@ __device__ __forceinline__ void stage_tile(const BlockDev* __restrict__ tab,
     if (!wb) {
       face_states<SHOCK>(q, wstride, 1, scale, wl, wr);
     } else {
-      const double* pref = REF + 2 * rs_ + jt * nc1;
-      const double* dref = REF + 3 * rs_ + jt * nc1;
       // the perturbation of p (v = IPR) and rho (v = IDN) at cell c, even-
       // mirrored into the x1 wall ghosts
       auto pert = [&](int v, int c) -> real {
         if (c < il && phys_in) c = 2 * il - 1 - c;
         if (c >= iu1 && phys_out) c = 2 * iu1 - 1 - c;
-        const real* col = W + v * wstride + (hj + jt) * nc1;
-        if (v == IPR) return real(col_p(col, pbc, c) - pref[c]);
-        return real((double)col[c] - dref[c]);
+        return (v == IPR ? PP : PD)[jt * nc1 + c];
       };
 #pragma unroll
       for (int v = 0; v < NHYDRO; ++v) {
@@ -656,42 +729,26 @@ __device__ __forceinline__ void stage_tile(const BlockDev* __restrict__ tab,
     }
     if (wb) {
       // face-form work + corrected potential-energy work - the cell work
-      const double* x1f = B.x1f;
-      const double* x = B.x1v + il;
       const int k = ii;
       const real* fm = F1 + IDN * f1stride + jt * nf1;  // fm[k] = face il+k
       auto drho = [&](int kk) -> real {
         real vmd = (a1 * fm[kk + 1] - a1 * fm[kk]) / vol;
         return mdt * vmd;
       };
-      real hi = real(B.grav1 * (x1f[i + 1] - B.x1v[i]));
-      real lo = real(B.grav1 * (x1f[i] - B.x1v[i]));
+      // the x1 geometry's constants of interior cell k (slope weights w0,
+      // w1, w2 of the corrected PE, g h^2 / 12, g dz above and below the
+      // centre), precomputed per block in FP64
+      const double* xt = B.x1tab + 6 * k;
+      real hi = real(xt[4]);
+      real lo = real(xt[5]);
       real fgw = rdt * ((hi * (a1 * fm[k + 1]) - lo * (a1 * fm[k])) / vol);
       if (nx1 >= 3) {
-        double w0_, w1_, w2_;
-        if (k == 0) {
-          double a = x[1] - x[0], b2 = x[2] - x[1];
-          w0_ = -(2. * a + b2) / (a * (a + b2));
-          w1_ = (a + b2) / (a * b2);
-          w2_ = -(a / ((a + b2) * b2));
-        } else if (k == nx1 - 1) {
-          double c = x[nx1 - 2] - x[nx1 - 3], d = x[nx1 - 1] - x[nx1 - 2];
-          w0_ = d / (c * (c + d));
-          w1_ = -((c + d) / (c * d));
-          w2_ = (c + 2. * d) / ((c + d) * d);
-        } else {
-          double hm = x[k] - x[k - 1], hp = x[k + 1] - x[k];
-          w0_ = -hp / (hm * (hm + hp));
-          w1_ = (hp - hm) / (hm * hp);
-          w2_ = hm / (hp * (hm + hp));
-        }
         int kc = k < 1 ? 1 : (k > nx1 - 2 ? nx1 - 2 : k);
         int k0 = kc - 1;
-        double h = x1f[i + 1] - x1f[i];
-        real gvar = real(B.grav1 * (h * h / 12.));
-        real sl = real(w0_) * drho(k0);
-        sl += real(w1_) * drho(k0 + 1);
-        sl += real(w2_) * drho(k0 + 2);
+        real gvar = real(xt[3]);
+        real sl = real(xt[0]) * drho(k0);
+        sl += real(xt[1]) * drho(k0 + 1);
+        sl += real(xt[2]) * drho(k0 + 2);
         fgw += gvar * sl;
       }
       const real rho = W[IDN * wstride + wc], vx = W[IVX * wstride + wc];

@@ -55,6 +55,10 @@ struct BlockDev {
   //   r_b[nc1] = rho_b g1 - (pf_b[i + 1] - pf_b[i]) / dx1
   // (null: the buffers hold totals)
   const double* base;
+  // with gravity: per interior x1 cell k, 6 FP64 constants of the geometry
+  // (the corrected-PE slope weights w0, w1, w2, grav1 h^2 / 12, and
+  // grav1 (x1f[i+1] - x1v[i]), grav1 (x1f[i] - x1v[i]) for i = ng + k)
+  const double* x1tab;
 };
 
 // offsets into BlockDev::base
