@@ -160,7 +160,8 @@ enum {
   SG_KERNEL_VIC_SOLVE = 2,    /* implicit solve: block-Thomas sweep */
   SG_KERNEL_VIC_FINISH = 3,   /* implicit solve: redistribution, update */
   SG_KERNEL_GHOST = 4,        /* ghost fill of the new state */
-  SG_NKERNEL = 5
+  SG_KERNEL_X3 = 5,           /* x3 faces of 3-D blocks */
+  SG_NKERNEL = 6
 };
 int sg_set_timing(sg_handle* h, int32_t on);
 int sg_kernel_times(sg_handle* h, double* ms, int64_t* launches);

@@ -682,14 +682,15 @@ static void riemann_face(const og_block* b, const double* wl, const double* wr,
 
 #define CELL(v, j, i) ((size_t)(v) * nc + (size_t)(j) * n1 + (size_t)(i))
 
-void og_tendency(const og_block* b, const double* w, double dt, double* du) {
-  build_tables();
+/* the tendency of one x2-x1 plane (the whole block when it is 2-D): w and
+ * du point at the plane's first cell, variables `ncell(b)` apart; f3 (3-D
+ * only) at the plane's x3 face fluxes, the next plane's face n1 n2 further,
+ * added to the divergence after x1 and x2 as CoordinateImpl::divergence does
+ * (src/coord/coordinate.cpp:618-662) */
+static void tendency_plane(const og_block* b, const double* w, double dt,
+                           double* du, const double* f3) {
   const int n1 = b->nc1, n2 = b->nc2, ng = b->ng;
   const size_t nc = ncell(b);
-  if (b->nc3 > 1) { /* the 3-D path is not restated */
-    memset(du, 0, sizeof(double) * 5 * nc);
-    return;
-  }
   const int has2 = n2 > 1;
   const int il = ng, iu1 = n1 - ng; /* interior x1 cells il..iu1-1 */
   const int jl = has2 ? ng : 0, ju1 = has2 ? n2 - ng : 1;
@@ -888,8 +889,11 @@ void og_tendency(const og_block* b, const double* w, double dt, double* du) {
 
   /* (5-6) divergence and du = -dt div on the interior */
   const double a1 = b->dx3 * b->dx2, a2 = b->dx3 * b->dx1;
+  const double a3 = b->dx2 * b->dx1;
   const double vol = b->dx3 * (b->dx2 * b->dx1);
-  memset(du, 0, sizeof(double) * 5 * nc);
+  const size_t plane = (size_t)n1 * n2;
+  for (int v = 0; v < 5; ++v)
+    for (size_t q = 0; q < plane; ++q) du[v * nc + q] = 0.;
   const double mdt = -dt;
   for (int v = 0; v < 5; ++v)
     for (int j = jl; j < ju1; ++j)
@@ -897,6 +901,7 @@ void og_tendency(const og_block* b, const double* w, double dt, double* du) {
         size_t q = CELL(v, j, i);
         double dv = a1 * f1[q + 1] - a1 * f1[q];
         if (has2) dv = dv + (a2 * f2[q + n1] - a2 * f2[q]);
+        if (f3) dv = dv + (a3 * f3[q + plane] - a3 * f3[q]);
         du[q] = mdt * (dv / vol);
       }
 
@@ -985,6 +990,31 @@ void og_tendency(const og_block* b, const double* w, double dt, double* du) {
   free(f2);
   free(vf1);
   free(vf2);
+}
+
+void og_tendency(const og_block* b, const double* w, double dt, double* du) {
+  build_tables();
+  const size_t nc = ncell(b);
+  if (b->nc3 == 1) {
+    tendency_plane(b, w, dt, du, NULL);
+    return;
+  }
+  /* 3-D (no viscosity, no covariance row): the x3 face fluxes of every
+   * line, reflecting x3 walls prescribed, then each x2-x1 plane */
+  const int n1 = b->nc1, n2 = b->nc2, n3 = b->nc3, ng = b->ng;
+  const size_t plane = (size_t)n1 * n2;
+  double* f3 = (double*)calloc(5 * nc, sizeof(double));
+  og_flux(b, w, 3, f3);
+  for (int side = 0; side < 2; ++side) {
+    if (b->bc[4 + side] != OG_BC_REFLECTING) continue;
+    int k = side ? n3 - ng : ng;
+    for (size_t q = 0; q < plane; ++q)
+      f3[OG_IDN * nc + k * plane + q] = f3[OG_IPR * nc + k * plane + q] = 0.;
+  }
+  memset(du, 0, sizeof(double) * 5 * nc);
+  for (int k = ng; k < n3 - ng; ++k)
+    tendency_plane(b, w + k * plane, dt, du + k * plane, f3 + k * plane);
+  free(f3);
 }
 #undef CELL
 

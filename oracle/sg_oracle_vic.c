@@ -499,11 +499,15 @@ int og_implicit(const og_block* b, const double* w, double dtc, double* du) {
   const int n1 = b->nc1, n2 = b->nc2, ng = b->ng;
   const size_t nc = (size_t)n1 * n2 * b->nc3;
   const int jl = n2 > 1 ? ng : 0, ju1 = n2 > 1 ? n2 - ng : 1;
+  const int n3 = b->nc3, kl = n3 > 1 ? ng : 0, ku1 = n3 > 1 ? n3 - ng : 1;
   const int n = n1 - 2 * ng;
+  const long nj = ju1 - jl, ncols = nj * (ku1 - kl);
   int failed = 0;
+  /* every (x2, x3) column of the interior */
 #pragma omp parallel for schedule(static) reduction(+ : failed)
-  for (int j = jl; j < ju1; ++j) {
-    size_t c = (size_t)j * n1 + ng;
+  for (long cidx = 0; cidx < ncols; ++cidx) {
+    int j = jl + (int)(cidx % nj), k = kl + (int)(cidx / nj);
+    size_t c = ((size_t)k * n2 + j) * n1 + ng;
     failed += vic_column(b, w + c, nc, du + c, n, dtc, b->x1f + ng, b->x1v + ng);
   }
   return failed;

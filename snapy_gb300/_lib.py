@@ -70,7 +70,7 @@ NOALLOC_MAX_BLOCKS = 64  # SG_NOALLOC_MAX_BLOCKS
 
 # SG_KERNEL_* of sg_kernel_times
 KERNELS = ("stage_kernel", "vic_assemble_kernel", "vic_solve_kernel",
-           "vic_finish_kernel", "ghost_kernel")
+           "vic_finish_kernel", "ghost_kernel", "x3_kernel")
 
 
 # every symbol include/snapy_gb300.h declares, with its ctypes signature

@@ -33,6 +33,8 @@ using sg::StageParams;
   extern "C" int sg_launch_vic##sfx(const BlockDev*, StageParams, size_t,     \
                                     size_t, int*, cudaStream_t,                \
                                     cudaEvent_t*);                             \
+  extern "C" int sg_launch_x3##sfx(const BlockDev*, StageParams, size_t,      \
+                                   cudaStream_t);                              \
   extern "C" int sg_launch_reduce##sfx(const BlockDev*, int, int,              \
                                        unsigned long long*, int*, size_t,      \
                                        cudaStream_t);
@@ -161,9 +163,11 @@ struct sg_handle {
   int32_t launches = 0;
   int* status = nullptr;  // per-block solve status bits (VIC failures)
   std::vector<double*> x1tabs;  // per-block geometry tables (gravity)
+  bool has3 = false;            // a 3-D block: the x3 sweep runs
   bool implicit = false;
   size_t max_icells = 0, max_icols = 0;
-  std::vector<size_t> scratch_bytes;
+  std::vector<size_t> scratch_bytes;  // per block: vic_bytes + the x3 part
+  std::vector<size_t> vic_bytes;
   int device = 0;
   // per-kernel timing (sg_set_timing): events recorded between the launches
   // of each eager sg_stage, reused from a pool; each pending interval is
@@ -212,9 +216,10 @@ int upload(sg_handle* h, cudaStream_t s) {
     for (int q = 0; q < 3; ++q)
       if (!h->host[b].buf[q])
         return fail(SG_ERR_STATE, "block %d buffer %d is not bound", b, q);
-    if (h->host[b].implicit && !h->host[b].vic)
-      return fail(SG_ERR_STATE, "block %d: the implicit solve's scratch is not "
-                  "bound (sg_bind_scratch)", b);
+    if ((h->host[b].implicit && !h->host[b].vic) ||
+        (h->host[b].nc3 > 1 && !h->host[b].dv3))
+      return fail(SG_ERR_STATE, "block %d: the scratch (implicit solve, x3 "
+                  "faces) is not bound (sg_bind_scratch)", b);
   }
   cudaError_t e = cudaMemcpyAsync(h->dev, h->host.data(),
                                   sizeof(BlockDev) * h->nblock,
@@ -270,10 +275,10 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
       return fail(SG_ERR_ARG, "block %d: sizes (%d, %d, %d)", b, d.nc3, d.nc2,
                   d.nc1);
     }
-    if (d.nc3 > 1) {
+    if (d.nc3 > 1 && (d.nu_iso > 0. || d.flux_cov)) {
       sg_destroy(h);
-      return fail(SG_ERR_UNSUPPORTED, "block %d: 3-D blocks (nc3 = %d)", b,
-                  d.nc3);
+      return fail(SG_ERR_UNSUPPORTED, "block %d: 3-D blocks are built without "
+                  "viscosity and without the covariance row", b);
     }
     for (int f = 0; f < 6; ++f)
       if (d.bc[f] < SG_BC_NONE || d.bc[f] > SG_BC_EXTRAPOLATION) {
@@ -372,7 +377,10 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
     }
     B.tj = d.tj > 0 ? d.tj : choose_tj(h, d, nblock);
     int nx2 = d.nc2 > 1 ? d.nc2 - 2 * d.ng : 1;
-    B.ntile = (nx2 + B.tj - 1) / B.tj;
+    int nx3 = d.nc3 > 1 ? d.nc3 - 2 * d.ng : 1;
+    // tiles: tj-wide x2 strips of every interior x3 plane
+    B.ntile = nx3 * ((nx2 + B.tj - 1) / B.tj);
+    if (d.nc3 > 1) h->has3 = true;
     B.tile0 = tile;
     tile += B.ntile;
     size_t sm = stage_smem(h, d, B.tj);
@@ -387,15 +395,20 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
     h->max_plane = std::max(h->max_plane, plane);
     h->max_cells = std::max(h->max_cells, plane);
     h->max_nc1 = std::max(h->max_nc1, d.nc1);
-    size_t icells = (size_t)(d.nc1 - 2 * d.ng) *
-                    (size_t)(d.nc2 > 1 ? d.nc2 - 2 * d.ng : 1);
-    h->scratch_bytes.push_back(d.implicit_scheme ? icells * sg::kVicDoublesPerCell *
-                                                       sizeof(double)
-                                                 : 0);
+    size_t icols = (size_t)(d.nc2 > 1 ? d.nc2 - 2 * d.ng : 1) *
+                   (size_t)(d.nc3 > 1 ? d.nc3 - 2 * d.ng : 1);
+    size_t icells = (size_t)(d.nc1 - 2 * d.ng) * icols;
+    // the block's scratch: the implicit solve's FP64 arrays, then (3-D) the
+    // x3 flux differences a3 dF3 of every interior cell in the storage type
+    size_t vic_bytes = d.implicit_scheme ? icells * sg::kVicDoublesPerCell *
+                                               sizeof(double)
+                                         : 0;
+    size_t dv3_bytes = d.nc3 > 1 ? 5 * icells * (f64(h) ? 8 : 4) : 0;
+    h->vic_bytes.push_back(vic_bytes);
+    h->scratch_bytes.push_back(vic_bytes + dv3_bytes);
     if (d.implicit_scheme) {
       h->max_icells = std::max(h->max_icells, icells);
-      h->max_icols = std::max(h->max_icols,
-                              (size_t)(d.nc2 > 1 ? d.nc2 - 2 * d.ng : 1));
+      h->max_icols = std::max(h->max_icols, icols);
     }
   }
   h->ntile = tile;
@@ -465,7 +478,10 @@ int sg_bind_scratch(sg_handle* h, int32_t block, void* scratch, size_t bytes) {
                 block, h->scratch_bytes[block], bytes);
   if (reinterpret_cast<uintptr_t>(scratch) % 16)
     return fail(SG_ERR_ARG, "sg_bind_scratch: misaligned scratch");
-  h->host[block].vic = static_cast<double*>(scratch);
+  BlockDev& B = h->host[block];
+  B.vic = B.implicit ? static_cast<double*>(scratch) : nullptr;
+  B.dv3 = B.nc3 > 1 ? static_cast<unsigned char*>(scratch) + h->vic_bytes[block]
+                    : nullptr;
   h->dirty = true;
   return 0;
 }
@@ -600,10 +616,10 @@ int sg_stage(sg_handle* h, int32_t stage, const double* dt_dev,
   p.dt = dt_dev;
   p.max_nc1 = h->max_nc1;
   // events between the launches when timing is on and the stream is not
-  // being captured: ev[0] stage ev[1] (assemble ev[2] solve ev[3] finish
-  // ev[4]) ghost ev[5]
-  cudaEvent_t ev[6] = {};
-  int eidx[6] = {};
+  // being captured: ev[0] (x3 ev[6]) stage ev[1] (assemble ev[2] solve
+  // ev[3] finish ev[4]) ghost ev[5]
+  cudaEvent_t ev[7] = {};
+  int eidx[7] = {};
   bool timed = false;
   if (h->timing) {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -612,18 +628,27 @@ int sg_stage(sg_handle* h, int32_t stage, const double* dt_dev,
     timed = cs == cudaStreamCaptureStatusNone;
   }
   if (timed) {
-    for (int k = 0; k < 6; ++k) {
+    for (int k = 0; k < 7; ++k) {
       rc = take_event(h, &eidx[k]);
       if (rc) return rc;
       ev[k] = h->events[eidx[k]];
     }
     cudaEventRecord(ev[0], s);
   }
+  int launches = 2;
+  if (h->has3) {
+    // the x3 faces of the 3-D blocks: their flux differences, which the
+    // stage kernel adds to its divergence after x1 and x2
+    rc = f64(h) ? sg_launch_x3_f64(h->dev, p, h->max_cells, s)
+                : sg_launch_x3_f32(h->dev, p, h->max_cells, s);
+    if (rc) return cuda_fail((cudaError_t)rc, "sg_stage: x3 sweep");
+    if (timed) cudaEventRecord(ev[6], s);
+    launches += 1;
+  }
   rc = f64(h) ? sg_launch_stage_f64(h->dev, p, h->smem, s)
               : sg_launch_stage_f32(h->dev, p, h->smem, s);
   if (rc) return cuda_fail((cudaError_t)rc, "sg_stage: stage kernel");
   if (timed) cudaEventRecord(ev[1], s);
-  int launches = 2;
   if (h->implicit) {
     rc = f64(h) ? sg_launch_vic_f64(h->dev, p, h->max_icells, h->max_icols,
                                     h->status, s, timed ? ev + 2 : nullptr)
@@ -638,7 +663,12 @@ int sg_stage(sg_handle* h, int32_t stage, const double* dt_dev,
   if (rc) return cuda_fail((cudaError_t)rc, "sg_stage: ghost kernel");
   if (timed) {
     cudaEventRecord(ev[5], s);
-    h->pending.push_back({SG_KERNEL_STAGE, eidx[0], eidx[1]});
+    if (h->has3) {
+      h->pending.push_back({SG_KERNEL_X3, eidx[0], eidx[6]});
+      h->pending.push_back({SG_KERNEL_STAGE, eidx[6], eidx[1]});
+    } else {
+      h->pending.push_back({SG_KERNEL_STAGE, eidx[0], eidx[1]});
+    }
     if (h->implicit) {
       h->pending.push_back({SG_KERNEL_VIC_ASSEMBLE, eidx[1], eidx[2]});
       h->pending.push_back({SG_KERNEL_VIC_SOLVE, eidx[2], eidx[3]});

@@ -148,6 +148,7 @@ __device__ __forceinline__ double col_p(const real* pres, const double* pb,
   return pb ? (double)pres[j] + pb[j] : (double)pres[j];
 }
 
+#ifndef SG_REAL_IS_FLOAT
 __device__ __forceinline__ void ref_scan(const real* rho, const real* pres,
                                          const double* pb, int nc1, int iu,
                                          double dx, double grav,
@@ -173,6 +174,7 @@ __device__ __forceinline__ void ref_scan(const real* rho, const real* pres,
   }
 }
 
+#else
 // the same face pressures with the sums taken by a warp (all 32 lanes call
 // it for one column): below the top cell psf_lo[i] = top + sum_{k=i..iu} dp_k
 // and psf_hi[i] = top + sum_{k=i+1..iu} dp_k; above it psf_lo[i] = top -
@@ -228,6 +230,8 @@ __device__ __forceinline__ void ref_scan_warp(const real* rho, const real* pres,
     carry = __shfl_sync(full, S, 31);
   }
 }
+
+#endif
 
 __device__ __forceinline__ double wall_rop(double r0, double r1, double k) {
   double q = r0 / r1, qk = k == floor(k) ? q : pow(q, k);
@@ -317,11 +321,15 @@ __device__ __forceinline__ void stage_tile(const BlockDev* __restrict__ tab,
                                            real* sm) {
   const int bi = find_block(tab, p.nblock, tile);
   const BlockDev& B = tab[bi];
-  const int t = tile - B.tile0;
   const int nc1 = B.nc1, nc2 = B.nc2, ng = B.ng;
   const int nx1 = nc1 - 2 * ng;
   const bool has2 = nc2 > 1;
   const int hj = has2 ? ng : 0;
+  // tile t of the block: x2 strip t % strips of interior x3 plane t / strips
+  const int strips = ((has2 ? nc2 - 2 * ng : 1) + B.tj - 1) / B.tj;
+  const int t = (tile - B.tile0) % strips;
+  const int kk = (tile - B.tile0) / strips;
+  const size_t koff = (size_t)(B.nc3 > 1 ? ng + kk : 0) * nc1 * nc2;
   const int j0 = (has2 ? ng : 0) + t * B.tj;
   const int jend = has2 ? nc2 - ng : 1;
   const int ntj = min(B.tj, jend - j0);
@@ -356,7 +364,7 @@ __device__ __forceinline__ void stage_tile(const BlockDev* __restrict__ tab,
   const int f2stride = (ntj + 1) * nx1;
 
   // (1) the tile and its x2 halo, U -> W
-  const size_t row0 = (size_t)(j0 - hj) * nc1;
+  const size_t row0 = koff + (size_t)(j0 - hj) * nc1;
   for (int idx = threadIdx.x; idx < R * nc1; idx += blockDim.x) {
     real uc[NHYDRO], wc[NHYDRO];
 #pragma unroll
@@ -688,8 +696,14 @@ __device__ __forceinline__ void stage_tile(const BlockDev* __restrict__ tab,
   for (int idx = threadIdx.x; idx < ntj * nx1; idx += blockDim.x) {
     const int jt = idx / nx1, ii = idx - jt * nx1;
     const int i = il + ii;
-    const size_t c = (size_t)(j0 + jt) * nc1 + i;
+    const size_t c = koff + (size_t)(j0 + jt) * nc1 + i;
     const int wc = (hj + jt) * nc1 + i;
+    // the cell's index among the interior cells (the implicit solve's and
+    // the x3 differences' layout)
+    const size_t nx2i = has2 ? nc2 - 2 * ng : 1;
+    const size_t icells = (size_t)nx1 * nx2i * (B.nc3 > 1 ? B.nc3 - 2 * ng : 1);
+    const size_t vci = ((size_t)kk * nx2i + (j0 + jt - (has2 ? ng : 0))) * nx1 + ii;
+    const real* dv3 = static_cast<const real*>(B.dv3);
     real du[NHYDRO];
 #pragma unroll
     for (int v = 0; v < NHYDRO; ++v) {
@@ -699,6 +713,7 @@ __device__ __forceinline__ void stage_tile(const BlockDev* __restrict__ tab,
         const real* f2 = F2 + v * f2stride + jt * nx1 + ii;
         dv = dv + (a2 * f2[nx1] - a2 * f2[0]);
       }
+      if (dv3) dv = dv + dv3[v * icells + vci];
       du[v] = mdt * (dv / vol);
     }
     if (wb) {
@@ -759,10 +774,8 @@ __device__ __forceinline__ void stage_tile(const BlockDev* __restrict__ tab,
       // the vertical implicit correction follows: hand the explicit
       // tendency to it (interior cell (column, layer) of the VIC scratch)
       double* DU = B.vic;
-      const size_t cells = (size_t)nx1 * (has2 ? nc2 - 2 * ng : 1);
-      const size_t vc = (size_t)(j0 + jt - (has2 ? ng : 0)) * nx1 + ii;
 #pragma unroll
-      for (int v = 0; v < NHYDRO; ++v) DU[v * cells + vc] = (double)du[v];
+      for (int v = 0; v < NHYDRO; ++v) DU[v * icells + vci] = (double)du[v];
       continue;
     }
 #pragma unroll
@@ -847,6 +860,95 @@ __global__ void __launch_bounds__(kThreads)
       const double* eb = base_e(B.base, nc1);
       q[IDN * plane + c] += real(rb[si] - rb[i]);
       q[IPR * plane + c] += real(eb[si] - eb[i]);
+    }
+  }
+}
+
+// the x3 faces of 3-D blocks (CoordinateImpl::divergence's x3 term,
+// src/coord/coordinate.cpp:650-656): one thread per (x1 cell, x2 row, chunk
+// of kX3Chunk x3 cells) walks the chunk's faces with a sliding window of six
+// primitives in registers, solves each face once and stores a3 (F3[k+1] -
+// F3[k]) of each cell, which the stage kernel adds to its divergence after
+// the x1 and x2 differences, the reference's order.  With a hydrostatic base the
+// pressure is the anomaly about the cell row's base, as on x2 faces; a
+// reflecting x3 wall zeroes the mass and energy rows of its face.
+constexpr int kX3Chunk = 16;
+
+template <int RK, bool SHOCK>
+__global__ void __launch_bounds__(kThreads)
+    x3_kernel(const BlockDev* __restrict__ tab, StageParams p) {
+  const BlockDev& B = tab[blockIdx.y];
+  if (B.nc3 == 1) return;
+  const int nc1 = B.nc1, nc2 = B.nc2, nc3 = B.nc3, ng = B.ng;
+  const int nx1 = nc1 - 2 * ng, nx2 = nc2 > 1 ? nc2 - 2 * ng : 1,
+            nx3 = nc3 - 2 * ng;
+  const int o2 = nc2 > 1 ? ng : 0;
+  const int nch = (nx3 + kX3Chunk - 1) / kX3Chunk;
+  const size_t plane = (size_t)nc1 * nc2 * nc3, kst = (size_t)nc1 * nc2;
+  const real* __restrict__ uin = static_cast<const real*>(B.buf[p.in]);
+  const real gammad = real(B.gammad);
+  const bool scale = p.scale != 0;
+  const double* rb = B.base ? base_rho(B.base, nc1) : nullptr;
+  const double* pbc = B.base ? base_p(B.base, nc1) : nullptr;
+  const real a3 = real(B.dx2 * B.dx1);
+  const bool wlo = B.bc[4] == kBcReflecting, whi = B.bc[5] == kBcReflecting;
+  const size_t total = (size_t)nx1 * nx2 * nch;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const int i = ng + (int)(e % nx1);
+    const int j = o2 + (int)((e / nx1) % nx2);
+    const int ch = (int)(e / ((size_t)nx1 * nx2));
+    const int k0 = ng + ch * kX3Chunk;
+    const int k1 = min(k0 + kX3Chunk, ng + nx3);  // cells k0..k1-1
+    const size_t col = (size_t)j * nc1 + i;
+    const real pb = pbc ? real(pbc[i]) : real(0);
+    auto load = [&](int k, real* w) {
+      real uc[NHYDRO];
+#pragma unroll
+      for (int v = 0; v < NHYDRO; ++v) uc[v] = uin[v * plane + k * kst + col];
+      if (rb) uc[IDN] = real(rb[i]) + uc[IDN];
+      cons2prim<real>(uc, w, gammad);
+    };
+    // window: cells f-3 .. f+2 of face f
+    real W[6][NHYDRO];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) load(k0 - 3 + m, W[m]);
+    real fprev[NHYDRO];
+    for (int f = k0; f <= k1; ++f) {
+      load(f + 2, W[5]);
+      real wl[NHYDRO], wr[NHYDRO], flx[NHYDRO];
+#pragma unroll
+      for (int v = 0; v < NHYDRO; ++v) {
+        if (SHOCK || v == IDN) {
+          wl[v] = weno5_cp(W[0][v], W[1][v], W[2][v], W[3][v], W[4][v], scale);
+          wr[v] = weno5_cm(W[1][v], W[2][v], W[3][v], W[4][v], W[5][v], scale);
+        } else {
+          wl[v] = cp5_cp(W[0][v], W[1][v], W[2][v], W[3][v], W[4][v]);
+          wr[v] = cp5_cm(W[1][v], W[2][v], W[3][v], W[4][v], W[5][v]);
+        }
+      }
+      if (pbc)
+        lmars_flux_anom<real>(wl, wr, gammad, 3, pb, flx);
+      else
+        riemann<RK>(wl, wr, gammad, 3, flx);
+      if ((f == ng && wlo) || (f == ng + nx3 && whi))
+        flx[IDN] = flx[IPR] = real(0);
+      if (f > k0) {
+        // cell f - 1 between faces f - 1 and f
+        const int k = f - 1;
+        real* DV3 = static_cast<real*>(B.dv3);
+        const size_t cells = (size_t)nx1 * nx2 * nx3;
+        const size_t vc = ((size_t)(k - ng) * nx2 + (j - o2)) * nx1 + (i - ng);
+#pragma unroll
+        for (int v = 0; v < NHYDRO; ++v)
+          DV3[v * cells + vc] = a3 * flx[v] - a3 * fprev[v];
+      }
+#pragma unroll
+      for (int v = 0; v < NHYDRO; ++v) fprev[v] = flx[v];
+#pragma unroll
+      for (int m = 0; m < 5; ++m)
+#pragma unroll
+        for (int v = 0; v < NHYDRO; ++v) W[m][v] = W[m + 1][v];
     }
   }
 }
@@ -1070,6 +1172,21 @@ extern "C" int SG_NAME(sg_launch_stage)(const BlockDev* tab, StageParams p,
   }
   int grid = p.ntile < resident[kid][0] ? p.ntile : resident[kid][0];
   k<<<grid, kThreads, smem, stream>>>(tab, p);
+  return (int)cudaGetLastError();
+}
+
+extern "C" int SG_NAME(sg_launch_x3)(const BlockDev* tab, StageParams p,
+                                     size_t max_cells, cudaStream_t stream) {
+  void (*k)(const BlockDev*, StageParams) = nullptr;
+  if (p.riemann == kHllc)
+    k = p.shock ? x3_kernel<kHllc, true> : x3_kernel<kHllc, false>;
+  else
+    k = p.shock ? x3_kernel<kLmars, true> : x3_kernel<kLmars, false>;
+  // threads: cells / kX3Chunk per block (bounded by a few waves)
+  size_t work = max_cells / kX3Chunk + 1;
+  int gx = (int)((work + kThreads - 1) / kThreads);
+  if (gx > 2048) gx = 2048;
+  k<<<dim3(gx, p.nblock), kThreads, 0, stream>>>(tab, p);
   return (int)cudaGetLastError();
 }
 

@@ -59,6 +59,10 @@ struct BlockDev {
   // (the corrected-PE slope weights w0, w1, w2, grav1 h^2 / 12, and
   // grav1 (x1f[i+1] - x1v[i]), grav1 (x1f[i] - x1v[i]) for i = ng + k)
   const double* x1tab;
+  // 3-D: a3 (F3[k+1] - F3[k]) of every interior cell and variable, in the
+  // storage type, laid out (v, k, j, i) over the interior; written by the x3
+  // sweep, added to the divergence by the stage kernel
+  void* dv3;
 };
 
 // offsets into BlockDev::base

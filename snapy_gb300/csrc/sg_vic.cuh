@@ -36,7 +36,8 @@ __device__ __forceinline__ VicScratch vic_scratch(const BlockDev& B) {
   const int ng = B.ng;
   const size_t nx1 = B.nc1 - 2 * ng;
   const size_t nx2 = B.nc2 > 1 ? B.nc2 - 2 * ng : 1;
-  s.cells = nx1 * nx2;
+  const size_t nx3 = B.nc3 > 1 ? B.nc3 - 2 * ng : 1;
+  s.cells = nx1 * nx2 * nx3;
   s.du = B.vic;
   s.du0 = s.du + 5 * s.cells;
   s.A = s.du0 + 5 * s.cells;
@@ -46,6 +47,14 @@ __device__ __forceinline__ VicScratch vic_scratch(const BlockDev& B) {
   s.Z0 = s.D + 5 * s.cells;
   s.Z1 = s.Z0 + 5 * s.cells;
   return s;
+}
+
+// the padded (x3, x2) row of interior column `col` (x2 fastest)
+__device__ __forceinline__ size_t vic_row(const BlockDev& B, size_t col) {
+  const int ng = B.ng;
+  const size_t nx2 = B.nc2 > 1 ? B.nc2 - 2 * ng : 1;
+  const size_t j = col % nx2, k = col / nx2;
+  return (B.nc3 > 1 ? k + ng : 0) * B.nc2 + (B.nc2 > 1 ? j + ng : 0);
 }
 
 // bit of the per-block status word: a column's solve failed this step
@@ -221,7 +230,7 @@ __global__ void __launch_bounds__(kThreads)
        e += (size_t)gridDim.x * blockDim.x) {
     const int i = (int)(e % n);
     const size_t col = e / n;
-    const size_t jrow = B.nc2 > 1 ? col + ng : 0;
+    const size_t jrow = vic_row(B, col);
     const size_t base = jrow * nc1 + ng;  // padded cell of layer 0
     double wl[5], wr[5], wn[5];
     vic_prim(uin, plane, base + i - 1, B.gammad, wl, B.base, nc1);
@@ -667,7 +676,7 @@ __global__ void __launch_bounds__(32 * kVicWarps)
   const real* uin = static_cast<const real*>(B.buf[p.in]);
   const real* u0 = static_cast<const real*>(B.buf[p.u0]);
   real* uout = static_cast<real*>(B.buf[p.out]);
-  const size_t jrow = B.nc2 > 1 ? col + ng : 0;
+  const size_t jrow = vic_row(B, col);
   const size_t base = jrow * nc1 + ng;
   const double grav = B.grav1;
   const double vol = B.dx3 * (B.dx2 * B.dx1);

@@ -75,7 +75,11 @@ def scheme_of(options: MeshBlockOptions) -> dict:
             raise DeckError("integration/implicit-precision float32 is not built "
                             "(the implicit solve runs in FP64)")
     if c.nx3 > 1:
-        raise DeckError("3-D blocks are not built")
+        if h.diffusion is not None and h.diffusion.nu_iso:
+            raise DeckError("3-D blocks are built without forcing/diffusion")
+        if h.flux_covariance:
+            raise DeckError("3-D blocks are built without the covariance row: "
+                            "set dynamics/flux-covariance: false")
     intg = options.intg()
     return {
         "riemann": _lib.HLLC if h.riemann.type == "hllc" else _lib.LMARS,

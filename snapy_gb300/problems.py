@@ -95,3 +95,33 @@ def straka(options: MeshBlockOptions, device="cuda", dT=None, xc=None, zc=None,
                               torch.zeros_like(L))
     w[0] = w[4] / (Rd * temp)
     return w
+
+
+def convection3d(options: MeshBlockOptions, device="cuda", seed: int = 0) -> torch.Tensor:
+    """3-D planar dry convection at rest: the isentropic base state of
+    potential temperature Ts over p0 (as straka's) with potential-temperature
+    noise dtheta U[-1, 1], drawn from a generator seeded with `seed`, in the
+    cells whose centre lies in the lowest `layer` fraction of the x1 extent
+    (problem keys p0, Ts, dtheta, layer); x1 is vertical."""
+    c = options.coord()
+    p = options.problem
+    eos = options.hydro().eos
+    grav = -options.hydro().grav.grav1 if options.hydro().grav else 9.8
+    p0 = float(p.get("p0", 1.e5))
+    Ts = float(p.get("Ts", 300.))
+    dtheta = float(p.get("dtheta", 0.1))
+    layer = float(p.get("layer", 0.1))
+    Rd = RGAS / eos.weight
+    cv = Rd / (eos.gammad - 1.)
+    cp = cv + Rd
+    x1v = _centers(options, 1, device).view(1, 1, -1)
+    temp = (Ts - grav * x1v / cp).expand(c.nc3, c.nc2, c.nc1)
+    w = torch.zeros((5, c.nc3, c.nc2, c.nc1), dtype=torch.float64, device=device)
+    w[4] = p0 * torch.pow(temp / Ts, cp / Rd)
+    g = torch.Generator().manual_seed(int(seed))
+    noise = (2. * torch.rand((c.nc3, c.nc2, c.nc1), generator=g,
+                             dtype=torch.float64) - 1.) * dtheta
+    low = (x1v - c.x1min) < layer * (c.x1max - c.x1min)
+    noise = torch.where(low.cpu(), noise, torch.zeros_like(noise)).to(device)
+    w[0] = w[4] / (Rd * temp * (1. + noise / Ts))
+    return w
