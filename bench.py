@@ -56,7 +56,12 @@ WORKLOADS = {
     # {32..128}, seeded bubbles) in one handle: one persistent launch per
     # kernel and stage, each member's dt on the device, one graph per step
     "ensemble": "snapy_gb300/decks/straka.yaml",
+    # the serving trace: Poisson arrivals (20 req/s) of 3-D planar dry
+    # convection solves, (nx2, nx3, nx1) from {64, 96, 128}^2 x {64, 96},
+    # 200 RK3 steps each, FP32 bulk with the FP64 implicit solve
+    "serving": "snapy_gb300/decks/convection3d.yaml",
 }
+SERVE_RATE, SERVE_SEED = 20.0, 20261204
 ENSEMBLE_MEMBERS, ENSEMBLE_SEED = 64, 20261203
 
 
@@ -70,6 +75,10 @@ def parse():
     ap.add_argument("--precision", choices=["float64", "float32"], default=None)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--requests", type=int, default=8,
+                    help="serving: requests in the trace")
+    ap.add_argument("--serve-steps", type=int, default=200,
+                    help="serving: RK3 steps per request")
     return ap.parse_args()
 
 
@@ -616,8 +625,214 @@ def run_reference_ensemble(args):
     return 0
 
 
+def serving_trace(n, steps, precision=None):
+    """The serving trace: n requests with seeded sizes and seeds, exponential
+    inter-arrival times of mean 1 / SERVE_RATE."""
+    import torch
+    import snapy_gb300 as sg
+    from snapy_gb300 import problems
+    from snapy_gb300.serving import Request
+    g = torch.Generator().manual_seed(SERVE_SEED)
+    t, reqs = 0.0, []
+    for i in range(n):
+        t += float(-torch.log(torch.rand(1, generator=g, dtype=torch.float64)) / SERVE_RATE)
+        pick = lambda seq: seq[int(torch.randint(len(seq), (1,), generator=g))]
+        nx2, nx3, nx1 = pick((64, 96, 128)), pick((64, 96, 128)), pick((64, 96))
+        opts = sg.MeshBlockOptions.from_yaml(os.path.join(ROOT, WORKLOADS["serving"]))
+        c = opts.coord()
+        c.nx1, c.nx2, c.nx3 = nx1, nx2, nx3
+        c.x1max, c.x2max, c.x3max = nx1 * 50.0, nx2 * 50.0, nx3 * 50.0
+        if precision:
+            opts.hydro().precision = precision
+        seed = SERVE_SEED + 1 + i
+        reqs.append(Request(i, opts, (lambda o=opts, s=seed: problems.convection3d(o, "cpu", seed=s)),
+                            steps, t))
+    return reqs
+
+
+def serving_config(reqs, nranks):
+    return {"workload": f"serving trace: {len(reqs)} 3-D planar dry convection "
+                        f"solves, Poisson arrivals {SERVE_RATE:g}/s (seed "
+                        f"{SERVE_SEED}), (nx2, nx3, nx1) in {{64,96,128}}^2 x "
+                        f"{{64,96}} at 50 m, {reqs[0].steps} RK3 steps each, "
+                        f"lmars+weno5+rk3+VIC, {reqs[0].options.hydro().precision} "
+                        "bulk, FP64 implicit solve",
+            "requests": len(reqs), "steps_per_request": reqs[0].steps,
+            "cells": [r.cells for r in reqs],
+            "admission": "first come first served against free HBM",
+            "batching": "continuous: every running request in the same "
+                        "launches, handle rebuilt on admission/completion",
+            "l2": "inputs larger than L2 (no flush needed)",
+            "replicas": nranks,
+            "parallelism": "replicas" if nranks > 1 else "single"}
+
+
+def run_serving(args):
+    import torch
+    import torch.distributed as dist
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl", init_method="env://")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    import snapy_gb300 as sg
+    from snapy_gb300.serving import Server
+    # warm-up: a short trace compiles nothing but touches every code path
+    warm = serving_trace(2, max(3, args.warmup), args.precision)
+    for r in warm:
+        r.arrival = 0.0
+    Server(dev).run(warm)
+    reqs = serving_trace(args.requests, args.serve_steps, args.precision)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    srv = Server(dev, timing=True)
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        srv.run(reqs)
+        wall = time.perf_counter() - t0
+    bad = [r.rid for r in reqs if r.flags]
+    assert not bad, f"retry flags on requests {bad}"
+    total = sum(r.cells * r.steps for r in reqs)
+    gpu_s = sum(srv.gpu_step_ms) / 1e3
+    if world > 1:
+        t = torch.tensor([gpu_s, wall], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        gpu_s, wall = float(t[0]), float(t[1])
+    lat = sorted(r.latency for r in reqs)
+    q = lambda f: lat[min(len(lat) - 1, int(round(f * (len(lat) - 1))))]
+    kms = srv.kernel_ms
+    dom = max(kms, key=lambda k: kms[k][0])
+    cells_all = sum(r.cells for r in reqs)
+    per_cell = {"stage_kernel": 5 * 4 + 40, "x3_kernel": 5 * 4 * 2,
+                "vic_assemble_kernel": 5 * 4 + 40 + 40 + 600,
+                "vic_solve_kernel": 600 + 40 + 200 + 120 + 200 + 120 + 120,
+                "vic_finish_kernel": 120 + 15 * 4, "ghost_kernel": 0}
+    # a launch covers the running set; its cells vary, so the achieved
+    # bandwidth is the algorithmic bytes of all cell-steps over the kernel time
+    achieved = per_cell[dom] * total * 3 / (kms[dom][0] / 1e3) / 1e9
+    peak, peak_kind = peaks()
+    # the plain FP64 path on the same requests: each alone, its own FP64
+    # MeshBlock, a few steps (its per-cell-step rate)
+    plain_steps = 3
+    t_plain, n_plain = 0.0, 0
+    for r in reqs:
+        o64 = sg.MeshBlockOptions.from_yaml(os.path.join(ROOT, WORKLOADS["serving"]))
+        c, c0 = o64.coord(), r.options.coord()
+        c.nx1, c.nx2, c.nx3 = c0.nx1, c0.nx2, c0.nx3
+        c.x1max, c.x2max, c.x3max = c0.x1max, c0.x2max, c0.x3max
+        o64.hydro().precision = "float64"
+        blk = sg.MeshBlock(o64).to(dev)
+        vars = {"hydro_w": r.initial().to(dev)}
+        blk.initialize(vars)
+        for _ in range(5):  # eager steps and both graphs
+            blk.step(vars, blk.max_time_step(vars))
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        for _ in range(plain_steps):
+            blk.step(vars, blk.max_time_step(vars))
+        torch.cuda.synchronize()
+        t_plain += time.perf_counter() - t1
+        n_plain += r.cells * plain_steps
+        del blk, vars
+    plain = n_plain / t_plain
+    if rank == 0:
+        cb = None
+        if not args.no_cpu_baseline:
+            small = min(reqs, key=lambda r: r.cells)
+            cb = serving_cpu_baseline(small, args.cpu_seconds)
+        line = {
+            "metric": "cell-updates/s per RK3 step",
+            "value": total * world / gpu_s, "unit": "cell-updates/s",
+            "n_gpus": world, "steps": len(srv.gpu_step_ms), "warmup": args.warmup,
+            "ms_per_step": gpu_s / len(srv.gpu_step_ms) * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32" if reqs[0].options.hydro().precision == "float32" else "f64",
+            "data": "synthetic (seeded convection requests, seeded arrivals)",
+            "config": serving_config(reqs, world),
+            "latency": {"p50_s": q(0.5), "p99_s": q(0.99), "min_s": lat[0],
+                        "max_s": lat[-1], "unit": "s, arrival to result on host"},
+            "e2e": {"value": total * world / wall, "unit": "cell-updates/s",
+                    "h2d_bytes_per_step": srv.h2d_bytes / len(srv.gpu_step_ms),
+                    "d2h_bytes_per_step": srv.d2h_bytes / len(srv.gpu_step_ms),
+                    "note": "wall clock of the whole trace: arrivals, initial "
+                            "states host->device, results device->host"},
+            "plain_fp64": {"value": plain, "unit": "cell-updates/s",
+                           "how": f"each request alone, its own FP64 MeshBlock, "
+                                  f"{plain_steps} steps after warm-up, graphs on"},
+            "vs_plain_fp64": total / gpu_s / plain,
+            "max_running": srv.max_running, "handle_rebuilds": srv.rebuilds,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak,
+                         "peak_kind": peak_kind, "traffic": None, "kernel": dom,
+                         "mean_launch_us": kms[dom][0] / kms[dom][1] * 1e3,
+                         "limiter": "FP64 issue rate (one FP64 warp instruction "
+                                    "per SM sub-partition per 64 cycles)"},
+            "kernels": {k: {"launches": n, "mean_us": ms / n * 1e3,
+                            "share": ms / sum(v[0] for v in kms.values())}
+                        for k, (ms, n) in kms.items()},
+            "cpu_baseline": cb,
+            "clocks": clk.summary(),
+            "gpu_launches": srv.launches,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def serving_cpu_baseline(req, seconds):
+    """The CPU oracle (FP64, OpenMP on every host core) on the smallest
+    request of the trace, as many RK3 steps as fit in `seconds`."""
+    from oracle import oracle as O
+    O.build()
+    cores = os.cpu_count() or 1
+    ob = O.block_from_options(req.options, nthreads=cores)
+    u = ob.initialize(req.initial().numpy())
+    n, t0 = 0, time.perf_counter()
+    while True:
+        ob.step(u, req.options.intg().cfl * ob.max_dt(u))
+        n += 1
+        el = time.perf_counter() - t0
+        if (el >= seconds and n >= 1) or n >= 10000:
+            break
+    c = req.options.coord()
+    return {"value": req.cells * n / el, "unit": "cell-updates/s", "cores": cores,
+            "kind": "port",
+            "sample": f"{n} RK3 steps of the smallest request ({c.nx2}x{c.nx3}x"
+                      f"{c.nx1}), FP64, {el:.1f} s, OpenMP {cores} threads"}
+
+
+def run_reference_serving(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    reqs = serving_trace(args.requests, args.serve_steps, args.precision)
+    cb = serving_cpu_baseline(min(reqs, key=lambda r: r.cells),
+                              max(2.0, args.cpu_seconds))
+    val = cb["value"]
+    print(json.dumps({
+        "impl": "reference", "metric": "cell-updates/s per RK3 step",
+        "value": val, "unit": "cell-updates/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": reqs[0].cells / val * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded convection requests, seeded arrivals)",
+        "config": serving_config(reqs, 1), "cpu_baseline": cb,
+        "e2e": {"value": val, "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0}}), flush=True)
+    return 0
+
+
 def main():
     args = parse()
+    if args.workload == "serving":
+        if args.impl == "reference":
+            return run_reference_serving(args)
+        return run_serving(args)
     if args.workload == "ensemble":
         if args.impl == "reference":
             return run_reference_ensemble(args)

@@ -22,6 +22,29 @@ def _stream(stream: Optional[torch.cuda.Stream] = None) -> int:
     return s.cuda_stream
 
 
+def fill_base(t: torch.Tensor, w: torch.Tensor, d: dict) -> None:
+    """The FP64 hydrostatic base of an anomaly block (sg_block_desc.base)
+    from its initial primitives w: the horizontal mean of rho and p on each
+    x1 row, e_b = p_b / (gamma - 1), face pressures pf_b (mean of the two
+    cells beside a face, end faces copy the end cells) and the base's
+    residual r_b = rho_b g1 - (pf_b[i + 1] - pf_b[i]) / dx1.  Any base gives
+    the same equations; one near the state keeps the FP32 anomalies small."""
+    nc1, nc2, nc3, ng = d["nc1"], d["nc2"], d["nc3"], d["ng"]
+    j = slice(ng, nc2 - ng) if nc2 > 1 else slice(0, 1)
+    k = slice(ng, nc3 - ng) if nc3 > 1 else slice(0, 1)
+    rho = w[0, k, j, :].mean(dim=(0, 1))
+    pres = w[4, k, j, :].mean(dim=(0, 1))
+    pf = torch.empty(nc1 + 1, dtype=torch.float64, device=w.device)
+    pf[1:nc1] = 0.5 * (pres[:-1] + pres[1:])
+    pf[0], pf[nc1] = pres[0], pres[-1]
+    r = rho * d["grav1"] - (pf[1:] - pf[:-1]) / d["dx1"]
+    t[0:nc1] = rho
+    t[nc1:2 * nc1] = pres
+    t[2 * nc1:3 * nc1] = pres / (d["gammad"] - 1.0)
+    t[3 * nc1:4 * nc1 + 1] = pf
+    t[4 * nc1 + 1:5 * nc1 + 1] = r
+
+
 class Batch:
     """Blocks of one scheme; each block is a dict with nc1, nc2, nc3, ng,
     dx1, dx2, dx3, gammad, bc (6 ints) and optionally tj."""
@@ -163,28 +186,7 @@ class Batch:
                    "sg_init_from_prim")
 
     def _set_base(self, b: int, w: torch.Tensor) -> None:
-        """The FP64 hydrostatic base of an anomaly block from its initial
-        primitives: the horizontal mean of rho and p on each x1 row, e_b =
-        p_b / (gamma - 1), face pressures pf_b (mean of the two cells beside
-        a face, end faces copy the end cells) and the base's residual
-        r_b = rho_b g1 - (pf_b[i + 1] - pf_b[i]) / dx1.  Any base gives the
-        same equations; one near the state keeps the FP32 anomalies small."""
-        d = self.blocks[b]
-        nc1, nc2, nc3, ng = d["nc1"], d["nc2"], d["nc3"], d["ng"]
-        j = slice(ng, nc2 - ng) if nc2 > 1 else slice(0, 1)
-        k = slice(ng, nc3 - ng) if nc3 > 1 else slice(0, 1)
-        rho = w[0, k, j, :].mean(dim=(0, 1))
-        pres = w[4, k, j, :].mean(dim=(0, 1))
-        pf = torch.empty(nc1 + 1, dtype=torch.float64, device=w.device)
-        pf[1:nc1] = 0.5 * (pres[:-1] + pres[1:])
-        pf[0], pf[nc1] = pres[0], pres[-1]
-        r = rho * d["grav1"] - (pf[1:] - pf[:-1]) / d["dx1"]
-        t = self.bases[b]
-        t[0:nc1] = rho
-        t[nc1:2 * nc1] = pres
-        t[2 * nc1:3 * nc1] = pres / (d["gammad"] - 1.0)
-        t[3 * nc1:4 * nc1 + 1] = pf
-        t[4 * nc1 + 1:5 * nc1 + 1] = r
+        fill_base(self.bases[b], w, self.blocks[b])
 
     def totals(self, b: int, u: torch.Tensor) -> torch.Tensor:
         """The total conserved state (FP64) of block b's stored state u (an
