@@ -75,6 +75,10 @@ def parse():
     ap.add_argument("--precision", choices=["float64", "float32"], default=None)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--implicit-precision", choices=["float64", "float32"],
+                    default="float32",
+                    help="ensemble/serving: assembly of the implicit blocks "
+                         "(the block-tridiagonal solve is FP64 either way)")
     ap.add_argument("--requests", type=int, default=8,
                     help="serving: requests in the trace")
     ap.add_argument("--serve-steps", type=int, default=200,
@@ -422,10 +426,12 @@ def ensemble_cpu_baseline(members, seconds):
 
 def ensemble_config(members, precision, nranks):
     cells = sum(o.coord().nx1 * o.coord().nx2 for o, _ in members)
+    ip = members[0][0].hydro().icorr.precision
     return {"workload": f"ensemble of {len(members)} Straka-type members "
                         f"(nx2 in 128..512, nx1 in 32..128, 50 m, seed "
                         f"{ENSEMBLE_SEED}), lmars+weno5+rk3+VIC, {precision} "
                         "bulk, FP64 implicit solve",
+            "implicit_assembly": ip,
             "members": len(members), "cells": cells, "precision": precision,
             "gravity": True, "implicit": True,
             "dt": "each member's own CFL step, on the device, every step",
@@ -455,6 +461,9 @@ def run_ensemble(args):
     precision = args.precision or "float32"
     members = problems.ensemble_members(ENSEMBLE_MEMBERS, ENSEMBLE_SEED,
                                         precision=precision)
+    if precision == "float32":
+        for o, _ in members:
+            o.hydro().icorr.precision = args.implicit_precision
     cells = sum(o.coord().nx1 * o.coord().nx2 for o, _ in members)
     ens = Ensemble([o for o, _ in members], device=dev)
     ens.initialize([w for _, w in members])
@@ -625,7 +634,7 @@ def run_reference_ensemble(args):
     return 0
 
 
-def serving_trace(n, steps, precision=None):
+def serving_trace(n, steps, precision=None, implicit_precision=None):
     """The serving trace: n requests with seeded sizes and seeds, exponential
     inter-arrival times of mean 1 / SERVE_RATE."""
     import torch
@@ -644,6 +653,8 @@ def serving_trace(n, steps, precision=None):
         c.x1max, c.x2max, c.x3max = nx1 * 50.0, nx2 * 50.0, nx3 * 50.0
         if precision:
             opts.hydro().precision = precision
+        if opts.hydro().precision == "float32" and implicit_precision:
+            opts.hydro().icorr.precision = implicit_precision
         seed = SERVE_SEED + 1 + i
         reqs.append(Request(i, opts, (lambda o=opts, s=seed: problems.convection3d(o, "cpu", seed=s)),
                             steps, t))
@@ -658,6 +669,7 @@ def serving_config(reqs, nranks):
                         f"lmars+weno5+rk3+VIC, {reqs[0].options.hydro().precision} "
                         "bulk, FP64 implicit solve",
             "requests": len(reqs), "steps_per_request": reqs[0].steps,
+            "implicit_assembly": reqs[0].options.hydro().icorr.precision,
             "cells": [r.cells for r in reqs],
             "admission": "first come first served against free HBM",
             "batching": "continuous: every running request in the same "
@@ -680,11 +692,13 @@ def run_serving(args):
     import snapy_gb300 as sg
     from snapy_gb300.serving import Server
     # warm-up: a short trace compiles nothing but touches every code path
-    warm = serving_trace(2, max(3, args.warmup), args.precision)
+    warm = serving_trace(2, max(3, args.warmup), args.precision,
+                         args.implicit_precision)
     for r in warm:
         r.arrival = 0.0
     Server(dev).run(warm)
-    reqs = serving_trace(args.requests, args.serve_steps, args.precision)
+    reqs = serving_trace(args.requests, args.serve_steps, args.precision,
+                         args.implicit_precision)
     torch.cuda.synchronize()
     if world > 1:
         dist.barrier()

@@ -102,6 +102,10 @@ typedef struct sg_block_desc {
    * The contents may be written after sg_create, before sg_init_from_prim.
    * Must be null otherwise. */
   const double* base;
+  /* integration/implicit-precision: SG_F64 (default) or SG_F32, which
+   * assembles the implicit blocks in FP32 (SG_F32 storage only); the
+   * block-tridiagonal solve runs in FP64 either way */
+  int32_t implicit_precision;
 } sg_block_desc;
 
 int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,

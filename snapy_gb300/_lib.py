@@ -55,6 +55,7 @@ class BlockDesc(ctypes.Structure):
         ("x1v", _vp),
         ("implicit_scheme", _i32),
         ("base", _vp),
+        ("implicit_precision", _i32),
     ]
 
 

@@ -95,6 +95,7 @@ class Batch:
             a.x1f = f.data_ptr() if f is not None else None
             a.x1v = v.data_ptr() if v is not None else None
             a.implicit_scheme = int(d.get("implicit_scheme", 0))
+            a.implicit_precision = _lib.F32 if d.get("implicit_f32") else _lib.F64
         # FP32 under gravity: the state is stored as anomalies about an FP64
         # hydrostatic base per block (filled from the initial state)
         self.bases = []

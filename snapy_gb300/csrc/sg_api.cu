@@ -31,7 +31,7 @@ using sg::StageParams;
                                      double* const*, size_t,                   \
                                      cudaStream_t);                            \
   extern "C" int sg_launch_vic##sfx(const BlockDev*, StageParams, size_t,     \
-                                    size_t, int*, cudaStream_t,                \
+                                    size_t, int, int*, cudaStream_t,           \
                                     cudaEvent_t*);                             \
   extern "C" int sg_launch_x3##sfx(const BlockDev*, StageParams, size_t,      \
                                    cudaStream_t);                              \
@@ -164,6 +164,8 @@ struct sg_handle {
   int* status = nullptr;  // per-block solve status bits (VIC failures)
   std::vector<double*> x1tabs;  // per-block geometry tables (gravity)
   bool has3 = false;            // a 3-D block: the x3 sweep runs
+  size_t sum_icols = 0;         // implicit columns of all blocks
+  int wide = 0;  // enough columns for a thread per column in the finish
   bool implicit = false;
   size_t max_icells = 0, max_icols = 0;
   std::vector<size_t> scratch_bytes;  // per block: vic_bytes + the x3 part
@@ -352,6 +354,17 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
                   "FP32 blocks with gravity", b);
     }
     B.base = d.base;
+    if (d.implicit_precision != SG_F64 && d.implicit_precision != SG_F32) {
+      sg_destroy(h);
+      return fail(SG_ERR_ARG, "block %d: implicit_precision %d", b,
+                  d.implicit_precision);
+    }
+    if (d.implicit_precision == SG_F32 && scheme->dtype != SG_F32) {
+      sg_destroy(h);
+      return fail(SG_ERR_UNSUPPORTED, "block %d: implicit-precision float32 "
+                  "needs the FP32 state (dynamics/precision float32)", b);
+    }
+    B.implicit_f32 = d.implicit_scheme != 0 && d.implicit_precision == SG_F32;
     B.x1tab = nullptr;
     if (d.grav1 != 0.) {
       const int nx1 = d.nc1 - 2 * d.ng;
@@ -409,9 +422,16 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
     if (d.implicit_scheme) {
       h->max_icells = std::max(h->max_icells, icells);
       h->max_icols = std::max(h->max_icols, icols);
+      h->sum_icols += icols;
     }
   }
   h->ntile = tile;
+  {
+    // a full warp of columns for every SM sub-partition
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
+    h->wide = h->sum_icols >= (size_t)32 * 4 * sms;
+  }
   cudaError_t e = cudaMalloc(&h->dev, sizeof(BlockDev) * nblock);
   if (e == cudaSuccess)
     e = cudaMalloc(&h->red, sizeof(unsigned long long) * 4 * nblock);
@@ -651,9 +671,11 @@ int sg_stage(sg_handle* h, int32_t stage, const double* dt_dev,
   if (timed) cudaEventRecord(ev[1], s);
   if (h->implicit) {
     rc = f64(h) ? sg_launch_vic_f64(h->dev, p, h->max_icells, h->max_icols,
-                                    h->status, s, timed ? ev + 2 : nullptr)
+                                    h->wide, h->status, s,
+                                    timed ? ev + 2 : nullptr)
                 : sg_launch_vic_f32(h->dev, p, h->max_icells, h->max_icols,
-                                    h->status, s, timed ? ev + 2 : nullptr);
+                                    h->wide, h->status, s,
+                                    timed ? ev + 2 : nullptr);
     if (rc) return cuda_fail((cudaError_t)rc, "sg_stage: implicit solve");
     if (timed) cudaEventRecord(ev[4], s);
     launches += 3;

@@ -1221,8 +1221,8 @@ extern "C" int SG_NAME(sg_launch_init)(const BlockDev* tab, int nblock,
 // explicit tendency of the implicit blocks)
 extern "C" int SG_NAME(sg_launch_vic)(const BlockDev* tab, StageParams p,
                                       size_t max_cells, size_t max_cols,
-                                      int* status, cudaStream_t stream,
-                                      cudaEvent_t* ev) {
+                                      int wide, int* status,
+                                      cudaStream_t stream, cudaEvent_t* ev) {
   int ga = (int)((max_cells + kThreads - 1) / kThreads);
   if (ga > 4096) ga = 4096;
   vic_assemble_kernel<<<dim3(ga, p.nblock), kThreads, 0, stream>>>(tab, p);
@@ -1236,8 +1236,13 @@ extern "C" int SG_NAME(sg_launch_vic)(const BlockDev* tab, StageParams p,
   e = cudaGetLastError();
   if (e != cudaSuccess) return (int)e;
   if (ev) cudaEventRecord(ev[1], stream);
-  int gc = (int)((max_cols + kVicWarps - 1) / kVicWarps);
-  vic_finish_kernel<<<dim3(gc, p.nblock), 32 * kVicWarps, 0, stream>>>(tab, p);
+  if (wide) {
+    int gt = (int)((max_cols + kThreads - 1) / kThreads);
+    vic_finish_kernel<1><<<dim3(gt, p.nblock), kThreads, 0, stream>>>(tab, p);
+  } else {
+    int gc = (int)((max_cols + kVicWarps - 1) / kVicWarps);
+    vic_finish_kernel<32><<<dim3(gc, p.nblock), 32 * kVicWarps, 0, stream>>>(tab, p);
+  }
   return (int)cudaGetLastError();
 }
 

@@ -47,6 +47,7 @@ struct BlockDev {
   // and its FP64 scratch (kVicDoublesPerCell per interior cell), laid out
   // as in vic_scratch()
   int32_t implicit;
+  int32_t implicit_f32;  // implicit-precision float32: FP32 block assembly
   double* vic;
   // FP32 under gravity: the state buffers hold anomalies u - u_b about an
   // FP64 hydrostatic base that depends on x1 only, laid out as

@@ -22,7 +22,8 @@
 // shuffles, the 8 right-hand sides of the LU back-solve one per lane, the
 // factorisation on the warp's shared-memory tile), and the column's
 // redistribution, remainder and RK combine (vic_finish_kernel, one warp per
-// column).  Every product is summed in index order, so the results are bit
+// column, or one thread per column when the batch has columns enough to
+// fill every SM sub-partition).  Every product is summed in index order, so the results are bit
 // for bit the CPU oracle's.
 #pragma once
 
@@ -60,81 +61,84 @@ __device__ __forceinline__ size_t vic_row(const BlockDev& B, size_t col) {
 // bit of the per-block status word: a column's solve failed this step
 constexpr int kVicFailed = 32;
 
-__device__ __forceinline__ void vmat_mul(const double* a, const double* b,
-                                         double* out) {
+template <typename T>
+__device__ __forceinline__ void vmat_mul(const T* a, const T* b,
+                                         T* out) {
 #pragma unroll
   for (int r = 0; r < 5; ++r)
 #pragma unroll
     for (int c = 0; c < 5; ++c) {
-      double s = a[r * 5] * b[c];
+      T s = a[r * 5] * b[c];
 #pragma unroll
       for (int k = 1; k < 5; ++k) s += a[r * 5 + k] * b[k * 5 + c];
       out[r * 5 + c] = s;
     }
 }
 
-__device__ __forceinline__ void vflux_jacobian(double* J, double gm1,
-                                               const double* w) {
-  double v1 = w[1], v2 = w[2], v3 = w[3], rho = w[0], pres = w[4];
-  double s2 = v1 * v1 + v2 * v2 + v3 * v3;
-  double c1 = ((gm1 - 1) * s2 / 2 - (gm1 + 1) / gm1 * pres / rho) * v1;
-  double c2 = (gm1 + 1) / gm1 * pres / rho + s2 / 2 - gm1 * v1 * v1;
-  J[0] = 0; J[1] = 1.; J[2] = 0.; J[3] = 0.; J[4] = 0.;
-  J[5] = gm1 * s2 / 2 - v1 * v1; J[6] = (2. - gm1) * v1; J[7] = -gm1 * v2;
+template <typename T>
+__device__ __forceinline__ void vflux_jacobian(T* J, T gm1,
+                                               const T* w) {
+  T v1 = w[1], v2 = w[2], v3 = w[3], rho = w[0], pres = w[4];
+  T s2 = v1 * v1 + v2 * v2 + v3 * v3;
+  T c1 = ((gm1 - 1) * s2 / 2 - (gm1 + 1) / gm1 * pres / rho) * v1;
+  T c2 = (gm1 + 1) / gm1 * pres / rho + s2 / 2 - gm1 * v1 * v1;
+  J[0] = 0; J[1] = T(1.); J[2] = T(0.); J[3] = T(0.); J[4] = T(0.);
+  J[5] = gm1 * s2 / 2 - v1 * v1; J[6] = (T(2.) - gm1) * v1; J[7] = -gm1 * v2;
   J[8] = -gm1 * v3; J[9] = gm1;
-  J[10] = -v1 * v2; J[11] = v2; J[12] = v1; J[13] = 0.; J[14] = 0.;
-  J[15] = -v1 * v3; J[16] = v3; J[17] = 0.; J[18] = v1; J[19] = 0.;
+  J[10] = -v1 * v2; J[11] = v2; J[12] = v1; J[13] = T(0.); J[14] = T(0.);
+  J[15] = -v1 * v3; J[16] = v3; J[17] = T(0.); J[18] = v1; J[19] = T(0.);
   J[20] = c1; J[21] = c2; J[22] = -gm1 * v2 * v1; J[23] = -gm1 * v3 * v1;
   J[24] = (gm1 + 1) * v1;
 }
 
 // |A| = R |Lambda| R^-1 at the face between wl and wr (Roe average)
-__device__ __forceinline__ void vabs_jacobian(double* A, double gm1,
-                                              const double* wl,
-                                              const double* wr) {
-  double sqrtdl = sqrt(wl[0]), sqrtdr = sqrt(wr[0]);
-  double isdlpdr = 1.0 / (sqrtdl + sqrtdr);
-  double pr[5];
+template <typename T>
+__device__ __forceinline__ void vabs_jacobian(T* A, T gm1,
+                                              const T* wl,
+                                              const T* wr) {
+  T sqrtdl = sqrt(wl[0]), sqrtdr = sqrt(wr[0]);
+  T isdlpdr = T(1.0) / (sqrtdl + sqrtdr);
+  T pr[5];
   pr[0] = sqrtdl * sqrtdr;
   pr[1] = (sqrtdl * wl[1] + sqrtdr * wr[1]) * isdlpdr;
   pr[2] = (sqrtdl * wl[2] + sqrtdr * wr[2]) * isdlpdr;
   pr[3] = (sqrtdl * wl[3] + sqrtdr * wr[3]) * isdlpdr;
-  double el = wl[4] / gm1 +
-              0.5 * wl[0] * (wl[1] * wl[1] + wl[2] * wl[2] + wl[3] * wl[3]);
-  double er = wr[4] / gm1 +
-              0.5 * wr[0] * (wr[1] * wr[1] + wr[2] * wr[2] + wr[3] * wr[3]);
-  double hbar = ((el + wl[4]) / sqrtdl + (er + wr[4]) / sqrtdr) * isdlpdr;
-  pr[4] = (hbar - 0.5 * (pr[1] * pr[1] + pr[2] * pr[2] + pr[3] * pr[3])) *
-          gm1 / (gm1 + 1.) * pr[0];
-  double cs = sqrt(pr[4] * (gm1 + 1.) / pr[0]);
-  double r = pr[0], u = pr[1], v = pr[2], w = pr[3], p = pr[4];
-  double lam[5] = {fabs(u - cs), fabs(u), fabs(u + cs), fabs(u), fabs(u)};
-  double ke = 0.5 * (u * u + v * v + w * w);
-  double hp = (gm1 + 1.) / gm1 * p / r;
-  double h = hp + ke;
-  const double R[25] = {1.,         1., 1.,         0., 0.,  //
-                        u - cs,     u,  u + cs,     0., 0.,  //
-                        v,          v,  v,          1., 0.,  //
-                        w,          w,  w,          0., 1.,  //
+  T el = wl[4] / gm1 +
+              T(0.5) * wl[0] * (wl[1] * wl[1] + wl[2] * wl[2] + wl[3] * wl[3]);
+  T er = wr[4] / gm1 +
+              T(0.5) * wr[0] * (wr[1] * wr[1] + wr[2] * wr[2] + wr[3] * wr[3]);
+  T hbar = ((el + wl[4]) / sqrtdl + (er + wr[4]) / sqrtdr) * isdlpdr;
+  pr[4] = (hbar - T(0.5) * (pr[1] * pr[1] + pr[2] * pr[2] + pr[3] * pr[3])) *
+          gm1 / (gm1 + T(1.)) * pr[0];
+  T cs = sqrt(pr[4] * (gm1 + T(1.)) / pr[0]);
+  T r = pr[0], u = pr[1], v = pr[2], w = pr[3], p = pr[4];
+  T lam[5] = {fabs(u - cs), fabs(u), fabs(u + cs), fabs(u), fabs(u)};
+  T ke = T(0.5) * (u * u + v * v + w * w);
+  T hp = (gm1 + T(1.)) / gm1 * p / r;
+  T h = hp + ke;
+  const T R[25] = {T(1.),         T(1.), T(1.),         T(0.), T(0.),  //
+                        u - cs,     u,  u + cs,     T(0.), T(0.),  //
+                        v,          v,  v,          T(1.), T(0.),  //
+                        w,          w,  w,          T(0.), T(1.),  //
                         h - u * cs, ke, h + u * cs, v,  w};
-  const double Ri[25] = {(cs * ke + u * hp) / (2. * cs * hp),
-                         (-hp - cs * u) / (2. * cs * hp),
-                         -v / (2. * hp),
-                         -w / (2. * hp),
-                         1. / (2. * hp),
+  const T Ri[25] = {(cs * ke + u * hp) / (T(2.) * cs * hp),
+                         (-hp - cs * u) / (T(2.) * cs * hp),
+                         -v / (T(2.) * hp),
+                         -w / (T(2.) * hp),
+                         T(1.) / (T(2.) * hp),
                          (hp - ke) / hp,
                          u / hp,
                          v / hp,
                          w / hp,
-                         -1. / hp,
-                         (cs * ke - u * hp) / (2. * cs * hp),
-                         (hp - cs * u) / (2. * cs * hp),
-                         -v / (2. * hp),
-                         -w / (2. * hp),
-                         1. / (2. * hp),
-                         -v, 0., 1., 0., 0.,
-                         -w, 0., 0., 1., 0.};
-  double RL[25];
+                         -T(1.) / hp,
+                         (cs * ke - u * hp) / (T(2.) * cs * hp),
+                         (hp - cs * u) / (T(2.) * cs * hp),
+                         -v / (T(2.) * hp),
+                         -w / (T(2.) * hp),
+                         T(1.) / (T(2.) * hp),
+                         -v, T(0.), T(1.), T(0.), T(0.),
+                         -w, T(0.), T(0.), T(1.), T(0.)};
+  T RL[25];
 #pragma unroll
   for (int i = 0; i < 5; ++i)
 #pragma unroll
@@ -161,27 +165,18 @@ __device__ __forceinline__ void vic_prim(const real* u, size_t plane,
 }
 
 // the corrected-PE slope weights of layer k of n (centres x)
-__device__ __forceinline__ void vic_slope(const double* x, int n, int k,
-                                          double* wt, int* i0) {
-  if (k == 0) {
-    double a = x[1] - x[0], b = x[2] - x[1];
-    wt[0] = -(2. * a + b) / (a * (a + b));
-    wt[1] = (a + b) / (a * b);
-    wt[2] = -(a / ((a + b) * b));
-  } else if (k == n - 1) {
-    double c = x[n - 2] - x[n - 3], d = x[n - 1] - x[n - 2];
-    wt[0] = d / (c * (c + d));
-    wt[1] = -((c + d) / (c * d));
-    wt[2] = (c + 2. * d) / ((c + d) * d);
-  } else {
-    double hm = x[k] - x[k - 1], hp = x[k + 1] - x[k];
-    wt[0] = -hp / (hm * (hm + hp));
-    wt[1] = (hp - hm) / (hm * hp);
-    wt[2] = hm / (hp * (hm + hp));
-  }
+// the same weights from the block's x1 geometry table (computed once, with
+// these operations)
+__device__ __forceinline__ void vic_slope_tab(const BlockDev& B, int n, int k,
+                                              double* wt, int* i0) {
+  const double* t = B.x1tab + 6 * k;
+  wt[0] = t[0];
+  wt[1] = t[1];
+  wt[2] = t[2];
   int kc = k < 1 ? 1 : (k > n - 2 ? n - 2 : k);
   *i0 = kc - 1;
 }
+
 
 // the K rows of layer k: mid, lo, hi bands and the wall third points
 struct VicK {
@@ -189,14 +184,11 @@ struct VicK {
 };
 
 __device__ __forceinline__ VicK vic_krows(const BlockDev& B, int n, int k) {
-  const double* x = B.x1v + B.ng;
-  const double* f = B.x1f + B.ng;
   VicK K;
   double wt[3];
   int i0;
-  vic_slope(x, n, k, wt, &i0);
-  double h = f[k + 1] - f[k];
-  double gv = B.grav1 * (h * h / 12.);
+  vic_slope_tab(B, n, k, wt, &i0);
+  double gv = B.x1tab[6 * k + 3];  // grav1 h^2 / 12
   double bm = k == 0 ? wt[0] : (k == n - 1 ? wt[2] : wt[1]);
   double bl = k == 0 ? 0. : (k == n - 1 ? wt[1] : wt[0]);
   double bh = k == n - 1 ? 0. : (k == 0 ? wt[1] : wt[2]);
@@ -212,101 +204,126 @@ __device__ __forceinline__ VicK vic_krows(const BlockDev& B, int n, int k) {
 
 // (1) the blocks of every interior cell, the K coupling in their (IPR, IDN)
 // entries and du[IPR] -= K du0[IDN]
+// the blocks of interior cell e (column e / n, layer e % n) in the compute
+// type T: double, or float under implicit-precision float32 (the FP32
+// state's blocks; the block-tridiagonal solve stays FP64).  The FP64
+// instantiation performs the reference's operations in its order.
+template <typename T>
+__device__ __forceinline__ void vic_assemble_cell(const BlockDev& B,
+                                                  const VicScratch& S,
+                                                  const real* uin,
+                                                  double dtc, size_t e) {
+  const int ng = B.ng, nc1 = B.nc1, n = nc1 - 2 * ng;
+  const size_t plane = (size_t)nc1 * B.nc2 * B.nc3;
+  const T grav = T(B.grav1), gm1 = T(B.gammad - 1.);
+  const T area = T(B.dx3 * B.dx2), vol = T(B.dx3 * (B.dx2 * B.dx1));
+  const double* x1v = B.x1v + ng;
+  const double* x1f = B.x1f + ng;
+  const bool wood = n >= 3;
+  const int i = (int)(e % n);
+  const size_t col = e / n;
+  const size_t jrow = vic_row(B, col);
+  const size_t base = jrow * nc1 + ng;  // padded cell of layer 0
+  double wd[3][5];
+  vic_prim(uin, plane, base + i - 1, B.gammad, wd[0], B.base, nc1);
+  vic_prim(uin, plane, base + i, B.gammad, wd[1], B.base, nc1);
+  vic_prim(uin, plane, base + i + 1, B.gammad, wd[2], B.base, nc1);
+  T wl[5], wr[5], wn[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    wl[v] = T(wd[0][v]);
+    wr[v] = T(wd[1][v]);
+    wn[v] = T(wd[2][v]);
+  }
+  T Jp[25], Jc[25], Jn[25], Am[25], Ap[25];
+  const T gm1r = T(0.5 * (B.gammad + B.gammad) - 1.);
+  vflux_jacobian(Jp, gm1, wl);
+  vflux_jacobian(Jc, gm1, wr);
+  vabs_jacobian(Am, gm1r, wl, wr);
+  vflux_jacobian(Jn, gm1, wn);
+  vabs_jacobian(Ap, gm1r, wr, wn);
+  const T half_inv_vol = T(0.5) / vol;
+  const T lower = T(0.5) * area * T(x1v[i] - x1f[i]) / vol;
+  const T upper = T(0.5) * area * T(x1f[i + 1] - x1v[i]) / vol;
+  T a[25], b[25], c[25];
+#pragma unroll
+  for (int r = 0; r < 5; ++r)
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+      const int k = r * 5 + q;
+      T phi = (r == 1 && q == 0) || (r == 4 && q == 1) ? grav : T(0.);
+      a[k] = (Am[k] * area + Ap[k] * area + (area - area) * Jc[k]) *
+                 half_inv_vol - phi;
+      b[k] = -(Am[k] + Jp[k]) * area * half_inv_vol;
+      c[k] = -(Ap[k] - Jn[k]) * area * half_inv_vol;
+    }
+  const T rdt = T(1.) / T(dtc);
+#pragma unroll
+  for (int r = 0; r < 5; ++r) a[r * 5 + r] += rdt;
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    a[20 + k] -= grav * (upper * Ap[k] - lower * Am[k]);
+    b[20 + k] -= grav * lower * Am[k];
+    c[20 + k] += grav * upper * Ap[k];
+  }
+  a[21] += grav * (T(1.) - lower - upper);
+  b[21] -= grav * lower;
+  c[21] -= grav * upper;
+  const T bnd[5] = {T(1.), T(-1.), T(1.), T(1.), T(1.)};
+  if (i == 0)
+#pragma unroll
+    for (int r = 0; r < 5; ++r)
+#pragma unroll
+      for (int q = 0; q < 5; ++q) a[r * 5 + q] += b[r * 5 + q] * bnd[q];
+  if (i == n - 1)
+#pragma unroll
+    for (int r = 0; r < 5; ++r)
+#pragma unroll
+      for (int q = 0; q < 5; ++q) a[r * 5 + q] += c[r * 5 + q] * bnd[q];
+  const size_t cell = col * n + i;
+  double du0[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) {
+    du0[v] = S.du[v * S.cells + cell];
+    S.du0[v * S.cells + cell] = du0[v];
+  }
+  if (wood) {
+    VicK K = vic_krows(B, n, i);
+    a[20] -= T(K.mid) / T(dtc);
+    b[20] -= T(K.lo) / T(dtc);
+    c[20] -= T(K.hi) / T(dtc);
+    // du[IPR] -= (K du0[IDN])_i : the IDN row is read only (FP64 always)
+    const double* dn = S.du + col * n;
+    double s = K.mid * dn[i];
+    if (i >= 1) s += K.lo * dn[i - 1];
+    if (i <= n - 2) s += K.hi * dn[i + 1];
+    if (i == 0) s += K.t0 * dn[2];
+    if (i == n - 1) s += K.t1 * dn[n - 3];
+    S.du[4 * S.cells + cell] = du0[4] - s;
+  }
+#pragma unroll
+  for (int k = 0; k < 25; ++k) {
+    S.A[cell * 25 + k] = (double)a[k];
+    S.B[cell * 25 + k] = (double)b[k];
+    S.C[cell * 25 + k] = (double)c[k];
+  }
+}
+
 __global__ void __launch_bounds__(kThreads)
     vic_assemble_kernel(const BlockDev* __restrict__ tab, StageParams p) {
   const BlockDev& B = tab[blockIdx.y];
   if (!B.implicit) return;
   const VicScratch S = vic_scratch(B);
-  const int ng = B.ng, nc1 = B.nc1, n = nc1 - 2 * ng;
-  const size_t plane = (size_t)nc1 * B.nc2 * B.nc3;
   const real* uin = static_cast<const real*>(B.buf[p.in]);
   const double dtc = p.w2 * p.dt[blockIdx.y];
-  const double grav = B.grav1, gm1 = B.gammad - 1.;
-  const double area = B.dx3 * B.dx2, vol = B.dx3 * (B.dx2 * B.dx1);
-  const double* x1v = B.x1v + ng;
-  const double* x1f = B.x1f + ng;
-  const bool wood = n >= 3;
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < S.cells;
        e += (size_t)gridDim.x * blockDim.x) {
-    const int i = (int)(e % n);
-    const size_t col = e / n;
-    const size_t jrow = vic_row(B, col);
-    const size_t base = jrow * nc1 + ng;  // padded cell of layer 0
-    double wl[5], wr[5], wn[5];
-    vic_prim(uin, plane, base + i - 1, B.gammad, wl, B.base, nc1);
-    vic_prim(uin, plane, base + i, B.gammad, wr, B.base, nc1);
-    vic_prim(uin, plane, base + i + 1, B.gammad, wn, B.base, nc1);
-    double Jp[25], Jc[25], Jn[25], Am[25], Ap[25];
-    vflux_jacobian(Jp, gm1, wl);
-    vflux_jacobian(Jc, gm1, wr);
-    vabs_jacobian(Am, 0.5 * (B.gammad + B.gammad) - 1., wl, wr);
-    vflux_jacobian(Jn, gm1, wn);
-    vabs_jacobian(Ap, 0.5 * (B.gammad + B.gammad) - 1., wr, wn);
-    const double half_inv_vol = 0.5 / vol;
-    const double lower = 0.5 * area * (x1v[i] - x1f[i]) / vol;
-    const double upper = 0.5 * area * (x1f[i + 1] - x1v[i]) / vol;
-    double a[25], b[25], c[25];
-#pragma unroll
-    for (int r = 0; r < 5; ++r)
-#pragma unroll
-      for (int q = 0; q < 5; ++q) {
-        const int k = r * 5 + q;
-        double phi = (r == 1 && q == 0) || (r == 4 && q == 1) ? grav : 0.;
-        a[k] = (Am[k] * area + Ap[k] * area + (area - area) * Jc[k]) *
-                   half_inv_vol - phi;
-        b[k] = -(Am[k] + Jp[k]) * area * half_inv_vol;
-        c[k] = -(Ap[k] - Jn[k]) * area * half_inv_vol;
-      }
-    const double rdt = 1. / dtc;
-#pragma unroll
-    for (int r = 0; r < 5; ++r) a[r * 5 + r] += rdt;
-#pragma unroll
-    for (int k = 0; k < 5; ++k) {
-      a[20 + k] -= grav * (upper * Ap[k] - lower * Am[k]);
-      b[20 + k] -= grav * lower * Am[k];
-      c[20 + k] += grav * upper * Ap[k];
-    }
-    a[21] += grav * (1. - lower - upper);
-    b[21] -= grav * lower;
-    c[21] -= grav * upper;
-    const double bnd[5] = {1., -1., 1., 1., 1.};
-    if (i == 0)
-#pragma unroll
-      for (int r = 0; r < 5; ++r)
-#pragma unroll
-        for (int q = 0; q < 5; ++q) a[r * 5 + q] += b[r * 5 + q] * bnd[q];
-    if (i == n - 1)
-#pragma unroll
-      for (int r = 0; r < 5; ++r)
-#pragma unroll
-        for (int q = 0; q < 5; ++q) a[r * 5 + q] += c[r * 5 + q] * bnd[q];
-    const size_t cell = col * n + i;
-    double du0[5];
-#pragma unroll
-    for (int v = 0; v < 5; ++v) {
-      du0[v] = S.du[v * S.cells + cell];
-      S.du0[v * S.cells + cell] = du0[v];
-    }
-    if (wood) {
-      VicK K = vic_krows(B, n, i);
-      a[20] -= K.mid / dtc;
-      b[20] -= K.lo / dtc;
-      c[20] -= K.hi / dtc;
-      // du[IPR] -= (K du0[IDN])_i : the IDN row is read only
-      const double* dn = S.du + col * n;
-      double s = K.mid * dn[i];
-      if (i >= 1) s += K.lo * dn[i - 1];
-      if (i <= n - 2) s += K.hi * dn[i + 1];
-      if (i == 0) s += K.t0 * dn[2];
-      if (i == n - 1) s += K.t1 * dn[n - 3];
-      S.du[4 * S.cells + cell] = du0[4] - s;
-    }
-#pragma unroll
-    for (int k = 0; k < 25; ++k) {
-      S.A[cell * 25 + k] = a[k];
-      S.B[cell * 25 + k] = b[k];
-      S.C[cell * 25 + k] = c[k];
-    }
+#ifdef SG_REAL_IS_FLOAT
+    if (B.implicit_f32)
+      vic_assemble_cell<float>(B, S, uin, dtc, e);
+    else
+#endif
+      vic_assemble_cell<double>(B, S, uin, dtc, e);
   }
 }
 
@@ -662,16 +679,28 @@ constexpr int kVicWarps = 4;  // columns per CTA of the finish (a warp each)
 // column, one warp per column: the serial passes of the constituent column
 // (sums, face-mass prefix, availability clamp) on lane 0, the per-layer maps
 // on every lane
-__global__ void __launch_bounds__(32 * kVicWarps)
+template <int NL>
+__device__ __forceinline__ void vsync() {
+  if (NL > 1) vsync<NL>();
+}
+
+// NL lanes per column: 32 (a warp per column, kVicWarps per CTA: the serial
+// passes on lane 0, the per-layer maps on every lane) or 1 (a thread per
+// column, for batches with enough columns to fill the GPU: every FP64
+// instruction of the serial passes then serves 32 columns).  The operations
+// and their order are the same in both.
+template <int NL>
+__global__ void __launch_bounds__(NL == 32 ? 32 * kVicWarps : kThreads)
     vic_finish_kernel(const BlockDev* __restrict__ tab, StageParams p) {
   const BlockDev& B = tab[blockIdx.y];
   if (!B.implicit) return;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int lane = NL == 32 ? (threadIdx.x & 31) : 0;
   const VicScratch S = vic_scratch(B);
   const int ng = B.ng, nc1 = B.nc1, n = nc1 - 2 * ng;
   const size_t ncol = S.cells / n;
-  const size_t col = (size_t)blockIdx.x * kVicWarps + wid;
-  if (col >= ncol) return;
+  const size_t col = NL == 32 ? (size_t)blockIdx.x * kVicWarps + (threadIdx.x >> 5)
+                              : (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncol) return;  // whole warps leave together when NL = 32
   const size_t plane = (size_t)nc1 * B.nc2 * B.nc3;
   const real* uin = static_cast<const real*>(B.buf[p.in]);
   const real* u0 = static_cast<const real*>(B.buf[p.u0]);
@@ -694,14 +723,14 @@ __global__ void __launch_bounds__(32 * kVicWarps)
   double* mdn = mq + (n + 1);       // n: the dry-gas increment
   double* rho = mdn + n;            // n: the density of each layer
   if (ok) {
-    for (int i = lane; i < n; i += 32) {
+    for (int i = lane; i < n; i += NL) {
       double w[5];
       vic_prim(uin, plane, base + i, B.gammad, w, B.base, nc1);
       rho[i] = w[0];
       mdn[i] = 0.;
       mq[i] = (D[i * 5] - du[i]) * vol;  // staged: phi of layer i
     }
-    __syncwarp();
+    vsync<NL>();
     if (lane == 0) {
       double R = 0, Ssum = 0;
       for (int i = 0; i < n; ++i) {
@@ -730,8 +759,8 @@ __global__ void __launch_bounds__(32 * kVicWarps)
         avail = avail_up + q;
       }
     }
-    __syncwarp();
-    for (int i = lane; i < n; i += 32) {
+    vsync<NL>();
+    for (int i = lane; i < n; i += NL) {
       du[i] += mdn[i];
       du[cs + i] = D[i * 5 + 1];
       du[2 * cs + i] = D[i * 5 + 2];
@@ -746,16 +775,16 @@ __global__ void __launch_bounds__(32 * kVicWarps)
       double cw = -(dp_hi * mv_hi - dp_lo * mv_lo) / vol;
       du[4 * cs + i] = e + (pw + cw);
     }
-    __syncwarp();
+    vsync<NL>();
     if (wood) {
       // the remainder g1 sigma^2 s[du - du0] - K (raw - du0) of each layer,
       // from the final IDN row of its neighbours
       // staged in mdn (free again): every layer's work reads the IDN row
       // only, so the IPR row is written after all of them
-      for (int i = lane; i < n; i += 32) {
+      for (int i = lane; i < n; i += NL) {
         double wt[3];
         int i0;
-        vic_slope(x1v, n, i, wt, &i0);
+        vic_slope_tab(B, n, i, wt, &i0);
         VicK K = vic_krows(B, n, i);
         double mv0 = du[i0] - du0[i0], mv1 = du[i0 + 1] - du0[i0 + 1],
                mv2 = du[i0 + 2] - du0[i0 + 2];
@@ -772,15 +801,15 @@ __global__ void __launch_bounds__(32 * kVicWarps)
         wk -= s;
         mdn[i] = wk;
       }
-      __syncwarp();
-      for (int i = lane; i < n; i += 32) du[4 * cs + i] += mdn[i];
+      vsync<NL>();
+      for (int i = lane; i < n; i += NL) du[4 * cs + i] += mdn[i];
     }
-    __syncwarp();
+    vsync<NL>();
   }
   // the RK combine of the column (a failed column keeps the explicit du)
   const double* dsel = ok ? S.du + col * n : du0;
   const real w0 = real(p.w0), w1 = real(p.w1), w2 = real(p.w2);
-  for (int i = lane; i < n; i += 32) {
+  for (int i = lane; i < n; i += NL) {
     const size_t c = base + i;
 #pragma unroll
     for (int v = 0; v < NHYDRO; ++v) {

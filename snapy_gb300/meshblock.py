@@ -71,9 +71,9 @@ def scheme_of(options: MeshBlockOptions) -> dict:
         if h.icorr.scheme != 9:
             raise DeckError(f"integration/implicit-scheme {h.icorr.scheme}: the "
                             "full 5x5 scheme 9 is built")
-        if options.hydro().precision != "float64" and h.icorr.precision == "float32":
-            raise DeckError("integration/implicit-precision float32 is not built "
-                            "(the implicit solve runs in FP64)")
+        if options.hydro().precision == "float64" and h.icorr.precision == "float32":
+            raise DeckError("integration/implicit-precision float32 needs "
+                            "dynamics/precision float32")
     if c.nx3 > 1:
         if h.diffusion is not None and h.diffusion.nu_iso:
             raise DeckError("3-D blocks are built without forcing/diffusion")
@@ -116,7 +116,9 @@ def block_of(options: MeshBlockOptions, tj: int = 0) -> dict:
             "flux_cov": h.flux_covariance,
             "wb_wall_clamp": bool(h.extra.get("wb-wall-clamp", True)),
             "x1f": x1f, "x1v": x1v,
-            "implicit_scheme": h.icorr.scheme if h.icorr else 0}
+            "implicit_scheme": h.icorr.scheme if h.icorr else 0,
+            # FP32 assembly of the implicit blocks (the solve stays FP64)
+            "implicit_f32": bool(h.icorr) and h.icorr.precision == "float32"}
 
 
 @dataclass

@@ -118,6 +118,7 @@ def _descs(slots: List[_Slot]):
         a.x1f = sl.x1f.data_ptr()
         a.x1v = sl.x1v.data_ptr()
         a.implicit_scheme = int(d.get("implicit_scheme", 0))
+        a.implicit_precision = _lib.F32 if d.get("implicit_f32") else _lib.F64
         a.base = sl.base.data_ptr() if sl.base is not None else None
     return arr
 

@@ -43,10 +43,15 @@ def interior(opts, u):
     return u[:, :, ng:c.nc2 - ng, ng:c.nc1 - ng]
 
 
-@pytest.mark.parametrize("deck", ["straka_noimplicit.yaml", "straka.yaml"])
-def test_fp32_anomaly_against_fp64_oracle(oracle, cuda, deck):
+@pytest.mark.parametrize("deck,iprec", [("straka_noimplicit.yaml", None),
+                                        ("straka.yaml", "float64"),
+                                        ("straka.yaml", "float32")])
+def test_fp32_anomaly_against_fp64_oracle(oracle, cuda, deck, iprec):
+    """iprec float32: the implicit blocks assembled in FP32 (the solve FP64)."""
     nx1, nx2, nstep, dt = 48, 64, 40, 0.1
     opts = straka_window(deck, nx1, nx2, "float32")
+    if iprec:
+        opts.hydro().icorr.precision = iprec
     blk = sg.MeshBlock(opts).to(cuda)
     assert blk.dtype == torch.float32
     w = problems.straka(opts, "cpu", xc=1600.0, zc=1200.0, xr=800.0, zr=600.0)
@@ -64,7 +69,7 @@ def test_fp32_anomaly_against_fp64_oracle(oracle, cuda, deck):
     assert blk.check_redo(vars) == 0
     got = blk.total_u(vars).cpu().numpy()
     err = rel_l2(interior(opts, got), interior(opts, u))
-    print(f"\n{deck}: FP32 anomaly vs FP64 oracle after {nstep} steps, "
+    print(f"\n{deck} (implicit-precision {iprec}): FP32 anomaly vs FP64 oracle after {nstep} steps, "
           f"rel L2 per field (rho, m1, m2, m3, E): "
           + " ".join(f"{e:.2e}" for e in err))
     for v in (0, 1, 2, 4):

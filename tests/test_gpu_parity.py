@@ -293,3 +293,28 @@ def test_implicit_rest_state_balanced(cuda):
     for _ in range(10):
         blk.step(vars, 0.1)
     assert blk.prim()[1:4].abs().max().item() < 1e-9
+
+
+def test_implicit_wide_batch_parity(oracle, cuda):
+    """A block with columns enough to fill every SM sub-partition (20480)
+    takes the thread-per-column finish of the implicit solve: the same
+    operations in the same order, so parity holds as for the warp form."""
+    opts = sg.MeshBlockOptions.from_yaml(STRAKA_VIC)
+    c = opts.coord()
+    c.nx1, c.nx2 = 6, 20480
+    c.x1max, c.x2max = 6 * 50.0, 20480 * 50.0
+    opts.execution = "eager"
+    blk = sg.MeshBlock(opts).to(cuda)
+    w = problems.straka(opts, "cpu", xc=5000.0, zc=150.0, xr=2000.0, zr=100.0)
+    vars = {"hydro_w": w.to(cuda)}
+    blk.initialize(vars)
+    ob = oracle_block(oracle, opts)
+    u = ob.initialize(w.numpy())
+    for step in range(2):
+        dt = blk.max_time_step(vars)
+        for s in range(3):
+            blk.forward(vars, dt, s)
+            ob.stage(u, dt, s)
+        assert blk.check_redo(vars) == 0
+        err = rel_l2(vars["hydro_u"].cpu().numpy(), u)
+        assert err.max() <= TOL, (step, err)
