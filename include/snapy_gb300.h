@@ -172,6 +172,60 @@ int sg_kernel_times(sg_handle* h, double* ms, int64_t* launches);
 const char* sg_last_error(void);
 const char* sg_version(void);
 
+/* ---------------------------------------------------------------------
+ * The cubed sphere: shallow water on six gnomonic-equiangle panels of n x n
+ * cells (nghost 3, one radial cell), all in one handle.  The state is one
+ * buffer (6, 4, n + 6, n + 6) of the dtype per RK buffer: the geopotential
+ * Phi, the radial and the two covariant tangential momenta.  Replaces, for
+ * this layout, the hydro stage with the gnomonic coordinate
+ * (src/coord/gnomonic_equiangle.cpp:357-521, shallow_roe with dir yz,
+ * src/riemann/riemann_kernels.h:447-495), the seam flux single-valuing
+ * (src/layout/seam_register.cpp:35) and the cross-panel ghost exchange
+ * with edge interpolation (src/layout/cubed_sphere_layout.cpp:563-803,
+ * src/coord/gnomonic_equiangle.cpp:307-325,536-609) -- the exchange here is
+ * one gather over the six panels of this GPU.
+ * --------------------------------------------------------------------- */
+typedef struct sg_cs_handle sg_cs_handle;
+typedef struct sg_cs_desc {
+  int32_t n, ng, dtype, nstage;
+  double wght[3][3];
+  double cfl;
+  /* FP64 geometry on the device, one block of nc = n + 6: cos_c, sin_c, vol,
+   * x_ov_rD, y_ov_rC, width2, width3 ([nc][nc] each, x3 index slowest), then
+   * cos_f2, sin_f2, area2 ([nc][nc + 1] each), cos_f3, sin_f3, area3
+   * ([nc + 1][nc] each) */
+  const double* geo;
+  /* the seam halo: nghost rows of 24 doubles (dst, src0, src1 flat cell
+   * indices (panel nc + k) nc + j, the fraction x toward src1, per source
+   * its cosine and unit alpha/beta tangents, the ghost's tangents) */
+  const double* ghost_tab;
+  int32_t nghost;
+  /* the seam faces the non-owning panel takes: nseam rows of 18 doubles
+   * (dst direction 2|3, dst flat face, src direction, src flat face, sign,
+   * the source face cosine, source tangents, destination tangents) */
+  const double* seam_tab;
+  int32_t nseam;
+} sg_cs_desc;
+
+int sg_cs_create(const sg_cs_desc* desc, sg_cs_handle** out);
+int sg_cs_destroy(sg_cs_handle* h);
+/* the face-flux scratch the caller allocates and binds with the buffers */
+int sg_cs_scratch_bytes(const sg_cs_handle* h, size_t* bytes);
+int sg_cs_bind(sg_cs_handle* h, void* buf0, void* buf1, void* buf2,
+               void* scratch, size_t bytes);
+int sg_cs_set_current(sg_cs_handle* h, int32_t current);
+int sg_cs_rotation(const sg_cs_handle* h, int32_t* cur, int32_t* base);
+int sg_cs_set_rotation(sg_cs_handle* h, int32_t cur, int32_t base);
+int sg_cs_advance(sg_cs_handle* h, int32_t stage);
+/* one RK stage of all six panels, ending with the seam halo fill of the
+ * new state; dt_dev points at one device double */
+int sg_cs_stage(sg_cs_handle* h, int32_t stage, const double* dt_dev,
+                sg_stream_t stream);
+/* the seam halo of the current buffer (after loading a state) */
+int sg_cs_fill_seams(sg_cs_handle* h, sg_stream_t stream);
+/* dt_dev = cfl min over the interior of width / (|v| + sqrt(Phi)) */
+int sg_cs_max_dt(sg_cs_handle* h, double* dt_dev, sg_stream_t stream);
+
 /* Allocation-free time step.  No counterpart in the reference: it is for
  * callers that may not allocate device memory at all (a host that hands in
  * views of its own pre-allocated arena, a serving loop held to a fixed HBM

@@ -107,6 +107,9 @@ def lib():
         L.og_implicit.argtypes = [bp, _dp, ctypes.c_double, _dp]
         L.og_ref_column.argtypes = [bp, _dp, ctypes.c_size_t, _dp, _dp, _dp,
                                     _dp, _dp, _dp]
+        L.og_recon_batch.argtypes = [_dp, ctypes.c_long, ctypes.c_int,
+                                     ctypes.c_int, ctypes.c_int, _dp]
+        L.og_shallow_roe_batch.argtypes = [_dp, _dp, ctypes.c_long, ctypes.c_int, _dp]
         _lib = L
     return _lib
 

@@ -1092,3 +1092,57 @@ void og_initialize(const og_block* b, double* w, double* u) {
   og_prim2cons(b, w, u);
   og_apply_bc(b, u, 0);
 }
+
+/* ------------------------------------------------------------------ */
+/* batched face helpers for the cubed-sphere oracle (numpy plumbing)  */
+/* ------------------------------------------------------------------ */
+/* n 5-cell stencils (row-major n x 5): weno5 (weno != 0) or cp5, side 1 the
+ * cp row (the ILT state of the face above cell 2), 0 the cm row */
+void og_recon_batch(const double* st, long n, int weno, int side, int scale,
+                    double* out) {
+  build_tables();
+#pragma omp parallel for schedule(static) if (n > 4096)
+  for (long q = 0; q < n; ++q)
+    out[q] = weno ? og_weno5_face(st + 5 * q, side, scale)
+                  : og_cp5_face(st + 5 * q, side);
+}
+
+/* shallow_roe_impl (src/riemann/riemann_kernels.h:447-495) with dir yz:
+ * n faces, states wl, wr (n x 4: IDN = geopotential, IVX, IVY, IVZ), dim 2
+ * (x2 faces: normal IVY) or 1 (x3 faces: normal IVZ) */
+void og_shallow_roe_batch(const double* wl, const double* wr, long n, int dim,
+                          double* flx) {
+#pragma omp parallel for schedule(static) if (n > 4096)
+  for (long q = 0; q < n; ++q) {
+    const double* L = wl + 4 * q;
+    const double* R = wr + 4 * q;
+    double* F = flx + 4 * q;
+    const int ivx = dim == 2 ? 2 : 3, ivy = dim == 2 ? 3 : 2, ivz = 1;
+    double sqrtdl = sqrt(L[0]), sqrtdr = sqrt(R[0]);
+    double isdlpdr = 1. / (sqrtdl + sqrtdr);
+    double ubar = (L[ivx] * sqrtdl + R[ivx] * sqrtdr) * isdlpdr;
+    double vbar = (L[ivy] * sqrtdl + R[ivy] * sqrtdr) * isdlpdr;
+    double cbar = sqrt(0.5 * (L[0] + R[0]));
+    double del0 = R[0] - L[0], delx = R[ivx] - L[ivx], dely = R[ivy] - L[ivy];
+    double hbar = sqrt(L[0] * R[0]);
+    double a1 = 0.5 * (cbar * del0 - hbar * delx) / cbar;
+    double a2 = hbar * dely;
+    double a3 = 0.5 * (cbar * del0 + hbar * delx) / cbar;
+    double w0[4] = {0, 0, 0, 0}, w1[4] = {0, 0, 0, 0}, w2[4] = {0, 0, 0, 0};
+    w0[0] = a1;
+    w0[ivx] = a1 * (ubar - cbar);
+    w0[ivy] = a1 * vbar;
+    w1[ivy] = a2;
+    w2[0] = a3;
+    w2[ivx] = a3 * (ubar + cbar);
+    w2[ivy] = a3 * vbar;
+    double s0 = fabs(ubar - cbar), s1 = fabs(ubar), s2 = fabs(ubar + cbar);
+    F[0] = 0.5 * (L[0] * L[ivx] + R[0] * R[ivx]);
+    F[ivx] = 0.5 * (L[0] * L[ivx] * L[ivx] + 0.5 * L[0] * L[0] +
+                    R[0] * R[ivx] * R[ivx] + 0.5 * R[0] * R[0]);
+    F[ivy] = 0.5 * (L[0] * L[ivx] * L[ivy] + R[0] * R[ivx] * R[ivy]);
+    F[ivz] = 0;
+    for (int v = 0; v < 4; ++v)
+      F[v] -= 0.5 * (s0 * w0[v] + s1 * w1[v] + s2 * w2[v]);
+  }
+}

@@ -98,6 +98,12 @@ double og_max_dt(const og_block* b, const double* w);
 /* initialize: boundaries on w, W->U, boundaries on u */
 void og_initialize(const og_block* b, double* w, double* u);
 
+/* batched face helpers of the cubed-sphere oracle (oracle/cubed_sphere.py) */
+void og_recon_batch(const double* st, long n, int weno, int side, int scale,
+                    double* out);
+void og_shallow_roe_batch(const double* wl, const double* wr, long n, int dim,
+                          double* flx);
+
 #ifdef __cplusplus
 }
 #endif

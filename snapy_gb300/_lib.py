@@ -74,6 +74,14 @@ KERNELS = ("stage_kernel", "vic_assemble_kernel", "vic_solve_kernel",
            "vic_finish_kernel", "ghost_kernel", "x3_kernel")
 
 
+class CsDesc(ctypes.Structure):
+    """sg_cs_desc: the cubed-sphere handle's grid, scheme and tables."""
+    _fields_ = [("n", _i32), ("ng", _i32), ("dtype", _i32), ("nstage", _i32),
+                ("wght", (ctypes.c_double * 3) * 3), ("cfl", ctypes.c_double),
+                ("geo", _vp), ("ghost_tab", _vp), ("nghost", _i32),
+                ("seam_tab", _vp), ("nseam", _i32)]
+
+
 # every symbol include/snapy_gb300.h declares, with its ctypes signature
 SIGNATURES = {
     "sg_create": (ctypes.c_int, [ctypes.POINTER(Scheme), ctypes.POINTER(BlockDesc),
@@ -103,6 +111,17 @@ SIGNATURES = {
     "sg_version": (ctypes.c_char_p, []),
     "sg_max_dt_noalloc": (ctypes.c_int, [ctypes.POINTER(DtBlock), _i32, _i32,
                                          ctypes.c_double, _vp, _vp, _vp]),
+    "sg_cs_create": (ctypes.c_int, [ctypes.POINTER(CsDesc), ctypes.POINTER(_vp)]),
+    "sg_cs_destroy": (ctypes.c_int, [_vp]),
+    "sg_cs_scratch_bytes": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_size_t)]),
+    "sg_cs_bind": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, ctypes.c_size_t]),
+    "sg_cs_set_current": (ctypes.c_int, [_vp, _i32]),
+    "sg_cs_rotation": (ctypes.c_int, [_vp, ctypes.POINTER(_i32), ctypes.POINTER(_i32)]),
+    "sg_cs_set_rotation": (ctypes.c_int, [_vp, _i32, _i32]),
+    "sg_cs_advance": (ctypes.c_int, [_vp, _i32]),
+    "sg_cs_stage": (ctypes.c_int, [_vp, _i32, _vp, _vp]),
+    "sg_cs_fill_seams": (ctypes.c_int, [_vp, _vp]),
+    "sg_cs_max_dt": (ctypes.c_int, [_vp, _vp, _vp]),
 }
 
 _lib = None

@@ -1,0 +1,619 @@
+// The cubed-sphere shallow-water stage: six gnomonic-equiangle panels of
+// n x n cells (nghost 3, one radial cell) in ONE handle, FP64 or FP32 state
+// (6, 4, nc, nc): Phi, the radial and the two covariant tangential momenta.
+//
+// A stage is four launches, each over all six panels:
+//   cs_flux_kernel       every x2 and x3 face of the panels' interiors: the
+//                        primitives of its six-cell stencil (U/Phi, momenta
+//                        raised by the cell cosine), weno5 for Phi and cp5
+//                        for the velocities, the face-frame rotation, the
+//                        shallow-roe flux (dir yz) and its rotation back to
+//                        covariant components
+//                        (src/riemann/riemann.cpp:219-346 with
+//                        src/coord/gnomonic_equiangle.cpp:357-463,
+//                        src/riemann/riemann_kernels.h:447-495)
+//   cs_seam_flux_kernel  the seam faces of the non-owning panels take the
+//                        owner's flux through the global frame
+//                        (src/layout/seam_register.cpp:35)
+//   cs_update_kernel     (A2 dF2 + A3 dF3) / V minus the metric sources,
+//                        du = -dt div, and the RK combine
+//                        (src/coord/coordinate.cpp:618-662,
+//                        src/coord/gnomonic_equiangle.cpp:465-521)
+//   cs_ghost_kernel      the seam halo: a gather along the neighbour's edge
+//                        row with the momenta through the global frame
+//                        (src/layout/cubed_sphere_layout.cpp:563-803,
+//                        src/coord/gnomonic_equiangle.cpp:536-609)
+// All the seam geometry is in two tables built once on the host; the
+// kernels only gather.  Built with -fmad=false: FP64 runs the checker's
+// operations in its order.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include <string>
+
+#include "../../include/snapy_gb300.h"
+#include "sg_device.cuh"
+
+extern "C" int sg_fail_message(int code, const char* msg);
+
+namespace {
+
+using sg::IDN;
+using sg::IVX;
+using sg::IVY;
+using sg::IVZ;
+
+constexpr int kThreads = 256;
+constexpr int kNg = 3;
+constexpr int kGhostStride = 24;
+constexpr int kSeamStride = 18;
+
+// offsets of the geometry arrays in the device block (see sg_cs_desc)
+struct Geo {
+  const double *cos_c, *sin_c, *vol, *xr, *yr, *w2, *w3;
+  const double *cos_f2, *sin_f2, *a2, *cos_f3, *sin_f3, *a3;
+};
+
+__host__ __device__ inline Geo geo_of(const double* g, int nc) {
+  const size_t c = (size_t)nc * nc, f = (size_t)nc * (nc + 1);
+  Geo o;
+  o.cos_c = g;
+  o.sin_c = g + c;
+  o.vol = g + 2 * c;
+  o.xr = g + 3 * c;
+  o.yr = g + 4 * c;
+  o.w2 = g + 5 * c;
+  o.w3 = g + 6 * c;
+  o.cos_f2 = g + 7 * c;
+  o.sin_f2 = o.cos_f2 + f;
+  o.a2 = o.sin_f2 + f;
+  o.cos_f3 = o.a2 + f;
+  o.sin_f3 = o.cos_f3 + f;
+  o.a3 = o.sin_f3 + f;
+  return o;
+}
+
+struct CsParams {
+  int n, nc;
+  const double* geo;
+  const double* gtab;
+  int nghost;
+  const double* stab;
+  int nseam;
+  const void* in;
+  const void* u0;
+  void* out;
+  void* f2;
+  void* f3;
+  const double* dt;
+  double w0, w1, w2;
+};
+
+// U -> W of one cell: v = m / Phi, the tangential pair raised by cos
+template <typename T>
+__device__ __forceinline__ void sw_prim(const T* q, size_t pst, size_t c,
+                                        T cs, T* w) {
+  const T phi = q[c];
+  w[IDN] = phi;
+  const T v1 = q[pst + c] / phi, v2 = q[2 * pst + c] / phi,
+          v3 = q[3 * pst + c] / phi;
+  const T sth2 = T(1.) - cs * cs;
+  w[IVX] = v1;
+  w[IVY] = v2 / sth2 - v3 * cs / sth2;
+  w[IVZ] = -v2 * cs / sth2 + v3 / sth2;
+}
+
+// shallow_roe_impl with dir yz: DIM 2 (x2 faces, normal IVY) or 1 (x3)
+template <typename T, int DIM>
+__device__ __forceinline__ void shallow_roe(const T* L, const T* R, T* F) {
+  constexpr int ivx = DIM == 2 ? IVY : IVZ, ivy = DIM == 2 ? IVZ : IVY,
+                ivz = IVX;
+  T sqrtdl = sqrt(L[0]), sqrtdr = sqrt(R[0]);
+  T isdlpdr = T(1.) / (sqrtdl + sqrtdr);
+  T ubar = (L[ivx] * sqrtdl + R[ivx] * sqrtdr) * isdlpdr;
+  T vbar = (L[ivy] * sqrtdl + R[ivy] * sqrtdr) * isdlpdr;
+  T cbar = sqrt(T(0.5) * (L[0] + R[0]));
+  T del0 = R[0] - L[0], delx = R[ivx] - L[ivx], dely = R[ivy] - L[ivy];
+  T hbar = sqrt(L[0] * R[0]);
+  T a1 = T(0.5) * (cbar * del0 - hbar * delx) / cbar;
+  T a2 = hbar * dely;
+  T a3 = T(0.5) * (cbar * del0 + hbar * delx) / cbar;
+  T w0[4] = {0, 0, 0, 0}, w1[4] = {0, 0, 0, 0}, w2[4] = {0, 0, 0, 0};
+  w0[0] = a1;
+  w0[ivx] = a1 * (ubar - cbar);
+  w0[ivy] = a1 * vbar;
+  w1[ivy] = a2;
+  w2[0] = a3;
+  w2[ivx] = a3 * (ubar + cbar);
+  w2[ivy] = a3 * vbar;
+  T s0 = fabs(ubar - cbar), s1 = fabs(ubar), s2 = fabs(ubar + cbar);
+  F[0] = T(0.5) * (L[0] * L[ivx] + R[0] * R[ivx]);
+  F[ivx] = T(0.5) * (L[0] * L[ivx] * L[ivx] + T(0.5) * L[0] * L[0] +
+                     R[0] * R[ivx] * R[ivx] + T(0.5) * R[0] * R[0]);
+  F[ivy] = T(0.5) * (L[0] * L[ivx] * L[ivy] + R[0] * R[ivx] * R[ivy]);
+  F[ivz] = 0;
+#pragma unroll
+  for (int v = 0; v < 4; ++v)
+    F[v] -= T(0.5) * (s0 * w0[v] + s1 * w1[v] + s2 * w2[v]);
+}
+
+// the faces: thread e < 6 n (n + 1) an x2 face (panel, row k, face j), the
+// rest x3 faces (panel, face k, column j)
+template <typename T>
+__global__ void __launch_bounds__(kThreads) cs_flux_kernel(CsParams P) {
+  const int n = P.n, nc = P.nc;
+  const size_t pst = (size_t)nc * nc;  // one variable of a panel
+  const Geo G = geo_of(P.geo, nc);
+  const T* U = static_cast<const T*>(P.in);
+  const size_t nf = (size_t)6 * n * (n + 1);
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < 2 * nf;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const bool x2 = e < nf;
+    const size_t r = x2 ? e : e - nf;
+    int p, k, j;
+    if (x2) {  // faces j = ng..ng+n of rows k = ng..ng+n-1
+      j = kNg + (int)(r % (n + 1));
+      k = kNg + (int)((r / (n + 1)) % n);
+      p = (int)(r / ((size_t)(n + 1) * n));
+    } else {  // faces k = ng..ng+n of columns j = ng..ng+n-1
+      j = kNg + (int)(r % n);
+      k = kNg + (int)((r / n) % (n + 1));
+      p = (int)(r / ((size_t)n * (n + 1)));
+    }
+    const T* q = U + (size_t)p * 4 * pst;
+    T st[6][4];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) {
+      const int kk = x2 ? k : k - 3 + m, jj = x2 ? j - 3 + m : j;
+      const size_t c = (size_t)kk * nc + jj;
+      sw_prim<T>(q, pst, c, T(G.cos_c[c]), st[m]);
+    }
+    T wl[4], wr[4], F[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      if (v == IDN) {
+        wl[v] = sg::weno5_cp<T>(st[0][v], st[1][v], st[2][v], st[3][v], st[4][v], false);
+        wr[v] = sg::weno5_cm<T>(st[1][v], st[2][v], st[3][v], st[4][v], st[5][v], false);
+      } else {
+        wl[v] = sg::cp5_cp<T>(st[0][v], st[1][v], st[2][v], st[3][v], st[4][v]);
+        wr[v] = sg::cp5_cm<T>(st[1][v], st[2][v], st[3][v], st[4][v], st[5][v]);
+      }
+    }
+    const size_t fidx = x2 ? (size_t)k * (nc + 1) + j : (size_t)k * nc + j;
+    const T cs = T(x2 ? G.cos_f2[fidx] : G.cos_f3[fidx]);
+    const T sn = T(x2 ? G.sin_f2[fidx] : G.sin_f3[fidx]);
+    const T gi = T(1.0) / (sn * sn);
+    // to the face-local orthonormal frame (prim2local2_ / 3_)
+    auto to_face = [&](T* w) {
+      const T uu2 = w[IVY], uu3 = w[IVZ];
+      if (x2) {
+        const T T22 = T(1.0) / sqrt(gi), T32 = cs / sqrt(T(1.0)),
+                T33 = sqrt(T(1.0));
+        w[IVZ] = T32 * uu2 + T33 * uu3;
+        w[IVY] = T22 * uu2;
+      } else {
+        const T T22 = sqrt(T(1.0)), T23 = cs / sqrt(T(1.0)),
+                T33 = T(1.0) / sqrt(gi);
+        w[IVY] = T22 * uu2 + T23 * uu3;
+        w[IVZ] = T33 * uu3;
+      }
+    };
+    to_face(wl);
+    to_face(wr);
+    if (x2)
+      shallow_roe<T, 2>(wl, wr, F);
+    else
+      shallow_roe<T, 1>(wl, wr, F);
+    // back to covariant fluxes (flux2global2_ / 3_)
+    const T txy = F[IVY], txz = F[IVZ];
+    if (x2) {
+      const T T22 = sqrt(gi), T32 = -sqrt(gi) * cs / T(1.0),
+              T33 = T(1.0) / sqrt(T(1.0));
+      F[IVZ] = T32 * txy + T33 * txz;
+      F[IVY] = T22 * txy;
+    } else {
+      const T T22 = T(1.0) / sqrt(T(1.0)), T23 = -cs / T(1.0) * sqrt(gi),
+              T33 = sqrt(gi);
+      F[IVY] = T22 * txy + T23 * txz;
+      F[IVZ] = T33 * txz;
+    }
+    const T ty = F[IVY], tz = F[IVZ];
+    F[IVY] = ty + tz * cs;
+    F[IVZ] = tz + ty * cs;
+    T* out = static_cast<T*>(x2 ? P.f2 : P.f3);
+    const size_t fst = (size_t)nc * (nc + 1);  // one variable of a panel's faces
+#pragma unroll
+    for (int v = 0; v < 4; ++v) out[((size_t)p * 4 + v) * fst + fidx] = F[v];
+  }
+}
+
+// the owner's covariant flux pair raised at its face and projected on the
+// destination face's tangents, signed
+template <typename T>
+__global__ void __launch_bounds__(kThreads) cs_seam_flux_kernel(CsParams P) {
+  const int nc = P.nc;
+  const size_t fst = (size_t)nc * (nc + 1);
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < P.nseam;
+       e += gridDim.x * blockDim.x) {
+    const double* r = P.stab + (size_t)e * kSeamStride;
+    T* dst = static_cast<T*>((int)r[0] == 2 ? P.f2 : P.f3);
+    const T* src = static_cast<const T*>((int)r[2] == 2 ? P.f2 : P.f3);
+    const size_t di = (size_t)r[1], si = (size_t)r[3];
+    const size_t dp = di / fst, dc = di % fst, sp = si / fst, sc = si % fst;
+    auto at = [&](const T* a, size_t pn, int v, size_t c) {
+      return a[(pn * 4 + v) * fst + c];
+    };
+    const T sign = T(r[4]), c = T(r[5]);
+    const T m2 = at(src, sp, IVY, sc), m3 = at(src, sp, IVZ, sc);
+    const T s2 = T(1.) - c * c;
+    const T v2 = m2 / s2 - m3 * c / s2;
+    const T v3 = -m2 * c / s2 + m3 / s2;
+    T V[3];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) V[q] = T(r[6 + q]) * v2 + T(r[9 + q]) * v3;
+    const T fd = at(src, sp, IDN, sc), fr = at(src, sp, IVX, sc);
+    const T y = (V[0] * T(r[12]) + V[1] * T(r[13])) + V[2] * T(r[14]);
+    const T z = (V[0] * T(r[15]) + V[1] * T(r[16])) + V[2] * T(r[17]);
+    dst[(dp * 4 + IDN) * fst + dc] = sign * fd;
+    dst[(dp * 4 + IVX) * fst + dc] = sign * fr;
+    dst[(dp * 4 + IVY) * fst + dc] = sign * y;
+    dst[(dp * 4 + IVZ) * fst + dc] = sign * z;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) cs_update_kernel(CsParams P) {
+  const int n = P.n, nc = P.nc;
+  const size_t pst = (size_t)nc * nc, f2st = (size_t)nc * (nc + 1),
+               f3st = (size_t)(nc + 1) * nc;
+  const Geo G = geo_of(P.geo, nc);
+  const T* U = static_cast<const T*>(P.in);
+  const T* U0 = static_cast<const T*>(P.u0);
+  T* O = static_cast<T*>(P.out);
+  const T* F2 = static_cast<const T*>(P.f2);
+  const T* F3 = static_cast<const T*>(P.f3);
+  const T mdt = T(-P.dt[0]);
+  const T w0 = T(P.w0), w1 = T(P.w1), w2 = T(P.w2);
+  const size_t total = (size_t)6 * n * n;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const int j = kNg + (int)(e % n);
+    const int k = kNg + (int)((e / n) % n);
+    const int p = (int)(e / ((size_t)n * n));
+    const size_t c = (size_t)k * nc + j;
+    const T* q = U + (size_t)p * 4 * pst;
+    T w[4];
+    sw_prim<T>(q, pst, c, T(G.cos_c[c]), w);
+    const size_t i2 = (size_t)k * (nc + 1) + j, i3 = (size_t)k * nc + j;
+    const T a2lo = T(G.a2[i2]), a2hi = T(G.a2[i2 + 1]);
+    const T a3lo = T(G.a3[i3]), a3hi = T(G.a3[i3 + nc]);
+    const T vol = T(G.vol[c]);
+    T div[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const T* f2 = F2 + ((size_t)p * 4 + v) * f2st;
+      const T* f3 = F3 + ((size_t)p * 4 + v) * f3st;
+      const T d2 = a2hi * f2[i2 + 1] - a2lo * f2[i2];
+      const T d3 = a3hi * f3[i3 + nc] - a3lo * f3[i3];
+      div[v] = (d2 + d3) / vol;
+    }
+    const T pr = T(0.5) * (w[IDN] * w[IDN]);
+    const T sn = T(G.sin_c[c]);
+    const T sine2 = sn * sn;
+    div[IVY] -= T(G.xr[c]) * (pr + w[IDN] * w[IVZ] * w[IVZ] * sine2);
+    div[IVZ] -= T(G.yr[c]) * (pr + w[IDN] * w[IVY] * w[IVY] * sine2);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const size_t qi = ((size_t)p * 4 + v) * pst + c;
+      const T du = mdt * div[v];
+      O[qi] = w0 * U0[qi] + w1 * U[qi] + w2 * du;
+    }
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) cs_ghost_kernel(CsParams P, void* buf) {
+  const int nc = P.nc;
+  const size_t pst = (size_t)nc * nc;
+  T* Q = static_cast<T*>(buf);
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < P.nghost;
+       e += gridDim.x * blockDim.x) {
+    const double* r = P.gtab + (size_t)e * kGhostStride;
+    const size_t d = (size_t)r[0], s0 = (size_t)r[1], s1 = (size_t)r[2];
+    // flat (panel, k, j) -> the variable v of that cell
+    auto at = [&](size_t f, int v) -> size_t {
+      return ((f / pst) * 4 + v) * pst + f % pst;
+    };
+    const T x = T(r[3]);
+#pragma unroll
+    for (int v = IDN; v <= IVX; ++v) {
+      const T a = Q[at(s0, v)], b = Q[at(s1, v)];
+      Q[at(d, v)] = a + x * (b - a);
+    }
+    T V0[3], V1[3];
+    const size_t src[2] = {s0, s1};
+    T* Vs[2] = {V0, V1};
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      const double* g = r + 4 + 7 * s;
+      const T c = T(g[0]);
+      const T m2 = Q[at(src[s], IVY)], m3 = Q[at(src[s], IVZ)];
+      const T s2 = T(1.) - c * c;
+      const T v2 = m2 / s2 - m3 * c / s2;
+      const T v3 = -m2 * c / s2 + m3 / s2;
+#pragma unroll
+      for (int qq = 0; qq < 3; ++qq) Vs[s][qq] = T(g[1 + qq]) * v2 + T(g[4 + qq]) * v3;
+    }
+    T V[3];
+#pragma unroll
+    for (int qq = 0; qq < 3; ++qq) V[qq] = V0[qq] + x * (V1[qq] - V0[qq]);
+    Q[at(d, IVY)] = (V[0] * T(r[18]) + V[1] * T(r[19])) + V[2] * T(r[20]);
+    Q[at(d, IVZ)] = (V[0] * T(r[21]) + V[1] * T(r[22])) + V[2] * T(r[23]);
+  }
+}
+
+// order-preserving keys of doubles for an unsigned atomicMin
+constexpr unsigned long long kKeyInf = 0xfff0000000000000ull;  // key(+inf)
+__device__ __forceinline__ unsigned long long dkey(double x) {
+  unsigned long long k = __double_as_longlong(x);
+  return (k >> 63) ? ~k : (k | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double dunkey(unsigned long long k) {
+  return __longlong_as_double((k >> 63) ? (k & 0x7fffffffffffffffull) : ~k);
+}
+
+// min over the interior of width / (|v| + sqrt(Phi)) on x2 and x3
+template <typename T>
+__global__ void __launch_bounds__(kThreads) cs_dt_kernel(CsParams P, const void* buf,
+                                                         unsigned long long* key) {
+  const int n = P.n, nc = P.nc;
+  const size_t pst = (size_t)nc * nc;
+  const Geo G = geo_of(P.geo, nc);
+  const T* U = static_cast<const T*>(buf);
+  double m = INFINITY;
+  int nan = 0;
+  const size_t total = (size_t)6 * n * n;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const int j = kNg + (int)(e % n);
+    const int k = kNg + (int)((e / n) % n);
+    const int p = (int)(e / ((size_t)n * n));
+    const size_t c = (size_t)k * nc + j;
+    T w[4];
+    sw_prim<T>(U + (size_t)p * 4 * pst, pst, c, T(G.cos_c[c]), w);
+    const T cs = sqrt(w[IDN]);
+    const T d2 = T(G.w2[c]) / (fabs(w[IVY]) + cs);
+    const T d3 = T(G.w3[c]) / (fabs(w[IVZ]) + cs);
+    if (isnan(d2) || isnan(d3)) nan = 1;
+    m = fmin(m, (double)fmin(d2, d3));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    m = fmin(m, __shfl_xor_sync(0xffffffffu, m, o));
+    nan |= __shfl_xor_sync(0xffffffffu, nan, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(&key[0], dkey(m));
+    if (nan) atomicOr(&key[1], 1ull);
+  }
+}
+
+// dt = cfl min (NaN if any cell was), and the keys reset for the next call
+__global__ void cs_dt_finish(unsigned long long* key, double cfl, double* dt) {
+  dt[0] = key[1] ? __longlong_as_double(0x7ff8000000000000ll)
+                 : cfl * dunkey(key[0]);
+  key[0] = kKeyInf;
+  key[1] = 0;
+}
+
+thread_local std::string g_cs_err;
+
+int cs_fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  return sg_fail_message(code, buf);
+}
+
+int grid_for(size_t work) {
+  size_t g = (work + kThreads - 1) / kThreads;
+  if (g > 4096) g = 4096;
+  return (int)(g ? g : 1);
+}
+
+}  // namespace
+
+struct sg_cs_handle {
+  sg_cs_desc d;
+  void* buf[3] = {nullptr, nullptr, nullptr};
+  void* scratch = nullptr;
+  int cur = 0, base = 0;
+  unsigned long long* key = nullptr;
+};
+
+extern "C" {
+
+int sg_cs_create(const sg_cs_desc* d, sg_cs_handle** out) {
+  if (!d || !out) return cs_fail(SG_ERR_ARG, "sg_cs_create: null argument");
+  *out = nullptr;
+  if (d->n < 4 || d->ng != kNg)
+    return cs_fail(SG_ERR_ARG, "sg_cs_create: n %d (>= 4), nghost %d (3)", d->n, d->ng);
+  if (d->dtype != SG_F64 && d->dtype != SG_F32)
+    return cs_fail(SG_ERR_ARG, "sg_cs_create: dtype %d", d->dtype);
+  if (!d->geo || !d->ghost_tab || !d->seam_tab || d->nghost <= 0 || d->nseam <= 0)
+    return cs_fail(SG_ERR_ARG, "sg_cs_create: the geometry and seam tables are required");
+  if (d->nstage < 1 || d->nstage > 3)
+    return cs_fail(SG_ERR_ARG, "sg_cs_create: nstage %d", d->nstage);
+  auto* h = new sg_cs_handle();
+  h->d = *d;
+  // key[0]: the min key, key[1]: a NaN flag
+  cudaError_t e = cudaMalloc(&h->key, 2 * sizeof(unsigned long long));
+  if (e == cudaSuccess) {
+    const unsigned long long init[2] = {kKeyInf, 0};
+    e = cudaMemcpy(h->key, init, sizeof(init), cudaMemcpyHostToDevice);
+  }
+  if (e != cudaSuccess) {
+    if (h->key) cudaFree(h->key);
+    delete h;
+    return cs_fail(SG_ERR_CUDA, "sg_cs_create: %s", cudaGetErrorString(e));
+  }
+  *out = h;
+  return 0;
+}
+
+int sg_cs_destroy(sg_cs_handle* h) {
+  if (!h) return 0;
+  if (h->key) cudaFree(h->key);
+  delete h;
+  return 0;
+}
+
+int sg_cs_scratch_bytes(const sg_cs_handle* h, size_t* bytes) {
+  if (!h || !bytes) return cs_fail(SG_ERR_ARG, "sg_cs_scratch_bytes: null");
+  const size_t nc = (size_t)h->d.n + 2 * kNg;
+  const size_t s = h->d.dtype == SG_F64 ? 8 : 4;
+  *bytes = 2 * 6 * 4 * nc * (nc + 1) * s;  // F2 and F3
+  return 0;
+}
+
+int sg_cs_bind(sg_cs_handle* h, void* b0, void* b1, void* b2, void* scratch,
+               size_t bytes) {
+  size_t need = 0;
+  if (!h) return cs_fail(SG_ERR_ARG, "sg_cs_bind: null handle");
+  sg_cs_scratch_bytes(h, &need);
+  if (!b0 || !b1 || !b2 || b0 == b1 || b1 == b2 || b0 == b2)
+    return cs_fail(SG_ERR_ARG, "sg_cs_bind: three distinct non-null buffers needed");
+  if (!scratch || bytes < need)
+    return cs_fail(SG_ERR_ARG, "sg_cs_bind: the flux scratch needs %zu bytes", need);
+  h->buf[0] = b0, h->buf[1] = b1, h->buf[2] = b2;
+  h->scratch = scratch;
+  return 0;
+}
+
+int sg_cs_set_current(sg_cs_handle* h, int32_t cur) {
+  if (!h || cur < 0 || cur > 2) return cs_fail(SG_ERR_ARG, "sg_cs_set_current: %d", cur);
+  h->cur = h->base = cur;
+  return 0;
+}
+
+int sg_cs_rotation(const sg_cs_handle* h, int32_t* cur, int32_t* base) {
+  if (!h || !cur || !base) return cs_fail(SG_ERR_ARG, "sg_cs_rotation: null");
+  *cur = h->cur;
+  *base = h->base;
+  return 0;
+}
+
+int sg_cs_set_rotation(sg_cs_handle* h, int32_t cur, int32_t base) {
+  if (!h || cur < 0 || cur > 2 || base < 0 || base > 2)
+    return cs_fail(SG_ERR_ARG, "sg_cs_set_rotation: %d %d", cur, base);
+  h->cur = cur;
+  h->base = base;
+  return 0;
+}
+
+static void cs_plan(const sg_cs_handle* h, int stage, int* in, int* u0, int* out) {
+  *in = h->cur;
+  *u0 = stage == 0 ? h->cur : h->base;
+  int o = 0;
+  while (o == *in || o == *u0) ++o;
+  *out = o;
+}
+
+int sg_cs_advance(sg_cs_handle* h, int32_t stage) {
+  if (!h || stage < 0 || stage >= h->d.nstage)
+    return cs_fail(SG_ERR_ARG, "sg_cs_advance: stage %d", stage);
+  int in, u0, out;
+  cs_plan(h, stage, &in, &u0, &out);
+  if (stage == 0) h->base = h->cur;
+  h->cur = out;
+  return 0;
+}
+
+static CsParams cs_params(const sg_cs_handle* h) {
+  CsParams P = {};
+  P.n = h->d.n;
+  P.nc = h->d.n + 2 * kNg;
+  P.geo = h->d.geo;
+  P.gtab = h->d.ghost_tab;
+  P.nghost = h->d.nghost;
+  P.stab = h->d.seam_tab;
+  P.nseam = h->d.nseam;
+  const size_t nc = P.nc;
+  const size_t s = h->d.dtype == SG_F64 ? 8 : 4;
+  P.f2 = h->scratch;
+  P.f3 = static_cast<unsigned char*>(h->scratch) + 6 * 4 * nc * (nc + 1) * s;
+  return P;
+}
+
+int sg_cs_fill_seams(sg_cs_handle* h, sg_stream_t stream) {
+  if (!h || !h->buf[0]) return cs_fail(SG_ERR_STATE, "sg_cs_fill_seams: buffers not bound");
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  CsParams P = cs_params(h);
+  if (h->d.dtype == SG_F64)
+    cs_ghost_kernel<double><<<grid_for(P.nghost), kThreads, 0, s>>>(P, h->buf[h->cur]);
+  else
+    cs_ghost_kernel<float><<<grid_for(P.nghost), kThreads, 0, s>>>(P, h->buf[h->cur]);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? 0 : cs_fail(SG_ERR_CUDA, "sg_cs_fill_seams: %s", cudaGetErrorString(e));
+}
+
+int sg_cs_stage(sg_cs_handle* h, int32_t stage, const double* dt_dev,
+                sg_stream_t stream) {
+  if (!h || !dt_dev) return cs_fail(SG_ERR_ARG, "sg_cs_stage: null argument");
+  if (!h->buf[0]) return cs_fail(SG_ERR_STATE, "sg_cs_stage: buffers not bound");
+  if (stage < 0 || stage >= h->d.nstage)
+    return cs_fail(SG_ERR_ARG, "sg_cs_stage: stage %d of %d", stage, h->d.nstage);
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  int in, u0, out;
+  cs_plan(h, stage, &in, &u0, &out);
+  CsParams P = cs_params(h);
+  P.in = h->buf[in];
+  P.u0 = h->buf[u0];
+  P.out = h->buf[out];
+  P.dt = dt_dev;
+  P.w0 = h->d.wght[stage][0];
+  P.w1 = h->d.wght[stage][1];
+  P.w2 = h->d.wght[stage][2];
+  const size_t faces = (size_t)2 * 6 * P.n * (P.n + 1);
+  const size_t cells = (size_t)6 * P.n * P.n;
+  if (h->d.dtype == SG_F64) {
+    cs_flux_kernel<double><<<grid_for(faces), kThreads, 0, s>>>(P);
+    cs_seam_flux_kernel<double><<<grid_for(P.nseam), kThreads, 0, s>>>(P);
+    cs_update_kernel<double><<<grid_for(cells), kThreads, 0, s>>>(P);
+    cs_ghost_kernel<double><<<grid_for(P.nghost), kThreads, 0, s>>>(P, P.out);
+  } else {
+    cs_flux_kernel<float><<<grid_for(faces), kThreads, 0, s>>>(P);
+    cs_seam_flux_kernel<float><<<grid_for(P.nseam), kThreads, 0, s>>>(P);
+    cs_update_kernel<float><<<grid_for(cells), kThreads, 0, s>>>(P);
+    cs_ghost_kernel<float><<<grid_for(P.nghost), kThreads, 0, s>>>(P, P.out);
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cs_fail(SG_ERR_CUDA, "sg_cs_stage: %s", cudaGetErrorString(e));
+  if (stage == 0) h->base = h->cur;
+  h->cur = out;
+  return 0;
+}
+
+int sg_cs_max_dt(sg_cs_handle* h, double* dt_dev, sg_stream_t stream) {
+  if (!h || !dt_dev) return cs_fail(SG_ERR_ARG, "sg_cs_max_dt: null argument");
+  if (!h->buf[0]) return cs_fail(SG_ERR_STATE, "sg_cs_max_dt: buffers not bound");
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  CsParams P = cs_params(h);
+  const size_t cells = (size_t)6 * P.n * P.n;
+  int g = grid_for(cells);
+  if (g > 256) g = 256;
+  if (h->d.dtype == SG_F64)
+    cs_dt_kernel<double><<<g, kThreads, 0, s>>>(P, h->buf[h->cur], h->key);
+  else
+    cs_dt_kernel<float><<<g, kThreads, 0, s>>>(P, h->buf[h->cur], h->key);
+  cs_dt_finish<<<1, 1, 0, s>>>(h->key, h->d.cfl, dt_dev);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? 0 : cs_fail(SG_ERR_CUDA, "sg_cs_max_dt: %s", cudaGetErrorString(e));
+}
+
+}  // extern "C"

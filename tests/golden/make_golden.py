@@ -21,6 +21,38 @@ from oracle import oracle as O  # noqa: E402
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_faces.npz")
 
 
+SHALLOW = os.path.join(os.path.dirname(os.path.abspath(__file__)), "shallow_roe.npz")
+
+
+def main_shallow(n=1000, seed=20261205):
+    """The reference's shallow_roe_impl (src/riemann/riemann_kernels.h:447-495)
+    with dir yz on seeded shallow-water states: geopotential in [50, 12000],
+    velocities N(0, 30), for the x2 (dim 2) and x3 (dim 1) faces."""
+    O.build()
+    R = O.ref()
+    if R is None:
+        raise SystemExit("the reference shim was not built (no reference tree)")
+    rng = np.random.default_rng(seed)
+    wl = np.zeros((n, 4))
+    wr = np.zeros((n, 4))
+    for w in (wl, wr):
+        w[:, 0] = rng.uniform(50.0, 12000.0, n)
+        w[:, 1:] = rng.normal(0.0, 30.0, (n, 3))
+    # equal states and tiny jumps too
+    wr[: n // 10] = wl[: n // 10]
+    wr[n // 10: n // 5] = wl[n // 10: n // 5] * (1 + 1e-9 * rng.normal(size=(n // 10, 4)))
+    dims = np.array([2, 1])
+    flux = np.zeros((2, n, 4))
+    for di, dim in enumerate(dims):
+        for i in range(n):
+            a, b = np.ascontiguousarray(wl[i]), np.ascontiguousarray(wr[i])
+            f = np.zeros(4)
+            R.ref_shallow_roe(O.ptr(f), O.ptr(a), O.ptr(b), int(dim), 1)
+            flux[di, i] = f
+    np.savez_compressed(SHALLOW, wl=wl, wr=wr, dims=dims, flux=flux)
+    print("wrote", SHALLOW)
+
+
 def main(n=1000, seed=20261203):
     O.build()
     R = O.ref()
@@ -115,4 +147,7 @@ def main(n=1000, seed=20261203):
 
 
 if __name__ == "__main__":
-    main()
+    if "--shallow" in sys.argv:
+        main_shallow()
+    else:
+        main()
