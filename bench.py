@@ -60,7 +60,13 @@ WORKLOADS = {
     # convection solves, (nx2, nx3, nx1) from {64, 96, 128}^2 x {64, 96},
     # 200 RK3 steps each, FP32 bulk with the FP64 implicit solve
     "serving": "snapy_gb300/decks/convection3d.yaml",
+    # shallow water on the cubed sphere: 6 panels of 96 x 96 cells, radius
+    # 6.371e6 m, mean depth 1000 m, a 100 m Gaussian bump of width 0.1 rad
+    # at a seeded lon/lat, at rest; weno5 + shallow-roe + rk3, FP32 state,
+    # the seam halo filled every stage
+    "cubed-sphere": None,
 }
+CS_N, CS_SEED = 96, 20261206
 SERVE_RATE, SERVE_SEED = 20.0, 20261204
 ENSEMBLE_MEMBERS, ENSEMBLE_SEED = 64, 20261203
 
@@ -841,8 +847,175 @@ def run_reference_serving(args):
     return 0
 
 
+def cs_config(n, precision, nranks):
+    return {"workload": f"cubed sphere shallow water: 6 panels x {n}x{n}, "
+                        "radius 6.371e6 m, depth 1000 m, 100 m Gaussian bump "
+                        f"(0.1 rad, seed {CS_SEED}), weno5+shallow-roe+rk3, "
+                        f"{precision}, seam halo every stage",
+            "cells": 6 * n * n, "panels": 6, "n": n, "precision": precision,
+            "dt": "the CFL step on the device, every step",
+            "l2": "flushed between timed steps (512 MiB write; the state fits in L2)",
+            "graphs": "one step graph per buffer rotation, captured before the warm-up",
+            "replicas": nranks, "parallelism": "replicas" if nranks > 1 else "single"}
+
+
+def cs_cpu_baseline(n, seconds):
+    """The cubed-sphere oracle (numpy plumbing over the C oracle's face
+    functions, FP64, OpenMP) on the same grid, as many RK3 steps as fit."""
+    import numpy as np
+    from oracle import oracle as O
+    from oracle.cubed_sphere import CubedSphere
+    from snapy_gb300 import cubed_sphere as cs
+    O.build()
+    g = cs.geometry(n, 6.371e6)
+    o = CubedSphere(n, g, cs.ghost_table(n, g), cs.seam_table(n, g), cs.RK3, 0.9)
+    u = cs.bump(n, seed=CS_SEED)
+    o.fill(u)
+    u0 = np.zeros_like(u)
+    k, t0 = 0, time.perf_counter()
+    while True:
+        dt = o.max_dt(u)
+        for st in range(3):
+            o.stage(u, u0, dt, st)
+        k += 1
+        el = time.perf_counter() - t0
+        if (el >= seconds and k >= 1) or k >= 10000:
+            break
+    return {"value": 6 * n * n * k / el, "unit": "cell-updates/s",
+            "cores": os.cpu_count() or 1, "kind": "port",
+            "sample": f"{k} RK3 steps of the same 6 x {n}x{n} sphere, FP64, "
+                      f"{el:.1f} s (numpy over the C oracle, OpenMP)"}
+
+
+def run_cubed_sphere(args):
+    import torch
+    import torch.distributed as dist
+    from snapy_gb300 import cubed_sphere as cs
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl", init_method="env://")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    precision = args.precision or "float32"
+    dtype = torch.float32 if precision == "float32" else torch.float64
+    n = CS_N
+    sp = cs.SphereSW(n, dtype=dtype, device=dev)
+    u_init = cs.bump(n, seed=CS_SEED)
+    sp.initialize(u_init)
+    for _ in range(8):
+        if sp.captures >= 2:
+            break
+        sp.step()
+    for _ in range(max(3, args.warmup)):
+        sp.step()
+    torch.cuda.synchronize()
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            flush.zero_()
+            ev[k][0].record(stream)
+            sp.step()
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    t_total = sum(step_ms) / 1e3
+    if world > 1:
+        t = torch.tensor([t_total], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_total = float(t.item())
+    cells = 6 * n * n
+    value = cells * args.steps * world / t_total
+    assert torch.isfinite(sp.state()).all()
+    # one stage (flux, seam flux, update, seam halo) timed alone, L2 flushed
+    s_bytes = 4 if dtype == torch.float32 else 8
+    stage_ms, stage_bytes = [], []
+    for k in range(min(args.steps, 20)):
+        for st in range(3):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            sp._chk(sp.L.sg_cs_stage(sp.h, st, sp.dt.data_ptr(), stream.cuda_stream), "sg_cs_stage")
+            e1.record(stream)
+            stage_ms.append((e0, e1))
+            stage_bytes.append((2 if st == 0 else 3) * 4 * s_bytes * cells)
+    torch.cuda.synchronize()
+    durs = [a.elapsed_time(b) / 1e3 for a, b in stage_ms]
+    achieved = sum(stage_bytes) / sum(durs) / 1e9
+    peak, peak_kind = peaks()
+    # end to end with host buffers
+    host = torch.empty(sp.state().shape, dtype=dtype).pin_memory()
+    host.copy_(sp.state())
+    nbytes = host.numel() * host.element_size()
+    e2e_steps = max(5, min(args.steps, 50))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        sp.state().copy_(host, non_blocking=True)
+        sp.step()
+        host.copy_(sp.state(), non_blocking=True)
+    torch.cuda.synchronize()
+    e2e_t = time.perf_counter() - t0
+    if rank == 0:
+        cb = None if args.no_cpu_baseline else cs_cpu_baseline(n, args.cpu_seconds)
+        print(json.dumps({
+            "metric": "cell-updates/s per RK3 step",
+            "value": value, "unit": "cell-updates/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t_total / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32" if dtype == torch.float32 else "f64",
+            "data": "synthetic (seeded Gaussian bump)",
+            "config": cs_config(n, precision, world),
+            "e2e": {"value": cells * e2e_steps * world / e2e_t, "unit": "cell-updates/s",
+                    "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak,
+                         "peak_kind": peak_kind, "traffic": None,
+                         "kernel": "one stage: cs_flux + cs_seam_flux + cs_update + cs_ghost",
+                         "bytes_per_launch": statistics.mean(stage_bytes),
+                         "mean_launch_us": statistics.mean(durs) * 1e6},
+            "cpu_baseline": cb, "clocks": clk.summary(),
+            "gpu_launches": args.steps * (2 + 3 * 4),
+            "step_ms_median": statistics.median(step_ms)}), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def run_reference_cubed_sphere(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    cb = cs_cpu_baseline(CS_N, max(2.0, args.cpu_seconds))
+    val = cb["value"]
+    print(json.dumps({
+        "impl": "reference", "metric": "cell-updates/s per RK3 step",
+        "value": val, "unit": "cell-updates/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 6 * CS_N * CS_N / val * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded Gaussian bump)",
+        "config": cs_config(CS_N, args.precision or "float32", 1), "cpu_baseline": cb,
+        "e2e": {"value": val, "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0}}), flush=True)
+    return 0
+
+
 def main():
     args = parse()
+    if args.workload == "cubed-sphere":
+        if args.impl == "reference":
+            return run_reference_cubed_sphere(args)
+        return run_cubed_sphere(args)
     if args.workload == "serving":
         if args.impl == "reference":
             return run_reference_serving(args)
