@@ -205,7 +205,16 @@ typedef struct sg_cs_desc {
    * the source face cosine, source tangents, destination tangents) */
   const double* seam_tab;
   int32_t nseam;
+  /* SG_F32: a reference geopotential Phi0 (> 0): the state's Phi row holds
+   * the anomaly Phi - Phi0, and the pressure Phi^2 / 2 is carried as the
+   * anomaly Phi0 Phi' + Phi'^2 / 2 (0: totals); SG_F64 ignores it and runs
+   * the reference's form on totals */
+  double phi_ref;
+  /* SG_CS_SHALLOW_ROE (the reference's shallow_roe_impl, dir yz) or
+   * SG_CS_HLLC (shallow-water HLLC, Toro 2001: no reference counterpart) */
+  int32_t riemann;
 } sg_cs_desc;
+enum { SG_CS_SHALLOW_ROE = 0, SG_CS_HLLC = 1 };
 
 int sg_cs_create(const sg_cs_desc* desc, sg_cs_handle** out);
 int sg_cs_destroy(sg_cs_handle* h);

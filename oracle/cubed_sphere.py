@@ -15,7 +15,8 @@ gnomonic coordinate of src/coord/gnomonic_equiangle.cpp):
   x2 / x3 face states, weno5 for Phi and cp5 for the velocities
   (reconstruct.cpp:151-187);
   to the face frame (prim2local2_/3_, gnomonic_equiangle.cpp:357-398),
-  shallow_roe with dir yz (riemann_kernels.h:447-495), back to covariant
+  shallow_roe with dir yz (riemann_kernels.h:447-495) or the product's
+  shallow-water HLLC (og_hllc_sw_batch), back to covariant
   fluxes (flux2global2_/3_, :414-463);
   the seam faces single-valued (src/layout/seam_register.cpp:35);
   div = (A2 dF2 + A3 dF3) / V (coordinate.cpp:618-662), minus the metric
@@ -41,12 +42,12 @@ def _recon(st: np.ndarray, weno: bool, side: int) -> np.ndarray:
     return out
 
 
-def _roe(wl: np.ndarray, wr: np.ndarray, dim: int) -> np.ndarray:
+def _roe(wl: np.ndarray, wr: np.ndarray, dim: int, hllc: bool = False) -> np.ndarray:
     wl = np.ascontiguousarray(wl.reshape(-1, 4))
     wr = np.ascontiguousarray(wr.reshape(-1, 4))
     f = np.zeros_like(wl)
-    O.lib().og_shallow_roe_batch(O.ptr(wl.ravel()), O.ptr(wr.ravel()),
-                                 wl.shape[0], dim, O.ptr(f.ravel()))
+    fn = O.lib().og_hllc_sw_batch if hllc else O.lib().og_shallow_roe_batch
+    fn(O.ptr(wl.ravel()), O.ptr(wr.ravel()), wl.shape[0], dim, O.ptr(f.ravel()))
     return f
 
 
@@ -54,8 +55,9 @@ class CubedSphere:
     """Six panels (6, 4, nc, nc) FP64: Phi, and the radial and the two
     covariant tangential momenta."""
 
-    def __init__(self, n, geo, ghost_tab, seam_tab, wght, cfl):
+    def __init__(self, n, geo, ghost_tab, seam_tab, wght, cfl, riemann="shallow-roe"):
         self.n, self.g = n, geo
+        self.hllc = riemann == "hllc"
         self.gt, self.st = ghost_tab, seam_tab
         self.wght, self.cfl = wght, cfl
         self.nc = n + 2 * NG
@@ -133,7 +135,7 @@ class CubedSphere:
         shape = wl.shape
         wl4 = np.moveaxis(wl, 1, -1)
         wr4 = np.moveaxis(wr, 1, -1)
-        f = _roe(wl4, wr4, 2 if axis == 2 else 1).reshape(wl4.shape)
+        f = _roe(wl4, wr4, 2 if axis == 2 else 1, self.hllc).reshape(wl4.shape)
         f = np.moveaxis(f, -1, 1).copy()
         txy, txz = f[:, IVY].copy(), f[:, IVZ].copy()
         if axis == 2:

@@ -110,6 +110,7 @@ def lib():
         L.og_recon_batch.argtypes = [_dp, ctypes.c_long, ctypes.c_int,
                                      ctypes.c_int, ctypes.c_int, _dp]
         L.og_shallow_roe_batch.argtypes = [_dp, _dp, ctypes.c_long, ctypes.c_int, _dp]
+        L.og_hllc_sw_batch.argtypes = [_dp, _dp, ctypes.c_long, ctypes.c_int, _dp]
         _lib = L
     return _lib
 

@@ -103,6 +103,8 @@ void og_recon_batch(const double* st, long n, int weno, int side, int scale,
                     double* out);
 void og_shallow_roe_batch(const double* wl, const double* wr, long n, int dim,
                           double* flx);
+void og_hllc_sw_batch(const double* wl, const double* wr, long n, int dim,
+                      double* flx);
 
 #ifdef __cplusplus
 }

@@ -79,7 +79,8 @@ class CsDesc(ctypes.Structure):
     _fields_ = [("n", _i32), ("ng", _i32), ("dtype", _i32), ("nstage", _i32),
                 ("wght", (ctypes.c_double * 3) * 3), ("cfl", ctypes.c_double),
                 ("geo", _vp), ("ghost_tab", _vp), ("nghost", _i32),
-                ("seam_tab", _vp), ("nseam", _i32)]
+                ("seam_tab", _vp), ("nseam", _i32), ("phi_ref", ctypes.c_double),
+                ("riemann", _i32)]
 
 
 # every symbol include/snapy_gb300.h declares, with its ctypes signature

@@ -90,14 +90,19 @@ struct CsParams {
   void* f3;
   const double* dt;
   double w0, w1, w2;
+  double phi0;  // FP32: the reference geopotential of the pressure anomaly
+  int hllc;     // 1: HLLC for shallow water, 0: shallow-roe (dir yz)
 };
 
-// U -> W of one cell: v = m / Phi, the tangential pair raised by cos
+// U -> W of one cell: v = m / Phi, the tangential pair raised by cos.
+// With phi0 > 0 (the FP32 state) the stored Phi row is the anomaly
+// Phi - phi0: w[IDN] stays the anomaly (what the reconstruction reads) and
+// the velocities divide by the total
 template <typename T>
 __device__ __forceinline__ void sw_prim(const T* q, size_t pst, size_t c,
-                                        T cs, T* w) {
-  const T phi = q[c];
-  w[IDN] = phi;
+                                        T cs, T* w, T phi0 = T(0)) {
+  const T phi = phi0 > T(0) ? phi0 + q[c] : q[c];
+  w[IDN] = q[c];
   const T v1 = q[pst + c] / phi, v2 = q[2 * pst + c] / phi,
           v3 = q[3 * pst + c] / phi;
   const T sth2 = T(1.) - cs * cs;
@@ -106,18 +111,28 @@ __device__ __forceinline__ void sw_prim(const T* q, size_t pst, size_t c,
   w[IVZ] = -v2 * cs / sth2 + v3 / sth2;
 }
 
-// shallow_roe_impl with dir yz: DIM 2 (x2 faces, normal IVY) or 1 (x3)
+// shallow_roe_impl with dir yz: DIM 2 (x2 faces, normal IVY) or 1 (x3).
+// phi0 > 0 (the FP32 state): L[0], R[0] are the anomalies Phi' = Phi - phi0
+// the state stores, the totals are formed for the wave speeds and the mass
+// flux, and the normal momentum flux carries the pressure anomaly
+// phi0 Phi' + Phi'^2 / 2 in place of Phi^2 / 2: the constant phi0^2 / 2 it
+// leaves out has no divergence once the metric source leaves it out too
+// (the lake at rest), and FP32 would lose the anomaly under it
 template <typename T, int DIM>
-__device__ __forceinline__ void shallow_roe(const T* L, const T* R, T* F) {
+__device__ __forceinline__ void shallow_roe(const T* L, const T* R, T* F,
+                                            T phi0) {
   constexpr int ivx = DIM == 2 ? IVY : IVZ, ivy = DIM == 2 ? IVZ : IVY,
                 ivz = IVX;
-  T sqrtdl = sqrt(L[0]), sqrtdr = sqrt(R[0]);
+  // Phi of the two sides (the anomalies L[0], R[0] plus phi0 when phi0 > 0)
+  const T pL = phi0 > T(0) ? phi0 + L[0] : L[0];
+  const T pR = phi0 > T(0) ? phi0 + R[0] : R[0];
+  T sqrtdl = sqrt(pL), sqrtdr = sqrt(pR);
   T isdlpdr = T(1.) / (sqrtdl + sqrtdr);
   T ubar = (L[ivx] * sqrtdl + R[ivx] * sqrtdr) * isdlpdr;
   T vbar = (L[ivy] * sqrtdl + R[ivy] * sqrtdr) * isdlpdr;
-  T cbar = sqrt(T(0.5) * (L[0] + R[0]));
+  T cbar = sqrt(T(0.5) * (pL + pR));
   T del0 = R[0] - L[0], delx = R[ivx] - L[ivx], dely = R[ivy] - L[ivy];
-  T hbar = sqrt(L[0] * R[0]);
+  T hbar = sqrt(pL * pR);
   T a1 = T(0.5) * (cbar * del0 - hbar * delx) / cbar;
   T a2 = hbar * dely;
   T a3 = T(0.5) * (cbar * del0 + hbar * delx) / cbar;
@@ -130,14 +145,73 @@ __device__ __forceinline__ void shallow_roe(const T* L, const T* R, T* F) {
   w2[ivx] = a3 * (ubar + cbar);
   w2[ivy] = a3 * vbar;
   T s0 = fabs(ubar - cbar), s1 = fabs(ubar), s2 = fabs(ubar + cbar);
-  F[0] = T(0.5) * (L[0] * L[ivx] + R[0] * R[ivx]);
-  F[ivx] = T(0.5) * (L[0] * L[ivx] * L[ivx] + T(0.5) * L[0] * L[0] +
-                     R[0] * R[ivx] * R[ivx] + T(0.5) * R[0] * R[0]);
-  F[ivy] = T(0.5) * (L[0] * L[ivx] * L[ivy] + R[0] * R[ivx] * R[ivy]);
+  if (phi0 > T(0)) {
+    const T dl = L[0], dr = R[0];
+    const T ql = phi0 * dl + T(0.5) * dl * dl, qr = phi0 * dr + T(0.5) * dr * dr;
+    F[0] = T(0.5) * (pL * L[ivx] + pR * R[ivx]);
+    F[ivx] = T(0.5) * (pL * L[ivx] * L[ivx] + ql + pR * R[ivx] * R[ivx] + qr);
+    F[ivy] = T(0.5) * (pL * L[ivx] * L[ivy] + pR * R[ivx] * R[ivy]);
+  } else {
+    F[0] = T(0.5) * (L[0] * L[ivx] + R[0] * R[ivx]);
+    F[ivx] = T(0.5) * (L[0] * L[ivx] * L[ivx] + T(0.5) * L[0] * L[0] +
+                       R[0] * R[ivx] * R[ivx] + T(0.5) * R[0] * R[0]);
+    F[ivy] = T(0.5) * (L[0] * L[ivx] * L[ivy] + R[0] * R[ivx] * R[ivy]);
+  }
   F[ivz] = 0;
 #pragma unroll
   for (int v = 0; v < 4; ++v)
     F[v] -= T(0.5) * (s0 * w0[v] + s1 * w1[v] + s2 * w2[v]);
+}
+
+// HLLC for shallow water in geopotential form (Toro 2001, ch. 10): Davis /
+// Einfeldt wave speeds S_L = min(u_L - c_L, u_R - c_R), S_R = max(u_L + c_L,
+// u_R + c_R) with c = sqrt(Phi), HLL for Phi and the normal momentum, the
+// tangential momentum upwinded across the contact S*.  The reference has no
+// shallow-water HLLC; the oracle's og_hllc_sw_batch is its checker.  phi0 as
+// in shallow_roe (a constant in the normal momentum flux passes through HLL
+// unchanged, so its anomaly form is exact).
+template <typename T, int DIM>
+__device__ __forceinline__ void hllc_sw(const T* L, const T* R, T* F, T phi0) {
+  constexpr int ivx = DIM == 2 ? IVY : IVZ, ivy = DIM == 2 ? IVZ : IVY,
+                ivz = IVX;
+  const T hL = phi0 > T(0) ? phi0 + L[0] : L[0];
+  const T hR = phi0 > T(0) ? phi0 + R[0] : R[0];
+  const T cl = sqrt(hL), cr = sqrt(hR);
+  const T ul = L[ivx], ur = R[ivx];
+  const T sl = fmin(ul - cl, ur - cr), sr = fmax(ul + cl, ur + cr);
+  const T ml = hL * ul, mr = hR * ur;
+  const T fl0 = ml, fr0 = mr;
+  T pl, pr;
+  if (phi0 > T(0)) {
+    const T dl = L[0], dr = R[0];
+    pl = phi0 * dl + T(0.5) * dl * dl;
+    pr = phi0 * dr + T(0.5) * dr * dr;
+  } else {
+    pl = T(0.5) * L[0] * L[0];
+    pr = T(0.5) * R[0] * R[0];
+  }
+  const T fl1 = ml * ul + pl, fr1 = mr * ur + pr;
+  T f0, f1, f2;
+  if (sl >= T(0)) {
+    f0 = fl0;
+    f1 = fl1;
+    f2 = fl0 * L[ivy];
+  } else if (sr <= T(0)) {
+    f0 = fr0;
+    f1 = fr1;
+    f2 = fr0 * R[ivy];
+  } else {
+    const T inv = T(1.) / (sr - sl);
+    f0 = (sr * fl0 - sl * fr0 + sl * sr * (R[0] - L[0])) * inv;
+    f1 = (sr * fl1 - sl * fr1 + sl * sr * (mr - ml)) * inv;
+    const T den = hR * (ur - sr) - hL * (ul - sl);
+    const T ss = (sl * hR * (ur - sr) - sr * hL * (ul - sl)) / den;
+    f2 = ss >= T(0) ? f0 * L[ivy] : f0 * R[ivy];
+  }
+  F[0] = f0;
+  F[ivx] = f1;
+  F[ivy] = f2;
+  F[ivz] = T(0);
 }
 
 // the faces: thread e < 6 n (n + 1) an x2 face (panel, row k, face j), the
@@ -169,7 +243,7 @@ __global__ void __launch_bounds__(kThreads) cs_flux_kernel(CsParams P) {
     for (int m = 0; m < 6; ++m) {
       const int kk = x2 ? k : k - 3 + m, jj = x2 ? j - 3 + m : j;
       const size_t c = (size_t)kk * nc + jj;
-      sw_prim<T>(q, pst, c, T(G.cos_c[c]), st[m]);
+      sw_prim<T>(q, pst, c, T(G.cos_c[c]), st[m], T(P.phi0));
     }
     T wl[4], wr[4], F[4];
 #pragma unroll
@@ -203,10 +277,17 @@ __global__ void __launch_bounds__(kThreads) cs_flux_kernel(CsParams P) {
     };
     to_face(wl);
     to_face(wr);
-    if (x2)
-      shallow_roe<T, 2>(wl, wr, F);
-    else
-      shallow_roe<T, 1>(wl, wr, F);
+    if (P.hllc) {
+      if (x2)
+        hllc_sw<T, 2>(wl, wr, F, T(P.phi0));
+      else
+        hllc_sw<T, 1>(wl, wr, F, T(P.phi0));
+    } else {
+      if (x2)
+        shallow_roe<T, 2>(wl, wr, F, T(P.phi0));
+      else
+        shallow_roe<T, 1>(wl, wr, F, T(P.phi0));
+    }
     // back to covariant fluxes (flux2global2_ / 3_)
     const T txy = F[IVY], txz = F[IVZ];
     if (x2) {
@@ -286,7 +367,7 @@ __global__ void __launch_bounds__(kThreads) cs_update_kernel(CsParams P) {
     const size_t c = (size_t)k * nc + j;
     const T* q = U + (size_t)p * 4 * pst;
     T w[4];
-    sw_prim<T>(q, pst, c, T(G.cos_c[c]), w);
+    sw_prim<T>(q, pst, c, T(G.cos_c[c]), w, T(P.phi0));
     const size_t i2 = (size_t)k * (nc + 1) + j, i3 = (size_t)k * nc + j;
     const T a2lo = T(G.a2[i2]), a2hi = T(G.a2[i2 + 1]);
     const T a3lo = T(G.a3[i3]), a3hi = T(G.a3[i3 + nc]);
@@ -300,11 +381,18 @@ __global__ void __launch_bounds__(kThreads) cs_update_kernel(CsParams P) {
       const T d3 = a3hi * f3[i3 + nc] - a3lo * f3[i3];
       div[v] = (d2 + d3) / vol;
     }
-    const T pr = T(0.5) * (w[IDN] * w[IDN]);
+    // Phi and p = Phi^2 / 2; with phi0 > 0, the stored anomaly Phi' and
+    // the pressure anomaly phi0 Phi' + Phi'^2 / 2 (see shallow_roe)
+    T rho = w[IDN], pr = T(0.5) * (w[IDN] * w[IDN]);
+    if (P.phi0 > 0.) {
+      const T dp = w[IDN];
+      rho = T(P.phi0) + dp;
+      pr = T(P.phi0) * dp + T(0.5) * dp * dp;
+    }
     const T sn = T(G.sin_c[c]);
     const T sine2 = sn * sn;
-    div[IVY] -= T(G.xr[c]) * (pr + w[IDN] * w[IVZ] * w[IVZ] * sine2);
-    div[IVZ] -= T(G.yr[c]) * (pr + w[IDN] * w[IVY] * w[IVY] * sine2);
+    div[IVY] -= T(G.xr[c]) * (pr + rho * w[IVZ] * w[IVZ] * sine2);
+    div[IVZ] -= T(G.yr[c]) * (pr + rho * w[IVY] * w[IVY] * sine2);
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
       const size_t qi = ((size_t)p * 4 + v) * pst + c;
@@ -383,8 +471,8 @@ __global__ void __launch_bounds__(kThreads) cs_dt_kernel(CsParams P, const void*
     const int p = (int)(e / ((size_t)n * n));
     const size_t c = (size_t)k * nc + j;
     T w[4];
-    sw_prim<T>(U + (size_t)p * 4 * pst, pst, c, T(G.cos_c[c]), w);
-    const T cs = sqrt(w[IDN]);
+    sw_prim<T>(U + (size_t)p * 4 * pst, pst, c, T(G.cos_c[c]), w, T(P.phi0));
+    const T cs = sqrt(P.phi0 > 0. ? T(P.phi0) + w[IDN] : w[IDN]);
     const T d2 = T(G.w2[c]) / (fabs(w[IVY]) + cs);
     const T d3 = T(G.w3[c]) / (fabs(w[IVZ]) + cs);
     if (isnan(d2) || isnan(d3)) nan = 1;
@@ -447,6 +535,8 @@ int sg_cs_create(const sg_cs_desc* d, sg_cs_handle** out) {
     return cs_fail(SG_ERR_ARG, "sg_cs_create: dtype %d", d->dtype);
   if (!d->geo || !d->ghost_tab || !d->seam_tab || d->nghost <= 0 || d->nseam <= 0)
     return cs_fail(SG_ERR_ARG, "sg_cs_create: the geometry and seam tables are required");
+  if (d->riemann != SG_CS_SHALLOW_ROE && d->riemann != SG_CS_HLLC)
+    return cs_fail(SG_ERR_ARG, "sg_cs_create: riemann %d", d->riemann);
   if (d->nstage < 1 || d->nstage > 3)
     return cs_fail(SG_ERR_ARG, "sg_cs_create: nstage %d", d->nstage);
   auto* h = new sg_cs_handle();
@@ -543,6 +633,8 @@ static CsParams cs_params(const sg_cs_handle* h) {
   P.nghost = h->d.nghost;
   P.stab = h->d.seam_tab;
   P.nseam = h->d.nseam;
+  P.phi0 = h->d.dtype == SG_F32 ? h->d.phi_ref : 0.;
+  P.hllc = h->d.riemann == SG_CS_HLLC;
   const size_t nc = P.nc;
   const size_t s = h->d.dtype == SG_F64 ? 8 : 4;
   P.f2 = h->scratch;

@@ -300,11 +300,15 @@ class SphereSW:
 
     state (6, 4, n + 6, n + 6) in the dtype: Phi, the radial and the two
     covariant tangential momenta; the RK stages rotate three such buffers.
+    In FP32 the stored Phi row is the anomaly Phi - phi_ref (the geopotential
+    of the mean depth) and the pressure is carried as an anomaly about it:
+    ``totals()`` gives the FP64 totals.
     ``step`` advances one RK3 step with the device CFL time step (a captured
     graph after the first steps of each buffer rotation)."""
 
     def __init__(self, n: int, radius: float = 6.371e6, dtype=None, device=None,
-                 wght=RK3, cfl: float = 0.9, graphs: bool = True):
+                 wght=RK3, cfl: float = 0.9, graphs: bool = True,
+                 phi_ref: float = 9.81 * 1000.0, riemann: str = "shallow-roe"):
         import ctypes
         import torch
         from . import _lib
@@ -332,6 +336,12 @@ class SphereSW:
         d.geo, d.ghost_tab, d.seam_tab = (self._geo.data_ptr(), self._gt.data_ptr(),
                                           self._st.data_ptr())
         d.nghost, d.nseam = gt.shape[0], st.shape[0]
+        # FP32: the pressure as an anomaly about Phi0 (the mean depth's
+        # geopotential); FP64 keeps the reference's form
+        d.phi_ref = float(phi_ref)
+        if riemann not in ("shallow-roe", "hllc"):
+            raise ValueError(f"riemann-solver '{riemann}': shallow-roe or hllc")
+        d.riemann = 1 if riemann == "hllc" else 0
         self.nstage = len(wght)
         h = ctypes.c_void_p()
         with torch.cuda.device(dev):
@@ -346,6 +356,7 @@ class SphereSW:
                    "sg_cs_bind")
         _lib.check(self.L.sg_cs_set_current(h, 0), "sg_cs_set_current")
         self.dt = torch.zeros(1, dtype=torch.float64, device=dev)
+        self.phi0 = float(phi_ref) if self.dtype == torch.float32 else 0.0
         self.graphs = graphs
         self._graphs, self._seen = {}, set()
         self.replays = self.captures = 0
@@ -384,7 +395,10 @@ class SphereSW:
         is filled here)."""
         with self.torch.cuda.device(self.device):
             self._chk(self.L.sg_cs_set_current(self.h, 0), "sg_cs_set_current")
-            self.store[0].copy_(self.torch.as_tensor(u).to(self.device, self.dtype))
+            u = self.torch.as_tensor(u).to(self.device, self.torch.float64).clone()
+            if self.phi0:
+                u[:, IDN] -= self.phi0  # the stored anomaly, formed in FP64
+            self.store[0].copy_(u.to(self.dtype))
             self._chk(self.L.sg_cs_fill_seams(self.h, self._stream()), "sg_cs_fill_seams")
         self.time = 0.0
 
@@ -442,8 +456,15 @@ class SphereSW:
                 self._launch(fixed)
                 self._seen.add(key)
 
+    def totals(self):
+        """The current conserved state with Phi as a total (FP64)."""
+        u = self.state().double()
+        if self.phi0:
+            u[:, IDN] += self.phi0
+        return u
+
     def mass(self) -> float:
         """The total of Phi over the six panels' interiors, times the cell
         volume (FP64 on the host)."""
-        u = self.state()[:, IDN, NG:NG + self.n, NG:NG + self.n].double().cpu().numpy()
+        u = self.totals()[:, IDN, NG:NG + self.n, NG:NG + self.n].cpu().numpy()
         return float((u * self.geo["vol"][NG:NG + self.n, NG:NG + self.n]).sum())

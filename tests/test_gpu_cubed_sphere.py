@@ -13,10 +13,11 @@ pytestmark = pytest.mark.gpu
 NG = cs.NG
 
 
-def oracle_sphere(n):
+def oracle_sphere(n, riemann="shallow-roe"):
     from oracle.cubed_sphere import CubedSphere
     g = cs.geometry(n, 6.371e6)
-    return CubedSphere(n, g, cs.ghost_table(n, g), cs.seam_table(n, g), cs.RK3, 0.9)
+    return CubedSphere(n, g, cs.ghost_table(n, g), cs.seam_table(n, g), cs.RK3, 0.9,
+                       riemann=riemann)
 
 
 def interior(u, n):
@@ -48,11 +49,13 @@ def test_seam_fill_matches_oracle(cuda):
     assert np.array_equal(flat(got)[:, d], flat(u)[:, d])
 
 
-def test_stage_parity_fp64(cuda):
+@pytest.mark.parametrize("riemann", ["shallow-roe", "hllc"])
+def test_stage_parity_fp64(cuda, riemann):
     n = 16
-    o = oracle_sphere(n)
+    o = oracle_sphere(n, riemann)
     u = cs.bump(n, seed=5, width=0.4)
-    sp = cs.SphereSW(n, dtype=torch.float64, device=cuda, graphs=False)
+    sp = cs.SphereSW(n, dtype=torch.float64, device=cuda, graphs=False,
+                     riemann=riemann)
     sp.initialize(u)
     o.fill(u)
     u0 = np.zeros_like(u)
@@ -83,11 +86,15 @@ def test_mass_and_lake_at_rest(cuda):
     assert sp.state()[:, 1:, NG:NG + n, NG:NG + n].abs().max().item() < 1e-8
 
 
-def test_fp32_against_fp64_oracle(cuda):
+@pytest.mark.parametrize("riemann", ["shallow-roe", "hllc"])
+def test_fp32_against_fp64_oracle(cuda, riemann):
+    """FP32 state storing Phi as an anomaly about the mean depth's
+    geopotential, the pressure carried as an anomaly too: within the FP32
+    bar (relative L2 1e-5) of the FP64 oracle."""
     n = 24
-    o = oracle_sphere(n)
+    o = oracle_sphere(n, riemann)
     u = cs.bump(n, seed=7, width=0.3)
-    sp = cs.SphereSW(n, dtype=torch.float32, device=cuda)
+    sp = cs.SphereSW(n, dtype=torch.float32, device=cuda, riemann=riemann)
     sp.initialize(u)
     o.fill(u)
     u0 = np.zeros_like(u)
@@ -96,7 +103,7 @@ def test_fp32_against_fp64_oracle(cuda):
         sp.step(dt)
         for s in range(3):
             o.stage(u, u0, dt, s)
-    err = rel_l2(interior(sp.state().double().cpu().numpy(), n), interior(u, n))
-    print(f"\ncubed sphere n={n}: FP32 vs FP64 oracle after 10 steps, rel L2 "
-          f"(Phi, m2, m3): {err[0]:.2e} {err[2]:.2e} {err[3]:.2e}")
-    assert err[0] <= 1e-5 and max(err[2], err[3]) <= 1e-3
+    err = rel_l2(interior(sp.totals().cpu().numpy(), n), interior(u, n))
+    print(f"\ncubed sphere n={n} ({riemann}): FP32 vs FP64 oracle after 10 steps, "
+          f"rel L2 (Phi, m2, m3): {err[0]:.2e} {err[2]:.2e} {err[3]:.2e}")
+    assert err[[0, 2, 3]].max() <= 1e-5
