@@ -169,6 +169,43 @@ enum {
 };
 int sg_set_timing(sg_handle* h, int32_t on);
 int sg_kernel_times(sg_handle* h, double* ms, int64_t* launches);
+
+/* The FluxRegister's step fields (src/hydro/flux_register.hpp:337-349,
+ * request_step_field / step_field / end_stage):
+ *   S_d <- w1_s S_d + w2_s dt T_d   after every stage s, S_d = 0 at stage 0,
+ * in FP64 whatever the storage type, where T_d is the stage's face-flux
+ * total of direction d (1 = x1, 2 = x2, 3 = x3): the Riemann flux, the
+ * diffusion energy row, the prescribed wall faces (rows IDN and IPR zero on
+ * a reflecting wall) and, with the implicit solve, its x1 face transfers
+ * ("vic.mass_dry" on row IDN, "vic.momentum_t" on rows IVY and IVZ,
+ * src/implicit/implicit_hydro.cpp:625-673).  Each field is
+ * (5, nc3, nc2, nc1) FP64 on the device; the face of index f along d is
+ * the face below cell f, and the faces of the interior cells (f = ng ..
+ * nc_d - ng along d, interior across) are written, the rest never.  Under
+ * SG_F32 with a base the normal-momentum row is the total flux (the base
+ * face pressure added back in FP64).  s1, s2, s3 may each be null (not
+ * requested); a direction the block does not have must be null.  An
+ * implicit block with s1 also needs sg_step_scratch_bytes of FP64 scratch
+ * (16-byte aligned), where its stage stages T_1 for the solve's posts.
+ * The fields are read from the device table, so binding takes effect from
+ * the next stage, captured graphs included. */
+int sg_step_scratch_bytes(const sg_handle* h, int32_t block, size_t* bytes);
+int sg_bind_step_fields(sg_handle* h, int32_t block, double* s1, double* s2,
+                        double* s3, void* scratch, size_t bytes);
+/* The budget sums (BudgetConsumer::totals and ::boundary,
+ * src/diagnostics/budget.cpp:68-155), FP64 on the device, 5 rows per block
+ * (mass, momentum 1-3, energy), out[5 b + row]:
+ *   totals:   sum over the interior cells of the current state's total u
+ *             (the base added back under SG_F32) times the cell volume;
+ *   boundary: the outward transfer of the step fields through the block's
+ *             boundary faces (reflecting and extrapolation faces; periodic
+ *             faces and faces with no boundary function are not boundary),
+ *             sum of sign A_f S_d with sign -1 on a lower, +1 on an upper
+ *             face; accumulate != 0 adds it to out (the consumer's pending
+ *             sum), else stores it. */
+int sg_budget_totals(sg_handle* h, double* out_dev, sg_stream_t stream);
+int sg_budget_boundary(sg_handle* h, double* out_dev, int32_t accumulate,
+                       sg_stream_t stream);
 const char* sg_last_error(void);
 const char* sg_version(void);
 

@@ -61,6 +61,8 @@ class OgBlock(ctypes.Structure):
         ("x1f", _dp),
         ("x1v", _dp),
         ("x2v", _dp),
+        ("step", _dp * 3),
+        ("total", _dp * 3),
     ]
 
 
@@ -249,3 +251,65 @@ class Block:
         f = np.zeros(self.shape)
         lib().og_flux(ctypes.byref(self.b), ptr(w), d, ptr(f))
         return f
+
+    # -- the FluxRegister's step fields and register totals -----------------
+    def request_step_field(self, dim: int) -> np.ndarray:
+        """S_dim (FP64, zero), updated by every stage from here on."""
+        if not hasattr(self, "_steps"):
+            self._steps = [None, None, None]
+        if self._steps[dim - 1] is None:
+            self._steps[dim - 1] = np.zeros(self.shape)
+            self.b.step[dim - 1] = ptr(self._steps[dim - 1])
+        return self._steps[dim - 1]
+
+    def step_field(self, dim: int) -> np.ndarray:
+        return self._steps[dim - 1]
+
+    def keep_totals(self, dim: int) -> np.ndarray:
+        """The buffer each stage copies its register total T_dim into."""
+        if not hasattr(self, "_totals"):
+            self._totals = [None, None, None]
+        if self._totals[dim - 1] is None:
+            self._totals[dim - 1] = np.zeros(self.shape)
+            self.b.total[dim - 1] = ptr(self._totals[dim - 1])
+        return self._totals[dim - 1]
+
+
+# ---------------------------------------------------------------------------
+# the budget sums, restated (BudgetConsumer::totals and ::boundary,
+# src/diagnostics/budget.cpp:68-155) -- the checker of the device sums
+# ---------------------------------------------------------------------------
+def _interior(b: OgBlock):
+    out = []
+    for n in (b.nc3, b.nc2, b.nc1):
+        out.append(slice(b.ng, n - b.ng) if n > 1 else slice(0, 1))
+    return tuple(out)
+
+
+def budget_totals(blk: Block, u: np.ndarray) -> np.ndarray:
+    """(5,) sum over the interior of u times the cell volume."""
+    b = blk.b
+    vol = b.dx3 * (b.dx2 * b.dx1)
+    return np.array([(u[v][_interior(b)] * vol).sum() for v in range(5)])
+
+
+def budget_boundary(blk: Block, steps) -> np.ndarray:
+    """(5,) sum of sign A_f S_d on the reflecting and extrapolation faces of
+    the interior cells (sign -1 lower, +1 upper)."""
+    b = blk.b
+    area = [b.dx3 * b.dx2, b.dx3 * b.dx1, b.dx2 * b.dx1]
+    nc = [b.nc1, b.nc2, b.nc3]
+    out = np.zeros(5)
+    for d in range(3):
+        S = steps[d] if d < len(steps) else None
+        if S is None or nc[d] <= 1:
+            continue
+        for side in (0, 1):
+            if b.bc[2 * d + side] not in (BC_REFLECTING, BC_EXTRAPOLATION):
+                continue
+            w = (1.0 if side else -1.0) * area[d]
+            idx = list(_interior(b))
+            ax = 2 - d  # (k, j, i) axis of direction d
+            idx[ax] = nc[d] - b.ng if side else b.ng
+            out += (S[(slice(None),) + tuple(idx)] * w).reshape(5, -1).sum(axis=1)
+    return out

@@ -687,8 +687,11 @@ static void riemann_face(const og_block* b, const double* wl, const double* wr,
  * only) at the plane's x3 face fluxes, the next plane's face n1 n2 further,
  * added to the divergence after x1 and x2 as CoordinateImpl::divergence does
  * (src/coord/coordinate.cpp:618-662) */
+/* t1, t2 (optional): the plane's register totals T_1, T_2 on the faces of
+ * the interior cells, as the divergence reads them */
 static void tendency_plane(const og_block* b, const double* w, double dt,
-                           double* du, const double* f3) {
+                           double* du, const double* f3, double* t1,
+                           double* t2) {
   const int n1 = b->nc1, n2 = b->nc2, ng = b->ng;
   const size_t nc = ncell(b);
   const int has2 = n2 > 1;
@@ -986,17 +989,27 @@ static void tendency_plane(const og_block* b, const double* w, double dt,
       }
     }
   }
+  if (t1)
+    for (int v = 0; v < 5; ++v)
+      for (int j = jl; j < ju1; ++j)
+        for (int f = il; f <= iu1; ++f) t1[CELL(v, j, f)] = f1[CELL(v, j, f)];
+  if (t2 && has2)
+    for (int v = 0; v < 5; ++v)
+      for (int j = jl; j <= ju1; ++j)
+        for (int i = il; i < iu1; ++i) t2[CELL(v, j, i)] = f2[CELL(v, j, i)];
   free(f1);
   free(f2);
   free(vf1);
   free(vf2);
 }
 
-void og_tendency(const og_block* b, const double* w, double dt, double* du) {
+/* the tendency, and the register totals T_d into T[d - 1] where set */
+static void tendency_reg(const og_block* b, const double* w, double dt,
+                         double* du, double* const* T) {
   build_tables();
   const size_t nc = ncell(b);
   if (b->nc3 == 1) {
-    tendency_plane(b, w, dt, du, NULL);
+    tendency_plane(b, w, dt, du, NULL, T[0], T[1]);
     return;
   }
   /* 3-D (no viscosity, no covariance row): the x3 face fluxes of every
@@ -1013,8 +1026,48 @@ void og_tendency(const og_block* b, const double* w, double dt, double* du) {
   }
   memset(du, 0, sizeof(double) * 5 * nc);
   for (int k = ng; k < n3 - ng; ++k)
-    tendency_plane(b, w + k * plane, dt, du + k * plane, f3 + k * plane);
+    tendency_plane(b, w + k * plane, dt, du + k * plane, f3 + k * plane,
+                   T[0] ? T[0] + k * plane : NULL,
+                   T[1] ? T[1] + k * plane : NULL);
+  if (T[2]) {
+    const int jl = n2 > 1 ? ng : 0, ju1 = n2 > 1 ? n2 - ng : 1;
+    for (int v = 0; v < 5; ++v)
+      for (int k = ng; k <= n3 - ng; ++k)
+        for (int j = jl; j < ju1; ++j)
+          for (int i = ng; i < n1 - ng; ++i) {
+            size_t q = v * nc + k * plane + (size_t)j * n1 + i;
+            T[2][q] = f3[q];
+          }
+  }
   free(f3);
+}
+
+void og_tendency(const og_block* b, const double* w, double dt, double* du) {
+  double* none[3] = {NULL, NULL, NULL};
+  tendency_reg(b, w, dt, du, none);
+}
+
+/* S_d <- w1 S_d + w2 dt T_d on the faces of the interior cells
+ * (FluxRegister::end_stage, src/hydro/flux_register.cpp:761-776, its device
+ * axpy src/utils/step_dt.cu:14-34: the add's alpha form, fused); stage 0
+ * starts from S_d = 0 (begin_step) */
+static void step_recursion(const og_block* b, int d, const double* T,
+                           double* S, double w1, double w2dt, int first) {
+  const int nc[3] = {b->nc1, b->nc2, b->nc3}, ng = b->ng;
+  const size_t n = ncell(b);
+  int lo[3], hi[3]; /* inclusive ranges of (i, j, k) */
+  for (int a = 0; a < 3; ++a) {
+    lo[a] = nc[a] > 1 ? ng : 0;
+    hi[a] = nc[a] > 1 ? nc[a] - ng - 1 : 0;
+  }
+  hi[d - 1] += 1; /* the faces of the interior cells, both ends */
+  for (int v = 0; v < 5; ++v)
+    for (int k = lo[2]; k <= hi[2]; ++k)
+      for (int j = lo[1]; j <= hi[1]; ++j)
+        for (int i = lo[0]; i <= hi[0]; ++i) {
+          size_t q = v * n + ((size_t)k * nc[1] + j) * nc[0] + i;
+          S[q] = first ? fma(w2dt, T[q], 0.) : fma(w2dt, T[q], S[q] * w1);
+        }
 }
 #undef CELL
 
@@ -1028,11 +1081,36 @@ void og_stage(const og_block* b, double* u, double* u0, double dt, int stage) {
   double* w = (double*)malloc(sizeof(double) * nall);
   double* du = (double*)malloc(sizeof(double) * nall);
   og_cons2prim(b, u, w);
-  og_tendency(b, w, dt, du);
+  /* the register totals where a step field or the totals are asked for */
+  double* T[3] = {NULL, NULL, NULL};
+  const int active[3] = {b->nc1 > 1, b->nc2 > 1, b->nc3 > 1};
+  for (int d = 0; d < 3; ++d)
+    if (active[d] && (b->step[d] || b->total[d]))
+      T[d] = (double*)calloc(nall, sizeof(double));
+  tendency_reg(b, w, dt, du, T);
   const double* wt = b->wght[stage];
   /* the vertical implicit correction with dt_corr = wght2 dt
-   * (hydro_forward.cpp:1153-1168) */
-  if (b->implicit_scheme == 9) og_implicit(b, w, wt[2] * dt, du);
+   * (hydro_forward.cpp:1153-1168); its posts enter T_1, whose wall faces
+   * are prescribed again after it (hydro_forward.cpp:1195-1196) */
+  if (b->implicit_scheme == 9) {
+    og_implicit_reg(b, w, wt[2] * dt, du, T[0], dt);
+    if (T[0]) {
+      const int n1 = b->nc1, ng = b->ng;
+      for (size_t r = 0; r < nc / n1; ++r)
+        for (int side = 0; side < 2; ++side) {
+          if (b->bc[side] != OG_BC_REFLECTING) continue;
+          size_t q = r * n1 + (side ? n1 - ng : ng);
+          T[0][OG_IDN * nc + q] = T[0][OG_IPR * nc + q] = 0.;
+        }
+    }
+  }
+  for (int d = 0; d < 3; ++d) {
+    if (!T[d]) continue;
+    if (b->step[d])
+      step_recursion(b, d + 1, T[d], b->step[d], wt[1], wt[2] * dt, stage == 0);
+    if (b->total[d]) memcpy(b->total[d], T[d], sizeof(double) * nall);
+    free(T[d]);
+  }
   /* the RK combine runs on every cell; du is zero outside the interior */
 #pragma omp parallel for schedule(static) if (nall > 4096)
   for (long q = 0; q < (long)nall; ++q)

@@ -53,6 +53,12 @@ typedef struct og_block {
   const double* x1f;
   const double* x1v;
   const double* x2v;
+  /* the FluxRegister's FP64 step fields S_d (5, nc3, nc2, nc1), face f along
+   * d below cell f, updated by og_stage on the faces of the interior cells
+   * (NULL: not requested), and, when set, the stage's face totals T_d on the
+   * same faces (FluxRegister::total after HydroImpl::forward) */
+  double* step[3];
+  double* total[3];
 } og_block;
 
 /* ---- unit functions (pinned against the reference headers) ---- */
@@ -88,6 +94,10 @@ void og_tendency(const og_block* b, const double* w, double dt, double* du);
  * corrected one; dtc = wght2 dt.  Returns the number of failed columns
  * (their du is left as it came in) */
 int og_implicit(const og_block* b, const double* w, double dtc, double* du);
+/* the same, posting the solve's x1 face transfers into the register total
+ * t1 (5, nc3, nc2, nc1) with the step's dt (null t1: none) */
+int og_implicit_reg(const og_block* b, const double* w, double dtc, double* du,
+                    double* t1, double dt);
 /* the well-balanced x1 reference of one column (w strided by `plane`):
  * psf_lo, psf_hi, pref, dsf, dref [nc1] and dsf_lr [2][nc1] */
 void og_ref_column(const og_block* b, const double* w, size_t plane,

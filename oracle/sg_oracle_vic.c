@@ -215,8 +215,13 @@ static void slope_stencil(const double* x, int n, double* wt0, double* wt1,
 
 /* one column: n interior layers; w, du (5 rows each) with row stride `st`
  * and cell stride 1, w readable at layers -1 and n (ghosts) */
+/* t1 (optional): the column's x1 register totals at faces 0..n, strided by
+ * st per variable; the solve posts its face transfers into them
+ * (ImplicitHydroImpl::post_, src/implicit/implicit_hydro.cpp:625-673) with
+ * kdt = dt A_f, the step's dt */
 static int vic_column(const og_block* b, const double* w, size_t st, double* du,
-                      int n, double dtc, const double* x1f, const double* x1v) {
+                      int n, double dtc, const double* x1f, const double* x1v,
+                      double* t1, double kdt) {
   const double grav = b->grav1, gm1 = b->gammad - 1.;
   const double area = b->dx3 * b->dx2, vol = b->dx3 * (b->dx2 * b->dx1);
   M5* A = (M5*)malloc(sizeof(M5) * n);
@@ -479,6 +484,26 @@ static int vic_column(const og_block* b, const double* w, size_t st, double* du,
       free(mv);
       free(rw);
     }
+    if (t1) {
+      /* "vic.mass_dry": the clamped dry transfer q of each face over dt A
+       * (zero on the walls), row IDN; "vic.momentum_t" (full matrix): minus
+       * the prefix of V (du - du0) of the tangential rows from the bottom
+       * wall, top face included, over dt A, rows IVY and IVZ */
+      for (int f = 0; f <= n; ++f)
+        t1[OG_IDN * st + f] = t1[OG_IDN * st + f] + mf_q[f] / kdt;
+      double sy = 0., sz = 0.;
+      for (int f = 0; f <= n; ++f) {
+        double py = 0., pz = 0.;
+        if (f > 0) {
+          sy = sy + (dl[f - 1][2] - du0[2 * n + f - 1]) * vol;
+          sz = sz + (dl[f - 1][3] - du0[3 * n + f - 1]) * vol;
+          py = -sy;
+          pz = -sz;
+        }
+        t1[OG_IVY * st + f] = t1[OG_IVY * st + f] + py / kdt;
+        t1[OG_IVZ * st + f] = t1[OG_IVZ * st + f] + pz / kdt;
+      }
+    }
     free(mf_dn);
     free(mf_M);
     free(mf_q);
@@ -496,6 +521,11 @@ static int vic_column(const og_block* b, const double* w, size_t st, double* du,
 }
 
 int og_implicit(const og_block* b, const double* w, double dtc, double* du) {
+  return og_implicit_reg(b, w, dtc, du, NULL, 0.);
+}
+
+int og_implicit_reg(const og_block* b, const double* w, double dtc, double* du,
+                    double* t1, double dt) {
   const int n1 = b->nc1, n2 = b->nc2, ng = b->ng;
   const size_t nc = (size_t)n1 * n2 * b->nc3;
   const int jl = n2 > 1 ? ng : 0, ju1 = n2 > 1 ? n2 - ng : 1;
@@ -508,7 +538,8 @@ int og_implicit(const og_block* b, const double* w, double dtc, double* du) {
   for (long cidx = 0; cidx < ncols; ++cidx) {
     int j = jl + (int)(cidx % nj), k = kl + (int)(cidx / nj);
     size_t c = ((size_t)k * n2 + j) * n1 + ng;
-    failed += vic_column(b, w + c, nc, du + c, n, dtc, b->x1f + ng, b->x1v + ng);
+    failed += vic_column(b, w + c, nc, du + c, n, dtc, b->x1f + ng, b->x1v + ng,
+                         t1 ? t1 + c : NULL, dt * (b->dx3 * b->dx2));
   }
   return failed;
 }

@@ -105,6 +105,10 @@ SIGNATURES = {
     "sg_prim": (ctypes.c_int, [_vp, ctypes.POINTER(_vp), _vp]),
     "sg_tile": (ctypes.c_int, [_vp, _i32, ctypes.POINTER(_i32)]),
     "sg_launches_per_stage": (ctypes.c_int, [_vp, ctypes.POINTER(_i32)]),
+    "sg_step_scratch_bytes": (ctypes.c_int, [_vp, _i32, ctypes.POINTER(ctypes.c_size_t)]),
+    "sg_bind_step_fields": (ctypes.c_int, [_vp, _i32, _vp, _vp, _vp, _vp, ctypes.c_size_t]),
+    "sg_budget_totals": (ctypes.c_int, [_vp, _vp, _vp]),
+    "sg_budget_boundary": (ctypes.c_int, [_vp, _vp, _i32, _vp]),
     "sg_set_timing": (ctypes.c_int, [_vp, _i32]),
     "sg_kernel_times": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double),
                                        ctypes.POINTER(ctypes.c_int64)]),

@@ -130,6 +130,10 @@ class Batch:
                 _lib.check(self.L.sg_bind_scratch(self.h, b, t.data_ptr(), nb.value),
                            "sg_bind_scratch")
                 self.scratch.append(t)
+        # the FluxRegister's step fields per block and direction, and the
+        # implicit blocks' staging scratch for them (request_step_field)
+        self.steps = [[None, None, None] for _ in range(self.nblock)]
+        self.step_scratch = [None] * self.nblock
         self.dt = torch.zeros(self.nblock, dtype=torch.float64, device=device)
         self.redo = torch.zeros(self.nblock, dtype=torch.int32, device=device)
         self.flags = torch.zeros(self.nblock, dtype=torch.int32, device=device)
@@ -253,3 +257,59 @@ class Batch:
         cnt = (ctypes.c_int64 * n)()
         _lib.check(self.L.sg_kernel_times(self.h, ms, cnt), "sg_kernel_times")
         return {k: (ms[i], cnt[i]) for i, k in enumerate(_lib.KERNELS) if cnt[i]}
+
+    # -- the FluxRegister's step fields and the budget sums ------------------
+    def request_step_field(self, b: int, dim: int) -> torch.Tensor:
+        """Allocate and bind the FP64 step field S_dim of block b
+        (FluxRegister::request_step_field, src/hydro/flux_register.hpp:270):
+        (5, nc3, nc2, nc1), zero, written by every stage from the next step
+        on.  Returns the field."""
+        if dim not in (1, 2, 3):
+            raise ValueError(f"request_step_field: dim {dim}")
+        nc = {1: self.blocks[b]["nc1"], 2: self.blocks[b]["nc2"],
+              3: self.blocks[b]["nc3"]}[dim]
+        if nc <= 1:
+            raise ValueError(f"request_step_field: block {b} has no x{dim} faces")
+        if self.steps[b][dim - 1] is None:
+            self.steps[b][dim - 1] = torch.zeros(self.shapes[b], dtype=torch.float64,
+                                                 device=self.device)
+        self._bind_steps(b)
+        return self.steps[b][dim - 1]
+
+    def step_field(self, b: int, dim: int) -> Optional[torch.Tensor]:
+        return self.steps[b][dim - 1]
+
+    def _bind_steps(self, b: int) -> None:
+        f = self.steps[b]
+        nb = ctypes.c_size_t()
+        _lib.check(self.L.sg_step_scratch_bytes(self.h, b, ctypes.byref(nb)),
+                   "sg_step_scratch_bytes")
+        if f[0] is not None and nb.value and self.step_scratch[b] is None:
+            self.step_scratch[b] = torch.empty(nb.value // 8, dtype=torch.float64,
+                                               device=self.device)
+        t = self.step_scratch[b]
+        ptr = [x.data_ptr() if x is not None else None for x in f]
+        _lib.check(self.L.sg_bind_step_fields(
+            self.h, b, ptr[0], ptr[1], ptr[2],
+            t.data_ptr() if t is not None else None,
+            t.numel() * 8 if t is not None else 0), "sg_bind_step_fields")
+
+    def budget_totals(self, stream=None, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """(nblock, 5) FP64 on the device: each block's interior sum of the
+        total conserved state times the cell volume."""
+        if out is None:
+            out = torch.empty((self.nblock, 5), dtype=torch.float64, device=self.device)
+        _lib.check(self.L.sg_budget_totals(self.h, out.data_ptr(), _stream(stream)),
+                   "sg_budget_totals")
+        return out
+
+    def budget_boundary(self, out: Optional[torch.Tensor] = None,
+                        accumulate: bool = False, stream=None) -> torch.Tensor:
+        """(nblock, 5) FP64 on the device: the outward transfer of the step
+        fields through each block's boundary faces; accumulate adds it to
+        out."""
+        if out is None:
+            out = torch.zeros((self.nblock, 5), dtype=torch.float64, device=self.device)
+        _lib.check(self.L.sg_budget_boundary(self.h, out.data_ptr(), int(bool(accumulate)),
+                                             _stream(stream)), "sg_budget_boundary")
+        return out

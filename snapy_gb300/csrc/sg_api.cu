@@ -37,7 +37,11 @@ using sg::StageParams;
                                    cudaStream_t);                              \
   extern "C" int sg_launch_reduce##sfx(const BlockDev*, int, int,              \
                                        unsigned long long*, int*, size_t,      \
-                                       cudaStream_t);
+                                       cudaStream_t);                          \
+  extern "C" int sg_launch_budget_totals##sfx(const BlockDev*, int, int,       \
+                                              double*, cudaStream_t);          \
+  extern "C" int sg_launch_budget_boundary##sfx(const BlockDev*, int, double*, \
+                                                int, cudaStream_t);
 SG_DECLARE(_f64)
 SG_DECLARE(_f32)
 
@@ -222,6 +226,9 @@ int upload(sg_handle* h, cudaStream_t s) {
         (h->host[b].nc3 > 1 && !h->host[b].dv3))
       return fail(SG_ERR_STATE, "block %d: the scratch (implicit solve, x3 "
                   "faces) is not bound (sg_bind_scratch)", b);
+    if (h->host[b].implicit && h->host[b].step[0] && !h->host[b].t1)
+      return fail(SG_ERR_STATE, "block %d: the x1 step field of an implicit "
+                  "block needs its scratch (sg_bind_step_fields)", b);
   }
   cudaError_t e = cudaMemcpyAsync(h->dev, h->host.data(),
                                   sizeof(BlockDev) * h->nblock,
@@ -506,6 +513,75 @@ int sg_bind_scratch(sg_handle* h, int32_t block, void* scratch, size_t bytes) {
   return 0;
 }
 
+int sg_step_scratch_bytes(const sg_handle* h, int32_t block, size_t* bytes) {
+  if (!h || !bytes || block < 0 || block >= h->nblock)
+    return fail(SG_ERR_ARG, "sg_step_scratch_bytes: block %d", block);
+  const BlockDev& B = h->host[block];
+  size_t nx1 = B.nc1 - 2 * B.ng;
+  size_t ncols = (B.nc2 > 1 ? B.nc2 - 2 * B.ng : 1) *
+                 (size_t)(B.nc3 > 1 ? B.nc3 - 2 * B.ng : 1);
+  *bytes = B.implicit ? 5 * (nx1 + 1) * ncols * sizeof(double) : 0;
+  return 0;
+}
+
+int sg_bind_step_fields(sg_handle* h, int32_t block, double* s1, double* s2,
+                        double* s3, void* scratch, size_t bytes) {
+  if (!h || block < 0 || block >= h->nblock)
+    return fail(SG_ERR_ARG, "sg_bind_step_fields: block %d", block);
+  BlockDev& B = h->host[block];
+  if ((s2 && B.nc2 <= 1) || (s3 && B.nc3 <= 1))
+    return fail(SG_ERR_ARG, "sg_bind_step_fields: block %d has no x%d faces",
+                block, s2 && B.nc2 <= 1 ? 2 : 3);
+  for (double* f : {s1, s2, s3})
+    if (reinterpret_cast<uintptr_t>(f) % 8)
+      return fail(SG_ERR_ARG, "sg_bind_step_fields: misaligned field");
+  size_t need = 0;
+  sg_step_scratch_bytes(h, block, &need);
+  if (s1 && need) {
+    if (!scratch || bytes < need)
+      return fail(SG_ERR_ARG, "sg_bind_step_fields: block %d needs %zu bytes "
+                  "of scratch, got %zu", block, need, bytes);
+    if (reinterpret_cast<uintptr_t>(scratch) % 16)
+      return fail(SG_ERR_ARG, "sg_bind_step_fields: misaligned scratch");
+  }
+  B.step[0] = s1;
+  B.step[1] = s2;
+  B.step[2] = s3;
+  B.t1 = s1 && need ? static_cast<double*>(scratch) : nullptr;
+  h->dirty = true;
+  // the table goes to the device now when it can: a replayed graph reads it
+  // without another sg_stage call to upload it
+  for (int b = 0; b < h->nblock; ++b)
+    for (int q = 0; q < 3; ++q)
+      if (!h->host[b].buf[q]) return 0;
+  return upload(h, nullptr);
+}
+
+int sg_budget_totals(sg_handle* h, double* out_dev, sg_stream_t stream) {
+  if (!h || !out_dev) return fail(SG_ERR_ARG, "sg_budget_totals: null");
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  int rc = upload(h, s);
+  if (rc) return rc;
+  rc = f64(h) ? sg_launch_budget_totals_f64(h->dev, h->nblock, h->cur, out_dev, s)
+              : sg_launch_budget_totals_f32(h->dev, h->nblock, h->cur, out_dev, s);
+  if (rc) return cuda_fail((cudaError_t)rc, "sg_budget_totals");
+  return 0;
+}
+
+int sg_budget_boundary(sg_handle* h, double* out_dev, int32_t accumulate,
+                       sg_stream_t stream) {
+  if (!h || !out_dev) return fail(SG_ERR_ARG, "sg_budget_boundary: null");
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  int rc = upload(h, s);
+  if (rc) return rc;
+  rc = f64(h) ? sg_launch_budget_boundary_f64(h->dev, h->nblock, out_dev,
+                                              accumulate, s)
+              : sg_launch_budget_boundary_f32(h->dev, h->nblock, out_dev,
+                                              accumulate, s);
+  if (rc) return cuda_fail((cudaError_t)rc, "sg_budget_boundary");
+  return 0;
+}
+
 int sg_set_current(sg_handle* h, int32_t current) {
   if (!h || current < 0 || current > 2)
     return fail(SG_ERR_ARG, "sg_set_current: %d", current);
@@ -634,6 +710,7 @@ int sg_stage(sg_handle* h, int32_t stage, const double* dt_dev,
   p.w1 = h->scheme.wght[stage][1];
   p.w2 = h->scheme.wght[stage][2];
   p.dt = dt_dev;
+  p.first = stage == 0;
   p.max_nc1 = h->max_nc1;
   // events between the launches when timing is on and the stream is not
   // being captured: ev[0] (x3 ev[6]) stage ev[1] (assemble ev[2] solve

@@ -52,6 +52,16 @@ __device__ __forceinline__ int find_block(const BlockDev* tab, int nblock,
   return lo;
 }
 
+// the FluxRegister's step-field recursion at one face
+// (FluxRegister::end_stage, src/hydro/flux_register.cpp:761-776):
+// S <- w1 S + w2 dt T in FP64, the add's alpha form fused as the
+// reference's device axpy is (src/utils/step_dt.cu:14-34); at stage 0 the
+// field starts from zero (begin_step), so w1 S is +0
+__device__ __forceinline__ void step_set(double* s, double t, double w1,
+                                         double w2dt, bool first) {
+  *s = first ? fma(w2dt, t, 0.) : fma(w2dt, t, *s * w1);
+}
+
 // face states of 5 consecutive cells: ILT (cp, the -side of the upper face of
 // the centre cell) and IRT (cm, the +side of its lower face)
 template <bool WENO>
@@ -686,6 +696,48 @@ __device__ __forceinline__ void stage_tile(const BlockDev* __restrict__ tab,
   }
   __syncthreads();
 
+  // the stage's face totals T_1, T_2 are final here: the FluxRegister's
+  // step fields (FP64; under a base the normal-momentum row gets the base
+  // face pressure back).  An implicit block stages T_1 for the solve's
+  // posts, which its finish kernel adds before the recursion.  Each face
+  // has one writer: x2 faces shared by two tiles go to the upper tile,
+  // except the block's last face
+  if (B.step[0] || B.step[1]) {
+    const double w1s = p.w1, w2dt = p.w2 * dt;
+    const bool first = p.first != 0;
+    const size_t nx2i = has2 ? nc2 - 2 * ng : 1;
+    if (double* S1 = B.step[0]) {
+      const size_t ncols = nx2i * (B.nc3 > 1 ? B.nc3 - 2 * ng : 1);
+      for (int idx = threadIdx.x; idx < ntj * nf1; idx += blockDim.x) {
+        const int jt = idx / nf1, fi = idx - jt * nf1, f = il + fi;
+        const size_t col = (size_t)kk * nx2i + (j0 + jt - hj);
+        const size_t c = koff + (size_t)(j0 + jt) * nc1 + f;
+#pragma unroll
+        for (int v = 0; v < NHYDRO; ++v) {
+          double t = (double)F1[v * f1stride + idx];
+          if (pbf && v == IVX) t = t + pbf[f];
+          if (B.implicit)
+            B.t1[((size_t)v * ncols + col) * nf1 + fi] = t;
+          else
+            step_set(S1 + v * plane + c, t, w1s, w2dt, first);
+        }
+      }
+    }
+    if (double* S2 = B.step[1]) {
+      for (int idx = threadIdx.x; idx < (ntj + 1) * nx1; idx += blockDim.x) {
+        const int jf = idx / nx1, i = il + (idx - jf * nx1);
+        if (jf == ntj && j0 + ntj != jend) continue;
+        const size_t c = koff + (size_t)(j0 + jf) * nc1 + i;
+#pragma unroll
+        for (int v = 0; v < NHYDRO; ++v) {
+          double t = (double)F2[v * f2stride + idx];
+          if (pbc && v == IVY) t = t + pbc[i];
+          step_set(S2 + v * plane + c, t, w1s, w2dt, first);
+        }
+      }
+    }
+  }
+
   // (6) divergence, du = -dt div, gravity, viscous momentum, the x1 gravity
   // energy correction, and the RK combine on the interior cells
   const real a1 = real(B.dx3 * B.dx2), a2 = real(B.dx3 * B.dx1);
@@ -933,6 +985,18 @@ __global__ void __launch_bounds__(kThreads)
         riemann<RK>(wl, wr, gammad, 3, flx);
       if ((f == ng && wlo) || (f == ng + nx3 && whi))
         flx[IDN] = flx[IPR] = real(0);
+      // the x3 step field; a chunk owns its faces but the top one, which
+      // the next chunk owns, except the block's last face
+      if (B.step[2] && (f < k1 || k1 == ng + nx3)) {
+        const double w2dt = p.w2 * p.dt[blockIdx.y];
+        double* S3 = B.step[2] + (size_t)f * kst + col;
+#pragma unroll
+        for (int v = 0; v < NHYDRO; ++v) {
+          double t = (double)flx[v];
+          if (pbc && v == IVZ) t = t + pbc[i];
+          step_set(S3 + v * plane, t, p.w1, w2dt, p.first != 0);
+        }
+      }
       if (f > k0) {
         // cell f - 1 between faces f - 1 and f
         const int k = f - 1;
@@ -1126,6 +1190,105 @@ __global__ void __launch_bounds__(kThreads)
 
 #include "sg_vic.cuh"
 
+// ---------------------------------------------------------------------------
+// the budget sums (BudgetConsumer::totals and ::boundary,
+// src/diagnostics/budget.cpp:68-155): one CTA per block, each thread sums a
+// fixed stride of the cells (or faces), then a fixed-order tree, so the
+// sums are the same on every run and in a captured graph
+// ---------------------------------------------------------------------------
+constexpr int kBudgetThreads = 512;
+
+__device__ void budget_reduce(double* acc, double* out, bool accumulate) {
+  __shared__ double sh[NHYDRO][kBudgetThreads];
+  const int t = threadIdx.x;
+#pragma unroll
+  for (int v = 0; v < NHYDRO; ++v) sh[v][t] = acc[v];
+  __syncthreads();
+  for (int s = kBudgetThreads / 2; s > 0; s >>= 1) {
+    if (t < s) {
+#pragma unroll
+      for (int v = 0; v < NHYDRO; ++v) sh[v][t] = sh[v][t] + sh[v][t + s];
+    }
+    __syncthreads();
+  }
+  if (t < NHYDRO) out[t] = accumulate ? out[t] + sh[t][0] : sh[t][0];
+}
+
+// sum over the interior of the total u (the base added back) times the
+// cell volume, per row
+__global__ void __launch_bounds__(kBudgetThreads)
+    budget_totals_kernel(const BlockDev* __restrict__ tab, int which,
+                         double* out) {
+  const BlockDev& B = tab[blockIdx.x];
+  const int nc1 = B.nc1, nc2 = B.nc2, nc3 = B.nc3, ng = B.ng;
+  const int nx1 = nc1 - 2 * ng, nx2 = nc2 > 1 ? nc2 - 2 * ng : 1,
+            nx3 = nc3 > 1 ? nc3 - 2 * ng : 1;
+  const int o2 = nc2 > 1 ? ng : 0, o3 = nc3 > 1 ? ng : 0;
+  const size_t plane = (size_t)nc1 * nc2 * nc3;
+  const real* u = static_cast<const real*>(B.buf[which]);
+  const double* rb = B.base ? base_rho(B.base, nc1) : nullptr;
+  const double* eb = B.base ? base_e(B.base, nc1) : nullptr;
+  const double vol = B.dx3 * (B.dx2 * B.dx1);
+  const size_t n = (size_t)nx1 * nx2 * nx3;
+  double acc[NHYDRO] = {0., 0., 0., 0., 0.};
+  for (size_t e = threadIdx.x; e < n; e += kBudgetThreads) {
+    const int i = ng + (int)(e % nx1);
+    const size_t jk = e / nx1;
+    const int j = o2 + (int)(jk % nx2), k = o3 + (int)(jk / nx2);
+    const size_t c = ((size_t)k * nc2 + j) * nc1 + i;
+#pragma unroll
+    for (int v = 0; v < NHYDRO; ++v) {
+      double x = (double)u[v * plane + c];
+      if (rb && v == IDN) x = x + rb[i];
+      if (eb && v == IPR) x = x + eb[i];
+      acc[v] += x * vol;
+    }
+  }
+  budget_reduce(acc, out + NHYDRO * blockIdx.x, false);
+}
+
+// the outward transfer of the step fields through the boundary faces: on
+// each boundary face of the interior cells, sign A_f S_d (sign -1 on the
+// lower, +1 on the upper face of direction d)
+__global__ void __launch_bounds__(kBudgetThreads)
+    budget_boundary_kernel(const BlockDev* __restrict__ tab, double* out,
+                           int accumulate) {
+  const BlockDev& B = tab[blockIdx.x];
+  const int nc[3] = {B.nc1, B.nc2, B.nc3};
+  const int ng = B.ng;
+  const size_t plane = (size_t)nc[0] * nc[1] * nc[2];
+  const double area[3] = {B.dx3 * B.dx2, B.dx3 * B.dx1, B.dx2 * B.dx1};
+  int lo[3], nx[3];
+  for (int a = 0; a < 3; ++a) {
+    lo[a] = nc[a] > 1 ? ng : 0;
+    nx[a] = nc[a] > 1 ? nc[a] - 2 * ng : 1;
+  }
+  double acc[NHYDRO] = {0., 0., 0., 0., 0.};
+  for (int d = 0; d < 3; ++d) {
+    const double* S = B.step[d];
+    if (!S) continue;
+    // the two transverse axes of direction d, fastest first
+    const int ta = d == 0 ? 1 : 0, tb = d == 2 ? 1 : 2;
+    const size_t nt = (size_t)nx[ta] * nx[tb];
+    for (int side = 0; side < 2; ++side) {
+      const int bc = B.bc[2 * d + side];
+      if (bc != kBcReflecting && bc != kBcExtrapolation) continue;
+      const double w = (side ? 1. : -1.) * area[d];
+      const int f = side ? nc[d] - ng : ng;
+      for (size_t e = threadIdx.x; e < nt; e += kBudgetThreads) {
+        int idx[3];
+        idx[d] = f;
+        idx[ta] = lo[ta] + (int)(e % nx[ta]);
+        idx[tb] = lo[tb] + (int)(e / nx[ta]);
+        const size_t c = ((size_t)idx[2] * nc[1] + idx[1]) * nc[0] + idx[0];
+#pragma unroll
+        for (int v = 0; v < NHYDRO; ++v) acc[v] += S[v * plane + c] * w;
+      }
+    }
+  }
+  budget_reduce(acc, out + NHYDRO * blockIdx.x, accumulate != 0);
+}
+
 }  // namespace
 }  // namespace sg
 
@@ -1254,5 +1417,22 @@ extern "C" int SG_NAME(sg_launch_reduce)(const BlockDev* tab, int nblock,
   if (gx > 64) gx = 64;
   reduce_kernel<<<dim3(gx, nblock), kThreads, 0, stream>>>(tab, which, red,
                                                            flag);
+  return (int)cudaGetLastError();
+}
+
+extern "C" int SG_NAME(sg_launch_budget_totals)(const BlockDev* tab,
+                                                int nblock, int which,
+                                                double* out,
+                                                cudaStream_t stream) {
+  budget_totals_kernel<<<nblock, kBudgetThreads, 0, stream>>>(tab, which, out);
+  return (int)cudaGetLastError();
+}
+
+extern "C" int SG_NAME(sg_launch_budget_boundary)(const BlockDev* tab,
+                                                  int nblock, double* out,
+                                                  int accumulate,
+                                                  cudaStream_t stream) {
+  budget_boundary_kernel<<<nblock, kBudgetThreads, 0, stream>>>(tab, out,
+                                                                accumulate);
   return (int)cudaGetLastError();
 }

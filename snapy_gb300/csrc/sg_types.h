@@ -64,6 +64,12 @@ struct BlockDev {
   // storage type, laid out (v, k, j, i) over the interior; written by the x3
   // sweep, added to the divergence by the stage kernel
   void* dv3;
+  // the FluxRegister's FP64 step fields S_d (5, nc3, nc2, nc1), face f
+  // along d below cell f (null: not requested), and, for an implicit block
+  // with S_1, the stage's x1 totals T_1 staged for the solve's posts,
+  // laid out (v, column, face) over the interior columns and nx1 + 1 faces
+  double* step[3];
+  double* t1;
 };
 
 // offsets into BlockDev::base
@@ -87,6 +93,7 @@ struct StageParams {
   int32_t scale;        // InterpOptions::scale
   double w0, w1, w2;    // RK weights of this stage
   const double* dt;     // device scalar: the host dt or a captured graph's
+  int32_t first;        // stage 0: the step fields start from zero
   int32_t smem_rows;    // x1 lines held in shared memory per tile
   int32_t max_nc1;
 };

@@ -806,6 +806,52 @@ __global__ void __launch_bounds__(NL == 32 ? 32 * kVicWarps : kThreads)
     }
     vsync<NL>();
   }
+  // the x1 step field of an implicit block (FluxRegister::end_stage after
+  // ImplicitHydroImpl::post_, src/implicit/implicit_hydro.cpp:625-673): the
+  // stage's T_1 plus the solve's face transfers per unit area and time,
+  // "vic.mass_dry" q / (dt A) on row IDN and "vic.momentum_t"
+  // -sum_{k < f} (du - du0)_k V / (dt A) on rows IVY and IVZ (the prefix from
+  // the bottom wall, top face included), then the prescribed wall faces.  A
+  // failed column posts nothing.  Each face's adds run in the reference's
+  // order, +0 posts included (a -0 total becomes +0)
+  if (double* S1 = B.step[0]) {
+    const double dt = p.dt[blockIdx.y];
+    const double kdt = dt * (B.dx3 * B.dx2);
+    const double w1s = p.w1, w2dt = p.w2 * dt;
+    const bool first = p.first != 0;
+    const int nf = n + 1;
+    const double* T = B.t1;
+    const bool wlo = B.bc[0] == kBcReflecting, whi = B.bc[1] == kBcReflecting;
+    auto tot = [&](int v, int f) { return T[((size_t)v * ncol + col) * nf + f]; };
+    auto at = [&](int v, int f) { return S1 + v * plane + jrow * nc1 + ng + f; };
+    for (int f = lane; f < nf; f += NL) {
+      double t0 = tot(IDN, f), t1 = tot(IVX, f), t4 = tot(IPR, f);
+      if (ok) t0 = t0 + mq[f] / kdt;
+      if ((f == 0 && wlo) || (f == n && whi)) t0 = t4 = 0.;
+      step_set(at(IDN, f), t0, w1s, w2dt, first);
+      step_set(at(IVX, f), t1, w1s, w2dt, first);
+      step_set(at(IPR, f), t4, w1s, w2dt, first);
+    }
+    if (lane == 0) {
+      double sy = 0., sz = 0.;
+      for (int f = 0; f < nf; ++f) {
+        double ty = tot(IVY, f), tz = tot(IVZ, f);
+        if (ok) {
+          double py = 0., pz = 0.;
+          if (f > 0) {
+            sy = sy + (D[(f - 1) * 5 + 2] - du0[2 * cs + f - 1]) * vol;
+            sz = sz + (D[(f - 1) * 5 + 3] - du0[3 * cs + f - 1]) * vol;
+            py = -sy;
+            pz = -sz;
+          }
+          ty = ty + py / kdt;
+          tz = tz + pz / kdt;
+        }
+        step_set(at(IVY, f), ty, w1s, w2dt, first);
+        step_set(at(IVZ, f), tz, w1s, w2dt, first);
+      }
+    }
+  }
   // the RK combine of the column (a failed column keeps the explicit du)
   const double* dsel = ok ? S.du + col * n : du0;
   const real w0 = real(p.w0), w1 = real(p.w1), w2 = real(p.w2);

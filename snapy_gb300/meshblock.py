@@ -121,6 +121,44 @@ def block_of(options: MeshBlockOptions, tj: int = 0) -> dict:
             "implicit_f32": bool(h.icorr) and h.icorr.precision == "float32"}
 
 
+class FluxRegister:
+    """The step fields of a block's FluxRegister
+    (src/hydro/flux_register.hpp:241-402): S_d <- w1 S_d + w2 dt T_d after
+    every stage, in FP64, over the stage's face-flux totals T_d (the Riemann
+    flux, the diffusion energy row, the prescribed walls and the implicit
+    solve's x1 posts).  The totals themselves are not kept: the stage kernel
+    folds them into S_d where it makes them."""
+
+    def __init__(self, block: "MeshBlock"):
+        self._blk = block
+
+    def _active(self, dim: int) -> bool:
+        c = self._blk.options.coord()
+        return {1: c.nc1, 2: c.nc2, 3: c.nc3}.get(dim, 1) > 1
+
+    def request_step_field(self, dim: int) -> None:
+        """A reader asks for S_dim; it holds the step's sum from the next
+        step on (request_step_field, flux_register.hpp:270)."""
+        if not self._active(dim):
+            raise RuntimeError(f"[FluxRegister] request_step_field: direction "
+                               f"{dim} has no faces in this block")
+        self._blk._step_dims.add(dim)
+        if self._blk._batch is not None:
+            with torch.cuda.device(self._blk.device):
+                self._blk._batch.request_step_field(0, dim)
+
+    def has_step_field(self, dim: int) -> bool:
+        return dim in self._blk._step_dims
+
+    def step_field(self, dim: int) -> torch.Tensor:
+        """S_dim, (5, nc3, nc2, nc1) FP64 on the block's device; the faces of
+        the interior cells are written, the rest stay zero."""
+        if dim not in self._blk._step_dims:
+            raise RuntimeError(f"[FluxRegister] step_field({dim}) was not "
+                               "requested")
+        return self._blk.batch.step_field(0, dim)
+
+
 @dataclass
 class _Intg:
     options: object
@@ -150,6 +188,7 @@ class MeshBlock:
         self._report = {"captures": 0, "replays": 0, "eager": 0, "graphs": 0,
                         "host": 0}
         self._seen = set()
+        self._step_dims = set()  # the requested FluxRegister step fields
 
     # -- module-like API -----------------------------------------------------
     def to(self, device, dtype: Optional[torch.dtype] = None) -> "MeshBlock":
@@ -172,7 +211,14 @@ class MeshBlock:
     def batch(self) -> Batch:
         if self._batch is None:
             self._batch = Batch(self._scheme, [self._block], self.device, self.dtype)
+            for d in sorted(self._step_dims):
+                self._batch.request_step_field(0, d)
         return self._batch
+
+    def flux_register(self) -> "FluxRegister":
+        """The block's FluxRegister (HydroImpl::flux_register,
+        src/hydro/hydro.hpp:135): its FP64 step fields."""
+        return FluxRegister(self)
 
     def nc(self):
         c = self.options.coord()
