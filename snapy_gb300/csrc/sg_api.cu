@@ -95,8 +95,11 @@ __global__ void finish_check_kernel(int nblock, unsigned long long* red,
   if (!(rmin > 1.001 * dfloor)) f |= 1;
   if (!(pmin > 1.001 * pfloor)) f |= 1;
   if (nan[b]) f |= 1 | 8;
-  // bit 5: a column of the vertical implicit solve failed this step
-  if (status[b]) f |= 32;
+  // bit 5: a column of the vertical implicit solve failed this step; bit 6:
+  // a tile's shared-memory staging did not arrive in time (the stage kernel
+  // gave up on it)
+  if (status[b] & ~sg::kStatusStaging) f |= 32;
+  if (status[b] & sg::kStatusStaging) f |= 64;
   status[b] = 0;
   flags[b] = f;
   red[4 * b] = red[4 * b + 1] = red[4 * b + 2] = kKeyInf;
@@ -711,6 +714,7 @@ int sg_stage(sg_handle* h, int32_t stage, const double* dt_dev,
   p.w2 = h->scheme.wght[stage][2];
   p.dt = dt_dev;
   p.first = stage == 0;
+  p.status = h->status;
   p.max_nc1 = h->max_nc1;
   // events between the launches when timing is on and the stream is not
   // being captured: ev[0] (x3 ev[6]) stage ev[1] (assemble ev[2] solve

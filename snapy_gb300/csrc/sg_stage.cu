@@ -62,6 +62,50 @@ __device__ __forceinline__ void step_set(double* s, double t, double w1,
   *s = first ? fma(w2dt, t, 0.) : fma(w2dt, t, *s * w1);
 }
 
+// ---- shared-memory staging by 1-D bulk copies (TMA) on an mbarrier ----
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n"
+               "fence.mbarrier_init.release.cluster;" ::"r"(smem_u32(bar)),
+               "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+                   smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n"
+      " mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// global -> this CTA's shared memory, `bytes` (a multiple of 16) from two
+// 16-byte aligned addresses, completing on `bar`
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src,
+                                         uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes "
+      "[%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+// the generic-proxy accesses before it are ordered before later bulk copies
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+// polls of a staging wait (64 ns apart) before the tile is given up
+constexpr int kStagingPolls = 1 << 22;
+
 // face states of 5 consecutive cells: ILT (cp, the -side of the upper face of
 // the centre cell) and IRT (cm, the +side of its lower face)
 template <bool WENO>
@@ -326,9 +370,10 @@ __device__ __forceinline__ void ref_cell(const double* ropc,
 
 // one tile of the batch: `tj` x2 columns of one block over its full x1
 template <int RK, bool SHOCK>
-__device__ __forceinline__ void stage_tile(const BlockDev* __restrict__ tab,
+__device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
                                            const StageParams& p, int tile,
-                                           real* sm) {
+                                           real* sm, uint64_t* bar,
+                                           uint32_t& phase, int* fail) {
   const int bi = find_block(tab, p.nblock, tile);
   const BlockDev& B = tab[bi];
   const int nc1 = B.nc1, nc2 = B.nc2, ng = B.ng;
@@ -373,18 +418,63 @@ __device__ __forceinline__ void stage_tile(const BlockDev* __restrict__ tab,
   real* F2 = sm + L.f2;
   const int f2stride = (ntj + 1) * nx1;
 
-  // (1) the tile and its x2 halo, U -> W
+  // (1) the tile and its x2 halo, U -> W.  The R rows of a variable are one
+  // contiguous span of R nc1 values; where every span starts and ends on 16
+  // bytes, one thread stages the five spans by bulk copies (TMA) into W and
+  // the tile converts in place, else every thread loads its cells
   const size_t row0 = koff + (size_t)(j0 - hj) * nc1;
-  for (int idx = threadIdx.x; idx < R * nc1; idx += blockDim.x) {
-    real uc[NHYDRO], wc[NHYDRO];
+  const uint32_t span = (uint32_t)(R * nc1 * sizeof(real));
+  const bool bulk =
+      span % 16 == 0 && (plane * sizeof(real)) % 16 == 0 &&
+      (reinterpret_cast<uintptr_t>(uin + row0) % 16) == 0;
+  if (bulk) {
+    if (threadIdx.x == 0) {
+      fence_proxy_async();  // the previous tile's reads of W come first
+      mbar_expect_tx(bar, NHYDRO * span);
 #pragma unroll
-    for (int v = 0; v < NHYDRO; ++v) uc[v] = uin[v * plane + row0 + idx];
-    // with a base: rho_b + rho', and p' = (g - 1)(E' - ke) since p_b is
-    // (g - 1) e_b
-    if (rb) uc[IDN] = real(rb[idx % nc1]) + uc[IDN];
-    cons2prim<real>(uc, wc, gammad);
+      for (int v = 0; v < NHYDRO; ++v)
+        bulk_g2s(W + v * wstride, uin + v * plane + row0, span, bar);
+      bool ok = false;
+      for (int it = 0; it < kStagingPolls; ++it) {
+        if (mbar_test(bar, phase)) {
+          ok = true;
+          break;
+        }
+        __nanosleep(64);
+      }
+      if (!ok) {
+        // give the tile up: flag the block, then wait (bounded again) for
+        // the copies still in flight before the CTA leaves
+        atomicOr(&p.status[bi], kStatusStaging);
+        for (int it = 0; it < kStagingPolls && !mbar_test(bar, phase); ++it)
+          __nanosleep(1024);
+      }
+      *fail = ok ? 0 : 1;
+    }
+    __syncthreads();
+    phase ^= 1u;
+    if (*fail) return false;
+    for (int idx = threadIdx.x; idx < R * nc1; idx += blockDim.x) {
+      real uc[NHYDRO], wc[NHYDRO];
 #pragma unroll
-    for (int v = 0; v < NHYDRO; ++v) W[v * wstride + idx] = wc[v];
+      for (int v = 0; v < NHYDRO; ++v) uc[v] = W[v * wstride + idx];
+      if (rb) uc[IDN] = real(rb[idx % nc1]) + uc[IDN];
+      cons2prim<real>(uc, wc, gammad);
+#pragma unroll
+      for (int v = 0; v < NHYDRO; ++v) W[v * wstride + idx] = wc[v];
+    }
+  } else {
+    for (int idx = threadIdx.x; idx < R * nc1; idx += blockDim.x) {
+      real uc[NHYDRO], wc[NHYDRO];
+#pragma unroll
+      for (int v = 0; v < NHYDRO; ++v) uc[v] = uin[v * plane + row0 + idx];
+      // with a base: rho_b + rho', and p' = (g - 1)(E' - ke) since p_b is
+      // (g - 1) e_b
+      if (rb) uc[IDN] = real(rb[idx % nc1]) + uc[IDN];
+      cons2prim<real>(uc, wc, gammad);
+#pragma unroll
+      for (int v = 0; v < NHYDRO; ++v) W[v * wstride + idx] = wc[v];
+    }
   }
   __syncthreads();
 
@@ -836,6 +926,7 @@ __device__ __forceinline__ void stage_tile(const BlockDev* __restrict__ tab,
       uout[q] = w0 * u0[q] + w1 * uin[q] + w2 * du[v];
     }
   }
+  return true;
 }
 
 // the stage of every tile of the batch in ONE persistent launch: a grid of
@@ -846,8 +937,13 @@ __global__ void __launch_bounds__(kThreads)
     stage_kernel(const BlockDev* __restrict__ tab, StageParams p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   real* sm = reinterpret_cast<real*>(smem_raw);
+  __shared__ uint64_t bar;  // the staging barrier, one phase per bulk tile
+  __shared__ int fail;
+  if (threadIdx.x == 0) mbar_init(&bar, 1);
+  __syncthreads();
+  uint32_t phase = 0;
   for (int tile = blockIdx.x; tile < p.ntile; tile += gridDim.x) {
-    stage_tile<RK, SHOCK>(tab, p, tile, sm);
+    if (!stage_tile<RK, SHOCK>(tab, p, tile, sm, &bar, phase, &fail)) return;
     __syncthreads();  // the next tile reuses the shared memory
   }
 }

@@ -83,6 +83,9 @@ __host__ __device__ inline const double* base_r(const double* b, int nc1) { retu
 // a, b, c (25 each), the solution and the two Woodbury vectors (5 each)
 constexpr int kVicDoublesPerCell = 100;
 
+// a tile's bulk-copy wait ran out (status bit; the step is rejected)
+constexpr int32_t kStatusStaging = 1 << 30;
+
 // what a stage launch needs besides the table
 struct StageParams {
   int32_t nblock;
@@ -94,6 +97,8 @@ struct StageParams {
   double w0, w1, w2;    // RK weights of this stage
   const double* dt;     // device scalar: the host dt or a captured graph's
   int32_t first;        // stage 0: the step fields start from zero
+  int32_t* status;      // per-block status bits (kStatusStaging: a tile's
+                        // staging wait ran out)
   int32_t smem_rows;    // x1 lines held in shared memory per tile
   int32_t max_nc1;
 };
