@@ -394,6 +394,7 @@ def run_native(args):
             "execution_report": rep,
             "step_ms_median": statistics.median(step_ms),
             "tile_tj": b.tile(0),
+            "schedule": b.schedule,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -549,6 +550,7 @@ def run_ensemble(args):
         t = torch.tensor([e2e_t], device=dev, dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_t = float(t.item())
+    schedule = ens.batch.schedule
     del ens
 
     # the plain FP64 GPU path on the same members
@@ -594,6 +596,7 @@ def run_ensemble(args):
                                   "after another, own CFL dt (host read), "
                                   "step graphs on", "steps": plain_steps},
             "vs_plain_fp64": value / plain,
+            "schedule": schedule,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak,
                          "peak_kind": peak_kind, "traffic": None,

@@ -136,7 +136,9 @@ int sg_fill_ghosts(sg_handle* h, sg_stream_t stream);
 int sg_max_dt(sg_handle* h, const int32_t* redo_dev, double* dt_dev_out,
               sg_stream_t stream);
 /* per-block retry flags into flags_dev (int32[nblock]): bit 0 floor, bit 3
- * NaN, bit 5 a failed column of the implicit solve (meshblock_redo.cpp) */
+ * NaN, bit 5 a failed column of the implicit solve (meshblock_redo.cpp),
+ * bit 6 a tile whose shared-memory staging did not arrive within the stage
+ * kernel's bounded wait (the tile was not computed) */
 int sg_check(sg_handle* h, int32_t* flags_dev, sg_stream_t stream);
 /* initialize (MeshBlockImpl::initialize, src/mesh/meshblock.cpp:306-420):
  * the boundary functions fill the ghosts of the FP64 primitives w_in[b]
@@ -169,6 +171,26 @@ enum {
 };
 int sg_set_timing(sg_handle* h, int32_t on);
 int sg_kernel_times(sg_handle* h, double* ms, int64_t* launches);
+
+/* The schedule autotuner (no counterpart in the reference, whose stage is a
+ * fixed chain of library calls).  sg_autotune times the stage's kernels on
+ * this handle's own blocks and current state: every tile width of
+ * 1, 2, 4, 8, 16, 32 x2 columns (the same request for every block, each
+ * clamped to its x2 extent and halved until its tile fits the shared
+ * memory), then, with an implicit solve, its finish as a warp per column
+ * and as a thread per column, and keeps the fastest.  The results do not
+ * depend on either choice (same operations, same order).  The trial
+ * launches read the current state and write only the rotation's free
+ * buffer and the solve's scratch; the step fields and the status bits are
+ * left as they were.  Not inside a stream capture; graphs captured before
+ * must be captured again.  Outputs (each may be null): tj_out[nblock] the
+ * tile widths, *finish_out the finish form (1 warp, 2 thread; 0 when there
+ * is no solve), ms_out[2] the best stage and solve milliseconds per launch.
+ * sg_set_schedule applies a stored choice (tj null or 0: the library's
+ * rule; finish 0: the library's rule). */
+int sg_autotune(sg_handle* h, int32_t reps, int32_t* tj_out,
+                int32_t* finish_out, double* ms_out, sg_stream_t stream);
+int sg_set_schedule(sg_handle* h, const int32_t* tj, int32_t finish);
 
 /* The FluxRegister's step fields (src/hydro/flux_register.hpp:337-349,
  * request_step_field / step_field / end_stage):

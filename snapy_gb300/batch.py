@@ -58,6 +58,9 @@ class Batch:
         self.device = device
         self.dtype = dtype
         self.nblock = len(blocks)
+        self.scheme_key = [int(scheme["riemann"]), int(bool(scheme["shock"])),
+                           int(bool(scheme["scale"]))]
+        self.schedule = None  # the autotuner's choice, once tuned
         sch = _lib.Scheme()
         sch.dtype = _DT[dtype]
         sch.riemann = scheme["riemann"]
@@ -313,3 +316,13 @@ class Batch:
         _lib.check(self.L.sg_budget_boundary(self.h, out.data_ptr(), int(bool(accumulate)),
                                              _stream(stream)), "sg_budget_boundary")
         return out
+
+    # -- the schedule autotuner ---------------------------------------------
+    def autotune(self, reps: int = 3, use_cache: bool = True) -> dict:
+        """Time the tile widths and the implicit finish forms on this
+        batch's blocks and current state (or recall a cached choice) and
+        apply the fastest; see ``snapy_gb300.autotune``."""
+        from . import autotune as _at
+        with torch.cuda.device(self.device):
+            self.schedule = _at.tune(self, reps=reps, use_cache=use_cache)
+        return self.schedule

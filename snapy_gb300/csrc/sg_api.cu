@@ -8,6 +8,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <array>
 #include <string>
 #include <vector>
 
@@ -173,8 +174,11 @@ struct sg_handle {
   bool has3 = false;            // a 3-D block: the x3 sweep runs
   size_t sum_icols = 0;         // implicit columns of all blocks
   int wide = 0;  // enough columns for a thread per column in the finish
+  int wide_auto = 0;  // that rule's own answer (finish form 0)
   bool implicit = false;
   size_t max_icells = 0, max_icols = 0;
+  std::vector<sg_block_desc> descs;   // as created (tile re-layout)
+  int32_t finish = 0;  // implicit finish form: 0 auto, 1 warp, 2 thread
   std::vector<size_t> scratch_bytes;  // per block: vic_bytes + the x3 part
   std::vector<size_t> vic_bytes;
   int device = 0;
@@ -243,11 +247,220 @@ int upload(sg_handle* h, cudaStream_t s) {
   return 0;
 }
 
+// the tiles of every block for the tile widths tj (null or 0: the library's
+// choice), each clamped to the block's x2 extent and halved until its tile
+// fits the opt-in shared memory
+int relayout(sg_handle* h, const int32_t* tj) {
+  int optin = 0;
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin,
+                         h->device);
+  int tile = 0;
+  size_t smem = 0;
+  for (int b = 0; b < h->nblock; ++b) {
+    const sg_block_desc& d = h->descs[b];
+    BlockDev& B = h->host[b];
+    const int nx2 = d.nc2 > 1 ? d.nc2 - 2 * d.ng : 1;
+    const int nx3 = d.nc3 > 1 ? d.nc3 - 2 * d.ng : 1;
+    int t = tj && tj[b] > 0 ? tj[b] : (d.tj > 0 ? d.tj : choose_tj(h, d, h->nblock));
+    if (d.nc2 <= 1) t = 1;
+    if (t > nx2) t = nx2;
+    while (t > 1 && (long)stage_smem(h, d, t) > optin) t = (t + 1) / 2;
+    const size_t sm = stage_smem(h, d, t);
+    if ((long)sm > optin)
+      return fail(SG_ERR_UNSUPPORTED, "block %d: a tile needs %zu B of "
+                  "shared memory (limit %d)", b, sm, optin);
+    B.tj = t;
+    B.ntile = nx3 * ((nx2 + t - 1) / t);
+    B.tile0 = tile;
+    tile += B.ntile;
+    smem = std::max(smem, sm);
+  }
+  h->ntile = tile;
+  h->smem = smem;
+  h->dirty = true;
+  return 0;
+}
+
 }  // namespace
 
 extern "C" {
 
 const char* sg_last_error(void) { return g_err.c_str(); }
+
+int sg_set_schedule(sg_handle* h, const int32_t* tj, int32_t finish) {
+  if (!h || finish < 0 || finish > 2)
+    return fail(SG_ERR_ARG, "sg_set_schedule: finish form %d", finish);
+  int rc = relayout(h, tj);
+  if (rc) return rc;
+  h->finish = finish;
+  h->wide = finish == 0 ? h->wide_auto : (finish == 2 ? 1 : 0);
+  return 0;
+}
+
+int sg_autotune(sg_handle* h, int32_t reps, int32_t* tj_out,
+                int32_t* finish_out, double* ms_out, sg_stream_t stream) {
+  if (!h) return fail(SG_ERR_ARG, "sg_autotune: null handle");
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cs) != cudaSuccess ||
+      cs != cudaStreamCaptureStatusNone)
+    return fail(SG_ERR_STATE, "sg_autotune: not inside a stream capture");
+  if (reps < 1) reps = 1;
+  int rc = upload(h, s);
+  if (rc) return rc;
+  const int nb = h->nblock;
+  // the trials leave the step fields, the status bits and the state alone:
+  // fields out of the table, status saved, and the trials write only the
+  // rotation's free buffer (and the solve's scratch)
+  std::vector<std::array<double*, 4>> saved(nb);
+  for (int b = 0; b < nb; ++b) {
+    BlockDev& B = h->host[b];
+    saved[b] = {B.step[0], B.step[1], B.step[2], B.t1};
+    B.step[0] = B.step[1] = B.step[2] = B.t1 = nullptr;
+  }
+  std::vector<int32_t> prev_tj(nb);
+  for (int b = 0; b < nb; ++b) prev_tj[b] = h->host[b].tj;
+  int* st_save = nullptr;
+  double* dt = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t e = cudaMalloc(&st_save, sizeof(int) * nb);
+  if (e == cudaSuccess) e = cudaMalloc(&dt, sizeof(double) * nb);
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(st_save, h->status, sizeof(int) * nb,
+                        cudaMemcpyDeviceToDevice, s);
+  std::vector<int32_t> best_tj = prev_tj;
+  double best_ms = 1e300, best_vic = 0.;
+  int best_finish = h->finish;
+  if (e == cudaSuccess) {
+    h->dirty = true;
+    rc = upload(h, s);
+    // a realistic dt: the blocks' own CFL step
+    if (!rc) rc = sg_max_dt(h, nullptr, dt, stream);
+    StageParams p;
+    memset(&p, 0, sizeof(p));
+    p.nblock = nb;
+    p.in = p.u0 = h->cur;
+    p.out = h->cur != h->base ? 3 - h->cur - h->base : (h->cur + 1) % 3;
+    p.riemann = h->scheme.riemann;
+    p.shock = h->scheme.shock;
+    p.scale = h->scheme.scale;
+    p.w0 = h->scheme.wght[0][0];
+    p.w1 = h->scheme.wght[0][1];
+    p.w2 = h->scheme.wght[0][2];
+    p.dt = dt;
+    p.first = 1;
+    p.status = h->status;
+    p.max_nc1 = h->max_nc1;
+    auto stage = [&]() -> int {
+      p.ntile = h->ntile;
+      int r = 0;
+      if (h->has3)
+        r = f64(h) ? sg_launch_x3_f64(h->dev, p, h->max_cells, s)
+                   : sg_launch_x3_f32(h->dev, p, h->max_cells, s);
+      if (!r)
+        r = f64(h) ? sg_launch_stage_f64(h->dev, p, h->smem, s)
+                   : sg_launch_stage_f32(h->dev, p, h->smem, s);
+      return r ? cuda_fail((cudaError_t)r, "sg_autotune: trial stage") : 0;
+    };
+    auto vic = [&]() -> int {
+      int r = f64(h) ? sg_launch_vic_f64(h->dev, p, h->max_icells, h->max_icols,
+                                         h->wide, h->status, s, nullptr)
+                     : sg_launch_vic_f32(h->dev, p, h->max_icells, h->max_icols,
+                                         h->wide, h->status, s, nullptr);
+      return r ? cuda_fail((cudaError_t)r, "sg_autotune: trial solve") : 0;
+    };
+    auto timed = [&](auto&& launch, double* ms) -> int {
+      int r = launch();  // warm
+      if (r) return r;
+      cudaEventRecord(e0, s);
+      for (int k = 0; k < reps && !r; ++k) r = launch();
+      cudaEventRecord(e1, s);
+      if (r) return r;
+      cudaError_t x = cudaEventSynchronize(e1);
+      if (x != cudaSuccess) return cuda_fail(x, "sg_autotune: trial timing");
+      float f = 0.f;
+      cudaEventElapsedTime(&f, e0, e1);
+      *ms = f / reps;
+      return 0;
+    };
+    // (1) the tile width, the same request for every block
+    std::vector<std::vector<int32_t>> tried;
+    for (int c : {1, 2, 4, 8, 16, 32}) {
+      if (rc) break;
+      std::vector<int32_t> req(nb, c);
+      rc = relayout(h, req.data());
+      if (rc) break;
+      std::vector<int32_t> got(nb);
+      for (int b = 0; b < nb; ++b) got[b] = h->host[b].tj;
+      bool seen = false;
+      for (auto& t : tried) seen = seen || t == got;
+      if (seen) continue;
+      tried.push_back(got);
+      rc = upload(h, s);
+      double ms = 0.;
+      if (!rc) rc = timed(stage, &ms);
+      if (rc) break;
+      if (ms < best_ms) {
+        best_ms = ms;
+        best_tj = got;
+      }
+    }
+    if (!rc) rc = relayout(h, best_tj.data());
+    if (!rc) rc = upload(h, s);
+    // (2) the implicit solve's finish: a warp per column or a thread per
+    // column (the stage's explicit tendency is in the scratch first)
+    if (!rc && h->implicit) {
+      rc = stage();
+      double best = 1e300;
+      for (int form : {1, 2}) {
+        if (rc) break;
+        h->wide = form == 2;
+        double ms = 0.;
+        rc = timed(vic, &ms);
+        if (!rc && ms < best) {
+          best = ms;
+          best_finish = form;
+          best_vic = ms;
+        }
+      }
+      h->finish = best_finish;
+      h->wide = best_finish == 2;
+    }
+    if (!rc) {
+      e = cudaMemcpyAsync(h->status, st_save, sizeof(int) * nb,
+                          cudaMemcpyDeviceToDevice, s);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+      if (e != cudaSuccess) rc = cuda_fail(e, "sg_autotune: restore");
+    }
+  } else {
+    rc = cuda_fail(e, "sg_autotune: setup");
+  }
+  for (int b = 0; b < nb; ++b) {
+    BlockDev& B = h->host[b];
+    B.step[0] = saved[b][0];
+    B.step[1] = saved[b][1];
+    B.step[2] = saved[b][2];
+    B.t1 = saved[b][3];
+  }
+  if (rc) relayout(h, prev_tj.data());
+  h->dirty = true;
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(st_save);
+  cudaFree(dt);
+  if (rc) return rc;
+  rc = upload(h, s);
+  if (rc) return rc;
+  for (int b = 0; b < nb && tj_out; ++b) tj_out[b] = h->host[b].tj;
+  if (finish_out) *finish_out = h->finish;
+  if (ms_out) {
+    ms_out[0] = best_ms;
+    ms_out[1] = best_vic;
+  }
+  return 0;
+}
 
 // records `msg` as the calling thread's last error for entry points defined
 // in other translation units; returns `code`
@@ -273,6 +486,7 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
                          h->device);
   h->nblock = nblock;
   h->host.resize(nblock);
+  h->descs.assign(blocks, blocks + nblock);
   int tile = 0;
   for (int b = 0; b < nblock; ++b) {
     const sg_block_desc& d = blocks[b];
@@ -440,7 +654,8 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
     // a full warp of columns for every SM sub-partition
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
-    h->wide = h->sum_icols >= (size_t)32 * 4 * sms;
+    h->wide_auto = h->sum_icols >= (size_t)32 * 4 * sms;
+    h->wide = h->wide_auto;
   }
   cudaError_t e = cudaMalloc(&h->dev, sizeof(BlockDev) * nblock);
   if (e == cudaSuccess)

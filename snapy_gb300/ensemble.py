@@ -62,10 +62,16 @@ class Ensemble:
             n += c.nx1 * c.nx2 * c.nx3
         return n
 
-    def initialize(self, ws: List[torch.Tensor]) -> None:
+    def initialize(self, ws: List[torch.Tensor], autotune: Optional[bool] = None) -> None:
+        """The members' initial primitives; then (autotune None: as the first
+        member's integration/autotune) the schedule autotuner on the batch."""
         ws = [w.to(self.device, torch.float64).contiguous() for w in ws]
         with torch.cuda.device(self.device):
             self.batch.init_from_prim(ws)
+            if self.members[0].autotune if autotune is None else autotune:
+                self.batch.autotune()
+                self._graphs.clear()
+                self._seen.clear()
         self.time.zero_()
 
     def state(self, k: int) -> torch.Tensor:

@@ -242,6 +242,12 @@ class MeshBlock:
             vars["hydro_w"] = w = w.contiguous()
         with torch.cuda.device(self.device):
             self.batch.init_from_prim([w])
+            # integration/autotune: the tile width and finish form measured
+            # on this block (not when the caller fixed the tile width)
+            if self.options.autotune and not self._block.get("tj"):
+                self.batch.autotune()
+                self._graphs.clear()
+                self._seen.clear()
             u = self.batch.current(0)
         vars["hydro_u"] = torch.empty(0, dtype=self.dtype, device=self.device).set_(u)
         self.intg.current_redo = 0

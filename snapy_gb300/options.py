@@ -358,7 +358,7 @@ class IntegratorOptions:
                    {"type", "cfl", "tlim", "nlim", "ncycle_out", "max-redo",
                     "max_redo", "implicit-scheme", "implicit-precision",
                     "implicit-fallback-fp64", "execution", "execution-strict",
-                    "restart"})
+                    "restart", "autotune"})
         op.type = str(_get(node, "type", op.type))
         op.cfl = float(_get(node, "cfl", op.cfl))
         op.tlim = float(_get(node, "tlim", op.tlim))
@@ -385,6 +385,9 @@ class MeshBlockOptions:
         self.bcnames: List[str] = []
         self.execution = "auto"
         self.execution_strict = False
+        # integration/autotune (no counterpart in the reference): time the
+        # stage's tile widths and finish forms on the block at initialize
+        self.autotune = True
         self.verbose = False
         self.basename = ""
         self.problem: Dict[str, Any] = {}
@@ -433,6 +436,7 @@ class MeshBlockOptions:
         intg = config.get("integration") or {}
         op.execution = str(intg.get("execution", "auto"))
         op.execution_strict = bool(intg.get("execution-strict", False))
+        op.autotune = bool(intg.get("autotune", True))
         if op.execution not in ("auto", "eager", "cuda-graph"):
             raise DeckError("integration/execution must be auto, eager or "
                             f"cuda-graph, got '{op.execution}'")
