@@ -368,6 +368,25 @@ __device__ __forceinline__ unsigned long long vbits(double x) {
   return static_cast<unsigned long long>(__double_as_longlong(x));
 }
 
+// finite, tested on the exponent bits (integer pipes, not the FP64 one)
+__device__ __forceinline__ bool vfinite(double x) {
+  return ((__double_as_longlong(x) >> 52) & 0x7ff) != 0x7ff;
+}
+
+// a / b from r = 1 / b (the correctly rounded reciprocal): q0 = a r, the
+// exact residual a - b q0 by one fma, then q0 + e r rounded once.  For
+// normal operands and quotient this is the correctly rounded quotient, the
+// same bits as a / b (Markstein, "Computation of elementary functions on
+// the IBM RISC System/6000 processor", IBM J. Res. Dev. 34 (1990), and
+// "IA-64 and Elementary Functions" (2000), the division theorem); it costs
+// one multiply and two fmas where a division is a longer sequence, and the
+// reciprocal is shared by every quotient with the same divisor
+__device__ __forceinline__ double div_rcp(double a, double b, double r) {
+  const double q0 = a * r;
+  const double e = fma(-b, q0, a);
+  return fma(e, r, q0);
+}
+
 template <typename T>
 __device__ __forceinline__ T vpick5(int k, T a0, T a1, T a2, T a3, T a4) {
   return k == 0 ? a0 : k == 1 ? a1 : k == 2 ? a2 : k == 3 ? a3 : a4;
@@ -377,15 +396,16 @@ __device__ __forceinline__ T vpick5(int k, T a0, T a1, T a2, T a3, T a4) {
 // block's columns; vv, scale and indx are per-lane copies of the row data)
 template <int J>
 __device__ __forceinline__ void vlu_step(double (&x)[5], double (&vv)[5],
-                                         double (&scale)[5], int (&indx)[5],
-                                         bool& good, int q, bool colane) {
+                                         double (&scale)[5], double (&rsc)[5],
+                                         int (&indx)[5], bool& good, int q,
+                                         bool colane) {
   // pivot search on column J: the last row of the largest vv |a|
   unsigned long long best = 0ull;
   int imax = J;
 #pragma unroll
   for (int i2 = J; i2 < 5; ++i2) {
     double dum = vv[i2] * fabs(x[i2]);
-    if (q == J) good = good && isfinite(dum);
+    if (q == J) good = good && vfinite(dum);
     if (vbits(dum) >= best) {
       best = vbits(dum);
       imax = i2;
@@ -405,6 +425,9 @@ __device__ __forceinline__ void vlu_step(double (&x)[5], double (&vv)[5],
       double t = scale[J];
       scale[J] = scale[i2];
       scale[i2] = t;
+      t = rsc[J];
+      rsc[J] = rsc[i2];
+      rsc[i2] = t;
     }
   if (J < 4) {
     double dinv = 1.0 / vshfl(x[J], J);
@@ -424,6 +447,7 @@ __device__ __forceinline__ void vlu_step(double (&x)[5], double (&vv)[5],
 struct VicSolveSmem {
   double lu[kVicCols][25];         // the factorised block of each column
   double vec[kVicCols][2][15];     // back substitution: d, z0, z1 of a layer
+  double rd[kVicCols][5];          // 1 / the diagonal of each factorisation
 };
 
 __global__ void __launch_bounds__(32)
@@ -442,6 +466,7 @@ __global__ void __launch_bounds__(32)
   // a group past the last column shadows it and never stores
   const size_t cc = valid ? col : ncol - 1;
   const double dtc = p.w2 * p.dt[blockIdx.y];
+  const double rdtc = 1.0 / dtc;  // every du / dt_corr divides by it
   const bool wood = n >= 3;
   const int m = wood ? 8 : 6;  // right-hand sides in use
   double* A = S.A + cc * n * 25;
@@ -457,7 +482,7 @@ __global__ void __launch_bounds__(32)
   // the input screen: du of every layer finite
   bool fin = true;
   for (int e = q; e < 5 * n; e += kVicLanes)
-    fin = fin && isfinite(du[(size_t)(e / n) * S.cells + (e % n)]);
+    fin = fin && vfinite(du[(size_t)(e / n) * S.cells + (e % n)]);
   // every ballot runs on all 32 lanes: evaluate before combining
   const bool fin_all = vgroup_all(fin, g);
   bool ok = valid && fin_all;
@@ -487,7 +512,7 @@ __global__ void __launch_bounds__(32)
       }
     }
     // du / dt_corr, one row per lane, gathered on lane 5
-    double dq = q < 5 ? du[(size_t)q * S.cells + i] / dtc : 0.;
+    double dq = q < 5 ? div_rcp(du[(size_t)q * S.cells + i], dtc, rdtc) : 0.;
 #pragma unroll
     for (int r = 0; r < 5; ++r) {
       double v = vshfl(dq, r);
@@ -514,7 +539,7 @@ __global__ void __launch_bounds__(32)
     unsigned long long mx[5];
 #pragma unroll
     for (int r = 0; r < 5; ++r) {
-      if (colane) good = good && isfinite(x[r]);
+      if (colane) good = good && vfinite(x[r]);
       mx[r] = colane ? vbits(fabs(x[r])) : 0ull;
     }
 #pragma unroll
@@ -524,7 +549,7 @@ __global__ void __launch_bounds__(32)
         unsigned long long o = __shfl_xor_sync(full, mx[r], off, kVicLanes);
         mx[r] = o > mx[r] ? o : mx[r];
       }
-    double scale[5], vv[5];
+    double scale[5], vv[5], rsc[5];
 #pragma unroll
     for (int r = 0; r < 5; ++r) {
       scale[r] = __longlong_as_double(static_cast<long long>(mx[r]));
@@ -535,26 +560,30 @@ __global__ void __launch_bounds__(32)
                           scale[3], scale[4]);
       double inv = 1.0 / big;
 #pragma unroll
-      for (int r = 0; r < 5; ++r) vv[r] = vshfl(inv, r);
+      for (int r = 0; r < 5; ++r) vv[r] = rsc[r] = vshfl(inv, r);
     }
 #pragma unroll
-    for (int r = 0; r < 5; ++r) good = good && isfinite(vv[r]);
+    for (int r = 0; r < 5; ++r) good = good && vfinite(vv[r]);
     int indx[5];
-    vlu_step<0>(x, vv, scale, indx, good, q, colane);
-    vlu_step<1>(x, vv, scale, indx, good, q, colane);
-    vlu_step<2>(x, vv, scale, indx, good, q, colane);
-    vlu_step<3>(x, vv, scale, indx, good, q, colane);
-    vlu_step<4>(x, vv, scale, indx, good, q, colane);
+    vlu_step<0>(x, vv, scale, rsc, indx, good, q, colane);
+    vlu_step<1>(x, vv, scale, rsc, indx, good, q, colane);
+    vlu_step<2>(x, vv, scale, rsc, indx, good, q, colane);
+    vlu_step<3>(x, vv, scale, rsc, indx, good, q, colane);
+    vlu_step<4>(x, vv, scale, rsc, indx, good, q, colane);
     if (colane) {
 #pragma unroll
-      for (int r = 0; r < 5; ++r) good = good && isfinite(x[r]);
+      for (int r = 0; r < 5; ++r) good = good && vfinite(x[r]);
       // the pivot tolerance of every step, on the final diagonal and scale
+      // (|d| / scale, from the scale's reciprocal carried through the swaps)
       double dg = vpick5(q, x[0], x[1], x[2], x[3], x[4]);
       double sc = vpick5(q, scale[0], scale[1], scale[2], scale[3], scale[4]);
-      good = good && !(fabs(dg) / sc <= 8. * 5 * 2.220446049250313e-16);
-      // stage the factors for every lane's back-solve
+      double rs = vpick5(q, rsc[0], rsc[1], rsc[2], rsc[3], rsc[4]);
+      good = good && !(div_rcp(fabs(dg), sc, rs) <= 8. * 5 * 2.220446049250313e-16);
+      // stage the factors, and the diagonal's reciprocals, for every lane's
+      // back-solve
 #pragma unroll
       for (int r = 0; r < 5; ++r) sm.lu[g][r * 5 + q] = x[r];
+      sm.rd[g][q] = 1.0 / dg;
     }
     const bool good_all = vgroup_all(good, g);
     ok = ok && good_all;
@@ -585,12 +614,12 @@ __global__ void __launch_bounds__(32)
 #pragma unroll
       for (int jj = rr + 1; jj < 5; ++jj)
         sol[rr] = sol[rr] - lu[rr * 5 + jj] * sol[jj];
-      sol[rr] = sol[rr] / lu[rr * 5 + rr];
+      sol[rr] = div_rcp(sol[rr], lu[rr * 5 + rr], sm.rd[g][rr]);
     }
     bool f = true;
     if (q < m) {
 #pragma unroll
-      for (int r = 0; r < 5; ++r) f = f && isfinite(sol[r]);
+      for (int r = 0; r < 5; ++r) f = f && vfinite(sol[r]);
     }
     const bool f_all = vgroup_all(f, g);
     ok = ok && f_all;
@@ -662,7 +691,7 @@ __global__ void __launch_bounds__(32)
     __syncwarp();
     bool f = true;
     if (ok)
-      for (int e = q; e < 5 * n; e += kVicLanes) f = f && isfinite(D[e]);
+      for (int e = q; e < 5 * n; e += kVicLanes) f = f && vfinite(D[e]);
     const bool d_all = vgroup_all(f, g);
     ok = ok && d_all;
   }
@@ -715,7 +744,7 @@ __global__ void __launch_bounds__(NL == 32 ? 32 * kVicWarps : kThreads)
   double* du = S.du + col * n;      // row v at du[v * cells + i]
   const double* du0 = S.du0 + col * n;
   const size_t cs = S.cells;
-  const bool ok = isfinite(D[0]);
+  const bool ok = vfinite(D[0]);
   const bool wood = n >= 3;
   // work arrays of the column, in the (now free) Woodbury scratch
   double* mM = S.Z0 + col * n * 5;  // n + 1: the face mass below layer i
