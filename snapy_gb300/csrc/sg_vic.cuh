@@ -75,6 +75,21 @@ __device__ __forceinline__ void vmat_mul(const T* a, const T* b,
     }
 }
 
+// a / b from r = 1 / b (the correctly rounded reciprocal): q0 = a r, the
+// exact residual a - b q0 by one fma, then q0 + e r rounded once.  For
+// normal operands and quotient this is the correctly rounded quotient, the
+// same bits as a / b (Markstein, "Computation of elementary functions on
+// the IBM RISC System/6000 processor", IBM J. Res. Dev. 34 (1990), and
+// "IA-64 and Elementary Functions" (2000), the division theorem); it costs
+// one multiply and two fmas where a division is a longer sequence, and the
+// reciprocal is shared by every quotient with the same divisor
+template <typename T>
+__device__ __forceinline__ T vdiv(T a, T b, T r) {
+  const T q0 = a * r;
+  const T e = fma(-b, q0, a);
+  return fma(e, r, q0);
+}
+
 template <typename T>
 __device__ __forceinline__ void vflux_jacobian(T* J, T gm1,
                                                const T* w) {
@@ -96,6 +111,10 @@ template <typename T>
 __device__ __forceinline__ void vabs_jacobian(T* A, T gm1,
                                               const T* wl,
                                               const T* wr) {
+  // every quotient as written below; those sharing a divisor divide by
+  // its reciprocal (vdiv: the same bits), and 1 / (2 hp), -1 / hp are the
+  // reciprocals themselves
+  const T gp1 = gm1 + T(1.), rgm1 = T(1.) / gm1, rgp1 = T(1.) / gp1;
   T sqrtdl = sqrt(wl[0]), sqrtdr = sqrt(wr[0]);
   T isdlpdr = T(1.0) / (sqrtdl + sqrtdr);
   T pr[5];
@@ -103,39 +122,42 @@ __device__ __forceinline__ void vabs_jacobian(T* A, T gm1,
   pr[1] = (sqrtdl * wl[1] + sqrtdr * wr[1]) * isdlpdr;
   pr[2] = (sqrtdl * wl[2] + sqrtdr * wr[2]) * isdlpdr;
   pr[3] = (sqrtdl * wl[3] + sqrtdr * wr[3]) * isdlpdr;
-  T el = wl[4] / gm1 +
+  T el = vdiv(wl[4], gm1, rgm1) +
               T(0.5) * wl[0] * (wl[1] * wl[1] + wl[2] * wl[2] + wl[3] * wl[3]);
-  T er = wr[4] / gm1 +
+  T er = vdiv(wr[4], gm1, rgm1) +
               T(0.5) * wr[0] * (wr[1] * wr[1] + wr[2] * wr[2] + wr[3] * wr[3]);
   T hbar = ((el + wl[4]) / sqrtdl + (er + wr[4]) / sqrtdr) * isdlpdr;
-  pr[4] = (hbar - T(0.5) * (pr[1] * pr[1] + pr[2] * pr[2] + pr[3] * pr[3])) *
-          gm1 / (gm1 + T(1.)) * pr[0];
-  T cs = sqrt(pr[4] * (gm1 + T(1.)) / pr[0]);
+  pr[4] = vdiv((hbar - T(0.5) * (pr[1] * pr[1] + pr[2] * pr[2] + pr[3] * pr[3])) *
+                   gm1, gp1, rgp1) * pr[0];
+  const T rr = T(1.) / pr[0];
+  T cs = sqrt(vdiv(pr[4] * gp1, pr[0], rr));
   T r = pr[0], u = pr[1], v = pr[2], w = pr[3], p = pr[4];
   T lam[5] = {fabs(u - cs), fabs(u), fabs(u + cs), fabs(u), fabs(u)};
   T ke = T(0.5) * (u * u + v * v + w * w);
-  T hp = (gm1 + T(1.)) / gm1 * p / r;
+  T hp = vdiv(vdiv(gp1, gm1, rgm1) * p, r, rr);
   T h = hp + ke;
+  const T d1 = T(2.) * cs * hp, d2 = T(2.) * hp;
+  const T r1 = T(1.) / d1, r2 = T(1.) / d2, rh = T(1.) / hp;
   const T R[25] = {T(1.),         T(1.), T(1.),         T(0.), T(0.),  //
                         u - cs,     u,  u + cs,     T(0.), T(0.),  //
                         v,          v,  v,          T(1.), T(0.),  //
                         w,          w,  w,          T(0.), T(1.),  //
                         h - u * cs, ke, h + u * cs, v,  w};
-  const T Ri[25] = {(cs * ke + u * hp) / (T(2.) * cs * hp),
-                         (-hp - cs * u) / (T(2.) * cs * hp),
-                         -v / (T(2.) * hp),
-                         -w / (T(2.) * hp),
-                         T(1.) / (T(2.) * hp),
-                         (hp - ke) / hp,
-                         u / hp,
-                         v / hp,
-                         w / hp,
-                         -T(1.) / hp,
-                         (cs * ke - u * hp) / (T(2.) * cs * hp),
-                         (hp - cs * u) / (T(2.) * cs * hp),
-                         -v / (T(2.) * hp),
-                         -w / (T(2.) * hp),
-                         T(1.) / (T(2.) * hp),
+  const T Ri[25] = {vdiv(cs * ke + u * hp, d1, r1),
+                         vdiv(-hp - cs * u, d1, r1),
+                         vdiv(-v, d2, r2),
+                         vdiv(-w, d2, r2),
+                         r2,
+                         vdiv(hp - ke, hp, rh),
+                         vdiv(u, hp, rh),
+                         vdiv(v, hp, rh),
+                         vdiv(w, hp, rh),
+                         -rh,
+                         vdiv(cs * ke - u * hp, d1, r1),
+                         vdiv(hp - cs * u, d1, r1),
+                         vdiv(-v, d2, r2),
+                         vdiv(-w, d2, r2),
+                         r2,
                          -v, T(0.), T(1.), T(0.), T(0.),
                          -w, T(0.), T(0.), T(1.), T(0.)};
   T RL[25];
@@ -243,8 +265,9 @@ __device__ __forceinline__ void vic_assemble_cell(const BlockDev& B,
   vflux_jacobian(Jn, gm1, wn);
   vabs_jacobian(Ap, gm1r, wr, wn);
   const T half_inv_vol = T(0.5) / vol;
-  const T lower = T(0.5) * area * T(x1v[i] - x1f[i]) / vol;
-  const T upper = T(0.5) * area * T(x1f[i + 1] - x1v[i]) / vol;
+  const T rvol = T(1.) / vol;
+  const T lower = vdiv(T(0.5) * area * T(x1v[i] - x1f[i]), vol, rvol);
+  const T upper = vdiv(T(0.5) * area * T(x1f[i + 1] - x1v[i]), vol, rvol);
   T a[25], b[25], c[25];
 #pragma unroll
   for (int r = 0; r < 5; ++r)
@@ -289,9 +312,9 @@ __device__ __forceinline__ void vic_assemble_cell(const BlockDev& B,
   }
   if (wood) {
     VicK K = vic_krows(B, n, i);
-    a[20] -= T(K.mid) / T(dtc);
-    b[20] -= T(K.lo) / T(dtc);
-    c[20] -= T(K.hi) / T(dtc);
+    a[20] -= vdiv(T(K.mid), T(dtc), rdt);
+    b[20] -= vdiv(T(K.lo), T(dtc), rdt);
+    c[20] -= vdiv(T(K.hi), T(dtc), rdt);
     // du[IPR] -= (K du0[IDN])_i : the IDN row is read only (FP64 always)
     const double* dn = S.du + col * n;
     double s = K.mid * dn[i];
@@ -373,18 +396,8 @@ __device__ __forceinline__ bool vfinite(double x) {
   return ((__double_as_longlong(x) >> 52) & 0x7ff) != 0x7ff;
 }
 
-// a / b from r = 1 / b (the correctly rounded reciprocal): q0 = a r, the
-// exact residual a - b q0 by one fma, then q0 + e r rounded once.  For
-// normal operands and quotient this is the correctly rounded quotient, the
-// same bits as a / b (Markstein, "Computation of elementary functions on
-// the IBM RISC System/6000 processor", IBM J. Res. Dev. 34 (1990), and
-// "IA-64 and Elementary Functions" (2000), the division theorem); it costs
-// one multiply and two fmas where a division is a longer sequence, and the
-// reciprocal is shared by every quotient with the same divisor
 __device__ __forceinline__ double div_rcp(double a, double b, double r) {
-  const double q0 = a * r;
-  const double e = fma(-b, q0, a);
-  return fma(e, r, q0);
+  return vdiv<double>(a, b, r);
 }
 
 template <typename T>
@@ -738,6 +751,7 @@ __global__ void __launch_bounds__(NL == 32 ? 32 * kVicWarps : kThreads)
   const size_t base = jrow * nc1 + ng;
   const double grav = B.grav1;
   const double vol = B.dx3 * (B.dx2 * B.dx1);
+  const double rvol = 1. / vol;  // the quotients by vol divide by it (vdiv)
   const double* x1v = B.x1v + ng;
   const double* x1f = B.x1f + ng;
   const double* D = S.D + col * n * 5;
@@ -767,9 +781,10 @@ __global__ void __launch_bounds__(NL == 32 ? 32 * kVicWarps : kThreads)
         Ssum += rho[i] * vol;
       }
       double M = 0;
+      const double rss = 1. / Ssum;
       for (int i = 0; i < n; ++i) {
         mM[i] = M;
-        M -= mq[i] - R * (rho[i] * vol / Ssum);
+        M -= mq[i] - R * vdiv(rho[i] * vol, Ssum, rss);
       }
       mM[n] = 0.;
       for (int i = 0; i <= n; ++i) mq[i] = 0.;
@@ -782,8 +797,9 @@ __global__ void __launch_bounds__(NL == 32 ? 32 * kVicWarps : kThreads)
         double q = Mf > 0 ? Mf * 1. : Mf * 1.;
         if (q > avail) q = avail;
         if (q < -avail_up) q = -avail_up;
-        mdn[i] -= q / vol;
-        mdn[i + 1] += q / vol;
+        const double qv = vdiv(q, vol, rvol);
+        mdn[i] -= qv;
+        mdn[i + 1] += qv;
         mq[i + 1] = q;
         avail = avail_up + q;
       }
@@ -795,13 +811,13 @@ __global__ void __launch_bounds__(NL == 32 ? 32 * kVicWarps : kThreads)
       du[2 * cs + i] = D[i * 5 + 2];
       du[3 * cs + i] = D[i * 5 + 3];
       double e = D[i * 5 + 4];
-      double projected = (mM[i] - mM[i + 1]) / vol;
+      double projected = vdiv(mM[i] - mM[i + 1], vol, rvol);
       double ph = -grav * x1v[i];
       double pw = ph * (D[i * 5] - du0[i] - projected);
       double dp_lo = -grav * (x1f[i] - x1v[i]);
       double dp_hi = -grav * (x1f[i + 1] - x1v[i]);
       double mv_lo = mq[i] - mM[i], mv_hi = mq[i + 1] - mM[i + 1];
-      double cw = -(dp_hi * mv_hi - dp_lo * mv_lo) / vol;
+      double cw = vdiv(-(dp_hi * mv_hi - dp_lo * mv_lo), vol, rvol);
       du[4 * cs + i] = e + (pw + cw);
     }
     vsync<NL>();
@@ -845,7 +861,7 @@ __global__ void __launch_bounds__(NL == 32 ? 32 * kVicWarps : kThreads)
   // order, +0 posts included (a -0 total becomes +0)
   if (double* S1 = B.step[0]) {
     const double dt = p.dt[blockIdx.y];
-    const double kdt = dt * (B.dx3 * B.dx2);
+    const double kdt = dt * (B.dx3 * B.dx2), rkdt = 1. / kdt;
     const double w1s = p.w1, w2dt = p.w2 * dt;
     const bool first = p.first != 0;
     const int nf = n + 1;
@@ -855,7 +871,7 @@ __global__ void __launch_bounds__(NL == 32 ? 32 * kVicWarps : kThreads)
     auto at = [&](int v, int f) { return S1 + v * plane + jrow * nc1 + ng + f; };
     for (int f = lane; f < nf; f += NL) {
       double t0 = tot(IDN, f), t1 = tot(IVX, f), t4 = tot(IPR, f);
-      if (ok) t0 = t0 + mq[f] / kdt;
+      if (ok) t0 = t0 + vdiv(mq[f], kdt, rkdt);
       if ((f == 0 && wlo) || (f == n && whi)) t0 = t4 = 0.;
       step_set(at(IDN, f), t0, w1s, w2dt, first);
       step_set(at(IVX, f), t1, w1s, w2dt, first);
@@ -873,8 +889,8 @@ __global__ void __launch_bounds__(NL == 32 ? 32 * kVicWarps : kThreads)
             py = -sy;
             pz = -sz;
           }
-          ty = ty + py / kdt;
-          tz = tz + pz / kdt;
+          ty = ty + vdiv(py, kdt, rkdt);
+          tz = tz + vdiv(pz, kdt, rkdt);
         }
         step_set(at(IVY, f), ty, w1s, w2dt, first);
         step_set(at(IVZ, f), tz, w1s, w2dt, first);
