@@ -175,7 +175,7 @@ int sg_kernel_times(sg_handle* h, double* ms, int64_t* launches);
 /* The schedule autotuner (no counterpart in the reference, whose stage is a
  * fixed chain of library calls).  sg_autotune times the stage's kernels on
  * this handle's own blocks and current state: every tile width of
- * 1, 2, 4, 8, 16, 32 x2 columns (the same request for every block, each
+ * 1, 2, 3, 4, 6, 8, 12, 16, 24, 32 x2 columns (the same request for every block, each
  * clamped to its x2 extent and halved until its tile fits the shared
  * memory), then, with an implicit solve, its finish as a warp per column
  * and as a thread per column, and keeps the fastest.  The results do not

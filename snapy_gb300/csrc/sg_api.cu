@@ -387,7 +387,7 @@ int sg_autotune(sg_handle* h, int32_t reps, int32_t* tj_out,
     };
     // (1) the tile width, the same request for every block
     std::vector<std::vector<int32_t>> tried;
-    for (int c : {1, 2, 4, 8, 16, 32}) {
+    for (int c : {1, 2, 3, 4, 6, 8, 12, 16, 24, 32}) {
       if (rc) break;
       std::vector<int32_t> req(nb, c);
       rc = relayout(h, req.data());
