@@ -51,15 +51,20 @@ constexpr int kNg = 3;
 constexpr int kGhostStride = 24;
 constexpr int kSeamStride = 18;
 
-// offsets of the geometry arrays in the device block (see sg_cs_desc)
+// offsets of the geometry arrays in the device block (see sg_cs_desc); the
+// FP32 kernels read an FP32 copy made at sg_cs_create (the same values their
+// per-use conversions gave, without a conversion per use)
+template <typename T>
 struct Geo {
-  const double *cos_c, *sin_c, *vol, *xr, *yr, *w2, *w3;
-  const double *cos_f2, *sin_f2, *a2, *cos_f3, *sin_f3, *a3;
+  const T *cos_c, *sin_c, *vol, *xr, *yr, *w2, *w3;
+  const T *cos_f2, *sin_f2, *a2, *cos_f3, *sin_f3, *a3;
 };
 
-__host__ __device__ inline Geo geo_of(const double* g, int nc) {
+template <typename T>
+__host__ __device__ inline Geo<T> geo_of(const void* gv, int nc) {
+  const T* g = static_cast<const T*>(gv);
   const size_t c = (size_t)nc * nc, f = (size_t)nc * (nc + 1);
-  Geo o;
+  Geo<T> o;
   o.cos_c = g;
   o.sin_c = g + c;
   o.vol = g + 2 * c;
@@ -78,10 +83,11 @@ __host__ __device__ inline Geo geo_of(const double* g, int nc) {
 
 struct CsParams {
   int n, nc;
-  const double* geo;
-  const double* gtab;
+  // the geometry, the ghost table and the seam table in the state's type
+  const void* geo;
+  const void* gtab;
   int nghost;
-  const double* stab;
+  const void* stab;
   int nseam;
   const void* in;
   const void* u0;
@@ -216,11 +222,12 @@ __device__ __forceinline__ void hllc_sw(const T* L, const T* R, T* F, T phi0) {
 
 // the faces: thread e < 6 n (n + 1) an x2 face (panel, row k, face j), the
 // rest x3 faces (panel, face k, column j)
-template <typename T>
+template <typename T, bool HLLC>
 __global__ void __launch_bounds__(kThreads) cs_flux_kernel(CsParams P) {
   const int n = P.n, nc = P.nc;
   const size_t pst = (size_t)nc * nc;  // one variable of a panel
-  const Geo G = geo_of(P.geo, nc);
+  const Geo<T> G = geo_of<T>(P.geo, nc);
+  const T phi0 = T(P.phi0);
   const T* U = static_cast<const T*>(P.in);
   const size_t nf = (size_t)6 * n * (n + 1);
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < 2 * nf;
@@ -243,7 +250,7 @@ __global__ void __launch_bounds__(kThreads) cs_flux_kernel(CsParams P) {
     for (int m = 0; m < 6; ++m) {
       const int kk = x2 ? k : k - 3 + m, jj = x2 ? j - 3 + m : j;
       const size_t c = (size_t)kk * nc + jj;
-      sw_prim<T>(q, pst, c, T(G.cos_c[c]), st[m], T(P.phi0));
+      sw_prim<T>(q, pst, c, T(G.cos_c[c]), st[m], phi0);
     }
     T wl[4], wr[4], F[4];
 #pragma unroll
@@ -277,16 +284,16 @@ __global__ void __launch_bounds__(kThreads) cs_flux_kernel(CsParams P) {
     };
     to_face(wl);
     to_face(wr);
-    if (P.hllc) {
+    if (HLLC) {
       if (x2)
-        hllc_sw<T, 2>(wl, wr, F, T(P.phi0));
+        hllc_sw<T, 2>(wl, wr, F, phi0);
       else
-        hllc_sw<T, 1>(wl, wr, F, T(P.phi0));
+        hllc_sw<T, 1>(wl, wr, F, phi0);
     } else {
       if (x2)
-        shallow_roe<T, 2>(wl, wr, F, T(P.phi0));
+        shallow_roe<T, 2>(wl, wr, F, phi0);
       else
-        shallow_roe<T, 1>(wl, wr, F, T(P.phi0));
+        shallow_roe<T, 1>(wl, wr, F, phi0);
     }
     // back to covariant fluxes (flux2global2_ / 3_)
     const T txy = F[IVY], txz = F[IVZ];
@@ -319,7 +326,7 @@ __global__ void __launch_bounds__(kThreads) cs_seam_flux_kernel(CsParams P) {
   const size_t fst = (size_t)nc * (nc + 1);
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < P.nseam;
        e += gridDim.x * blockDim.x) {
-    const double* r = P.stab + (size_t)e * kSeamStride;
+    const T* r = static_cast<const T*>(P.stab) + (size_t)e * kSeamStride;
     T* dst = static_cast<T*>((int)r[0] == 2 ? P.f2 : P.f3);
     const T* src = static_cast<const T*>((int)r[2] == 2 ? P.f2 : P.f3);
     const size_t di = (size_t)r[1], si = (size_t)r[3];
@@ -350,7 +357,8 @@ __global__ void __launch_bounds__(kThreads) cs_update_kernel(CsParams P) {
   const int n = P.n, nc = P.nc;
   const size_t pst = (size_t)nc * nc, f2st = (size_t)nc * (nc + 1),
                f3st = (size_t)(nc + 1) * nc;
-  const Geo G = geo_of(P.geo, nc);
+  const Geo<T> G = geo_of<T>(P.geo, nc);
+  const T phi0 = T(P.phi0);
   const T* U = static_cast<const T*>(P.in);
   const T* U0 = static_cast<const T*>(P.u0);
   T* O = static_cast<T*>(P.out);
@@ -367,7 +375,7 @@ __global__ void __launch_bounds__(kThreads) cs_update_kernel(CsParams P) {
     const size_t c = (size_t)k * nc + j;
     const T* q = U + (size_t)p * 4 * pst;
     T w[4];
-    sw_prim<T>(q, pst, c, T(G.cos_c[c]), w, T(P.phi0));
+    sw_prim<T>(q, pst, c, T(G.cos_c[c]), w, phi0);
     const size_t i2 = (size_t)k * (nc + 1) + j, i3 = (size_t)k * nc + j;
     const T a2lo = T(G.a2[i2]), a2hi = T(G.a2[i2 + 1]);
     const T a3lo = T(G.a3[i3]), a3hi = T(G.a3[i3 + nc]);
@@ -384,10 +392,10 @@ __global__ void __launch_bounds__(kThreads) cs_update_kernel(CsParams P) {
     // Phi and p = Phi^2 / 2; with phi0 > 0, the stored anomaly Phi' and
     // the pressure anomaly phi0 Phi' + Phi'^2 / 2 (see shallow_roe)
     T rho = w[IDN], pr = T(0.5) * (w[IDN] * w[IDN]);
-    if (P.phi0 > 0.) {
+    if (phi0 > T(0)) {
       const T dp = w[IDN];
-      rho = T(P.phi0) + dp;
-      pr = T(P.phi0) * dp + T(0.5) * dp * dp;
+      rho = phi0 + dp;
+      pr = phi0 * dp + T(0.5) * dp * dp;
     }
     const T sn = T(G.sin_c[c]);
     const T sine2 = sn * sn;
@@ -409,7 +417,7 @@ __global__ void __launch_bounds__(kThreads) cs_ghost_kernel(CsParams P, void* bu
   T* Q = static_cast<T*>(buf);
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < P.nghost;
        e += gridDim.x * blockDim.x) {
-    const double* r = P.gtab + (size_t)e * kGhostStride;
+    const T* r = static_cast<const T*>(P.gtab) + (size_t)e * kGhostStride;
     const size_t d = (size_t)r[0], s0 = (size_t)r[1], s1 = (size_t)r[2];
     // flat (panel, k, j) -> the variable v of that cell
     auto at = [&](size_t f, int v) -> size_t {
@@ -426,7 +434,7 @@ __global__ void __launch_bounds__(kThreads) cs_ghost_kernel(CsParams P, void* bu
     T* Vs[2] = {V0, V1};
 #pragma unroll
     for (int s = 0; s < 2; ++s) {
-      const double* g = r + 4 + 7 * s;
+      const T* g = r + 4 + 7 * s;
       const T c = T(g[0]);
       const T m2 = Q[at(src[s], IVY)], m3 = Q[at(src[s], IVZ)];
       const T s2 = T(1.) - c * c;
@@ -459,9 +467,12 @@ __global__ void __launch_bounds__(kThreads) cs_dt_kernel(CsParams P, const void*
                                                          unsigned long long* key) {
   const int n = P.n, nc = P.nc;
   const size_t pst = (size_t)nc * nc;
-  const Geo G = geo_of(P.geo, nc);
+  const Geo<T> G = geo_of<T>(P.geo, nc);
+  const T phi0 = T(P.phi0);
   const T* U = static_cast<const T*>(buf);
-  double m = INFINITY;
+  // the minimum in the state's type, widened once per warp (exact and
+  // monotone, so the same value as widening every cell)
+  T m = T(INFINITY);
   int nan = 0;
   const size_t total = (size_t)6 * n * n;
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
@@ -471,12 +482,12 @@ __global__ void __launch_bounds__(kThreads) cs_dt_kernel(CsParams P, const void*
     const int p = (int)(e / ((size_t)n * n));
     const size_t c = (size_t)k * nc + j;
     T w[4];
-    sw_prim<T>(U + (size_t)p * 4 * pst, pst, c, T(G.cos_c[c]), w, T(P.phi0));
-    const T cs = sqrt(P.phi0 > 0. ? T(P.phi0) + w[IDN] : w[IDN]);
+    sw_prim<T>(U + (size_t)p * 4 * pst, pst, c, T(G.cos_c[c]), w, phi0);
+    const T cs = sqrt(phi0 > T(0) ? phi0 + w[IDN] : w[IDN]);
     const T d2 = T(G.w2[c]) / (fabs(w[IVY]) + cs);
     const T d3 = T(G.w3[c]) / (fabs(w[IVZ]) + cs);
     if (isnan(d2) || isnan(d3)) nan = 1;
-    m = fmin(m, (double)fmin(d2, d3));
+    m = fmin(m, fmin(d2, d3));
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -484,7 +495,7 @@ __global__ void __launch_bounds__(kThreads) cs_dt_kernel(CsParams P, const void*
     nan |= __shfl_xor_sync(0xffffffffu, nan, o);
   }
   if ((threadIdx.x & 31) == 0) {
-    atomicMin(&key[0], dkey(m));
+    atomicMin(&key[0], dkey((double)m));
     if (nan) atomicOr(&key[1], 1ull);
   }
 }
@@ -516,8 +527,18 @@ int grid_for(size_t work) {
 
 }  // namespace
 
+__global__ void to_f32(const double* src, float* dst, size_t n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = (float)src[i];
+}
+
 struct sg_cs_handle {
   sg_cs_desc d;
+  // SG_F32: FP32 copies of the geometry and of the two seam tables
+  float* geo32 = nullptr;
+  float* gtab32 = nullptr;
+  float* stab32 = nullptr;
   void* buf[3] = {nullptr, nullptr, nullptr};
   void* scratch = nullptr;
   int cur = 0, base = 0;
@@ -547,8 +568,35 @@ int sg_cs_create(const sg_cs_desc* d, sg_cs_handle** out) {
     const unsigned long long init[2] = {kKeyInf, 0};
     e = cudaMemcpy(h->key, init, sizeof(init), cudaMemcpyHostToDevice);
   }
+  if (e == cudaSuccess && d->dtype == SG_F32) {
+    // the FP32 kernels read FP32 copies; the tables' flat indices (cells,
+    // and faces up to 6 nc (nc + 1)) stay exact in FP32 below 2^24
+    const size_t nc = (size_t)d->n + 2 * kNg;
+    if (6 * nc * (nc + 1) >= (size_t)1 << 24) {
+      cudaFree(h->key);
+      delete h;
+      return cs_fail(SG_ERR_UNSUPPORTED, "sg_cs_create: FP32 needs fewer than "
+                     "2^24 faces in the six panels (n %d)", d->n);
+    }
+    const size_t ng = 7 * nc * nc + 6 * nc * (nc + 1);
+    const size_t nt = (size_t)kGhostStride * d->nghost;
+    const size_t ns = (size_t)kSeamStride * d->nseam;
+    e = cudaMalloc(&h->geo32, ng * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&h->gtab32, nt * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&h->stab32, ns * sizeof(float));
+    if (e == cudaSuccess) {
+      to_f32<<<grid_for(ng), kThreads>>>(d->geo, h->geo32, ng);
+      to_f32<<<grid_for(nt), kThreads>>>(d->ghost_tab, h->gtab32, nt);
+      to_f32<<<grid_for(ns), kThreads>>>(d->seam_tab, h->stab32, ns);
+      e = cudaGetLastError();
+      if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    }
+  }
   if (e != cudaSuccess) {
     if (h->key) cudaFree(h->key);
+    cudaFree(h->geo32);
+    cudaFree(h->gtab32);
+    cudaFree(h->stab32);
     delete h;
     return cs_fail(SG_ERR_CUDA, "sg_cs_create: %s", cudaGetErrorString(e));
   }
@@ -559,6 +607,9 @@ int sg_cs_create(const sg_cs_desc* d, sg_cs_handle** out) {
 int sg_cs_destroy(sg_cs_handle* h) {
   if (!h) return 0;
   if (h->key) cudaFree(h->key);
+  cudaFree(h->geo32);
+  cudaFree(h->gtab32);
+  cudaFree(h->stab32);
   delete h;
   return 0;
 }
@@ -628,10 +679,11 @@ static CsParams cs_params(const sg_cs_handle* h) {
   CsParams P = {};
   P.n = h->d.n;
   P.nc = h->d.n + 2 * kNg;
-  P.geo = h->d.geo;
-  P.gtab = h->d.ghost_tab;
+  const bool f32 = h->d.dtype == SG_F32;
+  P.geo = f32 ? (const void*)h->geo32 : (const void*)h->d.geo;
+  P.gtab = f32 ? (const void*)h->gtab32 : (const void*)h->d.ghost_tab;
   P.nghost = h->d.nghost;
-  P.stab = h->d.seam_tab;
+  P.stab = f32 ? (const void*)h->stab32 : (const void*)h->d.seam_tab;
   P.nseam = h->d.nseam;
   P.phi0 = h->d.dtype == SG_F32 ? h->d.phi_ref : 0.;
   P.hllc = h->d.riemann == SG_CS_HLLC;
@@ -674,12 +726,14 @@ int sg_cs_stage(sg_cs_handle* h, int32_t stage, const double* dt_dev,
   const size_t faces = (size_t)2 * 6 * P.n * (P.n + 1);
   const size_t cells = (size_t)6 * P.n * P.n;
   if (h->d.dtype == SG_F64) {
-    cs_flux_kernel<double><<<grid_for(faces), kThreads, 0, s>>>(P);
+    (P.hllc ? cs_flux_kernel<double, true> : cs_flux_kernel<double, false>)
+        <<<grid_for(faces), kThreads, 0, s>>>(P);
     cs_seam_flux_kernel<double><<<grid_for(P.nseam), kThreads, 0, s>>>(P);
     cs_update_kernel<double><<<grid_for(cells), kThreads, 0, s>>>(P);
     cs_ghost_kernel<double><<<grid_for(P.nghost), kThreads, 0, s>>>(P, P.out);
   } else {
-    cs_flux_kernel<float><<<grid_for(faces), kThreads, 0, s>>>(P);
+    (P.hllc ? cs_flux_kernel<float, true> : cs_flux_kernel<float, false>)
+        <<<grid_for(faces), kThreads, 0, s>>>(P);
     cs_seam_flux_kernel<float><<<grid_for(P.nseam), kThreads, 0, s>>>(P);
     cs_update_kernel<float><<<grid_for(cells), kThreads, 0, s>>>(P);
     cs_ghost_kernel<float><<<grid_for(P.nghost), kThreads, 0, s>>>(P, P.out);
