@@ -391,6 +391,15 @@ __device__ __forceinline__ unsigned long long vbits(double x) {
   return static_cast<unsigned long long>(__double_as_longlong(x));
 }
 
+// a column's work array in the finish: element i at p[i s]
+struct VCol {
+  double* p;
+  size_t s;
+  __device__ __forceinline__ double& operator[](int i) const {
+    return p[(size_t)i * s];
+  }
+};
+
 // finite, tested on the exponent bits (integer pipes, not the FP64 one)
 __device__ __forceinline__ bool vfinite(double x) {
   return ((__double_as_longlong(x) >> 52) & 0x7ff) != 0x7ff;
@@ -761,10 +770,15 @@ __global__ void __launch_bounds__(NL == 32 ? 32 * kVicWarps : kThreads)
   const bool ok = vfinite(D[0]);
   const bool wood = n >= 3;
   // work arrays of the column, in the (now free) Woodbury scratch
-  double* mM = S.Z0 + col * n * 5;  // n + 1: the face mass below layer i
-  double* mq = mM + (n + 1);        // n + 1: the moved total mass
-  double* mdn = mq + (n + 1);       // n: the dry-gas increment
-  double* rho = mdn + n;            // n: the density of each layer
+  // the warp form keeps a column's arrays contiguous; the thread form
+  // interleaves the columns (index i at i ncol + col), so a warp's 32
+  // columns read and write consecutive doubles
+  const size_t ws = NL == 32 ? 1 : ncol;
+  double* const w0p = NL == 32 ? S.Z0 + col * n * 5 : S.Z0 + col;
+  const VCol mM{w0p, ws};                                  // n + 1: the face mass below layer i
+  const VCol mq{w0p + (size_t)(n + 1) * ws, ws};           // n + 1: the moved total mass
+  const VCol mdn{w0p + (size_t)(2 * n + 2) * ws, ws};      // n: the dry-gas increment
+  const VCol rho{w0p + (size_t)(3 * n + 2) * ws, ws};      // n: the density of each layer
   if (ok) {
     for (int i = lane; i < n; i += NL) {
       double w[5];
