@@ -195,6 +195,49 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+class Ranks:
+    """The replicas of a torchrun launch: one rank per GPU and no collective
+    on the data path (blocks, members and requests are independent).  The
+    job's timed interval is the slowest rank's (max over ranks), and a
+    rate counts every rank's units: ``job_rate``."""
+
+    def __init__(self, backend: str = "nccl"):
+        import torch.distributed as dist
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.backend = backend
+        self._dist = dist
+        if self.world > 1 and not dist.is_initialized():
+            dist.init_process_group(backend, init_method="env://")
+
+    def barrier(self) -> None:
+        if self.world > 1:
+            self._dist.barrier()
+
+    def max(self, x: float) -> float:
+        """x of the slowest rank (every rank gets it)."""
+        if self.world == 1:
+            return float(x)
+        import torch
+        dev = torch.device("cuda", self.local) if self.backend == "nccl" \
+            else torch.device("cpu")
+        t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+        self._dist.all_reduce(t, op=self._dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self) -> None:
+        if self.world > 1:
+            self._dist.barrier()
+            self._dist.destroy_process_group()
+
+
+def job_rate(units_per_rank: float, world: int, seconds_max: float) -> float:
+    """Whole-job throughput of weakly scaled replicas: every rank's units
+    over the slowest rank's time."""
+    return units_per_rank * world / seconds_max
+
+
 def cpu_baseline(opts, workload, seconds, u0_host=None):
     """The CPU oracle on every host core: cell-updates/s on a bounded sample
     (as many full RK3 steps of the same block as fit in `seconds`, >= 2)."""
@@ -254,13 +297,9 @@ def run_reference(args):
 
 def run_native(args):
     import torch
-    import torch.distributed as dist
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        dist.init_process_group("nccl", init_method="env://")
+    ranks = Ranks()
+    world, rank, local = ranks.world, ranks.rank, ranks.local
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
 
@@ -290,8 +329,7 @@ def run_native(args):
     # device-timed steps, cold L2 for each
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.steps)]
-    if world > 1:
-        dist.barrier()
+    ranks.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
         for k in range(args.steps):
@@ -302,11 +340,8 @@ def run_native(args):
         torch.cuda.synchronize()
     step_ms = [a.elapsed_time(b) for a, b in ev]
     t_total = sum(step_ms) / 1e3
-    if world > 1:
-        t = torch.tensor([t_total], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_total = float(t.item())
-    value = cells * args.steps * world / t_total
+    t_total = ranks.max(t_total)
+    value = job_rate(cells * args.steps, world, t_total)
 
     # roofline of the dominant kernel: the library records events around
     # each kernel of every eager stage on the launching stream
@@ -354,10 +389,7 @@ def run_native(args):
         u_host.copy_(vars["hydro_u"], non_blocking=True)
     torch.cuda.synchronize()
     e2e_t = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_t], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_t = float(t.item())
+    e2e_t = ranks.max(e2e_t)
     nbytes = u_host.numel() * u_host.element_size()
 
     rep = blk.execution_report()
@@ -375,7 +407,7 @@ def run_native(args):
             "dtype": "f64" if blk.dtype == torch.float64 else "f32",
             "data": "synthetic (the deck's initial state)",
             "config": config_of(opts, args.workload, args, world),
-            "e2e": {"value": cells * e2e_steps * world / e2e_t,
+            "e2e": {"value": job_rate(cells * e2e_steps, world, e2e_t),
                     "unit": "cell-updates/s", "h2d_bytes_per_step": nbytes,
                     "d2h_bytes_per_step": nbytes},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
@@ -397,9 +429,7 @@ def run_native(args):
             "schedule": b.schedule,
         }
         print(json.dumps(line), flush=True)
-    if world > 1:
-        dist.barrier()
-        dist.destroy_process_group()
+    ranks.close()
     return 0
 
 
@@ -454,12 +484,8 @@ def run_ensemble(args):
     FP64 GPU path on the same members: each its own FP64 MeshBlock, stepped
     one after another with its own CFL dt (graphs on)."""
     import torch
-    import torch.distributed as dist
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        dist.init_process_group("nccl", init_method="env://")
+    ranks = Ranks()
+    world, rank, local = ranks.world, ranks.rank, ranks.local
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
     import snapy_gb300 as sg
@@ -484,8 +510,7 @@ def run_ensemble(args):
     stream = torch.cuda.current_stream()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.steps)]
-    if world > 1:
-        dist.barrier()
+    ranks.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
         for k in range(args.steps):
@@ -495,11 +520,8 @@ def run_ensemble(args):
         torch.cuda.synchronize()
     step_ms = [a.elapsed_time(b) for a, b in ev]
     t_total = sum(step_ms) / 1e3
-    if world > 1:
-        t = torch.tensor([t_total], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_total = float(t.item())
-    value = cells * args.steps * world / t_total
+    t_total = ranks.max(t_total)
+    value = job_rate(cells * args.steps, world, t_total)
     flags = ens.check()
     assert int(flags.abs().sum()) == 0, f"ensemble retry flags {flags.tolist()}"
 
@@ -546,10 +568,7 @@ def run_ensemble(args):
             host[k].copy_(ens.state(k), non_blocking=True)
     torch.cuda.synchronize()
     e2e_t = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_t], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_t = float(t.item())
+    e2e_t = ranks.max(e2e_t)
     schedule = ens.batch.schedule
     del ens
 
@@ -588,7 +607,7 @@ def run_ensemble(args):
             "dtype": "f32" if precision == "float32" else "f64",
             "data": "synthetic (seeded Straka-type members)",
             "config": ensemble_config(members, precision, world),
-            "e2e": {"value": cells * e2e_steps * world / e2e_t,
+            "e2e": {"value": job_rate(cells * e2e_steps, world, e2e_t),
                     "unit": "cell-updates/s", "h2d_bytes_per_step": nbytes,
                     "d2h_bytes_per_step": nbytes},
             "plain_fp64": {"value": plain, "unit": "cell-updates/s",
@@ -612,9 +631,7 @@ def run_ensemble(args):
             "step_ms_median": statistics.median(step_ms),
         }
         print(json.dumps(line), flush=True)
-    if world > 1:
-        dist.barrier()
-        dist.destroy_process_group()
+    ranks.close()
     return 0
 
 
@@ -690,12 +707,8 @@ def serving_config(reqs, nranks):
 
 def run_serving(args):
     import torch
-    import torch.distributed as dist
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        dist.init_process_group("nccl", init_method="env://")
+    ranks = Ranks()
+    world, rank, local = ranks.world, ranks.rank, ranks.local
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
     import snapy_gb300 as sg
@@ -709,8 +722,7 @@ def run_serving(args):
     reqs = serving_trace(args.requests, args.serve_steps, args.precision,
                          args.implicit_precision)
     torch.cuda.synchronize()
-    if world > 1:
-        dist.barrier()
+    ranks.barrier()
     srv = Server(dev, timing=True)
     with ClockSampler(local) as clk:
         t0 = time.perf_counter()
@@ -720,10 +732,7 @@ def run_serving(args):
     assert not bad, f"retry flags on requests {bad}"
     total = sum(r.cells * r.steps for r in reqs)
     gpu_s = sum(srv.gpu_step_ms) / 1e3
-    if world > 1:
-        t = torch.tensor([gpu_s, wall], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        gpu_s, wall = float(t[0]), float(t[1])
+    gpu_s, wall = ranks.max(gpu_s), ranks.max(wall)
     lat = sorted(r.latency for r in reqs)
     q = lambda f: lat[min(len(lat) - 1, int(round(f * (len(lat) - 1))))]
     kms = srv.kernel_ms
@@ -768,7 +777,7 @@ def run_serving(args):
             cb = serving_cpu_baseline(small, args.cpu_seconds)
         line = {
             "metric": "cell-updates/s per RK3 step",
-            "value": total * world / gpu_s, "unit": "cell-updates/s",
+            "value": job_rate(total, world, gpu_s), "unit": "cell-updates/s",
             "n_gpus": world, "steps": len(srv.gpu_step_ms), "warmup": args.warmup,
             "ms_per_step": gpu_s / len(srv.gpu_step_ms) * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -777,7 +786,7 @@ def run_serving(args):
             "config": serving_config(reqs, world),
             "latency": {"p50_s": q(0.5), "p99_s": q(0.99), "min_s": lat[0],
                         "max_s": lat[-1], "unit": "s, arrival to result on host"},
-            "e2e": {"value": total * world / wall, "unit": "cell-updates/s",
+            "e2e": {"value": job_rate(total, world, wall), "unit": "cell-updates/s",
                     "h2d_bytes_per_step": srv.h2d_bytes / len(srv.gpu_step_ms),
                     "d2h_bytes_per_step": srv.d2h_bytes / len(srv.gpu_step_ms),
                     "note": "wall clock of the whole trace: arrivals, initial "
@@ -801,9 +810,7 @@ def run_serving(args):
             "gpu_launches": srv.launches,
         }
         print(json.dumps(line), flush=True)
-    if world > 1:
-        dist.barrier()
-        dist.destroy_process_group()
+    ranks.close()
     return 0
 
 
@@ -892,13 +899,9 @@ def cs_cpu_baseline(n, seconds):
 
 def run_cubed_sphere(args):
     import torch
-    import torch.distributed as dist
     from snapy_gb300 import cubed_sphere as cs
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        dist.init_process_group("nccl", init_method="env://")
+    ranks = Ranks()
+    world, rank, local = ranks.world, ranks.rank, ranks.local
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
     precision = args.precision or "float32"
@@ -918,8 +921,7 @@ def run_cubed_sphere(args):
     stream = torch.cuda.current_stream()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.steps)]
-    if world > 1:
-        dist.barrier()
+    ranks.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
         for k in range(args.steps):
@@ -930,12 +932,9 @@ def run_cubed_sphere(args):
         torch.cuda.synchronize()
     step_ms = [a.elapsed_time(b) for a, b in ev]
     t_total = sum(step_ms) / 1e3
-    if world > 1:
-        t = torch.tensor([t_total], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_total = float(t.item())
+    t_total = ranks.max(t_total)
     cells = 6 * n * n
-    value = cells * args.steps * world / t_total
+    value = job_rate(cells * args.steps, world, t_total)
     assert torch.isfinite(sp.state()).all()
     # one stage (flux, seam flux, update, seam halo) timed alone, L2 flushed
     s_bytes = 4 if dtype == torch.float32 else 8
@@ -977,7 +976,7 @@ def run_cubed_sphere(args):
             "dtype": "f32" if dtype == torch.float32 else "f64",
             "data": "synthetic (seeded Gaussian bump)",
             "config": cs_config(n, precision, world),
-            "e2e": {"value": cells * e2e_steps * world / e2e_t, "unit": "cell-updates/s",
+            "e2e": {"value": job_rate(cells * e2e_steps, world, e2e_t), "unit": "cell-updates/s",
                     "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak,
@@ -988,9 +987,7 @@ def run_cubed_sphere(args):
             "cpu_baseline": cb, "clocks": clk.summary(),
             "gpu_launches": args.steps * (2 + 3 * 4),
             "step_ms_median": statistics.median(step_ms)}), flush=True)
-    if world > 1:
-        dist.barrier()
-        dist.destroy_process_group()
+    ranks.close()
     return 0
 
 
