@@ -25,6 +25,22 @@ __device__ __forceinline__ T sqr(T x) {
   return x * x;
 }
 
+// a / b from r = 1 / b (the correctly rounded reciprocal): q0 = a r, the
+// exact residual a - b q0 by one fma, then q0 + e r rounded once.  For
+// normal operands and quotient this is the correctly rounded quotient, the
+// same bits as a / b (Markstein, "Computation of elementary functions on
+// the IBM RISC System/6000 processor", IBM J. Res. Dev. 34 (1990), and
+// "IA-64 and Elementary Functions" (2000), the division theorem); it costs
+// one multiply and two fmas where a division is a longer sequence, and the
+// reciprocal is shared by every quotient with the same divisor
+template <typename T>
+__device__ __forceinline__ T vdiv(T a, T b, T r) {
+  const T q0 = a * r;
+  const T e = fma(-b, q0, a);
+  return fma(e, r, q0);
+}
+
+
 // exp(x) for the well-balanced reference's anchor, written out so that the
 // GPU kernel and the CPU oracle evaluate the same operations and agree bit
 // for bit (libm's and CUDA's exp may differ by an ulp, which the anchor
@@ -248,12 +264,16 @@ __device__ __forceinline__ void lmars_flux(const T* wl, const T* wr, T gammad,
                                            int d, T* flx, T* face_pressure) {
   Axes ax = face_axes(d);
   const int ivx = ax.x, ivy = ax.y, ivz = ax.z;
-  T hl = wl[IPR] / (gammad - T(1)) / wl[IDN];
-  T hr = wr[IPR] / (gammad - T(1)) / wr[IDN];
+  // the quotients by gamma - 1 and by each side's density divide through
+  // the reciprocals (vdiv: the same bits)
+  const T gm1 = gammad - T(1), rgm1 = T(1) / gm1;
+  const T rl0 = T(1) / wl[IDN], rr0 = T(1) / wr[IDN];
+  T hl = vdiv(vdiv(wl[IPR], gm1, rgm1), wl[IDN], rl0);
+  T hr = vdiv(vdiv(wr[IPR], gm1, rgm1), wr[IDN], rr0);
   T l0 = wl[IDN], l1 = wl[ivx], l2 = wl[ivy], l3 = wl[ivz], l4 = wl[IPR];
   T r0 = wr[IDN], r1 = wr[ivx], r2 = wr[ivy], r3 = wr[ivz], r4 = wr[IPR];
-  hl += T(0.5) * (sqr(l1) + sqr(l2) + sqr(l3)) + l4 / l0;
-  hr += T(0.5) * (sqr(r1) + sqr(r2) + sqr(r3)) + r4 / r0;
+  hl += T(0.5) * (sqr(l1) + sqr(l2) + sqr(l3)) + vdiv(l4, l0, rl0);
+  hr += T(0.5) * (sqr(r1) + sqr(r2) + sqr(r3)) + vdiv(r4, r0, rr0);
   T rhobar = T(0.5) * (l0 + r0);
   T gamma_bar = T(0.5) * (gammad + gammad);
   T cbar = sqrt(T(0.5) * gamma_bar * (l4 + r4) / rhobar);
@@ -291,10 +311,12 @@ __device__ __forceinline__ void lmars_flux_anom(const T* wl, const T* wr,
   T l0 = wl[IDN], l1 = wl[ivx], l2 = wl[ivy], l3 = wl[ivz], l4 = wl[IPR];
   T r0 = wr[IDN], r1 = wr[ivx], r2 = wr[ivy], r3 = wr[ivz], r4 = wr[IPR];
   T pl = pb + l4, pr = pb + r4;
-  T hl = pl / (gammad - T(1)) / l0;
-  T hr = pr / (gammad - T(1)) / r0;
-  hl += T(0.5) * (sqr(l1) + sqr(l2) + sqr(l3)) + pl / l0;
-  hr += T(0.5) * (sqr(r1) + sqr(r2) + sqr(r3)) + pr / r0;
+  const T gm1 = gammad - T(1), rgm1 = T(1) / gm1;
+  const T rl0 = T(1) / l0, rr0 = T(1) / r0;
+  T hl = vdiv(vdiv(pl, gm1, rgm1), l0, rl0);
+  T hr = vdiv(vdiv(pr, gm1, rgm1), r0, rr0);
+  hl += T(0.5) * (sqr(l1) + sqr(l2) + sqr(l3)) + vdiv(pl, l0, rl0);
+  hr += T(0.5) * (sqr(r1) + sqr(r2) + sqr(r3)) + vdiv(pr, r0, rr0);
   T rhobar = T(0.5) * (l0 + r0);
   T cbar = sqrt(T(0.5) * gammad * (pl + pr) / rhobar);
   T pbar = T(0.5) * (l4 + r4) + T(0.5) * (rhobar * cbar) * (l1 - r1);
@@ -309,13 +331,16 @@ __device__ __forceinline__ void lmars_flux_anom(const T* wl, const T* wr,
   flx[IPR] = ubar * m0 * h;
 }
 
-// ideal-gas U->W of one cell (Cartesian: the metric raise is the identity)
+// ideal-gas U->W of one cell (Cartesian: the metric raise is the identity);
+// the three velocities divide by the density through its reciprocal (vdiv:
+// the same quotients)
 template <typename T>
 __device__ __forceinline__ void cons2prim(const T* u, T* w, T gammad) {
   w[IDN] = u[IDN];
-  w[IVX] = u[IVX] / w[IDN];
-  w[IVY] = u[IVY] / w[IDN];
-  w[IVZ] = u[IVZ] / w[IDN];
+  const T rd = T(1.) / w[IDN];
+  w[IVX] = vdiv(u[IVX], w[IDN], rd);
+  w[IVY] = vdiv(u[IVY], w[IDN], rd);
+  w[IVZ] = vdiv(u[IVZ], w[IDN], rd);
   T ke = T(0.5) * (w[IVX] * u[IVX] + w[IVY] * u[IVY] + w[IVZ] * u[IVZ]);
   T ie = u[IPR] - ke;
   w[IPR] = (gammad - T(1.)) * ie;

@@ -661,16 +661,19 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
   if (visc) {
     // without x2 only the tile row itself (rr = 1) is needed
     const int rlo = has2 ? 0 : 1, nr = has2 ? ntj + 2 : 1, nci = nx1 + 2;
+    // quotients by a shared divisor divide through its reciprocal (vdiv:
+    // the same bits)
+    const real d1 = real(2.) * real(B.dx1), d2 = real(2.) * real(B.dx2);
+    const real rd1 = real(1.) / d1, rd2 = real(1.) / d2;
     for (int idx = threadIdx.x; idx < nr * nci; idx += blockDim.x) {
       const int rr = rlo + idx / nci, i = il - 1 + (idx - (rr - rlo) * nci);
       const int r = hj + rr - 1;  // W row
       const real* vx = W + IVX * wstride + r * nc1;
       real dv = real(0);
-      dv += (vx[i + 1] - vx[i - 1]) / (real(2.) * real(B.dx1));
+      dv += vdiv(vx[i + 1] - vx[i - 1], d1, rd1);
       if (has2) {
         const real* vy = W + IVY * wstride;
-        dv += (vy[(r + 1) * nc1 + i] - vy[(r - 1) * nc1 + i]) /
-              (real(2.) * real(B.dx2));
+        dv += vdiv(vy[(r + 1) * nc1 + i] - vy[(r - 1) * nc1 + i], d2, rd2);
       }
       DIVV[rr * nc1 + i] = dv;
     }
@@ -689,8 +692,9 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
         const real* h = COV + cstride + jf * nc1;
         const real* un = COV + 2 * cstride + jf * nc1;
         real s2rho = s2 * rho[i];
-        real d1h = (h[i + 1] - h[i - 1]) / dx1;
-        real dun = (un[i + 1] - un[i - 1]) / dx1;
+        const real rdx1 = real(1.) / dx1;
+        real d1h = vdiv(h[i + 1] - h[i - 1], dx1, rdx1);
+        real dun = vdiv(un[i + 1] - un[i - 1], dx1, rdx1);
         F2[IPR * f2stride + idx] += s2rho * d1h * dun;
       }
       const int jface = j0 + jf;
@@ -706,6 +710,9 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
   if (visc) {
     const real nu = real(B.nu_iso);
     const real dx1 = real(B.dx1), dx2 = real(B.dx2);
+    const real rdx1 = real(1.) / dx1, rdx2 = real(1.) / dx2;
+    const real d2x1 = real(2.) * dx1, d2x2 = real(2.) * dx2;
+    const real rd2x1 = real(1.) / d2x1, rd2x2 = real(1.) / d2x2;
     const real* vx = W + IVX * wstride;
     const real* vy = W + IVY * wstride;
     const real* vz = W + IVZ * wstride;
@@ -735,12 +742,12 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
 #pragma unroll
       for (int ivar = 0; ivar < 3; ++ivar) {
         const real* vc = ivar == 0 ? vx : (ivar == 1 ? vy : vz);
-        real stress = (vc[o + f] - vc[o + f - 1]) / dx1;
+        real stress = vdiv(vc[o + f] - vc[o + f - 1], dx1, rdx1);
         if (ivar == 0) {
           stress = real(2.) * stress - real(2. / 3.) * divf;
         } else if (ivar == 1 && has2) {
-          real below = (vx[o + nc1 + f - 1] - vx[o - nc1 + f - 1]) / (real(2.) * dx2);
-          real above = (vx[o + nc1 + f] - vx[o - nc1 + f]) / (real(2.) * dx2);
+          real below = vdiv(vx[o + nc1 + f - 1] - vx[o - nc1 + f - 1], d2x2, rd2x2);
+          real above = vdiv(vx[o + nc1 + f] - vx[o - nc1 + f], d2x2, rd2x2);
           stress += real(0.5) * (above + below);
         }
         real mf = -nu * rf * stress;
@@ -764,12 +771,12 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
 #pragma unroll
         for (int ivar = 0; ivar < 3; ++ivar) {
           const real* vc = ivar == 0 ? vx : (ivar == 1 ? vy : vz);
-          real stress = (vc[o + i] - vc[om + i]) / dx2;
+          real stress = vdiv(vc[o + i] - vc[om + i], dx2, rdx2);
           if (ivar == 1) {
             stress = real(2.) * stress - real(2. / 3.) * divf;
           } else if (ivar == 0) {
-            real below = (vy[om + i + 1] - vy[om + i - 1]) / (real(2.) * dx1);
-            real above = (vy[o + i + 1] - vy[o + i - 1]) / (real(2.) * dx1);
+            real below = vdiv(vy[om + i + 1] - vy[om + i - 1], d2x1, rd2x1);
+            real above = vdiv(vy[o + i + 1] - vy[o + i - 1], d2x1, rd2x1);
             stress += real(0.5) * (above + below);
           }
           real mf = -nu * rf * stress;
@@ -832,6 +839,7 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
   // energy correction, and the RK combine on the interior cells
   const real a1 = real(B.dx3 * B.dx2), a2 = real(B.dx3 * B.dx1);
   const real vol = real(B.dx3 * (B.dx2 * B.dx1));
+  const real rvol = real(1.) / vol;  // every quotient by vol divides by it
   const real rdt = real(dt), mdt = real(-dt);
   const real w0 = real(p.w0), w1 = real(p.w1), w2 = real(p.w2);
   const real g = real(B.grav1);
@@ -856,7 +864,7 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
         dv = dv + (a2 * f2[nx1] - a2 * f2[0]);
       }
       if (dv3) dv = dv + dv3[v * icells + vci];
-      du[v] = mdt * (dv / vol);
+      du[v] = mdt * vdiv(dv, vol, rvol);
     }
     if (wb) {
       const real rho = W[IDN * wstride + wc], vx = W[IVX * wstride + wc];
@@ -881,7 +889,7 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
           const real* f2 = VF2 + (v - IVX) * f2stride + jt * nx1 + ii;
           dv = dv + (a2 * f2[nx1] - a2 * f2[0]);
         }
-        du[v] = du[v] - rdt * (dv / vol);
+        du[v] = du[v] - rdt * vdiv(dv, vol, rvol);
       }
     }
     if (wb) {
@@ -889,7 +897,7 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
       const int k = ii;
       const real* fm = F1 + IDN * f1stride + jt * nf1;  // fm[k] = face il+k
       auto drho = [&](int kk) -> real {
-        real vmd = (a1 * fm[kk + 1] - a1 * fm[kk]) / vol;
+        real vmd = vdiv(a1 * fm[kk + 1] - a1 * fm[kk], vol, rvol);
         return mdt * vmd;
       };
       // the x1 geometry's constants of interior cell k (slope weights w0,
@@ -898,7 +906,7 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
       const double* xt = B.x1tab + 6 * k;
       real hi = real(xt[4]);
       real lo = real(xt[5]);
-      real fgw = rdt * ((hi * (a1 * fm[k + 1]) - lo * (a1 * fm[k])) / vol);
+      real fgw = rdt * vdiv(hi * (a1 * fm[k + 1]) - lo * (a1 * fm[k]), vol, rvol);
       if (nx1 >= 3) {
         int kc = k < 1 ? 1 : (k > nx1 - 2 ? nx1 - 2 : k);
         int k0 = kc - 1;

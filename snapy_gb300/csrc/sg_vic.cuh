@@ -75,21 +75,6 @@ __device__ __forceinline__ void vmat_mul(const T* a, const T* b,
     }
 }
 
-// a / b from r = 1 / b (the correctly rounded reciprocal): q0 = a r, the
-// exact residual a - b q0 by one fma, then q0 + e r rounded once.  For
-// normal operands and quotient this is the correctly rounded quotient, the
-// same bits as a / b (Markstein, "Computation of elementary functions on
-// the IBM RISC System/6000 processor", IBM J. Res. Dev. 34 (1990), and
-// "IA-64 and Elementary Functions" (2000), the division theorem); it costs
-// one multiply and two fmas where a division is a longer sequence, and the
-// reciprocal is shared by every quotient with the same divisor
-template <typename T>
-__device__ __forceinline__ T vdiv(T a, T b, T r) {
-  const T q0 = a * r;
-  const T e = fma(-b, q0, a);
-  return fma(e, r, q0);
-}
-
 template <typename T>
 __device__ __forceinline__ void vflux_jacobian(T* J, T gm1,
                                                const T* w) {
