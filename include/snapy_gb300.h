@@ -140,6 +140,18 @@ int sg_max_dt(sg_handle* h, const int32_t* redo_dev, double* dt_dev_out,
  * bit 6 a tile whose shared-memory staging did not arrive within the stage
  * kernel's bounded wait (the tile was not computed) */
 int sg_check(sg_handle* h, int32_t* flags_dev, sg_stream_t stream);
+/* The retry decision on the device, after a step (MeshBlockImpl::apply_redo
+ * with local_redo_flag_tensor's flags, src/mesh/meshblock_redo.cpp:32-150):
+ * sg_check's flags into flags_dev, then per block a flagged block counts a
+ * redo (redo_dev[b] += 1) and gets its step-start state back in the current
+ * buffer, state_dev[b] = 1, or -1 once redo_dev[b] exceeds max_redo; a
+ * terminated block stays terminated and keeps its last accepted state
+ * (restored at every later call).  A block without flags gets redo_dev[b]
+ * = 0, state_dev[b] = 0.  sg_max_dt with the same redo_dev gives the
+ * retried blocks dt x 2^-redo.  No host read: a captured step graph can
+ * end with it.  Call it after a step's last stage, before the next step. */
+int sg_check_retry(sg_handle* h, int32_t* flags_dev, int32_t* redo_dev,
+                   int32_t max_redo, int32_t* state_dev, sg_stream_t stream);
 /* initialize (MeshBlockImpl::initialize, src/mesh/meshblock.cpp:306-420):
  * the boundary functions fill the ghosts of the FP64 primitives w_in[b]
  * (device pointers in a host array, written in place), and the current

@@ -111,6 +111,7 @@ SIGNATURES = {
     "sg_budget_boundary": (ctypes.c_int, [_vp, _vp, _i32, _vp]),
     "sg_autotune": (ctypes.c_int, [_vp, _i32, _vp, _vp, _vp, _vp]),
     "sg_set_schedule": (ctypes.c_int, [_vp, _vp, _i32]),
+    "sg_check_retry": (ctypes.c_int, [_vp, _vp, _vp, _i32, _vp, _vp]),
     "sg_set_timing": (ctypes.c_int, [_vp, _i32]),
     "sg_kernel_times": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double),
                                        ctypes.POINTER(ctypes.c_int64)]),

@@ -140,6 +140,8 @@ class Batch:
         self.dt = torch.zeros(self.nblock, dtype=torch.float64, device=device)
         self.redo = torch.zeros(self.nblock, dtype=torch.int32, device=device)
         self.flags = torch.zeros(self.nblock, dtype=torch.int32, device=device)
+        # the device retry decision: 0 accepted, 1 redo, -1 terminated
+        self.state = torch.zeros(self.nblock, dtype=torch.int32, device=device)
         self._w_ptrs = (ctypes.c_void_p * self.nblock)()
 
     def close(self) -> None:
@@ -233,6 +235,17 @@ class Batch:
 
     def restore(self) -> None:
         _lib.check(self.L.sg_restore(self.h), "sg_restore")
+
+    def check_retry(self, max_redo: int, stream=None) -> torch.Tensor:
+        """After a step, on the device: the flags, and per block a redo
+        (step-start state restored, redo += 1, state 1), a termination past
+        max_redo (state -1, kept) or an accepted step (redo and state 0).
+        The next max_dt halves the retried blocks' dt.  Returns the state."""
+        _lib.check(self.L.sg_check_retry(self.h, self.flags.data_ptr(),
+                                         self.redo.data_ptr(), int(max_redo),
+                                         self.state.data_ptr(), _stream(stream)),
+                   "sg_check_retry")
+        return self.state
 
     def fill_ghosts(self, stream=None) -> None:
         _lib.check(self.L.sg_fill_ghosts(self.h, _stream(stream)), "sg_fill_ghosts")

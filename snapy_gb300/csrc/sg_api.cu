@@ -88,7 +88,10 @@ __global__ void finish_dt_kernel(int nblock, unsigned long long* red, int* nan,
 // 1.001 x its floor (a NaN compares false, so it is a hit too); bit 3: NaN
 __global__ void finish_check_kernel(int nblock, unsigned long long* red,
                                     int* nan, int* status, double dfloor,
-                                    double pfloor, int32_t* flags) {
+                                    double pfloor, int32_t* flags,
+                                    int32_t* redo = nullptr,
+                                    int32_t* state = nullptr,
+                                    int max_redo = 0) {
   int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= nblock) return;
   double rmin = unkey(red[4 * b + 1]), pmin = unkey(red[4 * b + 2]);
@@ -103,8 +106,38 @@ __global__ void finish_check_kernel(int nblock, unsigned long long* red,
   if (status[b] & sg::kStatusStaging) f |= 64;
   status[b] = 0;
   flags[b] = f;
+  // the retry decision (MeshBlockImpl::apply_redo): a flagged block counts
+  // a redo and is restored (state 1), or is terminated past max_redo (state
+  // -1, kept from then on: its last accepted state is restored at every
+  // later check); an accepted step clears the count
+  if (redo) {
+    if (state[b] == -1) {
+    } else if (f) {
+      const int r = redo[b] + 1;
+      redo[b] = r;
+      state[b] = r > max_redo ? -1 : 1;
+    } else {
+      redo[b] = 0;
+      state[b] = 0;
+    }
+  }
   red[4 * b] = red[4 * b + 1] = red[4 * b + 2] = kKeyInf;
   nan[b] = 0;
+}
+
+// the step-start state back into the current buffer of every block whose
+// retry state is not 0 (4-byte words: both storage types)
+__global__ void restore_kernel(const BlockDev* __restrict__ tab, int cur,
+                               int base, const int32_t* state, int esz) {
+  const int b = blockIdx.y;
+  if (state[b] == 0) return;
+  const BlockDev& B = tab[b];
+  const size_t words = (size_t)5 * B.nc1 * B.nc2 * B.nc3 * esz / 4;
+  const uint32_t* src = static_cast<const uint32_t*>(B.buf[base]);
+  uint32_t* dst = static_cast<uint32_t*>(B.buf[cur]);
+  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < words;
+       q += (size_t)gridDim.x * blockDim.x)
+    dst[q] = src[q];
 }
 
 // the x1 geometry constants of the gravity-work correction for interior
@@ -1046,6 +1079,33 @@ int sg_check(sg_handle* h, int32_t* flags, sg_stream_t stream) {
       h->scheme.pressure_floor, flags);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "sg_check: finish");
+  return 0;
+}
+
+int sg_check_retry(sg_handle* h, int32_t* flags, int32_t* redo,
+                   int32_t max_redo, int32_t* state, sg_stream_t stream) {
+  if (!h || !flags || !redo || !state)
+    return fail(SG_ERR_ARG, "sg_check_retry: null");
+  if (max_redo < 0) return fail(SG_ERR_ARG, "sg_check_retry: max_redo %d", max_redo);
+  if (h->cur == h->base)
+    return fail(SG_ERR_STATE, "sg_check_retry: no step since the last one "
+                "began (the current buffer is the step-start buffer)");
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  int rc = upload(h, s);
+  if (rc) return rc;
+  rc = f64(h) ? sg_launch_reduce_f64(h->dev, h->nblock, h->cur, h->red,
+                                     h->nan, h->max_cells, s)
+              : sg_launch_reduce_f32(h->dev, h->nblock, h->cur, h->red,
+                                     h->nan, h->max_cells, s);
+  if (rc) return cuda_fail((cudaError_t)rc, "sg_check_retry: reduce");
+  finish_check_kernel<<<(h->nblock + 127) / 128, 128, 0, s>>>(
+      h->nblock, h->red, h->nan, h->status, h->scheme.density_floor,
+      h->scheme.pressure_floor, flags, redo, state, max_redo);
+  int gx = (int)std::min<size_t>((h->max_plane * 5 + 255) / 256, 1024);
+  restore_kernel<<<dim3(gx, h->nblock), 256, 0, s>>>(
+      h->dev, h->cur, h->base, state, f64(h) ? 8 : 4);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "sg_check_retry");
   return 0;
 }
 

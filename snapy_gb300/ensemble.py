@@ -25,7 +25,8 @@ from .options import DeckError, MeshBlockOptions
 class Ensemble:
     def __init__(self, members: Sequence[MeshBlockOptions],
                  device: Optional[torch.device] = None,
-                 dtype: Optional[torch.dtype] = None, graphs: bool = True):
+                 dtype: Optional[torch.dtype] = None, graphs: bool = True,
+                 retry: bool = False):
         if not members:
             raise ValueError("an ensemble needs at least one member")
         self.members = list(members)
@@ -44,6 +45,11 @@ class Ensemble:
                            self.device, dtype)
         self.nstage = len(schemes[0]["wght"])
         self.graphs = graphs
+        # retry on the device (MeshBlockImpl::apply_redo per member): each
+        # step ends with the check, a rejected member gets its step-start
+        # state back and its next dt halved, all inside the captured step
+        self.retry = retry
+        self.max_redo = self.members[0].intg().max_redo
         self._graphs = {}
         self._seen = set()
         self.replays = 0
@@ -90,7 +96,11 @@ class Ensemble:
             b.dt.copy_(fixed_dt)
         for s in range(self.nstage):
             b.stage(s)
-        self.time.add_(b.dt)
+        if self.retry:
+            state = b.check_retry(self.max_redo)
+            self.time.add_(torch.where(state == 0, b.dt, torch.zeros_like(b.dt)))
+        else:
+            self.time.add_(b.dt)
 
     def step(self, dt: Optional[torch.Tensor] = None) -> None:
         """One RK step of every member: each member's own CFL time step from
@@ -128,6 +138,17 @@ class Ensemble:
             else:
                 self._launch_step(dt)
                 self._seen.add(key)
+
+    @property
+    def redo(self) -> torch.Tensor:
+        """Per-member redo counts (device; retry mode)."""
+        return self.batch.redo
+
+    @property
+    def outcome(self) -> torch.Tensor:
+        """Per-member outcome of the last step (device; retry mode): 0
+        accepted, 1 rejected and restored, -1 terminated."""
+        return self.batch.state
 
     def check(self) -> torch.Tensor:
         """Per-member retry flags (one host read)."""
