@@ -126,6 +126,21 @@ def config_of(opts, workload, args, nranks):
     }
 
 
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of a
+# dominant kernel, from one ncu capture of the same workload and kernel
+# build: profiles/straka512x128_fp64_launches_and_kernels.md and
+# profiles/ensemble64_fp32_vic_launches_and_kernels.md
+NCU_TRAFFIC = {
+    ("straka", "float64", "vic_solve_kernel"): 42.009600e6 + 0.149248e6,
+    ("ensemble", "float32", "vic_solve_kernel"): 1.288739e9 + 0.550966e9,
+}
+
+
+def ncu_traffic(workload, precision, kernel):
+    """The captured DRAM bytes per launch, or None for an uncaptured case."""
+    return NCU_TRAFFIC.get((workload, precision, kernel))
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -412,7 +427,9 @@ def run_native(args):
                     "d2h_bytes_per_step": nbytes},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak,
-                         "peak_kind": peak_kind, "traffic": None,
+                         "peak_kind": peak_kind,
+                         "traffic": ncu_traffic(args.workload,
+                                                opts.hydro().precision, dom),
                          "kernel": dom,
                          "bytes_per_launch": per_launch[dom],
                          "mean_launch_us": dom_ms / dom_n * 1e3,
@@ -618,7 +635,8 @@ def run_ensemble(args):
             "schedule": schedule,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak,
-                         "peak_kind": peak_kind, "traffic": None,
+                         "peak_kind": peak_kind,
+                         "traffic": ncu_traffic("ensemble", precision, dom),
                          "kernel": dom, "bytes_per_launch": per_launch[dom],
                          "mean_launch_us": dom_ms / dom_n * 1e3,
                          "limiter": "FP64 issue rate (one FP64 warp "
