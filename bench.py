@@ -82,9 +82,19 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--implicit-precision", choices=["float64", "float32"],
-                    default="float32",
-                    help="ensemble/serving: assembly of the implicit blocks "
-                         "(the block-tridiagonal solve is FP64 either way)")
+                    default=None,
+                    help="FP32 state: float32 assembles the implicit blocks in "
+                         "FP32 and refines their solve to FP64 accuracy, "
+                         "float64 assembles and solves them in FP64 (default: "
+                         "float32 for ensemble and serving, the deck's for "
+                         "the others)")
+    ap.add_argument("--implicit-solve", choices=["refined", "direct"],
+                    default=None,
+                    help="the solve of float32-assembled implicit blocks: "
+                         "refined (FP32 sweeps corrected with FP64 residuals, "
+                         "the default) or direct (FP64 for every column)")
+    ap.add_argument("--implicit-corrections", type=int, choices=[1, 2, 3],
+                    default=None, help="the refined solve's corrections")
     ap.add_argument("--requests", type=int, default=8,
                     help="serving: requests in the trace")
     ap.add_argument("--serve-steps", type=int, default=200,
@@ -97,6 +107,13 @@ def load_options(args):
     opts = sg.MeshBlockOptions.from_yaml(os.path.join(ROOT, WORKLOADS[args.workload]))
     if args.precision:
         opts.hydro().precision = args.precision
+    if (args.implicit_precision and opts.hydro().icorr is not None
+            and opts.hydro().precision == "float32"):
+        opts.hydro().icorr.precision = args.implicit_precision
+    if args.implicit_solve:
+        opts.implicit_solve = args.implicit_solve
+    if args.implicit_corrections:
+        opts.implicit_corrections = args.implicit_corrections
     return opts
 
 
@@ -105,6 +122,21 @@ def initial_state(opts, workload, device):
     if workload == "sod":
         return problems.sod(opts, device)
     return problems.straka(opts, device)
+
+
+def implicit_solve(opts):
+    """How the implicit blocks are solved: FP32 assembly takes the refined
+    solve unless the deck asks for the direct one, FP64 assembly the direct
+    FP64 solve."""
+    ic = opts.hydro().icorr
+    if ic is None:
+        return None
+    if (opts.hydro().precision == "float32" and ic.precision == "float32"
+            and opts.implicit_solve == "refined"):
+        return ("refined to the FP64 solution: FP32 block-Thomas sweeps, "
+                f"{opts.implicit_corrections} corrections from FP64 residuals, "
+                "the FP64 solve for columns that do not converge")
+    return "direct FP64"
 
 
 def config_of(opts, workload, args, nranks):
@@ -119,6 +151,7 @@ def config_of(opts, workload, args, nranks):
         "precision": h.precision,
         "gravity": bool(h.grav and h.grav.grav1),
         "implicit": bool(h.icorr),
+        "implicit_solve": implicit_solve(opts),
         "l2": "flushed between timed steps (512 MiB write; the block fits in L2)",
         "graphs": "one per buffer rotation, captured before the warm-up steps",
         "replicas": nranks,
@@ -484,8 +517,9 @@ def ensemble_config(members, precision, nranks):
     return {"workload": f"ensemble of {len(members)} Straka-type members "
                         f"(nx2 in 128..512, nx1 in 32..128, 50 m, seed "
                         f"{ENSEMBLE_SEED}), lmars+weno5+rk3+VIC, {precision} "
-                        "bulk, FP64 implicit solve",
+                        "bulk, implicit solve to the FP64 solution",
             "implicit_assembly": ip,
+            "implicit_solve": implicit_solve(members[0][0]),
             "members": len(members), "cells": cells, "precision": precision,
             "gravity": True, "implicit": True,
             "dt": "each member's own CFL step, on the device, every step",
@@ -513,7 +547,10 @@ def run_ensemble(args):
                                         precision=precision)
     if precision == "float32":
         for o, _ in members:
-            o.hydro().icorr.precision = args.implicit_precision
+            o.hydro().icorr.precision = args.implicit_precision or "float32"
+    for o, _ in members:
+        o.implicit_solve = args.implicit_solve or o.implicit_solve
+        o.implicit_corrections = args.implicit_corrections or o.implicit_corrections
     cells = sum(o.coord().nx1 * o.coord().nx2 for o, _ in members)
     ens = Ensemble([o for o, _ in members], device=dev)
     ens.initialize([w for _, w in members])
@@ -678,7 +715,8 @@ def run_reference_ensemble(args):
     return 0
 
 
-def serving_trace(n, steps, precision=None, implicit_precision=None):
+def serving_trace(n, steps, precision=None, implicit_precision=None,
+                  implicit_solve=None, implicit_corrections=None):
     """The serving trace: n requests with seeded sizes and seeds, exponential
     inter-arrival times of mean 1 / SERVE_RATE."""
     import torch
@@ -699,6 +737,10 @@ def serving_trace(n, steps, precision=None, implicit_precision=None):
             opts.hydro().precision = precision
         if opts.hydro().precision == "float32" and implicit_precision:
             opts.hydro().icorr.precision = implicit_precision
+        if implicit_solve:
+            opts.implicit_solve = implicit_solve
+        if implicit_corrections:
+            opts.implicit_corrections = implicit_corrections
         seed = SERVE_SEED + 1 + i
         reqs.append(Request(i, opts, (lambda o=opts, s=seed: problems.convection3d(o, "cpu", seed=s)),
                             steps, t))
@@ -711,9 +753,10 @@ def serving_config(reqs, nranks):
                         f"{SERVE_SEED}), (nx2, nx3, nx1) in {{64,96,128}}^2 x "
                         f"{{64,96}} at 50 m, {reqs[0].steps} RK3 steps each, "
                         f"lmars+weno5+rk3+VIC, {reqs[0].options.hydro().precision} "
-                        "bulk, FP64 implicit solve",
+                        "bulk, implicit solve to the FP64 solution",
             "requests": len(reqs), "steps_per_request": reqs[0].steps,
             "implicit_assembly": reqs[0].options.hydro().icorr.precision,
+            "implicit_solve": implicit_solve(reqs[0].options),
             "cells": [r.cells for r in reqs],
             "admission": "first come first served against free HBM",
             "batching": "continuous: every running request in the same "
@@ -733,12 +776,14 @@ def run_serving(args):
     from snapy_gb300.serving import Server
     # warm-up: a short trace compiles nothing but touches every code path
     warm = serving_trace(2, max(3, args.warmup), args.precision,
-                         args.implicit_precision)
+                         args.implicit_precision or "float32",
+                         args.implicit_solve, args.implicit_corrections)
     for r in warm:
         r.arrival = 0.0
     Server(dev).run(warm)
     reqs = serving_trace(args.requests, args.serve_steps, args.precision,
-                         args.implicit_precision)
+                         args.implicit_precision or "float32",
+                         args.implicit_solve, args.implicit_corrections)
     torch.cuda.synchronize()
     ranks.barrier()
     srv = Server(dev, timing=True)

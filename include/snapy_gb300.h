@@ -200,6 +200,22 @@ int sg_kernel_times(sg_handle* h, double* ms, int64_t* launches);
  * is no solve), ms_out[2] the best stage and solve milliseconds per launch.
  * sg_set_schedule applies a stored choice (tj null or 0: the library's
  * rule; finish 0: the library's rule). */
+/* The implicit solve of integration/implicit-precision float32 blocks.  By
+ * default it is refined: the block-tridiagonal system of each column is
+ * solved by the block-Thomas sweep in FP32, then corrected `corrections`
+ * times (default 2, at most 3) with FP64 residuals (mixed-precision
+ * iterative refinement, the scheme of LAPACK's dsgesv), the solution
+ * accumulating in FP64.  A column whose FP32 factorisation fails, or whose
+ * last correction leaves an estimated error above 2^-44 of its solution,
+ * takes the direct FP64 solve.  corrections 0 runs the direct FP64 solve for
+ * every column (the FP64 blocks' solve, bitwise).  FP64 blocks always run
+ * the direct solve.  The forms agree to FP64 roundoff of the solution.  Not
+ * inside a stream capture; graphs captured before must be captured again. */
+int sg_set_solve(sg_handle* h, int32_t corrections);
+/* per block, the running count of columns the refined solve left to the
+ * direct FP64 solve (ImplicitHydroImpl's "implicit.fp64_columns" monitor,
+ * src/hydro/hydro.cpp:460-466); waits for the device */
+int sg_solve_fallbacks(sg_handle* h, int64_t* counts);
 int sg_autotune(sg_handle* h, int32_t reps, int32_t* tj_out,
                 int32_t* finish_out, double* ms_out, sg_stream_t stream);
 int sg_set_schedule(sg_handle* h, const int32_t* tj, int32_t finish);

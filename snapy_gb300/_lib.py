@@ -109,6 +109,8 @@ SIGNATURES = {
     "sg_bind_step_fields": (ctypes.c_int, [_vp, _i32, _vp, _vp, _vp, _vp, ctypes.c_size_t]),
     "sg_budget_totals": (ctypes.c_int, [_vp, _vp, _vp]),
     "sg_budget_boundary": (ctypes.c_int, [_vp, _vp, _i32, _vp]),
+    "sg_set_solve": (ctypes.c_int, [_vp, _i32]),
+    "sg_solve_fallbacks": (ctypes.c_int, [_vp, _vp]),
     "sg_autotune": (ctypes.c_int, [_vp, _i32, _vp, _vp, _vp, _vp]),
     "sg_set_schedule": (ctypes.c_int, [_vp, _vp, _i32]),
     "sg_check_retry": (ctypes.c_int, [_vp, _vp, _vp, _i32, _vp, _vp]),

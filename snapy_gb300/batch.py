@@ -339,3 +339,16 @@ class Batch:
         with torch.cuda.device(self.device):
             self.schedule = _at.tune(self, reps=reps, use_cache=use_cache)
         return self.schedule
+
+    def solve_fallbacks(self) -> List[int]:
+        """Per block, the columns the refined implicit solve has left to the
+        direct FP64 solve so far (the reference's implicit.fp64_columns)."""
+        out = (ctypes.c_int64 * self.nblock)()
+        _lib.check(self.L.sg_solve_fallbacks(self.h, out), "sg_solve_fallbacks")
+        return list(out)
+
+    def set_solve(self, corrections: int) -> None:
+        """The solve of implicit-precision float32 blocks: refined with that
+        many FP64-residual corrections (1 to 3; 2 by default), or 0 for the
+        direct FP64 solve of every column."""
+        _lib.check(self.L.sg_set_solve(self.h, int(corrections)), "sg_set_solve")

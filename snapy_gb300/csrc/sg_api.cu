@@ -203,12 +203,16 @@ struct sg_handle {
   int32_t max_nc1 = 0;
   int32_t launches = 0;
   int* status = nullptr;  // per-block solve status bits (VIC failures)
+  unsigned long long* fallbacks = nullptr;  // per block: refined-solve
+                                            // columns solved directly
   std::vector<double*> x1tabs;  // per-block geometry tables (gravity)
   bool has3 = false;            // a 3-D block: the x3 sweep runs
   size_t sum_icols = 0;         // implicit columns of all blocks
   int wide = 0;  // enough columns for a thread per column in the finish
   int wide_auto = 0;  // that rule's own answer (finish form 0)
   bool implicit = false;
+  int refine = 0;  // corrections of the refined implicit solve (0: direct)
+  int any_f32 = 0;  // a block assembles its implicit blocks in FP32
   size_t max_icells = 0, max_icols = 0;
   std::vector<sg_block_desc> descs;   // as created (tile re-layout)
   int32_t finish = 0;  // implicit finish form: 0 auto, 1 warp, 2 thread
@@ -320,6 +324,23 @@ extern "C" {
 
 const char* sg_last_error(void) { return g_err.c_str(); }
 
+int sg_set_solve(sg_handle* h, int32_t corrections) {
+  if (!h || corrections < 0 || corrections > 3)
+    return fail(SG_ERR_ARG, "sg_set_solve: %d corrections (0 to 3)",
+                corrections);
+  h->refine = h->any_f32 ? corrections : 0;
+  return 0;
+}
+
+int sg_solve_fallbacks(sg_handle* h, int64_t* counts) {
+  if (!h || !counts) return fail(SG_ERR_ARG, "sg_solve_fallbacks: null");
+  cudaError_t e = cudaMemcpy(counts, h->fallbacks,
+                             sizeof(unsigned long long) * h->nblock,
+                             cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "sg_solve_fallbacks");
+  return 0;
+}
+
 int sg_set_schedule(sg_handle* h, const int32_t* tj, int32_t finish) {
   if (!h || finish < 0 || finish > 2)
     return fail(SG_ERR_ARG, "sg_set_schedule: finish form %d", finish);
@@ -385,6 +406,8 @@ int sg_autotune(sg_handle* h, int32_t reps, int32_t* tj_out,
     p.dt = dt;
     p.first = 1;
     p.status = h->status;
+    p.refine = h->refine;
+    p.fallbacks = h->fallbacks;
     p.max_nc1 = h->max_nc1;
     auto stage = [&]() -> int {
       p.ntile = h->ntile;
@@ -622,6 +645,10 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
                   "needs the FP32 state (dynamics/precision float32)", b);
     }
     B.implicit_f32 = d.implicit_scheme != 0 && d.implicit_precision == SG_F32;
+    if (B.implicit_f32) {
+      h->any_f32 = 1;
+      h->refine = 2;
+    }
     B.x1tab = nullptr;
     if (d.grav1 != 0.) {
       const int nx1 = d.nc1 - 2 * d.ng;
@@ -673,6 +700,10 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
     size_t vic_bytes = d.implicit_scheme ? icells * sg::kVicDoublesPerCell *
                                                sizeof(double)
                                          : 0;
+    if (d.implicit_scheme && d.implicit_precision == SG_F32)
+      vic_bytes += (icells * sg::kVicFloatsPerCell +
+                    icols * sg::kVicFloatsPerColumn) * sizeof(float);
+    vic_bytes = (vic_bytes + 15) / 16 * 16;  // the x3 part starts aligned
     size_t dv3_bytes = d.nc3 > 1 ? 5 * icells * (f64(h) ? 8 : 4) : 0;
     h->vic_bytes.push_back(vic_bytes);
     h->scratch_bytes.push_back(vic_bytes + dv3_bytes);
@@ -697,6 +728,10 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
   if (e == cudaSuccess) e = cudaMalloc(&h->ptrs, sizeof(void*) * nblock);
   if (e == cudaSuccess) e = cudaMalloc(&h->status, sizeof(int) * nblock);
   if (e == cudaSuccess) e = cudaMemset(h->status, 0, sizeof(int) * nblock);
+  if (e == cudaSuccess)
+    e = cudaMalloc(&h->fallbacks, sizeof(unsigned long long) * nblock);
+  if (e == cudaSuccess)
+    e = cudaMemset(h->fallbacks, 0, sizeof(unsigned long long) * nblock);
   if (e == cudaSuccess) e = cudaMallocHost(&h->ptrs_host, sizeof(void*) * nblock);
   if (e != cudaSuccess) {
     sg_destroy(h);
@@ -719,6 +754,7 @@ int sg_destroy(sg_handle* h) {
   if (h->nan) cudaFree(h->nan);
   if (h->ptrs) cudaFree(h->ptrs);
   if (h->status) cudaFree(h->status);
+  if (h->fallbacks) cudaFree(h->fallbacks);
   if (h->ptrs_host) cudaFreeHost(h->ptrs_host);
   for (cudaEvent_t e : h->events) cudaEventDestroy(e);
   for (double* t : h->x1tabs) cudaFree(t);
@@ -963,6 +999,8 @@ int sg_stage(sg_handle* h, int32_t stage, const double* dt_dev,
   p.dt = dt_dev;
   p.first = stage == 0;
   p.status = h->status;
+  p.refine = h->refine;
+  p.fallbacks = h->fallbacks;
   p.max_nc1 = h->max_nc1;
   // events between the launches when timing is on and the stream is not
   // being captured: ev[0] (x3 ev[6]) stage ev[1] (assemble ev[2] solve

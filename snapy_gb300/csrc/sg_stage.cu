@@ -1496,9 +1496,25 @@ extern "C" int SG_NAME(sg_launch_vic)(const BlockDev* tab, StageParams p,
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return (int)e;
   if (ev) cudaEventRecord(ev[0], stream);
-  // one warp per column
-  // the solve: kVicCols columns per single-warp CTA
+  // the refined solve of implicit-precision float32 blocks (FP32 sweeps,
+  // FP64 residuals); the columns it does not converge are left to the
+  // direct solve
   int gs = (int)((max_cols + kVicCols - 1) / kVicCols);
+  if (p.refine) {
+    int gr = (int)((max_cells + kThreads - 1) / kThreads);
+    if (gr > 4096) gr = 4096;
+    const size_t cw = (max_cols + kCorrCols - 1) / kCorrCols;  // warps
+    const int gc = (int)((cw + kCorrWarps - 1) / kCorrWarps);
+    vic_solve32_kernel<<<dim3(gs, p.nblock), 32, 0, stream>>>(tab, p);
+    for (int k = 1; k <= p.refine; ++k) {
+      vic_residual_kernel<<<dim3(gr, p.nblock), kThreads, 0, stream>>>(tab, p);
+      vic_correct32_kernel<<<dim3(gc, p.nblock), 32 * kCorrWarps, 0, stream>>>(
+          tab, p, k == p.refine);
+    }
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return (int)e;
+  }
+  // the solve: kVicCols columns per single-warp CTA
   vic_solve_kernel<<<dim3(gs, p.nblock), 32, 0, stream>>>(tab, p, status);
   e = cudaGetLastError();
   if (e != cudaSuccess) return (int)e;

@@ -82,6 +82,16 @@ __host__ __device__ inline const double* base_r(const double* b, int nc1) { retu
 // doubles of VIC scratch per interior cell: du, du0 (5 each), the blocks
 // a, b, c (25 each), the solution and the two Woodbury vectors (5 each)
 constexpr int kVicDoublesPerCell = 100;
+// implicit-precision float32 blocks add, after the FP64 part, a part for
+// the refined solve: per interior cell the blocks A, B, C in FP32 (28 each:
+// 25 and a pad), the factors of the FP32 sweep's pivot blocks (32), its C'
+// blocks (28) and the residuals of the three right-hand sides (16: 15 and
+// a pad); per
+// interior column the largest update of each right-hand side in the last
+// pass (3), the largest |x| of each after the first (3) and the direct-solve
+// mask (1 int)
+constexpr int kVicFloatsPerCell = 160;
+constexpr int kVicFloatsPerColumn = 7;
 
 // a tile's bulk-copy wait ran out (status bit; the step is rejected)
 constexpr int32_t kStatusStaging = 1 << 30;
@@ -97,6 +107,10 @@ struct StageParams {
   double w0, w1, w2;    // RK weights of this stage
   const double* dt;     // device scalar: the host dt or a captured graph's
   int32_t first;        // stage 0: the step fields start from zero
+  int32_t refine;       // corrections of the refined implicit solve of
+                        // implicit-precision float32 blocks (0: direct)
+  unsigned long long* fallbacks;  // per block: columns the refined solve left
+                                  // to the direct FP64 solve (a running count)
   int32_t* status;      // per-block status bits (kStatusStaging: a tile's
                         // staging wait ran out)
   int32_t smem_rows;    // x1 lines held in shared memory per tile

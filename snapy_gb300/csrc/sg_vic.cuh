@@ -50,6 +50,42 @@ __device__ __forceinline__ VicScratch vic_scratch(const BlockDev& B) {
   return s;
 }
 
+// the refined-solve part of an implicit-precision float32 block's scratch
+// (after the FP64 part, 16-byte aligned): per cell the blocks A, B, C in
+// FP32 (25 each in rows of 5, padded to 28 for 16-byte loads), the pivot
+// blocks' LU factors (25, then the reciprocals of the diagonal (5) and the
+// pivot rows packed 3 bits each, padded to 32), the C' blocks (28) and the
+// residuals, then the sweep's y, of the three right-hand sides (15 and a
+// pad, row v of right-hand side k at 5 k + v); per column the largest update of each
+// right-hand side in the last pass (3), the largest |x| of each after the
+// first pass (3) and the direct-solve mask
+constexpr int kBlk32 = 28;  // floats per cell of A, B, C
+constexpr int kLu32 = 32;   // floats per cell of the factors
+constexpr int kR32 = 16;    // floats per cell of the residuals (15 and a pad)
+struct VicScratch32 {
+  float *A, *B, *C, *LU, *CP, *R, *stat;
+  int* mask;
+  size_t ncol;
+};
+
+__device__ __forceinline__ VicScratch32 vic_scratch32(const BlockDev& B,
+                                                      const VicScratch& S,
+                                                      int n) {
+  VicScratch32 t;
+  const size_t c = S.cells;
+  float* f = reinterpret_cast<float*>(B.vic + (size_t)kVicDoublesPerCell * c);
+  t.ncol = c / n;
+  t.A = f;
+  t.B = f + kBlk32 * c;
+  t.C = f + 2 * kBlk32 * c;
+  t.LU = f + 3 * kBlk32 * c;
+  t.CP = t.LU + kLu32 * c;
+  t.R = t.CP + kBlk32 * c;
+  t.stat = t.R + kR32 * c;
+  t.mask = reinterpret_cast<int*>(t.stat + 6 * t.ncol);
+  return t;
+}
+
 // the padded (x3, x2) row of interior column `col` (x2 fastest)
 __device__ __forceinline__ size_t vic_row(const BlockDev& B, size_t col) {
   const int ng = B.ng;
@@ -219,7 +255,8 @@ template <typename T>
 __device__ __forceinline__ void vic_assemble_cell(const BlockDev& B,
                                                   const VicScratch& S,
                                                   const real* uin,
-                                                  double dtc, size_t e) {
+                                                  double dtc, size_t e,
+                                                  bool f32copy) {
   const int ng = B.ng, nc1 = B.nc1, n = nc1 - 2 * ng;
   const size_t plane = (size_t)nc1 * B.nc2 * B.nc3;
   const T grav = T(B.grav1), gm1 = T(B.gammad - 1.);
@@ -315,6 +352,26 @@ __device__ __forceinline__ void vic_assemble_cell(const BlockDev& B,
     S.B[cell * 25 + k] = (double)b[k];
     S.C[cell * 25 + k] = (double)c[k];
   }
+  if (sizeof(T) == sizeof(float) && f32copy) {
+    // the refined solve's FP32 sweeps read these (the same values), in
+    // 16-byte stores (the row of 28 is 16-byte aligned)
+    const VicScratch32 F = vic_scratch32(B, S, n);
+    float4* a4 = reinterpret_cast<float4*>(F.A + cell * kBlk32);
+    float4* b4 = reinterpret_cast<float4*>(F.B + cell * kBlk32);
+    float4* c4 = reinterpret_cast<float4*>(F.C + cell * kBlk32);
+#pragma unroll
+    for (int e = 0; e < 6; ++e) {
+      a4[e] = make_float4((float)a[4 * e], (float)a[4 * e + 1],
+                          (float)a[4 * e + 2], (float)a[4 * e + 3]);
+      b4[e] = make_float4((float)b[4 * e], (float)b[4 * e + 1],
+                          (float)b[4 * e + 2], (float)b[4 * e + 3]);
+      c4[e] = make_float4((float)c[4 * e], (float)c[4 * e + 1],
+                          (float)c[4 * e + 2], (float)c[4 * e + 3]);
+    }
+    a4[6] = make_float4((float)a[24], 0.f, 0.f, 0.f);
+    b4[6] = make_float4((float)b[24], 0.f, 0.f, 0.f);
+    c4[6] = make_float4((float)c[24], 0.f, 0.f, 0.f);
+  }
 }
 
 __global__ void __launch_bounds__(kThreads)
@@ -328,10 +385,10 @@ __global__ void __launch_bounds__(kThreads)
        e += (size_t)gridDim.x * blockDim.x) {
 #ifdef SG_REAL_IS_FLOAT
     if (B.implicit_f32)
-      vic_assemble_cell<float>(B, S, uin, dtc, e);
+      vic_assemble_cell<float>(B, S, uin, dtc, e, p.refine != 0);
     else
 #endif
-      vic_assemble_cell<double>(B, S, uin, dtc, e);
+      vic_assemble_cell<double>(B, S, uin, dtc, e, false);
   }
 }
 
@@ -469,9 +526,18 @@ __global__ void __launch_bounds__(32)
   if ((size_t)blockIdx.x * kVicCols >= ncol) return;  // the whole warp
   const int lane = threadIdx.x, g = lane / kVicLanes, q = lane % kVicLanes;
   const size_t col = (size_t)blockIdx.x * kVicCols + g;
-  const bool valid = col < ncol;
-  // a group past the last column shadows it and never stores
-  const size_t cc = valid ? col : ncol - 1;
+  bool valid = col < ncol;
+  // an implicit-precision float32 block solves here only the columns its
+  // refined solve left to FP64 (the mask); a warp with none leaves at once
+  if (Bk.implicit_f32 && p.refine) {
+    const VicScratch32 F = vic_scratch32(Bk, S, n);
+    valid = valid && F.mask[col] != 0;
+    if (!__any_sync(0xffffffffu, valid)) return;
+    if (valid && q == 0) atomicAdd(&p.fallbacks[blockIdx.y], 1ull);
+  }
+  // a group past the last column (or unmasked) shadows a column and never
+  // stores
+  const size_t cc = col < ncol ? col : ncol - 1;
   const double dtc = p.w2 * p.dt[blockIdx.y];
   const double rdtc = 1.0 / dtc;  // every du / dt_corr divides by it
   const bool wood = n >= 3;
@@ -718,6 +784,720 @@ constexpr int kVicWarps = 4;  // columns per CTA of the finish (a warp each)
 template <int NL>
 __device__ __forceinline__ void vsync() {
   if (NL > 1) vsync<NL>();
+}
+
+// ---------------------------------------------------------------------------
+// the refined solve of implicit-precision float32 blocks.  The block-
+// tridiagonal system T x = b of every column (the right-hand sides du /
+// dt_corr and the two Woodbury unit vectors) is solved by the block-Thomas
+// sweep in FP32 (vic_solve32_kernel, the direct solve's lane layout), then
+// corrected p.refine times (1 to 3): the FP64 residual r = b - T x
+// (vic_residual_kernel, from the FP64 copies of the FP32-assembled blocks,
+// which are exact) is solved by the same FP32 sweep and added to x in FP64.
+// That is mixed-precision iterative refinement (the scheme of LAPACK's
+// dsgesv): x converges to the FP64 solution by a factor of about
+// kappa(T) eps32 per correction, the factorisation on the FP32 pipes and
+// only the residuals in FP64.  The solutions accumulate in the direct
+// solve's D, Z0, Z1.  A column whose FP32 factorisation fails or whose last
+// correction leaves an estimated error above 2^-44 of its solution takes the
+// direct FP64 solve instead (vic_solve_kernel, which reads the mask), as the
+// reference retries a failed FP32 column in FP64 (src/hydro/hydro.cpp:436-
+// 466).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float vshfl32(float v, int src) {
+  return __shfl_sync(0xffffffffu, v, src, kVicLanes);
+}
+
+__device__ __forceinline__ bool vfinite32(float x) {
+  return ((__float_as_uint(x) >> 23) & 0xffu) != 0xffu;
+}
+
+// step J of the FP32 factorisation on this lane's column x (the layout of
+// vlu_step: lanes q < 5 hold the block's columns, every lane keeps the row
+// data); the reciprocals are correctly rounded, the rest is FP32 arithmetic
+template <int J>
+__device__ __forceinline__ void vlu32_step(float (&x)[5], float (&vv)[5],
+                                           float (&scale)[5], int (&indx)[5],
+                                           bool& good, int q, bool colane) {
+  float best = -1.f;
+  int imax = J;
+#pragma unroll
+  for (int i2 = J; i2 < 5; ++i2) {
+    const float dum = vv[i2] * fabsf(x[i2]);
+    if (dum >= best) {
+      best = dum;
+      imax = i2;
+    }
+  }
+  imax = __shfl_sync(0xffffffffu, imax, J, kVicLanes);
+  indx[J] = imax;
+#pragma unroll
+  for (int i2 = J + 1; i2 < 5; ++i2) {
+    const bool sw = imax == i2;
+    const float xj = x[J], xi = x[i2];
+    if (colane) {
+      x[J] = sw ? xi : xj;
+      x[i2] = sw ? xj : xi;
+    }
+    const float vj = vv[J], vi = vv[i2];
+    vv[i2] = sw ? vj : vi;
+    const float sj = scale[J], si = scale[i2];
+    scale[J] = sw ? si : sj;
+    scale[i2] = sw ? sj : si;
+  }
+  if (J < 4) {
+    const float piv = vshfl32(x[J], J);
+    good = good && piv != 0.f;
+    const float dinv = __frcp_rn(piv);
+    float l[5];
+#pragma unroll
+    for (int i2 = J + 1; i2 < 5; ++i2) {
+      l[i2] = vshfl32(x[i2], J) * dinv;
+      if (q == J) x[i2] = l[i2];
+    }
+    if (colane && q > J) {
+#pragma unroll
+      for (int i2 = J + 1; i2 < 5; ++i2) x[i2] = fmaf(-l[i2], x[J], x[i2]);
+    }
+  }
+}
+
+struct VicSolve32Smem {
+  float lu[kVicCols][25];       // the factorised block of each column
+  float rd[kVicCols][5];        // 1 / the diagonal of each factorisation
+  float vec[kVicCols][2][15];   // back substitution: d, z0, z1 of a layer
+};
+
+// the first, factoring pass of the refined solve, kVicCols columns per
+// warp, lane q of a column owning right-hand-side column q of  lu [c' | y |
+// y0 | y1] = [c | b | e0 | e1]  as in vic_solve_kernel: the block-Thomas
+// sweep in FP32 for b = du / dt_corr and the unit vectors, x into D, Z0, Z1.
+// It keeps each layer's LU factors (with the diagonal's reciprocals and the
+// pivot rows), c' and y for the corrections, and per column the largest |x|
+// of each right-hand side; a column whose factorisation fails is masked
+__global__ void __launch_bounds__(32)
+    vic_solve32_kernel(const BlockDev* __restrict__ tab, StageParams p) {
+  __shared__ VicSolve32Smem sm;
+  const BlockDev& Bk = tab[blockIdx.y];
+  if (!Bk.implicit || !Bk.implicit_f32) return;
+  const VicScratch S = vic_scratch(Bk);
+  const int n = Bk.nc1 - 2 * Bk.ng;
+  const VicScratch32 F = vic_scratch32(Bk, S, n);
+  const size_t ncol = F.ncol;
+  if ((size_t)blockIdx.x * kVicCols >= ncol) return;
+  const int lane = threadIdx.x, g = lane / kVicLanes, q = lane % kVicLanes;
+  const size_t col = (size_t)blockIdx.x * kVicCols + g;
+  // a group past the last column shadows a column and never stores
+  const bool valid = col < ncol;
+  const size_t cc = valid ? col : ncol - 1;
+  bool ok = valid;
+  if (!__any_sync(0xffffffffu, ok)) return;
+  const double dtc = p.w2 * p.dt[blockIdx.y];
+  const bool wood = n >= 3;
+  const int m = wood ? 8 : 6;  // right-hand sides in use
+  const float* A = F.A + cc * n * kBlk32;
+  const float* Bm = F.B + cc * n * kBlk32;
+  const float* C = F.C + cc * n * kBlk32;
+  float* LU = F.LU + cc * n * kLu32;
+  float* CP = F.CP + cc * n * kBlk32;
+  float* R = F.R + cc * n * kR32;
+  const double* du = S.du + cc * n;
+  const float rdtc = (float)(1. / dtc);
+  const bool colane = q < 5;
+  const unsigned full = 0xffffffffu;
+
+  float s[5];  // this lane's y of the previous layer
+#pragma unroll
+  for (int k = 0; k < 5; ++k) s[k] = 0.f;
+  {
+    // ---- the forward sweep: lanes q < 5 carry the block's columns ----
+    // a layer's loads, issued one layer ahead: this lane's column of a and
+    // of c (q < 5), du / dt_corr of row q (q < 5) or the unit vectors, b
+    float xa[5], ca[5], dqa = 0.f;
+    float4 bn[kBlk32 / 4];
+    auto load = [&](int i) {
+#pragma unroll
+      for (int r = 0; r < 5; ++r) {
+        if (colane) {
+          xa[r] = A[i * kBlk32 + r * 5 + q];
+          ca[r] = C[i * kBlk32 + r * 5 + q];
+        } else {
+          xa[r] = (r == 4 && ((q == 6 && i == 0) || (q == 7 && i == n - 1)))
+                      ? 1.f : 0.f;
+          ca[r] = 0.f;
+        }
+      }
+      if (colane) dqa = (float)du[(size_t)q * S.cells + i] * rdtc;
+      const float4* b4 = reinterpret_cast<const float4*>(Bm + i * kBlk32);
+#pragma unroll
+      for (int k = 0; k < kBlk32 / 4; ++k) bn[k] = b4[k];
+    };
+    load(0);
+    for (int i = 0; i < n; ++i) {
+      if (!__any_sync(full, ok)) break;
+      float x[5], c5[5], b[kBlk32];
+#pragma unroll
+      for (int r = 0; r < 5; ++r) {
+        x[r] = xa[r];
+        c5[r] = ca[r];
+      }
+#pragma unroll
+      for (int k = 0; k < kBlk32 / 4; ++k) {
+        b[4 * k] = bn[k].x;
+        b[4 * k + 1] = bn[k].y;
+        b[4 * k + 2] = bn[k].z;
+        b[4 * k + 3] = bn[k].w;
+      }
+      const float dq = dqa;
+      if (i + 1 < n) load(i + 1);
+#pragma unroll
+      for (int r = 0; r < 5; ++r) {  // du / dt_corr gathered on lane 5
+        const float v = vshfl32(dq, r);
+        if (q == 5) x[r] = v;
+      }
+      if (i > 0) {
+#pragma unroll
+        for (int r = 0; r < 5; ++r) {
+          float t = x[r];
+#pragma unroll
+          for (int k = 0; k < 5; ++k) t = fmaf(-b[r * 5 + k], s[k], t);
+          x[r] = t;
+        }
+      }
+      // the factorisation, scaled partial pivoting
+      bool good = true;
+      unsigned mx[5];
+#pragma unroll
+      for (int r = 0; r < 5; ++r) {
+        if (colane) good = good && vfinite32(x[r]);
+        mx[r] = colane ? __float_as_uint(fabsf(x[r])) : 0u;
+      }
+#pragma unroll
+      for (int off = 4; off >= 1; off >>= 1)
+#pragma unroll
+        for (int r = 0; r < 5; ++r)
+          mx[r] = max(mx[r], __shfl_xor_sync(full, mx[r], off, kVicLanes));
+      float scale[5], vv[5];
+#pragma unroll
+      for (int r = 0; r < 5; ++r) {
+        scale[r] = __uint_as_float(mx[r]);
+        good = good && mx[r] != 0u;
+      }
+      {
+        const float big = vpick5(q < 5 ? q : 0, scale[0], scale[1], scale[2],
+                                 scale[3], scale[4]);
+        const float inv = __frcp_rn(big);
+#pragma unroll
+        for (int r = 0; r < 5; ++r) vv[r] = vshfl32(inv, r);
+      }
+      int indx[5];
+      vlu32_step<0>(x, vv, scale, indx, good, q, colane);
+      vlu32_step<1>(x, vv, scale, indx, good, q, colane);
+      vlu32_step<2>(x, vv, scale, indx, good, q, colane);
+      vlu32_step<3>(x, vv, scale, indx, good, q, colane);
+      vlu32_step<4>(x, vv, scale, indx, good, q, colane);
+      if (colane) {
+        const float dg = vpick5(q, x[0], x[1], x[2], x[3], x[4]);
+        const float sc =
+            vpick5(q, scale[0], scale[1], scale[2], scale[3], scale[4]);
+        // the pivot tolerance, in FP32's epsilon
+        good = good && vfinite32(dg) &&
+               fabsf(dg) > 8.f * 5.f * 1.1920929e-7f * sc;
+        const float rdg = __frcp_rn(dg);
+#pragma unroll
+        for (int r = 0; r < 5; ++r) sm.lu[g][r * 5 + q] = x[r];
+        sm.rd[g][q] = rdg;
+        // the factors for the corrections
+        if (valid) {
+#pragma unroll
+          for (int r = 0; r < 5; ++r) LU[i * kLu32 + r * 5 + q] = x[r];
+          LU[i * kLu32 + 25 + q] = rdg;
+          if (q == 0) {
+            int pk = 0;
+#pragma unroll
+            for (int j = 0; j < 5; ++j) pk |= indx[j] << (3 * j);
+            LU[i * kLu32 + 30] = __int_as_float(pk);
+          }
+        }
+      }
+      ok = ok && vgroup_all(good, g);
+      __syncwarp();
+      // the back-solve of this lane's right-hand side
+      float sol[5];
+#pragma unroll
+      for (int r = 0; r < 5; ++r) sol[r] = colane ? c5[r] : x[r];
+#pragma unroll
+      for (int rr = 0; rr < 5; ++rr) {
+        const int ip = indx[rr];
+#pragma unroll
+        for (int k = rr + 1; k < 5; ++k) {
+          const bool sw = ip == k;
+          const float a = sol[rr], c = sol[k];
+          sol[rr] = sw ? c : a;
+          sol[k] = sw ? a : c;
+        }
+      }
+      const float* lu = sm.lu[g];
+#pragma unroll
+      for (int rr = 1; rr < 5; ++rr)
+#pragma unroll
+        for (int jj = 0; jj < rr; ++jj)
+          sol[rr] = fmaf(-lu[rr * 5 + jj], sol[jj], sol[rr]);
+#pragma unroll
+      for (int rr = 4; rr >= 0; --rr) {
+#pragma unroll
+        for (int jj = rr + 1; jj < 5; ++jj)
+          sol[rr] = fmaf(-lu[rr * 5 + jj], sol[jj], sol[rr]);
+        sol[rr] = sol[rr] * sm.rd[g][rr];
+      }
+      if (valid) {
+        if (colane) {
+#pragma unroll
+          for (int r = 0; r < 5; ++r) CP[i * kBlk32 + r * 5 + q] = sol[r];
+        } else if (q < m) {
+#pragma unroll
+          for (int r = 0; r < 5; ++r) R[i * kR32 + (q - 5) * 5 + r] = sol[r];
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < 5; ++r) s[r] = sol[r];
+      __syncwarp();
+    }
+  }
+
+  // ---- back substitution: x_i = y_i - c'_i x_(i+1), into D, Z0, Z1 ----
+  // lane q handles the (vector, row) pairs q and q + 8 of the 15; a layer's
+  // c' row and y are loaded a layer ahead
+  float dmax[2] = {0.f, 0.f};
+  bool fin = true;
+  if (__any_sync(full, ok)) {
+    double* const D0 = S.D + cc * n * 5;
+    double* const Z0 = S.Z0 + cc * n * 5;
+    double* const Z1 = S.Z1 + cc * n * 5;
+    bool use[2];
+    double* xp[2];
+    int pr2[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int pr = q + kVicLanes * h;
+      pr2[h] = pr;
+      use[h] = pr < 15 && (pr < 5 || wood);
+      const int v = pr / 5, r = pr % 5;
+      xp[h] = (v == 0 ? D0 : (v == 1 ? Z0 : Z1)) + r;
+    }
+    float crn[2][5], yn[2];
+    auto bload = [&](int i) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        if (use[h]) {
+          const int r = pr2[h] % 5;
+#pragma unroll
+          for (int k = 0; k < 5; ++k) crn[h][k] = CP[i * kBlk32 + r * 5 + k];
+          yn[h] = R[i * kR32 + pr2[h]];
+        }
+      }
+    };
+    if (q >= 5) {
+#pragma unroll
+      for (int r = 0; r < 5; ++r) sm.vec[g][0][(q - 5) * 5 + r] = s[r];
+    }
+    if (n >= 2) bload(n - 2);
+    __syncwarp();
+    // the last layer: x = y
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      if (use[h]) {
+        const float val = sm.vec[g][0][pr2[h]];
+        if (ok) xp[h][(n - 1) * 5] = (double)val;
+        fin = fin && vfinite32(val);
+        dmax[h] = fmaxf(dmax[h], fabsf(val));
+      }
+    }
+    int cur = 0;
+    for (int i = n - 2; i >= 0; --i) {
+      float cr[2][5], y[2];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+#pragma unroll
+        for (int k = 0; k < 5; ++k) cr[h][k] = crn[h][k];
+        y[h] = yn[h];
+      }
+      if (i > 0) bload(i - 1);
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        if (use[h]) {
+          const float* xn = sm.vec[g][cur] + (pr2[h] / 5) * 5;
+          float t = y[h];
+#pragma unroll
+          for (int k = 0; k < 5; ++k) t = fmaf(-cr[h][k], xn[k], t);
+          sm.vec[g][cur ^ 1][pr2[h]] = t;
+          if (ok) xp[h][i * 5] = (double)t;
+          fin = fin && vfinite32(t);
+          dmax[h] = fmaxf(dmax[h], fabsf(t));
+        }
+      }
+      __syncwarp();
+      cur ^= 1;
+    }
+  }
+  ok = ok && vgroup_all(fin, g);
+  // the largest |x| of each right-hand side over the column's lanes
+  // (pairs: vector pr / 5): the solution's scale, and the first "update"
+  float dv[3];
+#pragma unroll
+  for (int v = 0; v < 3; ++v) {
+    float dl = 0.f;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int pr = q + kVicLanes * h;
+      if (pr < 15 && pr / 5 == v) dl = fmaxf(dl, dmax[h]);
+    }
+#pragma unroll
+    for (int off = 4; off >= 1; off >>= 1)
+      dl = fmaxf(dl, __shfl_xor_sync(full, dl, off, kVicLanes));
+    dv[v] = dl;
+  }
+  if (valid && ok && q < 3) {
+    float* st = F.stat + cc * 6;
+    const float d = vpick5(q, dv[0], dv[1], dv[2], 0.f, 0.f);
+    st[q] = d;
+    st[3 + q] = d;
+  }
+  if (valid && q == 0) F.mask[cc] = ok ? 0 : 1;
+}
+
+// a correction of the refined solve, one thread per column and right-hand
+// side (kCorrCols columns of three lanes per warp, kCorrWarps warps per
+// CTA): y_i = LU_i^-1 (r_i - b_i y_(i-1)) from the stored factors, then
+// d_i = y_i - c'_i d_(i+1), added to x in FP64.  Each sweep runs over a
+// ring of kCorrRing layers in shared memory that the warp fills with
+// asynchronous copies (cp.async) kCorrRing - 1 layers ahead: a column's
+// factors, b and residuals going forward, c', y and x going back.  Per
+// column and right-hand side the largest |d| is kept.  The last correction
+// decides convergence: the error it leaves is about |d| rho, rho = |d| /
+// |d_prev| the observed contraction, accepted at or below 2^-44 of the
+// largest |x|.  A converged column then gets the Woodbury step of the direct
+// solve; the others are masked for the direct FP64 solve
+constexpr int kCorrCols = 10;   // columns per warp (30 of its lanes)
+constexpr int kCorrWarps = 2;   // warps per CTA
+constexpr int kCorrRing = 4;    // layers in flight per warp
+// shared-memory row strides of a column's factors and residuals: multiples
+// of 4 floats (16-byte copies) that spread a warp's ten columns over the
+// banks (at most two columns per bank)
+constexpr int kLuRow = kLu32 + 4, kRRow = kR32 + 4;
+
+union __align__(16) CorrSlot {
+  struct {
+    float lu[kCorrCols][kLuRow];
+    float b[kCorrCols][kBlk32];
+    float r[kCorrCols][kRRow];
+  } f;  // forward
+  struct {
+    float cp[kCorrCols][kBlk32];
+    float y[32][5];
+    double x[32][5];
+  } g;  // back
+};
+
+__device__ __forceinline__ void cpa16(void* s, const void* g) {
+  const unsigned a = static_cast<unsigned>(__cvta_generic_to_shared(s));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(a), "l"(g)
+               : "memory");
+}
+__device__ __forceinline__ void cpa8(void* s, const void* g) {
+  const unsigned a = static_cast<unsigned>(__cvta_generic_to_shared(s));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(a), "l"(g)
+               : "memory");
+}
+__device__ __forceinline__ void cpa4(void* s, const void* g) {
+  const unsigned a = static_cast<unsigned>(__cvta_generic_to_shared(s));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(a), "l"(g)
+               : "memory");
+}
+__device__ __forceinline__ void cpa_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+// this thread's copies of all but the newest n groups are complete
+template <int N>
+__device__ __forceinline__ void cpa_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+__global__ void __launch_bounds__(32 * kCorrWarps)
+    vic_correct32_kernel(const BlockDev* __restrict__ tab, StageParams p,
+                         int last) {
+  __shared__ CorrSlot ring[kCorrWarps][kCorrRing];
+  const BlockDev& Bk = tab[blockIdx.y];
+  if (!Bk.implicit || !Bk.implicit_f32) return;
+  const VicScratch S = vic_scratch(Bk);
+  const int n = Bk.nc1 - 2 * Bk.ng;
+  const VicScratch32 F = vic_scratch32(Bk, S, n);
+  const size_t ncol = F.ncol;
+  const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+  const size_t warp = (size_t)blockIdx.x * kCorrWarps + wl;
+  if (warp * kCorrCols >= ncol) return;  // the whole warp
+  CorrSlot* sl = ring[wl];
+  const int cl = lane / 3, k = lane - 3 * cl;
+  const int base = 3 * cl;  // the column's first lane
+  const size_t col = warp * kCorrCols + cl;
+  const bool wood = n >= 3;
+  // a lane past the warp's columns shadows the warp's first column; it
+  // neither copies nor stores
+  const bool valid = cl < kCorrCols && col < ncol;
+  const size_t cc = valid ? col : warp * kCorrCols;
+  const bool live = valid && F.mask[cc] == 0;
+  const bool act = live && (k == 0 || wood);
+  const int cs = cl < kCorrCols ? cl : 0;  // the lane's column slot
+  const unsigned full = 0xffffffffu;
+  // true on every lane of this lane's column (inactive lanes agree)
+  auto all3 = [&](bool v) {
+    const unsigned bad = __ballot_sync(full, !v);
+    return ((bad >> base) & 7u) == 0u;
+  };
+  const float* LU = F.LU + cc * n * kLu32;
+  const float* Bm = F.B + cc * n * kBlk32;
+  const float* CP = F.CP + cc * n * kBlk32;
+  float* R = F.R + cc * n * kR32;
+  double* X = (k == 0 ? S.D : (k == 1 ? S.Z0 : S.Z1)) + cc * n * 5;
+
+  // ---- forward: y_i = LU_i^-1 (r_i - b_i y_(i-1)) ----
+  // the column's three lanes share the copies of its layer
+  auto fissue = [&](int i) {
+    if (live) {
+      CorrSlot& s = sl[i % kCorrRing];
+      for (int e = k; e < kLu32 / 4; e += 3)
+        cpa16(&s.f.lu[cs][4 * e], LU + i * kLu32 + 4 * e);
+      for (int e = k; e < kBlk32 / 4; e += 3)
+        cpa16(&s.f.b[cs][4 * e], Bm + i * kBlk32 + 4 * e);
+      for (int e = k; e < kR32 / 4; e += 3)
+        cpa16(&s.f.r[cs][4 * e], R + i * kR32 + 4 * e);
+    }
+  };
+#pragma unroll
+  for (int j = 0; j < kCorrRing - 1; ++j) {
+    if (j < n) fissue(j);
+    cpa_commit();
+  }
+  float y[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  for (int i = 0; i < n; ++i) {
+    if (i + kCorrRing - 1 < n) fissue(i + kCorrRing - 1);
+    cpa_commit();
+    cpa_wait<kCorrRing - 1>();
+    __syncwarp();
+    const CorrSlot& s = sl[i % kCorrRing];
+    if (act) {
+      const float* lu = s.f.lu[cs];
+      const float* b = s.f.b[cs];
+      float x[5];
+#pragma unroll
+      for (int r = 0; r < 5; ++r) x[r] = s.f.r[cs][k * 5 + r];
+      if (i > 0) {
+#pragma unroll
+        for (int r = 0; r < 5; ++r) {
+          float t = x[r];
+#pragma unroll
+          for (int q = 0; q < 5; ++q) t = fmaf(-b[r * 5 + q], y[q], t);
+          x[r] = t;
+        }
+      }
+      const int pk = __float_as_int(lu[30]);
+#pragma unroll
+      for (int rr = 0; rr < 5; ++rr) {
+        const int ip = (pk >> (3 * rr)) & 7;
+#pragma unroll
+        for (int q = rr + 1; q < 5; ++q) {
+          const bool sw = ip == q;
+          const float a = x[rr], c = x[q];
+          x[rr] = sw ? c : a;
+          x[q] = sw ? a : c;
+        }
+      }
+#pragma unroll
+      for (int rr = 1; rr < 5; ++rr)
+#pragma unroll
+        for (int jj = 0; jj < rr; ++jj)
+          x[rr] = fmaf(-lu[rr * 5 + jj], x[jj], x[rr]);
+#pragma unroll
+      for (int rr = 4; rr >= 0; --rr) {
+#pragma unroll
+        for (int jj = rr + 1; jj < 5; ++jj)
+          x[rr] = fmaf(-lu[rr * 5 + jj], x[jj], x[rr]);
+        x[rr] = x[rr] * lu[25 + rr];
+      }
+#pragma unroll
+      for (int r = 0; r < 5; ++r) {
+        R[i * kR32 + k * 5 + r] = x[r];  // y, for the way back
+        y[r] = x[r];
+      }
+    }
+    __syncwarp();  // the slot is read before it is refilled
+  }
+  cpa_wait<0>();
+  __syncwarp();
+
+  // ---- back: d_i = y_i - c'_i d_(i+1), x_i += d_i in FP64 ----
+  float dmax = 0.f;
+  bool fin = true;
+  if (act) {
+#pragma unroll
+    for (int r = 0; r < 5; ++r) {
+      X[(n - 1) * 5 + r] = X[(n - 1) * 5 + r] + (double)y[r];
+      fin = fin && vfinite32(y[r]);
+      dmax = fmaxf(dmax, fabsf(y[r]));
+    }
+  }
+  // step j of the way back is layer n - 2 - j
+  auto bissue = [&](int j) {
+    const int i = n - 2 - j;
+    CorrSlot& s = sl[j % kCorrRing];
+    if (live)
+      for (int e = k; e < kBlk32 / 4; e += 3)
+        cpa16(&s.g.cp[cs][4 * e], CP + i * kBlk32 + 4 * e);
+    if (act) {
+#pragma unroll
+      for (int r = 0; r < 5; ++r) {
+        cpa4(&s.g.y[lane][r], R + i * kR32 + k * 5 + r);
+        cpa8(&s.g.x[lane][r], X + i * 5 + r);
+      }
+    }
+  };
+#pragma unroll
+  for (int j = 0; j < kCorrRing - 1; ++j) {
+    if (j < n - 1) bissue(j);
+    cpa_commit();
+  }
+  for (int j = 0; j < n - 1; ++j) {
+    const int i = n - 2 - j;
+    if (j + kCorrRing - 1 < n - 1) bissue(j + kCorrRing - 1);
+    cpa_commit();
+    cpa_wait<kCorrRing - 1>();
+    __syncwarp();
+    const CorrSlot& s = sl[j % kCorrRing];
+    if (act) {
+      const float* cp = s.g.cp[cs];
+      float t[5];
+#pragma unroll
+      for (int r = 0; r < 5; ++r) {
+        float u = s.g.y[lane][r];
+#pragma unroll
+        for (int q = 0; q < 5; ++q) u = fmaf(-cp[r * 5 + q], y[q], u);
+        t[r] = u;
+      }
+#pragma unroll
+      for (int r = 0; r < 5; ++r) {
+        y[r] = t[r];
+        X[i * 5 + r] = s.g.x[lane][r] + (double)t[r];
+        fin = fin && vfinite32(t[r]);
+        dmax = fmaxf(dmax, fabsf(t[r]));
+      }
+    }
+    __syncwarp();
+  }
+  cpa_wait<0>();
+
+  float* st = F.stat + cc * 6;
+  if (!last) {
+    const bool colok = all3(!act || fin);
+    if (act) st[k] = dmax;
+    if (live && k == 0 && !colok) F.mask[cc] = 1;
+    return;
+  }
+  // convergence of every right-hand side of the column
+  bool cv = true;
+  if (act) {
+    const float dp = st[k];
+    const float rho = dp > 0.f ? fminf(dmax / dp, 1.f) : 0.f;
+    cv = fin && dmax * rho <= 0x1p-44f * st[3 + k];
+  }
+  // every ballot runs on all 32 lanes: evaluate before combining
+  const bool cv_all = all3(cv);
+  bool conv = live && cv_all;
+  bool f = true;
+  if (conv && wood) {
+    // the column's three lanes; x of every lane is stored
+    const unsigned cm = 7u << base;
+    __syncwarp(cm);
+    double* D = S.D + cc * n * 5;
+    const double* Z0 = S.Z0 + cc * n * 5;
+    const double* Z1 = S.Z1 + cc * n * 5;
+    const double dtc = p.w2 * p.dt[blockIdx.y];
+    VicK K0 = vic_krows(Bk, n, 0), K1 = vic_krows(Bk, n, n - 1);
+    const double k0 = -K0.t0 / dtc, k1 = -K1.t1 / dtc;
+    const int a0 = 2, a1 = n - 3;
+    const double m00 = 1. + k0 * Z0[a0 * 5], m01 = k0 * Z1[a0 * 5];
+    const double m10 = k1 * Z0[a1 * 5], m11 = 1. + k1 * Z1[a1 * 5];
+    const double r0 = k0 * D[a0 * 5], r1 = k1 * D[a1 * 5];
+    const double det = m00 * m11 - m01 * m10;
+    const double al0 = (m11 * r0 - m01 * r1) / det;
+    const double al1 = (m00 * r1 - m10 * r0) / det;
+    __syncwarp(cm);
+    for (int e = k; e < 5 * n; e += 3) {
+      double d = D[e];
+      d -= Z0[e] * al0;
+      d -= Z1[e] * al1;
+      D[e] = d;
+      f = f && vfinite(d);
+    }
+  }
+  const bool f_all = all3(f);
+  conv = conv && f_all;
+  if (valid && k == 0) F.mask[cc] = conv ? 0 : 1;
+}
+
+// the FP64 residual r = b - (B_i x_(i-1) + A_i x_i + C_i x_(i+1)) of every
+// cell and right-hand side (one thread per cell), from the FP64 blocks (the
+// FP32-assembled values, exact) and x in D, Z0, Z1; rounded to FP32 into R
+__global__ void __launch_bounds__(kThreads)
+    vic_residual_kernel(const BlockDev* __restrict__ tab, StageParams p) {
+  const BlockDev& B = tab[blockIdx.y];
+  if (!B.implicit || !B.implicit_f32) return;
+  const VicScratch S = vic_scratch(B);
+  const int n = B.nc1 - 2 * B.ng;
+  const VicScratch32 F = vic_scratch32(B, S, n);
+  const double dtc = p.w2 * p.dt[blockIdx.y];
+  const double rdtc = 1. / dtc;
+  const int nrhs = n >= 3 ? 3 : 1;
+  for (size_t cell = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+       cell < S.cells; cell += (size_t)gridDim.x * blockDim.x) {
+    const size_t col = cell / n;
+    const int i = (int)(cell - col * n);
+    if (F.mask[col]) continue;
+    const double* a = S.A + cell * 25;
+    const double* bl = S.B + cell * 25;
+    const double* c = S.C + cell * 25;
+    for (int k = 0; k < nrhs; ++k) {
+      const double* x = (k == 0 ? S.D : (k == 1 ? S.Z0 : S.Z1)) + cell * 5;
+      double t[5];
+#pragma unroll
+      for (int r = 0; r < 5; ++r)
+        t[r] = k == 0 ? vdiv(S.du[(size_t)r * S.cells + cell], dtc, rdtc)
+                      : ((r == 4 && i == (k == 1 ? 0 : n - 1)) ? 1. : 0.);
+#pragma unroll
+      for (int q = 0; q < 5; ++q) {
+        const double xc = x[q];
+#pragma unroll
+        for (int r = 0; r < 5; ++r) t[r] = fma(-a[r * 5 + q], xc, t[r]);
+      }
+      if (i > 0) {
+#pragma unroll
+        for (int q = 0; q < 5; ++q) {
+          const double xl = x[q - 5];
+#pragma unroll
+          for (int r = 0; r < 5; ++r) t[r] = fma(-bl[r * 5 + q], xl, t[r]);
+        }
+      }
+      if (i < n - 1) {
+#pragma unroll
+        for (int q = 0; q < 5; ++q) {
+          const double xu = x[q + 5];
+#pragma unroll
+          for (int r = 0; r < 5; ++r) t[r] = fma(-c[r * 5 + q], xu, t[r]);
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < 5; ++r) F.R[cell * kR32 + k * 5 + r] = (float)t[r];
+    }
+  }
 }
 
 // NL lanes per column: 32 (a warp per column, kVicWarps per CTA: the serial

@@ -43,6 +43,9 @@ class Ensemble:
         self.dtype = dtype
         self.batch = Batch(schemes[0], [block_of(m) for m in self.members],
                            self.device, dtype)
+        k = min(m.solve_corrections() for m in self.members)
+        if k != 2:
+            self.batch.set_solve(k)
         self.nstage = len(schemes[0]["wght"])
         self.graphs = graphs
         # retry on the device (MeshBlockImpl::apply_redo per member): each

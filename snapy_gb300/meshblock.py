@@ -211,6 +211,8 @@ class MeshBlock:
     def batch(self) -> Batch:
         if self._batch is None:
             self._batch = Batch(self._scheme, [self._block], self.device, self.dtype)
+            if self.options.solve_corrections() != 2:
+                self._batch.set_solve(self.options.solve_corrections())
             for d in sorted(self._step_dims):
                 self._batch.request_step_field(0, d)
         return self._batch

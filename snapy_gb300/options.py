@@ -358,7 +358,8 @@ class IntegratorOptions:
                    {"type", "cfl", "tlim", "nlim", "ncycle_out", "max-redo",
                     "max_redo", "implicit-scheme", "implicit-precision",
                     "implicit-fallback-fp64", "execution", "execution-strict",
-                    "restart", "autotune"})
+                    "restart", "autotune", "implicit-solve",
+                    "implicit-corrections"})
         op.type = str(_get(node, "type", op.type))
         op.cfl = float(_get(node, "cfl", op.cfl))
         op.tlim = float(_get(node, "tlim", op.tlim))
@@ -378,6 +379,11 @@ _BC_NAMES = {"reflecting", "periodic", "extrapolation", "outflow", "custom",
 class MeshBlockOptions:
     """The deck of one block (reference MeshBlockOptionsImpl)."""
 
+    def solve_corrections(self) -> int:
+        """sg_set_solve's argument for this deck: 0 for the direct FP64
+        solve, else the refined solve's corrections."""
+        return 0 if self.implicit_solve == "direct" else self.implicit_corrections
+
     def __init__(self):
         self._coord = CoordinateOptions()
         self._hydro = HydroOptions()
@@ -388,6 +394,12 @@ class MeshBlockOptions:
         # integration/autotune (no counterpart in the reference): time the
         # stage's tile widths and finish forms on the block at initialize
         self.autotune = True
+        # integration/implicit-solve (no counterpart in the reference): the
+        # solve of implicit-precision float32 blocks, "refined" (FP32 sweeps
+        # corrected with FP64 residuals to the FP64 solution) or "direct"
+        # (the FP64 solve of every column)
+        self.implicit_solve = "refined"
+        self.implicit_corrections = 2  # FP64-residual corrections (1 to 3)
         self.verbose = False
         self.basename = ""
         self.problem: Dict[str, Any] = {}
@@ -437,6 +449,14 @@ class MeshBlockOptions:
         op.execution = str(intg.get("execution", "auto"))
         op.execution_strict = bool(intg.get("execution-strict", False))
         op.autotune = bool(intg.get("autotune", True))
+        op.implicit_solve = str(intg.get("implicit-solve", "refined"))
+        if op.implicit_solve not in ("refined", "direct"):
+            raise DeckError("integration/implicit-solve must be refined or "
+                            f"direct, got '{op.implicit_solve}'")
+        op.implicit_corrections = int(intg.get("implicit-corrections", 2))
+        if not 1 <= op.implicit_corrections <= 3:
+            raise DeckError("integration/implicit-corrections must be 1 to 3, "
+                            f"got {op.implicit_corrections}")
         if op.execution not in ("auto", "eager", "cuda-graph"):
             raise DeckError("integration/execution must be auto, eager or "
                             f"cuda-graph, got '{op.execution}'")

@@ -73,6 +73,9 @@ def footprint(options: MeshBlockOptions, dtype: torch.dtype) -> int:
     b = 3 * 5 * nc * s
     if h.icorr is not None:
         b += icells * 100 * 8
+        if h.precision == "float32" and h.icorr.precision == "float32":
+            # the refined solve's FP32 part
+            b += (icells * 160 + (icells // c.nx1) * 7) * 4 + 16
     if c.nx3 > 1:
         b += 5 * icells * s
     b += 8 * (5 * c.nc1 + 1) + 16 * (c.nc1 + 1)
@@ -149,6 +152,9 @@ class _Handle:
                                              sl.scratch.numel() * 8),
                            "sg_bind_scratch")
         _lib.check(L.sg_set_current(h, 0), "sg_set_current")
+        k = min(sl.req.options.solve_corrections() for sl in slots)
+        if k != 2:
+            _lib.check(L.sg_set_solve(h, k), "sg_set_solve")
         self.dt = torch.zeros(n, dtype=torch.float64, device=device)
         self.redo = torch.zeros(n, dtype=torch.int32, device=device)
         self.flags = torch.zeros(n, dtype=torch.int32, device=device)

@@ -1,0 +1,81 @@
+"""The refined implicit solve of implicit-precision float32 blocks (FP32
+block-Thomas sweeps corrected with FP64 residuals) against the direct FP64
+solve of the same FP32-assembled system (sg_set_solve(h, 0)): the solution
+of every column to FP64 roundoff with one, two and three corrections, few
+columns left to the direct solve (the implicit.fp64_columns count), and the
+whole FP32 run within the FP32 bar of the FP64 oracle."""
+import numpy as np
+import pytest
+import torch
+
+import snapy_gb300 as sg
+from snapy_gb300 import _lib, problems
+
+pytestmark = pytest.mark.gpu
+
+
+def straka_fp32(nx1=48, nx2=40):
+    opts = sg.MeshBlockOptions.from_yaml("snapy_gb300/decks/straka.yaml")
+    c = opts.coord()
+    c.nx1, c.nx2, c.x1max, c.x2max = nx1, nx2, nx1 * 50.0, nx2 * 50.0
+    opts.hydro().precision = "float32"
+    opts.hydro().icorr.precision = "float32"
+    opts.execution = "eager"
+    opts.autotune = False
+    return opts
+
+
+def one_stage(cuda, opts, w, corrections):
+    """One stage; the solution D (du / dt_corr after the Woodbury step) of
+    every column, and the columns the refined solve left to FP64."""
+    blk = sg.MeshBlock(opts).to(cuda)
+    vars = {"hydro_w": w.to(cuda)}
+    blk.initialize(vars)
+    L = _lib.load()
+    blk.batch.set_solve(corrections)
+    dt = blk.max_time_step(vars)
+    blk.forward(vars, dt, 0)
+    torch.cuda.synchronize()
+    c = opts.coord()
+    cells = c.nx1 * c.nx2
+    D = blk.batch.scratch[0][85 * cells:90 * cells].clone()
+    return D, blk.batch.solve_fallbacks()[0]
+
+
+@pytest.mark.parametrize("corrections", [1, 2, 3])
+def test_refined_solution_is_the_direct_one(cuda, corrections):
+    opts = straka_fp32()
+    w = problems.straka(opts, "cpu", xc=1000.0, zc=1200.0, xr=800.0, zr=600.0)
+    Dr, fellback = one_stage(cuda, opts, w, corrections)
+    Dd, none = one_stage(cuda, opts, w, 0)
+    rel = (torch.linalg.norm(Dr - Dd) / torch.linalg.norm(Dd)).item()
+    ncol = opts.coord().nx2
+    print(f"\n{corrections} corrections vs the direct FP64 solve: rel L2 "
+          f"{rel:.2e}, {fellback} of {ncol} columns left to the direct solve")
+    assert none == 0
+    assert 0 <= fellback <= ncol
+    assert rel <= 1e-13
+    if corrections >= 2:
+        assert fellback <= ncol // 20
+
+
+def test_refined_run_against_fp64_oracle(oracle, cuda):
+    opts = straka_fp32()
+    w = problems.straka(opts, "cpu", xc=1000.0, zc=1200.0, xr=800.0, zr=600.0)
+    blk = sg.MeshBlock(opts).to(cuda)
+    vars = {"hydro_w": w.to(cuda)}
+    blk.initialize(vars)
+    ob = oracle.block_from_options(opts)
+    u = ob.initialize(w.numpy())
+    for _ in range(10):
+        dt = blk.max_time_step(vars)
+        blk.step(vars, dt)
+        assert blk.check_redo(vars) == 0
+        ob.step(u, dt)
+    got = blk.total_u(vars).double().cpu().numpy()
+    err = [np.linalg.norm(got[v] - u[v]) / max(np.linalg.norm(u[v]), 1e-300)
+           for v in range(5)]
+    print("\nFP32 + refined solve vs FP64 oracle, rel L2 per field:",
+          np.array2string(np.array(err), precision=2))
+    assert max(err) <= 1e-5
+    assert blk.batch.solve_fallbacks()[0] <= 10 * 3 * opts.coord().nx2 // 20

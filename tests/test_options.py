@@ -115,3 +115,20 @@ def test_no_cpu_path():
     opts = options(config("sod.yaml"))
     with pytest.raises(RuntimeError, match="CUDA"):
         sg.MeshBlock(opts).to("cpu")
+
+
+def test_implicit_solve_keys():
+    """integration.implicit-solve and implicit-corrections choose the solve
+    of float32-assembled implicit blocks: sg_set_solve's argument."""
+    cfg = copy.deepcopy(config("straka.yaml"))
+    assert options(cfg).solve_corrections() == 2
+    cfg["integration"]["implicit-corrections"] = 3
+    assert options(cfg).solve_corrections() == 3
+    cfg["integration"]["implicit-solve"] = "direct"
+    assert options(cfg).solve_corrections() == 0
+    for key, bad in (("implicit-solve", "float32"), ("implicit-corrections", 0),
+                     ("implicit-corrections", 4)):
+        cfg = copy.deepcopy(config("straka.yaml"))
+        cfg["integration"][key] = bad
+        with pytest.raises(DeckError, match=key):
+            options(cfg)
