@@ -161,17 +161,55 @@ def config_of(opts, workload, args, nranks):
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of a
 # dominant kernel, from one ncu capture of the same workload and kernel
-# build: profiles/straka512x128_fp64_launches_and_kernels.md and
-# profiles/ensemble64_fp32_vic_launches_and_kernels.md
+# build: profiles/straka512x128_fp64_launches_and_kernels.md,
+# profiles/ensemble64_fp32_vic_launches_and_kernels.md and
+# profiles/refined_solve_ensemble64_and_straka512x128_fp32.md
 NCU_TRAFFIC = {
     ("straka", "float64", "vic_solve_kernel"): 42.009600e6 + 0.149248e6,
     ("ensemble", "float32", "vic_solve_kernel"): 1.288739e9 + 0.550966e9,
+    # the refined phase: vic_solve32_kernel, 2 x (vic_residual_kernel,
+    # vic_correct32_kernel), vic_solve_kernel (masked columns only)
+    ("ensemble", "float32", "refined"): 6.2219e9,
+    ("straka", "float32", "refined"): 0.2025e9,
 }
 
 
 def ncu_traffic(workload, precision, kernel):
     """The captured DRAM bytes per launch, or None for an uncaptured case."""
     return NCU_TRAFFIC.get((workload, precision, kernel))
+
+
+FP64_ISSUE = ("FP64 issue rate (one FP64 warp instruction per SM sub-partition "
+              "per 64 cycles)")
+
+
+def refined(opts):
+    """True when the deck's implicit blocks take the refined solve."""
+    ic = opts.hydro().icorr
+    return bool(ic is not None and opts.hydro().precision == "float32"
+                and ic.precision == "float32" and opts.solve_corrections() > 0)
+
+
+def solve_phase(opts):
+    """The implicit solve phase timed as vic_solve_kernel (the events
+    between the assembly and the finish): what runs in it, its algorithmic
+    bytes per interior cell and what bounds it."""
+    if not refined(opts):
+        return ("vic_solve_kernel", 600 + 40 + 200 + 120 + 200 + 120 + 120,
+                FP64_ISSUE)
+    k = opts.solve_corrections()
+    # the FP32 sweep: A, B, C (300) and du (40) in; factors (128), c' (112),
+    # y (60) and x (120) out; back: c' and y in
+    first = 300 + 40 + 128 + 112 + 60 + 120 + 112 + 60
+    # a residual: FP64 blocks (600), x (120), du (40) in; r (60) out
+    residual = 600 + 120 + 40 + 60
+    # a correction: factors, b, r in and y out; back: c', y, x in, x out
+    correct = 128 + 112 + 64 + 60 + 112 + 60 + 120 + 120
+    return (f"refined solve phase: vic_solve32_kernel, then {k} x "
+            "(vic_residual_kernel, vic_correct32_kernel)",
+            first + k * (residual + correct),
+            "the FP64 residuals (FP64 issue rate) and the corrections' "
+            "per-layer latency")
 
 
 def peaks():
@@ -412,7 +450,7 @@ def run_native(args):
         "stage_kernel": ((5 * s_bytes + 40) if implicit else
                          5 * s_bytes * (2 + 3 + 3) / 3) * cells,
         "vic_assemble_kernel": (5 * s_bytes + 40 + 40 + 600) * cells,
-        "vic_solve_kernel": (600 + 40 + 200 + 120 + 200 + 120 + 120) * cells,
+        "vic_solve_kernel": solve_phase(opts)[1] * cells,
         "vic_finish_kernel": (120 + 15 * s_bytes) * cells,
         "ghost_kernel": 2 * 5 * s_bytes * ghost_cells,
     }
@@ -461,14 +499,19 @@ def run_native(args):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak,
                          "peak_kind": peak_kind,
-                         "traffic": ncu_traffic(args.workload,
-                                                opts.hydro().precision, dom),
+                         "traffic": ncu_traffic(
+                             args.workload, opts.hydro().precision,
+                             "refined" if dom == "vic_solve_kernel"
+                             and refined(opts) else dom),
                          "kernel": dom,
+                         "runs": solve_phase(opts)[0]
+                                 if dom == "vic_solve_kernel" else dom,
                          "bytes_per_launch": per_launch[dom],
                          "mean_launch_us": dom_ms / dom_n * 1e3,
-                         "limiter": "FP64 issue rate (one FP64 warp "
-                                    "instruction per SM per 16 cycles)"
-                                    if blk.dtype == torch.float64 else None},
+                         "limiter": solve_phase(opts)[2]
+                                    if dom == "vic_solve_kernel" else
+                                    FP64_ISSUE if blk.dtype == torch.float64
+                                    else None},
             "kernels": kernels,
             "cpu_baseline": cb,
             "clocks": clk.summary(),
@@ -593,7 +636,7 @@ def run_ensemble(args):
     per_launch = {
         "stage_kernel": (5 * s_bytes + 40) * cells,
         "vic_assemble_kernel": (5 * s_bytes + 40 + 40 + 600) * cells,
-        "vic_solve_kernel": (600 + 40 + 200 + 120 + 200 + 120 + 120) * cells,
+        "vic_solve_kernel": solve_phase(members[0][0])[1] * cells,
         "vic_finish_kernel": (120 + 15 * s_bytes) * cells,
         "ghost_kernel": 0,
     }
@@ -673,12 +716,17 @@ def run_ensemble(args):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak,
                          "peak_kind": peak_kind,
-                         "traffic": ncu_traffic("ensemble", precision, dom),
+                         "traffic": ncu_traffic(
+                             "ensemble", precision,
+                             "refined" if dom == "vic_solve_kernel"
+                             and refined(members[0][0]) else dom),
                          "kernel": dom, "bytes_per_launch": per_launch[dom],
+                         "runs": solve_phase(members[0][0])[0]
+                                 if dom == "vic_solve_kernel" else dom,
                          "mean_launch_us": dom_ms / dom_n * 1e3,
-                         "limiter": "FP64 issue rate (one FP64 warp "
-                                    "instruction per SM sub-partition per 64 "
-                                    "cycles)"},
+                         "limiter": solve_phase(members[0][0])[2]
+                                    if dom == "vic_solve_kernel" else
+                                    FP64_ISSUE},
             "kernels": kernels,
             "cpu_baseline": cb,
             "clocks": clk.summary(),
@@ -803,7 +851,7 @@ def run_serving(args):
     cells_all = sum(r.cells for r in reqs)
     per_cell = {"stage_kernel": 5 * 4 + 40, "x3_kernel": 5 * 4 * 2,
                 "vic_assemble_kernel": 5 * 4 + 40 + 40 + 600,
-                "vic_solve_kernel": 600 + 40 + 200 + 120 + 200 + 120 + 120,
+                "vic_solve_kernel": solve_phase(reqs[0].options)[1],
                 "vic_finish_kernel": 120 + 15 * 4, "ghost_kernel": 0}
     # a launch covers the running set; its cells vary, so the achieved
     # bandwidth is the algorithmic bytes of all cell-steps over the kernel time
@@ -862,9 +910,12 @@ def run_serving(args):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak,
                          "peak_kind": peak_kind, "traffic": None, "kernel": dom,
+                         "runs": solve_phase(reqs[0].options)[0]
+                                 if dom == "vic_solve_kernel" else dom,
                          "mean_launch_us": kms[dom][0] / kms[dom][1] * 1e3,
-                         "limiter": "FP64 issue rate (one FP64 warp instruction "
-                                    "per SM sub-partition per 64 cycles)"},
+                         "limiter": solve_phase(reqs[0].options)[2]
+                                    if dom == "vic_solve_kernel" else
+                                    FP64_ISSUE},
             "kernels": {k: {"launches": n, "mean_us": ms / n * 1e3,
                             "share": ms / sum(v[0] for v in kms.values())}
                         for k, (ms, n) in kms.items()},

@@ -1412,12 +1412,13 @@ __global__ void __launch_bounds__(32 * kCorrWarps)
   // every ballot runs on all 32 lanes: evaluate before combining
   const bool cv_all = all3(cv);
   bool conv = live && cv_all;
-  bool f = true;
-  if (conv && wood) {
-    // the column's three lanes; x of every lane is stored
-    const unsigned cm = 7u << base;
-    __syncwarp(cm);
-    double* D = S.D + cc * n * 5;
+  // the Woodbury step of each converged column: its first lane forms the
+  // two weights from D, Z0, Z1 at layers 2 and n - 3, then the whole warp
+  // updates the column's 5 n values of D, coalesced, one column at a time
+  __syncwarp();  // every lane's x is stored
+  double al0 = 0., al1 = 0.;
+  if (conv && wood && k == 0) {
+    const double* D = S.D + cc * n * 5;
     const double* Z0 = S.Z0 + cc * n * 5;
     const double* Z1 = S.Z1 + cc * n * 5;
     const double dtc = p.w2 * p.dt[blockIdx.y];
@@ -1428,20 +1429,32 @@ __global__ void __launch_bounds__(32 * kCorrWarps)
     const double m10 = k1 * Z0[a1 * 5], m11 = 1. + k1 * Z1[a1 * 5];
     const double r0 = k0 * D[a0 * 5], r1 = k1 * D[a1 * 5];
     const double det = m00 * m11 - m01 * m10;
-    const double al0 = (m11 * r0 - m01 * r1) / det;
-    const double al1 = (m00 * r1 - m10 * r0) / det;
-    __syncwarp(cm);
-    for (int e = k; e < 5 * n; e += 3) {
+    al0 = (m11 * r0 - m01 * r1) / det;
+    al1 = (m00 * r1 - m10 * r0) / det;
+  }
+  const unsigned wb = __ballot_sync(full, conv && wood && k == 0);
+  __syncwarp();  // the weights are read before D changes
+  bool bad = false;  // on a column's first lane: its D is not finite
+  for (int c = 0; c < kCorrCols; ++c) {
+    if (!((wb >> (3 * c)) & 1u)) continue;  // uniform over the warp
+    const double w0 = __shfl_sync(full, al0, 3 * c);
+    const double w1 = __shfl_sync(full, al1, 3 * c);
+    const size_t cw = warp * kCorrCols + c;
+    double* D = S.D + cw * n * 5;
+    const double* Z0 = S.Z0 + cw * n * 5;
+    const double* Z1 = S.Z1 + cw * n * 5;
+    bool f = true;
+    for (int e = lane; e < 5 * n; e += 32) {
       double d = D[e];
-      d -= Z0[e] * al0;
-      d -= Z1[e] * al1;
+      d -= Z0[e] * w0;
+      d -= Z1[e] * w1;
       D[e] = d;
       f = f && vfinite(d);
     }
+    const bool f_all = __all_sync(full, f);
+    if (lane == 3 * c) bad = !f_all;
   }
-  const bool f_all = all3(f);
-  conv = conv && f_all;
-  if (valid && k == 0) F.mask[cc] = conv ? 0 : 1;
+  if (valid && k == 0) F.mask[cc] = (conv && !bad) ? 0 : 1;
 }
 
 // the FP64 residual r = b - (B_i x_(i-1) + A_i x_i + C_i x_(i+1)) of every
