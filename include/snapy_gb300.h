@@ -106,6 +106,10 @@ typedef struct sg_block_desc {
    * assembles the implicit blocks in FP32 (SG_F32 storage only); the
    * block-tridiagonal solve runs in FP64 either way */
   int32_t implicit_precision;
+  /* scalar/nvar: passive scalars transported by the stage's mass flux
+   * (ScalarImpl, src/scalar/scalar.cpp:90-211); 0 for none.  Built for 1-D
+   * and 2-D blocks without the implicit solve */
+  int32_t nscalar;
 } sg_block_desc;
 
 int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
@@ -114,6 +118,10 @@ int sg_destroy(sg_handle* h);
 /* three device buffers per block, each (5, nc3, nc2, nc1) of the dtype; the
  * current state must be in buffer `current` (0..2) */
 int sg_bind(sg_handle* h, int32_t block, void* buf0, void* buf1, void* buf2);
+/* a block's three scalar buffers, each (nscalar, nc3, nc2, nc1) of the
+ * dtype: the tracer densities s (scalar_s), rotated with the state buffers
+ * (MeshBlockImpl's scalar StateStore rows, src/mesh/state_store.hpp) */
+int sg_bind_scalars(sg_handle* h, int32_t block, void* s0, void* s1, void* s2);
 /* the FP64 scratch of a block's vertical implicit solve (0 bytes without
  * one): the caller allocates it, 16-byte aligned, and binds it before the
  * first sg_stage (ImplicitHydroImpl::prepare, src/implicit/implicit_hydro.hpp) */
@@ -179,7 +187,8 @@ enum {
   SG_KERNEL_VIC_FINISH = 3,   /* implicit solve: redistribution, update */
   SG_KERNEL_GHOST = 4,        /* ghost fill of the new state */
   SG_KERNEL_X3 = 5,           /* x3 faces of 3-D blocks */
-  SG_NKERNEL = 6
+  SG_KERNEL_SCALAR = 6,       /* passive scalars: face fluxes and update */
+  SG_NKERNEL = 7
 };
 int sg_set_timing(sg_handle* h, int32_t on);
 int sg_kernel_times(sg_handle* h, double* ms, int64_t* launches);

@@ -63,6 +63,9 @@ class OgBlock(ctypes.Structure):
         ("x2v", _dp),
         ("step", _dp * 3),
         ("total", _dp * 3),
+        ("nscalar", ctypes.c_int),
+        ("scalar", _dp),
+        ("scalar0", _dp),
     ]
 
 
@@ -99,6 +102,7 @@ def lib():
         L.og_cons2prim.argtypes = [bp, _dp, _dp]
         L.og_prim2cons.argtypes = [bp, _dp, _dp]
         L.og_apply_bc.argtypes = [bp, _dp, ctypes.c_int]
+        L.og_scalar_bc.argtypes = [bp, _dp]
         L.og_flux.argtypes = [bp, _dp, ctypes.c_int, _dp]
         L.og_stage.argtypes = [bp, _dp, _dp, ctypes.c_double, ctypes.c_int]
         L.og_max_dt.restype = ctypes.c_double
@@ -264,6 +268,20 @@ class Block:
 
     def step_field(self, dim: int) -> np.ndarray:
         return self._steps[dim - 1]
+
+    # -- passive scalars (ScalarImpl, src/scalar/scalar.cpp:90-211) -----------
+    def set_scalars(self, s: np.ndarray) -> np.ndarray:
+        """Transport the tracer densities s (nscalar, nc3, nc2, nc1) with
+        every stage from here on; returns the array the stages advance."""
+        if self.b.implicit_scheme:
+            raise ValueError("the oracle transports scalars on explicit "
+                             "blocks only")
+        self._s = np.ascontiguousarray(s, dtype=np.float64).copy()
+        self._s0 = np.zeros_like(self._s)
+        self.b.nscalar = self._s.shape[0]
+        self.b.scalar, self.b.scalar0 = ptr(self._s), ptr(self._s0)
+        lib().og_scalar_bc(ctypes.byref(self.b), ptr(self._s))
+        return self._s
 
     def keep_totals(self, dim: int) -> np.ndarray:
         """The buffer each stage copies its register total T_dim into."""

@@ -1071,6 +1071,129 @@ static void step_recursion(const og_block* b, int d, const double* T,
 }
 #undef CELL
 
+/* the passive scalars' transport tendency ds = -dt div F_s
+ * (ScalarImpl::forward, src/scalar/scalar.cpp:90-211, for the dry case with
+ * neither limiter nor upper bound):
+ *   - the face mixing ratio r = s_f / rho_f of each side, s_f and rho_f the
+ *     scale-invariant reconstruction of the tracer density and of the total
+ *     dry density of the stage input with the hydro's scheme for every row,
+ *     floored at 0 (ReconstructImpl::forward without a hydro parent,
+ *     src/recon/reconstruct.cpp:258-262), the donor cell's r where rho_f
+ *     is not positive (scalar.cpp:100-104);
+ *   - the upwind flux F_s = F_m r of the side F_m > 0 selects (the left
+ *     state; else the right), F_m the hydro register's mass row of the face
+ *     (riemann.cpp:164-170, scalar.cpp:106-121);
+ *   - zero on the reflecting faces (boundary.prescribed, scalar.cpp:163-169);
+ *   - the area-weighted divergence, as the hydro's.
+ * fm[d - 1]: the mass flux along d (face f below cell f), or NULL */
+static void scalar_tendency(const og_block* b, const double* u,
+                            double* const* fm, double dt, const double* s,
+                            double* ds) {
+  const size_t nc = ncell(b);
+  const int ns = b->nscalar, ng = b->ng;
+  const int n[3] = {b->nc1, b->nc2, b->nc3};
+  const int weno = 1; /* the hydro's scheme: weno5 for density rows */
+  double* fs[3] = {NULL, NULL, NULL};
+  int lo[3], hi[3]; /* interior cells, inclusive */
+  for (int a = 0; a < 3; ++a) {
+    lo[a] = n[a] > 1 ? ng : 0;
+    hi[a] = n[a] > 1 ? n[a] - ng - 1 : 0;
+  }
+  for (int d = 1; d <= 3; ++d) {
+    if (!fm[d - 1]) continue;
+    fs[d - 1] = (double*)calloc((size_t)ns * nc, sizeof(double));
+    const size_t st = dir_stride(b, d);
+    int flo[3], fhi[3];
+    for (int a = 0; a < 3; ++a) {
+      flo[a] = lo[a];
+      fhi[a] = hi[a];
+    }
+    fhi[d - 1] += 1; /* the faces of the interior cells, both ends */
+    for (int k = flo[2]; k <= fhi[2]; ++k)
+      for (int j = flo[1]; j <= fhi[1]; ++j)
+        for (int i = flo[0]; i <= fhi[0]; ++i) {
+          const size_t q = ((size_t)k * n[1] + j) * n[0] + i;
+          const int f = d == 1 ? i : d == 2 ? j : k;
+          const int wall = (f == ng && b->bc[2 * (d - 1)] == OG_BC_REFLECTING) ||
+                           (f == n[d - 1] - ng &&
+                            b->bc[2 * (d - 1) + 1] == OG_BC_REFLECTING);
+          const double F = fm[d - 1][q];
+          /* the side F > 0 selects: ILT (cp, cells f-3..f+1, donor f-1);
+           * else IRT (cm, cells f-2..f+2, donor f) */
+          const int left = F > 0.;
+          const size_t c0 = q - (size_t)(left ? 3 : 2) * st;
+          const size_t donor = left ? q - st : q;
+          double rs[5];
+          for (int m = 0; m < 5; ++m) rs[m] = u[OG_IDN * nc + c0 + m * st];
+          double rf = weno5_point(rs, 1, left ? g_weno5_cp : g_weno5_cm, 1);
+          (void)weno;
+          if (rf < 0.) rf = 0.;
+          for (int v = 0; v < ns; ++v) {
+            double ss[5];
+            for (int m = 0; m < 5; ++m) ss[m] = s[v * nc + c0 + m * st];
+            double sf = weno5_point(ss, 1, left ? g_weno5_cp : g_weno5_cm, 1);
+            if (sf < 0.) sf = 0.;
+            const double r = rf > 0. ? sf / rf
+                                     : s[v * nc + donor] / u[OG_IDN * nc + donor];
+            fs[d - 1][v * nc + q] = wall ? 0. : F * r;
+          }
+        }
+  }
+  const double a1 = b->dx3 * b->dx2, a2 = b->dx3 * b->dx1;
+  const double a3 = b->dx2 * b->dx1;
+  const double vol = b->dx3 * (b->dx2 * b->dx1);
+  const double mdt = -dt;
+  memset(ds, 0, sizeof(double) * ns * nc);
+  for (int v = 0; v < ns; ++v)
+    for (int k = lo[2]; k <= hi[2]; ++k)
+      for (int j = lo[1]; j <= hi[1]; ++j)
+        for (int i = lo[0]; i <= hi[0]; ++i) {
+          const size_t q = v * nc + ((size_t)k * n[1] + j) * n[0] + i;
+          double dv = 0.;
+          if (fs[0]) dv = a1 * fs[0][q + 1] - a1 * fs[0][q];
+          if (fs[1]) dv = dv + (a2 * fs[1][q + n[0]] - a2 * fs[1][q]);
+          if (fs[2])
+            dv = dv + (a3 * fs[2][q + (size_t)n[0] * n[1]] - a3 * fs[2][q]);
+          ds[q] = mdt * (dv / vol);
+        }
+  for (int d = 0; d < 3; ++d) free(fs[d]);
+}
+
+/* kScalar boundary functions (bc_func.cpp:10-70): the hydro's, with no
+ * sign flip */
+void og_scalar_bc(const og_block* b, double* s) {
+  og_block sb = *b;
+  sb.nvar = b->nscalar;
+  for (int f = 0; f < 6; ++f) {
+    const int d = 1 + f / 2, side = f % 2, kind = b->bc[f];
+    const int nd = dir_size(b, d), ng = b->ng;
+    if (nd == 1 || kind == OG_BC_NONE) continue;
+    const size_t st = dir_stride(b, d), nc = ncell(b);
+    const int n1 = b->nc1, n2 = b->nc2, n3 = b->nc3;
+    const int la = d == 1 ? n2 : n1, lb = d == 3 ? n2 : n3;
+    for (int v = 0; v < sb.nvar; ++v)
+      for (int bi = 0; bi < lb; ++bi)
+        for (int a = 0; a < la; ++a) {
+          size_t base;
+          if (d == 1) base = ((size_t)bi * n2 + a) * n1;
+          else if (d == 2) base = (size_t)bi * n2 * n1 + a;
+          else base = (size_t)bi * n1 + a;
+          double* line = s + v * nc + base;
+          for (int g = 0; g < ng; ++g) {
+            const int dst = side ? nd - ng + g : g;
+            int src;
+            if (kind == OG_BC_REFLECTING)
+              src = side ? nd - ng - 1 - g : 2 * ng - 1 - g;
+            else if (kind == OG_BC_PERIODIC)
+              src = side ? ng + g : nd - 2 * ng + g;
+            else
+              src = side ? nd - ng - 1 : ng;
+            line[dst * st] = line[src * st];
+          }
+        }
+  }
+}
+
 void og_stage(const og_block* b, double* u, double* u0, double dt, int stage) {
 #ifdef _OPENMP
   if (b->nthreads > 0) omp_set_num_threads(b->nthreads);
@@ -1084,11 +1207,23 @@ void og_stage(const og_block* b, double* u, double* u0, double dt, int stage) {
   /* the register totals where a step field or the totals are asked for */
   double* T[3] = {NULL, NULL, NULL};
   const int active[3] = {b->nc1 > 1, b->nc2 > 1, b->nc3 > 1};
+  const int ns = b->scalar ? b->nscalar : 0;
   for (int d = 0; d < 3; ++d)
-    if (active[d] && (b->step[d] || b->total[d]))
+    if (active[d] && (b->step[d] || b->total[d] || ns > 0))
       T[d] = (double*)calloc(nall, sizeof(double));
   tendency_reg(b, w, dt, du, T);
   const double* wt = b->wght[stage];
+  /* the scalars ride on the register's mass row before the implicit posts
+   * enter T_1 (hydro_forward.cpp:918-922, scalar.cpp:106-116) */
+  double* ds = NULL;
+  if (ns > 0) {
+    double* fm[3] = {NULL, NULL, NULL};
+    for (int d = 0; d < 3; ++d)
+      if (T[d]) fm[d] = T[d] + OG_IDN * nc;
+    if (stage == 0) memcpy(b->scalar0, b->scalar, sizeof(double) * ns * nc);
+    ds = (double*)malloc(sizeof(double) * ns * nc);
+    scalar_tendency(b, u, fm, dt, b->scalar, ds);
+  }
   /* the vertical implicit correction with dt_corr = wght2 dt
    * (hydro_forward.cpp:1153-1168); its posts enter T_1, whose wall faces
    * are prescribed again after it (hydro_forward.cpp:1195-1196) */
@@ -1116,6 +1251,13 @@ void og_stage(const og_block* b, double* u, double* u0, double dt, int stage) {
   for (long q = 0; q < (long)nall; ++q)
     u[q] = wt[0] * u0[q] + wt[1] * u[q] + wt[2] * du[q];
   og_apply_bc(b, u, 0);
+  if (ns > 0) {
+    double* s = b->scalar;
+    for (size_t q = 0; q < (size_t)ns * nc; ++q)
+      s[q] = wt[0] * b->scalar0[q] + wt[1] * s[q] + wt[2] * ds[q];
+    og_scalar_bc(b, s);
+    free(ds);
+  }
   free(w);
   free(du);
 }

@@ -59,6 +59,12 @@ typedef struct og_block {
    * same faces (FluxRegister::total after HydroImpl::forward) */
   double* step[3];
   double* total[3];
+  /* scalar/nvar passive scalars (src/scalar/scalar.cpp:90-211): their
+   * densities (nscalar, nc3, nc2, nc1), advanced in place by og_stage, and
+   * the stage-0 backup; nscalar 0 or scalar NULL: none */
+  int nscalar;
+  double* scalar;
+  double* scalar0;
 } og_block;
 
 /* ---- unit functions (pinned against the reference headers) ---- */
@@ -82,6 +88,8 @@ void og_cons2prim(const og_block* b, const double* u, double* w);
 void og_prim2cons(const og_block* b, const double* w, double* u);
 /* boundary functions, faces in order 0..5; primitive selects kPrimitive */
 void og_apply_bc(const og_block* b, double* q, int primitive);
+/* the kScalar boundary functions on nscalar rows of tracer densities */
+void og_scalar_bc(const og_block* b, double* s);
 /* face fluxes of direction d (1 = x1, 2 = x2, 3 = x3) at every face */
 void og_flux(const og_block* b, const double* w, int d, double* flux);
 /* one RK stage: u is advanced in place; u0 holds the stage-0 backup */

@@ -56,6 +56,7 @@ class BlockDesc(ctypes.Structure):
         ("implicit_scheme", _i32),
         ("base", _vp),
         ("implicit_precision", _i32),
+        ("nscalar", _i32),
     ]
 
 
@@ -71,7 +72,7 @@ NOALLOC_MAX_BLOCKS = 64  # SG_NOALLOC_MAX_BLOCKS
 
 # SG_KERNEL_* of sg_kernel_times
 KERNELS = ("stage_kernel", "vic_assemble_kernel", "vic_solve_kernel",
-           "vic_finish_kernel", "ghost_kernel", "x3_kernel")
+           "vic_finish_kernel", "ghost_kernel", "x3_kernel", "scalar_kernel")
 
 
 class CsDesc(ctypes.Structure):
@@ -110,6 +111,7 @@ SIGNATURES = {
     "sg_budget_totals": (ctypes.c_int, [_vp, _vp, _vp]),
     "sg_budget_boundary": (ctypes.c_int, [_vp, _vp, _i32, _vp]),
     "sg_set_solve": (ctypes.c_int, [_vp, _i32]),
+    "sg_bind_scalars": (ctypes.c_int, [_vp, _i32, _vp, _vp, _vp]),
     "sg_solve_fallbacks": (ctypes.c_int, [_vp, _vp]),
     "sg_autotune": (ctypes.c_int, [_vp, _i32, _vp, _vp, _vp, _vp]),
     "sg_set_schedule": (ctypes.c_int, [_vp, _vp, _i32]),

@@ -99,6 +99,7 @@ class Batch:
             a.x1v = v.data_ptr() if v is not None else None
             a.implicit_scheme = int(d.get("implicit_scheme", 0))
             a.implicit_precision = _lib.F32 if d.get("implicit_f32") else _lib.F64
+            a.nscalar = int(d.get("nscalar", 0))
         # FP32 under gravity: the state is stored as anomalies about an FP64
         # hydrostatic base per block (filled from the initial state)
         self.bases = []
@@ -122,6 +123,18 @@ class Batch:
             _lib.check(self.L.sg_bind(self.h, b, st[0].data_ptr(),
                                       st[1].data_ptr(), st[2].data_ptr()),
                        "sg_bind")
+        # the passive scalars' three buffers per block, rotated with the state
+        self.sstore = []
+        for b, d in enumerate(blocks):
+            ns = int(d.get("nscalar", 0))
+            t = None
+            if ns:
+                t = torch.zeros((3, ns) + self.shapes[b][1:], dtype=dtype,
+                                device=device)
+                _lib.check(self.L.sg_bind_scalars(self.h, b, t[0].data_ptr(),
+                                                  t[1].data_ptr(), t[2].data_ptr()),
+                           "sg_bind_scalars")
+            self.sstore.append(t)
         # the FP64 scratch of the implicit solves (torch allocations)
         self.scratch = []
         for b in range(self.nblock):
@@ -163,6 +176,18 @@ class Batch:
 
     def current(self, b: int = 0) -> torch.Tensor:
         return self.store[b][self.current_index()]
+
+    def current_scalars(self, b: int = 0) -> Optional[torch.Tensor]:
+        """Block b's current tracer densities (nscalar, nc3, nc2, nc1), or
+        None without scalars."""
+        t = self.sstore[b]
+        return None if t is None else t[self.current_index()]
+
+    def init_scalars(self, b: int, s: torch.Tensor, stream=None) -> None:
+        """Block b's initial tracer densities into the current buffer, then
+        their ghost cells by the boundary functions."""
+        self.current_scalars(b).copy_(s)
+        self.fill_ghosts(stream)
 
     def rotation(self):
         c, b = ctypes.c_int32(), ctypes.c_int32()

@@ -42,7 +42,11 @@ using sg::StageParams;
   extern "C" int sg_launch_budget_totals##sfx(const BlockDev*, int, int,       \
                                               double*, cudaStream_t);          \
   extern "C" int sg_launch_budget_boundary##sfx(const BlockDev*, int, double*, \
-                                                int, cudaStream_t);
+                                                int, cudaStream_t);           \
+  extern "C" int sg_launch_scalar##sfx(const BlockDev*, StageParams, size_t,  \
+                                       cudaStream_t);                          \
+  extern "C" int sg_launch_scalar_ghost##sfx(const BlockDev*, int, int,       \
+                                             size_t, cudaStream_t);
 SG_DECLARE(_f64)
 SG_DECLARE(_f32)
 
@@ -138,6 +142,14 @@ __global__ void restore_kernel(const BlockDev* __restrict__ tab, int cur,
   for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < words;
        q += (size_t)gridDim.x * blockDim.x)
     dst[q] = src[q];
+  if (B.nscalar > 0) {  // the scalars' step-start state too
+    const size_t sw = (size_t)B.nscalar * B.nc1 * B.nc2 * B.nc3 * esz / 4;
+    const uint32_t* ss = static_cast<const uint32_t*>(B.sbuf[base]);
+    uint32_t* sd = static_cast<uint32_t*>(B.sbuf[cur]);
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < sw;
+         q += (size_t)gridDim.x * blockDim.x)
+      sd[q] = ss[q];
+  }
 }
 
 // the x1 geometry constants of the gravity-work correction for interior
@@ -218,6 +230,8 @@ struct sg_handle {
   int32_t finish = 0;  // implicit finish form: 0 auto, 1 warp, 2 thread
   std::vector<size_t> scratch_bytes;  // per block: vic_bytes + the x3 part
   std::vector<size_t> vic_bytes;
+  std::vector<size_t> dv3_bytes;  // per block: the x3 part of the scratch
+  bool scalars = false;           // some block transports passive scalars
   int device = 0;
   // per-kernel timing (sg_set_timing): events recorded between the launches
   // of each eager sg_stage, reused from a pool; each pending interval is
@@ -273,6 +287,10 @@ int upload(sg_handle* h, cudaStream_t s) {
     if (h->host[b].implicit && h->host[b].step[0] && !h->host[b].t1)
       return fail(SG_ERR_STATE, "block %d: the x1 step field of an implicit "
                   "block needs its scratch (sg_bind_step_fields)", b);
+    if (h->host[b].nscalar > 0 &&
+        (!h->host[b].sbuf[0] || !h->host[b].mflux[0]))
+      return fail(SG_ERR_STATE, "block %d: its scalar buffers or scratch are "
+                  "not bound (sg_bind_scalars, sg_bind_scratch)", b);
   }
   cudaError_t e = cudaMemcpyAsync(h->dev, h->host.data(),
                                   sizeof(BlockDev) * h->nblock,
@@ -645,6 +663,18 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
                   "needs the FP32 state (dynamics/precision float32)", b);
     }
     B.implicit_f32 = d.implicit_scheme != 0 && d.implicit_precision == SG_F32;
+    if (d.nscalar < 0 || d.nscalar > 16) {
+      sg_destroy(h);
+      return fail(SG_ERR_ARG, "block %d: nscalar %d (0 to 16)", b, d.nscalar);
+    }
+    if (d.nscalar > 0 && (d.implicit_scheme != 0 || d.nc3 > 1)) {
+      sg_destroy(h);
+      return fail(SG_ERR_UNSUPPORTED, "block %d: passive scalars are built for "
+                  "1-D and 2-D blocks without the implicit solve (the "
+                  "solve's tracer transfer is not built)", b);
+    }
+    B.nscalar = d.nscalar;
+    if (d.nscalar > 0) h->scalars = true;
     if (B.implicit_f32) {
       h->any_f32 = 1;
       h->refine = 2;
@@ -705,8 +735,14 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
                     icols * sg::kVicFloatsPerColumn) * sizeof(float);
     vic_bytes = (vic_bytes + 15) / 16 * 16;  // the x3 part starts aligned
     size_t dv3_bytes = d.nc3 > 1 ? 5 * icells * (f64(h) ? 8 : 4) : 0;
+    dv3_bytes = (dv3_bytes + 15) / 16 * 16;
+    // passive scalars: the FP64 mass flux and the scalars' face fluxes along
+    // x1 and x2 over the padded block
+    const size_t cells = (size_t)d.nc1 * d.nc2 * d.nc3;
+    size_t sc_bytes = d.nscalar > 0 ? 2 * (1 + (size_t)d.nscalar) * cells * 8 : 0;
     h->vic_bytes.push_back(vic_bytes);
-    h->scratch_bytes.push_back(vic_bytes + dv3_bytes);
+    h->dv3_bytes.push_back(dv3_bytes);
+    h->scratch_bytes.push_back(vic_bytes + dv3_bytes + sc_bytes);
     if (d.implicit_scheme) {
       h->max_icells = std::max(h->max_icells, icells);
       h->max_icols = std::max(h->max_icols, icols);
@@ -796,6 +832,31 @@ int sg_bind_scratch(sg_handle* h, int32_t block, void* scratch, size_t bytes) {
   B.vic = B.implicit ? static_cast<double*>(scratch) : nullptr;
   B.dv3 = B.nc3 > 1 ? static_cast<unsigned char*>(scratch) + h->vic_bytes[block]
                     : nullptr;
+  if (B.nscalar > 0) {
+    double* sc = reinterpret_cast<double*>(static_cast<unsigned char*>(scratch) +
+                                           h->vic_bytes[block] +
+                                           h->dv3_bytes[block]);
+    const size_t plane = (size_t)B.nc1 * B.nc2 * B.nc3;
+    B.mflux[0] = sc;
+    B.mflux[1] = sc + plane;
+    B.sflux[0] = sc + 2 * plane;
+    B.sflux[1] = sc + (2 + (size_t)B.nscalar) * plane;
+  }
+  h->dirty = true;
+  return 0;
+}
+
+int sg_bind_scalars(sg_handle* h, int32_t block, void* s0, void* s1, void* s2) {
+  if (!h || block < 0 || block >= h->nblock)
+    return fail(SG_ERR_ARG, "sg_bind_scalars: block %d", block);
+  BlockDev& B = h->host[block];
+  if (B.nscalar == 0)
+    return fail(SG_ERR_ARG, "sg_bind_scalars: block %d has no scalars", block);
+  if (!s0 || !s1 || !s2)
+    return fail(SG_ERR_ARG, "sg_bind_scalars: null buffer");
+  B.sbuf[0] = s0;
+  B.sbuf[1] = s1;
+  B.sbuf[2] = s2;
   h->dirty = true;
   return 0;
 }
@@ -1004,9 +1065,9 @@ int sg_stage(sg_handle* h, int32_t stage, const double* dt_dev,
   p.max_nc1 = h->max_nc1;
   // events between the launches when timing is on and the stream is not
   // being captured: ev[0] (x3 ev[6]) stage ev[1] (assemble ev[2] solve
-  // ev[3] finish ev[4]) ghost ev[5]
-  cudaEvent_t ev[7] = {};
-  int eidx[7] = {};
+  // ev[3] finish ev[4]) (scalars ev[7]) ghost ev[5]
+  cudaEvent_t ev[8] = {};
+  int eidx[8] = {};
   bool timed = false;
   if (h->timing) {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -1015,7 +1076,7 @@ int sg_stage(sg_handle* h, int32_t stage, const double* dt_dev,
     timed = cs == cudaStreamCaptureStatusNone;
   }
   if (timed) {
-    for (int k = 0; k < 7; ++k) {
+    for (int k = 0; k < 8; ++k) {
       rc = take_event(h, &eidx[k]);
       if (rc) return rc;
       ev[k] = h->events[eidx[k]];
@@ -1047,9 +1108,25 @@ int sg_stage(sg_handle* h, int32_t stage, const double* dt_dev,
     if (timed) cudaEventRecord(ev[4], s);
     launches += 3;
   }
+  if (h->scalars) {
+    // the passive scalars on the stage's mass flux: face fluxes, update
+    rc = f64(h) ? sg_launch_scalar_f64(h->dev, p, h->max_plane, s)
+                : sg_launch_scalar_f32(h->dev, p, h->max_plane, s);
+    if (rc) return cuda_fail((cudaError_t)rc, "sg_stage: scalars");
+    if (timed) cudaEventRecord(ev[7], s);
+    launches += 2;
+  }
   rc = f64(h) ? sg_launch_ghost_f64(h->dev, h->nblock, out, h->max_plane, s)
               : sg_launch_ghost_f32(h->dev, h->nblock, out, h->max_plane, s);
   if (rc) return cuda_fail((cudaError_t)rc, "sg_stage: ghost kernel");
+  if (h->scalars) {
+    rc = f64(h) ? sg_launch_scalar_ghost_f64(h->dev, h->nblock, out,
+                                             h->max_plane, s)
+                : sg_launch_scalar_ghost_f32(h->dev, h->nblock, out,
+                                             h->max_plane, s);
+    if (rc) return cuda_fail((cudaError_t)rc, "sg_stage: scalar ghosts");
+    launches += 1;
+  }
   if (timed) {
     cudaEventRecord(ev[5], s);
     if (h->has3) {
@@ -1058,14 +1135,18 @@ int sg_stage(sg_handle* h, int32_t stage, const double* dt_dev,
     } else {
       h->pending.push_back({SG_KERNEL_STAGE, eidx[0], eidx[1]});
     }
+    int last = eidx[1];  // the event before the scalars or the ghosts
     if (h->implicit) {
       h->pending.push_back({SG_KERNEL_VIC_ASSEMBLE, eidx[1], eidx[2]});
       h->pending.push_back({SG_KERNEL_VIC_SOLVE, eidx[2], eidx[3]});
       h->pending.push_back({SG_KERNEL_VIC_FINISH, eidx[3], eidx[4]});
-      h->pending.push_back({SG_KERNEL_GHOST, eidx[4], eidx[5]});
-    } else {
-      h->pending.push_back({SG_KERNEL_GHOST, eidx[1], eidx[5]});
+      last = eidx[4];
     }
+    if (h->scalars) {
+      h->pending.push_back({SG_KERNEL_SCALAR, last, eidx[7]});
+      last = eidx[7];
+    }
+    h->pending.push_back({SG_KERNEL_GHOST, last, eidx[5]});
   }
   if (stage == 0) h->base = h->cur;
   h->cur = out;
@@ -1081,6 +1162,13 @@ int sg_fill_ghosts(sg_handle* h, sg_stream_t stream) {
   rc = f64(h) ? sg_launch_ghost_f64(h->dev, h->nblock, h->cur, h->max_plane, s)
               : sg_launch_ghost_f32(h->dev, h->nblock, h->cur, h->max_plane, s);
   if (rc) return cuda_fail((cudaError_t)rc, "sg_fill_ghosts");
+  if (h->scalars) {
+    rc = f64(h) ? sg_launch_scalar_ghost_f64(h->dev, h->nblock, h->cur,
+                                             h->max_plane, s)
+                : sg_launch_scalar_ghost_f32(h->dev, h->nblock, h->cur,
+                                             h->max_plane, s);
+    if (rc) return cuda_fail((cudaError_t)rc, "sg_fill_ghosts: scalars");
+  }
   return 0;
 }
 

@@ -835,6 +835,25 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
     }
   }
 
+  // passive scalars ride on the stage's mass flux (the register's mass row,
+  // walls prescribed): every face of the tile's interior cells, FP64, with
+  // the step fields' one writer per face
+  if (B.nscalar > 0) {
+    for (int idx = threadIdx.x; idx < ntj * nf1; idx += blockDim.x) {
+      const int jt = idx / nf1, fi = idx - jt * nf1, f = il + fi;
+      B.mflux[0][koff + (size_t)(j0 + jt) * nc1 + f] =
+          (double)F1[IDN * f1stride + idx];
+    }
+    if (has2) {
+      for (int idx = threadIdx.x; idx < (ntj + 1) * nx1; idx += blockDim.x) {
+        const int jf = idx / nx1, i = il + (idx - jf * nx1);
+        if (jf == ntj && j0 + ntj != jend) continue;
+        B.mflux[1][koff + (size_t)(j0 + jf) * nc1 + i] =
+            (double)F2[IDN * f2stride + idx];
+      }
+    }
+  }
+
   // (6) divergence, du = -dt div, gravity, viscous momentum, the x1 gravity
   // energy correction, and the RK combine on the interior cells
   const real a1 = real(B.dx3 * B.dx2), a2 = real(B.dx3 * B.dx1);
@@ -1017,6 +1036,140 @@ __global__ void __launch_bounds__(kThreads)
       q[IDN * plane + c] += real(rb[si] - rb[i]);
       q[IPR * plane + c] += real(eb[si] - eb[i]);
     }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// passive scalars (ScalarImpl::forward, src/scalar/scalar.cpp:90-211, the
+// dry case without limiter or upper bound).  One thread per face of the
+// interior cells: the side the stage's mass flux F_m selects (F_m > 0: the
+// left state, the plus side of cell f - 1; else the right state, the minus
+// side of cell f) is reconstructed by scale-invariant WENO5 for the total
+// dry density and each tracer density, floored at 0 (ReconstructImpl::
+// forward without a hydro parent, src/recon/reconstruct.cpp:258-262); the
+// face ratio r = s_f / rho_f, or the donor cell's where rho_f is not
+// positive; the upwind flux F_s = F_m r (riemann.cpp:164-170), zero on the
+// reflecting faces (boundary.prescribed), FP64 as the reference keeps it
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads)
+    scalar_flux_kernel(const BlockDev* __restrict__ tab, StageParams p) {
+  const BlockDev& B = tab[blockIdx.y];
+  const int ns = B.nscalar;
+  if (ns == 0) return;
+  const int nc1 = B.nc1, nc2 = B.nc2, ng = B.ng;
+  const bool has2 = nc2 > 1;
+  const size_t plane = (size_t)nc1 * nc2;
+  const int nx1 = nc1 - 2 * ng, nx2 = has2 ? nc2 - 2 * ng : 1;
+  const int jl = has2 ? ng : 0;
+  const size_t n1f = (size_t)nx2 * (nx1 + 1);
+  const size_t n2f = has2 ? (size_t)(nx2 + 1) * nx1 : 0;
+  const real* u = static_cast<const real*>(B.buf[p.in]);
+  const real* s = static_cast<const real*>(B.sbuf[p.in]);
+  const double* rb = B.base ? base_rho(B.base, nc1) : nullptr;
+  // the total dry density (the state holds an anomaly under a base)
+  auto rho = [&](size_t c) -> real {
+    real v = u[IDN * plane + c];
+    if (rb) v = v + real(rb[c % nc1]);
+    return v;
+  };
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n1f + n2f;
+       t += (size_t)gridDim.x * blockDim.x) {
+    int d, i, j;  // the face along d below cell (j, i)
+    if (t < n1f) {
+      d = 0;
+      j = jl + (int)(t / (nx1 + 1));
+      i = ng + (int)(t % (nx1 + 1));
+    } else {
+      const size_t e = t - n1f;
+      d = 1;
+      j = ng + (int)(e / nx1);
+      i = ng + (int)(e % nx1);
+    }
+    const size_t q = (size_t)j * nc1 + i;
+    const size_t st = d == 0 ? 1 : (size_t)nc1;
+    const int f = d == 0 ? i : j, nd = d == 0 ? nc1 : nc2;
+    const bool wall = (f == ng && B.bc[2 * d] == kBcReflecting) ||
+                      (f == nd - ng && B.bc[2 * d + 1] == kBcReflecting);
+    const double F = B.mflux[d][q];
+    const bool left = F > 0.;
+    const size_t c0 = q - (left ? 3 : 2) * st;
+    const size_t donor = left ? q - st : q;
+    auto face = [&](real f0, real f1, real f2, real f3, real f4) -> real {
+      real v = left ? weno5_cp(f0, f1, f2, f3, f4, true)
+                    : weno5_cm(f0, f1, f2, f3, f4, true);
+      return v < real(0) ? real(0) : v;  // clamp_min: -0 stays
+    };
+    const real rf = face(rho(c0), rho(c0 + st), rho(c0 + 2 * st),
+                         rho(c0 + 3 * st), rho(c0 + 4 * st));
+    for (int v = 0; v < ns; ++v) {
+      const real* sv = s + (size_t)v * plane;
+      const real sf = face(sv[c0], sv[c0 + st], sv[c0 + 2 * st],
+                           sv[c0 + 3 * st], sv[c0 + 4 * st]);
+      const real r = rf > real(0) ? sf / rf : sv[donor] / rho(donor);
+      B.sflux[d][(size_t)v * plane + q] = wall ? 0. : F * (double)r;
+    }
+  }
+}
+
+// ds = -dt div F_s on the interior cells (the area-weighted divergence, in
+// the hydro's order), then the stage's combine s_out = w0 s0 + w1 s + w2 ds
+__global__ void __launch_bounds__(kThreads)
+    scalar_update_kernel(const BlockDev* __restrict__ tab, StageParams p) {
+  const BlockDev& B = tab[blockIdx.y];
+  const int ns = B.nscalar;
+  if (ns == 0) return;
+  const int nc1 = B.nc1, nc2 = B.nc2, ng = B.ng;
+  const bool has2 = nc2 > 1;
+  const size_t plane = (size_t)nc1 * nc2;
+  const int nx1 = nc1 - 2 * ng, nx2 = has2 ? nc2 - 2 * ng : 1;
+  const int jl = has2 ? ng : 0;
+  const double a1 = B.dx3 * B.dx2, a2 = B.dx3 * B.dx1;
+  const double vol = B.dx3 * (B.dx2 * B.dx1);
+  const double mdt = -p.dt[blockIdx.y];
+  const real* s0 = static_cast<const real*>(B.sbuf[p.u0]);
+  const real* s = static_cast<const real*>(B.sbuf[p.in]);
+  real* so = static_cast<real*>(B.sbuf[p.out]);
+  const size_t ncell = (size_t)nx1 * nx2 * ns;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < ncell;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const int v = (int)(t / ((size_t)nx1 * nx2));
+    const size_t e = t - (size_t)v * nx1 * nx2;
+    const int j = jl + (int)(e / nx1), i = ng + (int)(e % nx1);
+    const size_t q = (size_t)v * plane + (size_t)j * nc1 + i;
+    const double* F1 = B.sflux[0];
+    double dv = a1 * F1[q + 1] - a1 * F1[q];
+    if (has2) {
+      const double* F2 = B.sflux[1];
+      dv = dv + (a2 * F2[q + nc1] - a2 * F2[q]);
+    }
+    const double ds = mdt * (dv / vol);
+    so[q] = real(p.w0 * (double)s0[q] + p.w1 * (double)s[q] + p.w2 * ds);
+  }
+}
+
+// the scalars' ghost cells of sbuf[which]: the boundary functions of a
+// kScalar field (bc_func.cpp:10-70), the state's maps without sign flips
+__global__ void __launch_bounds__(kThreads)
+    scalar_ghost_kernel(const BlockDev* __restrict__ tab, int which) {
+  const BlockDev& B = tab[blockIdx.y];
+  if (B.nscalar == 0) return;
+  const int nc1 = B.nc1, nc2 = B.nc2, nc3 = B.nc3, ng = B.ng;
+  const size_t plane = (size_t)nc1 * nc2 * nc3;
+  real* q = static_cast<real*>(B.sbuf[which]);
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < plane;
+       c += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(c % nc1);
+    const int j = (int)((c / nc1) % nc2);
+    const int k = (int)(c / ((size_t)nc1 * nc2));
+    bool f1 = false, f2 = false, f3 = false;
+    const int si = ghost_src(i, nc1, ng, B.bc[0], B.bc[1], f1);
+    const int sj = ghost_src(j, nc2, ng, B.bc[2], B.bc[3], f2);
+    const int sk = ghost_src(k, nc3, ng, B.bc[4], B.bc[5], f3);
+    if (si == i && sj == j && sk == k) continue;  // interior
+    if (si < 0 || sj < 0 || sk < 0) continue;     // no boundary function
+    const size_t src = ((size_t)sk * nc2 + sj) * nc1 + si;
+    for (int v = 0; v < B.nscalar; ++v)
+      q[(size_t)v * plane + c] = q[(size_t)v * plane + src];
   }
 }
 
@@ -1454,6 +1607,29 @@ extern "C" int SG_NAME(sg_launch_x3)(const BlockDev* tab, StageParams p,
   int gx = (int)((work + kThreads - 1) / kThreads);
   if (gx > 2048) gx = 2048;
   k<<<dim3(gx, p.nblock), kThreads, 0, stream>>>(tab, p);
+  return (int)cudaGetLastError();
+}
+
+extern "C" int SG_NAME(sg_launch_scalar)(const BlockDev* tab, StageParams p,
+                                         size_t max_plane,
+                                         cudaStream_t stream) {
+  int gx = (int)((2 * max_plane + kThreads - 1) / kThreads);
+  if (gx > 2048) gx = 2048;
+  scalar_flux_kernel<<<dim3(gx, p.nblock), kThreads, 0, stream>>>(tab, p);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return (int)e;
+  int gu = (int)((max_plane + kThreads - 1) / kThreads);
+  if (gu > 2048) gu = 2048;
+  scalar_update_kernel<<<dim3(gu, p.nblock), kThreads, 0, stream>>>(tab, p);
+  return (int)cudaGetLastError();
+}
+
+extern "C" int SG_NAME(sg_launch_scalar_ghost)(const BlockDev* tab, int nblock,
+                                               int which, size_t max_plane,
+                                               cudaStream_t stream) {
+  int gx = (int)((max_plane + kThreads - 1) / kThreads);
+  if (gx > 1024) gx = 1024;
+  scalar_ghost_kernel<<<dim3(gx, nblock), kThreads, 0, stream>>>(tab, which);
   return (int)cudaGetLastError();
 }
 

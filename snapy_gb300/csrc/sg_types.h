@@ -70,6 +70,14 @@ struct BlockDev {
   // laid out (v, column, face) over the interior columns and nx1 + 1 faces
   double* step[3];
   double* t1;
+  // passive scalars: their three buffers (nscalar, nc3, nc2, nc1) in the
+  // storage type, rotated with buf; the stage's FP64 mass flux along x1 and
+  // x2 (face f below cell f, written by the stage kernel) and the scalars'
+  // FP64 face fluxes (nscalar rows of the same layout), in the scratch
+  int32_t nscalar;
+  void* sbuf[3];
+  double* mflux[2];
+  double* sflux[2];
 };
 
 // offsets into BlockDev::base

@@ -30,6 +30,9 @@ class Ensemble:
         if not members:
             raise ValueError("an ensemble needs at least one member")
         self.members = list(members)
+        if any(m.scalar_names for m in self.members):
+            raise DeckError("Ensemble: members with passive scalars are not "
+                            "built; step them as MeshBlocks")
         schemes = [scheme_of(m) for m in self.members]
         if any(s != schemes[0] for s in schemes[1:]):
             raise DeckError("ensemble members must share one scheme (solver, "

@@ -118,7 +118,8 @@ def block_of(options: MeshBlockOptions, tj: int = 0) -> dict:
             "x1f": x1f, "x1v": x1v,
             "implicit_scheme": h.icorr.scheme if h.icorr else 0,
             # FP32 assembly of the implicit blocks (the solve stays FP64)
-            "implicit_f32": bool(h.icorr) and h.icorr.precision == "float32"}
+            "implicit_f32": bool(h.icorr) and h.icorr.precision == "float32",
+            "nscalar": len(options.scalar_names)}
 
 
 class FluxRegister:
@@ -228,7 +229,11 @@ class MeshBlock:
 
     # -- reference API ---------------------------------------------------------
     def initialize(self, vars: dict):
-        """Boundary functions on hydro_w (in place), hydro_u = W->U(hydro_w)."""
+        """Boundary functions on hydro_w (in place), hydro_u = W->U(hydro_w);
+        with passive scalars, scalar_s = rho scalar_r (MeshBlockImpl::
+        finalize_initialization, src/mesh/meshblock.cpp:380-383) from the
+        required scalar_r (nscalar, nc3, nc2, nc1), ghosts by the boundary
+        functions."""
         if "hydro_w" not in vars:
             raise RuntimeError("initialize: hydro_w is required for hydro model.")
         w = vars["hydro_w"]
@@ -251,9 +256,29 @@ class MeshBlock:
                 self._graphs.clear()
                 self._seen.clear()
             u = self.batch.current(0)
+            ns = len(self.options.scalar_names)
+            if ns:
+                r = vars.get("scalar_r")
+                if r is None:
+                    raise RuntimeError("initialize: scalar_r is required")
+                if tuple(r.shape) != (ns,) + self.nc():
+                    raise RuntimeError("initialize: scalar_r has incorrect shape")
+                # the conserved (dry) density of the initial state, FP64
+                s = w[0].unsqueeze(0) * r.to(device=self.device, dtype=torch.float64)
+                self.batch.init_scalars(0, s.to(self.dtype))
+                sc = self.batch.current_scalars(0)
+                vars["scalar_s"] = torch.empty(0, dtype=self.dtype,
+                                               device=self.device).set_(sc)
         vars["hydro_u"] = torch.empty(0, dtype=self.dtype, device=self.device).set_(u)
         self.intg.current_redo = 0
         return vars, 0.0
+
+    def _publish(self, vars: dict) -> None:
+        """vars views the block's current storage (hydro_u, scalar_s)."""
+        b = self.batch
+        vars["hydro_u"].set_(b.current(0))
+        if "scalar_s" in vars and b.sstore[0] is not None:
+            vars["scalar_s"].set_(b.current_scalars(0))
 
     def _adopt(self, vars: dict) -> None:
         u = vars.get("hydro_u")
@@ -264,6 +289,11 @@ class MeshBlock:
             cur.copy_(u)  # a rebound hydro_u is copied into block storage
             u.set_(cur)
             self._report["host"] += 1
+        s = vars.get("scalar_s")
+        sc = self.batch.current_scalars(0)
+        if s is not None and sc is not None and s.data_ptr() != sc.data_ptr():
+            sc.copy_(s)  # and a rebound scalar_s
+            s.set_(sc)
 
     def forward(self, vars: dict, dt: float, stage: int) -> None:
         """One RK stage (MeshBlockImpl::forward, meshblock_advance.cpp:88).
@@ -293,7 +323,7 @@ class MeshBlock:
                 b.stage(stage)
                 self._seen.add(key)
                 self._report["eager"] += 1
-            vars["hydro_u"].set_(b.current(0))
+            self._publish(vars)
 
     def step(self, vars: dict, dt: float) -> None:
         """All stages of one step (the driver loop's ``for stage ...
@@ -320,7 +350,7 @@ class MeshBlock:
                     b.stage(s)
                 self._seen.add(key)
                 self._report["eager"] += 1
-            vars["hydro_u"].set_(b.current(0))
+            self._publish(vars)
 
     def _capture(self, stage, rot) -> torch.cuda.CUDAGraph:
         b = self.batch
@@ -357,7 +387,7 @@ class MeshBlock:
             flags = int(self.batch.check()[0].item())
             if flags:
                 self.batch.restore()
-                vars["hydro_u"].set_(self.batch.current(0))
+                self._publish(vars)
                 self.intg.current_redo += 1
                 self._refresh_w(vars)
                 if self.intg.current_redo > self.intg.options.max_redo:

@@ -376,6 +376,40 @@ _BC_NAMES = {"reflecting", "periodic", "extrapolation", "outflow", "custom",
              "solid", "fixed_temperature"}
 
 
+def _scalar_names(node, op) -> List[str]:
+    """The passive scalars of the deck's scalar section
+    (ScalarOptionsImpl::from_yaml, src/scalar/scalar_options.cpp): the
+    transport is built without the upper bound and with the upwind solver
+    and the hydro's WENO5 (scale-invariant, as the reference always
+    reconstructs a scalar)."""
+    if not node:
+        return []
+    check_keys(node, "scalar", {"verbose", "nvar", "upper-bound", "names",
+                                "reconstruct", "riemann-solver"})
+    names = [str(x) for x in (node.get("names") or [])]
+    nvar = int(node.get("nvar", len(names)))
+    if not names:
+        names = [f"scalar{n}" for n in range(nvar)]
+    if float(node.get("upper-bound", -1.0)) > 0.0:
+        raise DeckError("scalar/upper-bound: the upper-bound limiter is not built")
+    rs = node.get("riemann-solver")
+    if rs and str((rs or {}).get("type", "upwind")) != "upwind":
+        raise DeckError("scalar/riemann-solver: only upwind is built")
+    rc = node.get("reconstruct")
+    if rc and str((rc or {}).get("type", "weno5")) != "weno5":
+        raise DeckError("scalar/reconstruct: only weno5 is built")
+    if names:
+        h, c = op.hydro(), op.coord()
+        if h.icorr is not None:
+            raise DeckError("scalar: passive scalars with the vertical implicit "
+                            "solve are not built (its tracer transfer)")
+        if c.nx3 > 1:
+            raise DeckError("scalar: passive scalars on 3-D blocks are not built")
+        if h.eos.type == "shallow-water":
+            raise DeckError("scalar: passive scalars need a dry-air density")
+    return names
+
+
 class MeshBlockOptions:
     """The deck of one block (reference MeshBlockOptionsImpl)."""
 
@@ -400,6 +434,9 @@ class MeshBlockOptions:
         # (the FP64 solve of every column)
         self.implicit_solve = "refined"
         self.implicit_corrections = 2  # FP64-residual corrections (1 to 3)
+        # scalar/nvar, scalar/names: passive scalars (ScalarOptionsImpl,
+        # src/scalar/scalar.hpp)
+        self.scalar_names: List[str] = []
         self.verbose = False
         self.basename = ""
         self.problem: Dict[str, Any] = {}
@@ -464,6 +501,7 @@ class MeshBlockOptions:
             raise DeckError("integration/execution-strict needs execution: "
                             "cuda-graph (eager is never refused)")
         op._coord = CoordinateOptions.from_dict(config)
+        op.scalar_names = _scalar_names(config.get("scalar"), op)
         op.problem = dict(config.get("problem") or {})
         bcs = config.get("boundary-condition")
         if bcs is not None:

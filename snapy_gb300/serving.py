@@ -87,6 +87,9 @@ class _Slot:
     in."""
 
     def __init__(self, req: Request, device, dtype):
+        if req.options.scalar_names:
+            raise DeckError(f"request {req.rid}: passive scalars are not "
+                            "built for served requests")
         self.req = req
         self.desc = d = block_of(req.options)
         self.shape = (5, d["nc3"], d["nc2"], d["nc1"])
