@@ -66,6 +66,7 @@ class OgBlock(ctypes.Structure):
         ("nscalar", ctypes.c_int),
         ("scalar", _dp),
         ("scalar0", _dp),
+        ("vic_q", _dp),
     ]
 
 
@@ -273,9 +274,6 @@ class Block:
     def set_scalars(self, s: np.ndarray) -> np.ndarray:
         """Transport the tracer densities s (nscalar, nc3, nc2, nc1) with
         every stage from here on; returns the array the stages advance."""
-        if self.b.implicit_scheme:
-            raise ValueError("the oracle transports scalars on explicit "
-                             "blocks only")
         self._s = np.ascontiguousarray(s, dtype=np.float64).copy()
         self._s0 = np.zeros_like(self._s)
         self.b.nscalar = self._s.shape[0]

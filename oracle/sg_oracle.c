@@ -1194,6 +1194,51 @@ void og_scalar_bc(const og_block* b, double* s) {
   }
 }
 
+/* the scalars' share of the implicit solve's dry transfer
+ * (MeshBlockImpl::stage_advance, src/mesh/meshblock_advance.cpp:216-233): on
+ * each x1 face the transfer q carries the donor's ratio r = s / rho of the
+ * stage input (the cell below where q > 0), P = r q, capped by what the
+ * donor holds after the explicit transport (donor_cap_cpu,
+ * src/implicit/implicit_dispatch.cpp:54-70: along the column from the
+ * bottom, q within [-held above, held below + the face below's P]), then
+ * ds += (P - P_above) / V */
+static void scalar_vic(const og_block* b, const double* u, const double* s,
+                       const double* q, double* ds) {
+  const int n1 = b->nc1, n2 = b->nc2, ng = b->ng, ns = b->nscalar;
+  const size_t nc = ncell(b);
+  const int il = ng, iu = n1 - ng - 1;
+  const int jl = n2 > 1 ? ng : 0, ju1 = n2 > 1 ? n2 - ng : 1;
+  const double vol = b->dx3 * (b->dx2 * b->dx1);
+  double* P = (double*)malloc(sizeof(double) * (n1 + 1));
+  for (int v = 0; v < ns; ++v)
+    for (int j = jl; j < ju1; ++j) {
+      const size_t c = (size_t)j * n1;
+      const double* sv = s + v * nc + c;
+      double* dv = ds + v * nc + c;
+      const double* rho = u + OG_IDN * nc + c;
+      const double* qc = q + c;
+      for (int i = 0; i <= n1; ++i) P[i] = 0.;
+      for (int i = il; i <= iu + 1; ++i) {
+        const double M = qc[i];
+        const double r = M > 0. ? sv[i - 1] / rho[i - 1] : sv[i] / rho[i];
+        P[i] = r * M;
+      }
+      double avail = sv[il] + dv[il];
+      avail = (avail < 0. ? 0. : avail) * vol;
+      for (int i = il + 1; i <= iu; ++i) {
+        double up = sv[i] + dv[i];
+        up = (up < 0. ? 0. : up) * vol;
+        double Q = P[i];
+        if (Q > avail) Q = avail;
+        if (Q < -up) Q = -up;
+        P[i] = Q;
+        avail = up + Q;
+      }
+      for (int i = il; i <= iu; ++i) dv[i] = dv[i] + (P[i] - P[i + 1]) / vol;
+    }
+  free(P);
+}
+
 void og_stage(const og_block* b, double* u, double* u0, double dt, int stage) {
 #ifdef _OPENMP
   if (b->nthreads > 0) omp_set_num_threads(b->nthreads);
@@ -1227,8 +1272,12 @@ void og_stage(const og_block* b, double* u, double* u0, double dt, int stage) {
   /* the vertical implicit correction with dt_corr = wght2 dt
    * (hydro_forward.cpp:1153-1168); its posts enter T_1, whose wall faces
    * are prescribed again after it (hydro_forward.cpp:1195-1196) */
+  double* vq = NULL;
   if (b->implicit_scheme == 9) {
-    og_implicit_reg(b, w, wt[2] * dt, du, T[0], dt);
+    og_block bq = *b;
+    if (ns > 0) bq.vic_q = vq = (double*)calloc(nc, sizeof(double));
+    og_implicit_reg(&bq, w, wt[2] * dt, du, T[0], dt);
+    if (ns > 0) scalar_vic(b, u, b->scalar, vq, ds);
     if (T[0]) {
       const int n1 = b->nc1, ng = b->ng;
       for (size_t r = 0; r < nc / n1; ++r)
@@ -1258,6 +1307,7 @@ void og_stage(const og_block* b, double* u, double* u0, double dt, int stage) {
     og_scalar_bc(b, s);
     free(ds);
   }
+  free(vq);
   free(w);
   free(du);
 }

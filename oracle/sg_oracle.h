@@ -65,6 +65,10 @@ typedef struct og_block {
   int nscalar;
   double* scalar;
   double* scalar0;
+  /* og_stage's scratch for the implicit solve's face transfers (the
+   * scalars' share of them): the clamped dry transfer q of each x1 face,
+   * face f below cell f; set by og_stage itself */
+  double* vic_q;
 } og_block;
 
 /* ---- unit functions (pinned against the reference headers) ---- */

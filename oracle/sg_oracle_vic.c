@@ -219,9 +219,12 @@ static void slope_stencil(const double* x, int n, double* wt0, double* wt1,
  * st per variable; the solve posts its face transfers into them
  * (ImplicitHydroImpl::post_, src/implicit/implicit_hydro.cpp:625-673) with
  * kdt = dt A_f, the step's dt */
+/* qout (optional): the column's clamped dry transfer q of faces 0..n
+ * (MASS(IVY) of ImplicitHydroImpl's mass correction, zero on the walls and
+ * for a failed column), for the scalars' share of it */
 static int vic_column(const og_block* b, const double* w, size_t st, double* du,
                       int n, double dtc, const double* x1f, const double* x1v,
-                      double* t1, double kdt) {
+                      double* t1, double kdt, double* qout) {
   const double grav = b->grav1, gm1 = b->gammad - 1.;
   const double area = b->dx3 * b->dx2, vol = b->dx3 * (b->dx2 * b->dx1);
   M5* A = (M5*)malloc(sizeof(M5) * n);
@@ -504,6 +507,8 @@ static int vic_column(const og_block* b, const double* w, size_t st, double* du,
         t1[OG_IVZ * st + f] = t1[OG_IVZ * st + f] + pz / kdt;
       }
     }
+    if (qout)
+      for (int f = 0; f <= n; ++f) qout[f] = mf_q[f];
     free(mf_dn);
     free(mf_M);
     free(mf_q);
@@ -539,7 +544,8 @@ int og_implicit_reg(const og_block* b, const double* w, double dtc, double* du,
     int j = jl + (int)(cidx % nj), k = kl + (int)(cidx / nj);
     size_t c = ((size_t)k * n2 + j) * n1 + ng;
     failed += vic_column(b, w + c, nc, du + c, n, dtc, b->x1f + ng, b->x1v + ng,
-                         t1 ? t1 + c : NULL, dt * (b->dx3 * b->dx2));
+                         t1 ? t1 + c : NULL, dt * (b->dx3 * b->dx2),
+                         b->vic_q ? b->vic_q + c : NULL);
   }
   return failed;
 }

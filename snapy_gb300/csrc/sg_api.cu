@@ -44,7 +44,7 @@ using sg::StageParams;
   extern "C" int sg_launch_budget_boundary##sfx(const BlockDev*, int, double*, \
                                                 int, cudaStream_t);           \
   extern "C" int sg_launch_scalar##sfx(const BlockDev*, StageParams, size_t,  \
-                                       cudaStream_t);                          \
+                                       size_t, cudaStream_t);                  \
   extern "C" int sg_launch_scalar_ghost##sfx(const BlockDev*, int, int,       \
                                              size_t, cudaStream_t);
 SG_DECLARE(_f64)
@@ -667,11 +667,10 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
       sg_destroy(h);
       return fail(SG_ERR_ARG, "block %d: nscalar %d (0 to 16)", b, d.nscalar);
     }
-    if (d.nscalar > 0 && (d.implicit_scheme != 0 || d.nc3 > 1)) {
+    if (d.nscalar > 0 && d.nc3 > 1) {
       sg_destroy(h);
       return fail(SG_ERR_UNSUPPORTED, "block %d: passive scalars are built for "
-                  "1-D and 2-D blocks without the implicit solve (the "
-                  "solve's tracer transfer is not built)", b);
+                  "1-D and 2-D blocks", b);
     }
     B.nscalar = d.nscalar;
     if (d.nscalar > 0) h->scalars = true;
@@ -739,7 +738,7 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
     // passive scalars: the FP64 mass flux and the scalars' face fluxes along
     // x1 and x2 over the padded block
     const size_t cells = (size_t)d.nc1 * d.nc2 * d.nc3;
-    size_t sc_bytes = d.nscalar > 0 ? 2 * (1 + (size_t)d.nscalar) * cells * 8 : 0;
+    size_t sc_bytes = d.nscalar > 0 ? 3 * (1 + (size_t)d.nscalar) * cells * 8 : 0;
     h->vic_bytes.push_back(vic_bytes);
     h->dv3_bytes.push_back(dv3_bytes);
     h->scratch_bytes.push_back(vic_bytes + dv3_bytes + sc_bytes);
@@ -837,10 +836,13 @@ int sg_bind_scratch(sg_handle* h, int32_t block, void* scratch, size_t bytes) {
                                            h->vic_bytes[block] +
                                            h->dv3_bytes[block]);
     const size_t plane = (size_t)B.nc1 * B.nc2 * B.nc3;
+    const size_t ns = B.nscalar;
     B.mflux[0] = sc;
     B.mflux[1] = sc + plane;
     B.sflux[0] = sc + 2 * plane;
-    B.sflux[1] = sc + (2 + (size_t)B.nscalar) * plane;
+    B.sflux[1] = sc + (2 + ns) * plane;
+    B.sds = sc + (2 + 2 * ns) * plane;
+    B.vicq = sc + (2 + 3 * ns) * plane;
   }
   h->dirty = true;
   return 0;
@@ -1110,11 +1112,15 @@ int sg_stage(sg_handle* h, int32_t stage, const double* dt_dev,
   }
   if (h->scalars) {
     // the passive scalars on the stage's mass flux: face fluxes, update
-    rc = f64(h) ? sg_launch_scalar_f64(h->dev, p, h->max_plane, s)
-                : sg_launch_scalar_f32(h->dev, p, h->max_plane, s);
+    // (implicit blocks: the transport tendency, then the solve's transfer
+    // and the update per column)
+    rc = f64(h) ? sg_launch_scalar_f64(h->dev, p, h->max_plane,
+                                       h->implicit ? h->max_icols : 0, s)
+                : sg_launch_scalar_f32(h->dev, p, h->max_plane,
+                                       h->implicit ? h->max_icols : 0, s);
     if (rc) return cuda_fail((cudaError_t)rc, "sg_stage: scalars");
     if (timed) cudaEventRecord(ev[7], s);
-    launches += 2;
+    launches += h->implicit ? 3 : 2;
   }
   rc = f64(h) ? sg_launch_ghost_f64(h->dev, h->nblock, out, h->max_plane, s)
               : sg_launch_ghost_f32(h->dev, h->nblock, out, h->max_plane, s);

@@ -1143,7 +1143,10 @@ __global__ void __launch_bounds__(kThreads)
       dv = dv + (a2 * F2[q + nc1] - a2 * F2[q]);
     }
     const double ds = mdt * (dv / vol);
-    so[q] = real(p.w0 * (double)s0[q] + p.w1 * (double)s[q] + p.w2 * ds);
+    if (B.implicit)
+      B.sds[q] = ds;  // the solve's transfer and the update follow
+    else
+      so[q] = real(p.w0 * (double)s0[q] + p.w1 * (double)s[q] + p.w2 * ds);
   }
 }
 
@@ -1447,6 +1450,67 @@ __global__ void __launch_bounds__(kThreads)
 
 #include "sg_vic.cuh"
 
+// an implicit block's scalars after its solve, one thread per column and
+// scalar (MeshBlockImpl::stage_advance, src/mesh/meshblock_advance.cpp:
+// 216-233): each x1 face's transfer q carries the donor's ratio r = s / rho
+// of the stage input (the cell below where q > 0), P = r q; along the column
+// from the bottom each interior face's P is capped to [-held above, held
+// below + the face below's P], held = max(s + ds, 0) V (donor_cap_cpu,
+// src/implicit/implicit_dispatch.cpp:54-70); then ds += (P - P_above) / V
+// and the stage's combine
+__global__ void __launch_bounds__(kThreads)
+    scalar_vic_kernel(const BlockDev* __restrict__ tab, StageParams p) {
+  const BlockDev& B = tab[blockIdx.y];
+  const int ns = B.nscalar;
+  if (ns == 0 || !B.implicit) return;
+  const int nc1 = B.nc1, ng = B.ng, n = nc1 - 2 * ng;
+  const size_t plane = (size_t)nc1 * B.nc2 * B.nc3;
+  const size_t ncol = (size_t)(B.nc2 > 1 ? B.nc2 - 2 * ng : 1) *
+                      (B.nc3 > 1 ? B.nc3 - 2 * ng : 1);
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ncol * ns) return;
+  const int v = (int)(t / ncol);
+  const size_t col = t - (size_t)v * ncol;
+  const size_t row = vic_row(B, col) * nc1;
+  const real* s = static_cast<const real*>(B.sbuf[p.in]) + v * plane + row;
+  const real* s0 = static_cast<const real*>(B.sbuf[p.u0]) + v * plane + row;
+  real* so = static_cast<real*>(B.sbuf[p.out]) + v * plane + row;
+  const real* u = static_cast<const real*>(B.buf[p.in]) + IDN * plane + row;
+  const double* rb = B.base ? base_rho(B.base, nc1) : nullptr;
+  double* ds = B.sds + v * plane + row;
+  const double* q = B.vicq + row;
+  const double vol = B.dx3 * (B.dx2 * B.dx1);
+  const int il = ng, iu = ng + n - 1;
+  auto ratio = [&](int i) -> double {
+    real rho = u[i];
+    if (rb) rho = rho + real(rb[i]);
+    return (double)(s[i] / rho);
+  };
+  auto held = [&](int i) -> double {
+    const double h = (double)s[i] + ds[i];
+    return (h < 0. ? 0. : h) * vol;
+  };
+  auto carried = [&](int f) -> double {  // P of face f (below cell f)
+    const double M = q[f];
+    return (M > 0. ? ratio(f - 1) : ratio(f)) * M;
+  };
+  double avail = held(il);
+  double plo = carried(il);
+  for (int i = il; i <= iu; ++i) {
+    double pup = carried(i + 1);
+    if (i + 1 <= iu) {  // an interior face: the donor cap
+      const double up = held(i + 1);
+      if (pup > avail) pup = avail;
+      if (pup < -up) pup = -up;
+      avail = up + pup;
+    }
+    const double d = ds[i] + (plo - pup) / vol;
+    so[i] = real(p.w0 * (double)s0[i] + p.w1 * (double)s[i] + p.w2 * d);
+    plo = pup;
+  }
+}
+
+
 // ---------------------------------------------------------------------------
 // the budget sums (BudgetConsumer::totals and ::boundary,
 // src/diagnostics/budget.cpp:68-155): one CTA per block, each thread sums a
@@ -1611,7 +1675,7 @@ extern "C" int SG_NAME(sg_launch_x3)(const BlockDev* tab, StageParams p,
 }
 
 extern "C" int SG_NAME(sg_launch_scalar)(const BlockDev* tab, StageParams p,
-                                         size_t max_plane,
+                                         size_t max_plane, size_t max_icols,
                                          cudaStream_t stream) {
   int gx = (int)((2 * max_plane + kThreads - 1) / kThreads);
   if (gx > 2048) gx = 2048;
@@ -1621,6 +1685,12 @@ extern "C" int SG_NAME(sg_launch_scalar)(const BlockDev* tab, StageParams p,
   int gu = (int)((max_plane + kThreads - 1) / kThreads);
   if (gu > 2048) gu = 2048;
   scalar_update_kernel<<<dim3(gu, p.nblock), kThreads, 0, stream>>>(tab, p);
+  if (max_icols > 0) {  // implicit blocks: the solve's transfer per column
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return (int)e;
+    const int gv = (int)((16 * max_icols + kThreads - 1) / kThreads);
+    scalar_vic_kernel<<<dim3(gv, p.nblock), kThreads, 0, stream>>>(tab, p);
+  }
   return (int)cudaGetLastError();
 }
 

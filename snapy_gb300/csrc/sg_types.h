@@ -78,6 +78,11 @@ struct BlockDev {
   void* sbuf[3];
   double* mflux[2];
   double* sflux[2];
+  // an implicit block's scalars: their transport tendency ds (nscalar rows,
+  // FP64) and the solve's clamped dry transfer q of each x1 face (the
+  // finish kernel's, face f below cell f), for the transfer's share
+  double* sds;
+  double* vicq;
 };
 
 // offsets into BlockDev::base

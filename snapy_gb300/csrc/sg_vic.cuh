@@ -1643,6 +1643,11 @@ __global__ void __launch_bounds__(NL == 32 ? 32 * kVicWarps : kThreads)
     }
     vsync<NL>();
   }
+  // passive scalars: the clamped dry transfer of each x1 face (zero for a
+  // failed column), for their share of it
+  if (B.nscalar > 0)
+    for (int f = lane; f <= n; f += NL)
+      B.vicq[jrow * nc1 + ng + f] = ok ? (double)mq[f] : 0.;
   // the x1 step field of an implicit block (FluxRegister::end_stage after
   // ImplicitHydroImpl::post_, src/implicit/implicit_hydro.cpp:625-673): the
   // stage's T_1 plus the solve's face transfers per unit area and time,

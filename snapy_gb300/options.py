@@ -400,9 +400,6 @@ def _scalar_names(node, op) -> List[str]:
         raise DeckError("scalar/reconstruct: only weno5 is built")
     if names:
         h, c = op.hydro(), op.coord()
-        if h.icorr is not None:
-            raise DeckError("scalar: passive scalars with the vertical implicit "
-                            "solve are not built (its tracer transfer)")
         if c.nx3 > 1:
             raise DeckError("scalar: passive scalars on 3-D blocks are not built")
         if h.eos.type == "shallow-water":

@@ -1,9 +1,10 @@
 """Passive scalars on the GPU (the scalar kernels through the C ABI) against
-the oracle's restatement of ScalarImpl::forward: FP64 within 1e-12 of the
-oracle per tracer and hydro field after 10 steps (explicit Straka, 2-D, and
-a 1-D tube), the reference's own properties on the device (a uniform ratio
-stays uniform, the tracer is conserved in a closed box), FP32 within 1e-5,
-and the refusals of what is not built."""
+the oracle's restatement of ScalarImpl::forward and of the scalars' share of
+the implicit solve's dry transfer: FP64 within 1e-12 of the oracle per
+tracer and hydro field after 10 steps (Straka explicit and with the solve,
+and a 1-D tube), the reference's own properties on the device (a uniform
+ratio stays uniform, the tracer is conserved in a closed box), FP32 within
+1e-5, and the refusals of what is not built."""
 import copy
 
 import numpy as np
@@ -20,14 +21,16 @@ pytestmark = pytest.mark.gpu
 INNER = (slice(None), slice(3, -3), slice(3, -3))
 
 
-def straka(precision="float64", nx1=32, nx2=48):
-    cfg = copy.deepcopy(sg.options.yaml_lite.load(
-        "snapy_gb300/decks/straka_noimplicit.yaml"))
+def straka(precision="float64", nx1=32, nx2=48, deck="straka_noimplicit.yaml",
+           implicit_precision=None):
+    cfg = copy.deepcopy(sg.options.yaml_lite.load("snapy_gb300/decks/" + deck))
     cfg["scalar"] = {"nvar": 2, "names": ["uniform", "step"]}
     opts = sg.MeshBlockOptions.from_config(cfg)
     c = opts.coord()
     c.nx1, c.nx2, c.x1max, c.x2max = nx1, nx2, nx1 * 50.0, nx2 * 50.0
     opts.hydro().precision = precision
+    if implicit_precision:
+        opts.hydro().icorr.precision = implicit_precision
     opts.execution = "eager"
     opts.autotune = False
     return opts
@@ -61,14 +64,17 @@ def rel(a, b):
     return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
 
 
-def test_fp64_scalars_against_oracle(oracle, cuda):
-    opts = straka()
+@pytest.mark.parametrize("deck", ["straka_noimplicit.yaml", "straka.yaml"])
+def test_fp64_scalars_against_oracle(oracle, cuda, deck):
+    """Explicit, and with the vertical implicit solve (the scalars' share of
+    its dry transfer)."""
+    opts = straka(deck=deck)
     blk, vars, u, s = run_pair(cuda, opts, oracle)
     got_s = vars["scalar_s"].double().cpu().numpy()
     got_u = blk.total_u(vars).double().cpu().numpy()
     es = [rel(got_s[v][INNER], s[v][INNER]) for v in range(2)]
     eu = [rel(got_u[v][INNER], u[v][INNER]) for v in range(5) if np.linalg.norm(u[v]) > 0]
-    print("\nFP64 scalars vs oracle, rel L2:", es, "hydro:", max(eu))
+    print(f"\n{deck}: FP64 scalars vs oracle, rel L2:", es, "hydro:", max(eu))
     assert max(es) <= 1e-12 and max(eu) <= 1e-12
     # the reference's properties, on the device's result
     ratio = got_s[0][INNER] / got_u[0][INNER]
@@ -108,12 +114,14 @@ def test_fp64_scalar_tube_against_oracle(oracle, cuda):
     assert e <= 1e-12
 
 
-def test_fp32_scalars_against_fp64_oracle(oracle, cuda):
-    opts = straka("float32")
+@pytest.mark.parametrize("deck,ip", [("straka_noimplicit.yaml", None),
+                                     ("straka.yaml", "float32")])
+def test_fp32_scalars_against_fp64_oracle(oracle, cuda, deck, ip):
+    opts = straka("float32", deck=deck, implicit_precision=ip)
     blk, vars, u, s = run_pair(cuda, opts, oracle)
     got_s = vars["scalar_s"].double().cpu().numpy()
     es = [rel(got_s[v][INNER], s[v][INNER]) for v in range(2)]
-    print("\nFP32 scalars vs FP64 oracle, rel L2:", es)
+    print(f"\n{deck}: FP32 scalars vs FP64 oracle, rel L2:", es)
     assert max(es) <= 1e-5
 
 
@@ -139,9 +147,9 @@ def test_graphs_and_redo_carry_the_scalars(cuda):
 
 
 def test_scalar_refusals(cuda):
-    cfg = copy.deepcopy(sg.options.yaml_lite.load("snapy_gb300/decks/straka.yaml"))
+    cfg = copy.deepcopy(sg.options.yaml_lite.load("snapy_gb300/decks/convection3d.yaml"))
     cfg["scalar"] = {"nvar": 1}
-    with pytest.raises(DeckError, match="implicit"):
+    with pytest.raises(DeckError, match="3-D"):
         sg.MeshBlockOptions.from_config(cfg)
     opts = straka()
     with pytest.raises(DeckError, match="scalars"):

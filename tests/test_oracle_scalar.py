@@ -15,15 +15,15 @@ from snapy_gb300.options import DeckError
 from oracle import oracle
 
 
-def straka_explicit(nx1=32, nx2=48):
-    opts = sg.MeshBlockOptions.from_yaml("snapy_gb300/decks/straka_noimplicit.yaml")
+def straka_explicit(nx1=32, nx2=48, deck="straka_noimplicit.yaml"):
+    opts = sg.MeshBlockOptions.from_yaml("snapy_gb300/decks/" + deck)
     c = opts.coord()
     c.nx1, c.nx2, c.x1max, c.x2max = nx1, nx2, nx1 * 50.0, nx2 * 50.0
     return opts
 
 
-def run(nsteps=10):
-    opts = straka_explicit()
+def run(nsteps=10, deck="straka_noimplicit.yaml"):
+    opts = straka_explicit(deck=deck)
     ob = oracle.block_from_options(opts)
     w = problems.straka(opts, "cpu", xc=1000.0, zc=1200.0, xr=800.0,
                         zr=600.0).numpy()
@@ -41,8 +41,11 @@ def run(nsteps=10):
     return ob, u, s, m0, vol, inner, top0
 
 
-def test_uniform_ratio_conservation_and_transport():
-    ob, u, s, m0, vol, inner, top0 = run()
+@pytest.mark.parametrize("deck", ["straka_noimplicit.yaml", "straka.yaml"])
+def test_uniform_ratio_conservation_and_transport(deck):
+    """Explicit, and with the vertical implicit solve (the tracer's share of
+    its dry transfer, donor-capped)."""
+    ob, u, s, m0, vol, inner, top0 = run(deck=deck)
     assert np.isfinite(s).all()
     ratio = s[0][inner] / u[0][inner]
     assert np.abs(ratio / 0.37 - 1).max() <= 1e-13
@@ -65,8 +68,7 @@ def test_deck_scalar_section():
         bad["scalar"][extra[0]] = extra[1]
         with pytest.raises(DeckError, match=word):
             sg.MeshBlockOptions.from_config(bad)
-    imp = sg.options.yaml_lite.load("snapy_gb300/decks/straka.yaml")
-    imp = copy.deepcopy(imp)
-    imp["scalar"] = {"nvar": 1}
-    with pytest.raises(DeckError, match="implicit"):
-        sg.MeshBlockOptions.from_config(imp)
+    d3 = copy.deepcopy(sg.options.yaml_lite.load("snapy_gb300/decks/convection3d.yaml"))
+    d3["scalar"] = {"nvar": 1}
+    with pytest.raises(DeckError, match="3-D"):
+        sg.MeshBlockOptions.from_config(d3)
