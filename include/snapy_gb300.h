@@ -104,7 +104,8 @@ typedef struct sg_block_desc {
   const double* base;
   /* integration/implicit-precision: SG_F64 (default) or SG_F32, which
    * assembles the implicit blocks in FP32 (SG_F32 storage only); the
-   * block-tridiagonal solve runs in FP64 either way */
+   * block-tridiagonal solve is refined to the FP64 solution (sg_set_solve,
+   * below) or is the direct FP64 solve */
   int32_t implicit_precision;
   /* scalar/nvar: passive scalars transported by the stage's mass flux
    * (ScalarImpl, src/scalar/scalar.cpp:90-211); 0 for none.  Built for 1-D

@@ -249,8 +249,9 @@ __device__ __forceinline__ VicK vic_krows(const BlockDev& B, int n, int k) {
 // entries and du[IPR] -= K du0[IDN]
 // the blocks of interior cell e (column e / n, layer e % n) in the compute
 // type T: double, or float under implicit-precision float32 (the FP32
-// state's blocks; the block-tridiagonal solve stays FP64).  The FP64
-// instantiation performs the reference's operations in its order.
+// state's blocks, exact in FP32 and in the FP64 copies the residuals of the
+// refined solve read).  The FP64 instantiation performs the reference's
+// operations in its order.
 template <typename T>
 __device__ __forceinline__ void vic_assemble_cell(const BlockDev& B,
                                                   const VicScratch& S,

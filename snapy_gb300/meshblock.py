@@ -117,7 +117,8 @@ def block_of(options: MeshBlockOptions, tj: int = 0) -> dict:
             "wb_wall_clamp": bool(h.extra.get("wb-wall-clamp", True)),
             "x1f": x1f, "x1v": x1v,
             "implicit_scheme": h.icorr.scheme if h.icorr else 0,
-            # FP32 assembly of the implicit blocks (the solve stays FP64)
+            # FP32 assembly of the implicit blocks (the solve is refined to,
+            # or is, the FP64 solve: sg_set_solve)
             "implicit_f32": bool(h.icorr) and h.icorr.precision == "float32",
             "nscalar": len(options.scalar_names)}
 
