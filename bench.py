@@ -95,6 +95,10 @@ def parse():
                          "the default) or direct (FP64 for every column)")
     ap.add_argument("--implicit-corrections", type=int, choices=[1, 2, 3],
                     default=None, help="the refined solve's corrections")
+    ap.add_argument("--scalars", type=int, default=0,
+                    help="Straka and Sod workloads: passive tracers carried "
+                         "(the reference's Straka deck carries one, "
+                         "scalar/names [tracer])")
     ap.add_argument("--requests", type=int, default=8,
                     help="serving: requests in the trace")
     ap.add_argument("--serve-steps", type=int, default=200,
@@ -114,6 +118,8 @@ def load_options(args):
         opts.implicit_solve = args.implicit_solve
     if args.implicit_corrections:
         opts.implicit_corrections = args.implicit_corrections
+    if getattr(args, "scalars", 0):
+        opts.scalar_names = [f"tracer{k}" for k in range(args.scalars)]
     return opts
 
 
@@ -152,6 +158,7 @@ def config_of(opts, workload, args, nranks):
         "gravity": bool(h.grav and h.grav.grav1),
         "implicit": bool(h.icorr),
         "implicit_solve": implicit_solve(opts),
+        "scalars": len(opts.scalar_names),
         "l2": "flushed between timed steps (512 MiB write; the block fits in L2)",
         "graphs": "one per buffer rotation, captured before the warm-up steps",
         "replicas": nranks,
@@ -396,6 +403,15 @@ def run_native(args):
     blk = sg.MeshBlock(opts).to(dev)
     w = initial_state(opts, args.workload, dev)
     vars = {"hydro_w": w}
+    if opts.scalar_names:
+        # each tracer's ratio: a smooth field that varies along x1 and x2
+        ns = len(opts.scalar_names)
+        z = torch.linspace(0.0, 1.0, c.nc1, dtype=torch.float64, device=dev)
+        x = torch.linspace(0.0, 1.0, c.nc2, dtype=torch.float64, device=dev)
+        r = torch.stack([(1e-3 * (k + 1)) * (1.0 + 0.5 * torch.sin(6.0 * z)[None, :]
+                                              * torch.cos(4.0 * x)[:, None])
+                         for k in range(ns)])
+        vars["scalar_r"] = r.unsqueeze(1).expand(ns, c.nc3, c.nc2, c.nc1).contiguous()
     blk.initialize(vars)
     dt = blk.max_time_step(vars)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
@@ -453,6 +469,10 @@ def run_native(args):
         "vic_solve_kernel": solve_phase(opts)[1] * cells,
         "vic_finish_kernel": (120 + 15 * s_bytes) * cells,
         "ghost_kernel": 2 * 5 * s_bytes * ghost_cells,
+        # per tracer: s read twice (faces, update) and s0, s_out written, the
+        # two FP64 face fluxes written and read; the mass fluxes and rho once
+        "scalar_kernel": (len(opts.scalar_names) * (4 * s_bytes + 32) +
+                          16 + s_bytes) * cells,
     }
     dom = max(kt, key=lambda k: kt[k][0])
     dom_ms, dom_n = kt[dom]
@@ -463,20 +483,25 @@ def run_native(args):
                    "bytes_per_launch": per_launch.get(k)}
                for k, (ms, n) in kt.items()}
 
-    # end to end through the public API with host buffers
-    u_host = torch.empty(vars["hydro_u"].shape, dtype=blk.dtype).pin_memory()
-    u_host.copy_(vars["hydro_u"].cpu())
+    # end to end through the public API with host buffers (the tracers'
+    # densities too, when carried)
+    keys = ["hydro_u"] + (["scalar_s"] if "scalar_s" in vars else [])
+    hosts = {k: torch.empty(vars[k].shape, dtype=blk.dtype).pin_memory() for k in keys}
+    for k in keys:
+        hosts[k].copy_(vars[k].cpu())
     e2e_steps = max(5, min(args.steps, 100))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        vars["hydro_u"].copy_(u_host, non_blocking=True)
+        for k in keys:
+            vars[k].copy_(hosts[k], non_blocking=True)
         blk.step(vars, dt)
-        u_host.copy_(vars["hydro_u"], non_blocking=True)
+        for k in keys:
+            hosts[k].copy_(vars[k], non_blocking=True)
     torch.cuda.synchronize()
     e2e_t = time.perf_counter() - t0
     e2e_t = ranks.max(e2e_t)
-    nbytes = u_host.numel() * u_host.element_size()
+    nbytes = sum(h.numel() * h.element_size() for h in hosts.values())
 
     rep = blk.execution_report()
     line = None

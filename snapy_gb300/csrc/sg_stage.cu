@@ -1450,15 +1450,21 @@ __global__ void __launch_bounds__(kThreads)
 
 #include "sg_vic.cuh"
 
-// an implicit block's scalars after its solve, one thread per column and
+// an implicit block's scalars after its solve, one warp per column and
 // scalar (MeshBlockImpl::stage_advance, src/mesh/meshblock_advance.cpp:
 // 216-233): each x1 face's transfer q carries the donor's ratio r = s / rho
-// of the stage input (the cell below where q > 0), P = r q; along the column
-// from the bottom each interior face's P is capped to [-held above, held
-// below + the face below's P], held = max(s + ds, 0) V (donor_cap_cpu,
-// src/implicit/implicit_dispatch.cpp:54-70); then ds += (P - P_above) / V
-// and the stage's combine
-__global__ void __launch_bounds__(kThreads)
+// of the stage input (the cell below where q > 0), P = r q.  The donor cap
+// (donor_cap_cpu, src/implicit/implicit_dispatch.cpp:54-70) is tested on
+// every interior face at once: P above held below + the face below's P, or
+// under -held above, held = max(s + ds, 0) V; only a column where a face
+// binds walks from the bottom capping each face to [-held above, what the
+// cell below holds plus what it received].  A column with no binding face
+// is left as it is, as the reference's walk leaves it.  Then
+// ds += (P - P_above) / V and the stage's combine, coalesced over the
+// column.  P is kept in the x1 face-flux rows, which the update has read
+constexpr int kVicScalarWarps = 4;
+
+__global__ void __launch_bounds__(32 * kVicScalarWarps)
     scalar_vic_kernel(const BlockDev* __restrict__ tab, StageParams p) {
   const BlockDev& B = tab[blockIdx.y];
   const int ns = B.nscalar;
@@ -1467,18 +1473,20 @@ __global__ void __launch_bounds__(kThreads)
   const size_t plane = (size_t)nc1 * B.nc2 * B.nc3;
   const size_t ncol = (size_t)(B.nc2 > 1 ? B.nc2 - 2 * ng : 1) *
                       (B.nc3 > 1 ? B.nc3 - 2 * ng : 1);
-  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= ncol * ns) return;
-  const int v = (int)(t / ncol);
-  const size_t col = t - (size_t)v * ncol;
+  const int lane = threadIdx.x & 31;
+  const size_t task = (size_t)blockIdx.x * kVicScalarWarps + (threadIdx.x >> 5);
+  if (task >= ncol * ns) return;  // the whole warp
+  const int v = (int)(task / ncol);
+  const size_t col = task - (size_t)v * ncol;
   const size_t row = vic_row(B, col) * nc1;
   const real* s = static_cast<const real*>(B.sbuf[p.in]) + v * plane + row;
   const real* s0 = static_cast<const real*>(B.sbuf[p.u0]) + v * plane + row;
   real* so = static_cast<real*>(B.sbuf[p.out]) + v * plane + row;
   const real* u = static_cast<const real*>(B.buf[p.in]) + IDN * plane + row;
   const double* rb = B.base ? base_rho(B.base, nc1) : nullptr;
-  double* ds = B.sds + v * plane + row;
+  const double* ds = B.sds + v * plane + row;
   const double* q = B.vicq + row;
+  double* P = B.sflux[0] + v * plane + row;
   const double vol = B.dx3 * (B.dx2 * B.dx1);
   const int il = ng, iu = ng + n - 1;
   auto ratio = [&](int i) -> double {
@@ -1490,23 +1498,33 @@ __global__ void __launch_bounds__(kThreads)
     const double h = (double)s[i] + ds[i];
     return (h < 0. ? 0. : h) * vol;
   };
-  auto carried = [&](int f) -> double {  // P of face f (below cell f)
+  for (int f = il + lane; f <= iu + 1; f += 32) {
     const double M = q[f];
-    return (M > 0. ? ratio(f - 1) : ratio(f)) * M;
-  };
-  double avail = held(il);
-  double plo = carried(il);
-  for (int i = il; i <= iu; ++i) {
-    double pup = carried(i + 1);
-    if (i + 1 <= iu) {  // an interior face: the donor cap
-      const double up = held(i + 1);
-      if (pup > avail) pup = avail;
-      if (pup < -up) pup = -up;
-      avail = up + pup;
+    P[f] = (M > 0. ? ratio(f - 1) : ratio(f)) * M;
+  }
+  __syncwarp();
+  bool bind = false;
+  for (int f = il + 1 + lane; f <= iu; f += 32) {
+    const double cap = held(f - 1) + (f - 1 > il ? P[f - 1] : 0.);
+    bind = bind || P[f] > cap || P[f] < -held(f);
+  }
+  if (__any_sync(0xffffffffu, bind)) {
+    if (lane == 0) {
+      double avail = held(il);
+      for (int f = il + 1; f <= iu; ++f) {
+        const double up = held(f);
+        double Q = P[f];
+        if (Q > avail) Q = avail;
+        if (Q < -up) Q = -up;
+        P[f] = Q;
+        avail = up + Q;
+      }
     }
-    const double d = ds[i] + (plo - pup) / vol;
+    __syncwarp();
+  }
+  for (int i = il + lane; i <= iu; i += 32) {
+    const double d = ds[i] + (P[i] - P[i + 1]) / vol;
     so[i] = real(p.w0 * (double)s0[i] + p.w1 * (double)s[i] + p.w2 * d);
-    plo = pup;
   }
 }
 
@@ -1688,8 +1706,9 @@ extern "C" int SG_NAME(sg_launch_scalar)(const BlockDev* tab, StageParams p,
   if (max_icols > 0) {  // implicit blocks: the solve's transfer per column
     e = cudaGetLastError();
     if (e != cudaSuccess) return (int)e;
-    const int gv = (int)((16 * max_icols + kThreads - 1) / kThreads);
-    scalar_vic_kernel<<<dim3(gv, p.nblock), kThreads, 0, stream>>>(tab, p);
+    const int gv = (int)((16 * max_icols + kVicScalarWarps - 1) / kVicScalarWarps);
+    scalar_vic_kernel<<<dim3(gv, p.nblock), 32 * kVicScalarWarps, 0, stream>>>(
+        tab, p);
   }
   return (int)cudaGetLastError();
 }
