@@ -30,9 +30,6 @@ class Ensemble:
         if not members:
             raise ValueError("an ensemble needs at least one member")
         self.members = list(members)
-        if any(m.scalar_names for m in self.members):
-            raise DeckError("Ensemble: members with passive scalars are not "
-                            "built; step them as MeshBlocks")
         schemes = [scheme_of(m) for m in self.members]
         if any(s != schemes[0] for s in schemes[1:]):
             raise DeckError("ensemble members must share one scheme (solver, "
@@ -74,9 +71,12 @@ class Ensemble:
             n += c.nx1 * c.nx2 * c.nx3
         return n
 
-    def initialize(self, ws: List[torch.Tensor], autotune: Optional[bool] = None) -> None:
-        """The members' initial primitives; then (autotune None: as the first
-        member's integration/autotune) the schedule autotuner on the batch."""
+    def initialize(self, ws: List[torch.Tensor], autotune: Optional[bool] = None,
+                   rs: Optional[List[Optional[torch.Tensor]]] = None) -> None:
+        """The members' initial primitives (and, for members with passive
+        scalars, their ratios rs[k], scalar_s = rho r as MeshBlock.initialize
+        sets it); then (autotune None: as the first member's
+        integration/autotune) the schedule autotuner on the batch."""
         ws = [w.to(self.device, torch.float64).contiguous() for w in ws]
         with torch.cuda.device(self.device):
             self.batch.init_from_prim(ws)
@@ -84,7 +84,23 @@ class Ensemble:
                 self.batch.autotune()
                 self._graphs.clear()
                 self._seen.clear()
+            if any(m.scalar_names for m in self.members):
+                for k, m in enumerate(self.members):
+                    if not m.scalar_names:
+                        continue
+                    r = rs[k] if rs is not None else None
+                    if r is None:
+                        raise RuntimeError(f"initialize: member {k} needs its "
+                                           "scalar_r")
+                    s = ws[k][0].unsqueeze(0) * r.to(self.device, torch.float64)
+                    self.batch.current_scalars(k).copy_(s.to(self.dtype))
+                self.batch.fill_ghosts()
         self.time.zero_()
+
+    def scalars(self, k: int) -> Optional[torch.Tensor]:
+        """Member k's current tracer densities (a view of block storage), or
+        None without scalars."""
+        return self.batch.current_scalars(k)
 
     def state(self, k: int) -> torch.Tensor:
         """The current conserved state of member k (a view of block storage)."""
