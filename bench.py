@@ -119,7 +119,9 @@ def load_options(args):
     if args.implicit_corrections:
         opts.implicit_corrections = args.implicit_corrections
     if getattr(args, "scalars", 0):
+        # tracers are built without the x2 flux-covariance row
         opts.scalar_names = [f"tracer{k}" for k in range(args.scalars)]
+        opts.hydro().flux_covariance = False
     return opts
 
 
@@ -159,6 +161,7 @@ def config_of(opts, workload, args, nranks):
         "implicit": bool(h.icorr),
         "implicit_solve": implicit_solve(opts),
         "scalars": len(opts.scalar_names),
+        "flux_covariance": bool(opts.hydro().flux_covariance),
         "l2": "flushed between timed steps (512 MiB write; the block fits in L2)",
         "graphs": "one per buffer rotation, captured before the warm-up steps",
         "replicas": nranks,

@@ -667,10 +667,10 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
       sg_destroy(h);
       return fail(SG_ERR_ARG, "block %d: nscalar %d (0 to 16)", b, d.nscalar);
     }
-    if (d.nscalar > 0 && d.nc3 > 1) {
+    if (d.nscalar > 0 && (d.nc3 > 1 || (d.flux_cov && d.nc2 > 1))) {
       sg_destroy(h);
       return fail(SG_ERR_UNSUPPORTED, "block %d: passive scalars are built for "
-                  "1-D and 2-D blocks", b);
+                  "1-D and 2-D blocks without the x2 flux-covariance row", b);
     }
     B.nscalar = d.nscalar;
     if (d.nscalar > 0) h->scalars = true;

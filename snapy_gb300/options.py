@@ -402,6 +402,11 @@ def _scalar_names(node, op) -> List[str]:
         h, c = op.hydro(), op.coord()
         if c.nx3 > 1:
             raise DeckError("scalar: passive scalars on 3-D blocks are not built")
+        if c.nx2 > 1 and h.flux_covariance:
+            raise DeckError("scalar: passive scalars with the x2 flux-covariance "
+                            "row are not built (the scalar's covariance row and "
+                            "the positivity limiter it brings); set "
+                            "dynamics/flux-covariance: false")
         if h.eos.type == "shallow-water":
             raise DeckError("scalar: passive scalars need a dry-air density")
     return names

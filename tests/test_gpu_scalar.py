@@ -25,6 +25,7 @@ def straka(precision="float64", nx1=32, nx2=48, deck="straka_noimplicit.yaml",
            implicit_precision=None):
     cfg = copy.deepcopy(sg.options.yaml_lite.load("snapy_gb300/decks/" + deck))
     cfg["scalar"] = {"nvar": 2, "names": ["uniform", "step"]}
+    cfg["dynamics"]["flux-covariance"] = False
     opts = sg.MeshBlockOptions.from_config(cfg)
     c = opts.coord()
     c.nx1, c.nx2, c.x1max, c.x2max = nx1, nx2, nx1 * 50.0, nx2 * 50.0
@@ -150,6 +151,10 @@ def test_scalar_refusals(cuda):
     cfg = copy.deepcopy(sg.options.yaml_lite.load("snapy_gb300/decks/convection3d.yaml"))
     cfg["scalar"] = {"nvar": 1}
     with pytest.raises(DeckError, match="3-D"):
+        sg.MeshBlockOptions.from_config(cfg)
+    cfg = copy.deepcopy(sg.options.yaml_lite.load("snapy_gb300/decks/straka.yaml"))
+    cfg["scalar"] = {"nvar": 1}
+    with pytest.raises(DeckError, match="flux-covariance"):
         sg.MeshBlockOptions.from_config(cfg)
     opts = straka()
     blk = sg.MeshBlock(opts).to(cuda)

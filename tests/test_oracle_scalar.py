@@ -16,7 +16,9 @@ from oracle import oracle
 
 
 def straka_explicit(nx1=32, nx2=48, deck="straka_noimplicit.yaml"):
-    opts = sg.MeshBlockOptions.from_yaml("snapy_gb300/decks/" + deck)
+    cfg = copy.deepcopy(sg.options.yaml_lite.load("snapy_gb300/decks/" + deck))
+    cfg["dynamics"]["flux-covariance"] = False
+    opts = sg.MeshBlockOptions.from_config(cfg)
     c = opts.coord()
     c.nx1, c.nx2, c.x1max, c.x2max = nx1, nx2, nx1 * 50.0, nx2 * 50.0
     return opts
@@ -58,6 +60,11 @@ def test_uniform_ratio_conservation_and_transport(deck):
 def test_deck_scalar_section():
     cfg = sg.options.yaml_lite.load("snapy_gb300/decks/straka_noimplicit.yaml")
     cfg = copy.deepcopy(cfg)
+    cov = copy.deepcopy(cfg)
+    cov["scalar"] = {"nvar": 1}
+    with pytest.raises(DeckError, match="flux-covariance"):
+        sg.MeshBlockOptions.from_config(cov)
+    cfg["dynamics"]["flux-covariance"] = False
     cfg["scalar"] = {"nvar": 1, "names": ["tracer"]}
     assert sg.MeshBlockOptions.from_config(cfg).scalar_names == ["tracer"]
     cfg["scalar"] = {"nvar": 2}
