@@ -1208,11 +1208,13 @@ static void scalar_vic(const og_block* b, const double* u, const double* s,
   const size_t nc = ncell(b);
   const int il = ng, iu = n1 - ng - 1;
   const int jl = n2 > 1 ? ng : 0, ju1 = n2 > 1 ? n2 - ng : 1;
+  const int n3 = b->nc3, kl = n3 > 1 ? ng : 0, ku1 = n3 > 1 ? n3 - ng : 1;
   const double vol = b->dx3 * (b->dx2 * b->dx1);
   double* P = (double*)malloc(sizeof(double) * (n1 + 1));
   for (int v = 0; v < ns; ++v)
+    for (int k = kl; k < ku1; ++k)
     for (int j = jl; j < ju1; ++j) {
-      const size_t c = (size_t)j * n1;
+      const size_t c = ((size_t)k * n2 + j) * n1;
       const double* sv = s + v * nc + c;
       double* dv = ds + v * nc + c;
       const double* rho = u + OG_IDN * nc + c;

@@ -1056,13 +1056,15 @@ __global__ void __launch_bounds__(kThreads)
   const BlockDev& B = tab[blockIdx.y];
   const int ns = B.nscalar;
   if (ns == 0) return;
-  const int nc1 = B.nc1, nc2 = B.nc2, ng = B.ng;
-  const bool has2 = nc2 > 1;
-  const size_t plane = (size_t)nc1 * nc2;
-  const int nx1 = nc1 - 2 * ng, nx2 = has2 ? nc2 - 2 * ng : 1;
-  const int jl = has2 ? ng : 0;
-  const size_t n1f = (size_t)nx2 * (nx1 + 1);
-  const size_t n2f = has2 ? (size_t)(nx2 + 1) * nx1 : 0;
+  const int nc1 = B.nc1, nc2 = B.nc2, nc3 = B.nc3, ng = B.ng;
+  const bool has2 = nc2 > 1, has3 = nc3 > 1;
+  const size_t kst = (size_t)nc1 * nc2, plane = kst * nc3;
+  const int nx1 = nc1 - 2 * ng, nx2 = has2 ? nc2 - 2 * ng : 1,
+            nx3 = has3 ? nc3 - 2 * ng : 1;
+  const int jl = has2 ? ng : 0, kl = has3 ? ng : 0;
+  const size_t n1f = (size_t)nx3 * nx2 * (nx1 + 1);
+  const size_t n2f = has2 ? (size_t)nx3 * (nx2 + 1) * nx1 : 0;
+  const size_t n3f = has3 ? (size_t)(nx3 + 1) * nx2 * nx1 : 0;
   const real* u = static_cast<const real*>(B.buf[p.in]);
   const real* s = static_cast<const real*>(B.sbuf[p.in]);
   const double* rb = B.base ? base_rho(B.base, nc1) : nullptr;
@@ -1072,22 +1074,34 @@ __global__ void __launch_bounds__(kThreads)
     if (rb) v = v + real(rb[c % nc1]);
     return v;
   };
-  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n1f + n2f;
-       t += (size_t)gridDim.x * blockDim.x) {
-    int d, i, j;  // the face along d below cell (j, i)
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+       t < n1f + n2f + n3f; t += (size_t)gridDim.x * blockDim.x) {
+    int d, i, j, k;  // the face along d below cell (k, j, i)
     if (t < n1f) {
       d = 0;
-      j = jl + (int)(t / (nx1 + 1));
       i = ng + (int)(t % (nx1 + 1));
-    } else {
+      const size_t r = t / (nx1 + 1);
+      j = jl + (int)(r % nx2);
+      k = kl + (int)(r / nx2);
+    } else if (t < n1f + n2f) {
       const size_t e = t - n1f;
       d = 1;
-      j = ng + (int)(e / nx1);
       i = ng + (int)(e % nx1);
+      const size_t r = e / nx1;
+      j = ng + (int)(r % (nx2 + 1));
+      k = kl + (int)(r / (nx2 + 1));
+    } else {
+      const size_t e = t - n1f - n2f;
+      d = 2;
+      i = ng + (int)(e % nx1);
+      const size_t r = e / nx1;
+      j = jl + (int)(r % nx2);
+      k = ng + (int)(r / nx2);
     }
-    const size_t q = (size_t)j * nc1 + i;
-    const size_t st = d == 0 ? 1 : (size_t)nc1;
-    const int f = d == 0 ? i : j, nd = d == 0 ? nc1 : nc2;
+    const size_t q = (size_t)k * kst + (size_t)j * nc1 + i;
+    const size_t st = d == 0 ? 1 : (d == 1 ? (size_t)nc1 : kst);
+    const int f = d == 0 ? i : (d == 1 ? j : k);
+    const int nd = d == 0 ? nc1 : (d == 1 ? nc2 : nc3);
     const bool wall = (f == ng && B.bc[2 * d] == kBcReflecting) ||
                       (f == nd - ng && B.bc[2 * d + 1] == kBcReflecting);
     const double F = B.mflux[d][q];
@@ -1118,29 +1132,36 @@ __global__ void __launch_bounds__(kThreads)
   const BlockDev& B = tab[blockIdx.y];
   const int ns = B.nscalar;
   if (ns == 0) return;
-  const int nc1 = B.nc1, nc2 = B.nc2, ng = B.ng;
-  const bool has2 = nc2 > 1;
-  const size_t plane = (size_t)nc1 * nc2;
-  const int nx1 = nc1 - 2 * ng, nx2 = has2 ? nc2 - 2 * ng : 1;
-  const int jl = has2 ? ng : 0;
-  const double a1 = B.dx3 * B.dx2, a2 = B.dx3 * B.dx1;
+  const int nc1 = B.nc1, nc2 = B.nc2, nc3 = B.nc3, ng = B.ng;
+  const bool has2 = nc2 > 1, has3 = nc3 > 1;
+  const size_t kst = (size_t)nc1 * nc2, plane = kst * nc3;
+  const int nx1 = nc1 - 2 * ng, nx2 = has2 ? nc2 - 2 * ng : 1,
+            nx3 = has3 ? nc3 - 2 * ng : 1;
+  const int jl = has2 ? ng : 0, kl = has3 ? ng : 0;
+  const double a1 = B.dx3 * B.dx2, a2 = B.dx3 * B.dx1, a3 = B.dx2 * B.dx1;
   const double vol = B.dx3 * (B.dx2 * B.dx1);
   const double mdt = -p.dt[blockIdx.y];
   const real* s0 = static_cast<const real*>(B.sbuf[p.u0]);
   const real* s = static_cast<const real*>(B.sbuf[p.in]);
   real* so = static_cast<real*>(B.sbuf[p.out]);
-  const size_t ncell = (size_t)nx1 * nx2 * ns;
-  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < ncell;
-       t += (size_t)gridDim.x * blockDim.x) {
-    const int v = (int)(t / ((size_t)nx1 * nx2));
-    const size_t e = t - (size_t)v * nx1 * nx2;
-    const int j = jl + (int)(e / nx1), i = ng + (int)(e % nx1);
-    const size_t q = (size_t)v * plane + (size_t)j * nc1 + i;
+  const size_t inner = (size_t)nx1 * nx2 * nx3;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+       t < inner * ns; t += (size_t)gridDim.x * blockDim.x) {
+    const int v = (int)(t / inner);
+    const size_t e = t - (size_t)v * inner;
+    const int i = ng + (int)(e % nx1);
+    const size_t r = e / nx1;
+    const int j = jl + (int)(r % nx2), k = kl + (int)(r / nx2);
+    const size_t q = (size_t)v * plane + (size_t)k * kst + (size_t)j * nc1 + i;
     const double* F1 = B.sflux[0];
     double dv = a1 * F1[q + 1] - a1 * F1[q];
     if (has2) {
       const double* F2 = B.sflux[1];
       dv = dv + (a2 * F2[q + nc1] - a2 * F2[q]);
+    }
+    if (has3) {
+      const double* F3 = B.sflux[2];
+      dv = dv + (a3 * F3[q + kst] - a3 * F3[q]);
     }
     const double ds = mdt * (dv / vol);
     if (B.implicit)
@@ -1245,6 +1266,9 @@ __global__ void __launch_bounds__(kThreads)
         riemann<RK>(wl, wr, gammad, 3, flx);
       if ((f == ng && wlo) || (f == ng + nx3 && whi))
         flx[IDN] = flx[IPR] = real(0);
+      // passive scalars ride on the mass row (the step field's owner rule)
+      if (B.nscalar > 0 && (f < k1 || k1 == ng + nx3))
+        B.mflux[2][(size_t)f * kst + col] = (double)flx[IDN];
       // the x3 step field; a chunk owns its faces but the top one, which
       // the next chunk owns, except the block's last face
       if (B.step[2] && (f < k1 || k1 == ng + nx3)) {
@@ -1695,7 +1719,7 @@ extern "C" int SG_NAME(sg_launch_x3)(const BlockDev* tab, StageParams p,
 extern "C" int SG_NAME(sg_launch_scalar)(const BlockDev* tab, StageParams p,
                                          size_t max_plane, size_t max_icols,
                                          cudaStream_t stream) {
-  int gx = (int)((2 * max_plane + kThreads - 1) / kThreads);
+  int gx = (int)((3 * max_plane + kThreads - 1) / kThreads);
   if (gx > 2048) gx = 2048;
   scalar_flux_kernel<<<dim3(gx, p.nblock), kThreads, 0, stream>>>(tab, p);
   cudaError_t e = cudaGetLastError();

@@ -71,13 +71,14 @@ struct BlockDev {
   double* step[3];
   double* t1;
   // passive scalars: their three buffers (nscalar, nc3, nc2, nc1) in the
-  // storage type, rotated with buf; the stage's FP64 mass flux along x1 and
-  // x2 (face f below cell f, written by the stage kernel) and the scalars'
-  // FP64 face fluxes (nscalar rows of the same layout), in the scratch
+  // storage type, rotated with buf; the stage's FP64 mass flux along x1, x2
+  // and x3 (face f below cell f, written by the stage kernel and the x3
+  // sweep) and the scalars' FP64 face fluxes (nscalar rows of the same
+  // layout), in the scratch
   int32_t nscalar;
   void* sbuf[3];
-  double* mflux[2];
-  double* sflux[2];
+  double* mflux[3];
+  double* sflux[3];
   // an implicit block's scalars: their transport tendency ds (nscalar rows,
   // FP64) and the solve's clamped dry transfer q of each x1 face (the
   // finish kernel's, face f below cell f), for the transfer's share

@@ -148,10 +148,6 @@ def test_graphs_and_redo_carry_the_scalars(cuda):
 
 
 def test_scalar_refusals(cuda):
-    cfg = copy.deepcopy(sg.options.yaml_lite.load("snapy_gb300/decks/convection3d.yaml"))
-    cfg["scalar"] = {"nvar": 1}
-    with pytest.raises(DeckError, match="3-D"):
-        sg.MeshBlockOptions.from_config(cfg)
     cfg = copy.deepcopy(sg.options.yaml_lite.load("snapy_gb300/decks/straka.yaml"))
     cfg["scalar"] = {"nvar": 1}
     with pytest.raises(DeckError, match="flux-covariance"):
@@ -186,3 +182,35 @@ def test_ensemble_member_alone_equals_in_the_batch(cuda):
             blk.step(vars, float(dt[k]))
         assert torch.equal(ens.scalars(k), vars["scalar_s"]), k
         assert torch.equal(ens.state(k), vars["hydro_u"]), k
+
+
+def test_3d_scalars_against_oracle(oracle, cuda):
+    """A 3-D convection block (the serving deck, its vertical implicit solve
+    on the (x2, x3) columns) with a tracer: FP64 bitwise with the oracle."""
+    cfg = copy.deepcopy(sg.options.yaml_lite.load("snapy_gb300/decks/convection3d.yaml"))
+    cfg["scalar"] = {"nvar": 1}
+    opts = sg.MeshBlockOptions.from_config(cfg)
+    c = opts.coord()
+    c.nx1, c.nx2, c.nx3 = 16, 12, 10
+    c.x1max, c.x2max, c.x3max = 16 * 50.0, 12 * 50.0, 10 * 50.0
+    opts.hydro().precision = "float64"
+    opts.execution = "eager"
+    opts.autotune = False
+    w = problems.convection3d(opts, "cpu", seed=7)
+    z = np.linspace(0.0, 1.0, c.nc1)[None, None, None, :]
+    r = (1e-3 * (1.0 + 0.5 * np.sin(5.0 * z))) * np.ones((1, c.nc3, c.nc2, c.nc1))
+    blk = sg.MeshBlock(opts).to(cuda)
+    vars = {"hydro_w": w.to(cuda), "scalar_r": torch.from_numpy(r).to(cuda)}
+    blk.initialize(vars)
+    ob = oracle.block_from_options(opts)
+    u = ob.initialize(w.numpy())
+    s = ob.set_scalars(u[0] * r)
+    for _ in range(4):
+        dt = blk.max_time_step(vars)
+        blk.step(vars, dt)
+        ob.step(u, dt)
+    got = vars["scalar_s"].double().cpu().numpy()
+    inner = (slice(None), slice(3, -3), slice(3, -3), slice(3, -3))
+    e = rel(got[inner], s[inner])
+    print(f"\n3-D tracer vs oracle: rel L2 {e:.2e}")
+    assert e <= 1e-12

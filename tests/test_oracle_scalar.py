@@ -77,5 +77,4 @@ def test_deck_scalar_section():
             sg.MeshBlockOptions.from_config(bad)
     d3 = copy.deepcopy(sg.options.yaml_lite.load("snapy_gb300/decks/convection3d.yaml"))
     d3["scalar"] = {"nvar": 1}
-    with pytest.raises(DeckError, match="3-D"):
-        sg.MeshBlockOptions.from_config(d3)
+    assert sg.MeshBlockOptions.from_config(d3).scalar_names == ["scalar0"]
