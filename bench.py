@@ -20,9 +20,9 @@ on the host), dt fixed at the CFL step of the initial state.
 * cpu_baseline: the CPU oracle (the reference algorithm restated in C, FP64,
   OpenMP on every host core) on a bounded sample of the same workload.
 
---impl reference times that CPU path alone (the reference itself cannot be
-built here or on the GPU machine) and prints the same line with
-"impl": "reference".
+--impl reference times that CPU path alone (the reference itself, a libtorch
+C++ build with external dependencies, is not built on either machine) and
+prints the same line with "impl": "reference".
 Under torchrun (N > 1) every rank advances its own replica of the workload
 (the blocks are independent: replicas only), value = all ranks' cell-updates
 / the slowest rank's time.
