@@ -79,3 +79,37 @@ def test_refined_run_against_fp64_oracle(oracle, cuda):
           np.array2string(np.array(err), precision=2))
     assert max(err) <= 1e-5
     assert blk.batch.solve_fallbacks()[0] <= 10 * 3 * opts.coord().nx2 // 20
+
+
+def test_refined_solution_on_3d_columns(cuda):
+    """A 3-D convection block (the serving deck: FP32 state, implicit-precision
+    float32, the solve on the (x2, x3) columns): the refined solution equals
+    the direct FP64 one to FP64 roundoff, with few columns left to it."""
+    opts = sg.MeshBlockOptions.from_yaml("snapy_gb300/decks/convection3d.yaml")
+    c = opts.coord()
+    c.nx1, c.nx2, c.nx3 = 24, 12, 10
+    c.x1max, c.x2max, c.x3max = 24 * 50.0, 12 * 50.0, 10 * 50.0
+    opts.hydro().precision = "float32"
+    opts.hydro().icorr.precision = "float32"
+    opts.execution = "eager"
+    opts.autotune = False
+    w = problems.convection3d(opts, "cpu", seed=11)
+    cells = c.nx1 * c.nx2 * c.nx3
+    out = []
+    for k in (2, 0):
+        blk = sg.MeshBlock(opts).to(cuda)
+        vars = {"hydro_w": w.to(cuda)}
+        blk.initialize(vars)
+        blk.batch.set_solve(k)
+        dt = blk.max_time_step(vars)
+        blk.forward(vars, dt, 0)
+        torch.cuda.synchronize()
+        out.append((blk.batch.scratch[0][85 * cells:90 * cells].clone(),
+                    blk.batch.solve_fallbacks()[0]))
+    (Dr, fell), (Dd, none) = out
+    rel = (torch.linalg.norm(Dr - Dd) / torch.linalg.norm(Dd)).item()
+    ncol = c.nx2 * c.nx3
+    print(f"\n3-D refined vs direct FP64 solve: rel L2 {rel:.2e}, {fell} of "
+          f"{ncol} columns left to the direct solve")
+    assert none == 0 and 0 <= fell <= ncol // 20
+    assert rel <= 1e-13
