@@ -1195,7 +1195,7 @@ union __align__(16) CorrSlot {
   } f;  // forward
   struct {
     float cp[kCorrCols][kBlk32];
-    float y[32][5];
+    float y[kCorrCols][kRRow];  // the column's y rows, as the forward r
     double x[32][5];
   } g;  // back
 };
@@ -1208,11 +1208,6 @@ __device__ __forceinline__ void cpa16(void* s, const void* g) {
 __device__ __forceinline__ void cpa8(void* s, const void* g) {
   const unsigned a = static_cast<unsigned>(__cvta_generic_to_shared(s));
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(a), "l"(g)
-               : "memory");
-}
-__device__ __forceinline__ void cpa4(void* s, const void* g) {
-  const unsigned a = static_cast<unsigned>(__cvta_generic_to_shared(s));
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(a), "l"(g)
                : "memory");
 }
 __device__ __forceinline__ void cpa_commit() {
@@ -1351,15 +1346,15 @@ __global__ void __launch_bounds__(32 * kCorrWarps)
   auto bissue = [&](int j) {
     const int i = n - 2 - j;
     CorrSlot& s = sl[j % kCorrRing];
-    if (live)
+    if (live) {
       for (int e = k; e < kBlk32 / 4; e += 3)
         cpa16(&s.g.cp[cs][4 * e], CP + i * kBlk32 + 4 * e);
+      for (int e = k; e < kR32 / 4; e += 3)
+        cpa16(&s.g.y[cs][4 * e], R + i * kR32 + 4 * e);
+    }
     if (act) {
 #pragma unroll
-      for (int r = 0; r < 5; ++r) {
-        cpa4(&s.g.y[lane][r], R + i * kR32 + k * 5 + r);
-        cpa8(&s.g.x[lane][r], X + i * 5 + r);
-      }
+      for (int r = 0; r < 5; ++r) cpa8(&s.g.x[lane][r], X + i * 5 + r);
     }
   };
 #pragma unroll
@@ -1379,7 +1374,7 @@ __global__ void __launch_bounds__(32 * kCorrWarps)
       float t[5];
 #pragma unroll
       for (int r = 0; r < 5; ++r) {
-        float u = s.g.y[lane][r];
+        float u = s.g.y[cs][k * 5 + r];
 #pragma unroll
         for (int q = 0; q < 5; ++q) u = fmaf(-cp[r * 5 + q], y[q], u);
         t[r] = u;
