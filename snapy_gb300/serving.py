@@ -52,6 +52,9 @@ class Request:
     done: Optional[float] = None
     result: Optional[torch.Tensor] = None  # the final stored state (host)
     flags: int = 0
+    # a deck with passive scalars: -> FP64 scalar_r (nscalar, nc3, nc2, nc1)
+    tracers: Optional[Callable[[], torch.Tensor]] = None
+    result_scalars: Optional[torch.Tensor] = None  # the final scalar_s (host)
 
     @property
     def latency(self) -> Optional[float]:
@@ -78,6 +81,9 @@ def footprint(options: MeshBlockOptions, dtype: torch.dtype) -> int:
             b += (icells * 160 + (icells // c.nx1) * 7) * 4 + 16
     if c.nx3 > 1:
         b += 5 * icells * s
+    ns = len(options.scalar_names)
+    if ns:  # the tracers' buffers and their face scratch
+        b += 3 * ns * nc * s + 4 * (1 + ns) * nc * 8
     b += 8 * (5 * c.nc1 + 1) + 16 * (c.nc1 + 1)
     return b
 
@@ -87,13 +93,16 @@ class _Slot:
     in."""
 
     def __init__(self, req: Request, device, dtype):
-        if req.options.scalar_names:
-            raise DeckError(f"request {req.rid}: passive scalars are not "
-                            "built for served requests")
+        self.ns = len(req.options.scalar_names)
+        if self.ns and req.tracers is None:
+            raise DeckError(f"request {req.rid}: its deck carries passive "
+                            "scalars; the request needs their scalar_r (tracers)")
         self.req = req
         self.desc = d = block_of(req.options)
         self.shape = (5, d["nc3"], d["nc2"], d["nc1"])
         self.store = torch.empty((3,) + self.shape, dtype=dtype, device=device)
+        self.sstore = (torch.empty((3, self.ns) + self.shape[1:], dtype=dtype,
+                                   device=device) if self.ns else None)
         self.x1f = torch.as_tensor(d["x1f"], dtype=torch.float64, device=device)
         self.x1v = torch.as_tensor(d["x1v"], dtype=torch.float64, device=device)
         self.base = None
@@ -126,6 +135,7 @@ def _descs(slots: List[_Slot]):
         a.implicit_scheme = int(d.get("implicit_scheme", 0))
         a.implicit_precision = _lib.F32 if d.get("implicit_f32") else _lib.F64
         a.base = sl.base.data_ptr() if sl.base is not None else None
+        a.nscalar = int(d.get("nscalar", 0))
     return arr
 
 
@@ -145,6 +155,10 @@ class _Handle:
             sl.perm = (sl.cur, (sl.cur + 1) % 3, (sl.cur + 2) % 3)
             _lib.check(L.sg_bind(h, b, *(sl.store[q].data_ptr() for q in sl.perm)),
                        "sg_bind")
+            if sl.sstore is not None:
+                _lib.check(L.sg_bind_scalars(
+                    h, b, *(sl.sstore[q].data_ptr() for q in sl.perm)),
+                    "sg_bind_scalars")
             nb = ctypes.c_size_t()
             _lib.check(L.sg_scratch_bytes(h, b, ctypes.byref(nb)), "sg_scratch_bytes")
             if nb.value:
@@ -263,6 +277,14 @@ class Server:
             ptrs = (ctypes.c_void_p * 1)(w.data_ptr())
             _lib.check(self.L.sg_init_from_prim(tmp.h, ptrs, _stream(stream)),
                        "sg_init_from_prim")
+            if sl.ns:
+                # scalar_s = rho scalar_r from the FP64 initial density, as
+                # MeshBlock.initialize sets it, then its ghosts
+                r = req.tracers().to(self.device, torch.float64)
+                self.h2d_bytes += r.numel() * 8
+                sl.sstore[0].copy_((w[0].unsqueeze(0) * r).to(dtype))
+                _lib.check(self.L.sg_fill_ghosts(tmp.h, _stream(stream)),
+                           "sg_fill_ghosts")
         finally:
             tmp.close()
         sl.cur = 0
@@ -294,7 +316,9 @@ class Server:
                     req, ev, host, flags = item
                     if ev.query():
                         req.done = time.perf_counter() - t0
-                        req.result = host
+                        req.result = host[0] if isinstance(host, tuple) else host
+                        if isinstance(host, tuple):
+                            req.result_scalars = host[1]
                         req.flags = int(flags.item())
                         finishing.remove(item)
                 # first come, first served, while the memory fits
@@ -348,12 +372,19 @@ class Server:
                         b = running.index(sl)
                         host = torch.empty(sl.shape, dtype=dtype, pin_memory=True)
                         host.copy_(sl.store[sl.cur], non_blocking=True)
+                        if sl.sstore is not None:
+                            sh = torch.empty(sl.sstore.shape[1:], dtype=dtype,
+                                             pin_memory=True)
+                            sh.copy_(sl.sstore[sl.cur], non_blocking=True)
+                            self.d2h_bytes += sh.numel() * sh.element_size()
+                            host = (host, sh)
                         fh = torch.empty((), dtype=torch.int32, pin_memory=True)
                         fh.copy_(flags[b], non_blocking=True)
                         ev = torch.cuda.Event()
                         ev.record(stream)
                         finishing.append((sl.req, ev, host, fh))
-                        self.d2h_bytes += host.numel() * host.element_size()
+                        hh = host[0] if isinstance(host, tuple) else host
+                        self.d2h_bytes += hh.numel() * hh.element_size()
                     for sl in done_now:
                         running.remove(sl)
                         used -= sl.bytes

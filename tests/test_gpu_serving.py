@@ -70,3 +70,35 @@ def test_arrivals_are_served_in_order(cuda):
         assert b.admitted >= a.admitted
     assert all(r.done >= r.admitted >= r.arrival for r in reqs)
     assert len(srv.gpu_step_ms) >= 3 and srv.launches > 0
+
+
+def test_tracers_alone_equal_in_the_mix(cuda):
+    """Requests whose deck carries a passive tracer: each one's tracer
+    densities and state served alone equal those served in the mix, bit for
+    bit."""
+    import copy
+    import numpy as np
+    import snapy_gb300 as sg
+
+    def tracer_request(rid, n, seed):
+        cfg = copy.deepcopy(sg.options.yaml_lite.load(
+            "snapy_gb300/decks/convection3d.yaml"))
+        cfg["scalar"] = {"nvar": 1}
+        opts = sg.MeshBlockOptions.from_config(cfg)
+        c = opts.coord()
+        c.nx1, c.nx2, c.nx3 = n, 12, 10
+        c.x1max, c.x2max, c.x3max = n * 50.0, 12 * 50.0, 10 * 50.0
+        z = np.linspace(0.0, 1.0, c.nc1)[None, None, None, :]
+        r = torch.from_numpy(1e-3 * (1.0 + 0.5 * np.sin(5.0 * z))
+                             * np.ones((1, c.nc3, c.nc2, c.nc1)))
+        return Request(rid, opts,
+                       lambda: problems.convection3d(opts, "cpu", seed=seed), 4,
+                       tracers=lambda: r)
+
+    mix = [tracer_request(0, 16, 3), tracer_request(1, 24, 4)]
+    Server(cuda).run(mix)
+    for k, req in enumerate(mix):
+        alone = tracer_request(9, 16 if k == 0 else 24, 3 + k)
+        Server(cuda).run([alone])
+        assert torch.equal(req.result, alone.result), k
+        assert torch.equal(req.result_scalars, alone.result_scalars), k
