@@ -1108,7 +1108,9 @@ int sg_stage(sg_handle* h, int32_t stage, const double* dt_dev,
                                     timed ? ev + 2 : nullptr);
     if (rc) return cuda_fail((cudaError_t)rc, "sg_stage: implicit solve");
     if (timed) cudaEventRecord(ev[4], s);
-    launches += 3;
+    // assembly, solve, finish; the refined solve adds its FP32 sweep and a
+    // residual and a correction per correction
+    launches += 3 + (h->refine ? 1 + 2 * h->refine : 0);
   }
   if (h->scalars) {
     // the passive scalars on the stage's mass flux: face fluxes, update
