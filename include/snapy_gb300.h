@@ -347,8 +347,17 @@ typedef struct sg_dt_block {
   const void* u;      /* current conserved state, (5, nc3, nc2, nc1) */
   int32_t nc1, nc2, nc3, ng;
   double dx1, dx2, dx3, gammad;
-  double dt_src;      /* source-term bound (0: none) */
-  int32_t implicit;   /* 1: vertical implicit solve, x1 acoustic bound off */
+  double dt_src;      /* source-term bound, e.g. the diffusion limit
+                         dx_min^2 / (2 ndim nu); 0, negative, NaN or +inf:
+                         no bound */
+  int32_t implicit;   /* the deck's implicit-scheme number (0: none); bit 0
+                         (the vertical solve, as in scheme 9) drops the x1
+                         acoustic bound for blocks with more than one column,
+                         as sg_max_dt does */
+  const double* base; /* FP32 blocks under gravity: the FP64 hydrostatic base
+                         (rho_b | p_b | ..., nc1 each) that the state's
+                         anomalies are about, as in sg_block_desc.base;
+                         NULL otherwise (refused for FP64 blocks) */
 } sg_dt_block;
 int sg_max_dt_noalloc(const sg_dt_block* blocks, int32_t nblock, int32_t dtype,
                       double cfl, const int32_t* redo_dev, double* dt_out_dev,

@@ -76,7 +76,10 @@ def build(quiet: bool = True) -> None:
     if quiet:
         kw.update(stdout=subprocess.DEVNULL)
     subprocess.run(["make", "-s", "all"], **kw)
-    ref_root = os.environ.get("REFERENCE_ROOT", "/root/reference")
+    # the reference source tree: REFERENCE_ROOT, else the directory
+    # "reference" beside the repository
+    ref_root = os.environ.get("REFERENCE_ROOT") or os.path.abspath(
+        os.path.join(HERE, "..", "..", "reference"))
     if os.path.isdir(os.path.join(ref_root, "src")):
         subprocess.run(["make", "-s", "ref", f"REFERENCE_ROOT={ref_root}"], **kw)
 

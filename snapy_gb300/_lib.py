@@ -65,7 +65,8 @@ class DtBlock(ctypes.Structure):
     _fields_ = [("u", _vp), ("nc1", _i32), ("nc2", _i32), ("nc3", _i32),
                 ("ng", _i32), ("dx1", ctypes.c_double), ("dx2", ctypes.c_double),
                 ("dx3", ctypes.c_double), ("gammad", ctypes.c_double),
-                ("dt_src", ctypes.c_double), ("implicit", _i32)]
+                ("dt_src", ctypes.c_double), ("implicit", _i32),
+                ("base", _vp)]
 
 
 NOALLOC_MAX_BLOCKS = 64  # SG_NOALLOC_MAX_BLOCKS

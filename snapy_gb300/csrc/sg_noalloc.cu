@@ -87,7 +87,11 @@ __global__ void __launch_bounds__(kThreads)
     T uc[sg::NHYDRO], w[sg::NHYDRO];
 #pragma unroll
     for (int v = 0; v < sg::NHYDRO; ++v) uc[v] = u[v * plane + c];
+    // FP32 blocks under gravity hold anomalies about the FP64 base: the
+    // totals are formed as the handle path's reduction forms them
+    if (B.base) uc[sg::IDN] = T(B.base[i]) + uc[sg::IDN];
     sg::cons2prim<T>(uc, w, gammad);
+    if (B.base) w[sg::IPR] = T(B.base[nc1 + i]) + w[sg::IPR];
     const T cs = sqrt(gammad * w[sg::IPR] / w[sg::IDN]);
     if (nc1 > 1 && (B.implicit & 1) && !(nc2 == 1 && nc3 == 1))
       dtm = fmin(dtm, (double)(T(B.dx1) / (fabs(w[sg::IVX]) * T(p.cfl / 1.0))));
@@ -164,7 +168,12 @@ extern "C" int sg_max_dt_noalloc(const sg_dt_block* blocks, int32_t nblock,
     if (!B.u || B.nc1 < 1 || B.nc2 < 1 || B.nc3 < 1 || B.ng < 0)
       return sg_fail_message(SG_ERR_ARG, "sg_max_dt_noalloc: a block has a null "
                                          "state or a bad size");
+    if (B.base && dtype != SG_F32)
+      return sg_fail_message(SG_ERR_ARG, "sg_max_dt_noalloc: a hydrostatic "
+                                         "base is only used by FP32 blocks");
     p.blk[b] = B;
+    // no source-term bound: 0, negative, NaN or +inf all mean none
+    if (!(B.dt_src > 0.) || isinf(B.dt_src)) p.blk[b].dt_src = INFINITY;
     size_t cells = (size_t)B.nc1 * B.nc2 * B.nc3;
     if (cells > max_cells) max_cells = cells;
   }

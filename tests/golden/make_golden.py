@@ -1,11 +1,12 @@
 """Generate the golden face vectors from the reference's own kernels.
 
-Run in a container that holds the reference source tree (REFERENCE_ROOT,
-default /root/reference): it builds oracle/_ref/libsnapref.so from the
-reference's unmodified header-only kernels (recon_point.h, riemann_kernels.h,
-ideal_gas_impl.h, hydro_ref_x1_impl.h) and evaluates them on seeded random
-inputs.  The output, tests/golden/reference_faces.npz, travels with the repo
-so the oracle can be pinned where the reference is absent.
+Run where the reference source tree is present (REFERENCE_ROOT, default: the
+directory "reference" beside the repository): it builds
+oracle/_ref/libsnapref.so from the reference's unmodified header-only
+kernels (recon_point.h, riemann_kernels.h, ideal_gas_impl.h,
+hydro_ref_x1_impl.h) and evaluates them on seeded random inputs. The output,
+tests/golden/reference_faces.npz, travels with the repo so the oracle can be
+pinned where the reference is absent.
 
     python tests/golden/make_golden.py
 """
