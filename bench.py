@@ -1,11 +1,41 @@
-"""Benchmark of the MeshBlock hydro stage: cell-updates/s per RK3 step.
+"""Benchmark of the MeshBlock hydro stage: cell-updates/s per RK3 step,
+batched and served against the plain FP64 GPU path, with p50/p99 latency.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl native|reference]
-                    [--workload straka|sod] [--precision float64|float32]
+                    [--workload serving|ensemble|straka|cubed-sphere|sod|...]
+                    [--precision float64|float32]
 
-One JSON line on rank 0.  A step is one full RK3 step (three stages) of the
-workload's block on synthetic input (the deck's own initial state, generated
-on the host), dt fixed at the CFL step of the initial state.
+One JSON line on rank 0.
+
+The default workload, batched-served, is the metric's own pair:
+* the batched ensemble -- 64 seeded Straka-type members of uneven size
+  (nx2 in 128..512, nx1 in 32..128) in one handle, FP32 bulk with the
+  implicit solve refined to FP64, one graph per step, each member's CFL dt
+  on the device.  value = member cell-updates over the CUDA-event time of
+  exactly K timed steps (after W warm-up steps); e2e = the same with every
+  member's state copied host->device and back each step (pinned memory);
+* the serving trace (the line's "served" object) -- Poisson arrivals (20
+  req/s) of 3-D planar dry convection solves of 64^3 .. 128x128x96 cells,
+  200 RK3 steps each, admitted against an HBM budget (--serve-budget-gb,
+  8 GiB, so requests queue and join while others run) and advanced together
+  (continuous batching).  Its value is the cell-updates over the CUDA-event
+  time of its batched steps, its e2e the wall clock of the whole trace
+  through Server.run (arrivals, initial states in, results out), with
+  p50/p99 latency (arrival to result on host) and the admission wait.
+Both carry the plain FP64 GPU path on the same work (each block alone on its
+own FP64 MeshBlock) on the same clock: vs_plain_fp64 (CUDA events on both
+sides) and vs_plain_fp64_wall (wall clock on both sides); the served ratio
+is lifted to served_vs_plain_fp64.  The served object also holds
+alone_equals_mix (the smallest request run alone equals itself in the mix,
+bit for bit) and fp32_rel_l2_vs_fp64 (its FP32 error per field against the
+FP64 path at the served horizon).  roofline: B_alg (160 B per FP32
+cell-update per RK3 step: 5 reads + 3 writes of 5 variables) x the
+device-timed rate against the measured HBM peak; per-kernel times and the
+implementation's scratch bytes are reported apart.
+
+The other workloads (one block each unless named): a step is one full RK3
+step of the workload's block on synthetic input (the deck's own initial
+state, generated on the host), dt fixed at the CFL step of the initial state.
 
 * value: device-timed throughput (CUDA events on the launching stream around
   each step, L2 flushed between steps -- the block fits in L2, so each timed
@@ -13,10 +43,11 @@ on the host), dt fixed at the CFL step of the initial state.
 * e2e: the same steps through the public API with HOST buffers: each step
   copies the state host->device from pinned memory, advances it and copies it
   back (bytes counted from the copied tensors).
-* roofline: the dominant kernel's algorithmic bytes per launch over its mean
-  duration (CUDA events the library records around each kernel of an eager
-  stage, on the launching stream) against the measured HBM copy peak; the
-  "kernels" object gives every kernel's launches, mean time and share.
+* roofline: B_alg x the device-timed rate against the measured HBM copy
+  peak; the dominant kernel's own bytes per launch over its mean duration
+  (CUDA events the library records around each kernel of an eager stage, on
+  the launching stream) beside it, and the "kernels" object with every
+  kernel's launches, mean time and share.
 * cpu_baseline: the CPU oracle (the reference algorithm restated in C, FP64,
   OpenMP on every host core) on a bounded sample of the same workload.
 
@@ -43,7 +74,13 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+METRIC = "cell-updates/s per RK3 step, batched+served vs plain; p50/p99 latency at tol"
+
 WORKLOADS = {
+    # the default: the batched ensemble (the line's value, K steps) and the
+    # serving trace (its "served" object, p50/p99), each beside the plain
+    # FP64 GPU path on the same work
+    "batched-served": None,
     # the 2-D density-current shape of the Straka config: 512 x 128 cells at
     # 50 m, LMARS + WENO5 (cp5 for velocity/pressure) + RK3, reflecting walls
     # the Straka configuration: gravity (well-balanced x1 reference),
@@ -77,7 +114,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["native", "reference"], default="native")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="straka")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS),
+                    default="batched-served")
     ap.add_argument("--precision", choices=["float64", "float32"], default=None)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -99,8 +137,11 @@ def parse():
                     help="Straka and Sod workloads: passive tracers carried "
                          "(the reference's Straka deck carries one, "
                          "scalar/names [tracer])")
-    ap.add_argument("--requests", type=int, default=8,
+    ap.add_argument("--requests", type=int, default=24,
                     help="serving: requests in the trace")
+    ap.add_argument("--serve-budget-gb", type=float, default=8.0,
+                    help="serving: the HBM budget requests are admitted "
+                         "against (GiB; 0: the device's free memory)")
     ap.add_argument("--serve-steps", type=int, default=200,
                     help="serving: RK3 steps per request")
     return ap.parse_args()
@@ -167,26 +208,6 @@ def config_of(opts, workload, args, nranks):
         "replicas": nranks,
         "parallelism": "replicas" if nranks > 1 else "single",
     }
-
-
-# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of a
-# dominant kernel, from one ncu capture of the same workload and kernel
-# build: profiles/straka512x128_fp64_launches_and_kernels.md,
-# profiles/ensemble64_fp32_vic_launches_and_kernels.md and
-# profiles/refined_solve_ensemble64_and_straka512x128_fp32.md
-NCU_TRAFFIC = {
-    ("straka", "float64", "vic_solve_kernel"): 42.009600e6 + 0.149248e6,
-    ("ensemble", "float32", "vic_solve_kernel"): 1.288739e9 + 0.550966e9,
-    # the refined phase: vic_solve32_kernel, 2 x (vic_residual_kernel,
-    # vic_correct32_kernel), vic_solve_kernel (masked columns only)
-    ("ensemble", "float32", "refined"): 6.2371e9,
-    ("straka", "float32", "refined"): 0.2025e9,
-}
-
-
-def ncu_traffic(workload, precision, kernel):
-    """The captured DRAM bytes per launch, or None for an uncaptured case."""
-    return NCU_TRAFFIC.get((workload, precision, kernel))
 
 
 FP64_ISSUE = ("FP64 issue rate (one FP64 warp instruction per SM sub-partition "
@@ -524,18 +545,18 @@ def run_native(args):
             "e2e": {"value": job_rate(cells * e2e_steps, world, e2e_t),
                     "unit": "cell-updates/s", "h2d_bytes_per_step": nbytes,
                     "d2h_bytes_per_step": nbytes},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
-                         "unit": "GB/s", "frac": achieved / peak,
-                         "peak_kind": peak_kind,
-                         "traffic": ncu_traffic(
-                             args.workload, opts.hydro().precision,
-                             "refined" if dom == "vic_solve_kernel"
-                             and refined(opts) else dom),
-                         "kernel": dom,
-                         "runs": solve_phase(opts)[0]
-                                 if dom == "vic_solve_kernel" else dom,
-                         "bytes_per_launch": per_launch[dom],
-                         "mean_launch_us": dom_ms / dom_n * 1e3,
+            "roofline": {"bound": "hbm", "achieved": value * b_alg(s_bytes) / 1e9,
+                         "peak": peak, "unit": "GB/s",
+                         "frac": value * b_alg(s_bytes) / 1e9 / peak,
+                         "peak_kind": peak_kind, "traffic": None,
+                         "basis": f"B_alg = {b_alg(s_bytes)} B per cell-update "
+                                  "per RK3 step x the device-timed rate",
+                         "dominant_kernel": dom,
+                         "dominant_runs": solve_phase(opts)[0]
+                                          if dom == "vic_solve_kernel" else dom,
+                         "dominant_bytes_per_launch": per_launch[dom],
+                         "dominant_mean_launch_us": dom_ms / dom_n * 1e3,
+                         "dominant_kernel_gbs": achieved,
                          "limiter": solve_phase(opts)[2]
                                     if dom == "vic_solve_kernel" else
                                     FP64_ISSUE if blk.dtype == torch.float64
@@ -601,12 +622,13 @@ def ensemble_config(members, precision, nranks):
             "parallelism": "replicas" if nranks > 1 else "single"}
 
 
-def run_ensemble(args):
+def run_ensemble(args, ranks=None, emit=True):
     """The batched form: every member in one handle.  Beside it, the plain
     FP64 GPU path on the same members: each its own FP64 MeshBlock, stepped
-    one after another with its own CFL dt (graphs on)."""
+    one after another (graphs on).  Returns rank 0's line (None elsewhere)."""
     import torch
-    ranks = Ranks()
+    own = ranks is None
+    ranks = ranks or Ranks()
     world, rank, local = ranks.world, ranks.rank, ranks.local
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
@@ -697,30 +719,18 @@ def run_ensemble(args):
     schedule = ens.batch.schedule
     del ens
 
-    # the plain FP64 GPU path on the same members
-    plain_steps = max(2, min(args.steps, 5))
-    blocks = []
+    # the plain FP64 GPU path on the same members, both clocks
+    pairs = []
     for opts, w in members:
         o64 = sg.MeshBlockOptions.from_yaml(os.path.join(ROOT, WORKLOADS["ensemble"]))
         c, c0 = o64.coord(), opts.coord()
         c.nx1, c.nx2, c.x1max, c.x2max = c0.nx1, c0.nx2, c0.x1max, c0.x2max
         o64.hydro().precision = "float64"
-        blk = sg.MeshBlock(o64).to(dev)
-        vars = {"hydro_w": w.to(dev)}
-        blk.initialize(vars)
-        blocks.append((blk, vars))
-    for _ in range(6):  # eager steps and both graphs of every block
-        for blk, vars in blocks:
-            blk.step(vars, blk.max_time_step(vars))
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(plain_steps):
-        for blk, vars in blocks:
-            blk.step(vars, blk.max_time_step(vars))
-    torch.cuda.synchronize()
-    plain = cells * plain_steps / (time.perf_counter() - t0)
-    del blocks
+        pairs.append((o64, (lambda w=w: w)))
+    plain = plain_fp64_blocks(pairs, dev)
+    e2e_value = job_rate(cells * e2e_steps, world, e2e_t)
 
+    line = None
     if rank == 0:
         cb = None if args.no_cpu_baseline else ensemble_cpu_baseline(members, args.cpu_seconds)
         line = {
@@ -732,26 +742,32 @@ def run_ensemble(args):
             "dtype": "f32" if precision == "float32" else "f64",
             "data": "synthetic (seeded Straka-type members)",
             "config": ensemble_config(members, precision, world),
-            "e2e": {"value": job_rate(cells * e2e_steps, world, e2e_t),
+            "e2e": {"value": e2e_value,
                     "unit": "cell-updates/s", "h2d_bytes_per_step": nbytes,
                     "d2h_bytes_per_step": nbytes},
-            "plain_fp64": {"value": plain, "unit": "cell-updates/s",
+            "plain_fp64": {"device": plain["device"], "wall": plain["wall"],
+                           "unit": "cell-updates/s",
                            "how": "each member its own FP64 MeshBlock, one "
-                                  "after another, own CFL dt (host read), "
-                                  "step graphs on", "steps": plain_steps},
-            "vs_plain_fp64": value / plain,
+                                  "after another, graphs on; device: CUDA "
+                                  f"events around {plain['steps_per_request']} "
+                                  "steps at a fixed CFL dt; wall: the same "
+                                  "steps with the CFL dt read on the host"},
+            "vs_plain_fp64": value / plain["device"],
+            "vs_plain_fp64_wall": e2e_value / plain["wall"],
+            "clock_note": "vs_plain_fp64: CUDA-event time on both sides; "
+                          "vs_plain_fp64_wall: wall clock on both sides (the "
+                          "batched side with its host copies)",
             "schedule": schedule,
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
-                         "unit": "GB/s", "frac": achieved / peak,
-                         "peak_kind": peak_kind,
-                         "traffic": ncu_traffic(
-                             "ensemble", precision,
-                             "refined" if dom == "vic_solve_kernel"
-                             and refined(members[0][0]) else dom),
-                         "kernel": dom, "bytes_per_launch": per_launch[dom],
-                         "runs": solve_phase(members[0][0])[0]
-                                 if dom == "vic_solve_kernel" else dom,
-                         "mean_launch_us": dom_ms / dom_n * 1e3,
+            "roofline": {"bound": "hbm", "achieved": value * b_alg(s_bytes) / 1e9,
+                         "peak": peak, "unit": "GB/s",
+                         "frac": value * b_alg(s_bytes) / 1e9 / peak,
+                         "peak_kind": peak_kind, "traffic": None,
+                         "basis": f"B_alg = {b_alg(s_bytes)} B per cell-update "
+                                  "per RK3 step x the device-timed rate",
+                         "dominant_kernel": dom,
+                         "dominant_bytes_per_launch": per_launch[dom],
+                         "dominant_mean_launch_us": dom_ms / dom_n * 1e3,
+                         "dominant_kernel_gbs": achieved,
                          "limiter": solve_phase(members[0][0])[2]
                                     if dom == "vic_solve_kernel" else
                                     FP64_ISSUE},
@@ -761,9 +777,11 @@ def run_ensemble(args):
             "gpu_launches": args.steps * (2 + 3 * b.launches_per_stage()),
             "step_ms_median": statistics.median(step_ms),
         }
-        print(json.dumps(line), flush=True)
-    ranks.close()
-    return 0
+        if emit:
+            print(json.dumps(line), flush=True)
+    if own:
+        ranks.close()
+    return line
 
 
 def run_reference_ensemble(args):
@@ -823,7 +841,7 @@ def serving_trace(n, steps, precision=None, implicit_precision=None,
     return reqs
 
 
-def serving_config(reqs, nranks):
+def serving_config(reqs, nranks, budget=None):
     return {"workload": f"serving trace: {len(reqs)} 3-D planar dry convection "
                         f"solves, Poisson arrivals {SERVE_RATE:g}/s (seed "
                         f"{SERVE_SEED}), (nx2, nx3, nx1) in {{64,96,128}}^2 x "
@@ -834,7 +852,8 @@ def serving_config(reqs, nranks):
             "implicit_assembly": reqs[0].options.hydro().icorr.precision,
             "implicit_solve": implicit_solve(reqs[0].options),
             "cells": [r.cells for r in reqs],
-            "admission": "first come first served against free HBM",
+            "hbm_budget_bytes": budget,
+            "admission": "first come first served against the HBM budget",
             "batching": "continuous: every running request in the same "
                         "launches, handle rebuilt on admission/completion",
             "l2": "inputs larger than L2 (no flush needed)",
@@ -842,14 +861,122 @@ def serving_config(reqs, nranks):
             "parallelism": "replicas" if nranks > 1 else "single"}
 
 
-def run_serving(args):
+# algorithmic bytes per cell-update per RK3 step of a fused three-stage
+# SSP-RK3 that keeps u0: 5 reads + 3 writes of nvar = 5 values
+def b_alg(s_bytes: int, nvar: int = 5) -> int:
+    return 8 * nvar * s_bytes
+
+
+def plain_fp64(reqs, dev, steps=3):
+    """plain_fp64_blocks over serving requests: each grid shape of the trace
+    is measured once (on its first request), and the trace's plain time is
+    every request's cell-steps at its shape's rate."""
+    import copy
+    first = {}
+    for r in reqs:
+        c = r.options.coord()
+        first.setdefault((c.nx1, c.nx2, c.nx3), r)
+    rate = {}
+    for shape, r in first.items():
+        o64 = copy.deepcopy(r.options)
+        o64.hydro().precision = "float64"
+        rate[shape] = plain_fp64_blocks([(o64, r.initial)], dev, steps)
+    out = {"steps_per_request": steps, "shapes": len(rate)}
+    for clock in ("device", "wall"):
+        t = 0.0
+        for r in reqs:
+            c = r.options.coord()
+            t += r.cells * r.steps / rate[(c.nx1, c.nx2, c.nx3)][clock]
+        out[clock] = sum(r.cells * r.steps for r in reqs) / t
+    return out
+
+
+def plain_fp64_blocks(pairs, dev, steps=3):
+    """The plain FP64 GPU path on the same blocks: each alone, its own
+    FP64 MeshBlock (graphs on), one after another.
+
+    device: cell-updates over the CUDA-event time of `steps` steps per
+    request at that request's fixed CFL dt (no host read inside the timed
+    steps: the plain path at its fastest).
+    wall: the same requests stepped as a user drives MeshBlock -- the CFL dt
+    read on the host every step -- over host wall-clock time."""
     import torch
-    ranks = Ranks()
+    import snapy_gb300 as sg
+    stream = torch.cuda.current_stream()
+    dev_s, wall_s, n = 0.0, 0.0, 0
+    for o64, initial in pairs:
+        c = o64.coord()
+        cells = c.nx1 * c.nx2 * c.nx3
+        blk = sg.MeshBlock(o64).to(dev)
+        vars = {"hydro_w": initial().to(dev)}
+        blk.initialize(vars)
+        for _ in range(6):  # eager steps and both rotations' graphs
+            blk.step(vars, blk.max_time_step(vars))
+        dt = blk.max_time_step(vars)
+        torch.cuda.synchronize()
+        evs = []
+        for _ in range(steps):
+            e0, e1 = (torch.cuda.Event(enable_timing=True),
+                      torch.cuda.Event(enable_timing=True))
+            e0.record(stream)
+            blk.step(vars, dt)
+            e1.record(stream)
+            evs.append((e0, e1))
+        torch.cuda.synchronize()
+        dev_s += sum(a.elapsed_time(b) for a, b in evs) / 1e3
+        t1 = time.perf_counter()
+        for _ in range(steps):
+            blk.step(vars, blk.max_time_step(vars))
+        torch.cuda.synchronize()
+        wall_s += time.perf_counter() - t1
+        n += cells * steps
+        del blk, vars
+    return {"device": n / dev_s, "wall": n / wall_s, "steps_per_request": steps}
+
+
+def fp64_reference_state(req, dev):
+    """The request's FP64 state after its steps: the plain FP64 path
+    (bitwise the CPU oracle's FP64 path), each step at its own CFL dt."""
+    import copy
+    import torch
+    import snapy_gb300 as sg
+    o64 = copy.deepcopy(req.options)
+    o64.hydro().precision = "float64"
+    blk = sg.MeshBlock(o64).to(dev)
+    vars = {"hydro_w": req.initial().to(dev)}
+    blk.initialize(vars)
+    for _ in range(req.steps):
+        blk.step(vars, blk.max_time_step(vars))
+        assert blk.check_redo(vars) == 0
+    torch.cuda.synchronize()
+    return vars["hydro_u"].detach().cpu()
+
+
+def rel_l2_fields(got, want):
+    """Relative L2 of each of the five fields over the interior."""
+    sl = (slice(3, -3),) * (got.dim() - 1)
+    out = []
+    for v in range(5):
+        a, b = got[v][sl].double(), want[v][sl].double()
+        den = float(b.norm())
+        if den == 0.0:  # momenta at rest: scale by the density's momentum unit
+            den = float(want[0][sl].double().norm())
+        out.append(float((a - b).norm()) / den)
+    return out
+
+
+def run_serving(args, ranks=None, emit=True):
+    """The serving trace through Server.run, beside the plain FP64 path on
+    the same requests.  Returns rank 0's line (None elsewhere)."""
+    import copy
+    import torch
+    own = ranks is None
+    ranks = ranks or Ranks()
     world, rank, local = ranks.world, ranks.rank, ranks.local
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
-    import snapy_gb300 as sg
     from snapy_gb300.serving import Server
+    budget = int(args.serve_budget_gb * (1 << 30)) if args.serve_budget_gb else None
     # warm-up: a short trace compiles nothing but touches every code path
     warm = serving_trace(2, max(3, args.warmup), args.precision,
                          args.implicit_precision or "float32",
@@ -862,7 +989,7 @@ def run_serving(args):
                          args.implicit_solve, args.implicit_corrections)
     torch.cuda.synchronize()
     ranks.barrier()
-    srv = Server(dev, timing=True)
+    srv = Server(dev, hbm_budget=budget, timing=True)
     with ClockSampler(local) as clk:
         t0 = time.perf_counter()
         srv.run(reqs)
@@ -873,87 +1000,118 @@ def run_serving(args):
     gpu_s = sum(srv.gpu_step_ms) / 1e3
     gpu_s, wall = ranks.max(gpu_s), ranks.max(wall)
     lat = sorted(r.latency for r in reqs)
-    q = lambda f: lat[min(len(lat) - 1, int(round(f * (len(lat) - 1))))]
+    wait = sorted(r.admitted - r.arrival for r in reqs)
+    q = lambda xs, f: xs[min(len(xs) - 1, int(round(f * (len(xs) - 1))))]
     kms = srv.kernel_ms
     dom = max(kms, key=lambda k: kms[k][0])
-    cells_all = sum(r.cells for r in reqs)
-    per_cell = {"stage_kernel": 5 * 4 + 40, "x3_kernel": 5 * 4 * 2,
-                "vic_assemble_kernel": 5 * 4 + 40 + 40 + 600,
-                "vic_solve_kernel": solve_phase(reqs[0].options)[1],
-                "vic_finish_kernel": 120 + 15 * 4, "ghost_kernel": 0}
-    # a launch covers the running set; its cells vary, so the achieved
-    # bandwidth is the algorithmic bytes of all cell-steps over the kernel time
-    achieved = per_cell[dom] * total * 3 / (kms[dom][0] / 1e3) / 1e9
+    prec = reqs[0].options.hydro().precision
+    s_bytes = 4 if prec == "float32" else 8
+    value = job_rate(total, world, gpu_s)
     peak, peak_kind = peaks()
-    # the plain FP64 path on the same requests: each alone, its own FP64
-    # MeshBlock, a few steps (its per-cell-step rate)
-    plain_steps = 3
-    t_plain, n_plain = 0.0, 0
-    for r in reqs:
-        o64 = sg.MeshBlockOptions.from_yaml(os.path.join(ROOT, WORKLOADS["serving"]))
-        c, c0 = o64.coord(), r.options.coord()
-        c.nx1, c.nx2, c.nx3 = c0.nx1, c0.nx2, c0.nx3
-        c.x1max, c.x2max, c.x3max = c0.x1max, c0.x2max, c0.x3max
-        o64.hydro().precision = "float64"
-        blk = sg.MeshBlock(o64).to(dev)
-        vars = {"hydro_w": r.initial().to(dev)}
-        blk.initialize(vars)
-        for _ in range(5):  # eager steps and both graphs
-            blk.step(vars, blk.max_time_step(vars))
-        torch.cuda.synchronize()
-        t1 = time.perf_counter()
-        for _ in range(plain_steps):
-            blk.step(vars, blk.max_time_step(vars))
-        torch.cuda.synchronize()
-        t_plain += time.perf_counter() - t1
-        n_plain += r.cells * plain_steps
-        del blk, vars
-    plain = n_plain / t_plain
+    achieved = value * b_alg(s_bytes) / 1e9
+    ktot = sum(v[0] for v in kms.values())
+    # the same requests on the plain FP64 GPU path, both clocks
+    plain = plain_fp64(reqs, dev)
+    # the smallest request alone (a fresh server) equals itself in the mix,
+    # and its FP32 result against the FP64 path at the served horizon
+    small = min(reqs, key=lambda r: (r.cells, r.rid))
+    alone = copy.copy(small)
+    alone.arrival, alone.result, alone.done, alone.admitted = 0.0, None, None, None
+    Server(dev).run([alone])
+    same = bool(torch.equal(alone.result, small.result))
+    err = None
+    if prec == "float32":
+        want = fp64_reference_state(small, dev)
+        # the FP32 state holds anomalies about the FP64 hydrostatic base
+        # (the serving slot's, from the same initial state): add it back
+        from snapy_gb300.batch import fill_base
+        from snapy_gb300.meshblock import block_of
+        d = block_of(small.options)
+        nc1 = d["nc1"]
+        t = torch.zeros(5 * nc1 + 1, dtype=torch.float64, device=dev)
+        fill_base(t, small.initial().to(dev), d)
+        tot = small.result.double().clone()
+        tot[0] += t[0:nc1].cpu()
+        tot[4] += t[2 * nc1:3 * nc1].cpu()
+        err = rel_l2_fields(tot, want)
+    line = None
     if rank == 0:
         cb = None
         if not args.no_cpu_baseline:
-            small = min(reqs, key=lambda r: r.cells)
             cb = serving_cpu_baseline(small, args.cpu_seconds)
         line = {
             "metric": "cell-updates/s per RK3 step",
-            "value": job_rate(total, world, gpu_s), "unit": "cell-updates/s",
+            "value": value, "unit": "cell-updates/s",
             "n_gpus": world, "steps": len(srv.gpu_step_ms), "warmup": args.warmup,
             "ms_per_step": gpu_s / len(srv.gpu_step_ms) * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32" if reqs[0].options.hydro().precision == "float32" else "f64",
+            "dtype": "f32" if prec == "float32" else "f64",
             "data": "synthetic (seeded convection requests, seeded arrivals)",
-            "config": serving_config(reqs, world),
-            "latency": {"p50_s": q(0.5), "p99_s": q(0.99), "min_s": lat[0],
-                        "max_s": lat[-1], "unit": "s, arrival to result on host"},
+            "config": serving_config(reqs, world, srv.budget),
+            "latency": {"p50_s": q(lat, 0.5), "p99_s": q(lat, 0.99),
+                        "min_s": lat[0], "max_s": lat[-1],
+                        "admission_wait_p50_s": q(wait, 0.5),
+                        "admission_wait_p99_s": q(wait, 0.99),
+                        "unit": "s, arrival to result on host"},
             "e2e": {"value": job_rate(total, world, wall), "unit": "cell-updates/s",
                     "h2d_bytes_per_step": srv.h2d_bytes / len(srv.gpu_step_ms),
                     "d2h_bytes_per_step": srv.d2h_bytes / len(srv.gpu_step_ms),
-                    "note": "wall clock of the whole trace: arrivals, initial "
-                            "states host->device, results device->host"},
-            "plain_fp64": {"value": plain, "unit": "cell-updates/s",
-                           "how": f"each request alone, its own FP64 MeshBlock, "
-                                  f"{plain_steps} steps after warm-up, graphs on"},
-            "vs_plain_fp64": total / gpu_s / plain,
+                    "wall_s": wall,
+                    "note": "wall clock of the whole trace through Server.run: "
+                            "arrivals, initial states host->device, results "
+                            "device->host"},
+            "plain_fp64": {"device": plain["device"], "wall": plain["wall"],
+                           "unit": "cell-updates/s",
+                           "how": "each request alone, its own FP64 MeshBlock, "
+                                  "graphs on; device: CUDA events around "
+                                  f"{plain['steps_per_request']} steps at a fixed "
+                                  "CFL dt; wall: the same steps with the CFL dt "
+                                  "read on the host each step"},
+            "vs_plain_fp64": value / plain["device"],
+            "vs_plain_fp64_wall": job_rate(total, world, wall) / plain["wall"],
+            "clock_note": "vs_plain_fp64: CUDA-event time on both sides; "
+                          "vs_plain_fp64_wall: wall clock on both sides",
+            "alone_equals_mix": same,
+            "fp32_rel_l2_vs_fp64": err,
+            "fp32_check": (f"request {small.rid} ({small.cells} cells) after "
+                           f"{small.steps} steps, relative L2 per field "
+                           "(rho, m1, m2, m3, E) against the FP64 path"),
             "max_running": srv.max_running, "handle_rebuilds": srv.rebuilds,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak,
-                         "peak_kind": peak_kind, "traffic": None, "kernel": dom,
-                         "runs": solve_phase(reqs[0].options)[0]
-                                 if dom == "vic_solve_kernel" else dom,
-                         "mean_launch_us": kms[dom][0] / kms[dom][1] * 1e3,
+                         "peak_kind": peak_kind, "traffic": None,
+                         "basis": f"B_alg = {b_alg(s_bytes)} B per cell-update "
+                                  "per RK3 step (5 reads + 3 writes x 5 "
+                                  f"variables x {s_bytes} B) x the device-timed "
+                                  "cell-updates/s of the whole step",
+                         "dominant_kernel": dom,
+                         "dominant_share": kms[dom][0] / ktot,
+                         "scratch_bytes_per_cell_step": serving_scratch(reqs[0].options),
                          "limiter": solve_phase(reqs[0].options)[2]
-                                    if dom == "vic_solve_kernel" else
-                                    FP64_ISSUE},
+                                    if dom == "vic_solve_kernel" else FP64_ISSUE},
             "kernels": {k: {"launches": n, "mean_us": ms / n * 1e3,
-                            "share": ms / sum(v[0] for v in kms.values())}
+                            "share": ms / ktot}
                         for k, (ms, n) in kms.items()},
             "cpu_baseline": cb,
             "clocks": clk.summary(),
             "gpu_launches": srv.launches,
         }
-        print(json.dumps(line), flush=True)
-    ranks.close()
-    return 0
+        if emit:
+            print(json.dumps(line), flush=True)
+    if own:
+        ranks.close()
+    return line
+
+
+def serving_scratch(opts):
+    """Bytes of implementation scratch (the implicit solve's and the x3
+    sweep's) moved per interior cell per RK3 step: not algorithmic."""
+    c = opts.coord()
+    per_stage = solve_phase(opts)[1] + (40 + 600 + 40)  # solve phase, assembly
+    per_stage += 120  # the finish's D, du, du0
+    if c.nx3 > 1:
+        per_stage += 2 * 5 * 4  # a3 dF3 written and read
+    return 3 * per_stage
 
 
 def serving_cpu_baseline(req, seconds):
@@ -993,7 +1151,9 @@ def run_reference_serving(args):
         "ms_per_step": reqs[0].cells / val * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded convection requests, seeded arrivals)",
-        "config": serving_config(reqs, 1), "cpu_baseline": cb,
+        "config": serving_config(reqs, 1, int(args.serve_budget_gb * (1 << 30))
+                                 if args.serve_budget_gb else None),
+        "cpu_baseline": cb,
         "e2e": {"value": val, "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0}}), flush=True)
     return 0
@@ -1152,8 +1312,56 @@ def run_reference_cubed_sphere(args):
     return 0
 
 
+def run_batched_served(args):
+    """The default line: the batched ensemble (value, e2e, K steps timed)
+    with the serving trace as its "served" object; the headline latency and
+    the served-vs-plain ratio are lifted to the top level."""
+    ranks = Ranks()
+    line = run_ensemble(args, ranks, emit=False)
+    served = run_serving(args, ranks, emit=False)
+    if ranks.rank == 0:
+        line["metric"] = METRIC
+        line["config"]["workload"] = ("batched + served: " +
+                                      line["config"]["workload"] + "; " +
+                                      served["config"]["workload"])
+        line["latency"] = served["latency"]
+        line["served_vs_plain_fp64"] = served["vs_plain_fp64"]
+        line["served_vs_plain_fp64_wall"] = served["vs_plain_fp64_wall"]
+        line["served"] = served
+        line["gpu_launches"] += served["gpu_launches"]
+        print(json.dumps(line), flush=True)
+    ranks.close()
+    return 0
+
+
+def run_reference_batched_served(args):
+    """The reference arm of the default line: the CPU oracle on the
+    ensemble's members (value), with the served trace's CPU sample beside."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    import io
+    import contextlib
+    buf = io.StringIO()
+    with contextlib.redirect_stdout(buf):
+        run_reference_ensemble(args)
+    line = json.loads(buf.getvalue().strip().splitlines()[-1])
+    line["metric"] = METRIC
+    reqs = serving_trace(args.requests, args.serve_steps, args.precision)
+    line["config"]["workload"] = ("batched + served: " + line["config"]["workload"]
+                                  + "; " + serving_config(reqs, 1)["workload"])
+    line["served_cpu_baseline"] = serving_cpu_baseline(
+        min(reqs, key=lambda r: r.cells), max(2.0, args.cpu_seconds / 2))
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
+    if args.workload == "batched-served":
+        if args.impl == "reference":
+            return run_reference_batched_served(args)
+        return run_batched_served(args)
     if args.workload == "cubed-sphere":
         if args.impl == "reference":
             return run_reference_cubed_sphere(args)

@@ -221,6 +221,7 @@ class Server:
         self.L = _lib.load()
         self.max_running = 0
         self.rebuilds = 0
+        self.budget: Optional[int] = None  # the budget of the last run
         self.gpu_step_ms: List[float] = []
         self.launches = 0
         self.h2d_bytes = 0
@@ -302,6 +303,7 @@ class Server:
             if budget is None:
                 free, _ = torch.cuda.mem_get_info(self.device)
                 budget = max(0, free - self.reserve)
+            self.budget = budget
             pending = sorted(requests, key=lambda r: (r.arrival, r.rid))
             running: List[_Slot] = []
             finishing = []
