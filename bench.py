@@ -867,19 +867,28 @@ def b_alg(s_bytes: int, nvar: int = 5) -> int:
     return 8 * nvar * s_bytes
 
 
+def as_fp64(opts):
+    """A copy of a deck on the plain FP64 path: FP64 state, FP64 implicit
+    assembly and the direct solve."""
+    import copy
+    o = copy.deepcopy(opts)
+    o.hydro().precision = "float64"
+    if o.hydro().icorr is not None:
+        o.hydro().icorr.precision = "float64"
+    return o
+
+
 def plain_fp64(reqs, dev, steps=3):
     """plain_fp64_blocks over serving requests: each grid shape of the trace
     is measured once (on its first request), and the trace's plain time is
     every request's cell-steps at its shape's rate."""
-    import copy
     first = {}
     for r in reqs:
         c = r.options.coord()
         first.setdefault((c.nx1, c.nx2, c.nx3), r)
     rate = {}
     for shape, r in first.items():
-        o64 = copy.deepcopy(r.options)
-        o64.hydro().precision = "float64"
+        o64 = as_fp64(r.options)
         rate[shape] = plain_fp64_blocks([(o64, r.initial)], dev, steps)
     out = {"steps_per_request": steps, "shapes": len(rate)}
     for clock in ("device", "wall"):
@@ -937,12 +946,9 @@ def plain_fp64_blocks(pairs, dev, steps=3):
 def fp64_reference_state(req, dev):
     """The request's FP64 state after its steps: the plain FP64 path
     (bitwise the CPU oracle's FP64 path), each step at its own CFL dt."""
-    import copy
     import torch
     import snapy_gb300 as sg
-    o64 = copy.deepcopy(req.options)
-    o64.hydro().precision = "float64"
-    blk = sg.MeshBlock(o64).to(dev)
+    blk = sg.MeshBlock(as_fp64(req.options)).to(dev)
     vars = {"hydro_w": req.initial().to(dev)}
     blk.initialize(vars)
     for _ in range(req.steps):
