@@ -1185,8 +1185,7 @@ def cs_cpu_baseline(n, seconds):
     from oracle.cubed_sphere import CubedSphere
     from snapy_gb300 import cubed_sphere as cs
     O.build()
-    g = cs.geometry(n, 6.371e6)
-    o = CubedSphere(n, g, cs.ghost_table(n, g), cs.seam_table(n, g), cs.RK3, 0.9)
+    o = CubedSphere(n, cs.RK3, 0.9)
     u = cs.bump(n, seed=CS_SEED)
     o.fill(u)
     u0 = np.zeros_like(u)

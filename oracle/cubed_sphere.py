@@ -3,9 +3,10 @@ INFRASTRUCTURE ONLY -- the checker of the GPU path, never part of it.
 
 The array plumbing is numpy; the pointwise reconstruction (WENO5 / cp5) and
 the shallow-roe solver are the C oracle's (oracle/sg_oracle.c), pinned to the
-reference's kernels.  The grid geometry and the two seam tables are inputs,
-built by snapy_gb300.cubed_sphere on the host, as the Cartesian oracle takes
-its x1 faces; the tables are checked separately against analytic fields.
+reference's kernels.  The grid geometry and the panel-seam exchanges (the
+ghost halo, the face states at the seams, the single-valued seam fluxes) are
+oracle/cs_seams.py's restatement of the reference's own routines; nothing is
+taken from the product's tables.
 
 One stage follows the reference (src/hydro/hydro_forward.cpp with the
 gnomonic coordinate of src/coord/gnomonic_equiangle.cpp):
@@ -13,21 +14,24 @@ gnomonic coordinate of src/coord/gnomonic_equiangle.cpp):
   _cons2prim, src/eos/shallow_water.cpp:30-42; coord_vec_raise_impl,
   src/coord/coord_utils_impl.h:9-16);
   x2 / x3 face states, weno5 for Phi and cp5 for the velocities
-  (reconstruct.cpp:151-187);
+  (reconstruct.cpp:151-187), then the cross-panel face-state sync at the
+  seams (hydro_forward.cpp:719-757, cs_seams.seam_states_all);
   to the face frame (prim2local2_/3_, gnomonic_equiangle.cpp:357-398),
   shallow_roe with dir yz (riemann_kernels.h:447-495) or the product's
-  shallow-water HLLC (og_hllc_sw_batch), back to covariant
-  fluxes (flux2global2_/3_, :414-463);
-  the seam faces single-valued (src/layout/seam_register.cpp:35);
+  shallow-water HLLC (og_hllc_sw_batch, no reference counterpart), back to
+  covariant fluxes (flux2global2_/3_, :414-463);
+  the seam faces single-valued (reconcile_panel_seams, seam_register.cpp:35,
+  cs_seams.reconcile);
   div = (A2 dF2 + A3 dF3) / V (coordinate.cpp:618-662), minus the metric
   sources x_ov_rD (p + Phi v3 v3 sin^2), y_ov_rC (p + Phi v2 v2 sin^2),
   p = Phi^2 / 2 (gnomonic_equiangle.cpp:465-521); du = -dt div;
-  the RK combine, then the seam halo fill.
+  the RK combine, then the seam halo fill (cs_seams.fill).
 """
 from __future__ import annotations
 
 import numpy as np
 
+from . import cs_seams as R
 from . import oracle as O
 
 NG = 3
@@ -53,12 +57,13 @@ def _roe(wl: np.ndarray, wr: np.ndarray, dim: int, hllc: bool = False) -> np.nda
 
 class CubedSphere:
     """Six panels (6, 4, nc, nc) FP64: Phi, and the radial and the two
-    covariant tangential momenta."""
+    covariant tangential momenta, on the reference's geometry (radius r,
+    one radial cell [r, r + 1] as examples/shallow_splash.yaml has it)."""
 
-    def __init__(self, n, geo, ghost_tab, seam_tab, wght, cfl, riemann="shallow-roe"):
-        self.n, self.g = n, geo
+    def __init__(self, n, wght, cfl, riemann="shallow-roe", radius=6.371e6):
+        self.n = n
+        self.g = R.geometry(n, radius)
         self.hllc = riemann == "hllc"
-        self.gt, self.st = ghost_tab, seam_tab
         self.wght, self.cfl = wght, cfl
         self.nc = n + 2 * NG
 
@@ -77,48 +82,37 @@ class CubedSphere:
 
     def fill(self, u):
         """The seam halo of every panel (in place)."""
-        t = self.gt
-        flat = u.transpose(1, 0, 2, 3).reshape(4, -1)
-        d, s0, s1 = t[:, 0].astype(np.int64), t[:, 1].astype(np.int64), t[:, 2].astype(np.int64)
-        x = t[:, 3]
-        for v in (IDN, IVX):
-            a, b = flat[v, s0], flat[v, s1]
-            flat[v, d] = a + x * (b - a)
+        R.fill(u, self.g)
 
-        def glob(idx, c, ta, tb):
-            m2, m3 = flat[IVY, idx], flat[IVZ, idx]
-            s2 = 1. - c * c
-            v2 = m2 / s2 - m3 * c / s2
-            v3 = -m2 * c / s2 + m3 / s2
-            return [ta[:, q] * v2 + tb[:, q] * v3 for q in range(3)]
-
-        V0 = glob(s0, t[:, 4], t[:, 5:8], t[:, 8:11])
-        V1 = glob(s1, t[:, 11], t[:, 12:15], t[:, 15:18])
-        V = [V0[q] + x * (V1[q] - V0[q]) for q in range(3)]
-        ta, tb = t[:, 18:21], t[:, 21:24]
-        flat[IVY, d] = (V[0] * ta[:, 0] + V[1] * ta[:, 1]) + V[2] * ta[:, 2]
-        flat[IVZ, d] = (V[0] * tb[:, 0] + V[1] * tb[:, 1]) + V[2] * tb[:, 2]
-        u[:] = flat.reshape(4, 6, self.nc, self.nc).transpose(1, 0, 2, 3)
-
-    def _faces(self, w, axis):
-        """Face fluxes of one direction: x2 (axis 2: faces j = NG..NG+n of
-        rows k = NG..NG+n-1) or x3 (axis 1)."""
-        n, g = self.n, self.g
+    def _states(self, w, axis):
+        """Face states of one direction: x2 (axis 2: faces j = NG..NG+n of
+        rows k = NG..NG+n-1) or x3 (axis 1); (wl, wr) each (6, 4, ...)."""
+        n = self.n
         fi = np.arange(NG, NG + n + 1)  # faces
         ri = np.arange(NG, NG + n)      # rows
         if axis == 2:
             st = np.stack([w[:, :, ri][:, :, :, fi + o] for o in range(-3, 3)], -1)
-            cos, sin = g["cos_f2"][np.ix_(ri, fi)], g["sin_f2"][np.ix_(ri, fi)]
         else:
             st = np.stack([w[:, :, fi + o][:, :, :, ri] for o in range(-3, 3)], -1)
-            cos, sin = g["cos_f3"][np.ix_(fi, ri)], g["sin_f3"][np.ix_(fi, ri)]
-        # st: (6, 4, rows/faces..., 6 cells)
         wl = np.empty(st.shape[:-1])
         wr = np.empty(st.shape[:-1])
         for v in range(4):
             weno = v == IDN
             wl[:, v] = _recon(st[:, v, ..., 0:5], weno, 1).reshape(wl[:, v].shape)
             wr[:, v] = _recon(st[:, v, ..., 1:6], weno, 0).reshape(wr[:, v].shape)
+        return wl, wr
+
+    def _faces(self, wl, wr, axis):
+        """Face fluxes of one direction from its face states (seam states
+        already exchanged): x2 (axis 2) or x3 (axis 1)."""
+        n, g = self.n, self.g
+        fi = np.arange(NG, NG + n + 1)  # faces
+        ri = np.arange(NG, NG + n)      # rows
+        if axis == 2:
+            cos, sin = g["cos_f2"][np.ix_(ri, fi)], g["sin_f2"][np.ix_(ri, fi)]
+        else:
+            cos, sin = g["cos_f3"][np.ix_(fi, ri)], g["sin_f3"][np.ix_(fi, ri)]
+        wl, wr = wl.copy(), wr.copy()
         # to the face frame
         for w_ in (wl, wr):
             uu2, uu3 = w_[:, IVY].copy(), w_[:, IVZ].copy()
@@ -162,29 +156,14 @@ class CubedSphere:
         """Full face arrays F2 (6, 4, nc, nc+1), F3 (6, 4, nc+1, nc), zero
         outside the computed faces, seam faces single-valued."""
         n, nc = self.n, self.nc
+        w2l, w2r = self._states(w, 2)
+        w3l, w3r = self._states(w, 1)
+        R.seam_states_all(w2l, w2r, w3l, w3r, self.g)
         F2 = np.zeros((6, 4, nc, nc + 1))
         F3 = np.zeros((6, 4, nc + 1, nc))
-        F2[:, :, NG:NG + n, NG:NG + n + 1] = self._faces(w, 2)
-        F3[:, :, NG:NG + n + 1, NG:NG + n] = self._faces(w, 1)
-        f2 = F2.transpose(1, 0, 2, 3).reshape(4, -1)
-        f3 = F3.transpose(1, 0, 2, 3).reshape(4, -1)
-        src = {2: f2.copy(), 3: f3.copy()}
-        for row in self.st:
-            dd, di, sd, si, sign, c = int(row[0]), int(row[1]), int(row[2]), int(row[3]), row[4], row[5]
-            ta_s, tb_s, ta_d, tb_d = row[6:9], row[9:12], row[12:15], row[15:18]
-            s = src[sd]
-            dst = f2 if dd == 2 else f3
-            m2, m3 = s[IVY, si], s[IVZ, si]
-            s2 = 1. - c * c
-            v2 = m2 / s2 - m3 * c / s2
-            v3 = -m2 * c / s2 + m3 / s2
-            V = [ta_s[q] * v2 + tb_s[q] * v3 for q in range(3)]
-            dst[IDN, di] = sign * s[IDN, si]
-            dst[IVX, di] = sign * s[IVX, si]
-            dst[IVY, di] = sign * ((V[0] * ta_d[0] + V[1] * ta_d[1]) + V[2] * ta_d[2])
-            dst[IVZ, di] = sign * ((V[0] * tb_d[0] + V[1] * tb_d[1]) + V[2] * tb_d[2])
-        F2 = f2.reshape(4, 6, nc, nc + 1).transpose(1, 0, 2, 3)
-        F3 = f3.reshape(4, 6, nc + 1, nc).transpose(1, 0, 2, 3)
+        F2[:, :, NG:NG + n, NG:NG + n + 1] = self._faces(w2l, w2r, 2)
+        F3[:, :, NG:NG + n + 1, NG:NG + n] = self._faces(w3l, w3r, 1)
+        R.reconcile(F2, F3, self.g)
         return F2, F3
 
     def tendency(self, u, dt):

@@ -82,7 +82,7 @@ class CsDesc(ctypes.Structure):
                 ("wght", (ctypes.c_double * 3) * 3), ("cfl", ctypes.c_double),
                 ("geo", _vp), ("ghost_tab", _vp), ("nghost", _i32),
                 ("seam_tab", _vp), ("nseam", _i32), ("phi_ref", ctypes.c_double),
-                ("riemann", _i32)]
+                ("riemann", _i32), ("seam_state_tab", _vp), ("nseam_state", _i32)]
 
 
 # every symbol include/snapy_gb300.h declares, with its ctypes signature

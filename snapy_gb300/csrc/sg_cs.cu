@@ -50,6 +50,7 @@ constexpr int kThreads = 256;
 constexpr int kNg = 3;
 constexpr int kGhostStride = 24;
 constexpr int kSeamStride = 18;
+constexpr int kSeamStateStride = 16;
 
 // offsets of the geometry arrays in the device block (see sg_cs_desc); the
 // FP32 kernels read an FP32 copy made at sg_cs_create (the same values their
@@ -89,6 +90,7 @@ struct CsParams {
   int nghost;
   const void* stab;
   int nseam;
+  const void* sst;  // the seam face-state table (4 sides x n per panel)
   const void* in;
   const void* u0;
   void* out;
@@ -262,6 +264,47 @@ __global__ void __launch_bounds__(kThreads) cs_flux_kernel(CsParams P) {
         wl[v] = sg::cp5_cp<T>(st[0][v], st[1][v], st[2][v], st[3][v], st[4][v]);
         wr[v] = sg::cp5_cm<T>(st[1][v], st[2][v], st[3][v], st[4][v], st[5][v]);
       }
+    }
+    // a seam face: the exterior-side state is the neighbour panel's own
+    // interior-side state at the same face, its velocities mapped into this
+    // panel's frame (the reference's cross-panel face-state sync)
+    int side = -1, along = 0;
+    if (x2 && (j == kNg || j == kNg + n)) {
+      side = j == kNg ? 0 : 1;
+      along = k - kNg;
+    } else if (!x2 && (k == kNg || k == kNg + n)) {
+      side = k == kNg ? 2 : 3;
+      along = j - kNg;
+    }
+    if (side >= 0) {
+      const T* r = static_cast<const T*>(P.sst) +
+                   ((size_t)(p * 4 + side) * n + along) * kSeamStateStride;
+      const int qp = (int)r[0], c0 = (int)r[1], cst = (int)r[2];
+      const bool left = r[3] != T(0);
+      const T* qq = U + (size_t)qp * 4 * pst;
+      T s5[5][4];
+#pragma unroll
+      for (int m = 0; m < 5; ++m) {
+        const size_t c = (size_t)(c0 + m * cst);
+        sw_prim<T>(qq, pst, c, T(G.cos_c[c]), s5[m], phi0);
+      }
+      T we[4];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        if (v == IDN)
+          we[v] = left ? sg::weno5_cp<T>(s5[0][v], s5[1][v], s5[2][v], s5[3][v], s5[4][v], false)
+                       : sg::weno5_cm<T>(s5[0][v], s5[1][v], s5[2][v], s5[3][v], s5[4][v], false);
+        else
+          we[v] = left ? sg::cp5_cp<T>(s5[0][v], s5[1][v], s5[2][v], s5[3][v], s5[4][v])
+                       : sg::cp5_cm<T>(s5[0][v], s5[1][v], s5[2][v], s5[3][v], s5[4][v]);
+      }
+      const T* M = r + 4;
+      T* ext = (side == 0 || side == 2) ? wl : wr;
+      ext[IDN] = we[IDN];
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+        ext[IVX + a] = (M[3 * a] * we[IVX] + M[3 * a + 1] * we[IVY]) +
+                       M[3 * a + 2] * we[IVZ];
     }
     const size_t fidx = x2 ? (size_t)k * (nc + 1) + j : (size_t)k * nc + j;
     const T cs = T(x2 ? G.cos_f2[fidx] : G.cos_f3[fidx]);
@@ -539,6 +582,7 @@ struct sg_cs_handle {
   float* geo32 = nullptr;
   float* gtab32 = nullptr;
   float* stab32 = nullptr;
+  float* sst32 = nullptr;
   void* buf[3] = {nullptr, nullptr, nullptr};
   void* scratch = nullptr;
   int cur = 0, base = 0;
@@ -560,6 +604,9 @@ int sg_cs_create(const sg_cs_desc* d, sg_cs_handle** out) {
     return cs_fail(SG_ERR_ARG, "sg_cs_create: riemann %d", d->riemann);
   if (d->nstage < 1 || d->nstage > 3)
     return cs_fail(SG_ERR_ARG, "sg_cs_create: nstage %d", d->nstage);
+  if (!d->seam_state_tab || d->nseam_state != 24 * d->n)
+    return cs_fail(SG_ERR_ARG, "sg_cs_create: the seam face-state table needs "
+                   "24 n = %d rows (got %d)", 24 * d->n, d->nseam_state);
   auto* h = new sg_cs_handle();
   h->d = *d;
   // key[0]: the min key, key[1]: a NaN flag
@@ -581,13 +628,16 @@ int sg_cs_create(const sg_cs_desc* d, sg_cs_handle** out) {
     const size_t ng = 7 * nc * nc + 6 * nc * (nc + 1);
     const size_t nt = (size_t)kGhostStride * d->nghost;
     const size_t ns = (size_t)kSeamStride * d->nseam;
+    const size_t nss = (size_t)kSeamStateStride * d->nseam_state;
     e = cudaMalloc(&h->geo32, ng * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc(&h->gtab32, nt * sizeof(float));
     if (e == cudaSuccess) e = cudaMalloc(&h->stab32, ns * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&h->sst32, nss * sizeof(float));
     if (e == cudaSuccess) {
       to_f32<<<grid_for(ng), kThreads>>>(d->geo, h->geo32, ng);
       to_f32<<<grid_for(nt), kThreads>>>(d->ghost_tab, h->gtab32, nt);
       to_f32<<<grid_for(ns), kThreads>>>(d->seam_tab, h->stab32, ns);
+      to_f32<<<grid_for(nss), kThreads>>>(d->seam_state_tab, h->sst32, nss);
       e = cudaGetLastError();
       if (e == cudaSuccess) e = cudaDeviceSynchronize();
     }
@@ -597,6 +647,7 @@ int sg_cs_create(const sg_cs_desc* d, sg_cs_handle** out) {
     cudaFree(h->geo32);
     cudaFree(h->gtab32);
     cudaFree(h->stab32);
+    cudaFree(h->sst32);
     delete h;
     return cs_fail(SG_ERR_CUDA, "sg_cs_create: %s", cudaGetErrorString(e));
   }
@@ -610,6 +661,7 @@ int sg_cs_destroy(sg_cs_handle* h) {
   cudaFree(h->geo32);
   cudaFree(h->gtab32);
   cudaFree(h->stab32);
+  cudaFree(h->sst32);
   delete h;
   return 0;
 }
@@ -685,6 +737,7 @@ static CsParams cs_params(const sg_cs_handle* h) {
   P.nghost = h->d.nghost;
   P.stab = f32 ? (const void*)h->stab32 : (const void*)h->d.seam_tab;
   P.nseam = h->d.nseam;
+  P.sst = f32 ? (const void*)h->sst32 : (const void*)h->d.seam_state_tab;
   P.phi0 = h->d.dtype == SG_F32 ? h->d.phi_ref : 0.;
   P.hllc = h->d.riemann == SG_CS_HLLC;
   const size_t nc = P.nc;

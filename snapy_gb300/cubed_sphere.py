@@ -26,10 +26,13 @@ Seams (src/layout/cubed_sphere_layout.cpp:563-803, gnomonic_equiangle.cpp
 neighbour panel at the matching depth; along the edge it falls between two
 of the neighbour's cells.  The ghost takes the linear interpolation of those
 two (written about the first, so equal values are returned exactly); its
-momentum goes through the global frame: each source's covariant momentum is
-raised with its cell cosine to the unit (alpha, beta) tangents, written as a
-3-D vector, interpolated, and projected on the ghost's tangents (covariant
-components are projections).  Seam face fluxes are made single-valued as
+momentum goes through the local geographic frame, as the reference's seam
+exchange carries it (PanelRotation, src/coord/coord_rotation.cpp:105-147):
+each source's covariant momentum is raised with its cell cosine to the unit
+(alpha, beta) tangents and written in the (r, theta, phi) frame of its own
+cell, those components are interpolated, and the ghost's covariant pair is
+the vector with those components in the ghost's own frame, projected on the
+ghost's tangents (covariant components are projections).  Seam face fluxes are made single-valued as
 reconcile_panel_seams does (src/layout/seam_register.cpp:35): the lower
 panel owns a seam, the other takes its flux, momentum rows rotated the same
 way, with the sign flipped where both faces are the panels' low (or high)
@@ -58,10 +61,14 @@ SEAM_STRIDE = 18
 def geometry(n: int, r_in: float, dr: float = 1.0) -> Dict[str, np.ndarray]:
     """FP64 panel geometry on the padded grid, arrays indexed [k, j] (x3,
     x2); face arrays carry one more index along their direction."""
+    import torch
     nc = n + 2 * NG
     d = 0.5 * math.pi / n
-    x2f = -0.25 * math.pi + (np.arange(nc + 1) - NG) * d
-    x2v = -0.25 * math.pi + (np.arange(nc) - NG + 0.5) * d
+    # the faces as the reference lays a block's axis out: one linspace over
+    # the global range widened by the ghosts (src/coord/coordinate.cpp:438)
+    x2f = torch.linspace(-0.25 * math.pi - NG * d, 0.25 * math.pi + NG * d, nc + 1,
+                         dtype=torch.float64).numpy()
+    x2v = 0.5 * (x2f[:-1] + x2f[1:])
     x = np.tan(x2v)[None, :]
     xf = np.tan(x2f)[None, :]
     y = np.tan(x2v)[:, None]
@@ -127,6 +134,19 @@ def tangents(p: int, alpha, beta):
     return ta, tb
 
 
+def geo_frame(P: np.ndarray):
+    """The local geographic frame (r, theta, phi) at unit positions P
+    [..., 3]: r = P, theta = (x z / s, y z / s, -s), phi = (-y / s, x / s,
+    0), s = sqrt(x^2 + y^2) (the frame of PanelRotation,
+    src/coord/coord_rotation.cpp:12-58; no cell centre or ghost of an
+    even-sized grid lies on a pole)."""
+    x, y, z = P[..., 0], P[..., 1], P[..., 2]
+    s = np.sqrt(x * x + y * y)
+    th = np.stack([x * z / s, y * z / s, -s], axis=-1)
+    ph = np.stack([-y / s, x / s, np.zeros_like(s)], axis=-1)
+    return P, th, ph
+
+
 def on_panel(q: int, P: np.ndarray):
     """(alpha, beta) of unit vectors P on panel q (P . n_q > 0)."""
     n, ea, eb = FRAMES[q]
@@ -180,7 +200,13 @@ def ghost_table(n: int, geo: Dict[str, np.ndarray]) -> np.ndarray:
                 assert np.max(np.abs(perp - pi_)) < 1e-6, (p, side, depth)
                 u0 = np.clip(np.floor(u), 0, n - 2).astype(int)
                 x = u - u0
+                # the ghost's covariant pair from geographic components:
+                # m2 = V . ta_g with V = V_r r + V_th th + V_ph ph (at the
+                # ghost), so its row is (ta_g . r, ta_g . th, ta_g . ph)
                 ta_g, tb_g = tangents(p, al, be)
+                fr_g = geo_frame(P)
+                rows_a = np.stack([np.sum(ta_g * e, -1) for e in fr_g], -1)
+                rows_b = np.stack([np.sum(tb_g * e, -1) for e in fr_g], -1)
                 for m in range(n):
                     srcs = []
                     for s in (u0[m], u0[m] + 1):
@@ -190,9 +216,16 @@ def ghost_table(n: int, geo: Dict[str, np.ndarray]) -> np.ndarray:
                     row += [(sq * nc + sk) * nc + sj for sq, sk, sj in srcs]
                     row += [x[m]]
                     for sq, sk, sj in srcs:
-                        ta, tb = tangents(sq, geo["x2v"][sj], geo["x2v"][sk])
-                        row += [geo["cos_c"][sk, sj]] + list(ta) + list(tb)
-                    row += list(ta_g[m]) + list(tb_g[m])
+                        # a source's contravariant pair to geographic
+                        # components at the source cell: the unit tangents
+                        # written in its (r, theta, phi) frame
+                        a_s, b_s = geo["x2v"][sj], geo["x2v"][sk]
+                        ta, tb = tangents(sq, a_s, b_s)
+                        fr = geo_frame(point(sq, a_s, b_s))
+                        row += [geo["cos_c"][sk, sj]]
+                        row += [float(np.dot(ta, e)) for e in fr]
+                        row += [float(np.dot(tb, e)) for e in fr]
+                    row += list(rows_a[m]) + list(rows_b[m])
                     rows.append(row)
     t = np.array(rows, dtype=np.float64)
     assert t.shape[1] == GHOST_STRIDE
@@ -258,6 +291,68 @@ def seam_table(n: int, geo: Dict[str, np.ndarray]) -> np.ndarray:
     return np.ascontiguousarray(t)
 
 
+SEAM_STATE_STRIDE = 16
+
+
+def _side_faces(p: int, side: str, n: int):
+    """(alpha, beta) of the n interior faces of a side of panel p."""
+    d = 0.5 * math.pi / n
+    cen = -0.25 * math.pi + (np.arange(n) + 0.5) * d
+    e = 0.25 * math.pi
+    if side in ("L", "R"):
+        return np.full(n, -e if side == "L" else e), cen
+    return cen, np.full(n, -e if side == "B" else e)
+
+
+def seam_state_table(n: int) -> np.ndarray:
+    """One row of SEAM_STATE_STRIDE doubles per seam face, ordered (panel,
+    side L R B T, along): the neighbour panel q sharing the face, the first
+    of the five cells of q's own interior-side stencil (k nc + j of q's
+    padded panel), the stencil's stride (+1 along x2, +nc along x3), 1 if
+    that state is q's left state (q's R or T side) else 0, and the 3 x 3
+    map (row major) of contravariant velocities (radial, alpha, beta) in
+    q's unit basis at the face to this panel's: M = B_p^-1 B_q with B the
+    basis (r, t_alpha, t_beta) as columns."""
+    nc = n + 2 * NG
+    d = 0.5 * math.pi / n
+    e = 0.25 * math.pi
+    rows = np.zeros((6, 4, n, SEAM_STATE_STRIDE))
+    for p in range(6):
+        for si, side in enumerate(SIDES):
+            al, be = _side_faces(p, side, n)
+            P = point(p, al, be)
+            # the neighbour: the panel just beyond the edge
+            out = 1.01
+            q = _neighbour(p, point(p, al * out if side in "LR" else al,
+                                    be * out if side in "BT" else be))
+            aq, bq = on_panel(q, P)
+            if np.ptp(aq) < 1e-9 and abs(abs(aq[0]) - e) < 1e-9:
+                qside = "L" if aq[0] < 0 else "R"
+                mq = np.rint((bq + e) / d - 0.5).astype(int)
+            else:
+                assert np.ptp(bq) < 1e-9 and abs(abs(bq[0]) - e) < 1e-9
+                qside = "B" if bq[0] < 0 else "T"
+                mq = np.rint((aq + e) / d - 0.5).astype(int)
+            ta_p, tb_p = tangents(p, al, be)
+            ta_q, tb_q = tangents(q, aq, bq)
+            for m in range(n):
+                a = NG + mq[m]  # q's row (L / R) or column (B / T)
+                if qside == "R":
+                    c0, cst, left = a * nc + (NG + n - 3), 1, 1
+                elif qside == "L":
+                    c0, cst, left = a * nc + (NG - 2), 1, 0
+                elif qside == "T":
+                    c0, cst, left = (NG + n - 3) * nc + a, nc, 1
+                else:
+                    c0, cst, left = (NG - 2) * nc + a, nc, 0
+                Bp = np.stack([P[m], ta_p[m], tb_p[m]], axis=1)
+                Bq = np.stack([P[m], ta_q[m], tb_q[m]], axis=1)
+                M = np.linalg.solve(Bp, Bq)
+                rows[p, si, m, :4] = (q, c0, cst, left)
+                rows[p, si, m, 4:13] = M.ravel()
+    return np.ascontiguousarray(rows.reshape(-1, SEAM_STATE_STRIDE))
+
+
 def lonlat(p: int, alpha, beta):
     """Longitude and latitude of panel p's points."""
     P = point(p, alpha, beta)
@@ -320,11 +415,13 @@ class SphereSW:
         self.geo = geometry(n, radius)
         gt = ghost_table(n, self.geo)
         st = seam_table(n, self.geo)
+        sst = seam_state_table(n)
         dev = self.device
         self._geo = torch.as_tensor(np.concatenate([self.geo[k].ravel() for k in GEO_ORDER]),
                                     dtype=torch.float64, device=dev)
         self._gt = torch.as_tensor(gt, dtype=torch.float64, device=dev)
         self._st = torch.as_tensor(st, dtype=torch.float64, device=dev)
+        self._sst = torch.as_tensor(sst, dtype=torch.float64, device=dev)
         d = _lib.CsDesc()
         d.n, d.ng = n, NG
         d.dtype = _lib.F64 if self.dtype == torch.float64 else _lib.F32
@@ -336,6 +433,7 @@ class SphereSW:
         d.geo, d.ghost_tab, d.seam_tab = (self._geo.data_ptr(), self._gt.data_ptr(),
                                           self._st.data_ptr())
         d.nghost, d.nseam = gt.shape[0], st.shape[0]
+        d.seam_state_tab, d.nseam_state = self._sst.data_ptr(), sst.shape[0]
         # FP32: the pressure as an anomaly about Phi0 (the mean depth's
         # geopotential); FP64 keeps the reference's form
         d.phi_ref = float(phi_ref)

@@ -1,7 +1,8 @@
 """The cubed-sphere stage on the GPU (six panels, one handle) against the
-oracle: the seam halo and the stage in FP64 at relative L2 1e-12 (the same
-operations in the same order), mass conserved to roundoff, a lake at rest,
-and the FP32 state against the FP64 oracle."""
+oracle, whose geometry and seam exchanges restate the reference's own
+routines (oracle/cs_seams.py): the seam halo, the stage in FP64 at relative
+L2 1e-12 (n = 16, and the benchmark's 6 x 96^2 over 3 steps), mass conserved
+to roundoff, a lake at rest, and the FP32 state against the FP64 oracle."""
 import numpy as np
 import pytest
 import torch
@@ -15,9 +16,24 @@ NG = cs.NG
 
 def oracle_sphere(n, riemann="shallow-roe"):
     from oracle.cubed_sphere import CubedSphere
-    g = cs.geometry(n, 6.371e6)
-    return CubedSphere(n, g, cs.ghost_table(n, g), cs.seam_table(n, g), cs.RK3, 0.9,
-                       riemann=riemann)
+    return CubedSphere(n, cs.RK3, 0.9, riemann=riemann)
+
+
+def ghost_mask(n):
+    nc = n + 2 * NG
+    m = np.zeros((nc, nc), dtype=bool)
+    I = slice(NG, NG + n)
+    m[I, :NG] = m[I, NG + n:] = m[:NG, I] = m[NG + n:, I] = True
+    return m
+
+
+def errors(got, want):
+    """Relative L2 per field over the interior; the radial momentum row (0
+    on both sides up to the reference's round-off) against the tangential
+    momenta's norm."""
+    e = rel_l2(got, want)
+    e[1] = np.linalg.norm(got[:, 1] - want[:, 1]) / np.linalg.norm(want[:, 2:])
+    return e
 
 
 def interior(u, n):
@@ -44,9 +60,10 @@ def test_seam_fill_matches_oracle(cuda):
     sp.initialize(u)
     o.fill(u)
     got = sp.state().cpu().numpy()
-    d = o.gt[:, 0].astype(np.int64)
-    flat = lambda a: a.transpose(1, 0, 2, 3).reshape(4, -1)
-    assert np.array_equal(flat(got)[:, d], flat(u)[:, d])
+    m = ghost_mask(n)
+    assert np.abs(got[:, 0][:, m] - u[:, 0][:, m]).max() <= 1e-15 * 9500.
+    sc = np.abs(u[:, 2:][:, :, m]).max()
+    assert np.abs(got[:, 1:][:, :, m] - u[:, 1:][:, :, m]).max() <= 1e-13 * sc
 
 
 @pytest.mark.parametrize("riemann", ["shallow-roe", "hllc"])
@@ -65,8 +82,31 @@ def test_stage_parity_fp64(cuda, riemann):
         sp.step(dt)
         for s in range(3):
             o.stage(u, u0, dt, s)
-        err = rel_l2(interior(sp.state().cpu().numpy(), n), interior(u, n))
-        assert err[[0, 2, 3]].max() <= 1e-12, (step, err)
+        err = errors(interior(sp.state().cpu().numpy(), n), interior(u, n))
+        assert err.max() <= 1e-12, (step, err)
+
+
+def test_stage_parity_fp64_6x96(cuda):
+    """The benchmark's grid, 6 panels of 96 x 96, seeded bump: 3 RK3 steps
+    of the FP64 GPU path against the oracle at relative L2 1e-12 per field,
+    mass conserved to round-off."""
+    n = 96
+    o = oracle_sphere(n)
+    u = cs.bump(n, seed=20261206)
+    sp = cs.SphereSW(n, dtype=torch.float64, device=cuda, graphs=False)
+    sp.initialize(u)
+    o.fill(u)
+    m0 = o.mass(u)
+    u0 = np.zeros_like(u)
+    for step in range(3):
+        dt = float(sp.max_dt().item())
+        assert dt == pytest.approx(o.max_dt(u), rel=1e-15)
+        sp.step(dt)
+        for s in range(3):
+            o.stage(u, u0, dt, s)
+        err = errors(interior(sp.state().cpu().numpy(), n), interior(u, n))
+        assert err.max() <= 1e-12, (step, err)
+    assert abs(sp.mass() / m0 - 1) < 1e-13
 
 
 def test_mass_and_lake_at_rest(cuda):
