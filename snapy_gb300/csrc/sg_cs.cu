@@ -2,7 +2,7 @@
 // n x n cells (nghost 3, one radial cell) in ONE handle, FP64 or FP32 state
 // (6, 4, nc, nc): Phi, the radial and the two covariant tangential momenta.
 //
-// A stage is four launches, each over all six panels:
+// A stage is five launches, each over all six panels:
 //   cs_flux_kernel       every x2 and x3 face of the panels' interiors: the
 //                        primitives of its six-cell stencil (U/Phi, momenta
 //                        raised by the cell cosine), weno5 for Phi and cp5
@@ -12,18 +12,24 @@
 //                        (src/riemann/riemann.cpp:219-346 with
 //                        src/coord/gnomonic_equiangle.cpp:357-463,
 //                        src/riemann/riemann_kernels.h:447-495)
+//   cs_seam_face_kernel  the seam faces again, each with its exterior-side
+//                        state from the neighbour panel's own interior-side
+//                        reconstruction, mapped into this panel's frame at
+//                        the shared face (the cross-panel face-state sync,
+//                        src/hydro/hydro_forward.cpp:719-757)
 //   cs_seam_flux_kernel  the seam faces of the non-owning panels take the
-//                        owner's flux through the global frame
+//                        owner's flux through the Cartesian frame
 //                        (src/layout/seam_register.cpp:35)
 //   cs_update_kernel     (A2 dF2 + A3 dF3) / V minus the metric sources,
 //                        du = -dt div, and the RK combine
 //                        (src/coord/coordinate.cpp:618-662,
 //                        src/coord/gnomonic_equiangle.cpp:465-521)
 //   cs_ghost_kernel      the seam halo: a gather along the neighbour's edge
-//                        row with the momenta through the global frame
+//                        row with the momenta through each point's local
+//                        geographic frame (r, theta, phi)
 //                        (src/layout/cubed_sphere_layout.cpp:563-803,
 //                        src/coord/gnomonic_equiangle.cpp:536-609)
-// All the seam geometry is in two tables built once on the host; the
+// All the seam geometry is in three tables built once on the host; the
 // kernels only gather.  Built with -fmad=false: FP64 runs the checker's
 // operations in its order.
 #include <cuda_runtime.h>
@@ -222,30 +228,19 @@ __device__ __forceinline__ void hllc_sw(const T* L, const T* R, T* F, T phi0) {
   F[ivz] = T(0);
 }
 
-// the faces: thread e < 6 n (n + 1) an x2 face (panel, row k, face j), the
-// rest x3 faces (panel, face k, column j)
+// the flux of one face: panel p, an x2 face (row k, face j) or an x3 face
+// (face k, column j).  side >= 0 (a seam face, side L R B T of the panel,
+// `along` its index on that side) takes the exterior-side state from the
+// seam face-state table
 template <typename T, bool HLLC>
-__global__ void __launch_bounds__(kThreads) cs_flux_kernel(CsParams P) {
+__device__ __forceinline__ void cs_face(const CsParams& P, const Geo<T>& G,
+                                        int p, bool x2, int k, int j,
+                                        int side, int along) {
   const int n = P.n, nc = P.nc;
   const size_t pst = (size_t)nc * nc;  // one variable of a panel
-  const Geo<T> G = geo_of<T>(P.geo, nc);
   const T phi0 = T(P.phi0);
   const T* U = static_cast<const T*>(P.in);
-  const size_t nf = (size_t)6 * n * (n + 1);
-  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < 2 * nf;
-       e += (size_t)gridDim.x * blockDim.x) {
-    const bool x2 = e < nf;
-    const size_t r = x2 ? e : e - nf;
-    int p, k, j;
-    if (x2) {  // faces j = ng..ng+n of rows k = ng..ng+n-1
-      j = kNg + (int)(r % (n + 1));
-      k = kNg + (int)((r / (n + 1)) % n);
-      p = (int)(r / ((size_t)(n + 1) * n));
-    } else {  // faces k = ng..ng+n of columns j = ng..ng+n-1
-      j = kNg + (int)(r % n);
-      k = kNg + (int)((r / n) % (n + 1));
-      p = (int)(r / ((size_t)n * (n + 1)));
-    }
+  {
     const T* q = U + (size_t)p * 4 * pst;
     T st[6][4];
 #pragma unroll
@@ -268,14 +263,6 @@ __global__ void __launch_bounds__(kThreads) cs_flux_kernel(CsParams P) {
     // a seam face: the exterior-side state is the neighbour panel's own
     // interior-side state at the same face, its velocities mapped into this
     // panel's frame (the reference's cross-panel face-state sync)
-    int side = -1, along = 0;
-    if (x2 && (j == kNg || j == kNg + n)) {
-      side = j == kNg ? 0 : 1;
-      along = k - kNg;
-    } else if (!x2 && (k == kNg || k == kNg + n)) {
-      side = k == kNg ? 2 : 3;
-      along = j - kNg;
-    }
     if (side >= 0) {
       const T* r = static_cast<const T*>(P.sst) +
                    ((size_t)(p * 4 + side) * n + along) * kSeamStateStride;
@@ -358,6 +345,50 @@ __global__ void __launch_bounds__(kThreads) cs_flux_kernel(CsParams P) {
     const size_t fst = (size_t)nc * (nc + 1);  // one variable of a panel's faces
 #pragma unroll
     for (int v = 0; v < 4; ++v) out[((size_t)p * 4 + v) * fst + fidx] = F[v];
+  }
+}
+
+// the faces: thread e < 6 n (n + 1) an x2 face (panel, row k, face j), the
+// rest x3 faces (panel, face k, column j), each from its own panel's
+// stencils (the seam faces are redone by cs_seam_face_kernel)
+template <typename T, bool HLLC>
+__global__ void __launch_bounds__(kThreads) cs_flux_kernel(CsParams P) {
+  const int n = P.n;
+  const Geo<T> G = geo_of<T>(P.geo, P.nc);
+  const size_t nf = (size_t)6 * n * (n + 1);
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < 2 * nf;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const bool x2 = e < nf;
+    const size_t r = x2 ? e : e - nf;
+    int p, k, j;
+    if (x2) {  // faces j = ng..ng+n of rows k = ng..ng+n-1
+      j = kNg + (int)(r % (n + 1));
+      k = kNg + (int)((r / (n + 1)) % n);
+      p = (int)(r / ((size_t)(n + 1) * n));
+    } else {  // faces k = ng..ng+n of columns j = ng..ng+n-1
+      j = kNg + (int)(r % n);
+      k = kNg + (int)((r / n) % (n + 1));
+      p = (int)(r / ((size_t)n * (n + 1)));
+    }
+    cs_face<T, HLLC>(P, G, p, x2, k, j, -1, 0);
+  }
+}
+
+// the 24 n seam faces again, each with its exterior-side state from the
+// neighbour panel (thread e: panel e / 4n, side (e / n) % 4 in L R B T,
+// along e % n); launched after cs_flux_kernel so no warp of the bulk pass
+// diverges on them
+template <typename T, bool HLLC>
+__global__ void __launch_bounds__(kThreads) cs_seam_face_kernel(CsParams P) {
+  const int n = P.n;
+  const Geo<T> G = geo_of<T>(P.geo, P.nc);
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < 24 * n;
+       e += gridDim.x * blockDim.x) {
+    const int along = e % n, side = (e / n) % 4, p = e / (4 * n);
+    const bool x2 = side < 2;
+    const int edge = (side & 1) ? kNg + n : kNg;
+    const int k = x2 ? kNg + along : edge, j = x2 ? edge : kNg + along;
+    cs_face<T, HLLC>(P, G, p, x2, k, j, side, along);
   }
 }
 
@@ -781,12 +812,16 @@ int sg_cs_stage(sg_cs_handle* h, int32_t stage, const double* dt_dev,
   if (h->d.dtype == SG_F64) {
     (P.hllc ? cs_flux_kernel<double, true> : cs_flux_kernel<double, false>)
         <<<grid_for(faces), kThreads, 0, s>>>(P);
+    (P.hllc ? cs_seam_face_kernel<double, true> : cs_seam_face_kernel<double, false>)
+        <<<grid_for(24 * (size_t)P.n), kThreads, 0, s>>>(P);
     cs_seam_flux_kernel<double><<<grid_for(P.nseam), kThreads, 0, s>>>(P);
     cs_update_kernel<double><<<grid_for(cells), kThreads, 0, s>>>(P);
     cs_ghost_kernel<double><<<grid_for(P.nghost), kThreads, 0, s>>>(P, P.out);
   } else {
     (P.hllc ? cs_flux_kernel<float, true> : cs_flux_kernel<float, false>)
         <<<grid_for(faces), kThreads, 0, s>>>(P);
+    (P.hllc ? cs_seam_face_kernel<float, true> : cs_seam_face_kernel<float, false>)
+        <<<grid_for(24 * (size_t)P.n), kThreads, 0, s>>>(P);
     cs_seam_flux_kernel<float><<<grid_for(P.nseam), kThreads, 0, s>>>(P);
     cs_update_kernel<float><<<grid_for(cells), kThreads, 0, s>>>(P);
     cs_ghost_kernel<float><<<grid_for(P.nghost), kThreads, 0, s>>>(P, P.out);
