@@ -1003,6 +1003,43 @@ static void tendency_plane(const og_block* b, const double* w, double dt,
   free(vf2);
 }
 
+/* the covariance row of the x3 faces (HydroImpl::_flux_covariance with
+ * dim 3, src/hydro/hydro_forward.cpp:58-231; Cartesian: the IPR row of the
+ * x1-interior cells, sigma1^2 rho D1[h] D1[u_n] of the face means, added to
+ * the face flux before the walls, :800-826) on the faces of the interior
+ * (x2, x1) cells */
+static void x3_covariance(const og_block* b, const double* w, double* f3) {
+  const int n1 = b->nc1, n2 = b->nc2, n3 = b->nc3, ng = b->ng;
+  if (!(b->flux_cov && n1 >= 3)) return;
+  const size_t plane = (size_t)n1 * n2, nc = ncell(b);
+  const int il = ng, iu1 = n1 - ng;
+  const int jl = n2 > 1 ? ng : 0, ju1 = n2 > 1 ? n2 - ng : 1;
+  const long nk = n3 - 2 * ng + 1, nj = ju1 - jl;
+#pragma omp parallel for schedule(static)
+  for (long q = 0; q < nk * nj; ++q) {
+    const int k = ng + (int)(q / nj), j = jl + (int)(q % nj);
+    double h[n1], un[n1], rho[n1];
+    for (int i = il - 1; i <= iu1; ++i) {
+      double wl[5], wr[5], wb_[5];
+      face_lr(b, w + (size_t)j * n1 + i, plane, nc, k, wl, wr);
+      for (int v = 0; v < 5; ++v) wb_[v] = 0.5 * (wl[v] + wr[v]);
+      double p = wb_[OG_IPR];
+      double enth = p / (b->gammad - 1) + p;
+      rho[i] = wb_[OG_IDN];
+      h[i] = enth / rho[i];
+      un[i] = wb_[OG_IVZ];
+    }
+    for (int i = il; i < iu1; ++i) {
+      double dx1 = b->x1v[i + 1] - b->x1v[i - 1];
+      double s2 = b->dx1 * b->dx1 / 12.;
+      double s2rho = s2 * rho[i];
+      double d1h = (h[i + 1] - h[i - 1]) / dx1;
+      double dun = (un[i + 1] - un[i - 1]) / dx1;
+      f3[OG_IPR * nc + (size_t)k * plane + (size_t)j * n1 + i] += s2rho * d1h * dun;
+    }
+  }
+}
+
 /* the tendency, and the register totals T_d into T[d - 1] where set */
 static void tendency_reg(const og_block* b, const double* w, double dt,
                          double* du, double* const* T) {
@@ -1012,12 +1049,13 @@ static void tendency_reg(const og_block* b, const double* w, double dt,
     tendency_plane(b, w, dt, du, NULL, T[0], T[1]);
     return;
   }
-  /* 3-D (no viscosity, no covariance row): the x3 face fluxes of every
-   * line, reflecting x3 walls prescribed, then each x2-x1 plane */
+  /* 3-D (no viscosity): the x3 face fluxes of every line, the x3
+   * covariance row, reflecting x3 walls prescribed, then each x2-x1 plane */
   const int n1 = b->nc1, n2 = b->nc2, n3 = b->nc3, ng = b->ng;
   const size_t plane = (size_t)n1 * n2;
   double* f3 = (double*)calloc(5 * nc, sizeof(double));
   og_flux(b, w, 3, f3);
+  x3_covariance(b, w, f3);
   for (int side = 0; side < 2; ++side) {
     if (b->bc[4 + side] != OG_BC_REFLECTING) continue;
     int k = side ? n3 - ng : ng;

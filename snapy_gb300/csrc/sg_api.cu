@@ -575,10 +575,10 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
       return fail(SG_ERR_ARG, "block %d: sizes (%d, %d, %d)", b, d.nc3, d.nc2,
                   d.nc1);
     }
-    if (d.nc3 > 1 && (d.nu_iso > 0. || d.flux_cov)) {
+    if (d.nc3 > 1 && d.nu_iso > 0.) {
       sg_destroy(h);
       return fail(SG_ERR_UNSUPPORTED, "block %d: 3-D blocks are built without "
-                  "viscosity and without the covariance row", b);
+                  "viscosity", b);
     }
     for (int f = 0; f < 6; ++f)
       if (d.bc[f] < SG_BC_NONE || d.bc[f] > SG_BC_EXTRAPOLATION) {

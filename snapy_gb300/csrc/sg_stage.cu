@@ -1203,7 +1203,9 @@ __global__ void __launch_bounds__(kThreads)
 // primitives in registers, solves each face once and stores a3 (F3[k+1] -
 // F3[k]) of each cell, which the stage kernel adds to its divergence after
 // the x1 and x2 differences, the reference's order.  With a hydrostatic base the
-// pressure is the anomaly about the cell row's base, as on x2 faces; a
+// pressure is the anomaly about the cell row's base, as on x2 faces; the
+// covariance row (src/hydro/hydro_forward.cpp:58-231 with dim 3, added to
+// the face flux before the walls, :800-826) is added to the energy row; a
 // reflecting x3 wall zeroes the mass and energy rows of its face.
 constexpr int kX3Chunk = 16;
 
@@ -1225,12 +1227,32 @@ __global__ void __launch_bounds__(kThreads)
   const double* pbc = B.base ? base_p(B.base, nc1) : nullptr;
   const real a3 = real(B.dx2 * B.dx1);
   const bool wlo = B.bc[4] == kBcReflecting, whi = B.bc[5] == kBcReflecting;
-  const size_t total = (size_t)nx1 * nx2 * nch;
+  // the covariance row of the x3 faces (_flux_covariance, dim 3) needs each
+  // face's mean state on the x1 rows either side: a warp then covers 32
+  // consecutive x1 rows of one (x2, chunk) line -- 30 it owns and a row
+  // either side (an x1 ghost row at the column's ends) -- and trades the
+  // face means by shuffles; every lane of a warp runs the same faces
+  const bool cov = B.flux_cov && nc1 >= 3;
+  const int nw = (nx1 + 29) / 30;  // warps per (x2, chunk) line
+  const size_t total = cov ? (size_t)32 * nw * nx2 * nch
+                           : (size_t)nx1 * nx2 * nch;
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
        e += (size_t)gridDim.x * blockDim.x) {
-    const int i = ng + (int)(e % nx1);
-    const int j = o2 + (int)((e / nx1) % nx2);
-    const int ch = (int)(e / ((size_t)nx1 * nx2));
+    int i, j, ch;
+    bool own = true;
+    if (cov) {
+      const int lane = (int)(e & 31);
+      const size_t wdx = e >> 5;
+      const int row = ng - 1 + 30 * (int)(wdx % nw) + lane;
+      j = o2 + (int)((wdx / nw) % nx2);
+      ch = (int)(wdx / ((size_t)nw * nx2));
+      own = lane >= 1 && lane <= 30 && row < ng + nx1;
+      i = row < ng + nx1 ? row : ng + nx1;  // past the top ghost row: a copy
+    } else {
+      i = ng + (int)(e % nx1);
+      j = o2 + (int)((e / nx1) % nx2);
+      ch = (int)(e / ((size_t)nx1 * nx2));
+    }
     const int k0 = ng + ch * kX3Chunk;
     const int k1 = min(k0 + kX3Chunk, ng + nx3);  // cells k0..k1-1
     const size_t col = (size_t)j * nc1 + i;
@@ -1260,12 +1282,45 @@ __global__ void __launch_bounds__(kThreads)
           wr[v] = cp5_cm(W[1][v], W[2][v], W[3][v], W[4][v], W[5][v]);
         }
       }
+      real dcov = real(0);
+      if (cov) {
+        // the face mean's rho, h = (p / (gamma - 1) + p) / rho (p the
+        // total) and u_n; the covariance s2 rho D1[h] D1[u_n] of the owned
+        // rows from their neighbours' (the x2 row's operations)
+        real wb_[NHYDRO];
+#pragma unroll
+        for (int v = 0; v < NHYDRO; ++v) wb_[v] = real(0.5) * (wl[v] + wr[v]);
+        real pbar = wb_[IPR];
+        if (pbc) pbar = real(pbc[i]) + pbar;
+        const real enth = pbar / (gammad - real(1)) + pbar;
+        const real hh = enth / wb_[IDN], un = wb_[IVZ];
+        const unsigned full = 0xffffffffu;
+        const real hm = __shfl_up_sync(full, hh, 1), hp = __shfl_down_sync(full, hh, 1);
+        const real um = __shfl_up_sync(full, un, 1), up = __shfl_down_sync(full, un, 1);
+        if (own) {
+          const real dx1 = real(B.x1v[i + 1] - B.x1v[i - 1]);
+          const real s2 = real(B.dx1 * B.dx1 / 12.);
+          const real s2rho = s2 * wb_[IDN];
+          const real rdx1 = real(1.) / dx1;
+          const real d1h = vdiv(hp - hm, dx1, rdx1);
+          const real dun = vdiv(up - um, dx1, rdx1);
+          dcov = s2rho * d1h * dun;
+        }
+      }
       if (pbc)
         lmars_flux_anom<real>(wl, wr, gammad, 3, pb, flx);
       else
         riemann<RK>(wl, wr, gammad, 3, flx);
+      if (cov) flx[IPR] += dcov;
       if ((f == ng && wlo) || (f == ng + nx3 && whi))
         flx[IDN] = flx[IPR] = real(0);
+      if (!own) {  // a halo lane: its row's face means only
+#pragma unroll
+        for (int m = 0; m < 5; ++m)
+#pragma unroll
+          for (int v = 0; v < NHYDRO; ++v) W[m][v] = W[m + 1][v];
+        continue;
+      }
       // passive scalars ride on the mass row (the step field's owner rule)
       if (B.nscalar > 0 && (f < k1 || k1 == ng + nx3))
         B.mflux[2][(size_t)f * kst + col] = (double)flx[IDN];

@@ -77,9 +77,6 @@ def scheme_of(options: MeshBlockOptions) -> dict:
     if c.nx3 > 1:
         if h.diffusion is not None and h.diffusion.nu_iso:
             raise DeckError("3-D blocks are built without forcing/diffusion")
-        if h.flux_covariance:
-            raise DeckError("3-D blocks are built without the covariance row: "
-                            "set dynamics/flux-covariance: false")
     intg = options.intg()
     return {
         "riemann": _lib.HLLC if h.riemann.type == "hllc" else _lib.LMARS,

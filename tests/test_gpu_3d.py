@@ -1,7 +1,7 @@
 """3-D blocks (x3 faces by the x3 sweep, (x2, x3) columns of the implicit
-solve) against the oracle: FP64 parity at relative L2 1e-12, FP32 anomalies
-within 1e-5 of the FP64 oracle, and an x3-uniform 3-D block equal bit for
-bit to its 2-D slice."""
+solve) against the oracle: FP64 parity at relative L2 1e-12 with and without
+the flux-covariance row, FP32 anomalies within 1e-5 of the FP64 oracle, and
+an x3-uniform 3-D block equal bit for bit to its 2-D slice."""
 import numpy as np
 import pytest
 import torch
@@ -24,8 +24,9 @@ def rel_l2(a, b):
     return np.array(out)
 
 
-def conv_window(nx1, nx2, nx3, precision, implicit=True, dtheta=2.0):
+def conv_window(nx1, nx2, nx3, precision, implicit=True, dtheta=2.0, cov=True):
     opts = sg.MeshBlockOptions.from_yaml("snapy_gb300/decks/convection3d.yaml")
+    opts.hydro().flux_covariance = cov
     c = opts.coord()
     c.nx1, c.nx2, c.nx3 = nx1, nx2, nx3
     c.x1max, c.x2max, c.x3max = nx1 * 50.0, nx2 * 50.0, nx3 * 50.0
@@ -44,9 +45,12 @@ def interior(opts, u):
     return u[:, ng:c.nc3 - ng, ng:c.nc2 - ng, ng:c.nc1 - ng]
 
 
+@pytest.mark.parametrize("cov", [False, True])
 @pytest.mark.parametrize("implicit", [False, True])
-def test_3d_fp64_parity(oracle, cuda, implicit):
-    opts = conv_window(24, 12, 10, "float64", implicit)
+def test_3d_fp64_parity(oracle, cuda, implicit, cov):
+    """With the covariance row (the reference's default, on x2 and x3
+    faces) and without."""
+    opts = conv_window(24, 12, 10, "float64", implicit, cov=cov)
     blk = sg.MeshBlock(opts).to(cuda)
     w = problems.convection3d(opts, "cpu", seed=11)
     vars = {"hydro_w": w.to(cuda)}

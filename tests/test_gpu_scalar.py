@@ -189,6 +189,7 @@ def test_3d_scalars_against_oracle(oracle, cuda):
     on the (x2, x3) columns) with a tracer: FP64 bitwise with the oracle."""
     cfg = copy.deepcopy(sg.options.yaml_lite.load("snapy_gb300/decks/convection3d.yaml"))
     cfg["scalar"] = {"nvar": 1}
+    cfg["dynamics"]["flux-covariance"] = False  # tracers are built without it
     opts = sg.MeshBlockOptions.from_config(cfg)
     c = opts.coord()
     c.nx1, c.nx2, c.nx3 = 16, 12, 10

@@ -84,6 +84,7 @@ def test_tracers_alone_equal_in_the_mix(cuda):
         cfg = copy.deepcopy(sg.options.yaml_lite.load(
             "snapy_gb300/decks/convection3d.yaml"))
         cfg["scalar"] = {"nvar": 1}
+        cfg["dynamics"]["flux-covariance"] = False  # tracers: without it
         opts = sg.MeshBlockOptions.from_config(cfg)
         c = opts.coord()
         c.nx1, c.nx2, c.nx3 = n, 12, 10

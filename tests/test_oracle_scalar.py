@@ -77,4 +77,7 @@ def test_deck_scalar_section():
             sg.MeshBlockOptions.from_config(bad)
     d3 = copy.deepcopy(sg.options.yaml_lite.load("snapy_gb300/decks/convection3d.yaml"))
     d3["scalar"] = {"nvar": 1}
+    with pytest.raises(DeckError, match="flux-covariance"):
+        sg.MeshBlockOptions.from_config(d3)
+    d3["dynamics"]["flux-covariance"] = False
     assert sg.MeshBlockOptions.from_config(d3).scalar_names == ["scalar0"]

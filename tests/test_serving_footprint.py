@@ -13,6 +13,7 @@ def deck(scalars=0, precision="float32", implicit_precision="float32"):
     cfg = copy.deepcopy(sg.options.yaml_lite.load("snapy_gb300/decks/convection3d.yaml"))
     if scalars:
         cfg["scalar"] = {"nvar": scalars}
+        cfg["dynamics"]["flux-covariance"] = False  # tracers: without it
     opts = sg.MeshBlockOptions.from_config(cfg)
     opts.hydro().precision = precision
     opts.hydro().icorr.precision = implicit_precision
