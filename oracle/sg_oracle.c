@@ -35,6 +35,7 @@
  */
 #include "sg_oracle.h"
 
+#include <float.h>
 #include <math.h>
 #include <stddef.h>
 #include <stdlib.h>
@@ -1124,13 +1125,143 @@ static void step_recursion(const og_block* b, int d, const double* T,
  *   - zero on the reflecting faces (boundary.prescribed, scalar.cpp:163-169);
  *   - the area-weighted divergence, as the hydro's.
  * fm[d - 1]: the mass flux along d (face f below cell f), or NULL */
+/* the scalar face ratio of one side at face q along stride st
+ * (ScalarImpl::forward's face_r, src/scalar/scalar.cpp:100-104): left (ILT,
+ * cp over cells f-3..f+1, donor f-1) or right (IRT, cm over f-2..f+2, donor
+ * f); s_f / rho_f of the floored scale-invariant WENO5 faces, or the donor
+ * cell's ratio where rho_f is not positive */
+static double scalar_face_r(const double* u, const double* sv, size_t nc,
+                            size_t q, size_t st, int left) {
+  const size_t c0 = q - (size_t)(left ? 3 : 2) * st;
+  const size_t donor = left ? q - st : q;
+  double rs[5], ss[5];
+  for (int m = 0; m < 5; ++m) {
+    rs[m] = u[OG_IDN * nc + c0 + m * st];
+    ss[m] = sv[c0 + m * st];
+  }
+  double rf = weno5_point(rs, 1, left ? g_weno5_cp : g_weno5_cm, 1);
+  if (rf < 0.) rf = 0.;
+  double sf = weno5_point(ss, 1, left ? g_weno5_cp : g_weno5_cm, 1);
+  if (sf < 0.) sf = 0.;
+  return rf > 0. ? sf / rf : sv[donor] / u[OG_IDN * nc + donor];
+}
+
+/* the positivity limiter of the scalars (PositivityLimiter::apply with the
+ * scalar's inputs, src/hydro/flux_positivity.cpp:29-268, no carry):
+ *   theta_i = min(1, s_i V (1 - 4096 eps) / (dt out_i)), out_i the outgoing
+ *   A F_s over the faces the divergence uses (1 where nothing drains);
+ *   td the same of the dry density under the mass fluxes; phi = clamp(min
+ *   of the neighbours' s / rho / its own, 0, 1) (0 where s / rho <= 0);
+ *   theta <- theta + phi (min(theta / td, 1) - theta) where 0 < td < 1;
+ *   the ghosts by the kScalar boundary functions; each face flux times its
+ *   donor's theta (the lower cell where F_s > 0) */
+static void scalar_limit(const og_block* b, const double* u, double* const* fm,
+                         double dt, const double* s, double** fs) {
+  const size_t nc = ncell(b);
+  const int ns = b->nscalar, ng = b->ng;
+  const int n[3] = {b->nc1, b->nc2, b->nc3};
+  int lo[3], hi[3];
+  for (int a = 0; a < 3; ++a) {
+    lo[a] = n[a] > 1 ? ng : 0;
+    hi[a] = n[a] > 1 ? n[a] - ng - 1 : 0;
+  }
+  const double area[3] = {b->dx3 * b->dx2, b->dx3 * b->dx1, b->dx2 * b->dx1};
+  const double vol = b->dx3 * (b->dx2 * b->dx1);
+  const double margin = 4096. * DBL_EPSILON, tiny = DBL_MIN;
+  /* channel 0..ns-1: the scalars; channel ns: the dry density */
+  double* theta = (double*)malloc(sizeof(double) * (size_t)(ns + 1) * nc);
+  for (int v = 0; v <= ns; ++v) {
+    const double* f[3];
+    for (int d = 0; d < 3; ++d)
+      f[d] = fs[d] ? (v < ns ? fs[d] + (size_t)v * nc : fm[d]) : NULL;
+    const double* q = v < ns ? s + (size_t)v * nc : u + OG_IDN * nc;
+    double* th = theta + (size_t)v * nc;
+    for (size_t c = 0; c < nc; ++c) th[c] = 1.;
+    for (int k = lo[2]; k <= hi[2]; ++k)
+      for (int j = lo[1]; j <= hi[1]; ++j)
+        for (int i = lo[0]; i <= hi[0]; ++i) {
+          const size_t c = ((size_t)k * n[1] + j) * n[0] + i;
+          double out = 0.;
+          for (int d = 0; d < 3; ++d) {
+            if (!f[d]) continue;
+            const size_t st = dir_stride(b, d + 1);
+            const double up = area[d] * f[d][c + st], dn = area[d] * f[d][c];
+            out = out + ((up > 0. ? up : 0.) + (-dn > 0. ? -dn : 0.));
+          }
+          const double avail = (q[c] > 0. ? q[c] : 0.) * vol * (1. - margin);
+          const double drain = dt * out;
+          if (drain > 0.) {
+            const double t = avail / (drain > tiny ? drain : tiny);
+            th[c] = t < 1. ? t : 1.;
+          }
+        }
+  }
+  const double* td = theta + (size_t)ns * nc;
+  double* relaxed = (double*)malloc(sizeof(double) * (size_t)ns * nc);
+  for (int v = 0; v < ns; ++v)
+    for (size_t c = 0; c < nc; ++c) relaxed[(size_t)v * nc + c] = theta[(size_t)v * nc + c];
+  for (int v = 0; v < ns; ++v)
+    for (int k = lo[2]; k <= hi[2]; ++k)
+      for (int j = lo[1]; j <= hi[1]; ++j)
+        for (int i = lo[0]; i <= hi[0]; ++i) {
+          const size_t c = ((size_t)k * n[1] + j) * n[0] + i;
+          const double* sv = s + (size_t)v * nc;
+          const double qc = sv[c] / u[OG_IDN * nc + c];
+          double low = INFINITY;
+          for (int d = 0; d < 3; ++d) {
+            if (n[d] == 1 && d > 0) continue;
+            const size_t st = dir_stride(b, d + 1);
+            const double qm = sv[c - st] / u[OG_IDN * nc + c - st];
+            const double qp = sv[c + st] / u[OG_IDN * nc + c + st];
+            const double m = qm < qp ? qm : qp;
+            low = d == 0 ? m : (m < low ? m : low);
+          }
+          double phi = 0.;
+          if (qc > 0.) {
+            phi = low / qc;
+            phi = phi < 0. ? 0. : (phi > 1. ? 1. : phi);
+          }
+          const double t = theta[(size_t)v * nc + c], d0 = td[c];
+          if (d0 < 1. && d0 > 0.) {
+            const double r = t / d0;
+            relaxed[(size_t)v * nc + c] = t + phi * ((r < 1. ? r : 1.) - t);
+          }
+        }
+  og_scalar_bc(b, relaxed);
+  for (int d = 0; d < 3; ++d) {
+    if (!fs[d]) continue;
+    const size_t st = dir_stride(b, d + 1);
+    int flo[3], fhi[3];
+    for (int a = 0; a < 3; ++a) {
+      flo[a] = lo[a];
+      fhi[a] = hi[a];
+    }
+    fhi[d] += 1;
+    for (int v = 0; v < ns; ++v)
+      for (int k = flo[2]; k <= fhi[2]; ++k)
+        for (int j = flo[1]; j <= fhi[1]; ++j)
+          for (int i = flo[0]; i <= fhi[0]; ++i) {
+            const size_t c = ((size_t)k * n[1] + j) * n[0] + i;
+            double* F = fs[d] + (size_t)v * nc + c;
+            const double fac = *F > 0. ? relaxed[(size_t)v * nc + c - st]
+                                       : relaxed[(size_t)v * nc + c];
+            *F = *F * fac;
+          }
+  }
+  free(relaxed);
+  free(theta);
+}
+
 static void scalar_tendency(const og_block* b, const double* u,
-                            double* const* fm, double dt, const double* s,
-                            double* ds) {
+                            const double* w, double* const* fm, double dt,
+                            const double* s, double* ds) {
   const size_t nc = ncell(b);
   const int ns = b->nscalar, ng = b->ng;
   const int n[3] = {b->nc1, b->nc2, b->nc3};
   const int weno = 1; /* the hydro's scheme: weno5 for density rows */
+  /* with the covariance row (x2 / x3 faces) the shared positivity limiter
+   * runs too (scalar.cpp:145-160, 195-207) */
+  const int cov_on = b->flux_cov && b->nc1 >= 3 && (b->nc2 > 1 || b->nc3 > 1);
   double* fs[3] = {NULL, NULL, NULL};
   int lo[3], hi[3]; /* interior cells, inclusive */
   for (int a = 0; a < 3; ++a) {
@@ -1147,6 +1278,12 @@ static void scalar_tendency(const og_block* b, const double* u,
       fhi[a] = hi[a];
     }
     fhi[d - 1] += 1; /* the faces of the interior cells, both ends */
+    /* the covariance row of the x2 / x3 faces (scalar_flux_covariance,
+     * src/hydro/hydro_forward.cpp:233-300, Cartesian, no species: q the
+     * mean of the two sides' ratios, s2 rho D1[u_n] D1[q] with rho and u_n
+     * of the hydro's face means) */
+    const int cov = cov_on && d >= 2;
+    const size_t xst = 1; /* x1 neighbours of a face */
     for (int k = flo[2]; k <= fhi[2]; ++k)
       for (int j = flo[1]; j <= fhi[1]; ++j)
         for (int i = flo[0]; i <= fhi[0]; ++i) {
@@ -1156,27 +1293,41 @@ static void scalar_tendency(const og_block* b, const double* u,
                            (f == n[d - 1] - ng &&
                             b->bc[2 * (d - 1) + 1] == OG_BC_REFLECTING);
           const double F = fm[d - 1][q];
-          /* the side F > 0 selects: ILT (cp, cells f-3..f+1, donor f-1);
-           * else IRT (cm, cells f-2..f+2, donor f) */
+          /* the side F > 0 selects */
           const int left = F > 0.;
-          const size_t c0 = q - (size_t)(left ? 3 : 2) * st;
-          const size_t donor = left ? q - st : q;
-          double rs[5];
-          for (int m = 0; m < 5; ++m) rs[m] = u[OG_IDN * nc + c0 + m * st];
-          double rf = weno5_point(rs, 1, left ? g_weno5_cp : g_weno5_cm, 1);
           (void)weno;
-          if (rf < 0.) rf = 0.;
+          double un[3], rhof = 0.;
+          if (cov)
+            for (int m = -1; m <= 1; ++m) {
+              double wl[5], wr[5];
+              face_lr(b, w + q + m * (ptrdiff_t)xst - (size_t)f * st, st, nc, f,
+                      wl, wr);
+              un[m + 1] = 0.5 * (wl[d == 2 ? OG_IVY : OG_IVZ] +
+                                 wr[d == 2 ? OG_IVY : OG_IVZ]);
+              if (m == 0) rhof = 0.5 * (wl[OG_IDN] + wr[OG_IDN]);
+            }
           for (int v = 0; v < ns; ++v) {
-            double ss[5];
-            for (int m = 0; m < 5; ++m) ss[m] = s[v * nc + c0 + m * st];
-            double sf = weno5_point(ss, 1, left ? g_weno5_cp : g_weno5_cm, 1);
-            if (sf < 0.) sf = 0.;
-            const double r = rf > 0. ? sf / rf
-                                     : s[v * nc + donor] / u[OG_IDN * nc + donor];
-            fs[d - 1][v * nc + q] = wall ? 0. : F * r;
+            const double* sv = s + (size_t)v * nc;
+            const double r = scalar_face_r(u, sv, nc, q, st, left);
+            double fl = F * r;
+            if (cov) {
+              double qf[3];
+              for (int m = -1; m <= 1; ++m) {
+                const size_t qm = q + m * (ptrdiff_t)xst;
+                qf[m + 1] = 0.5 * (scalar_face_r(u, sv, nc, qm, st, 1) * 1. +
+                                   scalar_face_r(u, sv, nc, qm, st, 0) * 1.);
+              }
+              const double dx1 = b->x1v[i + 1] - b->x1v[i - 1];
+              const double s2 = b->dx1 * b->dx1 / 12.;
+              const double d1u = (un[2] - un[0]) / dx1;
+              const double d1q = (qf[2] - qf[0]) / dx1;
+              fl = fl + s2 * rhof * d1u * d1q;
+            }
+            fs[d - 1][v * nc + q] = wall ? 0. : fl;
           }
         }
   }
+  if (cov_on) scalar_limit(b, u, fm, dt, s, fs);
   const double a1 = b->dx3 * b->dx2, a2 = b->dx3 * b->dx1;
   const double a3 = b->dx2 * b->dx1;
   const double vol = b->dx3 * (b->dx2 * b->dx1);
@@ -1307,7 +1458,7 @@ void og_stage(const og_block* b, double* u, double* u0, double dt, int stage) {
       if (T[d]) fm[d] = T[d] + OG_IDN * nc;
     if (stage == 0) memcpy(b->scalar0, b->scalar, sizeof(double) * ns * nc);
     ds = (double*)malloc(sizeof(double) * ns * nc);
-    scalar_tendency(b, u, fm, dt, b->scalar, ds);
+    scalar_tendency(b, u, w, fm, dt, b->scalar, ds);
   }
   /* the vertical implicit correction with dt_corr = wght2 dt
    * (hydro_forward.cpp:1153-1168); its posts enter T_1, whose wall faces

@@ -667,11 +667,6 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
       sg_destroy(h);
       return fail(SG_ERR_ARG, "block %d: nscalar %d (0 to 16)", b, d.nscalar);
     }
-    if (d.nscalar > 0 && d.flux_cov && d.nc2 > 1) {
-      sg_destroy(h);
-      return fail(SG_ERR_UNSUPPORTED, "block %d: passive scalars are built "
-                  "without the x2 flux-covariance row", b);
-    }
     B.nscalar = d.nscalar;
     if (d.nscalar > 0) h->scalars = true;
     if (B.implicit_f32) {
@@ -738,7 +733,7 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
     // passive scalars: the FP64 mass flux and the scalars' face fluxes along
     // x1 and x2 over the padded block
     const size_t cells = (size_t)d.nc1 * d.nc2 * d.nc3;
-    size_t sc_bytes = d.nscalar > 0 ? 4 * (1 + (size_t)d.nscalar) * cells * 8 : 0;
+    size_t sc_bytes = d.nscalar > 0 ? (4 + 5 * (size_t)d.nscalar) * cells * 8 : 0;
     h->vic_bytes.push_back(vic_bytes);
     h->dv3_bytes.push_back(dv3_bytes);
     h->scratch_bytes.push_back(vic_bytes + dv3_bytes + sc_bytes);
@@ -843,6 +838,7 @@ int sg_bind_scratch(sg_handle* h, int32_t block, void* scratch, size_t bytes) {
     }
     B.sds = sc + (3 + 3 * ns) * plane;
     B.vicq = sc + (3 + 4 * ns) * plane;
+    B.stheta = sc + (4 + 4 * ns) * plane;
   }
   h->dirty = true;
   return 0;

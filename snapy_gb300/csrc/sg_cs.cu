@@ -2,7 +2,7 @@
 // n x n cells (nghost 3, one radial cell) in ONE handle, FP64 or FP32 state
 // (6, 4, nc, nc): Phi, the radial and the two covariant tangential momenta.
 //
-// A stage is five launches, each over all six panels:
+// A stage is four launches, each over all six panels:
 //   cs_flux_kernel       every x2 and x3 face of the panels' interiors: the
 //                        primitives of its six-cell stencil (U/Phi, momenta
 //                        raised by the cell cosine), weno5 for Phi and cp5
@@ -12,8 +12,8 @@
 //                        (src/riemann/riemann.cpp:219-346 with
 //                        src/coord/gnomonic_equiangle.cpp:357-463,
 //                        src/riemann/riemann_kernels.h:447-495)
-//   cs_seam_face_kernel  the seam faces again, each with its exterior-side
-//                        state from the neighbour panel's own interior-side
+//                        -- at a seam face with its exterior-side state
+//                        from the neighbour panel's own interior-side
 //                        reconstruction, mapped into this panel's frame at
 //                        the shared face (the cross-panel face-state sync,
 //                        src/hydro/hydro_forward.cpp:719-757)
@@ -349,15 +349,29 @@ __device__ __forceinline__ void cs_face(const CsParams& P, const Geo<T>& G,
 }
 
 // the faces: thread e < 6 n (n + 1) an x2 face (panel, row k, face j), the
-// rest x3 faces (panel, face k, column j), each from its own panel's
-// stencils (the seam faces are redone by cs_seam_face_kernel)
+// next 6 n (n + 1) the x3 faces (panel, face k, column j), each from its own
+// panel's stencils -- but for the seam faces, which the last 24 n threads
+// take (panel, side L R B T, along), each with its exterior-side state from
+// the neighbour panel.  The seam faces thus run in warps of their own, in
+// the same wave as the bulk, and no bulk warp diverges on them beyond an
+// idle lane
 template <typename T, bool HLLC>
-__global__ void __launch_bounds__(kThreads) cs_flux_kernel(CsParams P) {
+__global__ void __launch_bounds__(kThreads)
+    cs_flux_kernel(const __grid_constant__ CsParams P) {
   const int n = P.n;
   const Geo<T> G = geo_of<T>(P.geo, P.nc);
   const size_t nf = (size_t)6 * n * (n + 1);
-  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < 2 * nf;
-       e += (size_t)gridDim.x * blockDim.x) {
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+       e < 2 * nf + 24 * (size_t)n; e += (size_t)gridDim.x * blockDim.x) {
+    if (e >= 2 * nf) {
+      const int s = (int)(e - 2 * nf);
+      const int along = s % n, side = (s / n) % 4, p = s / (4 * n);
+      const bool x2 = side < 2;
+      const int edge = (side & 1) ? kNg + n : kNg;
+      const int k = x2 ? kNg + along : edge, j = x2 ? edge : kNg + along;
+      cs_face<T, HLLC>(P, G, p, x2, k, j, side, along);
+      continue;
+    }
     const bool x2 = e < nf;
     const size_t r = x2 ? e : e - nf;
     int p, k, j;
@@ -365,30 +379,14 @@ __global__ void __launch_bounds__(kThreads) cs_flux_kernel(CsParams P) {
       j = kNg + (int)(r % (n + 1));
       k = kNg + (int)((r / (n + 1)) % n);
       p = (int)(r / ((size_t)(n + 1) * n));
+      if (j == kNg || j == kNg + n) continue;  // a seam face
     } else {  // faces k = ng..ng+n of columns j = ng..ng+n-1
       j = kNg + (int)(r % n);
       k = kNg + (int)((r / n) % (n + 1));
       p = (int)(r / ((size_t)n * (n + 1)));
+      if (k == kNg || k == kNg + n) continue;  // a seam face
     }
     cs_face<T, HLLC>(P, G, p, x2, k, j, -1, 0);
-  }
-}
-
-// the 24 n seam faces again, each with its exterior-side state from the
-// neighbour panel (thread e: panel e / 4n, side (e / n) % 4 in L R B T,
-// along e % n); launched after cs_flux_kernel so no warp of the bulk pass
-// diverges on them
-template <typename T, bool HLLC>
-__global__ void __launch_bounds__(kThreads) cs_seam_face_kernel(CsParams P) {
-  const int n = P.n;
-  const Geo<T> G = geo_of<T>(P.geo, P.nc);
-  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < 24 * n;
-       e += gridDim.x * blockDim.x) {
-    const int along = e % n, side = (e / n) % 4, p = e / (4 * n);
-    const bool x2 = side < 2;
-    const int edge = (side & 1) ? kNg + n : kNg;
-    const int k = x2 ? kNg + along : edge, j = x2 ? edge : kNg + along;
-    cs_face<T, HLLC>(P, G, p, x2, k, j, side, along);
   }
 }
 
@@ -811,17 +809,13 @@ int sg_cs_stage(sg_cs_handle* h, int32_t stage, const double* dt_dev,
   const size_t cells = (size_t)6 * P.n * P.n;
   if (h->d.dtype == SG_F64) {
     (P.hllc ? cs_flux_kernel<double, true> : cs_flux_kernel<double, false>)
-        <<<grid_for(faces), kThreads, 0, s>>>(P);
-    (P.hllc ? cs_seam_face_kernel<double, true> : cs_seam_face_kernel<double, false>)
-        <<<grid_for(24 * (size_t)P.n), kThreads, 0, s>>>(P);
+        <<<grid_for(faces + 24 * (size_t)P.n), kThreads, 0, s>>>(P);
     cs_seam_flux_kernel<double><<<grid_for(P.nseam), kThreads, 0, s>>>(P);
     cs_update_kernel<double><<<grid_for(cells), kThreads, 0, s>>>(P);
     cs_ghost_kernel<double><<<grid_for(P.nghost), kThreads, 0, s>>>(P, P.out);
   } else {
     (P.hllc ? cs_flux_kernel<float, true> : cs_flux_kernel<float, false>)
-        <<<grid_for(faces), kThreads, 0, s>>>(P);
-    (P.hllc ? cs_seam_face_kernel<float, true> : cs_seam_face_kernel<float, false>)
-        <<<grid_for(24 * (size_t)P.n), kThreads, 0, s>>>(P);
+        <<<grid_for(faces + 24 * (size_t)P.n), kThreads, 0, s>>>(P);
     cs_seam_flux_kernel<float><<<grid_for(P.nseam), kThreads, 0, s>>>(P);
     cs_update_kernel<float><<<grid_for(cells), kThreads, 0, s>>>(P);
     cs_ghost_kernel<float><<<grid_for(P.nghost), kThreads, 0, s>>>(P, P.out);

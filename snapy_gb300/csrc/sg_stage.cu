@@ -1041,7 +1041,7 @@ __global__ void __launch_bounds__(kThreads)
 
 // ---------------------------------------------------------------------------
 // passive scalars (ScalarImpl::forward, src/scalar/scalar.cpp:90-211, the
-// dry case without limiter or upper bound).  One thread per face of the
+// dry case without the upper bound).  One thread per face of the
 // interior cells: the side the stage's mass flux F_m selects (F_m > 0: the
 // left state, the plus side of cell f - 1; else the right state, the minus
 // side of cell f) is reconstructed by scale-invariant WENO5 for the total
@@ -1049,8 +1049,32 @@ __global__ void __launch_bounds__(kThreads)
 // forward without a hydro parent, src/recon/reconstruct.cpp:258-262); the
 // face ratio r = s_f / rho_f, or the donor cell's where rho_f is not
 // positive; the upwind flux F_s = F_m r (riemann.cpp:164-170), zero on the
-// reflecting faces (boundary.prescribed), FP64 as the reference keeps it
+// reflecting faces (boundary.prescribed), FP64 as the reference keeps it.
+// With the flux-covariance row (x2 and x3 faces of blocks with nx1 >= 3) the
+// flux adds the tracer row s2 rho D1[u_n] D1[q] (HydroImpl::
+// scalar_flux_covariance, src/hydro/hydro_forward.cpp:233-300: q the mean
+// of the two sides' ratios, rho and u_n of the hydro's face means, D1 the
+// centred x1 difference), and the positivity limiter below follows.
 // ---------------------------------------------------------------------------
+// the ratio of one side of face q (stride st) of tracer sv
+template <typename RHO>
+__device__ __forceinline__ real scalar_face_ratio(const real* sv, RHO rho,
+                                                  size_t q, size_t st,
+                                                  bool left) {
+  const size_t c0 = q - (left ? 3 : 2) * st;
+  const size_t donor = left ? q - st : q;
+  auto face = [&](real f0, real f1, real f2, real f3, real f4) -> real {
+    real v = left ? weno5_cp(f0, f1, f2, f3, f4, true)
+                  : weno5_cm(f0, f1, f2, f3, f4, true);
+    return v < real(0) ? real(0) : v;  // clamp_min: -0 stays
+  };
+  const real rf = face(rho(c0), rho(c0 + st), rho(c0 + 2 * st),
+                       rho(c0 + 3 * st), rho(c0 + 4 * st));
+  const real sf = face(sv[c0], sv[c0 + st], sv[c0 + 2 * st], sv[c0 + 3 * st],
+                       sv[c0 + 4 * st]);
+  return rf > real(0) ? sf / rf : sv[donor] / rho(donor);
+}
+
 __global__ void __launch_bounds__(kThreads)
     scalar_flux_kernel(const BlockDev* __restrict__ tab, StageParams p) {
   const BlockDev& B = tab[blockIdx.y];
@@ -1068,6 +1092,9 @@ __global__ void __launch_bounds__(kThreads)
   const real* u = static_cast<const real*>(B.buf[p.in]);
   const real* s = static_cast<const real*>(B.sbuf[p.in]);
   const double* rb = B.base ? base_rho(B.base, nc1) : nullptr;
+  const real gammad = real(B.gammad);
+  const bool scale = p.scale != 0;
+  const bool covs = B.flux_cov && nc1 >= 3;
   // the total dry density (the state holds an anomaly under a base)
   auto rho = [&](size_t c) -> real {
     real v = u[IDN * plane + c];
@@ -1106,22 +1133,223 @@ __global__ void __launch_bounds__(kThreads)
                       (f == nd - ng && B.bc[2 * d + 1] == kBcReflecting);
     const double F = B.mflux[d][q];
     const bool left = F > 0.;
-    const size_t c0 = q - (left ? 3 : 2) * st;
-    const size_t donor = left ? q - st : q;
-    auto face = [&](real f0, real f1, real f2, real f3, real f4) -> real {
-      real v = left ? weno5_cp(f0, f1, f2, f3, f4, true)
-                    : weno5_cm(f0, f1, f2, f3, f4, true);
-      return v < real(0) ? real(0) : v;  // clamp_min: -0 stays
-    };
-    const real rf = face(rho(c0), rho(c0 + st), rho(c0 + 2 * st),
-                         rho(c0 + 3 * st), rho(c0 + 4 * st));
+    const bool cov = covs && d >= 1;
+    // the hydro's face means on the x1 rows i - 1, i, i + 1: the normal
+    // velocity, and rho on row i (the hydro's face states, its scheme)
+    real un[3] = {real(0), real(0), real(0)}, rhof = real(0);
+    if (cov) {
+      const int vn = d == 1 ? IVY : IVZ;
+      for (int m = -1; m <= 1; ++m) {
+        real wd[6], wv[6];
+        for (int o = 0; o < 6; ++o) {
+          const size_t c = q + m + (o - 3) * st;
+          real uc[NHYDRO], w[NHYDRO];
+#pragma unroll
+          for (int v = 0; v < NHYDRO; ++v) uc[v] = u[v * plane + c];
+          if (rb) uc[IDN] = real(rb[c % nc1]) + uc[IDN];
+          cons2prim<real>(uc, w, gammad);
+          wd[o] = w[IDN];
+          wv[o] = w[vn];
+        }
+        real vl, vr;
+        if (p.shock) {
+          vl = weno5_cp(wv[0], wv[1], wv[2], wv[3], wv[4], scale);
+          vr = weno5_cm(wv[1], wv[2], wv[3], wv[4], wv[5], scale);
+        } else {
+          vl = cp5_cp(wv[0], wv[1], wv[2], wv[3], wv[4]);
+          vr = cp5_cm(wv[1], wv[2], wv[3], wv[4], wv[5]);
+        }
+        un[m + 1] = real(0.5) * (vl + vr);
+        if (m == 0) {
+          const real dl = weno5_cp(wd[0], wd[1], wd[2], wd[3], wd[4], scale);
+          const real dr = weno5_cm(wd[1], wd[2], wd[3], wd[4], wd[5], scale);
+          rhof = real(0.5) * (dl + dr);
+        }
+      }
+    }
     for (int v = 0; v < ns; ++v) {
       const real* sv = s + (size_t)v * plane;
-      const real sf = face(sv[c0], sv[c0 + st], sv[c0 + 2 * st],
-                           sv[c0 + 3 * st], sv[c0 + 4 * st]);
-      const real r = rf > real(0) ? sf / rf : sv[donor] / rho(donor);
-      B.sflux[d][(size_t)v * plane + q] = wall ? 0. : F * (double)r;
+      const real r = scalar_face_ratio(sv, rho, q, st, left);
+      double fl = F * (double)r;
+      if (cov) {
+        real qf[3];
+        for (int m = -1; m <= 1; ++m)
+          qf[m + 1] = real(0.5) * (scalar_face_ratio(sv, rho, q + m, st, true) * real(1) +
+                                   scalar_face_ratio(sv, rho, q + m, st, false) * real(1));
+        const real dx1 = real(B.x1v[i + 1] - B.x1v[i - 1]);
+        const real s2 = real(B.dx1 * B.dx1 / 12.);
+        const real d1u = (un[2] - un[0]) / dx1;
+        const real d1q = (qf[2] - qf[0]) / dx1;
+        fl = fl + (double)(s2 * rhof * d1u * d1q);
+      }
+      B.sflux[d][(size_t)v * plane + q] = wall ? 0. : fl;
     }
+  }
+}
+
+// the positivity limiter of the scalars (PositivityLimiter::apply with the
+// scalars' inputs, src/hydro/flux_positivity.cpp:29-268; no energy carry):
+// one thread per interior cell and scalar.
+//   theta = min(1, s V (1 - 4096 eps) / (dt out)), out the outgoing A F_s
+//   over the cell's faces (1 where nothing drains); td the same of the dry
+//   density under the mass fluxes; phi = clamp(min of the neighbours'
+//   s / rho over each resolved axis / its own, 0, 1) (0 where s / rho is
+//   not positive); theta <- theta + phi (min(theta / td, 1) - theta) where
+//   0 < td < 1 (flux_positivity_relax)
+__global__ void __launch_bounds__(kThreads)
+    scalar_theta_kernel(const BlockDev* __restrict__ tab, StageParams p) {
+  const BlockDev& B = tab[blockIdx.y];
+  const int ns = B.nscalar;
+  if (ns == 0 || !(B.flux_cov && B.nc1 >= 3 && (B.nc2 > 1 || B.nc3 > 1))) return;
+  const int nc1 = B.nc1, nc2 = B.nc2, nc3 = B.nc3, ng = B.ng;
+  const bool has2 = nc2 > 1, has3 = nc3 > 1;
+  const size_t kst = (size_t)nc1 * nc2, plane = kst * nc3;
+  const int nx1 = nc1 - 2 * ng, nx2 = has2 ? nc2 - 2 * ng : 1,
+            nx3 = has3 ? nc3 - 2 * ng : 1;
+  const int jl = has2 ? ng : 0, kl = has3 ? ng : 0;
+  const double area[3] = {B.dx3 * B.dx2, B.dx3 * B.dx1, B.dx2 * B.dx1};
+  const double vol = B.dx3 * (B.dx2 * B.dx1);
+  const double dt = p.dt[blockIdx.y];
+  const double margin = 4096. * 2.220446049250313e-16;
+  const double tiny = 2.2250738585072014e-308;
+  const size_t st[3] = {1, (size_t)nc1, kst};
+  const bool act[3] = {true, has2, has3};
+  const real* u = static_cast<const real*>(B.buf[p.in]);
+  const real* s = static_cast<const real*>(B.sbuf[p.in]);
+  const double* rb = B.base ? base_rho(B.base, nc1) : nullptr;
+  auto rho = [&](size_t c) -> real {
+    real v = u[IDN * plane + c];
+    if (rb) v = v + real(rb[c % nc1]);
+    return v;
+  };
+  // theta of a channel: densities q (by a functor), face fluxes F[d]
+  auto theta_of = [&](size_t c, double qc, const double* const* F) {
+    double out = 0.;
+    for (int d = 0; d < 3; ++d) {
+      if (!act[d]) continue;
+      const double up = area[d] * F[d][c + st[d]], dn = area[d] * F[d][c];
+      out = out + ((up > 0. ? up : 0.) + (-dn > 0. ? -dn : 0.));
+    }
+    const double avail = (qc > 0. ? qc : 0.) * vol * (1. - margin);
+    const double drain = dt * out;
+    if (!(drain > 0.)) return 1.;
+    const double t = avail / (drain > tiny ? drain : tiny);
+    return t < 1. ? t : 1.;
+  };
+  const size_t inner = (size_t)nx1 * nx2 * nx3;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+       t < inner * ns; t += (size_t)gridDim.x * blockDim.x) {
+    const int v = (int)(t / inner);
+    const size_t e = t - (size_t)v * inner;
+    const int i = ng + (int)(e % nx1);
+    const size_t r = e / nx1;
+    const int j = jl + (int)(r % nx2), k = kl + (int)(r / nx2);
+    const size_t c = (size_t)k * kst + (size_t)j * nc1 + i;
+    const real* sv = s + (size_t)v * plane;
+    const double* Fs[3] = {B.sflux[0] + (size_t)v * plane,
+                           B.sflux[1] ? B.sflux[1] + (size_t)v * plane : nullptr,
+                           B.sflux[2] ? B.sflux[2] + (size_t)v * plane : nullptr};
+    const double* Fm[3] = {B.mflux[0], B.mflux[1], B.mflux[2]};
+    const double th = theta_of(c, (double)sv[c], Fs);
+    const double td = theta_of(c, (double)rho(c), Fm);
+    const double qc = (double)(sv[c] / rho(c));
+    double low = 0.;
+    for (int d = 0; d < 3; ++d) {
+      if (!act[d]) continue;
+      const double qm = (double)(sv[c - st[d]] / rho(c - st[d]));
+      const double qp = (double)(sv[c + st[d]] / rho(c + st[d]));
+      const double mm = qm < qp ? qm : qp;
+      low = d == 0 ? mm : (mm < low ? mm : low);
+    }
+    double phi = 0.;
+    if (qc > 0.) {
+      phi = low / qc;
+      phi = phi < 0. ? 0. : (phi > 1. ? 1. : phi);
+    }
+    double out = th;
+    if (td < 1. && td > 0.) {
+      const double rr = th / td;
+      out = th + phi * ((rr < 1. ? rr : 1.) - th);
+    }
+    B.stheta[(size_t)v * plane + c] = out;
+  }
+}
+
+// theta's ghost cells (flux_positivity_sync_theta_: the boundary functions
+// of a kScalar field), then each face flux of the interior cells times its
+// donor's theta (the lower cell where F_s > 0; flux_positivity_factor)
+__global__ void __launch_bounds__(kThreads)
+    scalar_theta_ghost_kernel(const BlockDev* __restrict__ tab) {
+  const BlockDev& B = tab[blockIdx.y];
+  if (B.nscalar == 0 || !(B.flux_cov && B.nc1 >= 3 && (B.nc2 > 1 || B.nc3 > 1)))
+    return;
+  const int nc1 = B.nc1, nc2 = B.nc2, nc3 = B.nc3, ng = B.ng;
+  const size_t plane = (size_t)nc1 * nc2 * nc3;
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < plane;
+       c += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(c % nc1);
+    const int j = (int)((c / nc1) % nc2);
+    const int k = (int)(c / ((size_t)nc1 * nc2));
+    bool f1 = false, f2 = false, f3 = false;
+    const int si = ghost_src(i, nc1, ng, B.bc[0], B.bc[1], f1);
+    const int sj = ghost_src(j, nc2, ng, B.bc[2], B.bc[3], f2);
+    const int sk = ghost_src(k, nc3, ng, B.bc[4], B.bc[5], f3);
+    if (si == i && sj == j && sk == k) continue;  // interior
+    for (int v = 0; v < B.nscalar; ++v)
+      B.stheta[(size_t)v * plane + c] =
+          (si < 0 || sj < 0 || sk < 0)
+              ? 1.
+              : B.stheta[(size_t)v * plane + ((size_t)sk * nc2 + sj) * nc1 + si];
+  }
+}
+
+__global__ void __launch_bounds__(kThreads)
+    scalar_scale_kernel(const BlockDev* __restrict__ tab) {
+  const BlockDev& B = tab[blockIdx.y];
+  const int ns = B.nscalar;
+  if (ns == 0 || !(B.flux_cov && B.nc1 >= 3 && (B.nc2 > 1 || B.nc3 > 1))) return;
+  const int nc1 = B.nc1, nc2 = B.nc2, nc3 = B.nc3, ng = B.ng;
+  const bool has2 = nc2 > 1, has3 = nc3 > 1;
+  const size_t kst = (size_t)nc1 * nc2, plane = kst * nc3;
+  const int nx1 = nc1 - 2 * ng, nx2 = has2 ? nc2 - 2 * ng : 1,
+            nx3 = has3 ? nc3 - 2 * ng : 1;
+  const int jl = has2 ? ng : 0, kl = has3 ? ng : 0;
+  const size_t n1f = (size_t)nx3 * nx2 * (nx1 + 1);
+  const size_t n2f = has2 ? (size_t)nx3 * (nx2 + 1) * nx1 : 0;
+  const size_t n3f = has3 ? (size_t)(nx3 + 1) * nx2 * nx1 : 0;
+  const size_t nf = n1f + n2f + n3f;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < nf * ns;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const int v = (int)(t / nf);
+    const size_t tf = t - (size_t)v * nf;
+    int d, i, j, k;
+    if (tf < n1f) {
+      d = 0;
+      i = ng + (int)(tf % (nx1 + 1));
+      const size_t r = tf / (nx1 + 1);
+      j = jl + (int)(r % nx2);
+      k = kl + (int)(r / nx2);
+    } else if (tf < n1f + n2f) {
+      const size_t e = tf - n1f;
+      d = 1;
+      i = ng + (int)(e % nx1);
+      const size_t r = e / nx1;
+      j = ng + (int)(r % (nx2 + 1));
+      k = kl + (int)(r / (nx2 + 1));
+    } else {
+      const size_t e = tf - n1f - n2f;
+      d = 2;
+      i = ng + (int)(e % nx1);
+      const size_t r = e / nx1;
+      j = jl + (int)(r % nx2);
+      k = ng + (int)(r / nx2);
+    }
+    const size_t q = (size_t)k * kst + (size_t)j * nc1 + i;
+    const size_t st = d == 0 ? 1 : (d == 1 ? (size_t)nc1 : kst);
+    double* F = B.sflux[d] + (size_t)v * plane + q;
+    const double* th = B.stheta + (size_t)v * plane;
+    const double fac = *F > 0. ? th[q - st] : th[q];
+    *F = *F * fac;
   }
 }
 
@@ -1781,6 +2009,13 @@ extern "C" int SG_NAME(sg_launch_scalar)(const BlockDev* tab, StageParams p,
   if (e != cudaSuccess) return (int)e;
   int gu = (int)((max_plane + kThreads - 1) / kThreads);
   if (gu > 2048) gu = 2048;
+  // the positivity limiter (blocks with the covariance row; the others
+  // return at once)
+  scalar_theta_kernel<<<dim3(gu, p.nblock), kThreads, 0, stream>>>(tab, p);
+  scalar_theta_ghost_kernel<<<dim3(gu, p.nblock), kThreads, 0, stream>>>(tab);
+  scalar_scale_kernel<<<dim3(gx, p.nblock), kThreads, 0, stream>>>(tab);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return (int)e;
   scalar_update_kernel<<<dim3(gu, p.nblock), kThreads, 0, stream>>>(tab, p);
   if (max_icols > 0) {  // implicit blocks: the solve's transfer per column
     e = cudaGetLastError();

@@ -84,6 +84,9 @@ struct BlockDev {
   // finish kernel's, face f below cell f), for the transfer's share
   double* sds;
   double* vicq;
+  // with the covariance row: the positivity limiter's theta of each scalar
+  // (nscalar rows, FP64), ghosts filled like the scalars'
+  double* stheta;
 };
 
 // offsets into BlockDev::base

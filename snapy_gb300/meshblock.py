@@ -15,6 +15,8 @@ caller rebinds is adopted (copied in) at the next stage.
 """
 from __future__ import annotations
 
+import os
+
 from dataclasses import dataclass
 from typing import Dict, Optional
 
@@ -270,6 +272,112 @@ class MeshBlock:
         vars["hydro_u"] = torch.empty(0, dtype=self.dtype, device=self.device).set_(u)
         self.intg.current_redo = 0
         return vars, 0.0
+
+    # -- restart (src/output/restart.cpp, src/mesh/meshblock_restart.cpp) ---
+    def write_restart(self, vars: dict, out_dir: str, basename: str = "snapy",
+                      number: int = 0, time: float = 0.0, final: bool = False,
+                      rank: int = 0, combine: bool = True) -> str:
+        """Write this block's restart part (RestartOutput::write_output_file,
+        src/output/restart.cpp:40-140) and, with `combine`, the restart
+        file of the parts present (combine_blocks); returns its path (the
+        part's without `combine`).  Every tensor of vars is written on the
+        CPU; hydro_u holds the conserved totals, and a block stored as
+        anomalies about an FP64 hydrostatic base adds the stored bits, the
+        base and the metadata [version, bits] with the grid faces."""
+        from . import restart as R
+        os.makedirs(out_dir, exist_ok=True)
+        with torch.cuda.device(self.device):
+            self._adopt(vars)
+            out = {}
+            skip_r = "scalar_s" in vars and "hydro_u" in vars
+            for name, var in vars.items():
+                if skip_r and name == "scalar_r":
+                    continue
+                if isinstance(var, torch.Tensor) and var.numel():
+                    out[name] = var.detach().cpu()
+            u = self.batch.current(0)
+            base = self.batch.bases[0]
+            if base is not None:
+                out["hydro_u"] = self.batch.totals(0, u).cpu()
+                out["hydro_u_stored"] = u.detach().cpu().clone()
+                out["hydro_ref"] = base.detach().cpu().clone()
+                out[R.HYDRO_RESTART_METADATA] = torch.tensor(
+                    [R.HYDRO_RESTART_VERSION, 32 if self.dtype == torch.float32 else 64],
+                    dtype=torch.int64)
+                c = self.options.coord()
+                for d, key in enumerate(R.HYDRO_REFERENCE_GRID):
+                    out[key] = torch.as_tensor(c.faces(d + 1), dtype=torch.float64)
+            else:
+                out["hydro_u"] = u.detach().cpu().clone()
+            sc = self.batch.current_scalars(0)
+            if sc is not None:
+                out["scalar_s"] = sc.detach().cpu().clone()
+        out["last_time"] = torch.tensor([float(time)], dtype=torch.float64)
+        out["last_cycle"] = torch.tensor([int(self.cycle)], dtype=torch.int64)
+        # the restart output's own schedule: its next file number and time
+        out["file_number"] = torch.tensor([number + (0 if final else 1)],
+                                          dtype=torch.int64)
+        out["next_time"] = torch.tensor([float(time)], dtype=torch.float64)
+        part = os.path.join(out_dir, R.part_name(basename, rank, number, final))
+        R.save_part(out, part)
+        return R.combine(out_dir, basename, number, final) if combine else part
+
+    def initialize_from_restart(self, vars: dict, fname: str,
+                                rank: int = 0) -> float:
+        """Resume from a restart file (MeshBlockImpl::_init_from_restart,
+        src/mesh/meshblock_restart.cpp:33-236): the block's part, the
+        required variables and the metadata checks; the cycle, the state
+        (an anomaly block takes its stored bits and its FP64 base back, so
+        the run continues bit for bit) and the tracers; vars gets every
+        other variable of the file on the device.  Returns the time."""
+        from . import restart as R
+        data = R.load_restart(fname, rank)
+        R.require(data)
+        c = self.options.coord()
+        R.check_restart_metadata(data, [c.faces(d) for d in (1, 2, 3)])
+        shape = (5,) + self.nc()
+        if tuple(data["hydro_u"].shape) != shape:
+            raise R.RestartError(f"restart: hydro_u has shape "
+                                 f"{tuple(data['hydro_u'].shape)}, the block {shape}")
+        self.cycle = int(data["last_cycle"].item())
+        t = float(data["last_time"].item())
+        with torch.cuda.device(self.device):
+            b = self.batch
+            b.set_current(0)
+            base = b.bases[0]
+            if base is not None:
+                if "hydro_ref" not in data or "hydro_u_stored" not in data:
+                    raise R.RestartError("restart: an anomaly block needs "
+                                         "hydro_ref and hydro_u_stored")
+                stored = data["hydro_u_stored"]
+                if stored.dtype != self.dtype or tuple(base.shape) != tuple(
+                        data["hydro_ref"].shape):
+                    raise R.RestartError("restart: the stored state's dtype or "
+                                         "its base does not fit the block")
+                base.copy_(data["hydro_ref"].to(self.device))
+                b.current(0).copy_(stored.to(self.device))
+            else:
+                b.current(0).copy_(data["hydro_u"].to(self.device, self.dtype))
+            sc = b.current_scalars(0)
+            if sc is not None:
+                if "scalar_s" not in data:
+                    raise R.RestartError("restart: the block carries passive "
+                                         "scalars; the file has no scalar_s")
+                sc.copy_(data["scalar_s"].to(self.device, self.dtype))
+                vars["scalar_s"] = torch.empty(0, dtype=self.dtype,
+                                               device=self.device).set_(sc)
+            skip = {"hydro_u", "hydro_u_stored", "hydro_ref", "scalar_s",
+                    R.HYDRO_RESTART_METADATA, *R.HYDRO_REFERENCE_GRID}
+            for name, tensor in data.items():
+                if name not in skip:
+                    vars[name] = tensor.to(self.device)
+            vars["hydro_u"] = torch.empty(0, dtype=self.dtype,
+                                          device=self.device).set_(b.current(0))
+            self._graphs.clear()
+            self._seen.clear()
+            self.intg.current_redo = 0
+            self._refresh_w(vars)
+        return t
 
     def _publish(self, vars: dict) -> None:
         """vars views the block's current storage (hydro_u, scalar_s)."""

@@ -400,11 +400,6 @@ def _scalar_names(node, op) -> List[str]:
         raise DeckError("scalar/reconstruct: only weno5 is built")
     if names:
         h, c = op.hydro(), op.coord()
-        if c.nx2 > 1 and h.flux_covariance:
-            raise DeckError("scalar: passive scalars with the x2 flux-covariance "
-                            "row are not built (the scalar's covariance row and "
-                            "the positivity limiter it brings); set "
-                            "dynamics/flux-covariance: false")
         if h.eos.type == "shallow-water":
             raise DeckError("scalar: passive scalars need a dry-air density")
     return names

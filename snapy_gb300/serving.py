@@ -83,7 +83,7 @@ def footprint(options: MeshBlockOptions, dtype: torch.dtype) -> int:
         b += 5 * icells * s
     ns = len(options.scalar_names)
     if ns:  # the tracers' buffers and their face scratch
-        b += 3 * ns * nc * s + 4 * (1 + ns) * nc * 8
+        b += 3 * ns * nc * s + (4 + 5 * ns) * nc * 8
     b += 8 * (5 * c.nc1 + 1) + 16 * (c.nc1 + 1)
     return b
 

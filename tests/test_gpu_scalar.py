@@ -4,7 +4,9 @@ the implicit solve's dry transfer: FP64 within 1e-12 of the oracle per
 tracer and hydro field after 10 steps (Straka explicit and with the solve,
 and a 1-D tube), the reference's own properties on the device (a uniform
 ratio stays uniform, the tracer is conserved in a closed box), FP32 within
-1e-5, and the refusals of what is not built."""
+1e-5, without and with the flux-covariance row (the scalars' covariance
+row and the shared positivity limiter), and the refusals of what is not
+built."""
 import copy
 
 import numpy as np
@@ -22,10 +24,10 @@ INNER = (slice(None), slice(3, -3), slice(3, -3))
 
 
 def straka(precision="float64", nx1=32, nx2=48, deck="straka_noimplicit.yaml",
-           implicit_precision=None):
+           implicit_precision=None, cov=False):
     cfg = copy.deepcopy(sg.options.yaml_lite.load("snapy_gb300/decks/" + deck))
     cfg["scalar"] = {"nvar": 2, "names": ["uniform", "step"]}
-    cfg["dynamics"]["flux-covariance"] = False
+    cfg["dynamics"]["flux-covariance"] = cov
     opts = sg.MeshBlockOptions.from_config(cfg)
     c = opts.coord()
     c.nx1, c.nx2, c.x1max, c.x2max = nx1, nx2, nx1 * 50.0, nx2 * 50.0
@@ -65,18 +67,24 @@ def rel(a, b):
     return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
 
 
+@pytest.mark.parametrize("cov", [False, True])
 @pytest.mark.parametrize("deck", ["straka_noimplicit.yaml", "straka.yaml"])
-def test_fp64_scalars_against_oracle(oracle, cuda, deck):
+def test_fp64_scalars_against_oracle(oracle, cuda, deck, cov):
     """Explicit, and with the vertical implicit solve (the scalars' share of
-    its dry transfer)."""
-    opts = straka(deck=deck)
+    its dry transfer); without and with the flux-covariance row (the
+    reference's default: the scalars' covariance row and the positivity
+    limiter)."""
+    opts = straka(deck=deck, cov=cov)
     blk, vars, u, s = run_pair(cuda, opts, oracle)
     got_s = vars["scalar_s"].double().cpu().numpy()
     got_u = blk.total_u(vars).double().cpu().numpy()
     es = [rel(got_s[v][INNER], s[v][INNER]) for v in range(2)]
     eu = [rel(got_u[v][INNER], u[v][INNER]) for v in range(5) if np.linalg.norm(u[v]) > 0]
-    print(f"\n{deck}: FP64 scalars vs oracle, rel L2:", es, "hydro:", max(eu))
+    print(f"\n{deck} cov={cov}: FP64 scalars vs oracle, rel L2:", es,
+          "hydro:", max(eu))
     assert max(es) <= 1e-12 and max(eu) <= 1e-12
+    if cov:
+        assert got_s[1][INNER].min() >= 0.0
     # the reference's properties, on the device's result
     ratio = got_s[0][INNER] / got_u[0][INNER]
     assert np.abs(ratio / 0.37 - 1).max() <= 1e-13
@@ -115,10 +123,11 @@ def test_fp64_scalar_tube_against_oracle(oracle, cuda):
     assert e <= 1e-12
 
 
+@pytest.mark.parametrize("cov", [False, True])
 @pytest.mark.parametrize("deck,ip", [("straka_noimplicit.yaml", None),
                                      ("straka.yaml", "float32")])
-def test_fp32_scalars_against_fp64_oracle(oracle, cuda, deck, ip):
-    opts = straka("float32", deck=deck, implicit_precision=ip)
+def test_fp32_scalars_against_fp64_oracle(oracle, cuda, deck, ip, cov):
+    opts = straka("float32", deck=deck, implicit_precision=ip, cov=cov)
     blk, vars, u, s = run_pair(cuda, opts, oracle)
     got_s = vars["scalar_s"].double().cpu().numpy()
     es = [rel(got_s[v][INNER], s[v][INNER]) for v in range(2)]
@@ -149,8 +158,8 @@ def test_graphs_and_redo_carry_the_scalars(cuda):
 
 def test_scalar_refusals(cuda):
     cfg = copy.deepcopy(sg.options.yaml_lite.load("snapy_gb300/decks/straka.yaml"))
-    cfg["scalar"] = {"nvar": 1}
-    with pytest.raises(DeckError, match="flux-covariance"):
+    cfg["scalar"] = {"nvar": 1, "upper-bound": 1.0}
+    with pytest.raises(DeckError, match="upper-bound"):
         sg.MeshBlockOptions.from_config(cfg)
     opts = straka()
     blk = sg.MeshBlock(opts).to(cuda)
@@ -184,12 +193,14 @@ def test_ensemble_member_alone_equals_in_the_batch(cuda):
         assert torch.equal(ens.state(k), vars["hydro_u"]), k
 
 
-def test_3d_scalars_against_oracle(oracle, cuda):
+@pytest.mark.parametrize("cov", [False, True])
+def test_3d_scalars_against_oracle(oracle, cuda, cov):
     """A 3-D convection block (the serving deck, its vertical implicit solve
-    on the (x2, x3) columns) with a tracer: FP64 bitwise with the oracle."""
+    on the (x2, x3) columns) with a tracer: FP64 with the oracle, without
+    and with the covariance row (x2 and x3 faces) and its limiter."""
     cfg = copy.deepcopy(sg.options.yaml_lite.load("snapy_gb300/decks/convection3d.yaml"))
     cfg["scalar"] = {"nvar": 1}
-    cfg["dynamics"]["flux-covariance"] = False  # tracers are built without it
+    cfg["dynamics"]["flux-covariance"] = cov
     opts = sg.MeshBlockOptions.from_config(cfg)
     c = opts.coord()
     c.nx1, c.nx2, c.nx3 = 16, 12, 10

@@ -15,17 +15,17 @@ from snapy_gb300.options import DeckError
 from oracle import oracle
 
 
-def straka_explicit(nx1=32, nx2=48, deck="straka_noimplicit.yaml"):
+def straka_explicit(nx1=32, nx2=48, deck="straka_noimplicit.yaml", cov=False):
     cfg = copy.deepcopy(sg.options.yaml_lite.load("snapy_gb300/decks/" + deck))
-    cfg["dynamics"]["flux-covariance"] = False
+    cfg["dynamics"]["flux-covariance"] = cov
     opts = sg.MeshBlockOptions.from_config(cfg)
     c = opts.coord()
     c.nx1, c.nx2, c.x1max, c.x2max = nx1, nx2, nx1 * 50.0, nx2 * 50.0
     return opts
 
 
-def run(nsteps=10, deck="straka_noimplicit.yaml"):
-    opts = straka_explicit(deck=deck)
+def run(nsteps=10, deck="straka_noimplicit.yaml", cov=False):
+    opts = straka_explicit(deck=deck, cov=cov)
     ob = oracle.block_from_options(opts)
     w = problems.straka(opts, "cpu", xc=1000.0, zc=1200.0, xr=800.0,
                         zr=600.0).numpy()
@@ -43,12 +43,17 @@ def run(nsteps=10, deck="straka_noimplicit.yaml"):
     return ob, u, s, m0, vol, inner, top0
 
 
+@pytest.mark.parametrize("cov", [False, True])
 @pytest.mark.parametrize("deck", ["straka_noimplicit.yaml", "straka.yaml"])
-def test_uniform_ratio_conservation_and_transport(deck):
+def test_uniform_ratio_conservation_and_transport(deck, cov):
     """Explicit, and with the vertical implicit solve (the tracer's share of
-    its dry transfer, donor-capped)."""
-    ob, u, s, m0, vol, inner, top0 = run(deck=deck)
+    its dry transfer, donor-capped); without and with the flux-covariance
+    row, whose scalar row and positivity limiter keep the stepped tracer
+    non-negative."""
+    ob, u, s, m0, vol, inner, top0 = run(deck=deck, cov=cov)
     assert np.isfinite(s).all()
+    if cov:
+        assert s[1][inner].min() >= 0.0
     ratio = s[0][inner] / u[0][inner]
     assert np.abs(ratio / 0.37 - 1).max() <= 1e-13
     for v in range(2):
@@ -62,8 +67,9 @@ def test_deck_scalar_section():
     cfg = copy.deepcopy(cfg)
     cov = copy.deepcopy(cfg)
     cov["scalar"] = {"nvar": 1}
-    with pytest.raises(DeckError, match="flux-covariance"):
-        sg.MeshBlockOptions.from_config(cov)
+    # with the covariance row (the default): the scalar's row and the
+    # positivity limiter are built
+    assert sg.MeshBlockOptions.from_config(cov).scalar_names == ["scalar0"]
     cfg["dynamics"]["flux-covariance"] = False
     cfg["scalar"] = {"nvar": 1, "names": ["tracer"]}
     assert sg.MeshBlockOptions.from_config(cfg).scalar_names == ["tracer"]
@@ -77,7 +83,6 @@ def test_deck_scalar_section():
             sg.MeshBlockOptions.from_config(bad)
     d3 = copy.deepcopy(sg.options.yaml_lite.load("snapy_gb300/decks/convection3d.yaml"))
     d3["scalar"] = {"nvar": 1}
-    with pytest.raises(DeckError, match="flux-covariance"):
-        sg.MeshBlockOptions.from_config(d3)
+    assert sg.MeshBlockOptions.from_config(d3).scalar_names == ["scalar0"]
     d3["dynamics"]["flux-covariance"] = False
     assert sg.MeshBlockOptions.from_config(d3).scalar_names == ["scalar0"]

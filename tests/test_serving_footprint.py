@@ -31,4 +31,4 @@ def test_footprint_counts_each_part():
     assert refined - plain == (icells * 160 + (icells // c.nx1) * 7) * 4 + 16
     # two tracers: three FP32 buffers each and the FP64 face scratch
     two = footprint(deck(scalars=2), torch.float32)
-    assert two - refined == 3 * 2 * nc * 4 + 4 * (1 + 2) * nc * 8
+    assert two - refined == 3 * 2 * nc * 4 + (4 + 5 * 2) * nc * 8
