@@ -139,6 +139,10 @@ def parse():
                          "scalar/names [tracer])")
     ap.add_argument("--requests", type=int, default=24,
                     help="serving: requests in the trace")
+    ap.add_argument("--no-plain", action="store_true",
+                    help="serving: skip the plain FP64 comparison and the "
+                         "alone/FP32 checks (for kernel profiles of the "
+                         "served launches alone)")
     ap.add_argument("--serve-budget-gb", type=float, default=8.0,
                     help="serving: the HBM budget requests are admitted "
                          "against (GiB; 0: the device's free memory)")
@@ -1017,16 +1021,18 @@ def run_serving(args, ranks=None, emit=True):
     achieved = value * b_alg(s_bytes) / 1e9
     ktot = sum(v[0] for v in kms.values())
     # the same requests on the plain FP64 GPU path, both clocks
-    plain = plain_fp64(reqs, dev)
+    plain = plain_fp64(reqs, dev) if not args.no_plain else \
+        {"device": float("nan"), "wall": float("nan"), "steps_per_request": 0}
     # the smallest request alone (a fresh server) equals itself in the mix,
     # and its FP32 result against the FP64 path at the served horizon
     small = min(reqs, key=lambda r: (r.cells, r.rid))
-    alone = copy.copy(small)
-    alone.arrival, alone.result, alone.done, alone.admitted = 0.0, None, None, None
-    Server(dev).run([alone])
-    same = bool(torch.equal(alone.result, small.result))
-    err = None
-    if prec == "float32":
+    same, err = None, None
+    if not args.no_plain:
+        alone = copy.copy(small)
+        alone.arrival, alone.result, alone.done, alone.admitted = 0.0, None, None, None
+        Server(dev).run([alone])
+        same = bool(torch.equal(alone.result, small.result))
+    if prec == "float32" and not args.no_plain:
         want = fp64_reference_state(small, dev)
         # the FP32 state holds anomalies about the FP64 hydrostatic base
         # (the serving slot's, from the same initial state): add it back
