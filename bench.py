@@ -1380,11 +1380,13 @@ def main():
     if args.workload == "serving":
         if args.impl == "reference":
             return run_reference_serving(args)
-        return run_serving(args)
+        run_serving(args)
+        return 0
     if args.workload == "ensemble":
         if args.impl == "reference":
             return run_reference_ensemble(args)
-        return run_ensemble(args)
+        run_ensemble(args)
+        return 0
     if args.impl == "reference":
         return run_reference(args)
     return run_native(args)
