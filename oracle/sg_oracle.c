@@ -690,9 +690,18 @@ static void riemann_face(const og_block* b, const double* wl, const double* wr,
  * (src/coord/coordinate.cpp:618-662) */
 /* t1, t2 (optional): the plane's register totals T_1, T_2 on the faces of
  * the interior cells, as the divergence reads them */
+/* 3-D viscosity's parts of a plane (NULL otherwise): the velocity
+ * divergence over the interior extended by one cell in every direction,
+ * and the x3 faces' viscous fluxes (5 rows), both at the plane's first
+ * cell like w */
+typedef struct {
+  const double* divv;
+  const double* vf3;
+} og_visc3;
+
 static void tendency_plane(const og_block* b, const double* w, double dt,
                            double* du, const double* f3, double* t1,
-                           double* t2) {
+                           double* t2, const og_visc3* v3) {
   const int n1 = b->nc1, n2 = b->nc2, ng = b->ng;
   const size_t nc = ncell(b);
   const int has2 = n2 > 1;
@@ -806,12 +815,17 @@ static void tendency_plane(const og_block* b, const double* w, double dt,
     int ja = has2 ? jl - 1 : 0, jb = has2 ? ju1 + 1 : 1;
     for (int j = ja; j < jb; ++j)
       for (int i = il - 1; i < iu1 + 1; ++i) {
+        if (v3) { /* 3-D: the whole divergence, x3 term included */
+          divv[(size_t)j * n1 + i] = v3->divv[(size_t)j * n1 + i];
+          continue;
+        }
         double dv = divv[(size_t)j * n1 + i];
         dv += (w[CELL(OG_IVX, j, i + 1)] - w[CELL(OG_IVX, j, i - 1)]) / (2. * b->dx1);
         if (has2)
           dv += (w[CELL(OG_IVY, j + 1, i)] - w[CELL(OG_IVY, j - 1, i)]) / (2. * b->dx2);
         divv[(size_t)j * n1 + i] = dv;
       }
+    const size_t pl = (size_t)n1 * n2; /* the next x3 plane */
     const double nu = b->nu_iso;
     /* x1 faces f = il..iu1, x2 cells jl..ju1-1 */
     int wall_lo = b->bc[0] == OG_BC_REFLECTING, wall_hi = b->bc[1] == OG_BC_REFLECTING;
@@ -843,6 +857,10 @@ static void tendency_plane(const og_block* b, const double* w, double dt,
             double below = (w[CELL(OG_IVX, j + 1, f - 1)] - w[CELL(OG_IVX, j - 1, f - 1)]) / (2. * b->dx2);
             double above = (w[CELL(OG_IVX, j + 1, f)] - w[CELL(OG_IVX, j - 1, f)]) / (2. * b->dx2);
             stress += 0.5 * (above + below);
+          } else if (ivar == 2 && v3) {
+            double below = (w[CELL(OG_IVX, j, f - 1) + pl] - w[CELL(OG_IVX, j, f - 1) - pl]) / (2. * b->dx3);
+            double above = (w[CELL(OG_IVX, j, f) + pl] - w[CELL(OG_IVX, j, f) - pl]) / (2. * b->dx3);
+            stress += 0.5 * (above + below);
           }
           double mf = -nu * rf * stress;
           vf1[CELL(v, j, f)] = mf;
@@ -865,6 +883,10 @@ static void tendency_plane(const og_block* b, const double* w, double dt,
             } else if (ivar == 0) {
               double below = (w[CELL(OG_IVY, j - 1, i + 1)] - w[CELL(OG_IVY, j - 1, i - 1)]) / (2. * b->dx1);
               double above = (w[CELL(OG_IVY, j, i + 1)] - w[CELL(OG_IVY, j, i - 1)]) / (2. * b->dx1);
+              stress += 0.5 * (above + below);
+            } else if (ivar == 2 && v3) {
+              double below = (w[CELL(OG_IVY, j - 1, i) + pl] - w[CELL(OG_IVY, j - 1, i) - pl]) / (2. * b->dx3);
+              double above = (w[CELL(OG_IVY, j, i) + pl] - w[CELL(OG_IVY, j, i) - pl]) / (2. * b->dx3);
               stress += 0.5 * (above + below);
             }
             double mf = -nu * rf * stress;
@@ -928,6 +950,7 @@ static void tendency_plane(const og_block* b, const double* w, double dt,
           size_t q = CELL(v, j, i);
           double dv = a1 * vf1[q + 1] - a1 * vf1[q];
           if (has2) dv = dv + (a2 * vf2[q + n1] - a2 * vf2[q]);
+          if (v3) dv = dv + (a3 * v3->vf3[q + plane] - a3 * v3->vf3[q]);
           du[q] = du[q] - dt * (dv / vol);
         }
   }
@@ -1041,13 +1064,76 @@ static void x3_covariance(const og_block* b, const double* w, double* f3) {
   }
 }
 
+/* 3-D viscosity (DiffusionImpl::cartesian_fluxes, src/forcing/
+ * diffusion.cpp:553-683, kinematic nu_iso): the velocity divergence on the
+ * interior extended by one cell in each direction (the x1, x2, x3 centred
+ * derivatives summed in that order) and the x3 faces' viscous fluxes of the
+ * interior (x2, x1) cells: rho the mean of the two cells, the stress of
+ * each velocity component (the normal one 2 dv3/dx3 - 2/3 div v, the others
+ * their x3 derivative plus the face mean of dv3/dx1, dv3/dx2), the momentum
+ * rows -nu rho stress, the energy row the sum of each component's face mean
+ * times its momentum row */
+static void x3_viscosity(const og_block* b, const double* w, double** divv_out,
+                         double** vf3_out) {
+  const int n1 = b->nc1, n2 = b->nc2, n3 = b->nc3, ng = b->ng;
+  const size_t nc = ncell(b), pl = (size_t)n1 * n2;
+  const int has2 = n2 > 1;
+  const int il = ng, iu1 = n1 - ng;
+  const int jl = has2 ? ng : 0, ju1 = has2 ? n2 - ng : 1;
+  double* divv = (double*)calloc(nc, sizeof(double));
+  double* vf3 = (double*)calloc(5 * nc, sizeof(double));
+#define W3(v, k, j, i) w[(size_t)(v) * nc + (size_t)(k) * pl + (size_t)(j) * n1 + (i)]
+  const int ja = has2 ? jl - 1 : 0, jb = has2 ? ju1 + 1 : 1;
+  for (int k = ng - 1; k <= n3 - ng; ++k)
+    for (int j = ja; j < jb; ++j)
+      for (int i = il - 1; i <= iu1; ++i) {
+        double dv = 0.;
+        dv += (W3(OG_IVX, k, j, i + 1) - W3(OG_IVX, k, j, i - 1)) / (2. * b->dx1);
+        if (has2)
+          dv += (W3(OG_IVY, k, j + 1, i) - W3(OG_IVY, k, j - 1, i)) / (2. * b->dx2);
+        dv += (W3(OG_IVZ, k + 1, j, i) - W3(OG_IVZ, k - 1, j, i)) / (2. * b->dx3);
+        divv[(size_t)k * pl + (size_t)j * n1 + i] = dv;
+      }
+  const double nu = b->nu_iso;
+  for (int k = ng; k <= n3 - ng; ++k)
+    for (int j = jl; j < ju1; ++j)
+      for (int i = il; i < iu1; ++i) {
+        const size_t c = (size_t)k * pl + (size_t)j * n1 + i;
+        double rf = 0.5 * (W3(OG_IDN, k, j, i) + W3(OG_IDN, k - 1, j, i));
+        double divf = 0.5 * (divv[c] + divv[c - pl]);
+        double e = 0.;
+        for (int ivar = 0; ivar < 3; ++ivar) {
+          int v = OG_IVX + ivar;
+          double stress = (W3(v, k, j, i) - W3(v, k - 1, j, i)) / b->dx3;
+          if (ivar == 2) {
+            stress = 2. * stress - (2. / 3.) * divf;
+          } else if (ivar == 0) {
+            double below = (W3(OG_IVZ, k - 1, j, i + 1) - W3(OG_IVZ, k - 1, j, i - 1)) / (2. * b->dx1);
+            double above = (W3(OG_IVZ, k, j, i + 1) - W3(OG_IVZ, k, j, i - 1)) / (2. * b->dx1);
+            stress += 0.5 * (above + below);
+          } else if (has2) {
+            double below = (W3(OG_IVZ, k - 1, j + 1, i) - W3(OG_IVZ, k - 1, j - 1, i)) / (2. * b->dx2);
+            double above = (W3(OG_IVZ, k, j + 1, i) - W3(OG_IVZ, k, j - 1, i)) / (2. * b->dx2);
+            stress += 0.5 * (above + below);
+          }
+          double mf = -nu * rf * stress;
+          vf3[(size_t)v * nc + c] = mf;
+          e += 0.5 * (W3(v, k, j, i) + W3(v, k - 1, j, i)) * mf;
+        }
+        vf3[(size_t)OG_IPR * nc + c] = e;
+      }
+#undef W3
+  *divv_out = divv;
+  *vf3_out = vf3;
+}
+
 /* the tendency, and the register totals T_d into T[d - 1] where set */
 static void tendency_reg(const og_block* b, const double* w, double dt,
                          double* du, double* const* T) {
   build_tables();
   const size_t nc = ncell(b);
   if (b->nc3 == 1) {
-    tendency_plane(b, w, dt, du, NULL, T[0], T[1]);
+    tendency_plane(b, w, dt, du, NULL, T[0], T[1], NULL);
     return;
   }
   /* 3-D (no viscosity): the x3 face fluxes of every line, the x3
@@ -1063,11 +1149,29 @@ static void tendency_reg(const og_block* b, const double* w, double dt,
     for (size_t q = 0; q < plane; ++q)
       f3[OG_IDN * nc + k * plane + q] = f3[OG_IPR * nc + k * plane + q] = 0.;
   }
+  double *divv3 = NULL, *vf3 = NULL;
+  if (b->nu_iso > 0.) {
+    x3_viscosity(b, w, &divv3, &vf3);
+    /* post_fluxes: the x3 energy row joins the totals; the walls again */
+    for (int k = ng; k <= n3 - ng; ++k)
+      for (size_t q = 0; q < plane; ++q)
+        f3[OG_IPR * nc + k * plane + q] += vf3[OG_IPR * nc + k * plane + q];
+    for (int side = 0; side < 2; ++side) {
+      if (b->bc[4 + side] != OG_BC_REFLECTING) continue;
+      int k = side ? n3 - ng : ng;
+      for (size_t q = 0; q < plane; ++q)
+        f3[OG_IDN * nc + k * plane + q] = f3[OG_IPR * nc + k * plane + q] = 0.;
+    }
+  }
   memset(du, 0, sizeof(double) * 5 * nc);
-  for (int k = ng; k < n3 - ng; ++k)
+  for (int k = ng; k < n3 - ng; ++k) {
+    og_visc3 v3 = {divv3 ? divv3 + k * plane : NULL, vf3 ? vf3 + k * plane : NULL};
     tendency_plane(b, w + k * plane, dt, du + k * plane, f3 + k * plane,
                    T[0] ? T[0] + k * plane : NULL,
-                   T[1] ? T[1] + k * plane : NULL);
+                   T[1] ? T[1] + k * plane : NULL, divv3 ? &v3 : NULL);
+  }
+  free(divv3);
+  free(vf3);
   if (T[2]) {
     const int jl = n2 > 1 ? ng : 0, ju1 = n2 > 1 ? n2 - ng : 1;
     for (int v = 0; v < 5; ++v)

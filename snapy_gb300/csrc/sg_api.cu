@@ -219,6 +219,7 @@ struct sg_handle {
                                             // columns solved directly
   std::vector<double*> x1tabs;  // per-block geometry tables (gravity)
   bool has3 = false;            // a 3-D block: the x3 sweep runs
+  bool visc3 = false;           // a 3-D block with viscosity: the prep runs
   size_t sum_icols = 0;         // implicit columns of all blocks
   int wide = 0;  // enough columns for a thread per column in the finish
   int wide_auto = 0;  // that rule's own answer (finish form 0)
@@ -427,6 +428,7 @@ int sg_autotune(sg_handle* h, int32_t reps, int32_t* tj_out,
     p.refine = h->refine;
     p.fallbacks = h->fallbacks;
     p.max_nc1 = h->max_nc1;
+    p.visc3 = h->visc3;
     auto stage = [&]() -> int {
       p.ntile = h->ntile;
       int r = 0;
@@ -574,11 +576,6 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
       sg_destroy(h);
       return fail(SG_ERR_ARG, "block %d: sizes (%d, %d, %d)", b, d.nc3, d.nc2,
                   d.nc1);
-    }
-    if (d.nc3 > 1 && d.nu_iso > 0.) {
-      sg_destroy(h);
-      return fail(SG_ERR_UNSUPPORTED, "block %d: 3-D blocks are built without "
-                  "viscosity", b);
     }
     for (int f = 0; f < 6; ++f)
       if (d.bc[f] < SG_BC_NONE || d.bc[f] > SG_BC_EXTRAPOLATION) {
@@ -728,8 +725,15 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
       vic_bytes += (icells * sg::kVicFloatsPerCell +
                     icols * sg::kVicFloatsPerColumn) * sizeof(float);
     vic_bytes = (vic_bytes + 15) / 16 * 16;  // the x3 part starts aligned
-    size_t dv3_bytes = d.nc3 > 1 ? 5 * icells * (f64(h) ? 8 : 4) : 0;
+    const size_t esz = f64(h) ? 8 : 4;
+    size_t dv3_bytes = d.nc3 > 1 ? 5 * icells * esz : 0;
     dv3_bytes = (dv3_bytes + 15) / 16 * 16;
+    if (d.nc3 > 1 && d.nu_iso > 0.) {
+      // the viscous prep planes and the x3 viscous momentum differences
+      const size_t cells3 = (size_t)d.nc1 * d.nc2 * d.nc3;
+      dv3_bytes += (5 * cells3 * esz + 15) / 16 * 16 + (3 * icells * esz + 15) / 16 * 16;
+      h->visc3 = true;
+    }
     // passive scalars: the FP64 mass flux and the scalars' face fluxes along
     // x1 and x2 over the padded block
     const size_t cells = (size_t)d.nc1 * d.nc2 * d.nc3;
@@ -826,6 +830,17 @@ int sg_bind_scratch(sg_handle* h, int32_t block, void* scratch, size_t bytes) {
   B.vic = B.implicit ? static_cast<double*>(scratch) : nullptr;
   B.dv3 = B.nc3 > 1 ? static_cast<unsigned char*>(scratch) + h->vic_bytes[block]
                     : nullptr;
+  B.visc3 = B.dv3v = nullptr;
+  if (B.nc3 > 1 && B.nu_iso > 0.) {
+    const size_t esz = f64(h) ? 8 : 4;
+    const size_t icells = (size_t)(B.nc1 - 2 * B.ng) *
+                          (B.nc2 > 1 ? B.nc2 - 2 * B.ng : 1) * (B.nc3 - 2 * B.ng);
+    const size_t cells3 = (size_t)B.nc1 * B.nc2 * B.nc3;
+    unsigned char* v = static_cast<unsigned char*>(B.dv3) +
+                       (5 * icells * esz + 15) / 16 * 16;
+    B.visc3 = v;
+    B.dv3v = v + (5 * cells3 * esz + 15) / 16 * 16;
+  }
   if (B.nscalar > 0) {
     double* sc = reinterpret_cast<double*>(static_cast<unsigned char*>(scratch) +
                                            h->vic_bytes[block] +
@@ -1061,6 +1076,7 @@ int sg_stage(sg_handle* h, int32_t stage, const double* dt_dev,
   p.refine = h->refine;
   p.fallbacks = h->fallbacks;
   p.max_nc1 = h->max_nc1;
+  p.visc3 = h->visc3;
   // events between the launches when timing is on and the stream is not
   // being captured: ev[0] (x3 ev[6]) stage ev[1] (assemble ev[2] solve
   // ev[3] finish ev[4]) (scalars ev[7]) ghost ev[5]
@@ -1089,7 +1105,7 @@ int sg_stage(sg_handle* h, int32_t stage, const double* dt_dev,
                 : sg_launch_x3_f32(h->dev, p, h->max_cells, s);
     if (rc) return cuda_fail((cudaError_t)rc, "sg_stage: x3 sweep");
     if (timed) cudaEventRecord(ev[6], s);
-    launches += 1;
+    launches += h->visc3 ? 2 : 1;  // with viscosity its prep first
   }
   rc = f64(h) ? sg_launch_stage_f64(h->dev, p, h->smem, s)
               : sg_launch_stage_f32(h->dev, p, h->smem, s);
@@ -1118,7 +1134,9 @@ int sg_stage(sg_handle* h, int32_t stage, const double* dt_dev,
                                        h->implicit ? h->max_icols : 0, s);
     if (rc) return cuda_fail((cudaError_t)rc, "sg_stage: scalars");
     if (timed) cudaEventRecord(ev[7], s);
-    launches += h->implicit ? 3 : 2;
+    // fluxes, the limiter's theta, its ghosts and the scaling, the update
+    // (implicit blocks: and the solve's transfer)
+    launches += h->implicit ? 6 : 5;
   }
   rc = f64(h) ? sg_launch_ghost_f64(h->dev, h->nblock, out, h->max_plane, s)
               : sg_launch_ghost_f32(h->dev, h->nblock, out, h->max_plane, s);

@@ -668,6 +668,11 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
     for (int idx = threadIdx.x; idx < nr * nci; idx += blockDim.x) {
       const int rr = rlo + idx / nci, i = il - 1 + (idx - (rr - rlo) * nci);
       const int r = hj + rr - 1;  // W row
+      if (B.visc3) {  // 3-D: the whole divergence, its x3 term included
+        DIVV[rr * nc1 + i] = static_cast<const real*>(B.visc3)[
+            koff + (size_t)(j0 + rr - 1) * nc1 + i];
+        continue;
+      }
       const real* vx = W + IVX * wstride + r * nc1;
       real dv = real(0);
       dv += vdiv(vx[i + 1] - vx[i - 1], d1, rd1);
@@ -749,6 +754,10 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
           real below = vdiv(vx[o + nc1 + f - 1] - vx[o - nc1 + f - 1], d2x2, rd2x2);
           real above = vdiv(vx[o + nc1 + f] - vx[o - nc1 + f], d2x2, rd2x2);
           stress += real(0.5) * (above + below);
+        } else if (ivar == 2 && B.visc3) {  // 3-D: dv1/dx3 of the two cells
+          const real* d31 = static_cast<const real*>(B.visc3) + plane +
+                            koff + (size_t)(j0 + jt) * nc1;
+          stress += real(0.5) * (d31[f] + d31[f - 1]);
         }
         real mf = -nu * rf * stress;
         VF1[ivar * f1stride + idx] = mf;
@@ -778,6 +787,11 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
             real below = vdiv(vy[om + i + 1] - vy[om + i - 1], d2x1, rd2x1);
             real above = vdiv(vy[o + i + 1] - vy[o + i - 1], d2x1, rd2x1);
             stress += real(0.5) * (above + below);
+          } else if (ivar == 2 && B.visc3) {  // 3-D: dv2/dx3 of the two cells
+            const real* d32 = static_cast<const real*>(B.visc3) + 2 * plane +
+                              koff + i;
+            stress += real(0.5) * (d32[(size_t)(j0 + jf) * nc1] +
+                                   d32[(size_t)(j0 + jf - 1) * nc1]);
           }
           real mf = -nu * rf * stress;
           VF2[ivar * f2stride + idx] = mf;
@@ -908,6 +922,8 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
           const real* f2 = VF2 + (v - IVX) * f2stride + jt * nx1 + ii;
           dv = dv + (a2 * f2[nx1] - a2 * f2[0]);
         }
+        if (B.dv3v)  // 3-D: the x3 faces' viscous difference
+          dv = dv + static_cast<const real*>(B.dv3v)[(v - IVX) * icells + vci];
         du[v] = du[v] - rdt * vdiv(dv, vol, rvol);
       }
     }
@@ -1437,6 +1453,58 @@ __global__ void __launch_bounds__(kThreads)
 // reflecting x3 wall zeroes the mass and energy rows of its face.
 constexpr int kX3Chunk = 16;
 
+// 3-D viscosity's prep (DiffusionImpl::cartesian_fluxes, src/forcing/
+// diffusion.cpp:553-683): on the interior extended by one cell in each
+// direction, the velocity divergence (the x1, x2, x3 centred derivatives
+// summed in that order) and the centred derivatives dv1/dx3, dv2/dx3 (the
+// x1 and x2 faces' shear along x3) and dv3/dx1, dv3/dx2 (the x3 faces'),
+// one thread per cell, into the block's five visc3 planes
+__global__ void __launch_bounds__(kThreads)
+    visc3_kernel(const BlockDev* __restrict__ tab, StageParams p) {
+  const BlockDev& B = tab[blockIdx.y];
+  if (B.nc3 == 1 || !(B.nu_iso > 0.)) return;
+  const int nc1 = B.nc1, nc2 = B.nc2, nc3 = B.nc3, ng = B.ng;
+  const bool has2 = nc2 > 1;
+  const size_t kst = (size_t)nc1 * nc2, plane = kst * nc3;
+  const int e1 = nc1 - 2 * ng + 2, e2 = has2 ? nc2 - 2 * ng + 2 : 1,
+            e3 = nc3 - 2 * ng + 2;
+  const int o2 = has2 ? ng - 1 : 0;
+  const real* u = static_cast<const real*>(B.buf[p.in]);
+  const real gammad = real(B.gammad);
+  const double* rb = B.base ? base_rho(B.base, nc1) : nullptr;
+  real* V = static_cast<real*>(B.visc3);
+  const real d2x1 = real(2.) * real(B.dx1), d2x2 = real(2.) * real(B.dx2),
+             d2x3 = real(2.) * real(B.dx3);
+  const real r1 = real(1.) / d2x1, r2 = real(1.) / d2x2, r3 = real(1.) / d2x3;
+  auto vel = [&](size_t c, int v) -> real {
+    real uc[NHYDRO], w[NHYDRO];
+#pragma unroll
+    for (int q = 0; q < NHYDRO; ++q) uc[q] = u[q * plane + c];
+    if (rb) uc[IDN] = real(rb[c % nc1]) + uc[IDN];
+    cons2prim<real>(uc, w, gammad);
+    return w[v];
+  };
+  const size_t total = (size_t)e1 * e2 * e3;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const int i = ng - 1 + (int)(e % e1);
+    const int j = o2 + (int)((e / e1) % e2);
+    const int k = ng - 1 + (int)(e / ((size_t)e1 * e2));
+    const size_t c = (size_t)k * kst + (size_t)j * nc1 + i;
+    real dv = real(0);
+    dv += vdiv(vel(c + 1, IVX) - vel(c - 1, IVX), d2x1, r1);
+    if (has2) dv += vdiv(vel(c + nc1, IVY) - vel(c - nc1, IVY), d2x2, r2);
+    dv += vdiv(vel(c + kst, IVZ) - vel(c - kst, IVZ), d2x3, r3);
+    V[c] = dv;
+    V[plane + c] = vdiv(vel(c + kst, IVX) - vel(c - kst, IVX), d2x3, r3);
+    V[2 * plane + c] = has2 ? vdiv(vel(c + kst, IVY) - vel(c - kst, IVY), d2x3, r3)
+                            : real(0);
+    V[3 * plane + c] = vdiv(vel(c + 1, IVZ) - vel(c - 1, IVZ), d2x1, r1);
+    V[4 * plane + c] = has2 ? vdiv(vel(c + nc1, IVZ) - vel(c - nc1, IVZ), d2x2, r2)
+                            : real(0);
+  }
+}
+
 template <int RK, bool SHOCK>
 __global__ void __launch_bounds__(kThreads)
     x3_kernel(const BlockDev* __restrict__ tab, StageParams p) {
@@ -1461,6 +1529,8 @@ __global__ void __launch_bounds__(kThreads)
   // either side (an x1 ghost row at the column's ends) -- and trades the
   // face means by shuffles; every lane of a warp runs the same faces
   const bool cov = B.flux_cov && nc1 >= 3;
+  const bool visc = B.nu_iso > 0.;
+  const size_t vplane = plane;  // one visc3 plane
   const int nw = (nx1 + 29) / 30;  // warps per (x2, chunk) line
   const size_t total = cov ? (size_t)32 * nw * nx2 * nch
                            : (size_t)nx1 * nx2 * nch;
@@ -1496,7 +1566,7 @@ __global__ void __launch_bounds__(kThreads)
     real W[6][NHYDRO];
 #pragma unroll
     for (int m = 0; m < 5; ++m) load(k0 - 3 + m, W[m]);
-    real fprev[NHYDRO];
+    real fprev[NHYDRO], vprev[3] = {real(0), real(0), real(0)};
     for (int f = k0; f <= k1; ++f) {
       load(f + 2, W[5]);
       real wl[NHYDRO], wr[NHYDRO], flx[NHYDRO];
@@ -1549,6 +1619,37 @@ __global__ void __launch_bounds__(kThreads)
           for (int v = 0; v < NHYDRO; ++v) W[m][v] = W[m + 1][v];
         continue;
       }
+      // viscosity: the x3 face's viscous fluxes between cells f - 1
+      // (W[2]) and f (W[3]); the energy row joins the total (post_fluxes,
+      // then the walls again), the momentum rows their own difference
+      real vfl[3] = {real(0), real(0), real(0)};
+      if (visc) {
+        const size_t c = (size_t)f * kst + col, cm = c - kst;
+        const real* VP = static_cast<const real*>(B.visc3);
+        const real nu = real(B.nu_iso);
+        const real dx3 = real(B.dx3), rdx3 = real(1.) / dx3;
+        const real rf = real(0.5) * (W[3][IDN] + W[2][IDN]);
+        const real divf = real(0.5) * (VP[c] + VP[cm]);
+        real e = real(0);
+#pragma unroll
+        for (int ivar = 0; ivar < 3; ++ivar) {
+          const int v = IVX + ivar;
+          real stress = vdiv(W[3][v] - W[2][v], dx3, rdx3);
+          if (ivar == 2) {
+            stress = real(2.) * stress - real(2. / 3.) * divf;
+          } else if (ivar == 0) {
+            stress += real(0.5) * (VP[3 * vplane + c] + VP[3 * vplane + cm]);
+          } else if (nc2 > 1) {
+            stress += real(0.5) * (VP[4 * vplane + c] + VP[4 * vplane + cm]);
+          }
+          const real mf = -nu * rf * stress;
+          vfl[ivar] = mf;
+          e += real(0.5) * (W[3][v] + W[2][v]) * mf;
+        }
+        flx[IPR] += e;
+        if ((f == ng && wlo) || (f == ng + nx3 && whi))
+          flx[IDN] = flx[IPR] = real(0);
+      }
       // passive scalars ride on the mass row (the step field's owner rule)
       if (B.nscalar > 0 && (f < k1 || k1 == ng + nx3))
         B.mflux[2][(size_t)f * kst + col] = (double)flx[IDN];
@@ -1573,9 +1674,17 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
         for (int v = 0; v < NHYDRO; ++v)
           DV3[v * cells + vc] = a3 * flx[v] - a3 * fprev[v];
+        if (visc) {
+          real* DVV = static_cast<real*>(B.dv3v);
+#pragma unroll
+          for (int q = 0; q < 3; ++q)
+            DVV[q * cells + vc] = a3 * vfl[q] - a3 * vprev[q];
+        }
       }
 #pragma unroll
       for (int v = 0; v < NHYDRO; ++v) fprev[v] = flx[v];
+#pragma unroll
+      for (int q = 0; q < 3; ++q) vprev[q] = vfl[q];
 #pragma unroll
       for (int m = 0; m < 5; ++m)
 #pragma unroll
@@ -1991,6 +2100,11 @@ extern "C" int SG_NAME(sg_launch_x3)(const BlockDev* tab, StageParams p,
     k = p.shock ? x3_kernel<kHllc, true> : x3_kernel<kHllc, false>;
   else
     k = p.shock ? x3_kernel<kLmars, true> : x3_kernel<kLmars, false>;
+  if (p.visc3) {  // viscosity's prep of the 3-D blocks first
+    int gv = (int)((max_cells + kThreads - 1) / kThreads);
+    if (gv > 2048) gv = 2048;
+    visc3_kernel<<<dim3(gv, p.nblock), kThreads, 0, stream>>>(tab, p);
+  }
   // threads: cells / kX3Chunk per block (bounded by a few waves)
   size_t work = max_cells / kX3Chunk + 1;
   int gx = (int)((work + kThreads - 1) / kThreads);

@@ -64,6 +64,13 @@ struct BlockDev {
   // storage type, laid out (v, k, j, i) over the interior; written by the x3
   // sweep, added to the divergence by the stage kernel
   void* dv3;
+  // 3-D with viscosity: per cell of the block (ghosts included, set on the
+  // interior extended by one cell) the velocity divergence and the centred
+  // derivatives dv1/dx3, dv2/dx3, dv3/dx1, dv3/dx2, five planes in the
+  // storage type (visc3_kernel); and a3 (V3[k+1] - V3[k]) of the x3 faces'
+  // viscous momentum rows (IVX, IVY, IVZ), laid out like dv3
+  void* visc3;
+  void* dv3v;
   // the FluxRegister's FP64 step fields S_d (5, nc3, nc2, nc1), face f
   // along d below cell f (null: not requested), and, for an implicit block
   // with S_1, the stage's x1 totals T_1 staged for the solve's posts,
@@ -132,6 +139,7 @@ struct StageParams {
                         // staging wait ran out)
   int32_t smem_rows;    // x1 lines held in shared memory per tile
   int32_t max_nc1;
+  int32_t visc3;        // some 3-D block has viscosity: visc3_kernel runs
 };
 
 }  // namespace sg

@@ -347,11 +347,15 @@ __device__ __forceinline__ void vic_assemble_cell(const BlockDev& B,
     if (i == n - 1) s += K.t1 * dn[n - 3];
     S.du[4 * S.cells + cell] = du0[4] - s;
   }
+  // the FP64 blocks, unless the refined solve reads the FP32 ones (exact:
+  // its residuals and the masked columns' direct solve widen them)
+  if (!(sizeof(T) == sizeof(float) && f32copy)) {
 #pragma unroll
-  for (int k = 0; k < 25; ++k) {
-    S.A[cell * 25 + k] = (double)a[k];
-    S.B[cell * 25 + k] = (double)b[k];
-    S.C[cell * 25 + k] = (double)c[k];
+    for (int k = 0; k < 25; ++k) {
+      S.A[cell * 25 + k] = (double)a[k];
+      S.B[cell * 25 + k] = (double)b[k];
+      S.C[cell * 25 + k] = (double)c[k];
+    }
   }
   if (sizeof(T) == sizeof(float) && f32copy) {
     // the refined solve's FP32 sweeps read these (the same values), in
@@ -546,6 +550,22 @@ __global__ void __launch_bounds__(32)
   double* A = S.A + cc * n * 25;
   const double* Bm = S.B + cc * n * 25;
   const double* C = S.C + cc * n * 25;
+  // the refined solve's masked columns: the blocks are the FP32 ones
+  // (assembled in FP32, exact), widened; a' still goes to the FP64 A
+  const bool blk32 = Bk.implicit_f32 && p.refine;
+  const int bst = blk32 ? kBlk32 : 25;  // the row of a cell's block
+  const float* A32 = nullptr;
+  const float* B32 = nullptr;
+  const float* C32 = nullptr;
+  if (blk32) {
+    const VicScratch32 F32 = vic_scratch32(Bk, S, n);
+    A32 = F32.A + cc * n * kBlk32;
+    B32 = F32.B + cc * n * kBlk32;
+    C32 = F32.C + cc * n * kBlk32;
+  }
+  auto blkA = [&](int e) -> double { return blk32 ? (double)A32[e] : A[e]; };
+  auto blkB = [&](int e) -> double { return blk32 ? (double)B32[e] : Bm[e]; };
+  auto blkC = [&](int e) -> double { return blk32 ? (double)C32[e] : C[e]; };
   double* D = S.D + cc * n * 5;
   double* Z0 = S.Z0 + cc * n * 5;
   double* Z1 = S.Z1 + cc * n * 5;
@@ -566,7 +586,7 @@ __global__ void __launch_bounds__(32)
 #pragma unroll
   for (int k = 0; k < 5; ++k) s[k] = 0.;
 #pragma unroll
-  for (int e = 0; e < 25; ++e) b[e] = Bm[e];
+  for (int e = 0; e < 25; ++e) b[e] = blkB(e);
   for (int i = 0; i < n; ++i) {
     if (!__any_sync(full, ok)) break;
     // this lane's column of a (q < 5), of c, and the right-hand sides
@@ -574,8 +594,8 @@ __global__ void __launch_bounds__(32)
     if (q < 5) {
 #pragma unroll
       for (int r = 0; r < 5; ++r) {
-        x[r] = A[i * 25 + r * 5 + q];
-        c5[r] = C[i * 25 + r * 5 + q];
+        x[r] = blkA(i * bst + r * 5 + q);
+        c5[r] = blkC(i * bst + r * 5 + q);
       }
     } else {
 #pragma unroll
@@ -604,7 +624,7 @@ __global__ void __launch_bounds__(32)
     }
     if (i + 1 < n) {
 #pragma unroll
-      for (int e = 0; e < 25; ++e) b[e] = Bm[(i + 1) * 25 + e];
+      for (int e = 0; e < 25; ++e) b[e] = blkB((i + 1) * bst + e);
     }
 
     // ---- the factorisation (lanes q < 5 hold the columns) ----
@@ -793,8 +813,8 @@ __device__ __forceinline__ void vsync() {
 // dt_corr and the two Woodbury unit vectors) is solved by the block-Thomas
 // sweep in FP32 (vic_solve32_kernel, the direct solve's lane layout), then
 // corrected p.refine times (1 to 3): the FP64 residual r = b - T x
-// (vic_residual_kernel, from the FP64 copies of the FP32-assembled blocks,
-// which are exact) is solved by the same FP32 sweep and added to x in FP64.
+// (vic_residual_kernel, from the FP32-assembled blocks widened to FP64,
+// which is exact) is solved by the same FP32 sweep and added to x in FP64.
 // That is mixed-precision iterative refinement (the scheme of LAPACK's
 // dsgesv): x converges to the FP64 solution by a factor of about
 // kappa(T) eps32 per correction, the factorisation on the FP32 pipes and
@@ -1454,8 +1474,8 @@ __global__ void __launch_bounds__(32 * kCorrWarps)
 }
 
 // the FP64 residual r = b - (B_i x_(i-1) + A_i x_i + C_i x_(i+1)) of every
-// cell and right-hand side (one thread per cell), from the FP64 blocks (the
-// FP32-assembled values, exact) and x in D, Z0, Z1; rounded to FP32 into R
+// cell and right-hand side (one thread per cell), from the FP32-assembled
+// blocks widened to FP64 (exact) and x in D, Z0, Z1; rounded to FP32 into R
 __global__ void __launch_bounds__(kThreads)
     vic_residual_kernel(const BlockDev* __restrict__ tab, StageParams p) {
   const BlockDev& B = tab[blockIdx.y];
@@ -1471,9 +1491,10 @@ __global__ void __launch_bounds__(kThreads)
     const size_t col = cell / n;
     const int i = (int)(cell - col * n);
     if (F.mask[col]) continue;
-    const double* a = S.A + cell * 25;
-    const double* bl = S.B + cell * 25;
-    const double* c = S.C + cell * 25;
+    // the FP32-assembled blocks (exact), widened
+    const float* a = F.A + cell * kBlk32;
+    const float* bl = F.B + cell * kBlk32;
+    const float* c = F.C + cell * kBlk32;
     for (int k = 0; k < nrhs; ++k) {
       const double* x = (k == 0 ? S.D : (k == 1 ? S.Z0 : S.Z1)) + cell * 5;
       double t[5];
@@ -1485,14 +1506,14 @@ __global__ void __launch_bounds__(kThreads)
       for (int q = 0; q < 5; ++q) {
         const double xc = x[q];
 #pragma unroll
-        for (int r = 0; r < 5; ++r) t[r] = fma(-a[r * 5 + q], xc, t[r]);
+        for (int r = 0; r < 5; ++r) t[r] = fma(-(double)a[r * 5 + q], xc, t[r]);
       }
       if (i > 0) {
 #pragma unroll
         for (int q = 0; q < 5; ++q) {
           const double xl = x[q - 5];
 #pragma unroll
-          for (int r = 0; r < 5; ++r) t[r] = fma(-bl[r * 5 + q], xl, t[r]);
+          for (int r = 0; r < 5; ++r) t[r] = fma(-(double)bl[r * 5 + q], xl, t[r]);
         }
       }
       if (i < n - 1) {
@@ -1500,7 +1521,7 @@ __global__ void __launch_bounds__(kThreads)
         for (int q = 0; q < 5; ++q) {
           const double xu = x[q + 5];
 #pragma unroll
-          for (int r = 0; r < 5; ++r) t[r] = fma(-c[r * 5 + q], xu, t[r]);
+          for (int r = 0; r < 5; ++r) t[r] = fma(-(double)c[r * 5 + q], xu, t[r]);
         }
       }
 #pragma unroll

@@ -76,9 +76,6 @@ def scheme_of(options: MeshBlockOptions) -> dict:
         if options.hydro().precision == "float64" and h.icorr.precision == "float32":
             raise DeckError("integration/implicit-precision float32 needs "
                             "dynamics/precision float32")
-    if c.nx3 > 1:
-        if h.diffusion is not None and h.diffusion.nu_iso:
-            raise DeckError("3-D blocks are built without forcing/diffusion")
     intg = options.intg()
     return {
         "riemann": _lib.HLLC if h.riemann.type == "hllc" else _lib.LMARS,
@@ -168,6 +165,50 @@ class _Intg:
     @property
     def stages(self):
         return self.options.stages
+
+
+class _BlockModule:
+    """A submodule view of a MeshBlock for module(name).buffer(name)."""
+
+    BUFFERS = {
+        "": ("hydro_u", "u0", "scalar_s", "x1f", "x1v", "x2f", "x2v", "x3f",
+             "x3v", "hydro_ref"),
+        "hydro": ("hydro_u", "u0", "hydro_ref"),
+        "coord": ("x1f", "x1v", "x2f", "x2v", "x3f", "x3v"),
+    }
+
+    def __init__(self, block: "MeshBlock", name: str):
+        self.block, self.name = block, name
+
+    @property
+    def options(self):
+        o = self.block.options
+        return {"": o, "hydro": o.hydro(), "coord": o.coord()}[self.name]
+
+    def buffer(self, name: str) -> torch.Tensor:
+        if name not in self.BUFFERS[self.name]:
+            raise KeyError(f"buffer '{name}' of module '{self.name}': "
+                           f"{list(self.BUFFERS[self.name])}")
+        blk = self.block
+        c = blk.options.coord()
+        if name[0] == "x":
+            d = int(name[1])
+            f = c.faces(d)
+            t = f if name.endswith("f") else 0.5 * (f[:-1] + f[1:])
+            return torch.as_tensor(t, dtype=torch.float64, device=blk.device)
+        b = blk.batch
+        if name == "hydro_u":
+            return b.current(0)
+        if name == "u0":
+            return b.store[0][b.rotation()[1]]
+        if name == "scalar_s":
+            s = b.current_scalars(0)
+            if s is None:
+                raise KeyError("buffer 'scalar_s': the block carries no scalars")
+            return s
+        if b.bases[0] is None:
+            raise KeyError("buffer 'hydro_ref': the block stores totals")
+        return b.bases[0]
 
 
 class MeshBlock:
@@ -272,6 +313,24 @@ class MeshBlock:
         vars["hydro_u"] = torch.empty(0, dtype=self.dtype, device=self.device).set_(u)
         self.intg.current_redo = 0
         return vars, 0.0
+
+    # -- module(name).buffer(name) (python/csrc/pyoptions.hpp:99-116) -------
+    def buffer(self, name: str) -> torch.Tensor:
+        """A named buffer of the block (the reference's named_buffers()):
+        "hydro_u" (the current state), "u0" (the stage-0 state, MeshBlock's
+        backup), "scalar_s", the coordinate's "x1f", "x1v", "x2f", "x2v",
+        "x3f", "x3v" (FP64, ghosts included) and, for a block stored as
+        anomalies, "hydro_ref" (its FP64 hydrostatic base)."""
+        return _BlockModule(self, "").buffer(name)
+
+    def module(self, name: str) -> "_BlockModule":
+        """A named submodule (the reference's named_modules()): "hydro" or
+        "coord" (or "" for the block), whose buffer(name) gives the
+        buffers above that belong to it."""
+        if name not in _BlockModule.BUFFERS:
+            raise KeyError(f"module '{name}': the block has "
+                           f"{sorted(k for k in _BlockModule.BUFFERS if k)}")
+        return _BlockModule(self, name)
 
     # -- restart (src/output/restart.cpp, src/mesh/meshblock_restart.cpp) ---
     def write_restart(self, vars: dict, out_dir: str, basename: str = "snapy",

@@ -24,9 +24,13 @@ def rel_l2(a, b):
     return np.array(out)
 
 
-def conv_window(nx1, nx2, nx3, precision, implicit=True, dtheta=2.0, cov=True):
+def conv_window(nx1, nx2, nx3, precision, implicit=True, dtheta=2.0, cov=True,
+                nu=0.0):
     opts = sg.MeshBlockOptions.from_yaml("snapy_gb300/decks/convection3d.yaml")
     opts.hydro().flux_covariance = cov
+    if nu:
+        from snapy_gb300.options import DiffusionOptions
+        opts.hydro().diffusion = DiffusionOptions(nu_iso=nu, raw={"nu_iso": nu})
     c = opts.coord()
     c.nx1, c.nx2, c.nx3 = nx1, nx2, nx3
     c.x1max, c.x2max, c.x3max = nx1 * 50.0, nx2 * 50.0, nx3 * 50.0
@@ -66,6 +70,47 @@ def test_3d_fp64_parity(oracle, cuda, implicit, cov):
         assert blk.check_redo(vars) == 0
         err = rel_l2(vars["hydro_u"].cpu().numpy(), u)
         assert err.max() <= TOL, (step, err)
+
+
+@pytest.mark.parametrize("implicit", [False, True])
+def test_3d_viscosity_fp64_parity(oracle, cuda, implicit):
+    """Viscosity on a 3-D block (nu_iso 75 m^2/s, the x1, x2 and x3 viscous
+    fluxes with their shear terms) with the covariance row, against the
+    oracle at 1e-12."""
+    opts = conv_window(20, 12, 10, "float64", implicit, nu=75.0)
+    blk = sg.MeshBlock(opts).to(cuda)
+    w = problems.convection3d(opts, "cpu", seed=13)
+    vars = {"hydro_w": w.to(cuda)}
+    blk.initialize(vars)
+    ob = oracle.block_from_options(opts)
+    u = ob.initialize(w.numpy())
+    for step in range(3):
+        dt = blk.max_time_step(vars)
+        assert dt == pytest.approx(opts.intg().cfl * ob.max_dt(u), rel=1e-14)
+        for s in range(3):
+            blk.forward(vars, dt, s)
+            ob.stage(u, dt, s)
+        assert blk.check_redo(vars) == 0
+        err = rel_l2(vars["hydro_u"].cpu().numpy(), u)
+        assert err.max() <= TOL, (step, err)
+
+
+def test_3d_viscosity_fp32_against_fp64_oracle(oracle, cuda):
+    opts = conv_window(20, 12, 10, "float32", True, nu=75.0)
+    blk = sg.MeshBlock(opts).to(cuda)
+    w = problems.convection3d(opts, "cpu", seed=17)
+    vars = {"hydro_w": w.to(cuda)}
+    blk.initialize(vars)
+    ob = oracle.block_from_options(opts)
+    u = ob.initialize(w.numpy())
+    dt = 0.9 * ob.max_dt(u)
+    for _ in range(10):
+        blk.step(vars, dt)
+        for s in range(3):
+            ob.stage(u, dt, s)
+    assert blk.check_redo(vars) == 0
+    err = rel_l2(interior(opts, blk.total_u(vars).cpu().numpy()), interior(opts, u))
+    assert err.max() <= TOL32, err
 
 
 def test_3d_fp32_anomaly_against_fp64_oracle(oracle, cuda):

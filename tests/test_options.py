@@ -96,10 +96,14 @@ def test_fp32_implicit_assembly_needs_the_fp32_state():
     _refused(cfg, "implicit-precision")
 
 
-def test_3d_blocks_refuse_diffusion():
+def test_3d_blocks_take_diffusion():
+    """3-D blocks run the viscous fluxes of all three directions; what the
+    diffusion section holds beyond nu_iso is refused by name."""
     cfg = copy.deepcopy(config("convection3d.yaml"))
     cfg.setdefault("forcing", {})["diffusion"] = {"nu_iso": 10.0}
-    _refused(cfg, "diffusion")
+    assert options(cfg).hydro().diffusion.nu_iso == 10.0
+    cfg["forcing"]["diffusion"]["kappa_iso"] = 0.1
+    _refused(cfg, "kappa_iso")
 
 
 def test_refused_boundary_and_stencil():
@@ -132,3 +136,12 @@ def test_implicit_solve_keys():
         cfg["integration"][key] = bad
         with pytest.raises(DeckError, match=key):
             options(cfg)
+
+
+def test_the_reference_import_name():
+    """``import snapy`` is the drop-in's own surface."""
+    import snapy
+    import snapy_gb300
+    assert snapy.MeshBlock is snapy_gb300.MeshBlock
+    assert snapy.MeshBlockOptions is snapy_gb300.MeshBlockOptions
+    assert (snapy.kIDN, snapy.kIPR) == (snapy_gb300.kIDN, snapy_gb300.kIPR)

@@ -8,25 +8,32 @@ import snapy_gb300 as sg
 from snapy_gb300 import problems
 
 
-def window(deck, nx1, nx2, nx3, cov=False):
+def window(deck, nx1, nx2, nx3, cov=False, visc=False):
     opts = sg.MeshBlockOptions.from_yaml(f"snapy_gb300/decks/{deck}")
     c = opts.coord()
     c.nx1, c.nx2, c.nx3 = nx1, nx2, nx3
     c.x1max, c.x2max, c.x3max = nx1 * 50.0, nx2 * 50.0, nx3 * 50.0
     h = opts.hydro()
-    h.diffusion = None
+    if not visc:
+        h.diffusion = None
     h.flux_covariance = cov
     if nx3 > 1:
         opts.bcnames = list(opts.bcnames[:4]) + ["periodic_inner", "periodic_outer"]
     return opts
 
 
-@pytest.mark.parametrize("cov", [False, True])
-@pytest.mark.parametrize("deck", ["straka.yaml", "straka_explicit.yaml"])
-def test_x3_uniform_3d_equals_2d(oracle, deck, cov):
-    """With the covariance row too: on x3 faces its u_n is zero."""
-    o2 = window(deck, 24, 16, 1, cov)
-    o3 = window(deck, 24, 16, 6, cov)
+@pytest.mark.parametrize("deck,cov,visc", [
+    ("straka.yaml", False, False), ("straka_explicit.yaml", False, False),
+    ("straka.yaml", True, False), ("straka_explicit.yaml", True, False),
+    ("straka.yaml", True, True)])
+def test_x3_uniform_3d_equals_2d(oracle, deck, cov, visc):
+    """With the covariance row too (on x3 faces its u_n is zero), and with
+    viscosity (the x3 derivatives vanish and the x3 faces' viscous fluxes are
+    uniform along x3)."""
+    o2 = window(deck, 24, 16, 1, cov, visc)
+    o3 = window(deck, 24, 16, 6, cov, visc)
+    if visc:
+        assert o3.hydro().diffusion is not None and o3.hydro().diffusion.nu_iso > 0
     w2 = problems.straka(o2, "cpu", xc=300.0, zc=600.0, xr=300.0, zr=300.0).numpy()
     c3 = o3.coord()
     w3 = np.ascontiguousarray(np.broadcast_to(w2, (5, c3.nc3) + w2.shape[2:]))
