@@ -1298,7 +1298,7 @@ def run_cubed_sphere(args):
                          "bytes_per_launch": statistics.mean(stage_bytes),
                          "mean_launch_us": statistics.mean(durs) * 1e6},
             "cpu_baseline": cb, "clocks": clk.summary(),
-            "gpu_launches": args.steps * (2 + 3 * 4),
+            "gpu_launches": args.steps * (2 + 3 * 5),
             "step_ms_median": statistics.median(step_ms)}), flush=True)
     ranks.close()
     return 0

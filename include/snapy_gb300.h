@@ -313,12 +313,12 @@ typedef struct sg_cs_desc {
   /* the face-state exchange at the seams (HydroImpl::forward's cross-panel
    * sync of hydro_wl / hydro_wr, src/hydro/hydro_forward.cpp:719-757): one
    * row of 16 doubles per seam face, 24 n rows ordered (panel, side L R B
-   * T, along): the neighbour panel, its first stencil cell (k nc + j), the
-   * stencil stride (+1 along x2, +nc along x3), 1 if the neighbour's
-   * interior-side state is its left state (its R / T side) else 0, then the
-   * 3 x 3 map of contravariant velocities (radial, alpha, beta) from the
-   * neighbour's face frame to this panel's at the shared face point (row
-   * major), then 3 unused */
+   * T, along): the neighbour panel, its side (0..3 for L R B T) and the
+   * face's along index on that side (whose interior-side state the
+   * neighbour's own reconstruction gives), a 0, then the 3 x 3 map of
+   * contravariant velocities (radial, alpha, beta) from the neighbour's
+   * face frame to this panel's at the shared face point (row major), then
+   * 3 unused */
   const double* seam_state_tab;
   int32_t nseam_state;
 } sg_cs_desc;

@@ -2,7 +2,7 @@
 // n x n cells (nghost 3, one radial cell) in ONE handle, FP64 or FP32 state
 // (6, 4, nc, nc): Phi, the radial and the two covariant tangential momenta.
 //
-// A stage is four launches, each over all six panels:
+// A stage is five launches, each over all six panels:
 //   cs_flux_kernel       every x2 and x3 face of the panels' interiors: the
 //                        primitives of its six-cell stencil (U/Phi, momenta
 //                        raised by the cell cosine), weno5 for Phi and cp5
@@ -12,10 +12,11 @@
 //                        (src/riemann/riemann.cpp:219-346 with
 //                        src/coord/gnomonic_equiangle.cpp:357-463,
 //                        src/riemann/riemann_kernels.h:447-495)
-//                        -- at a seam face with its exterior-side state
-//                        from the neighbour panel's own interior-side
-//                        reconstruction, mapped into this panel's frame at
-//                        the shared face (the cross-panel face-state sync,
+//                        (a seam face keeps its interior-side state)
+//   cs_seam_face_kernel  the seam faces again, each with its exterior-side
+//                        state the neighbour panel's own interior-side
+//                        state, mapped into this panel's frame at the
+//                        shared face (the cross-panel face-state sync,
 //                        src/hydro/hydro_forward.cpp:719-757)
 //   cs_seam_flux_kernel  the seam faces of the non-owning panels take the
 //                        owner's flux through the Cartesian frame
@@ -97,6 +98,7 @@ struct CsParams {
   const void* stab;
   int nseam;
   const void* sst;  // the seam face-state table (4 sides x n per panel)
+  void* sbuf;       // the seam faces' interior-side states (24 n x 4)
   const void* in;
   const void* u0;
   void* out;
@@ -229,10 +231,14 @@ __device__ __forceinline__ void hllc_sw(const T* L, const T* R, T* F, T phi0) {
 }
 
 // the flux of one face: panel p, an x2 face (row k, face j) or an x3 face
-// (face k, column j).  side >= 0 (a seam face, side L R B T of the panel,
-// `along` its index on that side) takes the exterior-side state from the
-// seam face-state table
-template <typename T, bool HLLC>
+// (face k, column j).  The bulk pass (SEAM false) reconstructs both sides
+// from the panel's own stencil; at a seam face (side >= 0: side L R B T of
+// the panel, `along` its index on that side) it also keeps its interior-side
+// state in the seam buffer.  The seam pass (SEAM true) takes the face's own
+// interior-side state and the neighbour's from that buffer, the neighbour's
+// velocities mapped into this panel's frame at the shared face (the
+// reference's cross-panel face-state sync), and redoes the flux
+template <typename T, bool HLLC, bool SEAM>
 __device__ __forceinline__ void cs_face(const CsParams& P, const Geo<T>& G,
                                         int p, bool x2, int k, int j,
                                         int side, int along) {
@@ -240,53 +246,47 @@ __device__ __forceinline__ void cs_face(const CsParams& P, const Geo<T>& G,
   const size_t pst = (size_t)nc * nc;  // one variable of a panel
   const T phi0 = T(P.phi0);
   const T* U = static_cast<const T*>(P.in);
+  T* SB = static_cast<T*>(P.sbuf);  // 4 values per seam face
   {
-    const T* q = U + (size_t)p * 4 * pst;
-    T st[6][4];
-#pragma unroll
-    for (int m = 0; m < 6; ++m) {
-      const int kk = x2 ? k : k - 3 + m, jj = x2 ? j - 3 + m : j;
-      const size_t c = (size_t)kk * nc + jj;
-      sw_prim<T>(q, pst, c, T(G.cos_c[c]), st[m], phi0);
-    }
     T wl[4], wr[4], F[4];
+    if (!SEAM) {
+      const T* q = U + (size_t)p * 4 * pst;
+      T st[6][4];
 #pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      if (v == IDN) {
-        wl[v] = sg::weno5_cp<T>(st[0][v], st[1][v], st[2][v], st[3][v], st[4][v], false);
-        wr[v] = sg::weno5_cm<T>(st[1][v], st[2][v], st[3][v], st[4][v], st[5][v], false);
-      } else {
-        wl[v] = sg::cp5_cp<T>(st[0][v], st[1][v], st[2][v], st[3][v], st[4][v]);
-        wr[v] = sg::cp5_cm<T>(st[1][v], st[2][v], st[3][v], st[4][v], st[5][v]);
+      for (int m = 0; m < 6; ++m) {
+        const int kk = x2 ? k : k - 3 + m, jj = x2 ? j - 3 + m : j;
+        const size_t c = (size_t)kk * nc + jj;
+        sw_prim<T>(q, pst, c, T(G.cos_c[c]), st[m], phi0);
       }
-    }
-    // a seam face: the exterior-side state is the neighbour panel's own
-    // interior-side state at the same face, its velocities mapped into this
-    // panel's frame (the reference's cross-panel face-state sync)
-    if (side >= 0) {
-      const T* r = static_cast<const T*>(P.sst) +
-                   ((size_t)(p * 4 + side) * n + along) * kSeamStateStride;
-      const int qp = (int)r[0], c0 = (int)r[1], cst = (int)r[2];
-      const bool left = r[3] != T(0);
-      const T* qq = U + (size_t)qp * 4 * pst;
-      T s5[5][4];
 #pragma unroll
-      for (int m = 0; m < 5; ++m) {
-        const size_t c = (size_t)(c0 + m * cst);
-        sw_prim<T>(qq, pst, c, T(G.cos_c[c]), s5[m], phi0);
+      for (int v = 0; v < 4; ++v) {
+        if (v == IDN) {
+          wl[v] = sg::weno5_cp<T>(st[0][v], st[1][v], st[2][v], st[3][v], st[4][v], false);
+          wr[v] = sg::weno5_cm<T>(st[1][v], st[2][v], st[3][v], st[4][v], st[5][v], false);
+        } else {
+          wl[v] = sg::cp5_cp<T>(st[0][v], st[1][v], st[2][v], st[3][v], st[4][v]);
+          wr[v] = sg::cp5_cm<T>(st[1][v], st[2][v], st[3][v], st[4][v], st[5][v]);
+        }
       }
+      if (side >= 0) {  // the interior side: the right one on L / B
+        const T* in = (side == 0 || side == 2) ? wr : wl;
+        T* b = SB + ((size_t)(p * 4 + side) * n + along) * 4;
+#pragma unroll
+        for (int v = 0; v < 4; ++v) b[v] = in[v];
+      }
+    } else {
+      const size_t own = (size_t)(p * 4 + side) * n + along;
+      const T* r = static_cast<const T*>(P.sst) + own * kSeamStateStride;
+      const size_t nb = ((size_t)((int)r[0] * 4 + (int)r[1])) * n + (int)r[2];
+      const T* M = r + 4;
+      T* in = (side == 0 || side == 2) ? wr : wl;
+      T* ext = (side == 0 || side == 2) ? wl : wr;
       T we[4];
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
-        if (v == IDN)
-          we[v] = left ? sg::weno5_cp<T>(s5[0][v], s5[1][v], s5[2][v], s5[3][v], s5[4][v], false)
-                       : sg::weno5_cm<T>(s5[0][v], s5[1][v], s5[2][v], s5[3][v], s5[4][v], false);
-        else
-          we[v] = left ? sg::cp5_cp<T>(s5[0][v], s5[1][v], s5[2][v], s5[3][v], s5[4][v])
-                       : sg::cp5_cm<T>(s5[0][v], s5[1][v], s5[2][v], s5[3][v], s5[4][v]);
+        in[v] = SB[own * 4 + v];
+        we[v] = SB[nb * 4 + v];
       }
-      const T* M = r + 4;
-      T* ext = (side == 0 || side == 2) ? wl : wr;
       ext[IDN] = we[IDN];
 #pragma unroll
       for (int a = 0; a < 3; ++a)
@@ -349,44 +349,49 @@ __device__ __forceinline__ void cs_face(const CsParams& P, const Geo<T>& G,
 }
 
 // the faces: thread e < 6 n (n + 1) an x2 face (panel, row k, face j), the
-// next 6 n (n + 1) the x3 faces (panel, face k, column j), each from its own
-// panel's stencils -- but for the seam faces, which the last 24 n threads
-// take (panel, side L R B T, along), each with its exterior-side state from
-// the neighbour panel.  The seam faces thus run in warps of their own, in
-// the same wave as the bulk, and no bulk warp diverges on them beyond an
-// idle lane
+// rest x3 faces (panel, face k, column j), each from its own panel's
+// stencils; a seam face keeps its interior-side state for the seam pass
 template <typename T, bool HLLC>
 __global__ void __launch_bounds__(kThreads)
     cs_flux_kernel(const __grid_constant__ CsParams P) {
   const int n = P.n;
   const Geo<T> G = geo_of<T>(P.geo, P.nc);
   const size_t nf = (size_t)6 * n * (n + 1);
-  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-       e < 2 * nf + 24 * (size_t)n; e += (size_t)gridDim.x * blockDim.x) {
-    if (e >= 2 * nf) {
-      const int s = (int)(e - 2 * nf);
-      const int along = s % n, side = (s / n) % 4, p = s / (4 * n);
-      const bool x2 = side < 2;
-      const int edge = (side & 1) ? kNg + n : kNg;
-      const int k = x2 ? kNg + along : edge, j = x2 ? edge : kNg + along;
-      cs_face<T, HLLC>(P, G, p, x2, k, j, side, along);
-      continue;
-    }
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < 2 * nf;
+       e += (size_t)gridDim.x * blockDim.x) {
     const bool x2 = e < nf;
     const size_t r = x2 ? e : e - nf;
-    int p, k, j;
+    int p, k, j, side = -1, along = 0;
     if (x2) {  // faces j = ng..ng+n of rows k = ng..ng+n-1
       j = kNg + (int)(r % (n + 1));
       k = kNg + (int)((r / (n + 1)) % n);
       p = (int)(r / ((size_t)(n + 1) * n));
-      if (j == kNg || j == kNg + n) continue;  // a seam face
+      if (j == kNg || j == kNg + n) side = j == kNg ? 0 : 1, along = k - kNg;
     } else {  // faces k = ng..ng+n of columns j = ng..ng+n-1
       j = kNg + (int)(r % n);
       k = kNg + (int)((r / n) % (n + 1));
       p = (int)(r / ((size_t)n * (n + 1)));
-      if (k == kNg || k == kNg + n) continue;  // a seam face
+      if (k == kNg || k == kNg + n) side = k == kNg ? 2 : 3, along = j - kNg;
     }
-    cs_face<T, HLLC>(P, G, p, x2, k, j, -1, 0);
+    cs_face<T, HLLC, false>(P, G, p, x2, k, j, side, along);
+  }
+}
+
+// the 24 n seam faces again from the seam buffer (thread e: panel e / 4n,
+// side (e / n) % 4 in L R B T, along e % n): the Riemann problem of the
+// face's own interior side and the neighbour's
+template <typename T, bool HLLC>
+__global__ void __launch_bounds__(kThreads)
+    cs_seam_face_kernel(const __grid_constant__ CsParams P) {
+  const int n = P.n;
+  const Geo<T> G = geo_of<T>(P.geo, P.nc);
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < 24 * n;
+       e += gridDim.x * blockDim.x) {
+    const int along = e % n, side = (e / n) % 4, p = e / (4 * n);
+    const bool x2 = side < 2;
+    const int edge = (side & 1) ? kNg + n : kNg;
+    const int k = x2 ? kNg + along : edge, j = x2 ? edge : kNg + along;
+    cs_face<T, HLLC, true>(P, G, p, x2, k, j, side, along);
   }
 }
 
@@ -699,7 +704,8 @@ int sg_cs_scratch_bytes(const sg_cs_handle* h, size_t* bytes) {
   if (!h || !bytes) return cs_fail(SG_ERR_ARG, "sg_cs_scratch_bytes: null");
   const size_t nc = (size_t)h->d.n + 2 * kNg;
   const size_t s = h->d.dtype == SG_F64 ? 8 : 4;
-  *bytes = 2 * 6 * 4 * nc * (nc + 1) * s;  // F2 and F3
+  // F2 and F3, then the seam faces' interior-side states
+  *bytes = 2 * 6 * 4 * nc * (nc + 1) * s + 24 * (size_t)h->d.n * 4 * s;
   return 0;
 }
 
@@ -773,6 +779,7 @@ static CsParams cs_params(const sg_cs_handle* h) {
   const size_t s = h->d.dtype == SG_F64 ? 8 : 4;
   P.f2 = h->scratch;
   P.f3 = static_cast<unsigned char*>(h->scratch) + 6 * 4 * nc * (nc + 1) * s;
+  P.sbuf = static_cast<unsigned char*>(h->scratch) + 2 * 6 * 4 * nc * (nc + 1) * s;
   return P;
 }
 
@@ -809,13 +816,17 @@ int sg_cs_stage(sg_cs_handle* h, int32_t stage, const double* dt_dev,
   const size_t cells = (size_t)6 * P.n * P.n;
   if (h->d.dtype == SG_F64) {
     (P.hllc ? cs_flux_kernel<double, true> : cs_flux_kernel<double, false>)
-        <<<grid_for(faces + 24 * (size_t)P.n), kThreads, 0, s>>>(P);
+        <<<grid_for(faces), kThreads, 0, s>>>(P);
+    (P.hllc ? cs_seam_face_kernel<double, true> : cs_seam_face_kernel<double, false>)
+        <<<grid_for(24 * (size_t)P.n), kThreads, 0, s>>>(P);
     cs_seam_flux_kernel<double><<<grid_for(P.nseam), kThreads, 0, s>>>(P);
     cs_update_kernel<double><<<grid_for(cells), kThreads, 0, s>>>(P);
     cs_ghost_kernel<double><<<grid_for(P.nghost), kThreads, 0, s>>>(P, P.out);
   } else {
     (P.hllc ? cs_flux_kernel<float, true> : cs_flux_kernel<float, false>)
-        <<<grid_for(faces + 24 * (size_t)P.n), kThreads, 0, s>>>(P);
+        <<<grid_for(faces), kThreads, 0, s>>>(P);
+    (P.hllc ? cs_seam_face_kernel<float, true> : cs_seam_face_kernel<float, false>)
+        <<<grid_for(24 * (size_t)P.n), kThreads, 0, s>>>(P);
     cs_seam_flux_kernel<float><<<grid_for(P.nseam), kThreads, 0, s>>>(P);
     cs_update_kernel<float><<<grid_for(cells), kThreads, 0, s>>>(P);
     cs_ghost_kernel<float><<<grid_for(P.nghost), kThreads, 0, s>>>(P, P.out);

@@ -306,14 +306,12 @@ def _side_faces(p: int, side: str, n: int):
 
 def seam_state_table(n: int) -> np.ndarray:
     """One row of SEAM_STATE_STRIDE doubles per seam face, ordered (panel,
-    side L R B T, along): the neighbour panel q sharing the face, the first
-    of the five cells of q's own interior-side stencil (k nc + j of q's
-    padded panel), the stencil's stride (+1 along x2, +nc along x3), 1 if
-    that state is q's left state (q's R or T side) else 0, and the 3 x 3
-    map (row major) of contravariant velocities (radial, alpha, beta) in
-    q's unit basis at the face to this panel's: M = B_p^-1 B_q with B the
-    basis (r, t_alpha, t_beta) as columns."""
-    nc = n + 2 * NG
+    side L R B T, along): the neighbour panel q sharing the face, q's side
+    (0..3 for L R B T) and the face's along index on it (so the seam buffer
+    row (4 q + side) n + along holds q's own interior-side state there), a
+    0, and the 3 x 3 map (row major) of contravariant velocities (radial,
+    alpha, beta) in q's unit basis at the face to this panel's:
+    M = B_p^-1 B_q with B the basis (r, t_alpha, t_beta) as columns."""
     d = 0.5 * math.pi / n
     e = 0.25 * math.pi
     rows = np.zeros((6, 4, n, SEAM_STATE_STRIDE))
@@ -336,19 +334,10 @@ def seam_state_table(n: int) -> np.ndarray:
             ta_p, tb_p = tangents(p, al, be)
             ta_q, tb_q = tangents(q, aq, bq)
             for m in range(n):
-                a = NG + mq[m]  # q's row (L / R) or column (B / T)
-                if qside == "R":
-                    c0, cst, left = a * nc + (NG + n - 3), 1, 1
-                elif qside == "L":
-                    c0, cst, left = a * nc + (NG - 2), 1, 0
-                elif qside == "T":
-                    c0, cst, left = (NG + n - 3) * nc + a, nc, 1
-                else:
-                    c0, cst, left = (NG - 2) * nc + a, nc, 0
                 Bp = np.stack([P[m], ta_p[m], tb_p[m]], axis=1)
                 Bq = np.stack([P[m], ta_q[m], tb_q[m]], axis=1)
                 M = np.linalg.solve(Bp, Bq)
-                rows[p, si, m, :4] = (q, c0, cst, left)
+                rows[p, si, m, :4] = (q, SIDES.index(qside), mq[m], 0)
                 rows[p, si, m, 4:13] = M.ravel()
     return np.ascontiguousarray(rows.reshape(-1, SEAM_STATE_STRIDE))
 

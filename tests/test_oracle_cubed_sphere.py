@@ -222,12 +222,12 @@ def test_hllc_is_close_to_shallow_roe_and_conservative():
 
 @pytest.mark.parametrize("n", [8, 24])
 def test_seam_state_table_is_the_references_face_state_sync(n):
-    """The product's seam face-state table, applied as the flux kernel
-    applies it (the neighbour's five-cell interior-side stencil, its
-    velocities mapped at the shared face), equals the restated cross-panel
-    face-state sync to round-off."""
+    """The product's seam face-state table, applied as the seam pass applies
+    it (the neighbour's own interior-side state at its side and along index,
+    its velocities mapped at the shared face), equals the restated
+    cross-panel face-state sync to round-off."""
     from oracle import cs_seams as R
-    from oracle.cubed_sphere import CubedSphere, _recon
+    from oracle.cubed_sphere import CubedSphere
     o = CubedSphere(n, cs.RK3, 0.9)
     u = cs.bump(n, seed=11, width=0.5)
     rng = np.random.default_rng(3)
@@ -236,20 +236,18 @@ def test_seam_state_table_is_the_references_face_state_sync(n):
     w = o.cons2prim(u)
     w2l, w2r = o._states(w, 2)
     w3l, w3r = o._states(w, 1)
+    # each side's interior-side states before the sync (L / B: the right
+    # state, R / T: the left), per panel (4, n)
+    inner = {0: lambda q: w2r[q][:, :, 0].copy(), 1: lambda q: w2l[q][:, :, n].copy(),
+             2: lambda q: w3r[q][:, 0, :].copy(), 3: lambda q: w3l[q][:, n, :].copy()}
+    before = {(q, si): inner[si](q) for q in range(6) for si in range(4)}
     R.seam_states_all(w2l, w2r, w3l, w3r, o.g)
-    nc = n + 2 * NG
     tab = cs.seam_state_table(n).reshape(6, 4, n, cs.SEAM_STATE_STRIDE)
     for p in range(6):
         for side in range(4):
             t = tab[p, side]
-            q, c0, cst, left = (t[:, i].astype(np.int64) for i in range(4))
-            cells = c0[:, None] + np.arange(5)[None, :] * cst[:, None]
-            st = np.stack([w[q[m]][:, cells[m] // nc, cells[m] % nc]
-                           for m in range(n)])          # (n, 4, 5)
-            we = np.empty((n, 4))
-            for v in range(4):
-                for m in range(n):
-                    we[m, v] = _recon(st[m, v][None, :], v == 0, int(left[m]))[0]
+            q, qs, mq = (t[:, i].astype(np.int64) for i in range(3))
+            we = np.stack([before[(int(q[m]), int(qs[m]))][:, mq[m]] for m in range(n)])
             M = t[:, 4:13].reshape(n, 3, 3)
             ext = we.copy()
             ext[:, 1:] = np.einsum("mab,mb->ma", M, we[:, 1:])
