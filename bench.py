@@ -140,9 +140,9 @@ def parse():
     ap.add_argument("--requests", type=int, default=24,
                     help="serving: requests in the trace")
     ap.add_argument("--no-plain", action="store_true",
-                    help="serving: skip the plain FP64 comparison and the "
-                         "alone/FP32 checks (for kernel profiles of the "
-                         "served launches alone)")
+                    help="ensemble and serving: skip the plain FP64 "
+                         "comparison (and the served alone/FP32 checks), for "
+                         "kernel profiles of the batched launches alone")
     ap.add_argument("--serve-budget-gb", type=float, default=8.0,
                     help="serving: the HBM budget requests are admitted "
                          "against (GiB; 0: the device's free memory)")
@@ -731,7 +731,8 @@ def run_ensemble(args, ranks=None, emit=True):
         c.nx1, c.nx2, c.x1max, c.x2max = c0.nx1, c0.nx2, c0.x1max, c0.x2max
         o64.hydro().precision = "float64"
         pairs.append((o64, (lambda w=w: w)))
-    plain = plain_fp64_blocks(pairs, dev)
+    plain = plain_fp64_blocks(pairs, dev) if not args.no_plain else \
+        {"device": float("nan"), "wall": float("nan"), "steps_per_request": 0}
     e2e_value = job_rate(cells * e2e_steps, world, e2e_t)
 
     line = None

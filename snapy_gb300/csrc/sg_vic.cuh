@@ -447,6 +447,28 @@ struct VCol {
   }
 };
 
+// a float widened to the double of the same value with integer operations
+// only: the FP64 kernels here are bound by the FP64 pipe, which the widening
+// instruction would also occupy.  Normal numbers rebias the exponent (127 ->
+// 1023) and shift the mantissa up 29 bits; zeros keep their sign; a
+// subnormal m 2^-149 is renormalised at its leading bit; infinities and NaNs
+// keep their payload (the quiet bit lands on the double's)
+__device__ __forceinline__ unsigned long long widen_bits(unsigned int b) {
+  const unsigned long long sgn = (unsigned long long)(b >> 31) << 63;
+  const unsigned int e = (b >> 23) & 0xffu;
+  const unsigned long long m = b & 0x7fffffu;
+  if (e == 0xffu) return sgn | (0x7ffull << 52) | (m << 29);
+  if (e != 0u) return sgn | ((unsigned long long)(e + 896u) << 52) | (m << 29);
+  if (m == 0u) return sgn;
+  const int k = 31 - __clz((int)m);  // the leading bit, 0..22
+  return sgn | ((unsigned long long)(k + 874) << 52) |
+         ((m << (52 - k)) & 0xfffffffffffffull);
+}
+
+__device__ __forceinline__ double widen_exact(float f) {
+  return __longlong_as_double((long long)widen_bits(__float_as_uint(f)));
+}
+
 // finite, tested on the exponent bits (integer pipes, not the FP64 one)
 __device__ __forceinline__ bool vfinite(double x) {
   return ((__double_as_longlong(x) >> 52) & 0x7ff) != 0x7ff;
@@ -563,9 +585,9 @@ __global__ void __launch_bounds__(32)
     B32 = F32.B + cc * n * kBlk32;
     C32 = F32.C + cc * n * kBlk32;
   }
-  auto blkA = [&](int e) -> double { return blk32 ? (double)A32[e] : A[e]; };
-  auto blkB = [&](int e) -> double { return blk32 ? (double)B32[e] : Bm[e]; };
-  auto blkC = [&](int e) -> double { return blk32 ? (double)C32[e] : C[e]; };
+  auto blkA = [&](int e) -> double { return blk32 ? widen_exact(A32[e]) : A[e]; };
+  auto blkB = [&](int e) -> double { return blk32 ? widen_exact(B32[e]) : Bm[e]; };
+  auto blkC = [&](int e) -> double { return blk32 ? widen_exact(C32[e]) : C[e]; };
   double* D = S.D + cc * n * 5;
   double* Z0 = S.Z0 + cc * n * 5;
   double* Z1 = S.Z1 + cc * n * 5;
@@ -804,7 +826,7 @@ constexpr int kVicWarps = 4;  // columns per CTA of the finish (a warp each)
 // on every lane
 template <int NL>
 __device__ __forceinline__ void vsync() {
-  if (NL > 1) vsync<NL>();
+  if (NL > 1) __syncwarp();
 }
 
 // ---------------------------------------------------------------------------
@@ -1506,14 +1528,14 @@ __global__ void __launch_bounds__(kThreads)
       for (int q = 0; q < 5; ++q) {
         const double xc = x[q];
 #pragma unroll
-        for (int r = 0; r < 5; ++r) t[r] = fma(-(double)a[r * 5 + q], xc, t[r]);
+        for (int r = 0; r < 5; ++r) t[r] = fma(-widen_exact(a[r * 5 + q]), xc, t[r]);
       }
       if (i > 0) {
 #pragma unroll
         for (int q = 0; q < 5; ++q) {
           const double xl = x[q - 5];
 #pragma unroll
-          for (int r = 0; r < 5; ++r) t[r] = fma(-(double)bl[r * 5 + q], xl, t[r]);
+          for (int r = 0; r < 5; ++r) t[r] = fma(-widen_exact(bl[r * 5 + q]), xl, t[r]);
         }
       }
       if (i < n - 1) {
@@ -1521,7 +1543,7 @@ __global__ void __launch_bounds__(kThreads)
         for (int q = 0; q < 5; ++q) {
           const double xu = x[q + 5];
 #pragma unroll
-          for (int r = 0; r < 5; ++r) t[r] = fma(-(double)c[r * 5 + q], xu, t[r]);
+          for (int r = 0; r < 5; ++r) t[r] = fma(-widen_exact(c[r * 5 + q]), xu, t[r]);
         }
       }
 #pragma unroll
