@@ -91,8 +91,12 @@ typedef struct sg_block_desc {
    * gravity work; may be null without gravity and covariance */
   const double* x1f;
   const double* x1v;
-  /* integration/implicit-scheme: 0 (none) or 9 (the full 5x5 vertical
-   * implicit solve, FP64; needs const-gravity and reflecting x1 walls) */
+  /* integration/implicit-scheme: 0 (none), 9 (the full 5x5 vertical
+   * implicit solve) or 1 (the partial 3x3 blocks of rows and columns
+   * {rho, m1, E}, the tangential momenta folded into the density column and
+   * carried by the face mass transfers; FP64 assembly only).  Both need
+   * const-gravity and reflecting x1 walls
+   * (src/implicit/implicit_hydro.hpp:25-41) */
   int32_t implicit_scheme;
   /* SG_F32 with gravity: the FP64 hydrostatic base the FP32 state is stored
    * about (the buffers hold u - u_b), 5 nc1 + 1 device doubles:

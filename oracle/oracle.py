@@ -115,6 +115,7 @@ def lib():
         L.og_tendency.argtypes = [bp, _dp, ctypes.c_double, _dp]
         L.og_implicit.restype = ctypes.c_int
         L.og_implicit.argtypes = [bp, _dp, ctypes.c_double, _dp]
+        L.og_vic_redistribute_partial.argtypes = [ctypes.c_int, _dp, _dp, _dp, _dp]
         L.og_ref_column.argtypes = [bp, _dp, ctypes.c_size_t, _dp, _dp, _dp,
                                     _dp, _dp, _dp]
         L.og_recon_batch.argtypes = [_dp, ctypes.c_long, ctypes.c_int,
@@ -180,6 +181,20 @@ def block_from_options(opts, nthreads=0):
                  flux_cov=h.flux_covariance, x1f=c.faces(1), x2f=c.faces(2),
                  implicit_scheme=h.icorr.scheme if h.icorr else 0,
                  cfl=opts.intg().cfl)
+
+
+def vic_redistribute_partial(w: np.ndarray, du: np.ndarray, vol: np.ndarray,
+                             delta: np.ndarray) -> np.ndarray:
+    """The partial matrix's redistribution of one column (the constituent
+    column, the tangential momenta carried by the face mass, the per-cell
+    map): w, du (5, n); vol (n,); delta (n, 3).  Returns the new du."""
+    w = np.ascontiguousarray(w, dtype=np.float64)
+    out = np.array(du, dtype=np.float64, order="C")
+    vol = np.ascontiguousarray(vol, dtype=np.float64)
+    delta = np.ascontiguousarray(delta, dtype=np.float64)
+    lib().og_vic_redistribute_partial(w.shape[1], ptr(w), ptr(out), ptr(vol),
+                                      ptr(delta))
+    return out
 
 
 def ptr(a: np.ndarray):

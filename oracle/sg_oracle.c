@@ -1568,7 +1568,7 @@ void og_stage(const og_block* b, double* u, double* u0, double dt, int stage) {
    * (hydro_forward.cpp:1153-1168); its posts enter T_1, whose wall faces
    * are prescribed again after it (hydro_forward.cpp:1195-1196) */
   double* vq = NULL;
-  if (b->implicit_scheme == 9) {
+  if (b->implicit_scheme == 9 || b->implicit_scheme == 1) {
     og_block bq = *b;
     if (ns > 0) bq.vic_q = vq = (double*)calloc(nc, sizeof(double));
     og_implicit_reg(&bq, w, wt[2] * dt, du, T[0], dt);

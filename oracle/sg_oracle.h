@@ -46,7 +46,8 @@ typedef struct og_block {
   double nu_iso;       /* forcing/diffusion/nu_iso (kinematic viscosity) */
   int flux_cov;        /* dynamics/flux-covariance */
   int wb_wall_clamp;   /* dynamics/wb-wall-clamp */
-  int implicit_scheme; /* integration/implicit-scheme: 0 off, 9 full 5x5 */
+  int implicit_scheme; /* integration/implicit-scheme: 0 off, 9 full 5x5,
+                          1 partial 3x3 */
   double cfl;          /* integration/cfl (the implicit x1 time-step rule) */
   /* geometry of the padded block: x1f[nc1 + 1], x1v[nc1] (the reference's
    * linspace faces), x2v[nc2] */
@@ -101,7 +102,8 @@ void og_stage(const og_block* b, double* u, double* u0, double dt, int stage);
 /* the hydro tendency of one stage (HydroImpl::forward): du on every cell
  * (zero outside the interior), from the primitives w */
 void og_tendency(const og_block* b, const double* w, double dt, double* du);
-/* the vertical implicit correction (scheme 9) of every interior column:
+/* the vertical implicit correction (scheme 9, or 1: the partial matrix) of
+ * every interior column:
  * du (the explicit tendency, gravity work included) is replaced by the
  * corrected one; dtc = wght2 dt.  Returns the number of failed columns
  * (their du is left as it came in) */
@@ -110,6 +112,11 @@ int og_implicit(const og_block* b, const double* w, double dtc, double* du);
  * t1 (5, nc3, nc2, nc1) with the step's dt (null t1: none) */
 int og_implicit_reg(const og_block* b, const double* w, double dtc, double* du,
                     double* t1, double dt);
+/* the partial matrix's redistribution of one column alone (constituent
+ * column, tangential momenta, per-cell map): n layers, w and du 5 x n,
+ * vol[n], delta n x 3 (total mass, m1, E) */
+void og_vic_redistribute_partial(int n, const double* w, double* du,
+                                 const double* vol, const double* delta);
 /* the well-balanced x1 reference of one column (w strided by `plane`):
  * psf_lo, psf_hi, pref, dsf, dref [nc1] and dsf_lr [2][nc1] */
 void og_ref_column(const og_block* b, const double* w, size_t plane,

@@ -1,8 +1,14 @@
 /*
  * CPU oracle, part 2: the vertical implicit correction (VIC) -- TEST
- * INFRASTRUCTURE ONLY.  FP64 restatement of the reference's full 5x5
- * block-tridiagonal column solve (implicit-scheme 9) on a Cartesian block
- * without solids or species:
+ * INFRASTRUCTURE ONLY.  FP64 restatement of the reference's block-
+ * tridiagonal column solve on a Cartesian block without solids or species:
+ * the full 5x5 blocks (implicit-scheme 9) and the partial 3x3 blocks of rows
+ * and columns {rho, m1, E} (implicit-scheme 1: the tangential momenta folded
+ * into the density column and the right-hand side, src/implicit/
+ * vic_assemble_impl.h:152-214; the 3x3 forward sweep by the explicit inverse,
+ * forward_sweep_impl.h:110-124; the donor transfer of the tangential momenta,
+ * vic_redistribute_impl.h:178-200; their face posts,
+ * implicit_hydro.cpp:520-530,662-666):
  *   src/implicit/implicit_hydro.cpp:301-560  ImplicitHydroImpl::forward_masked
  *   src/implicit/vic_assemble_impl.h:45-214  the blocks a, b, c of a cell
  *   src/implicit/flux_decomposition_impl.h   Roe average, eigenvectors, flux
@@ -187,6 +193,109 @@ static void lubksb5(M5 a, const int* indx, double b[5][8], int m) {
   }
 }
 
+/* ludcmp<double, 3, Implicit = true> (src/math/ludcmp.h): the partial
+ * matrix's sweep runs it only as the singularity screen */
+static int ludcmp3(double a[3][3]) {
+  int i, imax = 0, j, k, d;
+  double big, dum, sum, temp, vv[3], scale[3];
+  const double tolerance = 8. * 3 * 2.220446049250313e-16;
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c)
+      if (!isfinite(a[r][c])) return 0;
+  d = 1;
+  for (i = 0; i < 3; i++) {
+    big = 0.0;
+    for (j = 0; j < 3; j++)
+      if ((temp = fabs(a[i][j])) > big) big = temp;
+    if (big == 0.0) return 0;
+    scale[i] = big;
+    vv[i] = 1.0 / big;
+    if (!isfinite(vv[i])) return 0;
+  }
+  for (j = 0; j < 3; j++) {
+    for (i = 0; i < j; i++) {
+      sum = a[i][j];
+      for (k = 0; k < i; k++) sum -= a[i][k] * a[k][j];
+      if (!isfinite(sum)) return 0;
+      a[i][j] = sum;
+    }
+    big = 0.0;
+    for (i = j; i < 3; i++) {
+      sum = a[i][j];
+      for (k = 0; k < j; k++) sum -= a[i][k] * a[k][j];
+      if (!isfinite(sum)) return 0;
+      a[i][j] = sum;
+      dum = vv[i] * fabs(sum);
+      if (!isfinite(dum)) return 0;
+      if (dum >= big) {
+        big = dum;
+        imax = i;
+      }
+    }
+    if (j != imax) {
+      for (k = 0; k < 3; k++) {
+        dum = a[imax][k];
+        a[imax][k] = a[j][k];
+        a[j][k] = dum;
+      }
+      d = -d;
+      vv[imax] = vv[j];
+      temp = scale[imax];
+      scale[imax] = scale[j];
+      scale[j] = temp;
+    }
+    if (fabs(a[j][j]) / scale[j] <= tolerance) return 0;
+    if (j != 2) {
+      dum = (1.0 / a[j][j]);
+      for (i = j + 1; i < 3; i++) a[i][j] *= dum;
+    }
+  }
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c)
+      if (!isfinite(a[r][c])) return 0;
+  return d;
+}
+
+/* the inverse of a 3x3 block: the adjugate over the determinant, expanded
+ * along column 0 (the reference inverts the block with Eigen's fixed-size
+ * inverse, also a cofactor form; its order of operations is not restated) */
+static void inverse3(double inv[3][3], double a[3][3]) {
+  double c00 = a[1][1] * a[2][2] - a[1][2] * a[2][1];
+  double c10 = a[0][2] * a[2][1] - a[0][1] * a[2][2];
+  double c20 = a[0][1] * a[1][2] - a[0][2] * a[1][1];
+  double det = a[0][0] * c00 + a[1][0] * c10 + a[2][0] * c20;
+  double r = 1. / det;
+  inv[0][0] = c00 * r;
+  inv[0][1] = c10 * r;
+  inv[0][2] = c20 * r;
+  inv[1][0] = (a[1][2] * a[2][0] - a[1][0] * a[2][2]) * r;
+  inv[1][1] = (a[0][0] * a[2][2] - a[0][2] * a[2][0]) * r;
+  inv[1][2] = (a[0][2] * a[1][0] - a[0][0] * a[1][2]) * r;
+  inv[2][0] = (a[1][0] * a[2][1] - a[1][1] * a[2][0]) * r;
+  inv[2][1] = (a[0][1] * a[2][0] - a[0][0] * a[2][1]) * r;
+  inv[2][2] = (a[0][0] * a[1][1] - a[0][1] * a[1][0]) * r;
+}
+
+static void mat3_mul(double out[3][3], double a[3][3], double b[3][3]) {
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) {
+      double s = a[r][0] * b[0][c];
+      for (int k = 1; k < 3; ++k) s += a[r][k] * b[k][c];
+      out[r][c] = s;
+    }
+}
+
+static void mat3_vec(double out[3], double a[3][3], const double* v) {
+  for (int r = 0; r < 3; ++r) {
+    double s = a[r][0] * v[0];
+    for (int k = 1; k < 3; ++k) s += a[r][k] * v[k];
+    out[r] = s;
+  }
+}
+
+/* the rows and columns {rho, m1, E} of the partial matrix */
+static const int kRows3[3] = {0, 1, 4};
+
 /* the corrected-PE slope stencil of n cells at centres x (gravity_work.hpp
  * :93-115): weights wt[3][n], first index i0[n] */
 static void slope_stencil(const double* x, int n, double* wt0, double* wt1,
@@ -211,6 +320,95 @@ static void slope_stencil(const double* x, int n, double* wt0, double* wt1,
     int jj = k < 1 ? 1 : (k > n - 2 ? n - 2 : k);
     i0[k] = jj - 1;
   }
+}
+
+/* the redistribution of a solved column: vic_constituent_column (no
+ * species: the per-cell total-mass increments phi, the zero-sum face
+ * transfers M by prefix sum, the donor-upwinded dry transfer q with the
+ * sequential availability clamp), for the partial matrix
+ * vic_tangential_momentum_column (each face's moved total mass carries the
+ * donor cell's tangential velocity), then vic_redistribute_cell
+ * (src/implicit/vic_redistribute_impl.h:60-232).  w, du: 5 rows with row
+ * stride st; dl: the solution per layer (rows 0-4; the partial matrix's
+ * tangential rows hold the explicit du); vol per layer.  mf_dn[n] zeroed,
+ * mf_M[n + 1] and mf_q[n + 1] zeroed on entry. */
+static void redistribute_column(int n, const double* w, size_t st, double* du,
+                                V5* dl, const double* vol, int partial,
+                                double* mf_dn, double* mf_M, double* mf_q) {
+#define WV(v, i) w[(size_t)(v) * st + (i)]
+#define DU(v, i) du[(size_t)(v) * st + (i)]
+  double* phi = calloc(n, sizeof(double));
+  double R = 0, S = 0;
+  for (int i = 0; i < n; ++i) {
+    double explicit_total = DU(0, i);
+    phi[i] = (dl[i][0] - explicit_total) * vol[i];
+    R += phi[i];
+    S += WV(0, i) * vol[i];
+  }
+  double M = 0;
+  for (int i = 0; i < n; ++i) {
+    mf_M[i] = M;
+    M -= phi[i] - R * (WV(0, i) * vol[i] / S);
+  }
+  double avail = (WV(0, 0) * 1. + DU(0, 0)) * vol[0];
+  if (avail < 0) avail = 0;
+  for (int i = 0; i + 1 < n; ++i) {
+    double avail_up = (WV(0, i + 1) * 1. + DU(0, i + 1)) * vol[i + 1];
+    if (avail_up < 0) avail_up = 0;
+    double Mf = mf_M[i + 1];
+    double q = Mf > 0 ? Mf * 1. : Mf * 1.;
+    if (q > avail) q = avail;
+    if (q < -avail_up) q = -avail_up;
+    mf_dn[i] -= q / vol[i];
+    mf_dn[i + 1] += q / vol[i + 1];
+    mf_q[i + 1] = q;
+    avail = avail_up + q;
+  }
+  for (int i = 0; i < n; ++i) {
+    DU(0, i) += mf_dn[i];
+    DU(1, i) = dl[i][1];
+    DU(2, i) = dl[i][2];
+    DU(3, i) = dl[i][3];
+    DU(4, i) = dl[i][4];
+  }
+  if (partial)
+    for (int i = 0; i + 1 < n; ++i) {
+      double q = mf_q[i + 1];
+      int donor = q > 0 ? i : i + 1;
+      for (int t = 2; t < 4; ++t) {
+        double pm = q * WV(t, donor);
+        if (pm == 0) continue;
+        DU(t, i) -= pm / vol[i];
+        DU(t, i + 1) += pm / vol[i + 1];
+      }
+    }
+  free(phi);
+#undef WV
+#undef DU
+}
+
+/* the redistribution alone, for the reference's own known-answer property
+ * of the partial matrix (tests/test_backward_substitution.cpp:308-365):
+ * n layers, w and du 5 x n (row stride n), vol[n], delta n x 3 (the 3x3
+ * solution: total mass, m1, E) */
+void og_vic_redistribute_partial(int n, const double* w, double* du,
+                                 const double* vol, const double* delta) {
+  V5* dl = malloc(sizeof(V5) * n);
+  for (int i = 0; i < n; ++i) {
+    dl[i][0] = delta[3 * i];
+    dl[i][1] = delta[3 * i + 1];
+    dl[i][2] = du[2 * (size_t)n + i];
+    dl[i][3] = du[3 * (size_t)n + i];
+    dl[i][4] = delta[3 * i + 2];
+  }
+  double* mf_dn = calloc(n, sizeof(double));
+  double* mf_M = calloc(n + 1, sizeof(double));
+  double* mf_q = calloc(n + 1, sizeof(double));
+  redistribute_column(n, w, n, du, dl, vol, 1, mf_dn, mf_M, mf_q);
+  free(dl);
+  free(mf_dn);
+  free(mf_M);
+  free(mf_q);
 }
 
 /* one column: n interior layers; w, du (5 rows each) with row stride `st`
@@ -239,6 +437,17 @@ static int vic_column(const og_block* b, const double* w, size_t st, double* du,
   double *wt0 = malloc(sizeof(double) * n), *wt1 = malloc(sizeof(double) * n),
          *wt2 = malloc(sizeof(double) * n);
   int* i0 = malloc(sizeof(int) * n);
+  /* the partial matrix (implicit-scheme 1: bit 3 of the scheme clear) */
+  const int partial = !((b->implicit_scheme >> 3) & 1);
+  typedef double M3[3][3];
+  typedef double V3[3];
+  M3* A3 = partial ? (M3*)malloc(sizeof(M3) * n) : NULL;
+  M3* B3 = partial ? (M3*)malloc(sizeof(M3) * n) : NULL;
+  M3* C3 = partial ? (M3*)malloc(sizeof(M3) * n) : NULL;
+  V3* rc = partial ? (V3*)calloc(n, sizeof(V3)) : NULL; /* rhs_corr */
+  V3* d3 = partial ? (V3*)malloc(sizeof(V3) * n) : NULL;
+  V3* y0 = partial ? (V3*)malloc(sizeof(V3) * n) : NULL;
+  V3* y1 = partial ? (V3*)malloc(sizeof(V3) * n) : NULL;
   int ok = 1;
 #define WV(v, i) w[(size_t)(v) * st + (i)]
 #define DU(v, i) du[(size_t)(v) * st + (i)]
@@ -290,6 +499,45 @@ static int vic_column(const og_block* b, const double* w, size_t st, double* du,
     if (i == n - 1)
       for (int r = 0; r < 5; ++r)
         for (int c = 0; c < 5; ++c) A[i][r][c] += C[i][r][c] * bnd[c];
+    if (partial) {
+      /* the 3x3 blocks are the {rho, m1, E} rows and columns of the same
+       * entries (each entry is the same expression); the m_t columns of
+       * those rows (aT, bT, cT: columns IVY, IVZ with the same terms, the
+       * energy row's face work and the wall mirror included) fold into the
+       * density column at the cell's v_t and into the right-hand side at the
+       * frozen remainder q_t = du[m_t] - v_t du[rho]
+       * (vic_assemble_impl.h:167-213) */
+      double aT[3][2], bT[3][2], cT[3][2];
+      for (int r = 0; r < 3; ++r) {
+        for (int c = 0; c < 3; ++c) {
+          A3[i][r][c] = A[i][kRows3[r]][kRows3[c]];
+          B3[i][r][c] = B[i][kRows3[r]][kRows3[c]];
+          C3[i][r][c] = C[i][kRows3[r]][kRows3[c]];
+        }
+        for (int k = 0; k < 2; ++k) {
+          aT[r][k] = A[i][kRows3[r]][2 + k];
+          bT[r][k] = B[i][kRows3[r]][2 + k];
+          cT[r][k] = C[i][kRows3[r]][2 + k];
+        }
+      }
+      for (int r = 0; r < 3; ++r) rc[i][r] = 0.;
+      for (int side = 0; side < 3; ++side) {
+        int j = side == 0 ? i : (side == 1 ? i - 1 : i + 1);
+        if (side == 1 && i == 0) continue;     /* merged lower wall */
+        if (side == 2 && i == n - 1) continue; /* merged upper wall */
+        double(*blk)[3] = side == 0 ? A3[i] : (side == 1 ? B3[i] : C3[i]);
+        double(*tb)[2] = side == 0 ? aT : (side == 1 ? bT : cT);
+        double drho = DU(0, j);
+        for (int k = 0; k < 2; ++k) {
+          double v = WV(2 + k, j);
+          double q = DU(2 + k, j) - v * drho;
+          if (v != 0)
+            for (int r = 0; r < 3; ++r) blk[r][0] = blk[r][0] + tb[r][k] * v;
+          if (q != 0)
+            for (int r = 0; r < 3; ++r) rc[i][r] = rc[i][r] + tb[r][k] * q;
+        }
+      }
+    }
   }
   /* (2) couple_radial_exact: the corrected-PE rows K in the (IPR, IDN)
    * entry of the blocks, and the explicit part moved to the right side */
@@ -312,6 +560,12 @@ static int vic_column(const og_block* b, const double* w, size_t st, double* du,
     kt0 = gv[0] * wt2[0];
     kt1 = gv[n - 1] * wt0[n - 1];
     for (int i = 0; i < n; ++i) {
+      if (partial) {
+        A3[i][2][0] -= kmid[i] / dtc;
+        B3[i][2][0] -= klo[i] / dtc;
+        C3[i][2][0] -= khi[i] / dtc;
+        continue;
+      }
       A[i][4][0] -= kmid[i] / dtc;
       B[i][4][0] -= klo[i] / dtc;
       C[i][4][0] -= khi[i] / dtc;
@@ -326,8 +580,111 @@ static int vic_column(const og_block* b, const double* w, size_t st, double* du,
     for (int i = 0; i < n; ++i) DU(4, i) -= s[i];
     free(s);
   }
+  /* (3p) the partial matrix's forward sweep (ForwardSweep, N = 3): the
+   * right-hand side less the assembly's m_t term, the block inverted
+   * explicitly after the LU screen; then back substitution and Woodbury on
+   * the 3-vectors.  The solution goes to dl rows 0, 1, 4; the tangential
+   * rows keep the explicit du */
+  for (int i = 0; i < n && ok && partial; ++i) {
+    double rhs[3] = {DU(0, i) / dtc, DU(1, i) / dtc, DU(4, i) / dtc};
+    for (int r = 0; r < 3; ++r)
+      if (rc[i][r] != 0) rhs[r] -= rc[i][r];
+    if (i > 0) {
+      M3 t;
+      mat3_mul(t, B3[i], A3[i - 1]);
+      for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) A3[i][r][c] -= t[r][c];
+    }
+    M3 LU, inv;
+    memcpy(LU, A3[i], sizeof(M3));
+    if (ludcmp3(LU) == 0) {
+      ok = 0;
+      break;
+    }
+    inverse3(inv, A3[i]);
+    double t[3], u[3];
+    if (i > 0) {
+      mat3_vec(u, B3[i], d3[i - 1]);
+      for (int r = 0; r < 3; ++r) t[r] = rhs[r] - u[r];
+    } else {
+      for (int r = 0; r < 3; ++r) t[r] = rhs[r];
+    }
+    mat3_vec(d3[i], inv, t);
+    if (wood) {
+      double e0[3] = {0, 0, i == 0 ? 1. : 0.}, e1[3] = {0, 0, i == n - 1 ? 1. : 0.};
+      if (i > 0) {
+        mat3_vec(u, B3[i], y0[i - 1]);
+        for (int r = 0; r < 3; ++r) t[r] = e0[r] - u[r];
+      } else {
+        for (int r = 0; r < 3; ++r) t[r] = e0[r];
+      }
+      mat3_vec(y0[i], inv, t);
+      if (i > 0) {
+        mat3_vec(u, B3[i], y1[i - 1]);
+        for (int r = 0; r < 3; ++r) t[r] = e1[r] - u[r];
+      } else {
+        for (int r = 0; r < 3; ++r) t[r] = e1[r];
+      }
+      mat3_vec(y1[i], inv, t);
+    }
+    M3 ap;
+    mat3_mul(ap, inv, C3[i]);
+    memcpy(A3[i], ap, sizeof(M3));
+    for (int r = 0; r < 3; ++r) {
+      if (!isfinite(d3[i][r])) ok = 0;
+      for (int c = 0; c < 3; ++c)
+        if (!isfinite(A3[i][r][c])) ok = 0;
+    }
+  }
+  if (ok && partial) {
+    /* vic_backward_substitute: each vector only if its first layer is
+     * finite */
+    int f0 = 1, f1 = 1;
+    for (int r = 0; r < 3 && wood; ++r) {
+      if (!isfinite(y0[0][r])) f0 = 0;
+      if (!isfinite(y1[0][r])) f1 = 0;
+    }
+    for (int i = n - 2; i >= 0; --i) {
+      double t[3];
+      mat3_vec(t, A3[i], d3[i + 1]);
+      for (int r = 0; r < 3; ++r) d3[i][r] -= t[r];
+      if (wood && f0) {
+        mat3_vec(t, A3[i], y0[i + 1]);
+        for (int r = 0; r < 3; ++r) y0[i][r] -= t[r];
+      }
+      if (wood && f1) {
+        mat3_vec(t, A3[i], y1[i + 1]);
+        for (int r = 0; r < 3; ++r) y1[i][r] -= t[r];
+      }
+    }
+    if (wood) {
+      double k0 = -kt0 / dtc, k1 = -kt1 / dtc;
+      k0 = k0 * 1.;
+      k1 = k1 * 1.;
+      int a0 = 2, a1 = n - 3;
+      double m00 = 1. + k0 * y0[a0][0], m01 = k0 * y1[a0][0];
+      double m10 = k1 * y0[a1][0], m11 = 1. + k1 * y1[a1][0];
+      double r0 = k0 * d3[a0][0], r1 = k1 * d3[a1][0];
+      double det = m00 * m11 - m01 * m10;
+      double al0 = (m11 * r0 - m01 * r1) / det, al1 = (m00 * r1 - m10 * r0) / det;
+      for (int i = 0; i < n; ++i)
+        for (int r = 0; r < 3; ++r) {
+          d3[i][r] -= y0[i][r] * al0;
+          d3[i][r] -= y1[i][r] * al1;
+        }
+    }
+    for (int i = 0; i < n; ++i) {
+      dl[i][0] = d3[i][0];
+      dl[i][1] = d3[i][1];
+      dl[i][2] = DU(2, i);
+      dl[i][3] = DU(3, i);
+      dl[i][4] = d3[i][2];
+      for (int r = 0; r < 3; ++r)
+        if (!isfinite(d3[i][r])) ok = 0;
+    }
+  }
   /* (3) forward sweep (ForwardSweep<K = 2>, N = 5) */
-  for (int i = 0; i < n && ok; ++i) {
+  for (int i = 0; i < n && ok && !partial; ++i) {
     double rhs[5] = {DU(0, i) / dtc, DU(1, i) / dtc, DU(2, i) / dtc,
                      DU(3, i) / dtc, DU(4, i) / dtc};
     if (i > 0) {
@@ -380,7 +737,7 @@ static int vic_column(const og_block* b, const double* w, size_t st, double* du,
       }
     }
   }
-  if (ok) {
+  if (ok && !partial) {
     /* (4) back substitution */
     for (int i = n - 2; i >= 0; --i) {
       V5 t;
@@ -420,40 +777,10 @@ static int vic_column(const og_block* b, const double* w, size_t st, double* du,
     double* mf_dn = calloc(n, sizeof(double));   /* MASS(IDN) */
     double* mf_M = calloc(n + 1, sizeof(double)); /* MASS(IVX): face below i */
     double* mf_q = calloc(n + 1, sizeof(double)); /* MASS(IVZ): moved total */
-    double* phi = calloc(n, sizeof(double));
-    double R = 0, S = 0;
-    for (int i = 0; i < n; ++i) {
-      double explicit_total = DU(0, i);
-      phi[i] = (dl[i][0] - explicit_total) * vol;
-      R += phi[i];
-      S += WV(0, i) * vol;
-    }
-    double M = 0;
-    for (int i = 0; i < n; ++i) {
-      mf_M[i] = M;
-      M -= phi[i] - R * (WV(0, i) * vol / S);
-    }
-    double avail = (WV(0, 0) * 1. + DU(0, 0)) * vol;
-    if (avail < 0) avail = 0;
-    for (int i = 0; i + 1 < n; ++i) {
-      double avail_up = (WV(0, i + 1) * 1. + DU(0, i + 1)) * vol;
-      if (avail_up < 0) avail_up = 0;
-      double Mf = mf_M[i + 1];
-      double q = Mf > 0 ? Mf * 1. : Mf * 1.;
-      if (q > avail) q = avail;
-      if (q < -avail_up) q = -avail_up;
-      mf_dn[i] -= q / vol;
-      mf_dn[i + 1] += q / vol;
-      mf_q[i + 1] = q;
-      avail = avail_up + q;
-    }
-    for (int i = 0; i < n; ++i) {
-      DU(0, i) += mf_dn[i];
-      DU(1, i) = dl[i][1];
-      DU(2, i) = dl[i][2];
-      DU(3, i) = dl[i][3];
-      DU(4, i) = dl[i][4];
-    }
+    double* vols = malloc(sizeof(double) * n);
+    for (int i = 0; i < n; ++i) vols[i] = vol;
+    redistribute_column(n, w, st, du, dl, vols, partial, mf_dn, mf_M, mf_q);
+    free(vols);
     /* (7) book_remainder_: projection and clamp work, then the corrected-PE
      * remainder g1 sigma^2 s[du - du0] beyond what the matrix booked */
     for (int i = 0; i < n; ++i) {
@@ -494,8 +821,15 @@ static int vic_column(const og_block* b, const double* w, size_t st, double* du,
        * wall, top face included, over dt A, rows IVY and IVZ */
       for (int f = 0; f <= n; ++f)
         t1[OG_IDN * st + f] = t1[OG_IDN * st + f] + mf_q[f] / kdt;
+      /* partial matrix: "vic.momentum_t" is the donor transfer q w_t */
+      for (int f = 0; f <= n && partial; ++f) {
+        double q = mf_q[f];
+        int donor = q > 0. ? f - 1 : f;
+        t1[OG_IVY * st + f] = t1[OG_IVY * st + f] + q * WV(2, donor) / kdt;
+        t1[OG_IVZ * st + f] = t1[OG_IVZ * st + f] + q * WV(3, donor) / kdt;
+      }
       double sy = 0., sz = 0.;
-      for (int f = 0; f <= n; ++f) {
+      for (int f = 0; f <= n && !partial; ++f) {
         double py = 0., pz = 0.;
         if (f > 0) {
           sy = sy + (dl[f - 1][2] - du0[2 * n + f - 1]) * vol;
@@ -512,7 +846,6 @@ static int vic_column(const og_block* b, const double* w, size_t st, double* du,
     free(mf_dn);
     free(mf_M);
     free(mf_q);
-    free(phi);
   }
   if (!ok) /* a failed column keeps the explicit tendency */
     for (int v = 0; v < 5; ++v)
@@ -522,6 +855,7 @@ static int vic_column(const og_block* b, const double* w, size_t st, double* du,
   free(A); free(B); free(C); free(dl); free(z0); free(z1); free(du0);
   free(kmid); free(klo); free(khi); free(gv); free(wt0); free(wt1); free(wt2);
   free(i0);
+  free(A3); free(B3); free(C3); free(rc); free(d3); free(y0); free(y1);
   return ok ? 0 : 1;
 }
 

@@ -224,6 +224,7 @@ struct sg_handle {
   int wide = 0;  // enough columns for a thread per column in the finish
   int wide_auto = 0;  // that rule's own answer (finish form 0)
   bool implicit = false;
+  int vic_kinds = 0;  // bit 0: a block with the full 5x5 matrix, bit 1: 3x3
   int refine = 0;  // corrections of the refined implicit solve (0: direct)
   int any_f32 = 0;  // a block assembles its implicit blocks in FP32
   size_t max_icells = 0, max_icols = 0;
@@ -429,6 +430,7 @@ int sg_autotune(sg_handle* h, int32_t reps, int32_t* tj_out,
     p.fallbacks = h->fallbacks;
     p.max_nc1 = h->max_nc1;
     p.visc3 = h->visc3;
+    p.vic_kinds = h->vic_kinds;
     auto stage = [&]() -> int {
       p.ntile = h->ntile;
       int r = 0;
@@ -598,11 +600,19 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
     B.implicit = d.implicit_scheme;
     B.vic = nullptr;
     if (d.implicit_scheme != 0) {
-      if (d.implicit_scheme != 9) {
+      if (d.implicit_scheme != 9 && d.implicit_scheme != 1) {
         sg_destroy(h);
         return fail(SG_ERR_UNSUPPORTED, "block %d: implicit-scheme %d (the "
-                    "full 5x5 scheme 9 is built)", b, d.implicit_scheme);
+                    "full 5x5 scheme 9 and the partial 3x3 scheme 1 are "
+                    "built)", b, d.implicit_scheme);
       }
+      if (d.implicit_scheme == 1 && d.implicit_precision == SG_F32) {
+        sg_destroy(h);
+        return fail(SG_ERR_UNSUPPORTED, "block %d: implicit-scheme 1 "
+                    "assembles its blocks in FP64 (implicit-precision "
+                    "float32 is built for scheme 9)", b);
+      }
+      h->vic_kinds |= d.implicit_scheme == 9 ? 1 : 2;
       if (d.grav1 == 0. || d.bc[0] != SG_BC_REFLECTING ||
           d.bc[1] != SG_BC_REFLECTING || d.nc1 - 2 * d.ng < 3) {
         sg_destroy(h);
@@ -1077,6 +1087,7 @@ int sg_stage(sg_handle* h, int32_t stage, const double* dt_dev,
   p.fallbacks = h->fallbacks;
   p.max_nc1 = h->max_nc1;
   p.visc3 = h->visc3;
+  p.vic_kinds = h->vic_kinds;
   // events between the launches when timing is on and the stream is not
   // being captured: ev[0] (x3 ev[6]) stage ev[1] (assemble ev[2] solve
   // ev[3] finish ev[4]) (scalars ev[7]) ghost ev[5]
@@ -1122,7 +1133,8 @@ int sg_stage(sg_handle* h, int32_t stage, const double* dt_dev,
     if (timed) cudaEventRecord(ev[4], s);
     // assembly, solve, finish; the refined solve adds its FP32 sweep and a
     // residual and a correction per correction
-    launches += 3 + (h->refine ? 1 + 2 * h->refine : 0);
+    launches += 3 + (h->vic_kinds == 3 ? 1 : 0) +
+                (h->refine ? 1 + 2 * h->refine : 0);
   }
   if (h->scalars) {
     // the passive scalars on the stage's mass flux: face fluxes, update

@@ -20,6 +20,32 @@ namespace sg {
 
 enum { IDN = 0, IVX = 1, IVY = 2, IVZ = 3, IPR = 4, NHYDRO = 5 };
 
+// a float widened to the double of the same value with integer operations
+// only: the FP64 kernels here are bound by the FP64 pipe, which the widening
+// instruction would also occupy.  Normal numbers rebias the exponent (127 ->
+// 1023) and shift the mantissa up 29 bits; zeros keep their sign; a
+// subnormal m 2^-149 is renormalised at its leading bit; infinities and NaNs
+// keep their payload (the quiet bit lands on the double's)
+__device__ __forceinline__ unsigned long long widen_bits(unsigned int b) {
+  const unsigned long long sgn = (unsigned long long)(b >> 31) << 63;
+  const unsigned int e = (b >> 23) & 0xffu;
+  const unsigned long long m = b & 0x7fffffu;
+  if (e == 0xffu) return sgn | (0x7ffull << 52) | (m << 29);
+  if (e != 0u) return sgn | ((unsigned long long)(e + 896u) << 52) | (m << 29);
+  if (m == 0u) return sgn;
+  const int k = 31 - __clz((int)m);  // the leading bit, 0..22
+  return sgn | ((unsigned long long)(k + 874) << 52) |
+         ((m << (52 - k)) & 0xfffffffffffffull);
+}
+
+__device__ __forceinline__ double widen_exact(float f) {
+  return __longlong_as_double((long long)widen_bits(__float_as_uint(f)));
+}
+
+// a value of the storage type in FP64 (a float through the integer pipes)
+__device__ __forceinline__ double as_f64(double x) { return x; }
+__device__ __forceinline__ double as_f64(float x) { return widen_exact(x); }
+
 template <typename T>
 __device__ __forceinline__ T sqr(T x) {
   return x * x;

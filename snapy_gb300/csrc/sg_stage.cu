@@ -199,7 +199,7 @@ struct TileLayout {
 // where the column holds anomalies (pb non-null)
 __device__ __forceinline__ double col_p(const real* pres, const double* pb,
                                         int j) {
-  return pb ? (double)pres[j] + pb[j] : (double)pres[j];
+  return pb ? as_f64(pres[j]) + pb[j] : as_f64(pres[j]);
 }
 
 #ifndef SG_REAL_IS_FLOAT
@@ -208,11 +208,11 @@ __device__ __forceinline__ void ref_scan(const real* rho, const real* pres,
                                          double dx, double grav,
                                          double* psf_lo, double* psf_hi) {
   const double minp = 2.2250738585072014e-308;
-  double rdt_top = col_p(pres, pb, iu) / (double)rho[iu];
+  double rdt_top = col_p(pres, pb, iu) / as_f64(rho[iu]);
   double top = col_p(pres, pb, iu) * sg_exp(-grav * 0.5 * dx / rdt_top);
   double face = top;
   for (int i = iu; i >= 0; --i) {
-    double dp = grav * (double)rho[i] * dx;
+    double dp = grav * as_f64(rho[i]) * dx;
     double lo = face + dp, hi = face;
     psf_lo[i] = lo > minp ? lo : minp;
     psf_hi[i] = hi > minp ? hi : minp;
@@ -220,7 +220,7 @@ __device__ __forceinline__ void ref_scan(const real* rho, const real* pres,
   }
   face = top;
   for (int i = iu + 1; i < nc1; ++i) {
-    double dp = grav * (double)rho[i] * dx;
+    double dp = grav * as_f64(rho[i]) * dx;
     double lo = face, hi = lo - dp;
     psf_lo[i] = lo > minp ? lo : minp;
     psf_hi[i] = hi > minp ? hi : minp;
@@ -243,12 +243,12 @@ __device__ __forceinline__ void ref_scan_warp(const real* rho, const real* pres,
   const int lane = threadIdx.x & 31;
   const double minp = 2.2250738585072014e-308;
   const double ptop = col_p(pres, pb, iu);
-  const double rdt_top = ptop / (double)rho[iu];
+  const double rdt_top = ptop / as_f64(rho[iu]);
   const double top = ptop * sg_exp(-grav * 0.5 * dx / rdt_top);
   double carry = 0.;
   for (int c0 = iu; c0 >= 0; c0 -= 32) {
     const int i = c0 - lane;
-    double v = i >= 0 ? grav * (double)rho[i] * dx : 0.;
+    double v = i >= 0 ? grav * as_f64(rho[i]) * dx : 0.;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
       double t = __shfl_up_sync(full, v, d);
@@ -267,7 +267,7 @@ __device__ __forceinline__ void ref_scan_warp(const real* rho, const real* pres,
   carry = 0.;
   for (int c0 = iu + 1; c0 < nc1; c0 += 32) {
     const int i = c0 + lane;
-    double v = i < nc1 ? grav * (double)rho[i] * dx : 0.;
+    double v = i < nc1 ? grav * as_f64(rho[i]) * dx : 0.;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
       double t = __shfl_up_sync(full, v, d);
@@ -509,7 +509,7 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
       const int jt = idx / nc1, i = idx - jt * nc1;
       const real* rho = W + IDN * wstride + (hj + jt) * nc1;
       const real* pres = W + IPR * wstride + (hj + jt) * nc1;
-      REF[6 * rs_ + idx] = (double)rho[i] / col_p(pres, pbc, i);
+      REF[6 * rs_ + idx] = as_f64(rho[i]) / col_p(pres, pbc, i);
     }
     __syncthreads();
     for (int idx = threadIdx.x; idx < ntj * nc1; idx += blockDim.x) {
@@ -556,7 +556,7 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
       const real* rho = W + IDN * wstride + (hj + jt) * nc1;
       const real* pres = W + IPR * wstride + (hj + jt) * nc1;
       PP[idx] = real(col_p(pres, pbc, f) - REF[2 * rs_ + idx]);
-      PD[idx] = real((double)rho[f] - REF[3 * rs_ + idx]);
+      PD[idx] = real(as_f64(rho[f]) - REF[3 * rs_ + idx]);
     }
     __syncthreads();
   }
@@ -599,13 +599,13 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
       // the totals in FP64; the Riemann solve takes the anomaly about the
       // base face pressure where there is a base
       const double psf = REF[0 * rs_ + jt * nc1 + f];
-      double pl = (double)wl[IPR] + psf, pr = (double)wr[IPR] + psf;
+      double pl = as_f64(wl[IPR]) + psf, pr = as_f64(wr[IPR]) + psf;
       pl = pl > 0. ? pl : psf;
       pr = pr > 0. ? pr : psf;
       wl[IPR] = real(pbf ? pl - pbf[f] : pl);
       wr[IPR] = real(pbf ? pr - pbf[f] : pr);
-      real dl = real((double)wl[IDN] + REF[4 * rs_ + jt * nc1 + f]);
-      real dr = real((double)wr[IDN] + REF[5 * rs_ + jt * nc1 + f]);
+      real dl = real(as_f64(wl[IDN]) + REF[4 * rs_ + jt * nc1 + f]);
+      real dr = real(as_f64(wr[IDN]) + REF[5 * rs_ + jt * nc1 + f]);
       const real* rho = W + IDN * wstride + (hj + jt) * nc1;
       wl[IDN] = dl > real(0) ? dl : rho[f > 0 ? f - 1 : 0];
       wr[IDN] = dr > real(0) ? dr : rho[f];
@@ -825,7 +825,7 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
         const size_t c = koff + (size_t)(j0 + jt) * nc1 + f;
 #pragma unroll
         for (int v = 0; v < NHYDRO; ++v) {
-          double t = (double)F1[v * f1stride + idx];
+          double t = as_f64(F1[v * f1stride + idx]);
           if (pbf && v == IVX) t = t + pbf[f];
           if (B.implicit)
             B.t1[((size_t)v * ncols + col) * nf1 + fi] = t;
@@ -841,7 +841,7 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
         const size_t c = koff + (size_t)(j0 + jf) * nc1 + i;
 #pragma unroll
         for (int v = 0; v < NHYDRO; ++v) {
-          double t = (double)F2[v * f2stride + idx];
+          double t = as_f64(F2[v * f2stride + idx]);
           if (pbc && v == IVY) t = t + pbc[i];
           step_set(S2 + v * plane + c, t, w1s, w2dt, first);
         }
@@ -856,14 +856,14 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
     for (int idx = threadIdx.x; idx < ntj * nf1; idx += blockDim.x) {
       const int jt = idx / nf1, fi = idx - jt * nf1, f = il + fi;
       B.mflux[0][koff + (size_t)(j0 + jt) * nc1 + f] =
-          (double)F1[IDN * f1stride + idx];
+          as_f64(F1[IDN * f1stride + idx]);
     }
     if (has2) {
       for (int idx = threadIdx.x; idx < (ntj + 1) * nx1; idx += blockDim.x) {
         const int jf = idx / nx1, i = il + (idx - jf * nx1);
         if (jf == ntj && j0 + ntj != jend) continue;
         B.mflux[1][koff + (size_t)(j0 + jf) * nc1 + i] =
-            (double)F2[IDN * f2stride + idx];
+            as_f64(F2[IDN * f2stride + idx]);
       }
     }
   }
@@ -960,7 +960,7 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
       // tendency to it (interior cell (column, layer) of the VIC scratch)
       double* DU = B.vic;
 #pragma unroll
-      for (int v = 0; v < NHYDRO; ++v) DU[v * icells + vci] = (double)du[v];
+      for (int v = 0; v < NHYDRO; ++v) DU[v * icells + vci] = as_f64(du[v]);
       continue;
     }
 #pragma unroll
@@ -1652,7 +1652,7 @@ __global__ void __launch_bounds__(kThreads)
       }
       // passive scalars ride on the mass row (the step field's owner rule)
       if (B.nscalar > 0 && (f < k1 || k1 == ng + nx3))
-        B.mflux[2][(size_t)f * kst + col] = (double)flx[IDN];
+        B.mflux[2][(size_t)f * kst + col] = as_f64(flx[IDN]);
       // the x3 step field; a chunk owns its faces but the top one, which
       // the next chunk owns, except the block's last face
       if (B.step[2] && (f < k1 || k1 == ng + nx3)) {
@@ -1660,7 +1660,7 @@ __global__ void __launch_bounds__(kThreads)
         double* S3 = B.step[2] + (size_t)f * kst + col;
 #pragma unroll
         for (int v = 0; v < NHYDRO; ++v) {
-          double t = (double)flx[v];
+          double t = as_f64(flx[v]);
           if (pbc && v == IVZ) t = t + pbc[i];
           step_set(S3 + v * plane, t, p.w1, w2dt, p.first != 0);
         }
@@ -2200,15 +2200,21 @@ extern "C" int SG_NAME(sg_launch_vic)(const BlockDev* tab, StageParams p,
     const int gc = (int)((cw + kCorrWarps - 1) / kCorrWarps);
     vic_solve32_kernel<<<dim3(gs, p.nblock), 32, 0, stream>>>(tab, p);
     for (int k = 1; k <= p.refine; ++k) {
-      vic_residual_kernel<<<dim3(gr, p.nblock), kThreads, 0, stream>>>(tab, p);
+      vic_residual_kernel<<<dim3(gr, p.nblock), kThreads, 0, stream>>>(tab, p, k);
       vic_correct32_kernel<<<dim3(gc, p.nblock), 32 * kCorrWarps, 0, stream>>>(
           tab, p, k == p.refine);
     }
     e = cudaGetLastError();
     if (e != cudaSuccess) return (int)e;
   }
-  // the solve: kVicCols columns per single-warp CTA
-  vic_solve_kernel<<<dim3(gs, p.nblock), 32, 0, stream>>>(tab, p, status);
+  // the solve: the full matrix kVicCols columns per single-warp CTA, the
+  // partial one a thread per column
+  if (p.vic_kinds & 1)
+    vic_solve_kernel<<<dim3(gs, p.nblock), 32, 0, stream>>>(tab, p, status);
+  if (p.vic_kinds & 2) {
+    const int g3 = (int)((max_cols + kThreads - 1) / kThreads);
+    vic_solve3_kernel<<<dim3(g3, p.nblock), kThreads, 0, stream>>>(tab, p, status);
+  }
   e = cudaGetLastError();
   if (e != cudaSuccess) return (int)e;
   if (ev) cudaEventRecord(ev[1], stream);

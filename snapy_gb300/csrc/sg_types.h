@@ -43,7 +43,8 @@ struct BlockDev {
   const double* x1v;
   // the sources' time-step bound (the viscous dx^2 / (2 ndim nu)), or +inf
   double dt_src;
-  // the vertical implicit correction: scheme (0 off, 9 the full 5x5 blocks)
+  // the vertical implicit correction: scheme (0 off, 9 the full 5x5 blocks,
+  // 1 the partial 3x3 blocks of rows and columns {rho, m1, E})
   // and its FP64 scratch (kVicDoublesPerCell per interior cell), laid out
   // as in vic_scratch()
   int32_t implicit;
@@ -140,6 +141,9 @@ struct StageParams {
   int32_t smem_rows;    // x1 lines held in shared memory per tile
   int32_t max_nc1;
   int32_t visc3;        // some 3-D block has viscosity: visc3_kernel runs
+  int32_t vic_kinds;    // implicit blocks: bit 0 some with the full 5x5
+                        // matrix (scheme 9), bit 1 some with the partial
+                        // 3x3 one (scheme 1)
 };
 
 }  // namespace sg

@@ -198,7 +198,7 @@ __device__ __forceinline__ void vic_prim(const real* u, size_t plane,
                                          int nc1 = 0) {
   double uc[NHYDRO];
 #pragma unroll
-  for (int v = 0; v < NHYDRO; ++v) uc[v] = (double)u[v * plane + cell];
+  for (int v = 0; v < NHYDRO; ++v) uc[v] = as_f64(u[v * plane + cell]);
   if (base) {
     const int i = (int)(cell % nc1);
     uc[IDN] = base_rho(base, nc1)[i] + uc[IDN];
@@ -333,11 +333,63 @@ __device__ __forceinline__ void vic_assemble_cell(const BlockDev& B,
     du0[v] = S.du[v * S.cells + cell];
     S.du0[v * S.cells + cell] = du0[v];
   }
+  // the partial matrix (implicit-scheme 1; FP64 assembly only): its 3x3
+  // blocks are the {rho, m1, E} rows and columns of the same entries, and
+  // the m_t columns of those rows (the same terms, energy-row face work and
+  // wall mirror included) fold into the density column at the cell's v_t
+  // and into the right-hand side at the frozen remainder
+  // q_t = du[m_t] - v_t du[rho] (src/implicit/vic_assemble_impl.h:152-214);
+  // the neighbours' folds are skipped at the merged walls
+  const bool partial = B.implicit == 1;
+  T a3[9], b3[9], c3[9], rc[3] = {T(0.), T(0.), T(0.)};
+  if (partial) {
+    const int rows[3] = {0, 1, 4};
+    T aT[6], bT[6], cT[6];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        a3[r * 3 + q] = a[rows[r] * 5 + rows[q]];
+        b3[r * 3 + q] = b[rows[r] * 5 + rows[q]];
+        c3[r * 3 + q] = c[rows[r] * 5 + rows[q]];
+      }
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        aT[r * 2 + k] = a[rows[r] * 5 + 2 + k];
+        bT[r * 2 + k] = b[rows[r] * 5 + 2 + k];
+        cT[r * 2 + k] = c[rows[r] * 5 + 2 + k];
+      }
+    }
+    auto fold = [&](T* blk, const T* tb, int j, const double* wj) {
+      const double* dj = S.du + col * n + j;  // row v at dj[v * cells]
+      const T drho = T(dj[0]);
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        const T v = T(wj[2 + k]);
+        const T qt = T(dj[(size_t)(2 + k) * S.cells]) - v * drho;
+        if (v != T(0.))
+#pragma unroll
+          for (int r = 0; r < 3; ++r) blk[r * 3] = blk[r * 3] + tb[r * 2 + k] * v;
+        if (qt != T(0.))
+#pragma unroll
+          for (int r = 0; r < 3; ++r) rc[r] = rc[r] + tb[r * 2 + k] * qt;
+      }
+    };
+    fold(a3, aT, i, wd[1]);
+    if (i > 0) fold(b3, bT, i - 1, wd[0]);
+    if (i < n - 1) fold(c3, cT, i + 1, wd[2]);
+  }
   if (wood) {
     VicK K = vic_krows(B, n, i);
-    a[20] -= vdiv(T(K.mid), T(dtc), rdt);
-    b[20] -= vdiv(T(K.lo), T(dtc), rdt);
-    c[20] -= vdiv(T(K.hi), T(dtc), rdt);
+    if (partial) {
+      a3[6] -= vdiv(T(K.mid), T(dtc), rdt);
+      b3[6] -= vdiv(T(K.lo), T(dtc), rdt);
+      c3[6] -= vdiv(T(K.hi), T(dtc), rdt);
+    } else {
+      a[20] -= vdiv(T(K.mid), T(dtc), rdt);
+      b[20] -= vdiv(T(K.lo), T(dtc), rdt);
+      c[20] -= vdiv(T(K.hi), T(dtc), rdt);
+    }
     // du[IPR] -= (K du0[IDN])_i : the IDN row is read only (FP64 always)
     const double* dn = S.du + col * n;
     double s = K.mid * dn[i];
@@ -346,6 +398,19 @@ __device__ __forceinline__ void vic_assemble_cell(const BlockDev& B,
     if (i == 0) s += K.t0 * dn[2];
     if (i == n - 1) s += K.t1 * dn[n - 3];
     S.du[4 * S.cells + cell] = du0[4] - s;
+  }
+  if (partial) {
+    // a cell's row of 25: the 3x3 block, row-major, then (A only) the
+    // right-hand-side term of the fold
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      S.A[cell * 25 + k] = (double)a3[k];
+      S.B[cell * 25 + k] = (double)b3[k];
+      S.C[cell * 25 + k] = (double)c3[k];
+    }
+#pragma unroll
+    for (int r = 0; r < 3; ++r) S.A[cell * 25 + 9 + r] = (double)rc[r];
+    return;
   }
   // the FP64 blocks, unless the refined solve reads the FP32 ones (exact:
   // its residuals and the masked columns' direct solve widen them)
@@ -447,28 +512,6 @@ struct VCol {
   }
 };
 
-// a float widened to the double of the same value with integer operations
-// only: the FP64 kernels here are bound by the FP64 pipe, which the widening
-// instruction would also occupy.  Normal numbers rebias the exponent (127 ->
-// 1023) and shift the mantissa up 29 bits; zeros keep their sign; a
-// subnormal m 2^-149 is renormalised at its leading bit; infinities and NaNs
-// keep their payload (the quiet bit lands on the double's)
-__device__ __forceinline__ unsigned long long widen_bits(unsigned int b) {
-  const unsigned long long sgn = (unsigned long long)(b >> 31) << 63;
-  const unsigned int e = (b >> 23) & 0xffu;
-  const unsigned long long m = b & 0x7fffffu;
-  if (e == 0xffu) return sgn | (0x7ffull << 52) | (m << 29);
-  if (e != 0u) return sgn | ((unsigned long long)(e + 896u) << 52) | (m << 29);
-  if (m == 0u) return sgn;
-  const int k = 31 - __clz((int)m);  // the leading bit, 0..22
-  return sgn | ((unsigned long long)(k + 874) << 52) |
-         ((m << (52 - k)) & 0xfffffffffffffull);
-}
-
-__device__ __forceinline__ double widen_exact(float f) {
-  return __longlong_as_double((long long)widen_bits(__float_as_uint(f)));
-}
-
 // finite, tested on the exponent bits (integer pipes, not the FP64 one)
 __device__ __forceinline__ bool vfinite(double x) {
   return ((__double_as_longlong(x) >> 52) & 0x7ff) != 0x7ff;
@@ -546,7 +589,7 @@ __global__ void __launch_bounds__(32)
                      int* status) {
   __shared__ VicSolveSmem sm;
   const BlockDev& Bk = tab[blockIdx.y];
-  if (!Bk.implicit) return;
+  if (!Bk.implicit || Bk.implicit == 1) return;  // scheme 1: vic_solve3
   const VicScratch S = vic_scratch(Bk);
   const int n = Bk.nc1 - 2 * Bk.ng;
   const size_t ncol = S.cells / n;
@@ -813,6 +856,292 @@ __global__ void __launch_bounds__(32)
   }
   // a failed column is marked in its solution: the finish keeps du0
   if (valid && !ok && q == 0) {
+    D[0] = __longlong_as_double(0x7ff8000000000000ll);
+    atomicOr(&status[blockIdx.y], kVicFailed);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// (2p) the partial matrix (implicit-scheme 1): the 3x3 block-Thomas sweep of
+// ForwardSweep with N = 3 (src/implicit/forward_sweep_impl.h:30-131), one
+// thread per column: the right-hand side less the assembly's fold term, the
+// block screened by ludcmp<3> and inverted explicitly (adjugate over the
+// determinant), d = inv (rhs - b d_prev), a' = inv c, the two Woodbury unit
+// vectors of the energy row, then vic_backward_substitute (each vector only
+// if its first layer is finite) and the Woodbury update on the 3-vectors.
+// The solution leaves in D rows 0, 1 and 4 (the tangential rows keep the
+// explicit du; the finish moves them with the face mass).  Its chain is
+// short (about 200 FP64 operations per layer), so a thread per column keeps
+// every lane of an FP64 instruction on its own column.
+__device__ __forceinline__ bool vic_ludcmp3_ok(const double* m) {
+  double a[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    a[k] = m[k];
+    if (!vfinite(a[k])) return false;
+  }
+  double vv[3], scale[3];
+  const double tol = 8. * 3 * 2.220446049250313e-16;
+  for (int i = 0; i < 3; ++i) {
+    double big = 0.;
+    for (int j = 0; j < 3; ++j) {
+      const double t = fabs(a[i * 3 + j]);
+      if (t > big) big = t;
+    }
+    if (big == 0.) return false;
+    scale[i] = big;
+    vv[i] = 1.0 / big;
+    if (!vfinite(vv[i])) return false;
+  }
+  for (int j = 0; j < 3; ++j) {
+    for (int i = 0; i < j; ++i) {
+      double sum = a[i * 3 + j];
+      for (int k = 0; k < i; ++k) sum -= a[i * 3 + k] * a[k * 3 + j];
+      if (!vfinite(sum)) return false;
+      a[i * 3 + j] = sum;
+    }
+    double big = 0.;
+    int imax = 0;
+    for (int i = j; i < 3; ++i) {
+      double sum = a[i * 3 + j];
+      for (int k = 0; k < j; ++k) sum -= a[i * 3 + k] * a[k * 3 + j];
+      if (!vfinite(sum)) return false;
+      a[i * 3 + j] = sum;
+      const double dum = vv[i] * fabs(sum);
+      if (!vfinite(dum)) return false;
+      if (dum >= big) {
+        big = dum;
+        imax = i;
+      }
+    }
+    if (j != imax) {
+      for (int k = 0; k < 3; ++k) {
+        const double t = a[imax * 3 + k];
+        a[imax * 3 + k] = a[j * 3 + k];
+        a[j * 3 + k] = t;
+      }
+      vv[imax] = vv[j];
+      const double t = scale[imax];
+      scale[imax] = scale[j];
+      scale[j] = t;
+    }
+    if (fabs(a[j * 3 + j]) / scale[j] <= tol) return false;
+    if (j != 2) {
+      const double dum = 1.0 / a[j * 3 + j];
+      for (int i = j + 1; i < 3; ++i) a[i * 3 + j] *= dum;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 9; ++k)
+    if (!vfinite(a[k])) return false;
+  return true;
+}
+
+__device__ __forceinline__ void vmat3_mul(double* out, const double* a,
+                                          const double* b) {
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      double s = a[r * 3] * b[c];
+      s += a[r * 3 + 1] * b[3 + c];
+      s += a[r * 3 + 2] * b[6 + c];
+      out[r * 3 + c] = s;
+    }
+}
+
+__device__ __forceinline__ void vmat3_vec(double* out, const double* a,
+                                          const double* v) {
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    double s = a[r * 3] * v[0];
+    s += a[r * 3 + 1] * v[1];
+    s += a[r * 3 + 2] * v[2];
+    out[r] = s;
+  }
+}
+
+__global__ void __launch_bounds__(kThreads)
+    vic_solve3_kernel(const BlockDev* __restrict__ tab, StageParams p,
+                      int* status) {
+  const BlockDev& Bk = tab[blockIdx.y];
+  if (Bk.implicit != 1) return;
+  const VicScratch S = vic_scratch(Bk);
+  const int n = Bk.nc1 - 2 * Bk.ng;
+  const size_t ncol = S.cells / n;
+  const size_t col = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncol) return;
+  const double dtc = p.w2 * p.dt[blockIdx.y];
+  const double rdtc = 1. / dtc;  // du / dt_corr divides by it (vdiv)
+  const bool wood = n >= 3;
+  double* A = S.A + col * n * 25;
+  const double* Bm = S.B + col * n * 25;
+  const double* C = S.C + col * n * 25;
+  double* D = S.D + col * n * 5;
+  double* Z0 = S.Z0 + col * n * 5;
+  double* Z1 = S.Z1 + col * n * 5;
+  const double* du = S.du + col * n;  // row v at du[v * cells + i]
+  const size_t cs = S.cells;
+  bool ok = true;
+  for (int e = 0; e < 5 * n; ++e)
+    ok = ok && vfinite(du[(size_t)(e / n) * cs + (e % n)]);
+  double ap[9], dp[3], y0[3] = {0., 0., 0.}, y1[3] = {0., 0., 0.};
+  for (int i = 0; i < n && ok; ++i) {
+    double m[9], bb[9], cc[9], rc[3];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      m[k] = A[i * 25 + k];
+      bb[k] = Bm[i * 25 + k];
+      cc[k] = C[i * 25 + k];
+    }
+#pragma unroll
+    for (int r = 0; r < 3; ++r) rc[r] = A[i * 25 + 9 + r];
+    double rhs[3] = {vdiv(du[i], dtc, rdtc), vdiv(du[cs + i], dtc, rdtc),
+                     vdiv(du[4 * cs + i], dtc, rdtc)};
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+      if (rc[r] != 0.) rhs[r] -= rc[r];
+    if (i > 0) {
+      double t[9];
+      vmat3_mul(t, bb, ap);
+#pragma unroll
+      for (int k = 0; k < 9; ++k) m[k] -= t[k];
+    }
+    if (!vic_ludcmp3_ok(m)) {
+      ok = false;
+      break;
+    }
+    // the adjugate over the determinant, expanded along column 0
+    const double c00 = m[4] * m[8] - m[5] * m[7];
+    const double c10 = m[2] * m[7] - m[1] * m[8];
+    const double c20 = m[1] * m[5] - m[2] * m[4];
+    const double det = m[0] * c00 + m[3] * c10 + m[6] * c20;
+    const double rd = 1. / det;
+    const double inv[9] = {c00 * rd,
+                           c10 * rd,
+                           c20 * rd,
+                           (m[5] * m[6] - m[3] * m[8]) * rd,
+                           (m[0] * m[8] - m[2] * m[6]) * rd,
+                           (m[2] * m[3] - m[0] * m[5]) * rd,
+                           (m[3] * m[7] - m[4] * m[6]) * rd,
+                           (m[1] * m[6] - m[0] * m[7]) * rd,
+                           (m[0] * m[4] - m[1] * m[3]) * rd};
+    double t[3], u[3];
+    if (i > 0) {
+      vmat3_vec(u, bb, dp);
+#pragma unroll
+      for (int r = 0; r < 3; ++r) t[r] = rhs[r] - u[r];
+    } else {
+#pragma unroll
+      for (int r = 0; r < 3; ++r) t[r] = rhs[r];
+    }
+    vmat3_vec(dp, inv, t);
+    if (wood) {
+      if (i > 0) {
+        vmat3_vec(u, bb, y0);
+#pragma unroll
+        for (int r = 0; r < 3; ++r) t[r] = (r == 2 && i == 0 ? 1. : 0.) - u[r];
+      } else {
+        t[0] = 0.;
+        t[1] = 0.;
+        t[2] = 1.;
+      }
+      vmat3_vec(y0, inv, t);
+      if (i > 0) {
+        vmat3_vec(u, bb, y1);
+#pragma unroll
+        for (int r = 0; r < 3; ++r) t[r] = (r == 2 && i == n - 1 ? 1. : 0.) - u[r];
+      } else {
+        t[0] = 0.;
+        t[1] = 0.;
+        t[2] = i == n - 1 ? 1. : 0.;
+      }
+      vmat3_vec(y1, inv, t);
+    }
+    vmat3_mul(ap, inv, cc);
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      ok = ok && vfinite(dp[r]);
+#pragma unroll
+      for (int q = 0; q < 3; ++q) ok = ok && vfinite(ap[r * 3 + q]);
+    }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) A[i * 25 + k] = ap[k];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      D[i * 5 + r] = dp[r];
+      Z0[i * 5 + r] = y0[r];
+      Z1[i * 5 + r] = y1[r];
+    }
+  }
+  if (ok) {
+    bool f0 = wood, f1 = wood;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      f0 = f0 && vfinite(Z0[r]);
+      f1 = f1 && vfinite(Z1[r]);
+    }
+    for (int i = n - 2; i >= 0; --i) {
+      double a[9], t[3];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) a[k] = A[i * 25 + k];
+      vmat3_vec(t, a, dp);
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        dp[r] = D[i * 5 + r] - t[r];
+        D[i * 5 + r] = dp[r];
+      }
+      if (f0) {
+        vmat3_vec(t, a, y0);
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+          y0[r] = Z0[i * 5 + r] - t[r];
+          Z0[i * 5 + r] = y0[r];
+        }
+      }
+      if (f1) {
+        vmat3_vec(t, a, y1);
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+          y1[r] = Z1[i * 5 + r] - t[r];
+          Z1[i * 5 + r] = y1[r];
+        }
+      }
+    }
+    double al0 = 0., al1 = 0.;
+    if (wood) {
+      VicK K0 = vic_krows(Bk, n, 0), K1 = vic_krows(Bk, n, n - 1);
+      double k0 = -K0.t0 / dtc, k1 = -K1.t1 / dtc;
+      k0 = k0 * 1.;
+      k1 = k1 * 1.;
+      const int a0 = 2, a1 = n - 3;
+      double m00 = 1. + k0 * Z0[a0 * 5], m01 = k0 * Z1[a0 * 5];
+      double m10 = k1 * Z0[a1 * 5], m11 = 1. + k1 * Z1[a1 * 5];
+      double r0 = k0 * D[a0 * 5], r1 = k1 * D[a1 * 5];
+      double det = m00 * m11 - m01 * m10;
+      al0 = (m11 * r0 - m01 * r1) / det;
+      al1 = (m00 * r1 - m10 * r0) / det;
+    }
+    for (int i = 0; i < n; ++i) {
+      double d[3];
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        d[r] = D[i * 5 + r];
+        if (wood) {
+          d[r] -= Z0[i * 5 + r] * al0;
+          d[r] -= Z1[i * 5 + r] * al1;
+        }
+        ok = ok && vfinite(d[r]);
+      }
+      D[i * 5] = d[0];
+      D[i * 5 + 1] = d[1];
+      D[i * 5 + 2] = 0.;
+      D[i * 5 + 3] = 0.;
+      D[i * 5 + 4] = d[2];
+    }
+  }
+  // a failed column is marked in its solution: the finish keeps du0
+  if (!ok) {
     D[0] = __longlong_as_double(0x7ff8000000000000ll);
     atomicOr(&status[blockIdx.y], kVicFailed);
   }
@@ -1151,7 +1480,7 @@ __global__ void __launch_bounds__(32)
     for (int h = 0; h < 2; ++h) {
       if (use[h]) {
         const float val = sm.vec[g][0][pr2[h]];
-        if (ok) xp[h][(n - 1) * 5] = (double)val;
+        if (ok) xp[h][(n - 1) * 5] = widen_exact(val);
         fin = fin && vfinite32(val);
         dmax[h] = fmaxf(dmax[h], fabsf(val));
       }
@@ -1174,7 +1503,7 @@ __global__ void __launch_bounds__(32)
 #pragma unroll
           for (int k = 0; k < 5; ++k) t = fmaf(-cr[h][k], xn[k], t);
           sm.vec[g][cur ^ 1][pr2[h]] = t;
-          if (ok) xp[h][i * 5] = (double)t;
+          if (ok) xp[h][i * 5] = widen_exact(t);
           fin = fin && vfinite32(t);
           dmax[h] = fmaxf(dmax[h], fabsf(t));
         }
@@ -1376,10 +1705,14 @@ __global__ void __launch_bounds__(32 * kCorrWarps)
   // ---- back: d_i = y_i - c'_i d_(i+1), x_i += d_i in FP64 ----
   float dmax = 0.f;
   bool fin = true;
+  // a correction before the last keeps d for the next residual (r - T d),
+  // in the C scratch (unused by the refined solve otherwise)
+  float* DD = reinterpret_cast<float*>(S.C) + cc * n * kR32 + k * 5;
   if (act) {
 #pragma unroll
     for (int r = 0; r < 5; ++r) {
-      X[(n - 1) * 5 + r] = X[(n - 1) * 5 + r] + (double)y[r];
+      if (!last) DD[(n - 1) * kR32 + r] = y[r];
+      X[(n - 1) * 5 + r] = X[(n - 1) * 5 + r] + widen_exact(y[r]);
       fin = fin && vfinite32(y[r]);
       dmax = fmaxf(dmax, fabsf(y[r]));
     }
@@ -1424,7 +1757,8 @@ __global__ void __launch_bounds__(32 * kCorrWarps)
 #pragma unroll
       for (int r = 0; r < 5; ++r) {
         y[r] = t[r];
-        X[i * 5 + r] = s.g.x[lane][r] + (double)t[r];
+        if (!last) DD[i * kR32 + r] = t[r];
+        X[i * 5 + r] = s.g.x[lane][r] + widen_exact(t[r]);
         fin = fin && vfinite32(t[r]);
         dmax = fmaxf(dmax, fabsf(t[r]));
       }
@@ -1495,11 +1829,37 @@ __global__ void __launch_bounds__(32 * kCorrWarps)
   if (valid && k == 0) F.mask[cc] = (conv && !bad) ? 0 : 1;
 }
 
-// the FP64 residual r = b - (B_i x_(i-1) + A_i x_i + C_i x_(i+1)) of every
-// cell and right-hand side (one thread per cell), from the FP32-assembled
-// blocks widened to FP64 (exact) and x in D, Z0, Z1; rounded to FP32 into R
+// s_h + s_l += t d in float-float arithmetic, t and d floats: the product
+// split exactly by an FMA (the two-product of Dekker's method), the sum by
+// Knuth's two-sum; the low parts gather in s_l.  Every step is a single
+// rounding (__fmul_rn / __fadd_rn are never contracted)
+__device__ __forceinline__ void ff_madd(float& sh, float& sl, float t, float d) {
+  const float p = __fmul_rn(t, d);
+  const float e = __fmaf_rn(t, d, -p);
+  const float s2 = __fadd_rn(sh, p);
+  const float bp = __fadd_rn(s2, -sh);
+  const float err =
+      __fadd_rn(__fadd_rn(sh, -__fadd_rn(s2, -bp)), __fadd_rn(p, -bp));
+  sl = __fadd_rn(sl, __fadd_rn(err, e));
+  sh = s2;
+}
+
+// the residual r = b - (B_i x_(i-1) + A_i x_i + C_i x_(i+1)) of every cell
+// and right-hand side (one thread per cell), rounded to FP32 into R for the
+// correction's sweeps.
+// * The first correction (corr 1) forms it in FP64 from the FP32-assembled
+//   blocks widened to FP64 (exact) and x in D, Z0, Z1, and keeps the FP64 r
+//   (in the B scratch, which the refined solve does not use otherwise).
+// * A later correction forms it from the previous one: x grew by the FP32
+//   correction d (kept in the C scratch by vic_correct32_kernel), so
+//   r_new = r - T d.  T and d are floats, so T d is summed in float-float
+//   on the FP32 pipe (its error, 2^-48 of the sum of |t d| with |d| about
+//   2^-20 |x|, is far below the FP64 rounding of r); the two FP64 subtractions
+//   that remain replace 225 FP64 multiply-adds per cell.  The rounding of
+//   x += d in FP64 adds at most 2^-53 |x| to x, the FP64 residual's own level.
 __global__ void __launch_bounds__(kThreads)
-    vic_residual_kernel(const BlockDev* __restrict__ tab, StageParams p) {
+    vic_residual_kernel(const BlockDev* __restrict__ tab, StageParams p,
+                        int corr) {
   const BlockDev& B = tab[blockIdx.y];
   if (!B.implicit || !B.implicit_f32) return;
   const VicScratch S = vic_scratch(B);
@@ -1508,46 +1868,81 @@ __global__ void __launch_bounds__(kThreads)
   const double dtc = p.w2 * p.dt[blockIdx.y];
   const double rdtc = 1. / dtc;
   const int nrhs = n >= 3 ? 3 : 1;
+  const bool keep = corr < p.refine;  // a later correction reads r
+  const float* DD = reinterpret_cast<const float*>(S.C);
   for (size_t cell = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
        cell < S.cells; cell += (size_t)gridDim.x * blockDim.x) {
     const size_t col = cell / n;
     const int i = (int)(cell - col * n);
     if (F.mask[col]) continue;
-    // the FP32-assembled blocks (exact), widened
     const float* a = F.A + cell * kBlk32;
     const float* bl = F.B + cell * kBlk32;
     const float* c = F.C + cell * kBlk32;
     for (int k = 0; k < nrhs; ++k) {
-      const double* x = (k == 0 ? S.D : (k == 1 ? S.Z0 : S.Z1)) + cell * 5;
+      double* rb = S.B + cell * 25 + k * 5;
       double t[5];
+      if (corr == 1) {
+        const double* x = (k == 0 ? S.D : (k == 1 ? S.Z0 : S.Z1)) + cell * 5;
 #pragma unroll
-      for (int r = 0; r < 5; ++r)
-        t[r] = k == 0 ? vdiv(S.du[(size_t)r * S.cells + cell], dtc, rdtc)
-                      : ((r == 4 && i == (k == 1 ? 0 : n - 1)) ? 1. : 0.);
-#pragma unroll
-      for (int q = 0; q < 5; ++q) {
-        const double xc = x[q];
-#pragma unroll
-        for (int r = 0; r < 5; ++r) t[r] = fma(-widen_exact(a[r * 5 + q]), xc, t[r]);
-      }
-      if (i > 0) {
+        for (int r = 0; r < 5; ++r)
+          t[r] = k == 0 ? vdiv(S.du[(size_t)r * S.cells + cell], dtc, rdtc)
+                        : ((r == 4 && i == (k == 1 ? 0 : n - 1)) ? 1. : 0.);
 #pragma unroll
         for (int q = 0; q < 5; ++q) {
-          const double xl = x[q - 5];
+          const double xc = x[q];
 #pragma unroll
-          for (int r = 0; r < 5; ++r) t[r] = fma(-widen_exact(bl[r * 5 + q]), xl, t[r]);
+          for (int r = 0; r < 5; ++r) t[r] = fma(-widen_exact(a[r * 5 + q]), xc, t[r]);
         }
-      }
-      if (i < n - 1) {
+        if (i > 0) {
+#pragma unroll
+          for (int q = 0; q < 5; ++q) {
+            const double xl = x[q - 5];
+#pragma unroll
+            for (int r = 0; r < 5; ++r) t[r] = fma(-widen_exact(bl[r * 5 + q]), xl, t[r]);
+          }
+        }
+        if (i < n - 1) {
+#pragma unroll
+          for (int q = 0; q < 5; ++q) {
+            const double xu = x[q + 5];
+#pragma unroll
+            for (int r = 0; r < 5; ++r) t[r] = fma(-widen_exact(c[r * 5 + q]), xu, t[r]);
+          }
+        }
+      } else {
+        float sh[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, sl[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+        const float* dc = DD + cell * kR32 + k * 5;
 #pragma unroll
         for (int q = 0; q < 5; ++q) {
-          const double xu = x[q + 5];
+          const float dq = dc[q];
 #pragma unroll
-          for (int r = 0; r < 5; ++r) t[r] = fma(-widen_exact(c[r * 5 + q]), xu, t[r]);
+          for (int r = 0; r < 5; ++r) ff_madd(sh[r], sl[r], a[r * 5 + q], dq);
         }
+        if (i > 0) {
+#pragma unroll
+          for (int q = 0; q < 5; ++q) {
+            const float dq = dc[q - kR32];
+#pragma unroll
+            for (int r = 0; r < 5; ++r) ff_madd(sh[r], sl[r], bl[r * 5 + q], dq);
+          }
+        }
+        if (i < n - 1) {
+#pragma unroll
+          for (int q = 0; q < 5; ++q) {
+            const float dq = dc[q + kR32];
+#pragma unroll
+            for (int r = 0; r < 5; ++r) ff_madd(sh[r], sl[r], c[r * 5 + q], dq);
+          }
+        }
+#pragma unroll
+        for (int r = 0; r < 5; ++r)
+          t[r] = (rb[r] - widen_exact(sh[r])) - widen_exact(sl[r]);
       }
 #pragma unroll
-      for (int r = 0; r < 5; ++r) F.R[cell * kR32 + k * 5 + r] = (float)t[r];
+      for (int r = 0; r < 5; ++r) {
+        if (keep) rb[r] = t[r];
+        F.R[cell * kR32 + k * 5 + r] = (float)t[r];
+      }
     }
   }
 }
@@ -1596,6 +1991,11 @@ __global__ void __launch_bounds__(NL == 32 ? 32 * kVicWarps : kThreads)
   const VCol mq{w0p + (size_t)(n + 1) * ws, ws};           // n + 1: the moved total mass
   const VCol mdn{w0p + (size_t)(2 * n + 2) * ws, ws};      // n: the dry-gas increment
   const VCol rho{w0p + (size_t)(3 * n + 2) * ws, ws};      // n: the density of each layer
+  // the partial matrix (implicit-scheme 1): the tangential velocities of
+  // layers 0..n (n: the ghost above), in the (free) second Woodbury vector
+  const bool partial = B.implicit == 1;
+  double* const w1p = NL == 32 ? S.Z1 + col * n * 5 : S.Z1 + col;
+  const VCol vt2{w1p, ws}, vt3{w1p + (size_t)(n + 1) * ws, ws};
   if (ok) {
     for (int i = lane; i < n; i += NL) {
       double w[5];
@@ -1603,6 +2003,16 @@ __global__ void __launch_bounds__(NL == 32 ? 32 * kVicWarps : kThreads)
       rho[i] = w[0];
       mdn[i] = 0.;
       mq[i] = (D[i * 5] - du[i]) * vol;  // staged: phi of layer i
+      if (partial) {
+        vt2[i] = w[2];
+        vt3[i] = w[3];
+      }
+    }
+    if (partial && lane == 0) {
+      double w[5];
+      vic_prim(uin, plane, base + n, B.gammad, w, B.base, nc1);
+      vt2[n] = w[2];
+      vt3[n] = w[3];
     }
     vsync<NL>();
     if (lane == 0) {
@@ -1639,8 +2049,10 @@ __global__ void __launch_bounds__(NL == 32 ? 32 * kVicWarps : kThreads)
     for (int i = lane; i < n; i += NL) {
       du[i] += mdn[i];
       du[cs + i] = D[i * 5 + 1];
-      du[2 * cs + i] = D[i * 5 + 2];
-      du[3 * cs + i] = D[i * 5 + 3];
+      if (!partial) {  // the partial matrix keeps the explicit m_t rows
+        du[2 * cs + i] = D[i * 5 + 2];
+        du[3 * cs + i] = D[i * 5 + 3];
+      }
       double e = D[i * 5 + 4];
       double projected = vdiv(mM[i] - mM[i + 1], vol, rvol);
       double ph = -grav * x1v[i];
@@ -1650,6 +2062,23 @@ __global__ void __launch_bounds__(NL == 32 ? 32 * kVicWarps : kThreads)
       double mv_lo = mq[i] - mM[i], mv_hi = mq[i + 1] - mM[i + 1];
       double cw = vdiv(-(dp_hi * mv_hi - dp_lo * mv_lo), vol, rvol);
       du[4 * cs + i] = e + (pw + cw);
+    }
+    vsync<NL>();
+    if (partial && lane == 0) {
+      // vic_tangential_momentum_column (src/implicit/vic_redistribute_impl.h
+      // :178-200): each face's moved total mass carries the donor (upwind)
+      // cell's tangential velocity; a zero transfer leaves du as it is
+      for (int i = 0; i + 1 < n; ++i) {
+        const double q = mq[i + 1];
+        const int donor = q > 0 ? i : i + 1;
+        const double pm[2] = {q * vt2[donor], q * vt3[donor]};
+#pragma unroll
+        for (int t = 0; t < 2; ++t) {
+          if (pm[t] == 0) continue;
+          du[(2 + t) * cs + i] -= vdiv(pm[t], vol, rvol);
+          du[(2 + t) * cs + i + 1] += vdiv(pm[t], vol, rvol);
+        }
+      }
     }
     vsync<NL>();
     if (wood) {
@@ -1717,7 +2146,14 @@ __global__ void __launch_bounds__(NL == 32 ? 32 * kVicWarps : kThreads)
       double sy = 0., sz = 0.;
       for (int f = 0; f < nf; ++f) {
         double ty = tot(IVY, f), tz = tot(IVZ, f);
-        if (ok) {
+        if (ok && partial) {
+          // the partial matrix posts the donor transfer q w_t of each face
+          // (src/implicit/implicit_hydro.cpp:520-530,662-666)
+          const double q = mq[f];
+          const int donor = q > 0. ? f - 1 : f;
+          ty = ty + vdiv(q * vt2[donor], kdt, rkdt);
+          tz = tz + vdiv(q * vt3[donor], kdt, rkdt);
+        } else if (ok) {
           double py = 0., pz = 0.;
           if (f > 0) {
             sy = sy + (D[(f - 1) * 5 + 2] - du0[2 * cs + f - 1]) * vol;

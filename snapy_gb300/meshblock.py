@@ -70,9 +70,13 @@ def scheme_of(options: MeshBlockOptions) -> dict:
             raise DeckError(f"forcing/diffusion: {sorted(extra)} are not built "
                             "(nu_iso only)")
     if h.icorr is not None:
-        if h.icorr.scheme != 9:
+        if h.icorr.scheme not in (1, 9):
             raise DeckError(f"integration/implicit-scheme {h.icorr.scheme}: the "
-                            "full 5x5 scheme 9 is built")
+                            "full 5x5 scheme 9 and the partial 3x3 scheme 1 "
+                            "are built")
+        if h.icorr.scheme == 1 and h.icorr.precision == "float32":
+            raise DeckError("integration/implicit-precision float32 is built "
+                            "for implicit-scheme 9 (scheme 1 assembles in FP64)")
         if options.hydro().precision == "float64" and h.icorr.precision == "float32":
             raise DeckError("integration/implicit-precision float32 needs "
                             "dynamics/precision float32")

@@ -73,7 +73,8 @@ def test_create_refuses_what_is_not_built(cuda):
         (scheme(), block(implicit_precision=_lib.F32), UNSUPPORTED,
          "implicit-precision"),
         (scheme(), block(bc=[9] * 6), ARG, "boundary kind"),
-        (scheme(), block(nc2=10, nc3=10, nu_iso=1.0), UNSUPPORTED, "3-D"),
+        (scheme(), block(implicit_scheme=1, implicit_precision=_lib.F32, **grav),
+         UNSUPPORTED, "implicit-scheme 1"),
         (scheme(), block(grav1=-9.8), ARG, "x1 geometry"),
     ]
     for sch, blk, code, word in cases:
@@ -107,8 +108,9 @@ def test_cubed_sphere_fp32_index_limit(cuda):
     dummy = torch.zeros(16, dtype=torch.float64, device=cuda)
     d = _lib.CsDesc()
     d.n, d.ng, d.dtype, d.nstage = 1700, 3, _lib.F32, 3
-    d.geo = d.ghost_tab = d.seam_tab = dummy.data_ptr()
+    d.geo = d.ghost_tab = d.seam_tab = d.seam_state_tab = dummy.data_ptr()
     d.nghost, d.nseam, d.phi_ref, d.cfl = 1, 1, 9810.0, 0.4
+    d.nseam_state = 24 * d.n
     h = ctypes.c_void_p()
     assert L.sg_cs_create(ctypes.byref(d), ctypes.byref(h)) == UNSUPPORTED
     assert "2^24" in L.sg_last_error().decode() and not h.value
