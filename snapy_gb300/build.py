@@ -1,12 +1,14 @@
 """Build the in-tree CUDA library ``snapy_gb300/libsnapy_gb300.so`` (sm_103a).
 
-Three translation units, compiled in parallel with nvcc and linked into one
+The translation units below, compiled in parallel with nvcc and linked into one
 shared library whose C ABI is ``include/snapy_gb300.h``:
 
 * ``sg_stage.cu`` as FP64 with ``-fmad=false`` (the parity path: no
   contraction, the reference CPU path's rounding),
 * ``sg_stage.cu`` as FP32 (contraction allowed),
-* ``sg_api.cu`` (host bookkeeping and the small finishing kernels).
+* ``sg_api.cu`` (host bookkeeping and the small finishing kernels),
+* ``sg_cs.cu`` as the cubed sphere's host API with its FP64 kernels
+  (``-fmad=false``) and again as its FP32 kernels (contraction allowed).
 """
 from __future__ import annotations
 
@@ -46,6 +48,10 @@ def _units():
             units.append((os.path.join(CSRC, f),
                           os.path.join(BUILD, f[:-3] + ".o"),
                           common + ["-fmad=false"]))
+    # the cubed sphere's FP32 kernels again, contraction allowed
+    units.append((os.path.join(CSRC, "sg_cs.cu"),
+                  os.path.join(BUILD, "sg_cs_f32.o"),
+                  common + ["-DSG_CS_F32_UNIT"]))
     return units
 
 

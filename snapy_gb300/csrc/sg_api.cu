@@ -1133,7 +1133,8 @@ int sg_stage(sg_handle* h, int32_t stage, const double* dt_dev,
     if (timed) cudaEventRecord(ev[4], s);
     // assembly, solve, finish; the refined solve adds its FP32 sweep and a
     // residual and a correction per correction
-    launches += 3 + (h->vic_kinds == 3 ? 1 : 0) +
+    // (a wide batch's finish is three launches)
+    launches += 3 + (h->wide ? 2 : 0) + (h->vic_kinds == 3 ? 1 : 0) +
                 (h->refine ? 1 + 2 * h->refine : 0);
   }
   if (h->scalars) {

@@ -31,8 +31,11 @@
 //                        (src/layout/cubed_sphere_layout.cpp:563-803,
 //                        src/coord/gnomonic_equiangle.cpp:536-609)
 // All the seam geometry is in three tables built once on the host; the
-// kernels only gather.  Built with -fmad=false: FP64 runs the checker's
-// operations in its order.
+// kernels only gather.  This file is compiled twice: as the host API with
+// the FP64 kernels, built with -fmad=false (the oracle's operations in its
+// order), and with SG_CS_F32_UNIT defined as the FP32 kernels alone, with
+// contraction allowed (the FP32 path is held to a tolerance, not to the
+// oracle's rounding); the host calls those through cs_f32_*.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdarg.h>
@@ -45,6 +48,36 @@
 #include "sg_device.cuh"
 
 extern "C" int sg_fail_message(int code, const char* msg);
+
+// the launch parameters of every kernel, shared by the two translation units
+namespace sgcs {
+struct CsParams {
+  int n, nc;
+  // the geometry, the ghost table and the seam table in the state's type
+  const void* geo;
+  const void* gtab;
+  int nghost;
+  const void* stab;
+  int nseam;
+  const void* sst;  // the seam face-state table (4 sides x n per panel)
+  void* sbuf;       // the seam faces' interior-side states (24 n x 4)
+  const void* in;
+  const void* u0;
+  void* out;
+  void* f2;
+  void* f3;
+  const double* dt;
+  double w0, w1, w2;
+  double phi0;  // FP32: the reference geopotential of the pressure anomaly
+  int hllc;     // 1: HLLC for shallow water, 0: shallow-roe (dir yz)
+};
+
+// the FP32 launches, defined in the FP32 unit
+int f32_stage(const CsParams& P, size_t faces, size_t cells, cudaStream_t s);
+int f32_ghost(const CsParams& P, void* buf, cudaStream_t s);
+int f32_dt(const CsParams& P, const void* buf, unsigned long long* key, int g,
+           cudaStream_t s);
+}  // namespace sgcs
 
 namespace {
 
@@ -89,26 +122,7 @@ __host__ __device__ inline Geo<T> geo_of(const void* gv, int nc) {
   return o;
 }
 
-struct CsParams {
-  int n, nc;
-  // the geometry, the ghost table and the seam table in the state's type
-  const void* geo;
-  const void* gtab;
-  int nghost;
-  const void* stab;
-  int nseam;
-  const void* sst;  // the seam face-state table (4 sides x n per panel)
-  void* sbuf;       // the seam faces' interior-side states (24 n x 4)
-  const void* in;
-  const void* u0;
-  void* out;
-  void* f2;
-  void* f3;
-  const double* dt;
-  double w0, w1, w2;
-  double phi0;  // FP32: the reference geopotential of the pressure anomaly
-  int hllc;     // 1: HLLC for shallow water, 0: shallow-roe (dir yz)
-};
+using sgcs::CsParams;
 
 // U -> W of one cell: v = m / Phi, the tangential pair raised by cos.
 // With phi0 > 0 (the FP32 state) the stored Phi row is the anomaly
@@ -602,7 +616,48 @@ int grid_for(size_t work) {
   return (int)(g ? g : 1);
 }
 
+// the five launches of a stage, the seam halo and the dt reduction in T
+template <typename T>
+int launch_stage(const CsParams& P, size_t faces, size_t cells, cudaStream_t s) {
+  (P.hllc ? cs_flux_kernel<T, true> : cs_flux_kernel<T, false>)
+      <<<grid_for(faces), kThreads, 0, s>>>(P);
+  (P.hllc ? cs_seam_face_kernel<T, true> : cs_seam_face_kernel<T, false>)
+      <<<grid_for(24 * (size_t)P.n), kThreads, 0, s>>>(P);
+  cs_seam_flux_kernel<T><<<grid_for(P.nseam), kThreads, 0, s>>>(P);
+  cs_update_kernel<T><<<grid_for(cells), kThreads, 0, s>>>(P);
+  cs_ghost_kernel<T><<<grid_for(P.nghost), kThreads, 0, s>>>(P, P.out);
+  return (int)cudaGetLastError();
+}
+
+template <typename T>
+int launch_ghost(const CsParams& P, void* buf, cudaStream_t s) {
+  cs_ghost_kernel<T><<<grid_for(P.nghost), kThreads, 0, s>>>(P, buf);
+  return (int)cudaGetLastError();
+}
+
+template <typename T>
+int launch_dt(const CsParams& P, const void* buf, unsigned long long* key,
+              int g, cudaStream_t s) {
+  cs_dt_kernel<T><<<g, kThreads, 0, s>>>(P, buf, key);
+  return (int)cudaGetLastError();
+}
+
 }  // namespace
+
+#ifdef SG_CS_F32_UNIT
+namespace sgcs {
+int f32_stage(const CsParams& P, size_t faces, size_t cells, cudaStream_t s) {
+  return launch_stage<float>(P, faces, cells, s);
+}
+int f32_ghost(const CsParams& P, void* buf, cudaStream_t s) {
+  return launch_ghost<float>(P, buf, s);
+}
+int f32_dt(const CsParams& P, const void* buf, unsigned long long* key, int g,
+           cudaStream_t s) {
+  return launch_dt<float>(P, buf, key, g, s);
+}
+}  // namespace sgcs
+#else
 
 __global__ void to_f32(const double* src, float* dst, size_t n) {
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
@@ -787,11 +842,9 @@ int sg_cs_fill_seams(sg_cs_handle* h, sg_stream_t stream) {
   if (!h || !h->buf[0]) return cs_fail(SG_ERR_STATE, "sg_cs_fill_seams: buffers not bound");
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   CsParams P = cs_params(h);
-  if (h->d.dtype == SG_F64)
-    cs_ghost_kernel<double><<<grid_for(P.nghost), kThreads, 0, s>>>(P, h->buf[h->cur]);
-  else
-    cs_ghost_kernel<float><<<grid_for(P.nghost), kThreads, 0, s>>>(P, h->buf[h->cur]);
-  cudaError_t e = cudaGetLastError();
+  const int rc = h->d.dtype == SG_F64 ? launch_ghost<double>(P, h->buf[h->cur], s)
+                                      : sgcs::f32_ghost(P, h->buf[h->cur], s);
+  cudaError_t e = rc ? (cudaError_t)rc : cudaGetLastError();
   return e == cudaSuccess ? 0 : cs_fail(SG_ERR_CUDA, "sg_cs_fill_seams: %s", cudaGetErrorString(e));
 }
 
@@ -814,24 +867,9 @@ int sg_cs_stage(sg_cs_handle* h, int32_t stage, const double* dt_dev,
   P.w2 = h->d.wght[stage][2];
   const size_t faces = (size_t)2 * 6 * P.n * (P.n + 1);
   const size_t cells = (size_t)6 * P.n * P.n;
-  if (h->d.dtype == SG_F64) {
-    (P.hllc ? cs_flux_kernel<double, true> : cs_flux_kernel<double, false>)
-        <<<grid_for(faces), kThreads, 0, s>>>(P);
-    (P.hllc ? cs_seam_face_kernel<double, true> : cs_seam_face_kernel<double, false>)
-        <<<grid_for(24 * (size_t)P.n), kThreads, 0, s>>>(P);
-    cs_seam_flux_kernel<double><<<grid_for(P.nseam), kThreads, 0, s>>>(P);
-    cs_update_kernel<double><<<grid_for(cells), kThreads, 0, s>>>(P);
-    cs_ghost_kernel<double><<<grid_for(P.nghost), kThreads, 0, s>>>(P, P.out);
-  } else {
-    (P.hllc ? cs_flux_kernel<float, true> : cs_flux_kernel<float, false>)
-        <<<grid_for(faces), kThreads, 0, s>>>(P);
-    (P.hllc ? cs_seam_face_kernel<float, true> : cs_seam_face_kernel<float, false>)
-        <<<grid_for(24 * (size_t)P.n), kThreads, 0, s>>>(P);
-    cs_seam_flux_kernel<float><<<grid_for(P.nseam), kThreads, 0, s>>>(P);
-    cs_update_kernel<float><<<grid_for(cells), kThreads, 0, s>>>(P);
-    cs_ghost_kernel<float><<<grid_for(P.nghost), kThreads, 0, s>>>(P, P.out);
-  }
-  cudaError_t e = cudaGetLastError();
+  const int rc = h->d.dtype == SG_F64 ? launch_stage<double>(P, faces, cells, s)
+                                      : sgcs::f32_stage(P, faces, cells, s);
+  cudaError_t e = rc ? (cudaError_t)rc : cudaGetLastError();
   if (e != cudaSuccess) return cs_fail(SG_ERR_CUDA, "sg_cs_stage: %s", cudaGetErrorString(e));
   if (stage == 0) h->base = h->cur;
   h->cur = out;
@@ -847,12 +885,14 @@ int sg_cs_max_dt(sg_cs_handle* h, double* dt_dev, sg_stream_t stream) {
   int g = grid_for(cells);
   if (g > 256) g = 256;
   if (h->d.dtype == SG_F64)
-    cs_dt_kernel<double><<<g, kThreads, 0, s>>>(P, h->buf[h->cur], h->key);
+    launch_dt<double>(P, h->buf[h->cur], h->key, g, s);
   else
-    cs_dt_kernel<float><<<g, kThreads, 0, s>>>(P, h->buf[h->cur], h->key);
+    sgcs::f32_dt(P, h->buf[h->cur], h->key, g, s);
   cs_dt_finish<<<1, 1, 0, s>>>(h->key, h->d.cfl, dt_dev);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? 0 : cs_fail(SG_ERR_CUDA, "sg_cs_max_dt: %s", cudaGetErrorString(e));
 }
 
 }  // extern "C"
+
+#endif  // SG_CS_F32_UNIT

@@ -2219,8 +2219,13 @@ extern "C" int SG_NAME(sg_launch_vic)(const BlockDev* tab, StageParams p,
   if (e != cudaSuccess) return (int)e;
   if (ev) cudaEventRecord(ev[1], stream);
   if (wide) {
+    // three passes: per cell, the serial scans per column, per cell
     int gt = (int)((max_cols + kThreads - 1) / kThreads);
-    vic_finish_kernel<1><<<dim3(gt, p.nblock), kThreads, 0, stream>>>(tab, p);
+    int gc = (int)((max_cells + kThreads - 1) / kThreads);
+    if (gc > 8192) gc = 8192;
+    vic_finish_a_kernel<<<dim3(gc, p.nblock), kThreads, 0, stream>>>(tab, p);
+    vic_finish_b_kernel<<<dim3(gt, p.nblock), kThreads, 0, stream>>>(tab, p);
+    vic_finish_c_kernel<<<dim3(gc, p.nblock), kThreads, 0, stream>>>(tab, p);
   } else {
     int gc = (int)((max_cols + kVicWarps - 1) / kVicWarps);
     vic_finish_kernel<32><<<dim3(gc, p.nblock), 32 * kVicWarps, 0, stream>>>(tab, p);

@@ -2181,3 +2181,263 @@ __global__ void __launch_bounds__(NL == 32 ? 32 * kVicWarps : kThreads)
     }
   }
 }
+
+// ---------------------------------------------------------------------------
+// (3w) the finish of wide batches in three launches.  A thread per column
+// walks every layer serially and, with a few warps per SM, waits on memory
+// at each one; here only the constituent column's serial scans keep a
+// thread per column, and the per-layer work runs a thread per cell:
+//   vic_finish_a_kernel  per cell: the layer's density (and, for the partial
+//                        matrix, its tangential velocities) and phi =
+//                        (D_rho - du_rho) V
+//   vic_finish_b_kernel  per column: the sums R and S, the face-mass prefix
+//                        M, the availability clamp (q, the dry increment),
+//                        the scalars' face transfers and the x1 step field
+//   vic_finish_c_kernel  per cell: the map of the solution, the partial
+//                        matrix's tangential transfers, the gravity-work
+//                        remainder and the RK combine, from the inputs only
+//                        (no cell writes what another reads)
+// Every value takes the operations of vic_finish_kernel in its order, so
+// the results are the same bit for bit.  A column's work arrays stay in its
+// (free) Woodbury scratch, column-contiguous:
+//   Z0: mM [n + 1] | mq [n + 1] | mdn [n] | rho [n]
+//   Z1: vt2 [n + 1] | vt3 [n + 1] | phi [n]
+struct FinishCol {
+  double *mM, *mq, *mdn, *rho, *vt2, *vt3, *phi;
+};
+
+__device__ __forceinline__ FinishCol finish_col(const VicScratch& S,
+                                                size_t col, int n) {
+  double* z0 = S.Z0 + col * n * 5;
+  double* z1 = S.Z1 + col * n * 5;
+  return FinishCol{z0, z0 + (n + 1), z0 + (2 * n + 2), z0 + (3 * n + 2),
+                   z1, z1 + (n + 1), z1 + (2 * n + 2)};
+}
+
+__global__ void __launch_bounds__(kThreads)
+    vic_finish_a_kernel(const BlockDev* __restrict__ tab, StageParams p) {
+  const BlockDev& B = tab[blockIdx.y];
+  if (!B.implicit) return;
+  const VicScratch S = vic_scratch(B);
+  const int ng = B.ng, nc1 = B.nc1, n = nc1 - 2 * ng;
+  const size_t plane = (size_t)nc1 * B.nc2 * B.nc3;
+  const real* uin = static_cast<const real*>(B.buf[p.in]);
+  const double vol = B.dx3 * (B.dx2 * B.dx1);
+  const bool partial = B.implicit == 1;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < S.cells;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const size_t col = e / n;
+    const int i = (int)(e - col * n);
+    const double* D = S.D + col * n * 5;
+    if (!vfinite(D[0])) continue;
+    const size_t base = vic_row(B, col) * nc1 + ng;
+    const FinishCol F = finish_col(S, col, n);
+    double w[5];
+    vic_prim(uin, plane, base + i, B.gammad, w, B.base, nc1);
+    F.rho[i] = w[0];
+    F.phi[i] = (D[i * 5] - S.du[e]) * vol;
+    if (partial) {
+      F.vt2[i] = w[2];
+      F.vt3[i] = w[3];
+      if (i == n - 1) {  // the ghost above, the donor of the top face
+        vic_prim(uin, plane, base + n, B.gammad, w, B.base, nc1);
+        F.vt2[n] = w[2];
+        F.vt3[n] = w[3];
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kThreads)
+    vic_finish_b_kernel(const BlockDev* __restrict__ tab, StageParams p) {
+  const BlockDev& B = tab[blockIdx.y];
+  if (!B.implicit) return;
+  const VicScratch S = vic_scratch(B);
+  const int ng = B.ng, nc1 = B.nc1, n = nc1 - 2 * ng;
+  const size_t ncol = S.cells / n;
+  const size_t col = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= ncol) return;
+  const size_t plane = (size_t)nc1 * B.nc2 * B.nc3;
+  const size_t jrow = vic_row(B, col);
+  const double vol = B.dx3 * (B.dx2 * B.dx1);
+  const double rvol = 1. / vol;
+  const double* D = S.D + col * n * 5;
+  const double* du = S.du + col * n;
+  const double* du0 = S.du0 + col * n;
+  const size_t cs = S.cells;
+  const bool ok = vfinite(D[0]);
+  const bool partial = B.implicit == 1;
+  const FinishCol F = finish_col(S, col, n);
+  if (ok) {
+    double R = 0, Ssum = 0;
+    for (int i = 0; i < n; ++i) {
+      R += F.phi[i];
+      Ssum += F.rho[i] * vol;
+    }
+    double M = 0;
+    const double rss = 1. / Ssum;
+    for (int i = 0; i < n; ++i) {
+      F.mM[i] = M;
+      M -= F.phi[i] - R * vdiv(F.rho[i] * vol, Ssum, rss);
+    }
+    F.mM[n] = 0.;
+    F.mq[0] = 0.;
+    double avail = (F.rho[0] * 1. + du[0]) * vol;
+    if (avail < 0) avail = 0;
+    double dn = 0.;  // the dry increment of layer i, carried up
+    for (int i = 0; i + 1 < n; ++i) {
+      double avail_up = (F.rho[i + 1] * 1. + du[i + 1]) * vol;
+      if (avail_up < 0) avail_up = 0;
+      double Mf = F.mM[i + 1];
+      double q = Mf > 0 ? Mf * 1. : Mf * 1.;
+      if (q > avail) q = avail;
+      if (q < -avail_up) q = -avail_up;
+      const double qv = vdiv(q, vol, rvol);
+      F.mdn[i] = dn - qv;
+      dn = 0. + qv;
+      F.mq[i + 1] = q;
+      avail = avail_up + q;
+    }
+    F.mdn[n - 1] = dn;
+    F.mq[n] = 0.;
+  }
+  if (B.nscalar > 0)
+    for (int f = 0; f <= n; ++f)
+      B.vicq[jrow * nc1 + ng + f] = ok ? F.mq[f] : 0.;
+  // the x1 step field, as in vic_finish_kernel
+  if (double* S1 = B.step[0]) {
+    const double dt = p.dt[blockIdx.y];
+    const double kdt = dt * (B.dx3 * B.dx2), rkdt = 1. / kdt;
+    const double w1s = p.w1, w2dt = p.w2 * dt;
+    const bool first = p.first != 0;
+    const int nf = n + 1;
+    const double* T = B.t1;
+    const bool wlo = B.bc[0] == kBcReflecting, whi = B.bc[1] == kBcReflecting;
+    auto tot = [&](int v, int f) { return T[((size_t)v * ncol + col) * nf + f]; };
+    auto at = [&](int v, int f) { return S1 + v * plane + jrow * nc1 + ng + f; };
+    double sy = 0., sz = 0.;
+    for (int f = 0; f < nf; ++f) {
+      double t0 = tot(IDN, f), t1 = tot(IVX, f), t4 = tot(IPR, f);
+      if (ok) t0 = t0 + vdiv(F.mq[f], kdt, rkdt);
+      if ((f == 0 && wlo) || (f == n && whi)) t0 = t4 = 0.;
+      step_set(at(IDN, f), t0, w1s, w2dt, first);
+      step_set(at(IVX, f), t1, w1s, w2dt, first);
+      step_set(at(IPR, f), t4, w1s, w2dt, first);
+      double ty = tot(IVY, f), tz = tot(IVZ, f);
+      if (ok && partial) {
+        const double q = F.mq[f];
+        const int donor = q > 0. ? f - 1 : f;
+        ty = ty + vdiv(q * F.vt2[donor], kdt, rkdt);
+        tz = tz + vdiv(q * F.vt3[donor], kdt, rkdt);
+      } else if (ok) {
+        double py = 0., pz = 0.;
+        if (f > 0) {
+          sy = sy + (D[(f - 1) * 5 + 2] - du0[2 * cs + f - 1]) * vol;
+          sz = sz + (D[(f - 1) * 5 + 3] - du0[3 * cs + f - 1]) * vol;
+          py = -sy;
+          pz = -sz;
+        }
+        ty = ty + vdiv(py, kdt, rkdt);
+        tz = tz + vdiv(pz, kdt, rkdt);
+      }
+      step_set(at(IVY, f), ty, w1s, w2dt, first);
+      step_set(at(IVZ, f), tz, w1s, w2dt, first);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kThreads)
+    vic_finish_c_kernel(const BlockDev* __restrict__ tab, StageParams p) {
+  const BlockDev& B = tab[blockIdx.y];
+  if (!B.implicit) return;
+  const VicScratch S = vic_scratch(B);
+  const int ng = B.ng, nc1 = B.nc1, n = nc1 - 2 * ng;
+  const size_t plane = (size_t)nc1 * B.nc2 * B.nc3;
+  const real* uin = static_cast<const real*>(B.buf[p.in]);
+  const real* u0 = static_cast<const real*>(B.buf[p.u0]);
+  real* uout = static_cast<real*>(B.buf[p.out]);
+  const double grav = B.grav1;
+  const double vol = B.dx3 * (B.dx2 * B.dx1);
+  const double rvol = 1. / vol;
+  const double* x1v = B.x1v + ng;
+  const double* x1f = B.x1f + ng;
+  const size_t cs = S.cells;
+  const bool wood = n >= 3;
+  const bool partial = B.implicit == 1;
+  const real w0 = real(p.w0), w1 = real(p.w1), w2 = real(p.w2);
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < S.cells;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const size_t col = e / n;
+    const int i = (int)(e - col * n);
+    const double* D = S.D + col * n * 5;
+    const double* du = S.du + col * n;
+    const double* du0 = S.du0 + col * n;
+    const bool ok = vfinite(D[0]);
+    double d[5];
+    if (ok) {
+      const FinishCol F = finish_col(S, col, n);
+      d[0] = du[i] + F.mdn[i];
+      d[1] = D[i * 5 + 1];
+      if (!partial) {
+        d[2] = D[i * 5 + 2];
+        d[3] = D[i * 5 + 3];
+      } else {
+        // vic_tangential_momentum_column: the face below adds its transfer,
+        // then the face above takes its own (a zero transfer is skipped)
+        const double* vt[2] = {F.vt2, F.vt3};
+#pragma unroll
+        for (int t = 0; t < 2; ++t) {
+          double a = du[(2 + t) * cs + i];
+          if (i > 0) {
+            const double q = F.mq[i];
+            const double pm = q * vt[t][q > 0 ? i - 1 : i];
+            if (pm != 0) a += vdiv(pm, vol, rvol);
+          }
+          if (i + 1 < n) {
+            const double q = F.mq[i + 1];
+            const double pm = q * vt[t][q > 0 ? i : i + 1];
+            if (pm != 0) a -= vdiv(pm, vol, rvol);
+          }
+          d[2 + t] = a;
+        }
+      }
+      const double projected = vdiv(F.mM[i] - F.mM[i + 1], vol, rvol);
+      const double ph = -grav * x1v[i];
+      const double pw = ph * (D[i * 5] - du0[i] - projected);
+      const double dp_lo = -grav * (x1f[i] - x1v[i]);
+      const double dp_hi = -grav * (x1f[i + 1] - x1v[i]);
+      const double mv_lo = F.mq[i] - F.mM[i], mv_hi = F.mq[i + 1] - F.mM[i + 1];
+      const double cw = vdiv(-(dp_hi * mv_hi - dp_lo * mv_lo), vol, rvol);
+      double e4 = D[i * 5 + 4] + (pw + cw);
+      if (wood) {
+        double wt[3];
+        int i0;
+        vic_slope_tab(B, n, i, wt, &i0);
+        VicK K = vic_krows(B, n, i);
+        auto mv = [&](int k) { return (du[k] + F.mdn[k]) - du0[k]; };
+        double sl = wt[0] * mv(i0);
+        sl += wt[1] * mv(i0 + 1);
+        sl += wt[2] * mv(i0 + 2);
+        double wk = K.gv * sl;
+        auto rw = [&](int k) { return D[k * 5] - du0[k]; };
+        double s = K.mid * rw(i);
+        if (i >= 1) s += K.lo * rw(i - 1);
+        if (i <= n - 2) s += K.hi * rw(i + 1);
+        if (i == 0) s += K.t0 * rw(2);
+        if (i == n - 1) s += K.t1 * rw(n - 3);
+        wk -= s;
+        e4 += wk;
+      }
+      d[4] = e4;
+    } else {
+#pragma unroll
+      for (int v = 0; v < 5; ++v) d[v] = du0[v * cs + i];
+    }
+    const size_t c = vic_row(B, col) * nc1 + ng + i;
+#pragma unroll
+    for (int v = 0; v < NHYDRO; ++v) {
+      const size_t q = v * plane + c;
+      uout[q] = w0 * u0[q] + w1 * uin[q] + w2 * real(d[v]);
+    }
+  }
+}
