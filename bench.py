@@ -126,7 +126,7 @@ def parse():
                          "float64 assembles and solves them in FP64 (default: "
                          "float32 for ensemble and serving, the deck's for "
                          "the others)")
-    ap.add_argument("--implicit-solve", choices=["refined", "direct"],
+    ap.add_argument("--implicit-solve", choices=["refined", "direct", "fp32"],
                     default=None,
                     help="the solve of float32-assembled implicit blocks: "
                          "refined (FP32 sweeps corrected with FP64 residuals, "
@@ -184,12 +184,27 @@ def implicit_solve(opts):
     ic = opts.hydro().icorr
     if ic is None:
         return None
-    if (opts.hydro().precision == "float32" and ic.precision == "float32"
-            and opts.implicit_solve == "refined"):
-        return ("refined to the FP64 solution: FP32 block-Thomas sweeps, "
-                f"{opts.implicit_corrections} corrections from FP64 residuals, "
-                "the FP64 solve for columns that do not converge")
+    if opts.hydro().precision == "float32" and ic.precision == "float32":
+        if opts.implicit_solve == "refined":
+            return ("refined to the FP64 solution: FP32 block-Thomas sweeps, "
+                    f"{opts.implicit_corrections} corrections from FP64 "
+                    "residuals, the FP64 solve for columns that do not converge")
+        if opts.implicit_solve == "fp32":
+            return ("FP32 (the reference's FP32 implicit compute): the FP32 "
+                    "block-Thomas sweep and its Woodbury step, the FP64 solve "
+                    "for columns whose sweep fails")
     return "direct FP64"
+
+
+def solve_label(opts):
+    """A short name of the implicit solve the deck runs."""
+    ic = opts.hydro().icorr
+    if ic is None:
+        return "none"
+    if opts.hydro().precision == "float32" and ic.precision == "float32":
+        return {"refined": "refined to the FP64 solution", "fp32": "FP32",
+                "direct": "FP64"}[opts.implicit_solve]
+    return "FP64"
 
 
 def config_of(opts, workload, args, nranks):
@@ -613,7 +628,7 @@ def ensemble_config(members, precision, nranks):
     return {"workload": f"ensemble of {len(members)} Straka-type members "
                         f"(nx2 in 128..512, nx1 in 32..128, 50 m, seed "
                         f"{ENSEMBLE_SEED}), lmars+weno5+rk3+VIC, {precision} "
-                        "bulk, implicit solve to the FP64 solution",
+                        f"bulk, implicit solve {solve_label(members[0][0])}",
             "implicit_assembly": ip,
             "implicit_solve": implicit_solve(members[0][0]),
             "members": len(members), "cells": cells, "precision": precision,
@@ -852,7 +867,7 @@ def serving_config(reqs, nranks, budget=None):
                         f"{SERVE_SEED}), (nx2, nx3, nx1) in {{64,96,128}}^2 x "
                         f"{{64,96}} at 50 m, {reqs[0].steps} RK3 steps each, "
                         f"lmars+weno5+rk3+VIC, {reqs[0].options.hydro().precision} "
-                        "bulk, implicit solve to the FP64 solution",
+                        f"bulk, implicit solve {solve_label(reqs[0].options)}",
             "requests": len(reqs), "steps_per_request": reqs[0].steps,
             "implicit_assembly": reqs[0].options.hydro().icorr.precision,
             "implicit_solve": implicit_solve(reqs[0].options),

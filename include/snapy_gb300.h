@@ -222,9 +222,16 @@ int sg_kernel_times(sg_handle* h, double* ms, int64_t* launches);
  * accumulating in FP64.  A column whose FP32 factorisation fails, or whose
  * last correction leaves an estimated error above 2^-44 of its solution,
  * takes the direct FP64 solve.  corrections 0 runs the direct FP64 solve for
- * every column (the FP64 blocks' solve, bitwise).  FP64 blocks always run
- * the direct solve.  The forms agree to FP64 roundoff of the solution.  Not
- * inside a stream capture; graphs captured before must be captured again. */
+ * every column (the FP64 blocks' solve, bitwise).  corrections -1 is the
+ * reference's own FP32 compute of the implicit solve (PrecisionPolicy's
+ * kImplicit row in FP32, src/mesh/precision_policy.hpp:31-71): the FP32
+ * sweep and its Woodbury step, no corrections, the direct FP64 solve for
+ * the columns whose FP32 sweep fails (the reference's FP64 retry,
+ * integration/implicit-fallback-fp64).  FP64 blocks always run the direct
+ * solve.  The refined and direct forms agree to FP64 roundoff of the
+ * solution; the FP32 form to FP32 roundoff times the condition of the
+ * column.  Not inside a stream capture; graphs captured before must be
+ * captured again. */
 int sg_set_solve(sg_handle* h, int32_t corrections);
 /* per block, the running count of columns the refined solve left to the
  * direct FP64 solve (ImplicitHydroImpl's "implicit.fp64_columns" monitor,

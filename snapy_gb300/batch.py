@@ -374,6 +374,8 @@ class Batch:
 
     def set_solve(self, corrections: int) -> None:
         """The solve of implicit-precision float32 blocks: refined with that
-        many FP64-residual corrections (1 to 3; 2 by default), or 0 for the
-        direct FP64 solve of every column."""
+        many FP64-residual corrections (1 to 3; 2 by default), 0 for the
+        direct FP64 solve of every column, or -1 for the FP32 solve (the
+        reference's FP32 compute: the sweep alone, the FP64 solve for the
+        columns whose sweep fails)."""
         _lib.check(self.L.sg_set_solve(self.h, int(corrections)), "sg_set_solve")

@@ -345,8 +345,8 @@ extern "C" {
 const char* sg_last_error(void) { return g_err.c_str(); }
 
 int sg_set_solve(sg_handle* h, int32_t corrections) {
-  if (!h || corrections < 0 || corrections > 3)
-    return fail(SG_ERR_ARG, "sg_set_solve: %d corrections (0 to 3)",
+  if (!h || corrections < -1 || corrections > 3)
+    return fail(SG_ERR_ARG, "sg_set_solve: %d corrections (-1 to 3)",
                 corrections);
   h->refine = h->any_f32 ? corrections : 0;
   return 0;
@@ -1135,7 +1135,7 @@ int sg_stage(sg_handle* h, int32_t stage, const double* dt_dev,
     // residual and a correction per correction
     // (a wide batch's finish is three launches)
     launches += 3 + (h->wide ? 2 : 0) + (h->vic_kinds == 3 ? 1 : 0) +
-                (h->refine ? 1 + 2 * h->refine : 0);
+                (h->refine > 0 ? 1 + 2 * h->refine : (h->refine < 0 ? 2 : 0));
   }
   if (h->scalars) {
     // the passive scalars on the stage's mass flux: face fluxes, update

@@ -2189,9 +2189,9 @@ extern "C" int SG_NAME(sg_launch_vic)(const BlockDev* tab, StageParams p,
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return (int)e;
   if (ev) cudaEventRecord(ev[0], stream);
-  // the refined solve of implicit-precision float32 blocks (FP32 sweeps,
-  // FP64 residuals); the columns it does not converge are left to the
-  // direct solve
+  // implicit-precision float32 blocks: the FP32 sweep, then the refined
+  // solve's corrections (FP64 residuals), or (refine < 0) the FP32 solve's
+  // Woodbury step alone; the columns either leaves are solved directly
   int gs = (int)((max_cols + kVicCols - 1) / kVicCols);
   if (p.refine) {
     int gr = (int)((max_cells + kThreads - 1) / kThreads);
@@ -2199,6 +2199,11 @@ extern "C" int SG_NAME(sg_launch_vic)(const BlockDev* tab, StageParams p,
     const size_t cw = (max_cols + kCorrCols - 1) / kCorrCols;  // warps
     const int gc = (int)((cw + kCorrWarps - 1) / kCorrWarps);
     vic_solve32_kernel<<<dim3(gs, p.nblock), 32, 0, stream>>>(tab, p);
+    if (p.refine < 0) {  // the FP32 solve: its Woodbury step, no corrections
+      const size_t threads = max_cols * 32;
+      const int gw = (int)((threads + kThreads - 1) / kThreads);
+      vic_woodbury32_kernel<<<dim3(gw, p.nblock), kThreads, 0, stream>>>(tab, p);
+    }
     for (int k = 1; k <= p.refine; ++k) {
       vic_residual_kernel<<<dim3(gr, p.nblock), kThreads, 0, stream>>>(tab, p, k);
       vic_correct32_kernel<<<dim3(gc, p.nblock), 32 * kCorrWarps, 0, stream>>>(

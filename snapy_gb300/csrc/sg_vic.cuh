@@ -1829,6 +1829,48 @@ __global__ void __launch_bounds__(32 * kCorrWarps)
   if (valid && k == 0) F.mask[cc] = (conv && !bad) ? 0 : 1;
 }
 
+// implicit-solve fp32 (the reference's FP32 compute of the implicit solve,
+// the PrecisionPolicy's kImplicit row in FP32): after the FP32 sweep, the
+// Woodbury step of every column the sweep solved, in FP64 on its widened
+// FP32 solution, one warp per column (coalesced over the 5 n values); a
+// column whose sweep failed, or whose result is not finite, stays masked for
+// the direct FP64 solve (the reference's FP64 retry of the failed columns)
+__global__ void __launch_bounds__(kThreads)
+    vic_woodbury32_kernel(const BlockDev* __restrict__ tab, StageParams p) {
+  const BlockDev& Bk = tab[blockIdx.y];
+  if (!Bk.implicit || !Bk.implicit_f32) return;
+  const VicScratch S = vic_scratch(Bk);
+  const int n = Bk.nc1 - 2 * Bk.ng;
+  const VicScratch32 F = vic_scratch32(Bk, S, n);
+  const size_t col = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (col >= F.ncol || F.mask[col]) return;  // uniform over the warp
+  double* D = S.D + col * n * 5;
+  const double* Z0 = S.Z0 + col * n * 5;
+  const double* Z1 = S.Z1 + col * n * 5;
+  if (n < 3) return;  // no Woodbury step; the sweep screened the solution
+  const double dtc = p.w2 * p.dt[blockIdx.y];
+  VicK K0 = vic_krows(Bk, n, 0), K1 = vic_krows(Bk, n, n - 1);
+  const double k0 = -K0.t0 / dtc, k1 = -K1.t1 / dtc;
+  const int a0 = 2, a1 = n - 3;
+  const double m00 = 1. + k0 * Z0[a0 * 5], m01 = k0 * Z1[a0 * 5];
+  const double m10 = k1 * Z0[a1 * 5], m11 = 1. + k1 * Z1[a1 * 5];
+  const double r0 = k0 * D[a0 * 5], r1 = k1 * D[a1 * 5];
+  const double det = m00 * m11 - m01 * m10;
+  const double al0 = (m11 * r0 - m01 * r1) / det;
+  const double al1 = (m00 * r1 - m10 * r0) / det;
+  __syncwarp();  // every lane has read the weights' inputs
+  bool f = true;
+  for (int e = lane; e < 5 * n; e += 32) {
+    double d = D[e];
+    d -= Z0[e] * al0;
+    d -= Z1[e] * al1;
+    D[e] = d;
+    f = f && vfinite(d);
+  }
+  if (!__all_sync(0xffffffffu, f) && lane == 0) F.mask[col] = 1;
+}
+
 // s_h + s_l += t d in float-float arithmetic, t and d floats: the product
 // split exactly by an FMA (the two-product of Dekker's method), the sum by
 // Knuth's two-sum; the low parts gather in s_l.  Every step is a single

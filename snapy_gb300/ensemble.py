@@ -19,7 +19,7 @@ import torch
 
 from .batch import Batch
 from .meshblock import block_of, scheme_of
-from .options import DeckError, MeshBlockOptions
+from .options import DeckError, MeshBlockOptions, shared_solve
 
 
 class Ensemble:
@@ -43,7 +43,7 @@ class Ensemble:
         self.dtype = dtype
         self.batch = Batch(schemes[0], [block_of(m) for m in self.members],
                            self.device, dtype)
-        k = min(m.solve_corrections() for m in self.members)
+        k = shared_solve(m.solve_corrections() for m in self.members)
         if k != 2:
             self.batch.set_solve(k)
         self.nstage = len(schemes[0]["wght"])

@@ -405,13 +405,29 @@ def _scalar_names(node, op) -> List[str]:
     return names
 
 
+def shared_solve(ks) -> int:
+    """The one solve form of blocks batched in a handle, from their decks'
+    sg_set_solve arguments: the direct FP64 solve if any block asks for it,
+    else the refined solve with the fewest corrections any block asks for,
+    else the FP32 solve."""
+    ks = list(ks)
+    if 0 in ks:
+        return 0
+    pos = [k for k in ks if k > 0]
+    return min(pos) if pos else -1
+
+
 class MeshBlockOptions:
     """The deck of one block (reference MeshBlockOptionsImpl)."""
 
     def solve_corrections(self) -> int:
         """sg_set_solve's argument for this deck: 0 for the direct FP64
-        solve, else the refined solve's corrections."""
-        return 0 if self.implicit_solve == "direct" else self.implicit_corrections
+        solve, -1 for the FP32 solve, else the refined solve's corrections."""
+        if self.implicit_solve == "direct":
+            return 0
+        if self.implicit_solve == "fp32":
+            return -1
+        return self.implicit_corrections
 
     def __init__(self):
         self._coord = CoordinateOptions()
@@ -425,8 +441,9 @@ class MeshBlockOptions:
         self.autotune = True
         # integration/implicit-solve (no counterpart in the reference): the
         # solve of implicit-precision float32 blocks, "refined" (FP32 sweeps
-        # corrected with FP64 residuals to the FP64 solution) or "direct"
-        # (the FP64 solve of every column)
+        # corrected with FP64 residuals to the FP64 solution), "direct" (the
+        # FP64 solve of every column) or "fp32" (the reference's own FP32
+        # compute: the FP32 sweep alone, the FP64 retry of failed columns)
         self.implicit_solve = "refined"
         self.implicit_corrections = 2  # FP64-residual corrections (1 to 3)
         # scalar/nvar, scalar/names: passive scalars (ScalarOptionsImpl,
@@ -482,9 +499,9 @@ class MeshBlockOptions:
         op.execution_strict = bool(intg.get("execution-strict", False))
         op.autotune = bool(intg.get("autotune", True))
         op.implicit_solve = str(intg.get("implicit-solve", "refined"))
-        if op.implicit_solve not in ("refined", "direct"):
-            raise DeckError("integration/implicit-solve must be refined or "
-                            f"direct, got '{op.implicit_solve}'")
+        if op.implicit_solve not in ("refined", "direct", "fp32"):
+            raise DeckError("integration/implicit-solve must be refined, "
+                            f"direct or fp32, got '{op.implicit_solve}'")
         op.implicit_corrections = int(intg.get("implicit-corrections", 2))
         if not 1 <= op.implicit_corrections <= 3:
             raise DeckError("integration/implicit-corrections must be 1 to 3, "

@@ -38,7 +38,7 @@ import torch
 from . import _lib
 from .batch import _DT, _stream, fill_base
 from .meshblock import block_of, scheme_of
-from .options import DeckError, MeshBlockOptions
+from .options import DeckError, MeshBlockOptions, shared_solve
 
 
 @dataclass
@@ -169,7 +169,7 @@ class _Handle:
                                              sl.scratch.numel() * 8),
                            "sg_bind_scratch")
         _lib.check(L.sg_set_current(h, 0), "sg_set_current")
-        k = min(sl.req.options.solve_corrections() for sl in slots)
+        k = shared_solve(sl.req.options.solve_corrections() for sl in slots)
         if k != 2:
             _lib.check(L.sg_set_solve(h, k), "sg_set_solve")
         self.dt = torch.zeros(n, dtype=torch.float64, device=device)

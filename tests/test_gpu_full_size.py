@@ -10,9 +10,11 @@
 * FP32 bulk against the FP64 path at the served horizon, 200 RK3 steps, on
   the same dt sequence: the Straka block (FP32 with the implicit solve
   refined to FP64) and a 3-D convection request of 64^3 cells (the serving
-  trace's smallest size), relative L2 <= 1e-5 per field of the totals.  The
-  FP64 GPU path stands in for the oracle over those lengths: it is bitwise
-  the oracle's in the tests above.
+  trace's smallest size), relative L2 <= 1e-5 per field of the totals; and
+  the same with the FP32 implicit solve (the reference's own FP32 compute),
+  whose error is recorded against a looser bar.  The FP64 GPU path stands in
+  for the oracle over those lengths: it is bitwise the oracle's in the tests
+  above.
 """
 import numpy as np
 import pytest
@@ -116,16 +118,27 @@ def _served_horizon(cuda, opts64, opts32, w, steps):
     return rel_l2(b32.total_u(v32).cpu().numpy(), v64["hydro_u"].cpu().numpy())
 
 
-def test_straka_512x128_fp32_at_the_served_horizon(cuda):
+# the FP32 implicit solve (the reference's own FP32 compute) is not held to
+# the 1e-5 bar: its error at the served horizon is recorded against 2e-4
+BAR = {"refined": FP32_TOL, "fp32": 2e-4}
+
+
+@pytest.mark.parametrize("solve", ["refined", "fp32"])
+def test_straka_512x128_fp32_at_the_served_horizon(cuda, solve):
+    """FP32 with the implicit solve refined to FP64 (within 1e-5 of the FP64
+    path), and with the FP32 solve (7.3e-5 measured)."""
     o64 = sg.MeshBlockOptions.from_yaml(STRAKA)
     o32 = sg.MeshBlockOptions.from_yaml(STRAKA)
     o32.hydro().precision = "float32"
-    o32.hydro().icorr.precision = "float32"  # the refined solve
+    o32.hydro().icorr.precision = "float32"
+    o32.implicit_solve = solve
     err = _served_horizon(cuda, o64, o32, problems.straka(o64, "cpu"), 200)
-    assert err.max() <= FP32_TOL, err
+    print(f"\nStraka 512x128 FP32 ({solve} solve) vs FP64 after 200 steps: {err}")
+    assert err.max() <= BAR[solve], err
 
 
-def test_convection_64cubed_fp32_at_the_served_horizon(cuda):
+@pytest.mark.parametrize("solve", ["refined", "fp32"])
+def test_convection_64cubed_fp32_at_the_served_horizon(cuda, solve):
     def conv(prec):
         o = sg.MeshBlockOptions.from_yaml(CONV)
         c = o.coord()
@@ -134,8 +147,10 @@ def test_convection_64cubed_fp32_at_the_served_horizon(cuda):
         o.hydro().precision = prec
         if prec == "float32":
             o.hydro().icorr.precision = "float32"
+            o.implicit_solve = solve
         return o
     o64, o32 = conv("float64"), conv("float32")
     err = _served_horizon(cuda, o64, o32,
                           problems.convection3d(o64, "cpu", seed=20261205), 200)
-    assert err.max() <= FP32_TOL, err
+    print(f"\n64^3 convection FP32 ({solve} solve) vs FP64 after 200 steps: {err}")
+    assert err.max() <= BAR[solve], err
