@@ -42,6 +42,47 @@ __device__ __forceinline__ double widen_exact(float f) {
   return __longlong_as_double((long long)widen_bits(__float_as_uint(f)));
 }
 
+// a double rounded to the nearest float (ties to even) with integer
+// operations only, for the same reason: the conversion instruction runs on
+// the FP64 pipe.  Overflow gives infinity, results below the normal range
+// are rounded to float subnormals (or zero), NaNs stay NaNs (quiet, the
+// payload's top bits kept)
+__device__ __forceinline__ unsigned int narrow_bits(unsigned long long d) {
+  const unsigned int sgn = (unsigned int)(d >> 63) << 31;
+  const int e = (int)((d >> 52) & 0x7ff);
+  const unsigned long long m = d & 0xfffffffffffffull;
+  if (e == 0x7ff)
+    return sgn | 0x7f800000u | (m ? (0x400000u | (unsigned int)(m >> 29)) : 0u);
+  int ef = e - 1023 + 127;  // the float's biased exponent
+  if (ef >= 255) return sgn | 0x7f800000u;
+  const unsigned long long M = m | (e ? (1ull << 52) : 0ull);
+  int sh = 29;  // the bits a normal float drops
+  if (ef <= 0) {  // a float subnormal, or zero
+    sh = 30 - ef;
+    if (sh > 54) return sgn;
+    ef = 0;
+  }
+  unsigned long long keep = M >> sh;
+  const unsigned long long rem = M & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+  if (rem > half || (rem == half && (keep & 1))) keep += 1;
+  // a normal keeps its implicit bit at 23; a carry out of the mantissa bumps
+  // the exponent (254 -> infinity)
+  return sgn | (ef ? ((unsigned int)ef << 23) + (unsigned int)(keep - (1ull << 23))
+                   : (unsigned int)keep);
+}
+
+__device__ __forceinline__ float narrow_exact(double x) {
+  return __uint_as_float(narrow_bits((unsigned long long)__double_as_longlong(x)));
+}
+
+// a double in the storage type (to a float through the integer pipes)
+template <typename T>
+__device__ __forceinline__ T as_real(double x);
+template <>
+__device__ __forceinline__ double as_real<double>(double x) { return x; }
+template <>
+__device__ __forceinline__ float as_real<float>(double x) { return narrow_exact(x); }
+
 // a value of the storage type in FP64 (a float through the integer pipes)
 __device__ __forceinline__ double as_f64(double x) { return x; }
 __device__ __forceinline__ double as_f64(float x) { return widen_exact(x); }

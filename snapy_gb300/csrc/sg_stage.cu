@@ -687,12 +687,12 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
 
   // (5) the x2 covariance row, then the x2 wall faces
   if (has2) {
+    const real s2 = real(B.dx1 * B.dx1 / 12.);
     for (int idx = threadIdx.x; idx < (ntj + 1) * nx1; idx += blockDim.x) {
       const int jf = idx / nx1, ii = idx - jf * nx1, i = il + ii;
       if (L.cov) {
         const double* x1v = B.x1v;
         real dx1 = real(x1v[i + 1] - x1v[i - 1]);
-        real s2 = real(B.dx1 * B.dx1 / 12.);
         const real* rho = COV + jf * nc1;
         const real* h = COV + cstride + jf * nc1;
         const real* un = COV + 2 * cstride + jf * nc1;

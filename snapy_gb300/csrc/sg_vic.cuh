@@ -207,6 +207,23 @@ __device__ __forceinline__ void vic_prim(const real* u, size_t plane,
   cons2prim<double>(uc, w, gammad);
 }
 
+// the same primitives in FP32 (FP32 assembly): the state in FP32, the base
+// rounded to FP32 and added to the anomaly in FP32
+__device__ __forceinline__ void vic_prim32(const real* u, size_t plane,
+                                           size_t cell, float gammad,
+                                           float* w, const double* base,
+                                           int nc1) {
+  float uc[NHYDRO];
+#pragma unroll
+  for (int v = 0; v < NHYDRO; ++v) uc[v] = (float)u[v * plane + cell];
+  if (base) {
+    const int i = (int)(cell % nc1);
+    uc[IDN] = narrow_exact(base_rho(base, nc1)[i]) + uc[IDN];
+    uc[IPR] = narrow_exact(base_e(base, nc1)[i]) + uc[IPR];
+  }
+  cons2prim<float>(uc, w, gammad);
+}
+
 // the corrected-PE slope weights of layer k of n (centres x)
 // the same weights from the block's x1 geometry table (computed once, with
 // these operations)
@@ -252,16 +269,36 @@ __device__ __forceinline__ VicK vic_krows(const BlockDev& B, int n, int k) {
 // state's blocks, exact in FP32 and in the FP64 copies the residuals of the
 // refined solve read).  The FP64 instantiation performs the reference's
 // operations in its order.
+// a block's constants of the assembly in the compute type, formed once per
+// launch (the cell loop reloads what it reads from the block table)
+template <typename T>
+struct AsmConst {
+  T grav, gm1, gm1r, area, vol, half_inv_vol, rvol, rdt, dtc, gammad;
+  __device__ AsmConst(const BlockDev& B, double dtc_) {
+    gammad = T(B.gammad);
+    grav = T(B.grav1);
+    gm1 = T(B.gammad - 1.);
+    gm1r = T(0.5 * (B.gammad + B.gammad) - 1.);
+    area = T(B.dx3 * B.dx2);
+    vol = T(B.dx3 * (B.dx2 * B.dx1));
+    half_inv_vol = T(0.5) / vol;
+    rvol = T(1.) / vol;
+    dtc = T(dtc_);
+    rdt = T(1.) / dtc;
+  }
+};
+
 template <typename T>
 __device__ __forceinline__ void vic_assemble_cell(const BlockDev& B,
                                                   const VicScratch& S,
                                                   const real* uin,
                                                   double dtc, size_t e,
-                                                  bool f32copy) {
+                                                  bool f32copy,
+                                                  const AsmConst<T>& kc) {
   const int ng = B.ng, nc1 = B.nc1, n = nc1 - 2 * ng;
   const size_t plane = (size_t)nc1 * B.nc2 * B.nc3;
-  const T grav = T(B.grav1), gm1 = T(B.gammad - 1.);
-  const T area = T(B.dx3 * B.dx2), vol = T(B.dx3 * (B.dx2 * B.dx1));
+  const T grav = kc.grav, gm1 = kc.gm1;
+  const T area = kc.area, vol = kc.vol;
   const double* x1v = B.x1v + ng;
   const double* x1f = B.x1f + ng;
   const bool wood = n >= 3;
@@ -269,28 +306,36 @@ __device__ __forceinline__ void vic_assemble_cell(const BlockDev& B,
   const size_t col = e / n;
   const size_t jrow = vic_row(B, col);
   const size_t base = jrow * nc1 + ng;  // padded cell of layer 0
-  double wd[3][5];
-  vic_prim(uin, plane, base + i - 1, B.gammad, wd[0], B.base, nc1);
-  vic_prim(uin, plane, base + i, B.gammad, wd[1], B.base, nc1);
-  vic_prim(uin, plane, base + i + 1, B.gammad, wd[2], B.base, nc1);
   T wl[5], wr[5], wn[5];
+  if constexpr (sizeof(T) == sizeof(float)) {
+    // FP32 assembly: the primitives in FP32 from the FP32 state and the
+    // base rounded to FP32 (the blocks are FP32 either way)
+    vic_prim32(uin, plane, base + i - 1, kc.gammad, wl, B.base, nc1);
+    vic_prim32(uin, plane, base + i, kc.gammad, wr, B.base, nc1);
+    vic_prim32(uin, plane, base + i + 1, kc.gammad, wn, B.base, nc1);
+  } else {
+    double wd[3][5];
+    vic_prim(uin, plane, base + i - 1, B.gammad, wd[0], B.base, nc1);
+    vic_prim(uin, plane, base + i, B.gammad, wd[1], B.base, nc1);
+    vic_prim(uin, plane, base + i + 1, B.gammad, wd[2], B.base, nc1);
 #pragma unroll
-  for (int v = 0; v < 5; ++v) {
-    wl[v] = T(wd[0][v]);
-    wr[v] = T(wd[1][v]);
-    wn[v] = T(wd[2][v]);
+    for (int v = 0; v < 5; ++v) {
+      wl[v] = T(wd[0][v]);
+      wr[v] = T(wd[1][v]);
+      wn[v] = T(wd[2][v]);
+    }
   }
   T Jp[25], Jc[25], Jn[25], Am[25], Ap[25];
-  const T gm1r = T(0.5 * (B.gammad + B.gammad) - 1.);
+  const T gm1r = kc.gm1r;
   vflux_jacobian(Jp, gm1, wl);
   vflux_jacobian(Jc, gm1, wr);
   vabs_jacobian(Am, gm1r, wl, wr);
   vflux_jacobian(Jn, gm1, wn);
   vabs_jacobian(Ap, gm1r, wr, wn);
-  const T half_inv_vol = T(0.5) / vol;
-  const T rvol = T(1.) / vol;
-  const T lower = vdiv(T(0.5) * area * T(x1v[i] - x1f[i]), vol, rvol);
-  const T upper = vdiv(T(0.5) * area * T(x1f[i + 1] - x1v[i]), vol, rvol);
+  const T half_inv_vol = kc.half_inv_vol;
+  const T rvol = kc.rvol;
+  const T lower = vdiv(T(0.5) * area * as_real<T>(x1v[i] - x1f[i]), vol, rvol);
+  const T upper = vdiv(T(0.5) * area * as_real<T>(x1f[i + 1] - x1v[i]), vol, rvol);
   T a[25], b[25], c[25];
 #pragma unroll
   for (int r = 0; r < 5; ++r)
@@ -303,7 +348,7 @@ __device__ __forceinline__ void vic_assemble_cell(const BlockDev& B,
       b[k] = -(Am[k] + Jp[k]) * area * half_inv_vol;
       c[k] = -(Ap[k] - Jn[k]) * area * half_inv_vol;
     }
-  const T rdt = T(1.) / T(dtc);
+  const T rdt = kc.rdt;
 #pragma unroll
   for (int r = 0; r < 5; ++r) a[r * 5 + r] += rdt;
 #pragma unroll
@@ -360,12 +405,12 @@ __device__ __forceinline__ void vic_assemble_cell(const BlockDev& B,
         cT[r * 2 + k] = c[rows[r] * 5 + 2 + k];
       }
     }
-    auto fold = [&](T* blk, const T* tb, int j, const double* wj) {
+    auto fold = [&](T* blk, const T* tb, int j, const T* wj) {
       const double* dj = S.du + col * n + j;  // row v at dj[v * cells]
       const T drho = T(dj[0]);
 #pragma unroll
       for (int k = 0; k < 2; ++k) {
-        const T v = T(wj[2 + k]);
+        const T v = wj[2 + k];
         const T qt = T(dj[(size_t)(2 + k) * S.cells]) - v * drho;
         if (v != T(0.))
 #pragma unroll
@@ -375,20 +420,20 @@ __device__ __forceinline__ void vic_assemble_cell(const BlockDev& B,
           for (int r = 0; r < 3; ++r) rc[r] = rc[r] + tb[r * 2 + k] * qt;
       }
     };
-    fold(a3, aT, i, wd[1]);
-    if (i > 0) fold(b3, bT, i - 1, wd[0]);
-    if (i < n - 1) fold(c3, cT, i + 1, wd[2]);
+    fold(a3, aT, i, wr);
+    if (i > 0) fold(b3, bT, i - 1, wl);
+    if (i < n - 1) fold(c3, cT, i + 1, wn);
   }
   if (wood) {
     VicK K = vic_krows(B, n, i);
     if (partial) {
-      a3[6] -= vdiv(T(K.mid), T(dtc), rdt);
-      b3[6] -= vdiv(T(K.lo), T(dtc), rdt);
-      c3[6] -= vdiv(T(K.hi), T(dtc), rdt);
+      a3[6] -= vdiv(as_real<T>(K.mid), kc.dtc, rdt);
+      b3[6] -= vdiv(as_real<T>(K.lo), kc.dtc, rdt);
+      c3[6] -= vdiv(as_real<T>(K.hi), kc.dtc, rdt);
     } else {
-      a[20] -= vdiv(T(K.mid), T(dtc), rdt);
-      b[20] -= vdiv(T(K.lo), T(dtc), rdt);
-      c[20] -= vdiv(T(K.hi), T(dtc), rdt);
+      a[20] -= vdiv(as_real<T>(K.mid), kc.dtc, rdt);
+      b[20] -= vdiv(as_real<T>(K.lo), kc.dtc, rdt);
+      c[20] -= vdiv(as_real<T>(K.hi), kc.dtc, rdt);
     }
     // du[IPR] -= (K du0[IDN])_i : the IDN row is read only (FP64 always)
     const double* dn = S.du + col * n;
@@ -451,15 +496,19 @@ __global__ void __launch_bounds__(kThreads)
   const VicScratch S = vic_scratch(B);
   const real* uin = static_cast<const real*>(B.buf[p.in]);
   const double dtc = p.w2 * p.dt[blockIdx.y];
-  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < S.cells;
-       e += (size_t)gridDim.x * blockDim.x) {
 #ifdef SG_REAL_IS_FLOAT
-    if (B.implicit_f32)
-      vic_assemble_cell<float>(B, S, uin, dtc, e, p.refine != 0);
-    else
-#endif
-      vic_assemble_cell<double>(B, S, uin, dtc, e, false);
+  if (B.implicit_f32) {
+    const AsmConst<float> kc(B, dtc);
+    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < S.cells;
+         e += (size_t)gridDim.x * blockDim.x)
+      vic_assemble_cell<float>(B, S, uin, dtc, e, p.refine != 0, kc);
+    return;
   }
+#endif
+  const AsmConst<double> kc(B, dtc);
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < S.cells;
+       e += (size_t)gridDim.x * blockDim.x)
+    vic_assemble_cell<double>(B, S, uin, dtc, e, false, kc);
 }
 
 // ludcmp<double, 5, Implicit> on a row-major 5x5 in shared memory
