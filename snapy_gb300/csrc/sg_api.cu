@@ -225,6 +225,7 @@ struct sg_handle {
   int wide_auto = 0;  // that rule's own answer (finish form 0)
   bool implicit = false;
   int vic_kinds = 0;  // bit 0: a block with the full 5x5 matrix, bit 1: 3x3
+  bool ref32 = false;  // an FP32 block under gravity: base_ref_kernel runs
   int refine = 0;  // corrections of the refined implicit solve (0: direct)
   int any_f32 = 0;  // a block assembles its implicit blocks in FP32
   size_t max_icells = 0, max_icols = 0;
@@ -431,6 +432,7 @@ int sg_autotune(sg_handle* h, int32_t reps, int32_t* tj_out,
     p.max_nc1 = h->max_nc1;
     p.visc3 = h->visc3;
     p.vic_kinds = h->vic_kinds;
+    p.ref32 = h->ref32;
     auto stage = [&]() -> int {
       p.ntile = h->ntile;
       int r = 0;
@@ -681,10 +683,14 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
       h->refine = 2;
     }
     B.x1tab = nullptr;
+    B.refb = nullptr;
     if (d.grav1 != 0.) {
       const int nx1 = d.nc1 - 2 * d.ng;
+      // FP32: the base reference table follows the geometry table
+      const bool r32 = scheme->dtype == SG_F32;
+      const size_t nref = r32 ? 1 + 4 * ((size_t)d.nc1 + 1) : 0;
       double* t = nullptr;
-      cudaError_t e = cudaMalloc(&t, sizeof(double) * 6 * (size_t)nx1);
+      cudaError_t e = cudaMalloc(&t, sizeof(double) * (6 * (size_t)nx1 + nref));
       if (e == cudaSuccess) {
         h->x1tabs.push_back(t);
         x1tab_kernel<<<(nx1 + 127) / 128, 128>>>(d.x1f, d.x1v, d.ng, nx1,
@@ -698,6 +704,10 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
         return rc;
       }
       B.x1tab = t;
+      if (r32) {
+        B.refb = t + 6 * (size_t)nx1;
+        h->ref32 = true;
+      }
     }
     if (d.grav1 != 0. && (d.bc[0] == SG_BC_PERIODIC || d.bc[1] == SG_BC_PERIODIC)) {
       sg_destroy(h);
@@ -1088,6 +1098,7 @@ int sg_stage(sg_handle* h, int32_t stage, const double* dt_dev,
   p.max_nc1 = h->max_nc1;
   p.visc3 = h->visc3;
   p.vic_kinds = h->vic_kinds;
+  p.ref32 = h->ref32;
   // events between the launches when timing is on and the stream is not
   // being captured: ev[0] (x3 ev[6]) stage ev[1] (assemble ev[2] solve
   // ev[3] finish ev[4]) (scalars ev[7]) ghost ev[5]
@@ -1108,7 +1119,7 @@ int sg_stage(sg_handle* h, int32_t stage, const double* dt_dev,
     }
     cudaEventRecord(ev[0], s);
   }
-  int launches = 2;
+  int launches = h->ref32 ? 3 : 2;  // (with the base reference's refresh)
   if (h->has3) {
     // the x3 faces of the 3-D blocks: their flux differences, which the
     // stage kernel adds to its divergence after x1 and x2

@@ -228,63 +228,6 @@ __device__ __forceinline__ void ref_scan(const real* rho, const real* pres,
   }
 }
 
-#else
-// the same face pressures with the sums taken by a warp (all 32 lanes call
-// it for one column): below the top cell psf_lo[i] = top + sum_{k=i..iu} dp_k
-// and psf_hi[i] = top + sum_{k=i+1..iu} dp_k; above it psf_lo[i] = top -
-// sum_{k=iu+1..i-1} dp_k and psf_hi[i] = top - sum_{k=iu+1..i} dp_k, with
-// dp_k = grav rho_k dx.  The sums are warp prefix sums in chunks of 32, so
-// their rounding differs from the serial scan's (used by the FP32 build).
-__device__ __forceinline__ void ref_scan_warp(const real* rho, const real* pres,
-                                              const double* pb, int nc1,
-                                              int iu, double dx, double grav,
-                                              double* psf_lo, double* psf_hi) {
-  const unsigned full = 0xffffffffu;
-  const int lane = threadIdx.x & 31;
-  const double minp = 2.2250738585072014e-308;
-  const double ptop = col_p(pres, pb, iu);
-  const double rdt_top = ptop / as_f64(rho[iu]);
-  const double top = ptop * sg_exp(-grav * 0.5 * dx / rdt_top);
-  double carry = 0.;
-  for (int c0 = iu; c0 >= 0; c0 -= 32) {
-    const int i = c0 - lane;
-    double v = i >= 0 ? grav * as_f64(rho[i]) * dx : 0.;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      double t = __shfl_up_sync(full, v, d);
-      if (lane >= d) v += t;
-    }
-    const double S = carry + v;  // sum over cells i..iu
-    double above = __shfl_up_sync(full, S, 1);
-    if (lane == 0) above = carry;
-    if (i >= 0) {
-      double lo = top + S, hi = top + above;
-      psf_lo[i] = lo > minp ? lo : minp;
-      psf_hi[i] = hi > minp ? hi : minp;
-    }
-    carry = __shfl_sync(full, S, 31);
-  }
-  carry = 0.;
-  for (int c0 = iu + 1; c0 < nc1; c0 += 32) {
-    const int i = c0 + lane;
-    double v = i < nc1 ? grav * as_f64(rho[i]) * dx : 0.;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      double t = __shfl_up_sync(full, v, d);
-      if (lane >= d) v += t;
-    }
-    const double S = carry + v;  // sum over cells iu+1..i
-    double below = __shfl_up_sync(full, S, 1);
-    if (lane == 0) below = carry;
-    if (i < nc1) {
-      double lo = top - below, hi = top - S;
-      psf_lo[i] = lo > minp ? lo : minp;
-      psf_hi[i] = hi > minp ? hi : minp;
-    }
-    carry = __shfl_sync(full, S, 31);
-  }
-}
-
 #endif
 
 __device__ __forceinline__ double wall_rop(double r0, double r1, double k) {
@@ -367,6 +310,190 @@ __device__ __forceinline__ void ref_cell(const double* ropc,
   dref[i] = cell_pref * rs;
   dsf[i] = lo * rf;
 }
+
+// the six-face stencil ref_cell tries for cell i, if any (at most one
+// applies to a cell): its first face, its weight row and its direction
+template <typename W6>
+__device__ __forceinline__ bool ref_stencil(int i, int nc1, int iu,
+                                            bool phys_in, bool phys_out,
+                                            bool wall_clamp, const W6* w6,
+                                            const W6 (*w6e)[6], int* start,
+                                            const W6** wt, bool* rev) {
+  const int il = nc1 - 1 - iu;
+  const bool thin = (iu - il + 1) < 5, fits = iu >= 4;
+  const bool wall_in = wall_clamp && phys_in && i >= il && i < il + 2;
+  const bool wall_out = wall_clamp && phys_out && i > iu - 2 && i <= iu;
+  *rev = false;
+  if (i >= 2 && i < nc1 - 2 && !wall_in && !wall_out) {
+    *start = i - 2;
+    *wt = w6;
+    return true;
+  }
+  if (wall_in && fits && !(thin && phys_out)) {
+    *start = il;
+    *wt = w6e[i - il];
+    return true;
+  }
+  if (wall_out && fits && !(thin && phys_in)) {
+    const int s0 = iu + 1 - 5;
+    *start = s0;
+    *wt = w6e[4 - (i - s0)];
+    *rev = true;
+    return true;
+  }
+  if (!phys_in && i < 2) {
+    *start = 0;
+    *wt = w6e[i];
+    return true;
+  }
+  if (!phys_out && i >= nc1 - 2) {
+    *start = nc1 - 5;
+    *wt = w6e[4 - (i - (nc1 - 5))];
+    *rev = true;
+    return true;
+  }
+  return false;
+}
+
+#ifdef SG_REAL_IS_FLOAT
+// ---------------------------------------------------------------------------
+// The FP32 build's well-balanced reference in anomaly form.  The state is
+// stored as anomalies about the FP64 base (rho_b, p_b, pf_b), and the
+// reference is linear in the face pressures: the scan of a column gives
+//   PF(f) = top + sum g dx rho_k = [top_b + sum g dx rho_b,k] + (top - top_b)
+//           + sum g dx rho'_k,
+// so PF(f) - pf_b(f) = Eb(f) + (top - top_b) + sum g dx rho'_k, with Eb the
+// base's own scan less pf_b.  Eb, the base's top face pressure and the base
+// parts of the cell pressures (the mid value, the two faces and the stencil,
+// each less p_b) are formed in FP64 once per block and stage
+// (base_ref_kernel); a tile forms top - top_b once per column in FP64 and the
+// rest in FP32 on anomalies, so no FP32 value carries the 1e5 Pa base.  The
+// densities stay totals, as in the tile's primitives.
+__constant__ float c_w6f[6] = {(float)(11. / 1440.), (float)(-31. / 480.),
+                               (float)(401. / 720.), (float)(401. / 720.),
+                               (float)(-31. / 480.), (float)(11. / 1440.)};
+__constant__ float c_w6ef[2][6] = {
+    {(float)(95. / 288.), (float)(1427. / 1440.), (float)(-133. / 240.),
+     (float)(241. / 720.), (float)(-173. / 1440.), (float)(3. / 160.)},
+    {(float)(-3. / 160.), (float)(637. / 1440.), (float)(511. / 720.),
+     (float)(-43. / 240.), (float)(77. / 1440.), (float)(-11. / 1440.)}};
+
+struct RefTab {
+  const float *pbf, *pb, *eb, *cmid, *clo, *chi, *cst;
+};
+
+__device__ __forceinline__ RefTab ref_tab(const double* refb, int nc1) {
+  const float* t = reinterpret_cast<const float*>(refb + 1);
+  RefTab r;
+  r.pbf = t;
+  r.pb = r.pbf + (nc1 + 1);
+  r.eb = r.pb + nc1;
+  r.cmid = r.eb + (nc1 + 1);
+  r.clo = r.cmid + nc1;
+  r.chi = r.clo + nc1;
+  r.cst = r.chi + nc1;
+  return r;
+}
+
+// one warp per block
+__global__ void __launch_bounds__(32) base_ref_kernel(const BlockDev* tab) {
+  const BlockDev& B = tab[blockIdx.x];
+  if (!B.refb || !B.base) return;
+  const int nc1 = B.nc1, iu = nc1 - 1 - B.ng;
+  const int lane = threadIdx.x;
+  const unsigned full = 0xffffffffu;
+  const double* rb = base_rho(B.base, nc1);
+  const double* pb = base_p(B.base, nc1);
+  const double* pbf = base_pf(B.base, nc1);
+  float* t = reinterpret_cast<float*>(B.refb + 1);
+  float* tpbf = t;
+  float* tpb = tpbf + (nc1 + 1);
+  float* teb = tpb + nc1;
+  float* tmid = teb + (nc1 + 1);
+  float* tlo = tmid + nc1;
+  float* thi = tlo + nc1;
+  float* tst = thi + nc1;
+  const double grav = -B.grav1, dx = B.dx1;
+  const double ptop = pb[iu];
+  const double top = ptop * sg_exp(-grav * 0.5 * dx / (ptop / rb[iu]));
+  if (lane == 0) B.refb[0] = top;
+  // the base's scanned face pressures, ref_scan's sums as warp prefix sums
+  double carry = 0.;
+  for (int c0 = iu; c0 >= 0; c0 -= 32) {
+    const int i = c0 - lane;
+    double v = i >= 0 ? grav * rb[i] * dx : 0.;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const double u = __shfl_up_sync(full, v, d);
+      if (lane >= d) v += u;
+    }
+    const double S = carry + v;
+    if (i >= 0) teb[i] = (float)((top + S) - pbf[i]);
+    carry = __shfl_sync(full, S, 31);
+  }
+  carry = 0.;
+  for (int c0 = iu + 1; c0 <= nc1; c0 += 32) {
+    const int f = c0 + lane, k = f - 1;
+    double v = (k > iu && k < nc1) ? grav * rb[k] * dx : 0.;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const double u = __shfl_up_sync(full, v, d);
+      if (lane >= d) v += u;
+    }
+    const double S = carry + v;
+    if (f <= nc1) teb[f] = (float)((top - S) - pbf[f]);
+    carry = __shfl_sync(full, S, 31);
+  }
+  const bool phys_in = B.bc[0] != kBcNone, phys_out = B.bc[1] != kBcNone;
+  for (int i = lane; i <= nc1; i += 32) {
+    tpbf[i] = (float)pbf[i];
+    if (i == nc1) break;
+    tpb[i] = (float)pb[i];
+    tmid[i] = (float)(0.5 * (pbf[i] + pbf[i + 1]) - pb[i]);
+    tlo[i] = (float)(pbf[i] - pb[i]);
+    thi[i] = (float)(pbf[i + 1] - pb[i]);
+    int s0;
+    const double* wt;
+    bool rev;
+    double c = 0.;
+    if (ref_stencil<double>(i, nc1, iu, phys_in, phys_out,
+                            B.wb_wall_clamp != 0, c_w6, c_w6e, &s0, &wt,
+                            &rev)) {
+      for (int m = 0; m < 6; ++m) c += wt[rev ? 5 - m : m] * pbf[s0 + m];
+      c -= pb[i];
+    }
+    tst[i] = (float)c;
+  }
+}
+
+__device__ __forceinline__ float wall_rop_f(float r0, float r1, float k) {
+  float q = r0 / r1, qk = k == floorf(k) ? q : powf(q, k);
+  for (int n = 1; k == floorf(k) && n < k; ++n) qk *= q;
+  float e = r1 > r0 ? r0 * qk : r0 + k * (r0 - r1);
+  return e > 0.f ? e : r0;
+}
+
+__device__ __forceinline__ float rop_smooth_f(const float* ropc, int i,
+                                              int jlo, int jhi, bool ext_lo,
+                                              bool ext_hi) {
+  if (!(ext_lo && i - 2 < jlo) && !(ext_hi && i + 2 > jhi))
+    return ropc[i < jlo ? jlo : (i > jhi ? jhi : i)];
+  float v[5];
+#pragma unroll
+  for (int m = -2; m <= 2; ++m) {
+    const int j = i + m;
+    if (j < jlo)
+      v[m + 2] = ext_lo ? wall_rop_f(ropc[jlo], ropc[jlo + 1], (float)(jlo - j))
+                        : ropc[jlo];
+    else if (j > jhi)
+      v[m + 2] = ext_hi ? wall_rop_f(ropc[jhi], ropc[jhi - 1], (float)(j - jhi))
+                        : ropc[jhi];
+    else
+      v[m + 2] = ropc[j];
+  }
+  return (v[0] + 4.f * v[1] + 6.f * v[2] + 4.f * v[3] + v[4]) / 16.f;
+}
+#endif
 
 // one tile of the batch: `tj` x2 columns of one block over its full x1
 template <int RK, bool SHOCK>
@@ -485,25 +612,141 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
   const int iu = nc1 - 1 - ng;
   real* PP = sm + L.pert;  // p - pref of each tile cell
   real* PD = PP + rs_;     // rho - dref
-  if (wb) {
 #ifdef SG_REAL_IS_FLOAT
-    // one warp per column: the face-pressure scan as a warp prefix sum (the
-    // FP32 build is checked against the FP64 oracle at 1e-5; the FP64 build
-    // keeps the reference's serial order below)
+  // the FP32 reference (anomalies of the face and cell pressures about the
+  // base, densities as totals), in the reference region as floats: per
+  // column PFa [nc1 + 1] (face pressure - pf_b), rop, pref' (cell pressure
+  // - p_b), dref, dsf_l, dsf_r
+  float* RF = reinterpret_cast<float*>(REF);
+  const int cs1 = nc1 + 1, rsf = ntj * cs1;
+  if (wb) {
+    const RefTab T = ref_tab(B.refb, nc1);
+    const float gdx = (float)(-B.grav1 * B.dx1);
+    // a warp per column: top - top_b in FP64, then the anomalies' prefix
+    // sums of g dx rho' (the stored density anomalies) in FP32
     for (int jt = threadIdx.x >> 5; jt < ntj; jt += blockDim.x >> 5) {
+      const int lane = threadIdx.x & 31;
+      const unsigned full = 0xffffffffu;
+      const real* ra = uin + row0 + (size_t)(hj + jt) * nc1;
+      const real* pres = W + IPR * wstride + (hj + jt) * nc1;
+      float* PFa = RF + jt * cs1;
+      const double ptop = pbc[iu] + as_f64(pres[iu]);
+      const double rtop = rb[iu] + as_f64(ra[iu]);
+      const double top = ptop * sg_exp(B.grav1 * 0.5 * B.dx1 / (ptop / rtop));
+      const float tp = (float)(top - B.refb[0]);
+      float carry = 0.f;
+      for (int c0 = iu; c0 >= 0; c0 -= 32) {
+        const int i = c0 - lane;
+        float v = i >= 0 ? gdx * ra[i] : 0.f;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+          const float u = __shfl_up_sync(full, v, d);
+          if (lane >= d) v += u;
+        }
+        const float S = carry + v;  // over cells i..iu
+        if (i >= 0) PFa[i] = (tp + S) + T.eb[i];
+        carry = __shfl_sync(full, S, 31);
+      }
+      carry = 0.f;
+      for (int c0 = iu + 1; c0 <= nc1; c0 += 32) {
+        const int f = c0 + lane, k = f - 1;
+        float v = (k > iu && k < nc1) ? gdx * ra[k] : 0.f;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+          const float u = __shfl_up_sync(full, v, d);
+          if (lane >= d) v += u;
+        }
+        const float S = carry + v;  // over cells iu+1..f-1
+        if (f <= nc1) PFa[f] = (tp - S) + T.eb[f];
+        carry = __shfl_sync(full, S, 31);
+      }
+    }
+    // rho / p of every cell once (totals: p = p_b + p')
+    for (int idx = threadIdx.x; idx < ntj * nc1; idx += blockDim.x) {
+      const int jt = idx / nc1, i = idx - jt * nc1;
       const real* rho = W + IDN * wstride + (hj + jt) * nc1;
       const real* pres = W + IPR * wstride + (hj + jt) * nc1;
-      ref_scan_warp(rho, pres, pbc, nc1, iu, B.dx1, -B.grav1,
-                    REF + 0 * rs_ + jt * nc1, REF + 1 * rs_ + jt * nc1);
+      RF[rsf + jt * cs1 + i] = rho[i] / (T.pb[i] + pres[i]);
     }
+    __syncthreads();
+    // ref_cell on the anomalies: the mid value, the faces and the stencil
+    // relative to p_b (their base parts from the table)
+    const bool wclamp = B.wb_wall_clamp != 0;
+    const int jlo = (wclamp && phys_in) ? il : 0;
+    const int jhi = (wclamp && phys_out) ? iu : nc1 - 1;
+    const bool ext_lo = wclamp && phys_in && il + 1 <= iu;
+    const bool ext_hi = wclamp && phys_out && iu - 1 >= il;
+    for (int idx = threadIdx.x; idx < ntj * nc1; idx += blockDim.x) {
+      const int jt = idx / nc1, i = idx - jt * nc1;
+      const float* PFa = RF + jt * cs1;
+      const float* rop = RF + rsf + jt * cs1;
+      const float lo = PFa[i] + T.clo[i], hi = PFa[i + 1] + T.chi[i];
+      const float lower = fminf(lo, hi), upper = fmaxf(lo, hi);
+      float cell = 0.5f * (PFa[i] + PFa[i + 1]) + T.cmid[i];
+      int s0;
+      const float* wt;
+      bool rev;
+      if (ref_stencil<float>(i, nc1, iu, phys_in, phys_out, wclamp, c_w6f,
+                             c_w6ef, &s0, &wt, &rev)) {
+        float value = 0.f;
+        for (int m = 0; m < 6; ++m) value += wt[rev ? 5 - m : m] * PFa[s0 + m];
+        value += T.cst[i];
+        if (value >= lower && value <= upper) cell = value;
+      }
+      const float rs = rop_smooth_f(rop, i, jlo, jhi, ext_lo, ext_hi);
+      const float rf =
+          i > 0 ? 0.5f * (rop_smooth_f(rop, i - 1, jlo, jhi, ext_lo, ext_hi) + rs)
+                : rs;
+      RF[2 * rsf + jt * cs1 + i] = cell;
+      RF[3 * rsf + jt * cs1 + i] = (T.pb[i] + cell) * rs;
+      RF[4 * rsf + jt * cs1 + i] = (T.pbf[i] + PFa[i]) * rf;
+    }
+    __syncthreads();
+    // dsf_lr: the cp5 rows on dref guarded by the two cells' range, a
+    // reflecting wall face the mean of its sides; then PP, PD
+    for (int idx = threadIdx.x; idx < ntj * nc1; idx += blockDim.x) {
+      const int jt = idx / nc1, f = idx - jt * nc1;
+      const float* dref = RF + 3 * rsf + jt * cs1;
+      float* DL = RF + 4 * rsf + jt * cs1;
+      float* DR = RF + 5 * rsf + jt * cs1;
+      const float dsf = DL[f];
+      float l = dsf, r = dsf;
+      if (nc1 >= 6 && f >= 2 && f <= nc1 - 2) {
+        const float a = dref[f - 1], c = dref[f];
+        const float lo = fminf(a, c), hi = fmaxf(a, c);
+        if (f <= nc1 - 3) {
+          const float lin = cp5_cm<float>(dref[f - 2], dref[f - 1], dref[f],
+                                          dref[f + 1], dref[f + 2]);
+          if (lin >= lo && lin <= hi) r = lin;
+        }
+        if (f >= 3) {
+          const float lin = cp5_cp<float>(dref[f - 3], dref[f - 2], dref[f - 1],
+                                          dref[f], dref[f + 1]);
+          if (lin >= lo && lin <= hi) l = lin;
+        }
+        if ((f == il && B.bc[0] == kBcReflecting) ||
+            (f == iu + 1 && B.bc[1] == kBcReflecting)) {
+          const float mean = 0.5f * (l + r);
+          l = r = mean;
+        }
+      }
+      DL[f] = l;
+      DR[f] = r;
+      const real* rho = W + IDN * wstride + (hj + jt) * nc1;
+      const real* pres = W + IPR * wstride + (hj + jt) * nc1;
+      PP[idx] = pres[f] - RF[2 * rsf + jt * cs1 + f];
+      PD[idx] = rho[f] - dref[f];
+    }
+    __syncthreads();
+  }
 #else
+  if (wb) {
     for (int jt = threadIdx.x; jt < ntj; jt += blockDim.x) {
       const real* rho = W + IDN * wstride + (hj + jt) * nc1;
       const real* pres = W + IPR * wstride + (hj + jt) * nc1;
       ref_scan(rho, pres, pbc, nc1, iu, B.dx1, -B.grav1,
                REF + 0 * rs_ + jt * nc1, REF + 1 * rs_ + jt * nc1);
     }
-#endif
     // rho / p of every cell once (rop_smooth reads up to five per cell)
     for (int idx = threadIdx.x; idx < ntj * nc1; idx += blockDim.x) {
       const int jt = idx / nc1, i = idx - jt * nc1;
@@ -560,6 +803,7 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
     }
     __syncthreads();
   }
+#endif
 
   // (3) x1 faces il..iu1 of the tile rows; with gravity the face states are
   // the reference plus the reconstructed perturbation (WellBalancedX1)
@@ -596,6 +840,17 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
           wr[v] = cp5_cm(s[1], s[2], s[3], s[4], s[5]);
         }
       }
+#ifdef SG_REAL_IS_FLOAT
+      // the face pressure's anomaly about pf_b: the reconstructed
+      // perturbation plus the reference's anomaly (a total at or below zero
+      // takes the reference); the density a total
+      const float psfa = RF[jt * cs1 + f], pbff = ref_tab(B.refb, nc1).pbf[f];
+      float pl = wl[IPR] + psfa, pr = wr[IPR] + psfa;
+      wl[IPR] = pl + pbff > 0.f ? pl : psfa;
+      wr[IPR] = pr + pbff > 0.f ? pr : psfa;
+      real dl = wl[IDN] + RF[4 * rsf + jt * cs1 + f];
+      real dr = wr[IDN] + RF[5 * rsf + jt * cs1 + f];
+#else
       // the totals in FP64; the Riemann solve takes the anomaly about the
       // base face pressure where there is a base
       const double psf = REF[0 * rs_ + jt * nc1 + f];
@@ -606,12 +861,17 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
       wr[IPR] = real(pbf ? pr - pbf[f] : pr);
       real dl = real(as_f64(wl[IDN]) + REF[4 * rs_ + jt * nc1 + f]);
       real dr = real(as_f64(wr[IDN]) + REF[5 * rs_ + jt * nc1 + f]);
+#endif
       const real* rho = W + IDN * wstride + (hj + jt) * nc1;
       wl[IDN] = dl > real(0) ? dl : rho[f > 0 ? f - 1 : 0];
       wr[IDN] = dr > real(0) ? dr : rho[f];
     }
     if (pbf)
+#ifdef SG_REAL_IS_FLOAT
+      lmars_flux_anom<real>(wl, wr, gammad, 1, ref_tab(B.refb, nc1).pbf[f], flx);
+#else
       lmars_flux_anom<real>(wl, wr, gammad, 1, real(pbf[f]), flx);
+#endif
     else
       riemann<RK>(wl, wr, gammad, 1, flx);
     if ((fi == 0 && B.bc[0] == kBcReflecting) ||
@@ -2060,6 +2320,10 @@ extern "C" size_t SG_NAME(sg_stage_smem)(int nc1, int tj, int has2, int wb,
 
 extern "C" int SG_NAME(sg_launch_stage)(const BlockDev* tab, StageParams p,
                                         size_t smem, cudaStream_t stream) {
+#ifdef SG_REAL_IS_FLOAT
+  // the FP32 reference's base parts, from the base as it is now
+  if (p.ref32) base_ref_kernel<<<p.nblock, 32, 0, stream>>>(tab);
+#endif
   void (*k)(const BlockDev*, StageParams) = nullptr;
   if (p.riemann == kHllc)
     k = p.shock ? stage_kernel<kHllc, true> : stage_kernel<kHllc, false>;

@@ -57,6 +57,13 @@ struct BlockDev {
   //   r_b[nc1] = rho_b g1 - (pf_b[i + 1] - pf_b[i]) / dx1
   // (null: the buffers hold totals)
   const double* base;
+  // FP32 under gravity: the base's own well-balanced reference, refreshed
+  // every stage from `base` (base_ref_kernel): refb[0] the base's top face
+  // pressure (FP64), then as floats, with N = nc1: pbf [N + 1] and p_b [N]
+  // rounded to FP32, Eb [N + 1] (the base's scanned face pressure - pf_b),
+  // and per cell Cmid, Clo, Chi, Cst [N] (the base parts of the mid, lower,
+  // upper and stencil cell pressures, relative to p_b); null otherwise
+  double* refb;
   // with gravity: per interior x1 cell k, 6 FP64 constants of the geometry
   // (the corrected-PE slope weights w0, w1, w2, grav1 h^2 / 12, and
   // grav1 (x1f[i+1] - x1v[i]), grav1 (x1f[i] - x1v[i]) for i = ng + k)
@@ -141,6 +148,8 @@ struct StageParams {
   int32_t smem_rows;    // x1 lines held in shared memory per tile
   int32_t max_nc1;
   int32_t visc3;        // some 3-D block has viscosity: visc3_kernel runs
+  int32_t ref32;        // some FP32 block keeps its reference in FP32
+                        // (base_ref_kernel runs before the stage kernel)
   int32_t vic_kinds;    // implicit blocks: bit 0 some with the full 5x5
                         // matrix (scheme 9), bit 1 some with the partial
                         // 3x3 one (scheme 1)
