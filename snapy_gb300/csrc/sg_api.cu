@@ -156,7 +156,8 @@ __global__ void restore_kernel(const BlockDev* __restrict__ tab, int cur,
 // cell k of a block (BlockDev::x1tab); the stage kernel formerly evaluated
 // these per cell and launch, with the same operations
 __global__ void x1tab_kernel(const double* x1f, const double* x1v, int ng,
-                             int nx1, double grav1, double* tab) {
+                             int nx1, double grav1, double* tab,
+                             float* tab32) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= nx1) return;
   const int i = ng + k;
@@ -189,6 +190,12 @@ __global__ void x1tab_kernel(const double* x1f, const double* x1v, int ng,
   t[3] = gvar;
   t[4] = grav1 * (x1f[i + 1] - x1v[i]);
   t[5] = grav1 * (x1f[i] - x1v[i]);
+  if (tab32) {  // the same values rounded to FP32, and the covariance dx
+    float* f = tab32 + 8 * k;
+    for (int q = 0; q < 6; ++q) f[q] = (float)t[q];
+    f[6] = (float)(x1v[i + 1] - x1v[i - 1]);
+    f[7] = 0.f;
+  }
 }
 
 __global__ void init_red_kernel(int n, unsigned long long* red, int* nan) {
@@ -684,17 +691,20 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
     }
     B.x1tab = nullptr;
     B.refb = nullptr;
+    B.x1tab32 = nullptr;
     if (d.grav1 != 0.) {
       const int nx1 = d.nc1 - 2 * d.ng;
-      // FP32: the base reference table follows the geometry table
+      // FP32: the geometry table in FP32 and the base reference table
+      // follow the geometry table
       const bool r32 = scheme->dtype == SG_F32;
-      const size_t nref = r32 ? 1 + 4 * ((size_t)d.nc1 + 1) : 0;
+      const size_t nref = r32 ? 4 * (size_t)nx1 + 1 + 5 * ((size_t)d.nc1 + 1) : 0;
       double* t = nullptr;
       cudaError_t e = cudaMalloc(&t, sizeof(double) * (6 * (size_t)nx1 + nref));
       if (e == cudaSuccess) {
         h->x1tabs.push_back(t);
+        float* t32 = r32 ? reinterpret_cast<float*>(t + 6 * (size_t)nx1) : nullptr;
         x1tab_kernel<<<(nx1 + 127) / 128, 128>>>(d.x1f, d.x1v, d.ng, nx1,
-                                                 d.grav1, t);
+                                                 d.grav1, t, t32);
         e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaDeviceSynchronize();
       }
@@ -705,7 +715,8 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
       }
       B.x1tab = t;
       if (r32) {
-        B.refb = t + 6 * (size_t)nx1;
+        B.x1tab32 = reinterpret_cast<const float*>(t + 6 * (size_t)nx1);
+        B.refb = t + 10 * (size_t)nx1;
         h->ref32 = true;
       }
     }

@@ -379,7 +379,8 @@ __constant__ float c_w6ef[2][6] = {
      (float)(-43. / 240.), (float)(77. / 1440.), (float)(-11. / 1440.)}};
 
 struct RefTab {
-  const float *pbf, *pb, *eb, *cmid, *clo, *chi, *cst;
+  const float *pbf, *pb, *eb, *cmid, *clo, *chi, *cst, *rb, *rr;
+  const float* top;  // the base's top face pressure and exp(-c rho_b / p_b)
 };
 
 __device__ __forceinline__ RefTab ref_tab(const double* refb, int nc1) {
@@ -392,6 +393,9 @@ __device__ __forceinline__ RefTab ref_tab(const double* refb, int nc1) {
   r.clo = r.cmid + nc1;
   r.chi = r.clo + nc1;
   r.cst = r.chi + nc1;
+  r.rb = r.cst + nc1;
+  r.rr = r.rb + nc1;
+  r.top = r.rr + nc1;
   return r;
 }
 
@@ -413,10 +417,19 @@ __global__ void __launch_bounds__(32) base_ref_kernel(const BlockDev* tab) {
   float* tlo = tmid + nc1;
   float* thi = tlo + nc1;
   float* tst = thi + nc1;
+  float* trb = tst + nc1;
+  float* trr = trb + nc1;
+  float* ttop = trr + nc1;
   const double grav = -B.grav1, dx = B.dx1;
   const double ptop = pb[iu];
-  const double top = ptop * sg_exp(-grav * 0.5 * dx / (ptop / rb[iu]));
-  if (lane == 0) B.refb[0] = top;
+  const double eb_top = sg_exp(-grav * 0.5 * dx / (ptop / rb[iu]));
+  const double top = ptop * eb_top;
+  if (lane == 0) {
+    B.refb[0] = top;
+    ttop[0] = (float)top;
+    ttop[1] = (float)eb_top;
+  }
+  const double* rr = base_r(B.base, nc1);
   // the base's scanned face pressures, ref_scan's sums as warp prefix sums
   double carry = 0.;
   for (int c0 = iu; c0 >= 0; c0 -= 32) {
@@ -449,6 +462,8 @@ __global__ void __launch_bounds__(32) base_ref_kernel(const BlockDev* tab) {
     tpbf[i] = (float)pbf[i];
     if (i == nc1) break;
     tpb[i] = (float)pb[i];
+    trb[i] = (float)rb[i];
+    trr[i] = (float)rr[i];
     tmid[i] = (float)(0.5 * (pbf[i] + pbf[i + 1]) - pb[i]);
     tlo[i] = (float)(pbf[i] - pb[i]);
     thi[i] = (float)(pbf[i + 1] - pb[i]);
@@ -536,6 +551,25 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
   const double* pbc = base ? base_p(base, nc1) : nullptr;
   const double* pbf = base ? base_pf(base, nc1) : nullptr;
   const double* rrb = base ? base_r(base, nc1) : nullptr;
+#ifdef SG_REAL_IS_FLOAT
+  // the FP32 build reads the base (and the x1 geometry) from its FP32 tables
+  const RefTab T = base ? ref_tab(B.refb, nc1) : RefTab{};
+  auto rb_r = [&](int i) -> real { return T.rb[i]; };
+  auto pb_r = [&](int i) -> real { return T.pb[i]; };
+  auto rr_r = [&](int i) -> real { return T.rr[i]; };
+  auto xt_r = [&](int k, int q) -> real { return B.x1tab32[8 * k + q]; };
+  // (the covariance row also runs without gravity, where there is no table)
+  auto covdx_r = [&](int i) -> real {
+    return B.x1tab32 ? B.x1tab32[8 * (i - ng) + 6]
+                     : real(B.x1v[i + 1] - B.x1v[i - 1]);
+  };
+#else
+  auto rb_r = [&](int i) -> real { return real(rb[i]); };
+  auto pb_r = [&](int i) -> real { return real(pbc[i]); };
+  auto rr_r = [&](int i) -> real { return real(rrb[i]); };
+  auto xt_r = [&](int k, int q) -> real { return real(B.x1tab[6 * k + q]); };
+  auto covdx_r = [&](int i) -> real { return real(B.x1v[i + 1] - B.x1v[i - 1]); };
+#endif
 
   const int wstride = R * nc1;  // one variable of the W tile
   real* W = sm + L.w;
@@ -585,7 +619,7 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
       real uc[NHYDRO], wc[NHYDRO];
 #pragma unroll
       for (int v = 0; v < NHYDRO; ++v) uc[v] = W[v * wstride + idx];
-      if (rb) uc[IDN] = real(rb[idx % nc1]) + uc[IDN];
+      if (rb) uc[IDN] = rb_r(idx % nc1) + uc[IDN];
       cons2prim<real>(uc, wc, gammad);
 #pragma unroll
       for (int v = 0; v < NHYDRO; ++v) W[v * wstride + idx] = wc[v];
@@ -597,7 +631,7 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
       for (int v = 0; v < NHYDRO; ++v) uc[v] = uin[v * plane + row0 + idx];
       // with a base: rho_b + rho', and p' = (g - 1)(E' - ke) since p_b is
       // (g - 1) e_b
-      if (rb) uc[IDN] = real(rb[idx % nc1]) + uc[IDN];
+      if (rb) uc[IDN] = rb_r(idx % nc1) + uc[IDN];
       cons2prim<real>(uc, wc, gammad);
 #pragma unroll
       for (int v = 0; v < NHYDRO; ++v) W[v * wstride + idx] = wc[v];
@@ -620,8 +654,8 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
   float* RF = reinterpret_cast<float*>(REF);
   const int cs1 = nc1 + 1, rsf = ntj * cs1;
   if (wb) {
-    const RefTab T = ref_tab(B.refb, nc1);
     const float gdx = (float)(-B.grav1 * B.dx1);
+    const float cg = 0.5f * gdx;  // g dx / 2
     // a warp per column: top - top_b in FP64, then the anomalies' prefix
     // sums of g dx rho' (the stored density anomalies) in FP32
     for (int jt = threadIdx.x >> 5; jt < ntj; jt += blockDim.x >> 5) {
@@ -630,10 +664,14 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
       const real* ra = uin + row0 + (size_t)(hj + jt) * nc1;
       const real* pres = W + IPR * wstride + (hj + jt) * nc1;
       float* PFa = RF + jt * cs1;
-      const double ptop = pbc[iu] + as_f64(pres[iu]);
-      const double rtop = rb[iu] + as_f64(ra[iu]);
-      const double top = ptop * sg_exp(B.grav1 * 0.5 * B.dx1 / (ptop / rtop));
-      const float tp = (float)(top - B.refb[0]);
+      // top - top_b, top = p exp(-c rho / p) at the top cell, in FP32 on the
+      // anomalies: with x = -c (rho' p_b - rho_b p') / (p_b (p_b + p')),
+      // top - top_b = top_b expm1(x) + E_b p' (1 + expm1(x))
+      const float pbt = T.pb[iu], rbt = T.rb[iu];
+      const float pa = pres[iu], rhoa = ra[iu];
+      const float x = -cg * (rhoa * pbt - rbt * pa) / (pbt * (pbt + pa));
+      const float em = expm1f(x);
+      const float tp = T.top[0] * em + T.top[1] * pa * (1.f + em);
       float carry = 0.f;
       for (int c0 = iu; c0 >= 0; c0 -= 32) {
         const int i = c0 - lane;
@@ -844,7 +882,7 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
       // the face pressure's anomaly about pf_b: the reconstructed
       // perturbation plus the reference's anomaly (a total at or below zero
       // takes the reference); the density a total
-      const float psfa = RF[jt * cs1 + f], pbff = ref_tab(B.refb, nc1).pbf[f];
+      const float psfa = RF[jt * cs1 + f], pbff = T.pbf[f];
       float pl = wl[IPR] + psfa, pr = wr[IPR] + psfa;
       wl[IPR] = pl + pbff > 0.f ? pl : psfa;
       wr[IPR] = pr + pbff > 0.f ? pr : psfa;
@@ -868,7 +906,7 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
     }
     if (pbf)
 #ifdef SG_REAL_IS_FLOAT
-      lmars_flux_anom<real>(wl, wr, gammad, 1, ref_tab(B.refb, nc1).pbf[f], flx);
+      lmars_flux_anom<real>(wl, wr, gammad, 1, T.pbf[f], flx);
 #else
       lmars_flux_anom<real>(wl, wr, gammad, 1, real(pbf[f]), flx);
 #endif
@@ -898,7 +936,7 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
 #pragma unroll
         for (int v = 0; v < NHYDRO; ++v) wb_[v] = real(0.5) * (wl[v] + wr[v]);
         real pbar = wb_[IPR];
-        if (pbc) pbar = real(pbc[i]) + pbar;  // the total
+        if (pbc) pbar = pb_r(i) + pbar;  // the total
         real enth = pbar / (gammad - real(1)) + pbar;
         COV[0 * cstride + jf * nc1 + i] = wb_[IDN];
         COV[1 * cstride + jf * nc1 + i] = enth / wb_[IDN];
@@ -906,7 +944,7 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
       }
       if (i >= il && i < iu1) {
         if (pbc)
-          lmars_flux_anom<real>(wl, wr, gammad, 2, real(pbc[i]), flx);
+          lmars_flux_anom<real>(wl, wr, gammad, 2, pb_r(i), flx);
         else
           riemann<RK>(wl, wr, gammad, 2, flx);
 #pragma unroll
@@ -951,8 +989,7 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
     for (int idx = threadIdx.x; idx < (ntj + 1) * nx1; idx += blockDim.x) {
       const int jf = idx / nx1, ii = idx - jf * nx1, i = il + ii;
       if (L.cov) {
-        const double* x1v = B.x1v;
-        real dx1 = real(x1v[i + 1] - x1v[i - 1]);
+        real dx1 = covdx_r(i);
         const real* rho = COV + jf * nc1;
         const real* h = COV + cstride + jf * nc1;
         const real* un = COV + 2 * cstride + jf * nc1;
@@ -1166,7 +1203,7 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
         // difference and weight balance to r_b (FP64), which leaves the
         // anomaly's weight rho' g
         const real rho_a = uin[IDN * plane + c];
-        du[IVX] += rdt * rho_a * g + rdt * real(rrb[i]);
+        du[IVX] += rdt * rho_a * g + rdt * rr_r(i);
       } else {
         du[IVX] += rdt * rho * g * real(1.);
       }
@@ -1198,17 +1235,16 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
       // the x1 geometry's constants of interior cell k (slope weights w0,
       // w1, w2 of the corrected PE, g h^2 / 12, g dz above and below the
       // centre), precomputed per block in FP64
-      const double* xt = B.x1tab + 6 * k;
-      real hi = real(xt[4]);
-      real lo = real(xt[5]);
+      real hi = xt_r(k, 4);
+      real lo = xt_r(k, 5);
       real fgw = rdt * vdiv(hi * (a1 * fm[k + 1]) - lo * (a1 * fm[k]), vol, rvol);
       if (nx1 >= 3) {
         int kc = k < 1 ? 1 : (k > nx1 - 2 ? nx1 - 2 : k);
         int k0 = kc - 1;
-        real gvar = real(xt[3]);
-        real sl = real(xt[0]) * drho(k0);
-        sl += real(xt[1]) * drho(k0 + 1);
-        sl += real(xt[2]) * drho(k0 + 2);
+        real gvar = xt_r(k, 3);
+        real sl = xt_r(k, 0) * drho(k0);
+        sl += xt_r(k, 1) * drho(k0 + 1);
+        sl += xt_r(k, 2) * drho(k0 + 2);
         fgw += gvar * sl;
       }
       const real rho = W[IDN * wstride + wc], vx = W[IVX * wstride + wc];

@@ -61,9 +61,13 @@ struct BlockDev {
   // every stage from `base` (base_ref_kernel): refb[0] the base's top face
   // pressure (FP64), then as floats, with N = nc1: pbf [N + 1] and p_b [N]
   // rounded to FP32, Eb [N + 1] (the base's scanned face pressure - pf_b),
-  // and per cell Cmid, Clo, Chi, Cst [N] (the base parts of the mid, lower,
-  // upper and stencil cell pressures, relative to p_b); null otherwise
+  // per cell Cmid, Clo, Chi, Cst [N] (the base parts of the mid, lower,
+  // upper and stencil cell pressures, relative to p_b), rho_b and r_b [N]
+  // rounded to FP32, and the top face's base pressure and exponential
+  // factor; and x1tab32, the x1 geometry table in FP32 (8 floats per
+  // interior cell: x1tab's 6, then x1v[i + 1] - x1v[i - 1]); null otherwise
   double* refb;
+  const float* x1tab32;
   // with gravity: per interior x1 cell k, 6 FP64 constants of the geometry
   // (the corrected-PE slope weights w0, w1, w2, grav1 h^2 / 12, and
   // grav1 (x1f[i+1] - x1v[i]), grav1 (x1f[i] - x1v[i]) for i = ng + k)
