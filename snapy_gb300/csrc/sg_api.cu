@@ -233,6 +233,7 @@ struct sg_handle {
   bool implicit = false;
   int vic_kinds = 0;  // bit 0: a block with the full 5x5 matrix, bit 1: 3x3
   bool ref32 = false;  // an FP32 block under gravity: base_ref_kernel runs
+  int asm_kinds = 0;   // implicit blocks assembled in FP64 (bit 0), FP32 (1)
   int refine = 0;  // corrections of the refined implicit solve (0: direct)
   int any_f32 = 0;  // a block assembles its implicit blocks in FP32
   size_t max_icells = 0, max_icols = 0;
@@ -440,6 +441,7 @@ int sg_autotune(sg_handle* h, int32_t reps, int32_t* tj_out,
     p.visc3 = h->visc3;
     p.vic_kinds = h->vic_kinds;
     p.ref32 = h->ref32;
+    p.asm_kinds = h->asm_kinds;
     auto stage = [&]() -> int {
       p.ntile = h->ntile;
       int r = 0;
@@ -679,6 +681,7 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
                   "needs the FP32 state (dynamics/precision float32)", b);
     }
     B.implicit_f32 = d.implicit_scheme != 0 && d.implicit_precision == SG_F32;
+    if (d.implicit_scheme != 0) h->asm_kinds |= B.implicit_f32 ? 2 : 1;
     if (d.nscalar < 0 || d.nscalar > 16) {
       sg_destroy(h);
       return fail(SG_ERR_ARG, "block %d: nscalar %d (0 to 16)", b, d.nscalar);
@@ -1110,6 +1113,7 @@ int sg_stage(sg_handle* h, int32_t stage, const double* dt_dev,
   p.visc3 = h->visc3;
   p.vic_kinds = h->vic_kinds;
   p.ref32 = h->ref32;
+  p.asm_kinds = h->asm_kinds;
   // events between the launches when timing is on and the stream is not
   // being captured: ev[0] (x3 ev[6]) stage ev[1] (assemble ev[2] solve
   // ev[3] finish ev[4]) (scalars ev[7]) ghost ev[5]
@@ -1157,6 +1161,7 @@ int sg_stage(sg_handle* h, int32_t stage, const double* dt_dev,
     // residual and a correction per correction
     // (a wide batch's finish is three launches)
     launches += 3 + (h->wide ? 2 : 0) + (h->vic_kinds == 3 ? 1 : 0) +
+                (h->asm_kinds == 3 ? 1 : 0) +
                 (h->refine > 0 ? 1 + 2 * h->refine : (h->refine < 0 ? 2 : 0));
   }
   if (h->scalars) {

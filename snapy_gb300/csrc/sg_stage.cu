@@ -2485,7 +2485,12 @@ extern "C" int SG_NAME(sg_launch_vic)(const BlockDev* tab, StageParams p,
                                       cudaStream_t stream, cudaEvent_t* ev) {
   int ga = (int)((max_cells + kThreads - 1) / kThreads);
   if (ga > 4096) ga = 4096;
-  vic_assemble_kernel<<<dim3(ga, p.nblock), kThreads, 0, stream>>>(tab, p);
+  if (p.asm_kinds & 1)
+    vic_assemble_kernel<double><<<dim3(ga, p.nblock), kThreads, 0, stream>>>(tab, p);
+#ifdef SG_REAL_IS_FLOAT
+  if (p.asm_kinds & 2)
+    vic_assemble_kernel<float><<<dim3(ga, p.nblock), kThreads, 0, stream>>>(tab, p);
+#endif
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return (int)e;
   if (ev) cudaEventRecord(ev[0], stream);

@@ -152,6 +152,8 @@ struct StageParams {
   int32_t smem_rows;    // x1 lines held in shared memory per tile
   int32_t max_nc1;
   int32_t visc3;        // some 3-D block has viscosity: visc3_kernel runs
+  int32_t asm_kinds;    // implicit blocks: bit 0 some assemble in FP64,
+                        // bit 1 some in FP32 (one kernel each)
   int32_t ref32;        // some FP32 block keeps its reference in FP32
                         // (base_ref_kernel runs before the stage kernel)
   int32_t vic_kinds;    // implicit blocks: bit 0 some with the full 5x5

@@ -489,26 +489,29 @@ __device__ __forceinline__ void vic_assemble_cell(const BlockDev& B,
   }
 }
 
-__global__ void __launch_bounds__(kThreads)
+// CTAs of the FP32 assembly resident per SM (the register budget it is held
+// to: 65536 / (256 kAsm32Ctas))
+#ifndef SG_ASM32_CTAS
+#define SG_ASM32_CTAS 2
+#endif
+constexpr int kAsm32Ctas = SG_ASM32_CTAS;
+
+// the assembly in the compute type T: the FP64 and FP32 forms are separate
+// kernels, so the FP32 one is not held to the FP64 one's register count
+template <typename T>
+__global__ void __launch_bounds__(kThreads, sizeof(T) == sizeof(float) ? kAsm32Ctas : 1)
     vic_assemble_kernel(const BlockDev* __restrict__ tab, StageParams p) {
   const BlockDev& B = tab[blockIdx.y];
-  if (!B.implicit) return;
+  if (!B.implicit || (B.implicit_f32 != 0) != (sizeof(T) == sizeof(float)))
+    return;
   const VicScratch S = vic_scratch(B);
   const real* uin = static_cast<const real*>(B.buf[p.in]);
   const double dtc = p.w2 * p.dt[blockIdx.y];
-#ifdef SG_REAL_IS_FLOAT
-  if (B.implicit_f32) {
-    const AsmConst<float> kc(B, dtc);
-    for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < S.cells;
-         e += (size_t)gridDim.x * blockDim.x)
-      vic_assemble_cell<float>(B, S, uin, dtc, e, p.refine != 0, kc);
-    return;
-  }
-#endif
-  const AsmConst<double> kc(B, dtc);
+  const AsmConst<T> kc(B, dtc);
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < S.cells;
        e += (size_t)gridDim.x * blockDim.x)
-    vic_assemble_cell<double>(B, S, uin, dtc, e, false, kc);
+    vic_assemble_cell<T>(B, S, uin, dtc, e, sizeof(T) == sizeof(float) && p.refine != 0,
+                         kc);
 }
 
 // ludcmp<double, 5, Implicit> on a row-major 5x5 in shared memory
