@@ -2519,8 +2519,12 @@ extern "C" int SG_NAME(sg_launch_vic)(const BlockDev* tab, StageParams p,
   }
   // the solve: the full matrix kVicCols columns per single-warp CTA, the
   // partial one a thread per column
-  if (p.vic_kinds & 1)
-    vic_solve_kernel<<<dim3(gs, p.nblock), 32, 0, stream>>>(tab, p, status);
+  if (p.vic_kinds & 1) {
+    if (p.refine)
+      vic_solve_kernel<true><<<dim3(gs, p.nblock), 32, 0, stream>>>(tab, p, status);
+    else
+      vic_solve_kernel<false><<<dim3(gs, p.nblock), 32, 0, stream>>>(tab, p, status);
+  }
   if (p.vic_kinds & 2) {
     const int g3 = (int)((max_cols + kThreads - 1) / kThreads);
     vic_solve3_kernel<<<dim3(g3, p.nblock), kThreads, 0, stream>>>(tab, p, status);

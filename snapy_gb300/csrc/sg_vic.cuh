@@ -636,6 +636,10 @@ struct VicSolveSmem {
   double rd[kVicCols][5];          // 1 / the diagonal of each factorisation
 };
 
+// BLK32: the refined solve's masked columns, whose blocks are the FP32 ones
+// (a separate instantiation, so the direct solve's block loads carry no
+// select)
+template <bool BLK32>
 __global__ void __launch_bounds__(32)
     vic_solve_kernel(const BlockDev* __restrict__ tab, StageParams p,
                      int* status) {
@@ -651,7 +655,7 @@ __global__ void __launch_bounds__(32)
   bool valid = col < ncol;
   // an implicit-precision float32 block solves here only the columns its
   // refined solve left to FP64 (the mask); a warp with none leaves at once
-  if (Bk.implicit_f32 && p.refine) {
+  if (BLK32 && Bk.implicit_f32) {
     const VicScratch32 F = vic_scratch32(Bk, S, n);
     valid = valid && F.mask[col] != 0;
     if (!__any_sync(0xffffffffu, valid)) return;
@@ -669,7 +673,7 @@ __global__ void __launch_bounds__(32)
   const double* C = S.C + cc * n * 25;
   // the refined solve's masked columns: the blocks are the FP32 ones
   // (assembled in FP32, exact), widened; a' still goes to the FP64 A
-  const bool blk32 = Bk.implicit_f32 && p.refine;
+  const bool blk32 = BLK32 && Bk.implicit_f32;
   const int bst = blk32 ? kBlk32 : 25;  // the row of a cell's block
   const float* A32 = nullptr;
   const float* B32 = nullptr;
