@@ -353,6 +353,22 @@ int sg_cs_stage(sg_cs_handle* h, int32_t stage, const double* dt_dev,
 int sg_cs_fill_seams(sg_cs_handle* h, sg_stream_t stream);
 /* dt_dev = cfl min over the interior of width / (|v| + sqrt(Phi)) */
 int sg_cs_max_dt(sg_cs_handle* h, double* dt_dev, sg_stream_t stream);
+/* The FluxRegister's step fields of the six panels (FluxRegister::end_stage
+ * after reconcile_panel_seams, src/hydro/flux_register.hpp:241-402,
+ * src/layout/seam_register.cpp:35): every stage sets S_d <- w1 S_d +
+ * w2 dt T_d on each interior face, FP64, from the stage's final face
+ * fluxes (seam faces single-valued); S_d = 0 at stage 0.  s2 and s3 are
+ * device doubles laid out (6, 4, nc, nc + 1) and (6, 4, nc + 1, nc),
+ * nc = n + 6 (face j of row k at [k][j]); both null unbinds.  An FP32
+ * state's normal-momentum rows get the constant phi_ref^2 / 2 of the
+ * pressure added back in FP64, so the fields mean what FP64's do. */
+int sg_cs_bind_step_fields(sg_cs_handle* h, double* s2, double* s3);
+/* The budget's row totals of the current state (BudgetConsumer's totals,
+ * src/diagnostics/budget.cpp:68-200): out[4] = sum over the interior cells
+ * of u V per variable (Phi, the radial and the two tangential momenta),
+ * FP64, an FP32 state's Phi with phi_ref added back; one fixed reduction
+ * order, so the sums repeat exactly.  out is device memory. */
+int sg_cs_budget_totals(sg_cs_handle* h, double* out, sg_stream_t stream);
 
 /* Allocation-free time step.  No counterpart in the reference: it is for
  * callers that may not allocate device memory at all (a host that hands in

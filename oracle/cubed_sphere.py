@@ -26,6 +26,10 @@ gnomonic coordinate of src/coord/gnomonic_equiangle.cpp):
   sources x_ov_rD (p + Phi v3 v3 sin^2), y_ov_rC (p + Phi v2 v2 sin^2),
   p = Phi^2 / 2 (gnomonic_equiangle.cpp:465-521); du = -dt div;
   the RK combine, then the seam halo fill (cs_seams.fill).
+With step fields requested, every stage also sets S_d <- w1 S_d + w2 dt T_d
+over the stage's final (reconciled) face fluxes (FluxRegister::end_stage,
+src/hydro/flux_register.hpp:241-402), S_d = 0 at stage 0; the budget's row
+totals are sum u V over the interior (budget.cpp:68-200).
 """
 from __future__ import annotations
 
@@ -66,6 +70,16 @@ class CubedSphere:
         self.hllc = riemann == "hllc"
         self.wght, self.cfl = wght, cfl
         self.nc = n + 2 * NG
+        self.steps = None  # the step fields S_2, S_3, once requested
+
+    def request_step_fields(self):
+        nc = self.nc
+        self.steps = {2: np.zeros((6, 4, nc, nc + 1)), 3: np.zeros((6, 4, nc + 1, nc))}
+        return self.steps
+
+    def budget_totals(self, u):
+        I = slice(NG, NG + self.n)
+        return (u[:, :, I, I] * self.g["vol"][I, I]).sum(axis=(0, 2, 3))
 
     def cons2prim(self, u):
         w = np.empty_like(u)
@@ -170,6 +184,7 @@ class CubedSphere:
         n, g = self.n, self.g
         w = self.cons2prim(u)
         F2, F3 = self.fluxes(w)
+        self.last_fluxes = (F2, F3)
         I = slice(NG, NG + n)
         a2, a3 = g["area2"], g["area3"]
         d2 = a2[I, NG + 1:NG + n + 1] * F2[:, :, I, NG + 1:NG + n + 1] - \
@@ -192,6 +207,13 @@ class CubedSphere:
             u0[:] = u
         du = self.tendency(u, dt)
         w0, w1, w2 = self.wght[s]
+        if self.steps is not None:
+            n, I, J = self.n, slice(NG, NG + self.n), slice(NG, NG + self.n + 1)
+            for d, F in zip((2, 3), self.last_fluxes):
+                sel = (slice(None), slice(None), I, J) if d == 2 else \
+                    (slice(None), slice(None), J, I)
+                S = self.steps[d]
+                S[sel] = (w2 * dt) * F[sel] if s == 0 else S[sel] * w1 + (w2 * dt) * F[sel]
         I = slice(NG, NG + self.n)
         u[:, :, I, I] = w0 * u0[:, :, I, I] + w1 * u[:, :, I, I] + w2 * du[:, :, I, I]
         self.fill(u)

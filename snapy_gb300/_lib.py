@@ -135,6 +135,8 @@ SIGNATURES = {
     "sg_cs_stage": (ctypes.c_int, [_vp, _i32, _vp, _vp]),
     "sg_cs_fill_seams": (ctypes.c_int, [_vp, _vp]),
     "sg_cs_max_dt": (ctypes.c_int, [_vp, _vp, _vp]),
+    "sg_cs_bind_step_fields": (ctypes.c_int, [_vp, _vp, _vp]),
+    "sg_cs_budget_totals": (ctypes.c_int, [_vp, _vp, _vp]),
 }
 
 _lib = None

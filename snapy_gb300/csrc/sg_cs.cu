@@ -70,6 +70,12 @@ struct CsParams {
   double w0, w1, w2;
   double phi0;  // FP32: the reference geopotential of the pressure anomaly
   int hllc;     // 1: HLLC for shallow water, 0: shallow-roe (dir yz)
+  // the FluxRegister's step fields S_2, S_3 (FP64, laid out as f2 / f3;
+  // null: not requested), the FP64 geometry, and whether this is stage 0
+  double* s2;
+  double* s3;
+  const void* geo64;
+  int first;
 };
 
 // the FP32 launches, defined in the FP32 unit
@@ -85,6 +91,7 @@ using sg::IDN;
 using sg::IVX;
 using sg::IVY;
 using sg::IVZ;
+using sg::as_f64;
 
 constexpr int kThreads = 256;
 constexpr int kNg = 3;
@@ -599,6 +606,45 @@ __global__ void cs_dt_finish(unsigned long long* key, double cfl, double* dt) {
   key[1] = 0;
 }
 
+// the budget's row totals (BudgetConsumer, src/diagnostics/budget.cpp:68-200):
+// sum over the interior cells of u V per variable, in FP64, an FP32 state's
+// Phi row with its reference added back; one CTA, a fixed stride and a
+// fixed tree, so the sums are the same on every run
+constexpr int kBudgetThreads = 256;
+template <typename T>
+__global__ void __launch_bounds__(kBudgetThreads)
+    cs_budget_kernel(CsParams P, const void* buf, double* out) {
+  __shared__ double red[4][kBudgetThreads];
+  const int n = P.n, nc = P.nc;
+  const size_t pst = (size_t)nc * nc;
+  const Geo<double> G = geo_of<double>(P.geo64, nc);
+  const T* U = static_cast<const T*>(buf);
+  double acc[4] = {0., 0., 0., 0.};
+  const size_t total = (size_t)6 * n * n;
+  for (size_t e = threadIdx.x; e < total; e += kBudgetThreads) {
+    const int j = kNg + (int)(e % n), k = kNg + (int)((e / n) % n);
+    const int p = (int)(e / ((size_t)n * n));
+    const size_t c = (size_t)k * nc + j;
+    const double vol = G.vol[c];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      double u = as_f64(U[((size_t)p * 4 + v) * pst + c]);
+      if (v == IDN && P.phi0 > 0.) u = P.phi0 + u;
+      acc[v] += u * vol;
+    }
+  }
+#pragma unroll
+  for (int v = 0; v < 4; ++v) red[v][threadIdx.x] = acc[v];
+  __syncthreads();
+  for (int h = kBudgetThreads / 2; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) red[v][threadIdx.x] += red[v][threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x < 4) out[threadIdx.x] = red[threadIdx.x][0];
+}
+
 thread_local std::string g_cs_err;
 
 int cs_fail(int code, const char* fmt, ...) {
@@ -616,6 +662,48 @@ int grid_for(size_t work) {
   return (int)(g ? g : 1);
 }
 
+// the step fields (FluxRegister::end_stage, src/hydro/flux_register.hpp
+// :241-402): S_d <- w1 S_d + w2 dt T_d on every interior face of both
+// directions, in FP64, from the stage's final face fluxes (the seam faces
+// single-valued).  An FP32 state's normal-momentum flux carries the
+// pressure anomaly phi0 Phi' + Phi'^2 / 2; the constant phi0^2 / 2 it leaves
+// out is added back here in FP64, through the face's rotation to covariant
+// components, so S_d means what the FP64 path's does
+template <typename T>
+__global__ void __launch_bounds__(kThreads) cs_step_kernel(CsParams P) {
+  const int n = P.n, nc = P.nc;
+  const size_t fst = (size_t)nc * (nc + 1);  // one variable of a panel's faces
+  const size_t per = (size_t)n * (n + 1);    // interior faces of one of them
+  const double w1 = P.w1, w2dt = P.w2 * P.dt[0];
+  const double p0 = 0.5 * (P.phi0 * P.phi0);
+  const Geo<double> G = geo_of<double>(P.geo64, nc);
+  const size_t total = 2 * (size_t)24 * per;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const bool x2 = e < (size_t)24 * per;
+    const size_t r = x2 ? e : e - (size_t)24 * per;
+    const int pv = (int)(r / per);  // panel * 4 + variable
+    const size_t a = r - (size_t)pv * per;
+    const int along = (int)(a % (n + 1)), across = (int)(a / (n + 1));
+    const size_t fidx = x2 ? (size_t)(kNg + across) * (nc + 1) + kNg + along
+                           : (size_t)(kNg + along) * nc + kNg + across;
+    const T* F = static_cast<const T*>(x2 ? P.f2 : P.f3);
+    double t = as_f64(F[(size_t)pv * fst + fidx]);
+    const int v = pv & 3;
+    if (p0 > 0. && v >= IVY) {
+      const double cs = x2 ? G.cos_f2[fidx] : G.cos_f3[fidx];
+      const double sn = x2 ? G.sin_f2[fidx] : G.sin_f3[fidx];
+      const double rg = sqrt(1.0 / (sn * sn));
+      // the normal flux's share in (F_IVY, F_IVZ) before the lowering
+      const double ty = x2 ? rg * p0 : (-cs * rg) * p0;
+      const double tz = x2 ? (-rg * cs) * p0 : rg * p0;
+      t += v == IVY ? ty + tz * cs : tz + ty * cs;
+    }
+    double* S = (x2 ? P.s2 : P.s3) + (size_t)pv * fst + fidx;
+    *S = P.first ? fma(w2dt, t, 0.) : fma(w2dt, t, *S * w1);
+  }
+}
+
 // the five launches of a stage, the seam halo and the dt reduction in T
 template <typename T>
 int launch_stage(const CsParams& P, size_t faces, size_t cells, cudaStream_t s) {
@@ -624,6 +712,8 @@ int launch_stage(const CsParams& P, size_t faces, size_t cells, cudaStream_t s) 
   (P.hllc ? cs_seam_face_kernel<T, true> : cs_seam_face_kernel<T, false>)
       <<<grid_for(24 * (size_t)P.n), kThreads, 0, s>>>(P);
   cs_seam_flux_kernel<T><<<grid_for(P.nseam), kThreads, 0, s>>>(P);
+  if (P.s2 && P.s3)
+    cs_step_kernel<T><<<grid_for(2 * (size_t)24 * P.n * (P.n + 1)), kThreads, 0, s>>>(P);
   cs_update_kernel<T><<<grid_for(cells), kThreads, 0, s>>>(P);
   cs_ghost_kernel<T><<<grid_for(P.nghost), kThreads, 0, s>>>(P, P.out);
   return (int)cudaGetLastError();
@@ -676,6 +766,8 @@ struct sg_cs_handle {
   void* scratch = nullptr;
   int cur = 0, base = 0;
   unsigned long long* key = nullptr;
+  double* s2 = nullptr;  // the step fields (FP64, caller's memory)
+  double* s3 = nullptr;
 };
 
 extern "C" {
@@ -832,6 +924,9 @@ static CsParams cs_params(const sg_cs_handle* h) {
   P.hllc = h->d.riemann == SG_CS_HLLC;
   const size_t nc = P.nc;
   const size_t s = h->d.dtype == SG_F64 ? 8 : 4;
+  P.s2 = h->s2;
+  P.s3 = h->s3;
+  P.geo64 = h->d.geo;
   P.f2 = h->scratch;
   P.f3 = static_cast<unsigned char*>(h->scratch) + 6 * 4 * nc * (nc + 1) * s;
   P.sbuf = static_cast<unsigned char*>(h->scratch) + 2 * 6 * 4 * nc * (nc + 1) * s;
@@ -865,6 +960,7 @@ int sg_cs_stage(sg_cs_handle* h, int32_t stage, const double* dt_dev,
   P.w0 = h->d.wght[stage][0];
   P.w1 = h->d.wght[stage][1];
   P.w2 = h->d.wght[stage][2];
+  P.first = stage == 0;
   const size_t faces = (size_t)2 * 6 * P.n * (P.n + 1);
   const size_t cells = (size_t)6 * P.n * P.n;
   const int rc = h->d.dtype == SG_F64 ? launch_stage<double>(P, faces, cells, s)
@@ -874,6 +970,28 @@ int sg_cs_stage(sg_cs_handle* h, int32_t stage, const double* dt_dev,
   if (stage == 0) h->base = h->cur;
   h->cur = out;
   return 0;
+}
+
+int sg_cs_bind_step_fields(sg_cs_handle* h, double* s2, double* s3) {
+  if (!h) return cs_fail(SG_ERR_ARG, "sg_cs_bind_step_fields: null handle");
+  if ((s2 == nullptr) != (s3 == nullptr))
+    return cs_fail(SG_ERR_ARG, "sg_cs_bind_step_fields: both fields or neither");
+  h->s2 = s2;
+  h->s3 = s3;
+  return 0;
+}
+
+int sg_cs_budget_totals(sg_cs_handle* h, double* out, sg_stream_t stream) {
+  if (!h || !out) return cs_fail(SG_ERR_ARG, "sg_cs_budget_totals: null argument");
+  if (!h->buf[0]) return cs_fail(SG_ERR_STATE, "sg_cs_budget_totals: buffers not bound");
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  CsParams P = cs_params(h);
+  if (h->d.dtype == SG_F64)
+    cs_budget_kernel<double><<<1, kBudgetThreads, 0, s>>>(P, h->buf[h->cur], out);
+  else
+    cs_budget_kernel<float><<<1, kBudgetThreads, 0, s>>>(P, h->buf[h->cur], out);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? 0 : cs_fail(SG_ERR_CUDA, "sg_cs_budget_totals: %s", cudaGetErrorString(e));
 }
 
 int sg_cs_max_dt(sg_cs_handle* h, double* dt_dev, sg_stream_t stream) {

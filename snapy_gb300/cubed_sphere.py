@@ -473,6 +473,38 @@ class SphereSW:
         from . import _lib
         _lib.check(rc, what)
 
+    def request_step_field(self, dim: int):
+        """The FluxRegister's step fields (both directions are kept):
+        S_d <- w1 S_d + w2 dt T_d over the stage's final face fluxes, FP64,
+        (6, 4, nc, nc + 1) for d = 2 and (6, 4, nc + 1, nc) for d = 3, face
+        j of row k at [..., k, j]; zero at stage 0 of every step."""
+        if dim not in (2, 3):
+            raise ValueError("the cubed sphere's step fields are d = 2, 3")
+        torch = self.torch
+        if getattr(self, "_steps", None) is None:
+            nc = self.nc
+            self._steps = {
+                2: torch.zeros((6, 4, nc, nc + 1), dtype=torch.float64, device=self.device),
+                3: torch.zeros((6, 4, nc + 1, nc), dtype=torch.float64, device=self.device)}
+            self._chk(self.L.sg_cs_bind_step_fields(self.h, self._steps[2].data_ptr(),
+                                                    self._steps[3].data_ptr()),
+                      "sg_cs_bind_step_fields")
+            self._graphs.clear()  # captured before the fields existed
+        return self._steps[dim]
+
+    def step_field(self, dim: int):
+        return self._steps[dim]
+
+    def budget_totals(self):
+        """The row totals sum u V over the interior cells (Phi, the radial
+        and the two tangential momenta), FP64, on the device."""
+        torch = self.torch
+        out = torch.empty(4, dtype=torch.float64, device=self.device)
+        with torch.cuda.device(self.device):
+            self._chk(self.L.sg_cs_budget_totals(self.h, out.data_ptr(), self._stream()),
+                      "sg_cs_budget_totals")
+        return out
+
     def state(self):
         """The current conserved state (a view of the handle's buffer)."""
         return self.store[self.rotation()[0]]

@@ -147,3 +147,48 @@ def test_fp32_against_fp64_oracle(cuda, riemann):
     print(f"\ncubed sphere n={n} ({riemann}): FP32 vs FP64 oracle after 10 steps, "
           f"rel L2 (Phi, m2, m3): {err[0]:.2e} {err[2]:.2e} {err[3]:.2e}")
     assert err[[0, 2, 3]].max() <= 1e-5
+
+
+def field_errors(got, want):
+    """A step field's relative L2: the Phi row alone, and the three momentum
+    rows together (the radial row is round-off on both sides, and a
+    transverse row can be small beside the normal one)."""
+    e0 = np.linalg.norm(got[:, 0] - want[:, 0]) / np.linalg.norm(want[:, 0])
+    e1 = np.linalg.norm(got[:, 1:] - want[:, 1:]) / np.linalg.norm(want[:, 1:])
+    return np.array([e0, e1])
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_step_fields_and_budget_against_oracle(cuda, dtype):
+    """The FluxRegister's step fields of the six panels (both directions,
+    every interior face, the seam faces single-valued) and the budget's row
+    totals against the oracle: FP64 at 1e-12 (the field update is one fused
+    multiply-add on the device, two roundings in the oracle); FP32 within
+    1e-5 (its normal-momentum rows with phi_ref^2 / 2 added back); the
+    total of Phi conserved to round-off."""
+    n = 16
+    o = oracle_sphere(n)
+    u = cs.bump(n, seed=5, width=0.4)
+    sp = cs.SphereSW(n, dtype=dtype, device=cuda, graphs=False)
+    sp.initialize(u)
+    S2 = sp.request_step_field(2)
+    S3 = sp.request_step_field(3)
+    o.fill(u)
+    So = o.request_step_fields()
+    t0 = sp.budget_totals().cpu().numpy()
+    assert np.allclose(t0, o.budget_totals(u), rtol=1e-13 if dtype == torch.float64 else 1e-6)
+    u0 = np.zeros_like(u)
+    tol = 1e-12 if dtype == torch.float64 else 1e-5
+    for step in range(3):
+        dt = float(o.max_dt(u))
+        sp.step(dt)
+        for s in range(3):
+            o.stage(u, u0, dt, s)
+        for got, want in ((S2, So[2]), (S3, So[3])):
+            e = field_errors(got.cpu().numpy(), want)
+            assert e.max() <= tol, (step, e)
+    print(f"\n{dtype}: step fields vs oracle, rel L2 (Phi row, momentum rows) "
+          f"{field_errors(S2.cpu().numpy(), So[2])} {field_errors(S3.cpu().numpy(), So[3])}")
+    t1 = sp.budget_totals().cpu().numpy()
+    assert abs(t1[0] / t0[0] - 1) <= (1e-13 if dtype == torch.float64 else 1e-6)
+    assert np.allclose(t1, o.budget_totals(u), rtol=tol, atol=tol * np.abs(t1).max())
