@@ -133,6 +133,13 @@ def parse():
                          "the default) or direct (FP64 for every column)")
     ap.add_argument("--implicit-corrections", type=int, choices=[1, 2, 3],
                     default=None, help="the refined solve's corrections")
+    ap.add_argument("--implicit-sweep", choices=["serial", "partitioned", "auto"],
+                    default=None,
+                    help="the elimination order of the FP64-assembled solve: "
+                         "serial (the reference's, bit for bit; the deck "
+                         "default), partitioned (four chunks per column at "
+                         "once and a separator system) or auto (the "
+                         "autotuner times both)")
     ap.add_argument("--scalars", type=int, default=0,
                     help="Straka and Sod workloads: passive tracers carried "
                          "(the reference's Straka deck carries one, "
@@ -163,6 +170,8 @@ def load_options(args):
         opts.implicit_solve = args.implicit_solve
     if args.implicit_corrections:
         opts.implicit_corrections = args.implicit_corrections
+    if getattr(args, "implicit_sweep", None):
+        opts.implicit_sweep = args.implicit_sweep
     if getattr(args, "scalars", 0):
         # tracers are built without the x2 flux-covariance row
         opts.scalar_names = [f"tracer{k}" for k in range(args.scalars)]
@@ -193,6 +202,11 @@ def implicit_solve(opts):
             return ("FP32 (the reference's FP32 implicit compute): the FP32 "
                     "block-Thomas sweep and its Woodbury step, the FP64 solve "
                     "for columns whose sweep fails")
+    if opts.implicit_sweep == "partitioned":
+        return ("direct FP64, partitioned: four chunks per column swept at "
+                "once, a separator system, then every layer")
+    if opts.implicit_sweep == "auto":
+        return "direct FP64, serial or partitioned as the autotuner chose"
     return "direct FP64"
 
 
@@ -244,6 +258,12 @@ def solve_phase(opts):
     """The implicit solve phase timed as vic_solve_kernel (the events
     between the assembly and the finish): what runs in it, its algorithmic
     bytes per interior cell and what bounds it."""
+    if not refined(opts) and opts.implicit_sweep == "partitioned":
+        # the chunk sweeps: A, B, C, du in; C', V', y out; back up the
+        # chunk: C', V', y in, E, F, Y out; every layer: E, F, Y in, x out;
+        # the Woodbury step: D, Z0, Z1 in, D out
+        return ("vic_psolve_kernel (the partitioned solve)",
+                640 + 520 + 520 + 520 + 520 + 120 + 120 + 40, FP64_ISSUE)
     if not refined(opts):
         return ("vic_solve_kernel", 600 + 40 + 200 + 120 + 200 + 120 + 120,
                 FP64_ISSUE)
@@ -678,12 +698,14 @@ def run_ensemble(args, ranks=None, emit=True):
           for _ in range(args.steps)]
     ranks.barrier()
     torch.cuda.synchronize()
+    fb0 = sum(ens.batch.solve_fallbacks())
     with ClockSampler(local) as clk:
         for k in range(args.steps):
             ev[k][0].record(stream)
             ens.step()
             ev[k][1].record(stream)
         torch.cuda.synchronize()
+    fb1 = sum(ens.batch.solve_fallbacks())
     step_ms = [a.elapsed_time(b) for a, b in ev]
     t_total = sum(step_ms) / 1e3
     t_total = ranks.max(t_total)
@@ -796,6 +818,12 @@ def run_ensemble(args, ranks=None, emit=True):
             "clocks": clk.summary(),
             "gpu_launches": args.steps * (2 + 3 * b.launches_per_stage()),
             "step_ms_median": statistics.median(step_ms),
+            "step_ms_range": [min(step_ms), max(step_ms)],
+            # the reference's implicit.fp64_columns monitor over the timed
+            # steps: columns the refined solve left to the direct FP64 solve
+            "implicit_fp64_columns": {
+                "timed_steps": fb1 - fb0,
+                "columns": sum(o.coord().nx2 for o, _ in members)},
         }
         if emit:
             print(json.dumps(line), flush=True)

@@ -237,6 +237,30 @@ int sg_set_solve(sg_handle* h, int32_t corrections);
  * direct FP64 solve (ImplicitHydroImpl's "implicit.fp64_columns" monitor,
  * src/hydro/hydro.cpp:460-466); waits for the device */
 int sg_solve_fallbacks(sg_handle* h, int64_t* counts);
+/* The order of elimination of the scheme-9 solve of FP64-assembled blocks
+ * (replaces the serial ForwardSweep column loop of
+ * src/implicit/forward_sweep_impl.h:30-131 and the back substitution of
+ * src/implicit/vic_kernels.h:100-160 for such blocks; the reference has only
+ * the serial order).  mode 0: the serial block-Thomas sweep, bit for bit the
+ * reference's operation order (the default).  mode 1: the partitioned form,
+ * for batches with too few columns to fill the GPU: each column in four
+ * chunks swept at once by one warp, then a 3-row system of the separator
+ * layers; the same solution to rounding (within 1e-12 relative), not bit
+ * for bit.  mode 2: sg_autotune times both and keeps the faster (the
+ * serial sweep until it runs).  Columns shorter than 16 layers, scheme-1
+ * and FP32-assembled blocks always take their own solve; a column whose
+ * partitioned solve fails any check is solved again serially, which
+ * decides its failure as the reference does, and counts in
+ * sg_solve_fallbacks.  Modes 1 and 2 allocate the form's region (400 B per
+ * interior cell of the served blocks) on first use.  Not inside a stream
+ * capture; graphs captured before must be captured again. */
+int sg_set_sweep(sg_handle* h, int32_t mode);
+/* whether the partitioned form runs now (1) or the serial one (0) */
+int sg_sweep(const sg_handle* h, int32_t* on);
+/* A check of the partitioned form's reciprocal (no counterpart in the
+ * reference): r[i] = its 1 / x[i] for n device doubles x, on the stream,
+ * for comparison with the IEEE division. */
+int sg_psw_rcp(const double* x, double* r, int64_t n, sg_stream_t stream);
 int sg_autotune(sg_handle* h, int32_t reps, int32_t* tj_out,
                 int32_t* finish_out, double* ms_out, sg_stream_t stream);
 int sg_set_schedule(sg_handle* h, const int32_t* tj, int32_t finish);

@@ -3,7 +3,9 @@
 ``sg_autotune`` (native, in ``libsnapy_gb300.so``) times the stage's kernels
 on a handle's own blocks and state for every tile width and both forms of
 the implicit solve's finish, and keeps the fastest; the results do not
-depend on the choice.  This module runs it once per configuration and keeps
+depend on the choice.  A handle in sweep mode 2 (``integration/implicit-sweep:
+auto``) also times the serial and the partitioned solve, whose results agree
+to rounding.  This module runs it once per configuration and keeps
 the choice in a JSON cache keyed by the device, the library version, the
 scheme and the blocks' shapes and physics, so a later handle of the same
 configuration applies it with ``sg_set_schedule`` and launches no trials.
@@ -50,7 +52,8 @@ def key(batch) -> str:
                        int(bool(d.get("implicit_f32"))), int(d.get("grav1", 0.0) != 0.0),
                        int(d.get("nu_iso", 0.0) > 0.0), int(bool(d.get("flux_cov", True))),
                        list(d["bc"])])
-    return json.dumps([dev, ver, str(batch.dtype), batch.scheme_key, blocks],
+    return json.dumps([dev, ver, str(batch.dtype), batch.scheme_key,
+                       getattr(batch, "sweep_mode", 0), blocks],
                       separators=(",", ":"))
 
 
@@ -81,7 +84,8 @@ def _store(path: Optional[str], k: str, entry: dict) -> None:
 
 def tune(batch, reps: int = 3, use_cache: bool = True, stream=None) -> dict:
     """Pick (or recall) the batch's schedule and apply it.  Returns
-    {"tj": [...], "finish": f, "stage_ms": ..., "solve_ms": ..., "cached": bool}."""
+    {"tj": [...], "finish": f, "stage_ms": ..., "solve_ms": ..., "sweep": 0|1,
+    "cached": bool}."""
     path = cache_path() if use_cache else None
     k = key(batch)
     entry = _load(path).get(k) if path else None
@@ -90,6 +94,9 @@ def tune(batch, reps: int = 3, use_cache: bool = True, stream=None) -> dict:
         tj = (ctypes.c_int32 * n)(*entry["tj"])
         _lib.check(batch.L.sg_set_schedule(batch.h, tj, int(entry["finish"])),
                    "sg_set_schedule")
+        if getattr(batch, "sweep_mode", 0) == 2:
+            _lib.check(batch.L.sg_set_sweep(batch.h, 1 if entry.get("sweep") else 0),
+                       "sg_set_sweep")
         return dict(entry, cached=True)
     tj = (ctypes.c_int32 * n)()
     fin = ctypes.c_int32()
@@ -97,7 +104,9 @@ def tune(batch, reps: int = 3, use_cache: bool = True, stream=None) -> dict:
     s = 0 if stream is None else stream.cuda_stream
     _lib.check(batch.L.sg_autotune(batch.h, reps, tj, ctypes.byref(fin), ms,
                                    ctypes.c_void_p(s)), "sg_autotune")
+    on = ctypes.c_int32()
+    _lib.check(batch.L.sg_sweep(batch.h, ctypes.byref(on)), "sg_sweep")
     entry = {"tj": list(tj), "finish": fin.value, "stage_ms": ms[0],
-             "solve_ms": ms[1]}
+             "solve_ms": ms[1], "sweep": on.value}
     _store(path, k, entry)
     return dict(entry, cached=False)

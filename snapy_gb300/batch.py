@@ -61,6 +61,7 @@ class Batch:
         self.scheme_key = [int(scheme["riemann"]), int(bool(scheme["shock"])),
                            int(bool(scheme["scale"]))]
         self.schedule = None  # the autotuner's choice, once tuned
+        self.sweep_mode = 0  # sg_set_sweep's mode (0: the serial sweep)
         sch = _lib.Scheme()
         sch.dtype = _DT[dtype]
         sch.riemann = scheme["riemann"]
@@ -371,6 +372,21 @@ class Batch:
         out = (ctypes.c_int64 * self.nblock)()
         _lib.check(self.L.sg_solve_fallbacks(self.h, out), "sg_solve_fallbacks")
         return list(out)
+
+    def set_sweep(self, mode: int) -> None:
+        """The order of elimination of the scheme-9 solve of FP64-assembled
+        blocks: 0 the serial sweep (the reference's order, bit for bit), 1
+        the partitioned form (four chunks per column at once and a
+        separator system; the same solution to rounding), 2 the autotuner's
+        choice between them (serial until it runs)."""
+        _lib.check(self.L.sg_set_sweep(self.h, int(mode)), "sg_set_sweep")
+        self.sweep_mode = int(mode)
+
+    def sweep(self) -> int:
+        """1 while the partitioned form runs, else 0."""
+        on = ctypes.c_int32()
+        _lib.check(self.L.sg_sweep(self.h, ctypes.byref(on)), "sg_sweep")
+        return on.value
 
     def set_solve(self, corrections: int) -> None:
         """The solve of implicit-precision float32 blocks: refined with that

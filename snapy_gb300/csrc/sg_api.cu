@@ -46,7 +46,9 @@ using sg::StageParams;
   extern "C" int sg_launch_scalar##sfx(const BlockDev*, StageParams, size_t,  \
                                        size_t, cudaStream_t);                  \
   extern "C" int sg_launch_scalar_ghost##sfx(const BlockDev*, int, int,       \
-                                             size_t, cudaStream_t);
+                                             size_t, cudaStream_t);             \
+  extern "C" int sg_launch_psw_rcp##sfx(const double*, double*, size_t,       \
+                                        cudaStream_t);
 SG_DECLARE(_f64)
 SG_DECLARE(_f32)
 
@@ -235,6 +237,15 @@ struct sg_handle {
   bool ref32 = false;  // an FP32 block under gravity: base_ref_kernel runs
   int asm_kinds = 0;   // implicit blocks assembled in FP64 (bit 0), FP32 (1)
   int refine = 0;  // corrections of the refined implicit solve (0: direct)
+  // the partitioned form of the scheme-9 solve of FP64-assembled blocks:
+  // the requested mode (sg_set_sweep: 0 serial, 1 partitioned, 2 the
+  // autotuner's choice), whether it runs now, and its region (per block,
+  // at psw_off[b]; the blocks it serves: FP64-assembled, scheme 9, at least
+  // kPswMinLayers layers)
+  int psw_mode = 0;
+  int psw_on = 0;
+  double* psw_mem = nullptr;
+  std::vector<size_t> psw_off;
   int any_f32 = 0;  // a block assembles its implicit blocks in FP32
   size_t max_icells = 0, max_icols = 0;
   std::vector<sg_block_desc> descs;   // as created (tile re-layout)
@@ -361,6 +372,70 @@ int sg_set_solve(sg_handle* h, int32_t corrections) {
   return 0;
 }
 
+namespace {
+// does block b take the partitioned form: FP64-assembled scheme 9 with
+// enough layers for four chunks
+bool psw_block(const sg_handle* h, int b) {
+  const BlockDev& B = h->host[b];
+  return B.implicit == 9 && !B.implicit_f32 &&
+         B.nc1 - 2 * B.ng >= sg::kPswMinLayers;
+}
+
+// point the served blocks at their regions (on) or at none (off)
+void psw_apply(sg_handle* h, int on) {
+  for (int b = 0; b < h->nblock; ++b)
+    h->host[b].psw = on && psw_block(h, b) ? h->psw_mem + h->psw_off[b] : nullptr;
+  h->psw_on = on;
+  h->dirty = true;
+}
+}  // namespace
+
+int sg_set_sweep(sg_handle* h, int32_t mode) {
+  if (!h || mode < 0 || mode > 2)
+    return fail(SG_ERR_ARG, "sg_set_sweep: mode %d (0 serial, 1 partitioned, "
+                "2 autotuned)", mode);
+  if (mode != 0 && !h->psw_mem) {
+    // the region: per served block 50 doubles per interior cell and an int
+    // per interior column, 16-byte aligned
+    size_t total = 0;
+    h->psw_off.assign(h->nblock, 0);
+    for (int b = 0; b < h->nblock; ++b) {
+      if (!psw_block(h, b)) continue;
+      const BlockDev& B = h->host[b];
+      const size_t n = B.nc1 - 2 * B.ng;
+      const size_t cols = (size_t)(B.nc2 > 1 ? B.nc2 - 2 * B.ng : 1) *
+                          (B.nc3 > 1 ? B.nc3 - 2 * B.ng : 1);
+      h->psw_off[b] = total;
+      size_t bytes = (sg::kPswDoublesPerCell * n * cols) * sizeof(double) +
+                     cols * sizeof(int);
+      total += (bytes + 15) / 16 * 2;  // in doubles
+    }
+    if (total) {
+      cudaError_t e = cudaMalloc(&h->psw_mem, total * sizeof(double));
+      if (e != cudaSuccess) return cuda_fail(e, "sg_set_sweep: region");
+    }
+  }
+  h->psw_mode = mode;
+  // a block table without served blocks keeps the serial solve
+  psw_apply(h, mode == 1 && h->psw_mem ? 1 : 0);
+  return 0;
+}
+
+int sg_psw_rcp(const double* x, double* r, int64_t n, sg_stream_t stream) {
+  if (n < 0 || (n > 0 && (!x || !r)))
+    return fail(SG_ERR_ARG, "sg_psw_rcp: null or negative size");
+  if (n == 0) return 0;
+  int e = sg_launch_psw_rcp_f64(x, r, (size_t)n,
+                                reinterpret_cast<cudaStream_t>(stream));
+  return e ? cuda_fail((cudaError_t)e, "sg_psw_rcp") : 0;
+}
+
+int sg_sweep(const sg_handle* h, int32_t* on) {
+  if (!h || !on) return fail(SG_ERR_ARG, "sg_sweep: null");
+  *on = h->psw_on;
+  return 0;
+}
+
 int sg_solve_fallbacks(sg_handle* h, int64_t* counts) {
   if (!h || !counts) return fail(SG_ERR_ARG, "sg_solve_fallbacks: null");
   cudaError_t e = cudaMemcpy(counts, h->fallbacks,
@@ -436,6 +511,7 @@ int sg_autotune(sg_handle* h, int32_t reps, int32_t* tj_out,
     p.first = 1;
     p.status = h->status;
     p.refine = h->refine;
+    p.psw = h->psw_on;
     p.fallbacks = h->fallbacks;
     p.max_nc1 = h->max_nc1;
     p.visc3 = h->visc3;
@@ -499,23 +575,39 @@ int sg_autotune(sg_handle* h, int32_t reps, int32_t* tj_out,
     if (!rc) rc = relayout(h, best_tj.data());
     if (!rc) rc = upload(h, s);
     // (2) the implicit solve's finish: a warp per column or a thread per
-    // column (the stage's explicit tendency is in the scratch first)
+    // column (the stage's explicit tendency is in the scratch first), and
+    // with sg_set_sweep mode 2 its solve serial or partitioned
     if (!rc && h->implicit) {
       rc = stage();
       double best = 1e300;
-      for (int form : {1, 2}) {
-        if (rc) break;
-        h->wide = form == 2;
-        double ms = 0.;
-        rc = timed(vic, &ms);
-        if (!rc && ms < best) {
-          best = ms;
-          best_finish = form;
-          best_vic = ms;
+      int best_sweep = h->psw_on;
+      const bool both = h->psw_mode == 2 && h->psw_mem;
+      for (int sweep = both ? 0 : h->psw_on; sweep <= (both ? 1 : h->psw_on);
+           ++sweep) {
+        if (both) {
+          psw_apply(h, sweep);
+          if (!rc) rc = upload(h, s);
+          p.psw = sweep;
+        }
+        for (int form : {1, 2}) {
+          if (rc) break;
+          h->wide = form == 2;
+          double ms = 0.;
+          rc = timed(vic, &ms);
+          if (!rc && ms < best) {
+            best = ms;
+            best_finish = form;
+            best_vic = ms;
+            best_sweep = sweep;
+          }
         }
       }
       h->finish = best_finish;
       h->wide = best_finish == 2;
+      if (both) {
+        psw_apply(h, best_sweep);
+        if (!rc) rc = upload(h, s);
+      }
     }
     if (!rc) {
       e = cudaMemcpyAsync(h->status, st_save, sizeof(int) * nb,
@@ -826,6 +918,7 @@ int sg_destroy(sg_handle* h) {
   if (h->ptrs_host) cudaFreeHost(h->ptrs_host);
   for (cudaEvent_t e : h->events) cudaEventDestroy(e);
   for (double* t : h->x1tabs) cudaFree(t);
+  if (h->psw_mem) cudaFree(h->psw_mem);
   delete h;
   return 0;
 }
@@ -1108,6 +1201,7 @@ int sg_stage(sg_handle* h, int32_t stage, const double* dt_dev,
   p.first = stage == 0;
   p.status = h->status;
   p.refine = h->refine;
+  p.psw = h->psw_on;
   p.fallbacks = h->fallbacks;
   p.max_nc1 = h->max_nc1;
   p.visc3 = h->visc3;
@@ -1162,7 +1256,8 @@ int sg_stage(sg_handle* h, int32_t stage, const double* dt_dev,
     // (a wide batch's finish is three launches)
     launches += 3 + (h->wide ? 2 : 0) + (h->vic_kinds == 3 ? 1 : 0) +
                 (h->asm_kinds == 3 ? 1 : 0) +
-                (h->refine > 0 ? 1 + 2 * h->refine : (h->refine < 0 ? 2 : 0));
+                (h->refine > 0 ? 2 + 2 * h->refine : (h->refine < 0 ? 3 : 0)) +
+                (h->psw_on ? 1 : 0);
   }
   if (h->scalars) {
     // the passive scalars on the stage's mass flux: face fluxes, update

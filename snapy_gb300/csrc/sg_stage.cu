@@ -2161,6 +2161,7 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 #include "sg_vic.cuh"
+#include "sg_psolve.cuh"
 
 // an implicit block's scalars after its solve, one warp per column and
 // scalar (MeshBlockImpl::stage_advance, src/mesh/meshblock_advance.cpp:
@@ -2340,6 +2341,15 @@ __global__ void __launch_bounds__(kBudgetThreads)
   budget_reduce(acc, out + NHYDRO * blockIdx.x, accumulate != 0);
 }
 
+// the partitioned solve's reciprocal on a device array (a check of its
+// error bound against the IEEE division)
+__global__ void psw_rcp_kernel(const double* __restrict__ x,
+                               double* __restrict__ r, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    r[i] = psw_rcp(x[i]);
+}
+
 }  // namespace
 }  // namespace sg
 
@@ -2514,11 +2524,21 @@ extern "C" int SG_NAME(sg_launch_vic)(const BlockDev* tab, StageParams p,
       vic_correct32_kernel<<<dim3(gc, p.nblock), 32 * kCorrWarps, 0, stream>>>(
           tab, p, k == p.refine);
     }
+    // the columns left to FP64: the partitioned FP64 solve first (a warp
+    // per column, four chunks at once), the serial one for what it cannot
+    vic_psolve_kernel<true><<<dim3((unsigned)max_cols, p.nblock), 32, 0, stream>>>(tab, p);
     e = cudaGetLastError();
     if (e != cudaSuccess) return (int)e;
   }
   // the solve: the full matrix kVicCols columns per single-warp CTA, the
-  // partial one a thread per column
+  // partial one a thread per column; blocks with the partitioned form take
+  // it first (a warp per column), the serial solve then only the columns
+  // it marked
+  if (p.psw) {
+    vic_psolve_kernel<false><<<dim3((unsigned)max_cols, p.nblock), 32, 0, stream>>>(tab, p);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return (int)e;
+  }
   if (p.vic_kinds & 1) {
     if (p.refine)
       vic_solve_kernel<true><<<dim3(gs, p.nblock), 32, 0, stream>>>(tab, p, status);
@@ -2544,6 +2564,14 @@ extern "C" int SG_NAME(sg_launch_vic)(const BlockDev* tab, StageParams p,
     int gc = (int)((max_cols + kVicWarps - 1) / kVicWarps);
     vic_finish_kernel<32><<<dim3(gc, p.nblock), 32 * kVicWarps, 0, stream>>>(tab, p);
   }
+  return (int)cudaGetLastError();
+}
+
+extern "C" int SG_NAME(sg_launch_psw_rcp)(const double* x, double* r,
+                                          size_t n, cudaStream_t stream) {
+  size_t g = (n + kThreads - 1) / kThreads;
+  if (g > 4096) g = 4096;
+  psw_rcp_kernel<<<(unsigned)g, kThreads, 0, stream>>>(x, r, n);
   return (int)cudaGetLastError();
 }
 

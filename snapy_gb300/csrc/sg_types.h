@@ -50,6 +50,11 @@ struct BlockDev {
   int32_t implicit;
   int32_t implicit_f32;  // implicit-precision float32: FP32 block assembly
   double* vic;
+  // the layer-parallel (partitioned) form of the scheme-9 solve of an
+  // FP64-assembled block (sg_set_sweep): its region, per interior cell the
+  // E and F blocks (25 doubles each), then one int per interior column
+  // (1: the serial solve redoes the column); null: the serial solve alone
+  double* psw;
   // FP32 under gravity: the state buffers hold anomalies u - u_b about an
   // FP64 hydrostatic base that depends on x1 only, laid out as
   //   rho_b[nc1] | p_b[nc1] | e_b[nc1] = p_b / (gamma - 1) | pf_b[nc1 + 1]
@@ -127,6 +132,10 @@ constexpr int kVicDoublesPerCell = 100;
 // pass (3), the largest |x| of each after the first (3) and the direct-solve
 // mask (1 int)
 constexpr int kVicFloatsPerCell = 160;
+// the partitioned form of the scheme-9 solve: columns of fewer layers take
+// the serial solve; its region holds two 5x5 blocks per interior cell
+constexpr int kPswMinLayers = 16;
+constexpr int kPswDoublesPerCell = 50;
 constexpr int kVicFloatsPerColumn = 7;
 
 // a tile's bulk-copy wait ran out (status bit; the step is rejected)
@@ -156,6 +165,8 @@ struct StageParams {
                         // bit 1 some in FP32 (one kernel each)
   int32_t ref32;        // some FP32 block keeps its reference in FP32
                         // (base_ref_kernel runs before the stage kernel)
+  int32_t psw;          // some block has the partitioned solve on
+                        // (vic_psolve_kernel runs before the serial one)
   int32_t vic_kinds;    // implicit blocks: bit 0 some with the full 5x5
                         // matrix (scheme 9), bit 1 some with the partial
                         // 3x3 one (scheme 1)

@@ -657,9 +657,20 @@ __global__ void __launch_bounds__(32)
   // refined solve left to FP64 (the mask); a warp with none leaves at once
   if (BLK32 && Bk.implicit_f32) {
     const VicScratch32 F = vic_scratch32(Bk, S, n);
-    valid = valid && F.mask[col] != 0;
+    const int mk = valid ? F.mask[col] : 0;
+    valid = valid && mk != 0;
     if (!__any_sync(0xffffffffu, valid)) return;
-    if (valid && q == 0) atomicAdd(&p.fallbacks[blockIdx.y], 1ull);
+    // mask 2: the partitioned FP64 solve took the column first and
+    // counted it
+    if (valid && mk == 1 && q == 0) atomicAdd(&p.fallbacks[blockIdx.y], 1ull);
+  }
+  // an FP64-assembled block with the partitioned form (vic_psolve_kernel,
+  // which ran first): only the columns it marked
+  if (Bk.psw && !Bk.implicit_f32) {
+    const int* mask =
+        reinterpret_cast<const int*>(Bk.psw + kPswDoublesPerCell * S.cells);
+    valid = valid && mask[col < ncol ? col : ncol - 1] != 0;
+    if (!__any_sync(0xffffffffu, valid)) return;
   }
   // a group past the last column (or unmasked) shadows a column and never
   // stores

@@ -19,7 +19,7 @@ import torch
 
 from .batch import Batch
 from .meshblock import block_of, scheme_of
-from .options import DeckError, MeshBlockOptions, shared_solve
+from .options import DeckError, MeshBlockOptions, shared_solve, shared_sweep
 
 
 class Ensemble:
@@ -46,6 +46,9 @@ class Ensemble:
         k = shared_solve(m.solve_corrections() for m in self.members)
         if k != 2:
             self.batch.set_solve(k)
+        sw = shared_sweep(m.sweep_mode() for m in self.members)
+        if sw:
+            self.batch.set_sweep(sw)
         self.nstage = len(schemes[0]["wght"])
         self.graphs = graphs
         # retry on the device (MeshBlockImpl::apply_redo per member): each

@@ -259,6 +259,8 @@ class MeshBlock:
             self._batch = Batch(self._scheme, [self._block], self.device, self.dtype)
             if self.options.solve_corrections() != 2:
                 self._batch.set_solve(self.options.solve_corrections())
+            if self.options.sweep_mode():
+                self._batch.set_sweep(self.options.sweep_mode())
             for d in sorted(self._step_dims):
                 self._batch.request_step_field(0, d)
         return self._batch

@@ -359,7 +359,7 @@ class IntegratorOptions:
                     "max_redo", "implicit-scheme", "implicit-precision",
                     "implicit-fallback-fp64", "execution", "execution-strict",
                     "restart", "autotune", "implicit-solve",
-                    "implicit-corrections"})
+                    "implicit-corrections", "implicit-sweep"})
         op.type = str(_get(node, "type", op.type))
         op.cfl = float(_get(node, "cfl", op.cfl))
         op.tlim = float(_get(node, "tlim", op.tlim))
@@ -405,6 +405,20 @@ def _scalar_names(node, op) -> List[str]:
     return names
 
 
+SWEEPS = {"serial": 0, "partitioned": 1, "auto": 2}
+
+
+def shared_sweep(modes) -> int:
+    """The one sg_set_sweep mode of blocks batched in a handle: the serial
+    sweep if any block asks for it (its results are bit for bit the
+    reference's order), the partitioned form if every block asks for it,
+    else the autotuner's choice."""
+    modes = list(modes)
+    if 0 in modes:
+        return 0
+    return 1 if all(m == 1 for m in modes) else 2
+
+
 def shared_solve(ks) -> int:
     """The one solve form of blocks batched in a handle, from their decks'
     sg_set_solve arguments: the direct FP64 solve if any block asks for it,
@@ -429,6 +443,10 @@ class MeshBlockOptions:
             return -1
         return self.implicit_corrections
 
+    def sweep_mode(self) -> int:
+        """sg_set_sweep's argument for this deck."""
+        return SWEEPS[self.implicit_sweep]
+
     def __init__(self):
         self._coord = CoordinateOptions()
         self._hydro = HydroOptions()
@@ -446,6 +464,13 @@ class MeshBlockOptions:
         # compute: the FP32 sweep alone, the FP64 retry of failed columns)
         self.implicit_solve = "refined"
         self.implicit_corrections = 2  # FP64-residual corrections (1 to 3)
+        # integration/implicit-sweep (no counterpart in the reference): the
+        # order of elimination of the scheme-9 solve of FP64-assembled
+        # blocks, "serial" (the reference's column sweep, bit for bit),
+        # "partitioned" (each column in four chunks swept at once and a
+        # separator system, for batches with few columns; the same solution
+        # to rounding) or "auto" (the autotuner times both)
+        self.implicit_sweep = "serial"
         # scalar/nvar, scalar/names: passive scalars (ScalarOptionsImpl,
         # src/scalar/scalar.hpp)
         self.scalar_names: List[str] = []
@@ -502,6 +527,10 @@ class MeshBlockOptions:
         if op.implicit_solve not in ("refined", "direct", "fp32"):
             raise DeckError("integration/implicit-solve must be refined, "
                             f"direct or fp32, got '{op.implicit_solve}'")
+        op.implicit_sweep = str(intg.get("implicit-sweep", "serial"))
+        if op.implicit_sweep not in SWEEPS:
+            raise DeckError("integration/implicit-sweep must be serial, "
+                            f"partitioned or auto, got '{op.implicit_sweep}'")
         op.implicit_corrections = int(intg.get("implicit-corrections", 2))
         if not 1 <= op.implicit_corrections <= 3:
             raise DeckError("integration/implicit-corrections must be 1 to 3, "

@@ -38,7 +38,7 @@ import torch
 from . import _lib
 from .batch import _DT, _stream, fill_base
 from .meshblock import block_of, scheme_of
-from .options import DeckError, MeshBlockOptions, shared_solve
+from .options import DeckError, MeshBlockOptions, shared_solve, shared_sweep
 
 
 @dataclass
@@ -172,6 +172,10 @@ class _Handle:
         k = shared_solve(sl.req.options.solve_corrections() for sl in slots)
         if k != 2:
             _lib.check(L.sg_set_solve(h, k), "sg_set_solve")
+        # the partitioned sweep when every request asks for it (a served
+        # handle runs no autotuner, so "auto" keeps the serial sweep)
+        if shared_sweep(sl.req.options.sweep_mode() for sl in slots) == 1:
+            _lib.check(L.sg_set_sweep(h, 1), "sg_set_sweep")
         self.dt = torch.zeros(n, dtype=torch.float64, device=device)
         self.redo = torch.zeros(n, dtype=torch.int32, device=device)
         self.flags = torch.zeros(n, dtype=torch.int32, device=device)

@@ -145,3 +145,24 @@ def test_the_reference_import_name():
     assert snapy.MeshBlock is snapy_gb300.MeshBlock
     assert snapy.MeshBlockOptions is snapy_gb300.MeshBlockOptions
     assert (snapy.kIDN, snapy.kIPR) == (snapy_gb300.kIDN, snapy_gb300.kIPR)
+
+
+def test_implicit_sweep_key():
+    """integration/implicit-sweep: serial (default), partitioned or auto;
+    a batch takes the serial sweep if any block asks for it."""
+    from snapy_gb300.options import DeckError, MeshBlockOptions, shared_sweep
+    base = {"geometry": {"type": "cartesian", "bounds": {"x1min": 0.0, "x1max": 1.0},
+                         "cells": {"nx1": 16, "nghost": 3}},
+            "dynamics": {"equation-of-state": {"type": "ideal-gas"},
+                         "riemann-solver": {"type": "hllc"}},
+            "integration": {"type": "rk3", "cfl": 0.4}}
+    assert MeshBlockOptions.from_config(base).sweep_mode() == 0
+    for name, mode in (("serial", 0), ("partitioned", 1), ("auto", 2)):
+        cfg = dict(base, integration=dict(base["integration"], **{"implicit-sweep": name}))
+        assert MeshBlockOptions.from_config(cfg).sweep_mode() == mode
+    bad = dict(base, integration=dict(base["integration"], **{"implicit-sweep": "cyclic"}))
+    with pytest.raises(DeckError):
+        MeshBlockOptions.from_config(bad)
+    assert shared_sweep([1, 1]) == 1
+    assert shared_sweep([1, 2]) == 2
+    assert shared_sweep([2, 0, 1]) == 0
