@@ -259,7 +259,7 @@ __device__ __forceinline__ void psw_sub_mv(double (&t)[5], const double* M,
 // BLK32 true: the FP32-assembled blocks' columns that the refined solve
 // (or the FP32 solve) left to the FP64 solve (mask 1), from their FP32
 // blocks widened; E and F go to the FP64 A and B slots, which such blocks
-// leave free by then.  A column it solves gets mask 0 (done), one it
+// leave free by then.  A column it solves gets mask 3 (done), one it
 // cannot mask 2 (the serial FP64 solve takes it, without counting it again)
 template <bool BLK32>
 __global__ void __launch_bounds__(32)
@@ -684,7 +684,7 @@ __global__ void __launch_bounds__(32)
   }
   if (lane == 0) {
     if (BLK32) {
-      *maskp = good ? 0 : 2;
+      *maskp = good ? 3 : 2;
     } else {
       *maskp = good ? 0 : 1;
       if (!good) atomicAdd(&p.fallbacks[blockIdx.y], 1ull);

@@ -130,7 +130,8 @@ constexpr int kVicDoublesPerCell = 100;
 // a pad); per
 // interior column the largest update of each right-hand side in the last
 // pass (3), the largest |x| of each after the first (3) and the direct-solve
-// mask (1 int)
+// mask (1 int: 0 accepted, 1 left to the FP64 solve, 2 left by the
+// partitioned FP64 solve to the serial one, 3 solved by the partitioned one)
 constexpr int kVicFloatsPerCell = 160;
 // the partitioned form of the scheme-9 solve: columns of fewer layers take
 // the serial solve; its region holds two 5x5 blocks per interior cell

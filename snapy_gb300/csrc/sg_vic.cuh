@@ -658,7 +658,7 @@ __global__ void __launch_bounds__(32)
   if (BLK32 && Bk.implicit_f32) {
     const VicScratch32 F = vic_scratch32(Bk, S, n);
     const int mk = valid ? F.mask[col] : 0;
-    valid = valid && mk != 0;
+    valid = valid && (mk == 1 || mk == 2);
     if (!__any_sync(0xffffffffu, valid)) return;
     // mask 2: the partitioned FP64 solve took the column first and
     // counted it
@@ -1847,6 +1847,7 @@ __global__ void __launch_bounds__(32 * kCorrWarps)
     const float dp = st[k];
     const float rho = dp > 0.f ? fminf(dmax / dp, 1.f) : 0.f;
     cv = fin && dmax * rho <= 0x1p-44f * st[3 + k];
+    st[k] = dmax;  // the last update, kept for inspection (nothing reads it)
   }
   // every ballot runs on all 32 lanes: evaluate before combining
   const bool cv_all = all3(cv);
