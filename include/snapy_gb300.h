@@ -255,6 +255,16 @@ int sg_solve_fallbacks(sg_handle* h, int64_t* counts);
  * interior cell of the served blocks) on first use.  Not inside a stream
  * capture; graphs captured before must be captured again. */
 int sg_set_sweep(sg_handle* h, int32_t mode);
+/* The RegisterMonitor counts of the last step (src/hydro/flux_register.hpp
+ * :61-178, the counters of src/hydro/hydro.cpp:175-192 that this path can
+ * raise): acc_dev[2 b + 0] += the x1/x2/x3 interior faces of block b whose
+ * HLLC contact pressure was clamped to zero (riemann.pstar_clamp),
+ * acc_dev[2 b + 1] += its columns the implicit solve left to the FP64 retry
+ * (implicit.fp64_columns).  acc_dev: 2 nblock device int64.  The counts
+ * start over at each step's first stage, so a rejected attempt's are gone
+ * when its retry begins, and an accepted step's stay until the next step
+ * (the monitor's census of accepted steps).  On the stream, no host sync. */
+int sg_add_step_counts(sg_handle* h, int64_t* acc_dev, sg_stream_t stream);
 /* whether the partitioned form runs now (1) or the serial one (0) */
 int sg_sweep(const sg_handle* h, int32_t* on);
 /* A check of the partitioned form's reciprocal (no counterpart in the

@@ -67,6 +67,7 @@ class OgBlock(ctypes.Structure):
         ("scalar", _dp),
         ("scalar0", _dp),
         ("vic_q", _dp),
+        ("monitor", ctypes.POINTER(ctypes.c_longlong)),
     ]
 
 
@@ -298,6 +299,14 @@ class Block:
         self.b.scalar, self.b.scalar0 = ptr(self._s), ptr(self._s0)
         lib().og_scalar_bc(ctypes.byref(self.b), ptr(self._s))
         return self._s
+
+    def count_monitor(self) -> np.ndarray:
+        """The monitor count the stages raise from here on, [0] the interior
+        faces whose HLLC contact pressure was clamped (riemann.pstar_clamp);
+        returns the array the stages add into."""
+        self._monitor = np.zeros(1, dtype=np.int64)
+        self.b.monitor = self._monitor.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong))
+        return self._monitor
 
     def keep_totals(self, dim: int) -> np.ndarray:
         """The buffer each stage copies its register total T_dim into."""

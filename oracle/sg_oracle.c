@@ -308,6 +308,15 @@ void og_cons2prim_cell(const double* u, double* w, double gammad, int s) {
 /* ------------------------------------------------------------------ */
 /* block operations                                                    */
 /* ------------------------------------------------------------------ */
+/* the monitor's riemann.pstar_clamp: an HLLC face whose contact pressure
+ * was clamped to zero (src/riemann/riemann.cpp:330-339) */
+static void count_clamp(const og_block* b, double cp) {
+  if (b->monitor && cp <= 0.0) {
+#pragma omp atomic
+    b->monitor[0] += 1;
+  }
+}
+
 void og_default_block(og_block* b) {
   memset(b, 0, sizeof(*b));
   b->nvar = 5;
@@ -458,10 +467,18 @@ void og_flux(const og_block* b, const double* w, int d, double* flux) {
         wl[v] = ilt[v * n + f];
         wr[v] = irt[v * n + f];
       }
-      if (b->riemann == OG_HLLC)
-        og_hllc_face(wl, wr, b->gammad, dim, fx, NULL);
-      else
+      if (b->riemann == OG_HLLC) {
+        double cp;
+        og_hllc_face(wl, wr, b->gammad, dim, fx, &cp);
+        /* the interior faces: f = ng..n-ng along the line, interior cells
+         * across it */
+        int ng = b->ng;
+        int inner_a = la == 1 || (a >= ng && a < la - ng);
+        int inner_b = lb == 1 || (bidx >= ng && bidx < lb - ng);
+        if (inner_a && inner_b && f >= ng && f <= n - ng) count_clamp(b, cp);
+      } else {
         og_lmars_face(wl, wr, b->gammad, dim, fx, NULL);
+      }
       for (int v = 0; v < 5; ++v) flux[v * nc + base + f * s] = fx[v];
     }
     free(ilt);
@@ -675,10 +692,13 @@ static void face_lr(const og_block* b, const double* line, size_t s,
 
 static void riemann_face(const og_block* b, const double* wl, const double* wr,
                          int d, double* fx) {
-  if (b->riemann == OG_HLLC)
-    og_hllc_face(wl, wr, b->gammad, 4 - d, fx, NULL);
-  else
+  if (b->riemann == OG_HLLC) {
+    double cp;
+    og_hllc_face(wl, wr, b->gammad, 4 - d, fx, &cp);
+    count_clamp(b, cp);
+  } else {
     og_lmars_face(wl, wr, b->gammad, 4 - d, fx, NULL);
+  }
 }
 
 #define CELL(v, j, i) ((size_t)(v) * nc + (size_t)(j) * n1 + (size_t)(i))

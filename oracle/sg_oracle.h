@@ -70,6 +70,11 @@ typedef struct og_block {
    * scalars' share of them): the clamped dry transfer q of each x1 face,
    * face f below cell f; set by og_stage itself */
   double* vic_q;
+  /* the RegisterMonitor count this path can raise in the stage
+   * (src/riemann/riemann.cpp:330-339): monitor[0] += the interior faces
+   * whose HLLC contact pressure was clamped to zero (riemann.pstar_clamp);
+   * NULL: not counted */
+  long long* monitor;
 } og_block;
 
 /* ---- unit functions (pinned against the reference headers) ---- */

@@ -117,6 +117,7 @@ SIGNATURES = {
     "sg_set_sweep": (ctypes.c_int, [_vp, _i32]),
     "sg_sweep": (ctypes.c_int, [_vp, ctypes.POINTER(_i32)]),
     "sg_psw_rcp": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp]),
+    "sg_add_step_counts": (ctypes.c_int, [_vp, _vp, _vp]),
     "sg_autotune": (ctypes.c_int, [_vp, _i32, _vp, _vp, _vp, _vp]),
     "sg_set_schedule": (ctypes.c_int, [_vp, _vp, _i32]),
     "sg_check_retry": (ctypes.c_int, [_vp, _vp, _vp, _i32, _vp, _vp]),

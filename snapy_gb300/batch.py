@@ -382,6 +382,17 @@ class Batch:
         _lib.check(self.L.sg_set_sweep(self.h, int(mode)), "sg_set_sweep")
         self.sweep_mode = int(mode)
 
+    def add_step_counts(self, acc: torch.Tensor, stream=None) -> torch.Tensor:
+        """acc (nblock, 2) int64 on the device += the last step's monitor
+        counts per block: riemann.pstar_clamp, implicit.fp64_columns."""
+        if acc.dtype != torch.int64 or tuple(acc.shape) != (self.nblock, 2) \
+                or not acc.is_contiguous() or acc.device != self.device:
+            raise ValueError("add_step_counts: a contiguous (nblock, 2) int64 "
+                             f"tensor on {self.device}")
+        _lib.check(self.L.sg_add_step_counts(self.h, acc.data_ptr(), _stream(stream)),
+                   "sg_add_step_counts")
+        return acc
+
     def sweep(self) -> int:
         """1 while the partitioned form runs, else 0."""
         on = ctypes.c_int32()

@@ -200,6 +200,13 @@ __global__ void x1tab_kernel(const double* x1f, const double* x1v, int ng,
   }
 }
 
+// acc[k] += counts[k] over the nblock * kCountSlots monitor counts
+__global__ void add_counts_kernel(int n, const unsigned long long* counts,
+                                  int64_t* acc) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) acc[k] += (int64_t)counts[k];
+}
+
 __global__ void init_red_kernel(int n, unsigned long long* red, int* nan) {
   int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= n) return;
@@ -226,6 +233,8 @@ struct sg_handle {
   int* status = nullptr;  // per-block solve status bits (VIC failures)
   unsigned long long* fallbacks = nullptr;  // per block: refined-solve
                                             // columns solved directly
+  unsigned long long* counts = nullptr;  // per block, kCountSlots: the
+                                         // current step's monitor counts
   std::vector<double*> x1tabs;  // per-block geometry tables (gravity)
   bool has3 = false;            // a 3-D block: the x3 sweep runs
   bool visc3 = false;           // a 3-D block with viscosity: the prep runs
@@ -428,6 +437,16 @@ int sg_psw_rcp(const double* x, double* r, int64_t n, sg_stream_t stream) {
   int e = sg_launch_psw_rcp_f64(x, r, (size_t)n,
                                 reinterpret_cast<cudaStream_t>(stream));
   return e ? cuda_fail((cudaError_t)e, "sg_psw_rcp") : 0;
+}
+
+int sg_add_step_counts(sg_handle* h, int64_t* acc_dev, sg_stream_t stream) {
+  if (!h || !acc_dev) return fail(SG_ERR_ARG, "sg_add_step_counts: null");
+  const int n = sg::kCountSlots * h->nblock;
+  add_counts_kernel<<<(n + 127) / 128, 128, 0,
+                      reinterpret_cast<cudaStream_t>(stream)>>>(n, h->counts,
+                                                                acc_dev);
+  cudaError_t e = cudaGetLastError();
+  return e != cudaSuccess ? cuda_fail(e, "sg_add_step_counts") : 0;
 }
 
 int sg_sweep(const sg_handle* h, int32_t* on) {
@@ -892,6 +911,10 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
     e = cudaMalloc(&h->fallbacks, sizeof(unsigned long long) * nblock);
   if (e == cudaSuccess)
     e = cudaMemset(h->fallbacks, 0, sizeof(unsigned long long) * nblock);
+  if (e == cudaSuccess)
+    e = cudaMalloc(&h->counts, sizeof(unsigned long long) * sg::kCountSlots * nblock);
+  if (e == cudaSuccess)
+    e = cudaMemset(h->counts, 0, sizeof(unsigned long long) * sg::kCountSlots * nblock);
   if (e == cudaSuccess) e = cudaMallocHost(&h->ptrs_host, sizeof(void*) * nblock);
   if (e != cudaSuccess) {
     sg_destroy(h);
@@ -915,6 +938,7 @@ int sg_destroy(sg_handle* h) {
   if (h->ptrs) cudaFree(h->ptrs);
   if (h->status) cudaFree(h->status);
   if (h->fallbacks) cudaFree(h->fallbacks);
+  if (h->counts) cudaFree(h->counts);
   if (h->ptrs_host) cudaFreeHost(h->ptrs_host);
   for (cudaEvent_t e : h->events) cudaEventDestroy(e);
   for (double* t : h->x1tabs) cudaFree(t);
@@ -1201,6 +1225,7 @@ int sg_stage(sg_handle* h, int32_t stage, const double* dt_dev,
   p.first = stage == 0;
   p.status = h->status;
   p.refine = h->refine;
+  p.counts = h->counts;
   p.psw = h->psw_on;
   p.fallbacks = h->fallbacks;
   p.max_nc1 = h->max_nc1;
@@ -1227,6 +1252,13 @@ int sg_stage(sg_handle* h, int32_t stage, const double* dt_dev,
       ev[k] = h->events[eidx[k]];
     }
     cudaEventRecord(ev[0], s);
+  }
+  if (stage == 0) {
+    // the monitor's counts start over with the step (a rejected attempt's
+    // counts are gone when its retry begins)
+    cudaError_t ze = cudaMemsetAsync(
+        h->counts, 0, sizeof(unsigned long long) * sg::kCountSlots * h->nblock, s);
+    if (ze != cudaSuccess) return cuda_fail(ze, "sg_stage: monitor counts");
   }
   int launches = h->ref32 ? 3 : 2;  // (with the base reference's refresh)
   if (h->has3) {

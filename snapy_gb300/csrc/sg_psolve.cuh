@@ -286,7 +286,7 @@ __global__ void __launch_bounds__(32)
     A32 = F32.A + col * n * kBlk32;
     B32 = F32.B + col * n * kBlk32;
     C32 = F32.C + col * n * kBlk32;
-    if (threadIdx.x == 0) atomicAdd(&p.fallbacks[blockIdx.y], 1ull);
+    if (threadIdx.x == 0) count_fp64_column(p, blockIdx.y);
   } else {
     W = psw_scratch(Bk, S.cells);
     maskp = W.mask + col;
@@ -686,6 +686,8 @@ __global__ void __launch_bounds__(32)
     if (BLK32) {
       *maskp = good ? 3 : 2;
     } else {
+      // (a column the reference's serial order would solve the same way:
+      // not its FP64 retry, so not in the monitor's count)
       *maskp = good ? 0 : 1;
       if (!good) atomicAdd(&p.fallbacks[blockIdx.y], 1ull);
     }

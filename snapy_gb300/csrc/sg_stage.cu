@@ -141,13 +141,19 @@ __device__ __forceinline__ void face_states(const real* q, int vstride,
   }
 }
 
+// nclamp: one more when HLLC's contact pressure was clamped to zero (the
+// monitor's riemann.pstar_clamp event, src/riemann/riemann.cpp:330-339)
 template <int RK>
 __device__ __forceinline__ void riemann(const real* wl, const real* wr,
-                                        real gammad, int d, real* flx) {
-  if (RK == kHllc)
-    hllc_flux<real>(wl, wr, gammad, d, flx, nullptr);
-  else
+                                        real gammad, int d, real* flx,
+                                        unsigned& nclamp) {
+  if (RK == kHllc) {
+    real cp;
+    hllc_flux<real>(wl, wr, gammad, d, flx, &cp);
+    nclamp += cp <= real(0) ? 1u : 0u;
+  } else {
     lmars_flux<real>(wl, wr, gammad, d, flx, nullptr);
+  }
 }
 
 // smem layout of a tile (counts in `real`), shared by the kernel and the
@@ -543,6 +549,7 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
   const bool scale = p.scale != 0;
   const int il = ng, iu1 = nc1 - ng;  // interior x1 cells il..iu1-1
   const double dt = p.dt[bi];
+  unsigned nclamp = 0;  // this thread's HLLC contact-pressure clamps
   // FP32 under gravity: the buffers hold anomalies about the FP64 base
   // (rho_b, 0, 0, 0, e_b)(x1); the tile keeps the total rho and the
   // pressure anomaly p - p_b, and every Riemann solve works on anomalies
@@ -911,7 +918,7 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
       lmars_flux_anom<real>(wl, wr, gammad, 1, real(pbf[f]), flx);
 #endif
     else
-      riemann<RK>(wl, wr, gammad, 1, flx);
+      riemann<RK>(wl, wr, gammad, 1, flx, nclamp);
     if ((fi == 0 && B.bc[0] == kBcReflecting) ||
         (fi == nx1 && B.bc[1] == kBcReflecting))
       flx[IDN] = flx[IPR] = real(0);
@@ -945,8 +952,12 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
       if (i >= il && i < iu1) {
         if (pbc)
           lmars_flux_anom<real>(wl, wr, gammad, 2, pb_r(i), flx);
-        else
-          riemann<RK>(wl, wr, gammad, 2, flx);
+        else {
+          // a tile's last face is the next tile's first: counted there
+          unsigned c = 0;
+          riemann<RK>(wl, wr, gammad, 2, flx, c);
+          if (jf < ntj || j0 + ntj == jend) nclamp += c;
+        }
 #pragma unroll
         for (int v = 0; v < NHYDRO; ++v)
           F2[v * f2stride + jf * nx1 + (i - il)] = flx[v];
@@ -1265,6 +1276,8 @@ __device__ __forceinline__ bool stage_tile(const BlockDev* __restrict__ tab,
       uout[q] = w0 * u0[q] + w1 * uin[q] + w2 * du[v];
     }
   }
+  if (nclamp && p.counts)
+    atomicAdd(&p.counts[bi * kCountSlots + kCountPstar], (unsigned long long)nclamp);
   return true;
 }
 
@@ -1903,8 +1916,14 @@ __global__ void __launch_bounds__(kThreads)
       }
       if (pbc)
         lmars_flux_anom<real>(wl, wr, gammad, 3, pb, flx);
-      else
-        riemann<RK>(wl, wr, gammad, 3, flx);
+      else {
+        // a chunk owns its faces but the top one (the next chunk's), except
+        // the block's last face
+        unsigned c = 0;
+        riemann<RK>(wl, wr, gammad, 3, flx, c);
+        if (c && own && (f < k1 || k1 == ng + nx3) && p.counts)
+          atomicAdd(&p.counts[blockIdx.y * kCountSlots + kCountPstar], 1ull);
+      }
       if (cov) flx[IPR] += dcov;
       if ((f == ng && wlo) || (f == ng + nx3 && whi))
         flx[IDN] = flx[IPR] = real(0);

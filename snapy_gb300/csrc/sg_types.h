@@ -139,6 +139,14 @@ constexpr int kPswMinLayers = 16;
 constexpr int kPswDoublesPerCell = 50;
 constexpr int kVicFloatsPerColumn = 7;
 
+// the monitor's counts of a step, per block (the RegisterMonitor counters
+// src/hydro/hydro.cpp:175-192 that this path can raise): HLLC faces whose
+// contact pressure was clamped to zero, and columns the implicit solve
+// left to its FP64 retry; zeroed at each step's first stage
+constexpr int kCountPstar = 0;
+constexpr int kCountFp64Columns = 1;
+constexpr int kCountSlots = 2;
+
 // a tile's bulk-copy wait ran out (status bit; the step is rejected)
 constexpr int32_t kStatusStaging = 1 << 30;
 
@@ -157,6 +165,8 @@ struct StageParams {
                         // implicit-precision float32 blocks (0: direct)
   unsigned long long* fallbacks;  // per block: columns the refined solve left
                                   // to the direct FP64 solve (a running count)
+  unsigned long long* counts;     // per block, kCountSlots: this step's
+                                  // monitor counts (null: none kept)
   int32_t* status;      // per-block status bits (kStatusStaging: a tile's
                         // staging wait ran out)
   int32_t smem_rows;    // x1 lines held in shared memory per tile

@@ -97,6 +97,13 @@ __device__ __forceinline__ size_t vic_row(const BlockDev& B, size_t col) {
 // bit of the per-block status word: a column's solve failed this step
 constexpr int kVicFailed = 32;
 
+// a column left to the FP64 solve: the running count and the step's
+// monitor count (implicit.fp64_columns)
+__device__ __forceinline__ void count_fp64_column(const StageParams& p, int b) {
+  atomicAdd(&p.fallbacks[b], 1ull);
+  if (p.counts) atomicAdd(&p.counts[b * kCountSlots + kCountFp64Columns], 1ull);
+}
+
 template <typename T>
 __device__ __forceinline__ void vmat_mul(const T* a, const T* b,
                                          T* out) {
@@ -662,7 +669,7 @@ __global__ void __launch_bounds__(32)
     if (!__any_sync(0xffffffffu, valid)) return;
     // mask 2: the partitioned FP64 solve took the column first and
     // counted it
-    if (valid && mk == 1 && q == 0) atomicAdd(&p.fallbacks[blockIdx.y], 1ull);
+    if (valid && mk == 1 && q == 0) count_fp64_column(p, blockIdx.y);
   }
   // an FP64-assembled block with the partitioned form (vic_psolve_kernel,
   // which ran first): only the columns it marked

@@ -341,15 +341,21 @@ class MeshBlock:
     # -- restart (src/output/restart.cpp, src/mesh/meshblock_restart.cpp) ---
     def write_restart(self, vars: dict, out_dir: str, basename: str = "snapy",
                       number: int = 0, time: float = 0.0, final: bool = False,
-                      rank: int = 0, combine: bool = True) -> str:
+                      rank: int = 0, combine: bool = True, budget=None,
+                      budget_fires: bool = False) -> str:
         """Write this block's restart part (RestartOutput::write_output_file,
         src/output/restart.cpp:40-140) and, with `combine`, the restart
         file of the parts present (combine_blocks); returns its path (the
         part's without `combine`).  Every tensor of vars is written on the
         CPU; hydro_u holds the conserved totals, and a block stored as
         anomalies about an FP64 hydrostatic base adds the stored bits, the
-        base and the metadata [version, bits] with the grid faces."""
+        base and the metadata [version, bits] with the grid faces.  With a
+        budget consumer, its open interval goes along as the budget carry
+        (BudgetOutput::save_carry, src/output/budget_series.cpp:224-227;
+        budget_fires: the budget records at this time in the same pass); a
+        carry read back from an earlier restart is not written again."""
         from . import restart as R
+        from .budget import CARRY_PREFIX, write_budget_carry
         os.makedirs(out_dir, exist_ok=True)
         with torch.cuda.device(self.device):
             self._adopt(vars)
@@ -357,6 +363,8 @@ class MeshBlock:
             skip_r = "scalar_s" in vars and "hydro_u" in vars
             for name, var in vars.items():
                 if skip_r and name == "scalar_r":
+                    continue
+                if name.startswith(CARRY_PREFIX):
                     continue
                 if isinstance(var, torch.Tensor) and var.numel():
                     out[name] = var.detach().cpu()
@@ -383,19 +391,25 @@ class MeshBlock:
         out["file_number"] = torch.tensor([number + (0 if final else 1)],
                                           dtype=torch.int64)
         out["next_time"] = torch.tensor([float(time)], dtype=torch.float64)
+        if budget is not None:
+            write_budget_carry(budget.carry(self, vars, budget_fires), out)
         part = os.path.join(out_dir, R.part_name(basename, rank, number, final))
         R.save_part(out, part)
         return R.combine(out_dir, basename, number, final) if combine else part
 
     def initialize_from_restart(self, vars: dict, fname: str,
-                                rank: int = 0) -> float:
+                                rank: int = 0, budget=None) -> float:
         """Resume from a restart file (MeshBlockImpl::_init_from_restart,
         src/mesh/meshblock_restart.cpp:33-236): the block's part, the
         required variables and the metadata checks; the cycle, the state
         (an anomaly block takes its stored bits and its FP64 base back, so
         the run continues bit for bit) and the tracers; vars gets every
-        other variable of the file on the device.  Returns the time."""
+        other variable of the file on the device.  With a budget consumer,
+        its interval resumes from the file's budget carry when the carry's
+        rows are the block's (BudgetOutput::load_carry); else it starts
+        afresh at the next observe.  Returns the time."""
         from . import restart as R
+        from .budget import ROWS, read_budget_carry
         data = R.load_restart(fname, rank)
         R.require(data)
         c = self.options.coord()
@@ -442,6 +456,8 @@ class MeshBlock:
             self._seen.clear()
             self.intg.current_redo = 0
             self._refresh_w(vars)
+            if budget is not None:
+                budget.resume(self, read_budget_carry(data, ROWS))
         return t
 
     def _publish(self, vars: dict) -> None:

@@ -124,3 +124,32 @@ def test_metadata_checks():
 def test_required_variables():
     with pytest.raises(R.RestartError, match="missing required variable: next_time"):
         R.require({"hydro_u": 0, "last_time": 0, "last_cycle": 0, "file_number": 0})
+
+
+def test_budget_carry_keys_round_trip():
+    """write_budget_carry / read_budget_carry (src/output/restart.cpp
+    :383-407): the six budget_carry.* keys, the row names packed as one
+    newline-terminated int8 tensor; a carry with other rows, or a file
+    without one, starts a new interval (None)."""
+    import numpy as np
+    from snapy_gb300 import budget as Bg
+    c = Bg.BudgetCarry(rows=list(Bg.ROWS), total_prev=np.arange(5.0),
+                       pending=np.full(5, 0.5),
+                       counter=np.arange(len(Bg.COUNTERS), dtype=np.int64),
+                       minimum=np.full(len(Bg.MINIMA), np.inf), interval=1.25)
+    out = {}
+    Bg.write_budget_carry(c, out)
+    assert sorted(out) == sorted(Bg.CARRY_PREFIX + k for k in (
+        "rows", "total_prev", "pending", "counter", "minimum", "interval"))
+    assert out[Bg.CARRY_PREFIX + "rows"].dtype == torch.int8
+    assert bytes(out[Bg.CARRY_PREFIX + "rows"].view(torch.uint8).tolist()) == \
+        ("\n".join(Bg.ROWS) + "\n").encode()
+    back = Bg.read_budget_carry(out, Bg.ROWS)
+    assert back.rows == Bg.ROWS and back.interval == 1.25
+    assert np.array_equal(back.total_prev, c.total_prev)
+    assert np.array_equal(back.counter, c.counter)
+    assert np.isinf(back.minimum).all()
+    assert Bg.read_budget_carry(out, Bg.ROWS[:4]) is None
+    del out[Bg.CARRY_PREFIX + "pending"]
+    assert Bg.read_budget_carry(out, Bg.ROWS) is None
+    Bg.write_budget_carry(None, out)  # an undefined carry writes nothing
