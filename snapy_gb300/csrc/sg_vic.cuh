@@ -1961,12 +1961,45 @@ __device__ __forceinline__ void ff_madd(float& sh, float& sl, float t, float d) 
   sh = s2;
 }
 
+// s_h + (m_h + m_l) += t d, t and d floats, to well beyond FP64 accuracy:
+// the product split exactly (Dekker's two-product by an FMA), its high part
+// added to s_h by Knuth's two-sum, and the two exact remainders (the sum's
+// rounding error and the product's low part) gathered in the float-float
+// pair m_h + m_l.  The pair holds terms of 2^-24 of the products, so its
+// own error is about 2^-48 of that: 2^-72 of the sum of |t d|
+__device__ __forceinline__ void ff_acc(float& mh, float& ml, float v) {
+  const float s2 = __fadd_rn(mh, v);
+  const float bp = __fadd_rn(s2, -mh);
+  ml = __fadd_rn(ml, __fadd_rn(__fadd_rn(mh, -__fadd_rn(s2, -bp)),
+                               __fadd_rn(v, -bp)));
+  mh = s2;
+}
+
+__device__ __forceinline__ void tf_madd(float& sh, float& mh, float& ml, float t,
+                                        float d) {
+  const float p = __fmul_rn(t, d);
+  const float e = __fmaf_rn(t, d, -p);
+  const float s2 = __fadd_rn(sh, p);
+  const float bp = __fadd_rn(s2, -sh);
+  const float err =
+      __fadd_rn(__fadd_rn(sh, -__fadd_rn(s2, -bp)), __fadd_rn(p, -bp));
+  sh = s2;
+  ff_acc(mh, ml, err);
+  ff_acc(mh, ml, e);
+}
+
 // the residual r = b - (B_i x_(i-1) + A_i x_i + C_i x_(i+1)) of every cell
 // and right-hand side (one thread per cell), rounded to FP32 into R for the
 // correction's sweeps.
-// * The first correction (corr 1) forms it in FP64 from the FP32-assembled
-//   blocks widened to FP64 (exact) and x in D, Z0, Z1, and keeps the FP64 r
-//   (in the B scratch, which the refined solve does not use otherwise).
+// * The first correction (corr 1) forms it from the FP32-assembled blocks
+//   and x in D, Z0, Z1, which the FP32 sweep wrote as floats widened
+//   (exact): T x as a sum of exact float products (tf_madd, on the FP32
+//   pipe, to about 2^-72 of the sum of |t x|), then b minus that sum in
+//   FP64 (three subtractions, the first exact); it keeps the FP64 r (in the
+//   B scratch, which the refined solve does not use otherwise).  Formed
+//   with FP64 multiply-adds instead, the sum took 225 FP64 instructions per
+//   cell and kept the FP64 pipe 83 % busy; its rounding, 2^-53 per add,
+//   was the coarser of the two.
 // * A later correction forms it from the previous one: x grew by the FP32
 //   correction d (kept in the C scratch by vic_correct32_kernel), so
 //   r_new = r - T d.  T and d are floats, so T d is summed in float-float
@@ -2000,31 +2033,35 @@ __global__ void __launch_bounds__(kThreads)
       double t[5];
       if (corr == 1) {
         const double* x = (k == 0 ? S.D : (k == 1 ? S.Z0 : S.Z1)) + cell * 5;
-#pragma unroll
-        for (int r = 0; r < 5; ++r)
-          t[r] = k == 0 ? vdiv(S.du[(size_t)r * S.cells + cell], dtc, rdtc)
-                        : ((r == 4 && i == (k == 1 ? 0 : n - 1)) ? 1. : 0.);
+        float sh[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, mh[5] = {0.f, 0.f, 0.f, 0.f, 0.f},
+              ml[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
         for (int q = 0; q < 5; ++q) {
-          const double xc = x[q];
+          const float xc = narrow_exact(x[q]);
 #pragma unroll
-          for (int r = 0; r < 5; ++r) t[r] = fma(-widen_exact(a[r * 5 + q]), xc, t[r]);
+          for (int r = 0; r < 5; ++r) tf_madd(sh[r], mh[r], ml[r], a[r * 5 + q], xc);
         }
         if (i > 0) {
 #pragma unroll
           for (int q = 0; q < 5; ++q) {
-            const double xl = x[q - 5];
+            const float xl = narrow_exact(x[q - 5]);
 #pragma unroll
-            for (int r = 0; r < 5; ++r) t[r] = fma(-widen_exact(bl[r * 5 + q]), xl, t[r]);
+            for (int r = 0; r < 5; ++r) tf_madd(sh[r], mh[r], ml[r], bl[r * 5 + q], xl);
           }
         }
         if (i < n - 1) {
 #pragma unroll
           for (int q = 0; q < 5; ++q) {
-            const double xu = x[q + 5];
+            const float xu = narrow_exact(x[q + 5]);
 #pragma unroll
-            for (int r = 0; r < 5; ++r) t[r] = fma(-widen_exact(c[r * 5 + q]), xu, t[r]);
+            for (int r = 0; r < 5; ++r) tf_madd(sh[r], mh[r], ml[r], c[r * 5 + q], xu);
           }
+        }
+#pragma unroll
+        for (int r = 0; r < 5; ++r) {
+          const double b = k == 0 ? vdiv(S.du[(size_t)r * S.cells + cell], dtc, rdtc)
+                                  : ((r == 4 && i == (k == 1 ? 0 : n - 1)) ? 1. : 0.);
+          t[r] = ((b - widen_exact(sh[r])) - widen_exact(mh[r])) - widen_exact(ml[r]);
         }
       } else {
         float sh[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, sl[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
@@ -2058,7 +2095,7 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
       for (int r = 0; r < 5; ++r) {
         if (keep) rb[r] = t[r];
-        F.R[cell * kR32 + k * 5 + r] = (float)t[r];
+        F.R[cell * kR32 + k * 5 + r] = narrow_exact(t[r]);
       }
     }
   }
