@@ -155,6 +155,12 @@ def parse():
                          "against (GiB; 0: the device's free memory)")
     ap.add_argument("--serve-steps", type=int, default=200,
                     help="serving: RK3 steps per request")
+    ap.add_argument("--plain-sweep", choices=["serial", "partitioned", "auto"],
+                    default="serial",
+                    help="ensemble and serving: the plain FP64 path's column "
+                         "solve order (serial: the reference's, bit for bit "
+                         "with the oracle; auto: the autotuner picks the "
+                         "faster of it and the partitioned form per block)")
     return ap.parse_args()
 
 
@@ -767,6 +773,7 @@ def run_ensemble(args, ranks=None, emit=True):
         c, c0 = o64.coord(), opts.coord()
         c.nx1, c.nx2, c.x1max, c.x2max = c0.nx1, c0.nx2, c0.x1max, c0.x2max
         o64.hydro().precision = "float64"
+        o64.implicit_sweep = args.plain_sweep
         pairs.append((o64, (lambda w=w: w)))
     plain = plain_fp64_blocks(pairs, dev) if not args.no_plain else \
         {"device": float("nan"), "wall": float("nan"), "steps_per_request": 0}
@@ -789,6 +796,7 @@ def run_ensemble(args, ranks=None, emit=True):
                     "d2h_bytes_per_step": nbytes},
             "plain_fp64": {"device": plain["device"], "wall": plain["wall"],
                            "unit": "cell-updates/s",
+                           "sweep": args.plain_sweep,
                            "how": "each member its own FP64 MeshBlock, one "
                                   "after another, graphs on; device: CUDA "
                                   f"events around {plain['steps_per_request']} "
@@ -926,7 +934,7 @@ def as_fp64(opts):
     return o
 
 
-def plain_fp64(reqs, dev, steps=3):
+def plain_fp64(reqs, dev, steps=3, sweep="serial"):
     """plain_fp64_blocks over serving requests: each grid shape of the trace
     is measured once (on its first request), and the trace's plain time is
     every request's cell-steps at its shape's rate."""
@@ -937,6 +945,7 @@ def plain_fp64(reqs, dev, steps=3):
     rate = {}
     for shape, r in first.items():
         o64 = as_fp64(r.options)
+        o64.implicit_sweep = sweep
         rate[shape] = plain_fp64_blocks([(o64, r.initial)], dev, steps)
     out = {"steps_per_request": steps, "shapes": len(rate)}
     for clock in ("device", "wall"):
@@ -1065,7 +1074,7 @@ def run_serving(args, ranks=None, emit=True):
     achieved = value * b_alg(s_bytes) / 1e9
     ktot = sum(v[0] for v in kms.values())
     # the same requests on the plain FP64 GPU path, both clocks
-    plain = plain_fp64(reqs, dev) if not args.no_plain else \
+    plain = plain_fp64(reqs, dev, sweep=args.plain_sweep) if not args.no_plain else \
         {"device": float("nan"), "wall": float("nan"), "steps_per_request": 0}
     # the smallest request alone (a fresh server) equals itself in the mix,
     # and its FP32 result against the FP64 path at the served horizon
@@ -1118,6 +1127,7 @@ def run_serving(args, ranks=None, emit=True):
                             "device->host"},
             "plain_fp64": {"device": plain["device"], "wall": plain["wall"],
                            "unit": "cell-updates/s",
+                           "sweep": args.plain_sweep,
                            "how": "each request alone, its own FP64 MeshBlock, "
                                   "graphs on; device: CUDA events around "
                                   f"{plain['steps_per_request']} steps at a fixed "
