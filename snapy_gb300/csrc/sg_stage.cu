@@ -2528,8 +2528,8 @@ extern "C" int SG_NAME(sg_launch_vic)(const BlockDev* tab, StageParams p,
   // Woodbury step alone; the columns either leaves are solved directly
   int gs = (int)((max_cols + kVicCols - 1) / kVicCols);
   if (p.refine) {
-    int gr = (int)((max_cells + kThreads - 1) / kThreads);
-    if (gr > 4096) gr = 4096;
+    int gr = (int)((max_cells + kResThreads - 1) / kResThreads);
+    if (gr > 4096 * (kThreads / kResThreads)) gr = 4096 * (kThreads / kResThreads);
     const size_t cw = (max_cols + kCorrCols - 1) / kCorrCols;  // warps
     const int gc = (int)((cw + kCorrWarps - 1) / kCorrWarps);
     vic_solve32_kernel<<<dim3(gs, p.nblock), 32, 0, stream>>>(tab, p);
@@ -2539,7 +2539,7 @@ extern "C" int SG_NAME(sg_launch_vic)(const BlockDev* tab, StageParams p,
       vic_woodbury32_kernel<<<dim3(gw, p.nblock), kThreads, 0, stream>>>(tab, p);
     }
     for (int k = 1; k <= p.refine; ++k) {
-      vic_residual_kernel<<<dim3(gr, p.nblock), kThreads, 0, stream>>>(tab, p, k);
+      vic_residual_kernel<<<dim3(gr, p.nblock), kResThreads, 0, stream>>>(tab, p, k);
       vic_correct32_kernel<<<dim3(gc, p.nblock), 32 * kCorrWarps, 0, stream>>>(
           tab, p, k == p.refine);
     }
@@ -2573,11 +2573,11 @@ extern "C" int SG_NAME(sg_launch_vic)(const BlockDev* tab, StageParams p,
   if (ev) cudaEventRecord(ev[1], stream);
   if (wide) {
     // three passes: per cell, the serial scans per column, per cell
-    int gt = (int)((max_cols + kThreads - 1) / kThreads);
+    int gt = (int)((max_cols + kFinishBThreads - 1) / kFinishBThreads);
     int gc = (int)((max_cells + kThreads - 1) / kThreads);
     if (gc > 8192) gc = 8192;
     vic_finish_a_kernel<<<dim3(gc, p.nblock), kThreads, 0, stream>>>(tab, p);
-    vic_finish_b_kernel<<<dim3(gt, p.nblock), kThreads, 0, stream>>>(tab, p);
+    vic_finish_b_kernel<<<dim3(gt, p.nblock), kFinishBThreads, 0, stream>>>(tab, p);
     vic_finish_c_kernel<<<dim3(gc, p.nblock), kThreads, 0, stream>>>(tab, p);
   } else {
     int gc = (int)((max_cols + kVicWarps - 1) / kVicWarps);

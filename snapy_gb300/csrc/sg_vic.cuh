@@ -2013,7 +2013,11 @@ __device__ __forceinline__ void tf_madd(float& sh, float& mh, float& ml, float t
 //   2^-20 |x|, is far below the FP64 rounding of r); the two FP64 subtractions
 //   that remain replace 225 FP64 multiply-adds per cell.  The rounding of
 //   x += d in FP64 adds at most 2^-53 |x| to x, the FP64 residual's own level.
-__global__ void __launch_bounds__(kThreads)
+#ifndef SG_RES_THREADS
+#define SG_RES_THREADS 256
+#endif
+constexpr int kResThreads = SG_RES_THREADS;
+__global__ void __launch_bounds__(kResThreads)
     vic_residual_kernel(const BlockDev* __restrict__ tab, StageParams p,
                         int corr) {
   const BlockDev& B = tab[blockIdx.y];
@@ -2408,7 +2412,14 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
-__global__ void __launch_bounds__(kThreads)
+// a thread per column: small CTAs spread a batch's few columns (21,120 for
+// the 64-member ensemble) over every SM (one box, the ensemble's finish:
+// 514 us per stage with 256 threads, 472 with 64, 463 with 32)
+#ifndef SG_FINISH_B_THREADS
+#define SG_FINISH_B_THREADS 32
+#endif
+constexpr int kFinishBThreads = SG_FINISH_B_THREADS;
+__global__ void __launch_bounds__(kFinishBThreads)
     vic_finish_b_kernel(const BlockDev* __restrict__ tab, StageParams p) {
   const BlockDev& B = tab[blockIdx.y];
   if (!B.implicit) return;
