@@ -1627,14 +1627,23 @@ __global__ void __launch_bounds__(32, 20)
 // |d_prev| the observed contraction, accepted at or below 2^-44 of the
 // largest |x|.  A converged column then gets the Woodbury step of the direct
 // solve; the others are masked for the direct FP64 solve
-constexpr int kCorrCols = 10;   // columns per warp (30 of its lanes)
+// (one box, the same runs: 10 columns with a 6-layer ring 3.33 ms per
+// stage on the ensemble, 8 with 8 layers 3.26 ms and the served trace
+// +0.5 %, 6 with 8 layers 3.29 ms)
+#ifndef SG_CORR_COLS
+#define SG_CORR_COLS 8
+#endif
+#ifndef SG_CORR_RING
+#define SG_CORR_RING 8
+#endif
+constexpr int kCorrCols = SG_CORR_COLS;  // columns per warp (3 lanes each)
 // (one warp per CTA with a 6-layer ring, 20 KB: measured against two warps
 // with a 4-layer ring on one box, the ensemble's solve phase 3.53 -> 3.31
 // ms per stage, the served trace +0.7 %)
 constexpr int kCorrWarps = 1;   // warps per CTA
-constexpr int kCorrRing = 6;    // layers in flight per warp
+constexpr int kCorrRing = SG_CORR_RING;  // layers in flight per warp
 // shared-memory row strides of a column's factors and residuals: multiples
-// of 4 floats (16-byte copies) that spread a warp's ten columns over the
+// of 4 floats (16-byte copies) that spread a warp's columns over the
 // banks (at most two columns per bank)
 constexpr int kLuRow = kLu32 + 4, kRRow = kR32 + 4;
 
