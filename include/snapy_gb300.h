@@ -94,7 +94,8 @@ typedef struct sg_block_desc {
   /* integration/implicit-scheme: 0 (none), 9 (the full 5x5 vertical
    * implicit solve) or 1 (the partial 3x3 blocks of rows and columns
    * {rho, m1, E}, the tangential momenta folded into the density column and
-   * carried by the face mass transfers; FP64 assembly only).  Both need
+   * carried by the face mass transfers; assembled in either precision,
+   * solved in FP64; the refined FP32 solve is scheme 9's).  Both need
    * const-gravity and reflecting x1 walls
    * (src/implicit/implicit_hydro.hpp:25-41) */
   int32_t implicit_scheme;

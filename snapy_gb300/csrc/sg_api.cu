@@ -728,12 +728,6 @@ int sg_create(const sg_scheme* scheme, const sg_block_desc* blocks,
                     "full 5x5 scheme 9 and the partial 3x3 scheme 1 are "
                     "built)", b, d.implicit_scheme);
       }
-      if (d.implicit_scheme == 1 && d.implicit_precision == SG_F32) {
-        sg_destroy(h);
-        return fail(SG_ERR_UNSUPPORTED, "block %d: implicit-scheme 1 "
-                    "assembles its blocks in FP64 (implicit-precision "
-                    "float32 is built for scheme 9)", b);
-      }
       h->vic_kinds |= d.implicit_scheme == 9 ? 1 : 2;
       if (d.grav1 == 0. || d.bc[0] != SG_BC_REFLECTING ||
           d.bc[1] != SG_BC_REFLECTING || d.nc1 - 2 * d.ng < 3) {

@@ -385,7 +385,8 @@ __device__ __forceinline__ void vic_assemble_cell(const BlockDev& B,
     du0[v] = S.du[v * S.cells + cell];
     S.du0[v * S.cells + cell] = du0[v];
   }
-  // the partial matrix (implicit-scheme 1; FP64 assembly only): its 3x3
+  // the partial matrix (implicit-scheme 1, assembled in FP64 or FP32 and
+  // solved in FP64 by vic_solve3_kernel): its 3x3
   // blocks are the {rho, m1, E} rows and columns of the same entries, and
   // the m_t columns of those rows (the same terms, energy-row face work and
   // wall mirror included) fold into the density column at the cell's v_t
@@ -1328,7 +1329,9 @@ __global__ void __launch_bounds__(32, 20)
     vic_solve32_kernel(const BlockDev* __restrict__ tab, StageParams p) {
   __shared__ VicSolve32Smem sm;
   const BlockDev& Bk = tab[blockIdx.y];
-  if (!Bk.implicit || !Bk.implicit_f32) return;
+  // (scheme-9 blocks only: a scheme-1 block assembled in FP32 is solved
+  // in FP64 by vic_solve3_kernel)
+  if (Bk.implicit != 9 || !Bk.implicit_f32) return;
   const VicScratch S = vic_scratch(Bk);
   const int n = Bk.nc1 - 2 * Bk.ng;
   const VicScratch32 F = vic_scratch32(Bk, S, n);
@@ -1684,7 +1687,9 @@ __global__ void __launch_bounds__(32 * kCorrWarps)
                          int last) {
   __shared__ CorrSlot ring[kCorrWarps][kCorrRing];
   const BlockDev& Bk = tab[blockIdx.y];
-  if (!Bk.implicit || !Bk.implicit_f32) return;
+  // (scheme-9 blocks only: a scheme-1 block assembled in FP32 is solved
+  // in FP64 by vic_solve3_kernel)
+  if (Bk.implicit != 9 || !Bk.implicit_f32) return;
   const VicScratch S = vic_scratch(Bk);
   const int n = Bk.nc1 - 2 * Bk.ng;
   const VicScratch32 F = vic_scratch32(Bk, S, n);
@@ -1928,7 +1933,9 @@ __global__ void __launch_bounds__(32 * kCorrWarps)
 __global__ void __launch_bounds__(kThreads)
     vic_woodbury32_kernel(const BlockDev* __restrict__ tab, StageParams p) {
   const BlockDev& Bk = tab[blockIdx.y];
-  if (!Bk.implicit || !Bk.implicit_f32) return;
+  // (scheme-9 blocks only: a scheme-1 block assembled in FP32 is solved
+  // in FP64 by vic_solve3_kernel)
+  if (Bk.implicit != 9 || !Bk.implicit_f32) return;
   const VicScratch S = vic_scratch(Bk);
   const int n = Bk.nc1 - 2 * Bk.ng;
   const VicScratch32 F = vic_scratch32(Bk, S, n);
@@ -2030,7 +2037,7 @@ __global__ void __launch_bounds__(kResThreads)
     vic_residual_kernel(const BlockDev* __restrict__ tab, StageParams p,
                         int corr) {
   const BlockDev& B = tab[blockIdx.y];
-  if (!B.implicit || !B.implicit_f32) return;
+  if (B.implicit != 9 || !B.implicit_f32) return;  // scheme 9 only
   const VicScratch S = vic_scratch(B);
   const int n = B.nc1 - 2 * B.ng;
   const VicScratch32 F = vic_scratch32(B, S, n);

@@ -74,9 +74,6 @@ def scheme_of(options: MeshBlockOptions) -> dict:
             raise DeckError(f"integration/implicit-scheme {h.icorr.scheme}: the "
                             "full 5x5 scheme 9 and the partial 3x3 scheme 1 "
                             "are built")
-        if h.icorr.scheme == 1 and h.icorr.precision == "float32":
-            raise DeckError("integration/implicit-precision float32 is built "
-                            "for implicit-scheme 9 (scheme 1 assembles in FP64)")
         if options.hydro().precision == "float64" and h.icorr.precision == "float32":
             raise DeckError("integration/implicit-precision float32 needs "
                             "dynamics/precision float32")

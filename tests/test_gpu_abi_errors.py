@@ -73,15 +73,18 @@ def test_create_refuses_what_is_not_built(cuda):
         (scheme(), block(implicit_precision=_lib.F32), UNSUPPORTED,
          "implicit-precision"),
         (scheme(), block(bc=[9] * 6), ARG, "boundary kind"),
-        (scheme(), block(implicit_scheme=1, implicit_precision=_lib.F32, **grav),
-         UNSUPPORTED, "implicit-scheme 1"),
         (scheme(), block(grav1=-9.8), ARG, "x1 geometry"),
     ]
     for sch, blk, code, word in cases:
         rc, h, msg = create(sch, blk)
         assert (rc, word in msg) == (code, True), (word, rc, msg)
-    # a valid block still builds
+    # a valid block still builds, and implicit-scheme 1 assembles in FP32 as
+    # scheme 9 does (an FP32 state under gravity: LMARS, about its base)
     assert create(scheme(), block())[0] == 0
+    rc, _, msg = create(scheme(_lib.F32, _lib.LMARS),
+                        block(implicit_scheme=1, implicit_precision=_lib.F32,
+                              base=base.data_ptr(), **grav))
+    assert rc == 0, msg
 
 
 def test_step_fields_need_their_direction_and_scratch(cuda):

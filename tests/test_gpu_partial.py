@@ -9,8 +9,9 @@ FP64 within 1e-12 relative L2 per field of the oracle: Straka windows (the
 warp-form finish; the thread form on a batch of 20,480 columns; x2 cells 40
 times the x1 ones, vertical acoustic Courant number near 40), the x1 step
 field with the partial matrix's momentum posts, a 3-D convection block, a
-tracer; FP32 state within 1e-5 of the FP64 oracle; a resting column stays at
-rest; members of both schemes in one batch each equal the member alone."""
+tracer; FP32 state within 1e-5 of the FP64 oracle, with the blocks assembled
+in FP64 or in FP32; a resting column stays at rest; members of both schemes
+in one batch each equal the member alone."""
 import copy
 
 import numpy as np
@@ -152,6 +153,46 @@ def test_fp32_state(oracle, cuda):
     err = rel_l2(got[inner], u[inner])
     print(f"\nFP32 scheme 1 vs FP64 oracle: {err}")
     assert err.max() <= 1e-5
+
+
+def test_fp32_assembly(oracle, cuda):
+    """implicit-precision float32: the partial blocks assembled in FP32 from
+    the FP32 state, solved in FP64 by the 3x3 column solve (the refined
+    solve is scheme 9's): within 1e-5 of the FP64 oracle after 10 steps, and
+    a batch with a scheme-9 FP32 member (its refined solve beside it) gives
+    each member its own result bit for bit."""
+    opts = straka(precision="float32")
+    opts.hydro().icorr.precision = "float32"
+    w = bubble(opts)
+    blk, vars, u, _, _ = run_pair(oracle, cuda, opts, w, 10, check=False)
+    got = blk.total_u(vars).double().cpu().numpy()
+    inner = (slice(None), slice(None), slice(3, -3), slice(3, -3))
+    err = rel_l2(got[inner], u[inner])
+    print(f"\nFP32 scheme 1, FP32 assembly, vs FP64 oracle: {err}")
+    assert err.max() <= 1e-5
+    # in one batch with a scheme-9 member whose blocks are FP32 too
+    o9 = straka(scheme=9, precision="float32", nx2=24)
+    o9.hydro().icorr.precision = "float32"
+    o1 = straka(scheme=1, precision="float32", nx2=40)
+    o1.hydro().icorr.precision = "float32"
+    for o in (o9, o1):
+        o.autotune = False
+    ws = [bubble(o9, xc=600.0), bubble(o1)]
+    alone = []
+    for o, w0 in zip((o9, o1), ws):
+        b = sg.MeshBlock(o).to(cuda)
+        v = {"hydro_w": w0.to(cuda)}
+        b.initialize(v)
+        for _ in range(3):
+            b.step(v, b.max_time_step(v))
+            assert b.check_redo(v) == 0
+        alone.append(v["hydro_u"].cpu().numpy())
+    ens = Ensemble([o9, o1], cuda, graphs=False)
+    ens.initialize([w0.to(cuda) for w0 in ws], autotune=False)
+    for _ in range(3):
+        ens.step()
+    for k in range(2):
+        assert np.array_equal(ens.state(k).cpu().numpy(), alone[k]), k
 
 
 def test_rest_state_stays_at_rest(cuda):

@@ -116,8 +116,9 @@ def test_deck_accepts_scheme_1():
     cfg["integration"]["implicit-precision"] = "float32"
     cfg["dynamics"]["precision"] = "float32"
     opts = sg.MeshBlockOptions.from_config(cfg)
-    with pytest.raises(sg.options.DeckError, match="scheme 9"):
-        sg.meshblock.scheme_of(opts)
+    sg.meshblock.scheme_of(opts)  # FP32 assembly, as for scheme 9
+    d = sg.meshblock.block_of(opts)
+    assert d["implicit_scheme"] == 1 and d["implicit_f32"]
     cfg["integration"]["implicit-scheme"] = 5
     with pytest.raises(sg.options.DeckError, match="scheme 1"):
         sg.meshblock.scheme_of(sg.MeshBlockOptions.from_config(cfg))
