@@ -461,7 +461,9 @@ class MeshBlockOptions:
         # solve of implicit-precision float32 blocks, "refined" (FP32 sweeps
         # corrected with FP64 residuals to the FP64 solution), "direct" (the
         # FP64 solve of every column) or "fp32" (the reference's own FP32
-        # compute: the FP32 sweep alone, the FP64 retry of failed columns)
+        # compute: the FP32 sweep alone, the FP64 retry of failed columns);
+        # scheme 9's only: scheme 1's FP32-assembled 3x3 blocks are solved
+        # directly in FP64
         self.implicit_solve = "refined"
         self.implicit_corrections = 2  # FP64-residual corrections (1 to 3)
         # integration/implicit-sweep (no counterpart in the reference): the
